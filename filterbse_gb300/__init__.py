@@ -1,0 +1,280 @@
+"""filterbse_gb300 -- GB300 (sm_103a) implementation of FilterBSE's filter hot path.
+
+The product is the C-ABI library ``libfbse_gpu.so`` (declared in
+``include/fbse.h``); this module is a thin ctypes binding used by the tests,
+``bench.py`` and Python callers.  Device memory is handed over as torch CUDA
+tensors (torch is used only as a device allocator here).  There is no CPU
+fallback: importing works without a GPU, but every compute call goes through
+the CUDA library and raises if it is missing or fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .build import LIB as _LIB_PATH
+
+__all__ = ["FbseError", "load", "Context", "samp_points", "newton_coeff", "init_filter_states",
+           "FP64", "MIXED", "EXPORTED"]
+
+FP64 = 0
+MIXED = 1
+
+EXPORTED = [
+    "fbse_create", "fbse_destroy", "fbse_last_error", "fbse_version", "fbse_alloc", "fbse_free",
+    "fbse_upload", "fbse_download", "fbse_sync", "fbse_stream", "fbse_hpsi", "fbse_hnorm",
+    "fbse_newton_filter", "fbse_energy_range", "fbse_normalize_all", "fbse_energy_all",
+    "fbse_ortho_diag_sigma", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
+    "fbse_init_filter_states",
+]
+
+
+class FbseError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fbse error {code}: {msg}")
+        self.code = code
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_long), ("ny", ctypes.c_long), ("nz", ctypes.c_long),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("ke_max", ctypes.c_double), ("nspin", ctypes.c_int), ("is_complex", ctypes.c_int),
+                ("so", ctypes.c_int), ("nl", ctypes.c_int), ("dkx", ctypes.c_double), ("dky", ctypes.c_double),
+                ("dkz", ctypes.c_double)]
+
+
+class ProjDesc(ctypes.Structure):
+    _fields_ = [("n_atoms", ctypes.c_long), ("npts", ctypes.c_long), ("nproj", ctypes.c_int),
+                ("nl", ctypes.POINTER(ctypes.c_long)), ("jxyz", ctypes.POINTER(ctypes.c_int)),
+                ("y1", ctypes.POINTER(ctypes.c_double)), ("so_proj", ctypes.POINTER(ctypes.c_double)),
+                ("nl_proj", ctypes.POINTER(ctypes.c_double)), ("nl_sign", ctypes.POINTER(ctypes.c_int)),
+                ("LS", ctypes.POINTER(ctypes.c_double))]
+
+
+_lib = None
+_D = ctypes.POINTER(ctypes.c_double)
+_VP = ctypes.c_void_p
+
+
+def load() -> ctypes.CDLL:
+    """Load libfbse_gpu.so (built in-tree by ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise FbseError(-6, f"{_LIB_PATH} is missing: build it with __graft_entry__.build()")
+    L = ctypes.CDLL(_LIB_PATH)
+    L.fbse_create.argtypes = [ctypes.POINTER(_VP), ctypes.POINTER(GridDesc), _D, ctypes.POINTER(ProjDesc), ctypes.c_int]
+    L.fbse_destroy.argtypes = [_VP]
+    L.fbse_destroy.restype = None
+    L.fbse_last_error.argtypes = [_VP]
+    L.fbse_last_error.restype = ctypes.c_char_p
+    L.fbse_stream.argtypes = [_VP]
+    L.fbse_stream.restype = _VP
+    L.fbse_sync.argtypes = [_VP]
+    for f in ("fbse_hpsi",):
+        getattr(L, f).argtypes = [_VP, _VP, _VP, ctypes.c_long]
+    L.fbse_hnorm.argtypes = [_VP, _VP, _VP, ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    L.fbse_newton_filter.argtypes = [_VP, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_double, ctypes.c_double,
+                                     _VP, ctypes.c_long, _VP]
+    L.fbse_energy_range.argtypes = [_VP, ctypes.c_long, ctypes.c_long, _D, _D, ctypes.POINTER(ctypes.c_long)]
+    L.fbse_normalize_all.argtypes = [_VP, _VP, ctypes.c_long, _D]
+    L.fbse_energy_all.argtypes = [_VP, _VP, ctypes.c_long, _D]
+    L.fbse_ortho_diag_sigma.argtypes = [_VP, _VP, ctypes.c_long, ctypes.POINTER(ctypes.c_long), _D, _D]
+    L.fbse_samp_points.argtypes = [ctypes.c_long, _D]
+    L.fbse_samp_points.restype = ctypes.c_double
+    L.fbse_newton_coeff.argtypes = [ctypes.c_long, ctypes.c_long, _D, _D, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, _D]
+    L.fbse_ran.argtypes = [ctypes.POINTER(ctypes.c_long)]
+    L.fbse_ran.restype = ctypes.c_double
+    L.fbse_init_filter_states.argtypes = [_D, ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_long, ctypes.POINTER(ctypes.c_long)]
+    L.fbse_init_filter_states.restype = ctypes.c_long
+    _lib = L
+    return L
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+# ---------------------------------------------------------------------------
+# host helpers (no GPU)
+# ---------------------------------------------------------------------------
+
+def samp_points(ncheby: int):
+    zn = np.empty(ncheby)
+    fk = load().fbse_samp_points(ncheby, _dp(zn))
+    return zn, fk
+
+
+def newton_coeff(zn, targets, vmin, de, dt):
+    zn = np.ascontiguousarray(zn, np.float64)
+    t = np.ascontiguousarray(targets, np.float64)
+    an = np.empty(2 * len(t) * len(zn))
+    rc = load().fbse_newton_coeff(len(zn), len(t), _dp(zn), _dp(t), vmin, de, dt, _dp(an))
+    if rc:
+        raise FbseError(rc, "fbse_newton_coeff")
+    return an.view(np.complex128).reshape(len(t), len(zn))
+
+
+def init_filter_states(n_filters, ngrid, nspin, is_complex, dv, seed):
+    stlen = (2 if is_complex else 1) * nspin * ngrid
+    out = np.empty(n_filters * stlen)
+    seeds = np.empty(n_filters * nspin, np.int64)
+    s = load().fbse_init_filter_states(_dp(out), n_filters, ngrid, nspin, int(is_complex), dv, seed,
+                                       seeds.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+    return out.reshape(n_filters, stlen), seeds, s
+
+
+# ---------------------------------------------------------------------------
+# device context
+# ---------------------------------------------------------------------------
+
+class Context:
+    """One fbse_ctx: grid, local potential, projector table, FFT plans.
+
+    grid: object/dict with nx, ny, nz, dx, dy, dz, ke_max; nspin, is_complex,
+    so, nl switches.  proj: object with nl, npts, jxyz, y1, proj (SO radial),
+    nlp (NL radial), sgn, nproj (the layout of the reference's nlc_st array)."""
+
+    def __init__(self, grid, pot, *, nspin=1, is_complex=False, so=False, nl=False, proj=None,
+                 precision=FP64, LS=None):
+        L = load()
+        dk = grid.dk() if hasattr(grid, "dk") else (0.0, 0.0, 0.0)
+        g = GridDesc(int(grid.nx), int(grid.ny), int(grid.nz), float(grid.dx), float(grid.dy), float(grid.dz),
+                     float(grid.ke_max), int(nspin), int(bool(is_complex)), int(bool(so)), int(bool(nl)),
+                     float(dk[0]), float(dk[1]), float(dk[2]))
+        self._keep = []
+        pd = None
+        if proj is not None and (so or nl):
+            nlc = np.ascontiguousarray(proj.nl, np.int64)
+            jx = np.ascontiguousarray(proj.jxyz, np.int32)
+            y1 = np.ascontiguousarray(proj.y1, np.float64)
+            sp = np.ascontiguousarray(proj.proj, np.float64)
+            npj = np.ascontiguousarray(proj.nlp, np.float64)
+            sg = np.ascontiguousarray(proj.sgn, np.int32)
+            ls = None if LS is None else np.ascontiguousarray(np.asarray(LS, np.complex128)).view(np.float64)
+            self._keep += [nlc, jx, y1, sp, npj, sg, ls]
+            pd = ProjDesc(len(nlc), int(proj.npts), int(proj.nproj), nlc.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                          jx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(y1), _dp(sp), _dp(npj),
+                          sg.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(ls) if ls is not None else None)
+        pot = np.ascontiguousarray(pot, np.float64)
+        h = _VP()
+        rc = L.fbse_create(ctypes.byref(h), ctypes.byref(g), _dp(pot), ctypes.byref(pd) if pd else None, precision)
+        self._h = h
+        self._L = L
+        if rc:
+            msg = L.fbse_last_error(h).decode() if h.value else "no CUDA device"
+            self.close()
+            raise FbseError(rc, msg)
+        self.grid = grid
+        self.nspin = nspin
+        self.is_complex = bool(is_complex)
+        self.precision = precision
+        self.ngrid = int(grid.nx) * int(grid.ny) * int(grid.nz)
+        self.stlen = (2 if is_complex else 1) * nspin * self.ngrid
+
+    # -- plumbing -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.fbse_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        if rc:
+            raise FbseError(rc, self._L.fbse_last_error(self._h).decode())
+
+    @property
+    def stream_handle(self) -> int:
+        return int(self._L.fbse_stream(self._h) or 0)
+
+    def sync(self):
+        self._chk(self._L.fbse_sync(self._h))
+
+    @staticmethod
+    def _ptr(t):
+        import torch
+        assert t.is_cuda and t.is_contiguous()
+        return ctypes.c_void_p(t.data_ptr())
+
+    @staticmethod
+    def _torch_sync():
+        import torch
+        torch.cuda.current_stream().synchronize()
+
+    def working_dtype(self):
+        import torch
+        return torch.complex64 if self.precision == MIXED else torch.complex128
+
+    # -- operators --------------------------------------------------------------
+    def hpsi(self, psi_in, psi_out, sync=True):
+        """psi_out = H psi_in for [n, nspin*ngrid] complex tensors (working precision)."""
+        self._torch_sync()
+        n = psi_in.shape[0] if psi_in.dim() > 1 else 1
+        self._chk(self._L.fbse_hpsi(self._h, self._ptr(psi_in), self._ptr(psi_out), n))
+        if sync:
+            self.sync()
+
+    def hnorm(self, psi_in, psi_out, vmin, de, zn, sync=True):
+        self._torch_sync()
+        n = psi_in.shape[0] if psi_in.dim() > 1 else 1
+        self._chk(self._L.fbse_hnorm(self._h, self._ptr(psi_in), self._ptr(psi_out), n, vmin, de, zn))
+        if sync:
+            self.sync()
+
+    def newton_filter(self, zn, an, vmin, de, psi0, out=None):
+        """filter_cycle for all starts: psi0 [nstart, stlen] float64 CUDA tensor;
+        returns [nstart, m, stlen] float64 CUDA tensor (psi_rank layout)."""
+        import torch
+        zn = np.ascontiguousarray(zn, np.float64)
+        an = np.ascontiguousarray(an, np.complex128)
+        m, nc = an.shape
+        nstart = psi0.shape[0]
+        if out is None:
+            out = torch.empty((nstart, m, self.stlen), dtype=torch.float64, device=psi0.device)
+        anv = an.view(np.float64).reshape(-1)
+        self._torch_sync()
+        self._chk(self._L.fbse_newton_filter(self._h, _dp(zn), _dp(anv), nc, m, vmin, de, self._ptr(psi0), nstart,
+                                             self._ptr(out)))
+        return out
+
+    def energy_range(self, seed=-874917403, max_iter=1500):
+        e0 = ctypes.c_double()
+        e1 = ctypes.c_double()
+        it = ctypes.c_long()
+        self._chk(self._L.fbse_energy_range(self._h, seed, max_iter, ctypes.byref(e0), ctypes.byref(e1),
+                                            ctypes.byref(it)))
+        return e0.value, e1.value, it.value
+
+    def normalize_all(self, psitot):
+        n = psitot.shape[0]
+        norms = np.empty(n)
+        self._torch_sync()
+        self._chk(self._L.fbse_normalize_all(self._h, self._ptr(psitot), n, _dp(norms)))
+        return norms
+
+    def energy_all(self, psitot):
+        n = psitot.shape[0]
+        e = np.empty(n)
+        self._torch_sync()
+        self._chk(self._L.fbse_energy_all(self._h, self._ptr(psitot), n, _dp(e)))
+        return e
+
+    def ortho_diag_sigma(self, psitot):
+        n = psitot.shape[0]
+        ev = np.empty(n)
+        sg = np.empty(n)
+        nk = ctypes.c_long()
+        self._torch_sync()
+        self._chk(self._L.fbse_ortho_diag_sigma(self._h, self._ptr(psitot), n, ctypes.byref(nk), _dp(ev), _dp(sg)))
+        k = nk.value
+        return k, ev[:k].copy(), sg[:k].copy()

@@ -1,0 +1,315 @@
+// C-ABI entry points of libfbse_gpu (declared in include/fbse.h).
+#include <cmath>
+#include <cstring>
+
+#include "fbse_internal.cuh"
+
+namespace fbse {
+
+int set_err(fbse_ctx *c, int code, const std::string &msg)
+{
+  if (c) c->err = msg;
+  return code;
+}
+
+int ensure(fbse_ctx *c, void **p, size_t *have, size_t need)
+{
+  if (*have >= need && *p) return FBSE_OK;
+  if (*p) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+  }
+  if (need == 0) return FBSE_OK;
+  if (cudaMalloc(p, need) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return set_err(c, FBSE_ERR_OOM, "device allocation of " + std::to_string(need) + " bytes failed");
+  }
+  *have = need;
+  return FBSE_OK;
+}
+
+int newton_filter(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
+                  const double *psi0, long nstart, double *filtered);
+int normalize_all(fbse_ctx *c, double *psitot, long n, double *norms);
+int energy_all(fbse_ctx *c, const double *psitot, long n, double *ene);
+int energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *emax, long *iters);
+int ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma);
+
+// per-axis 0.5 k^2 / N exactly as init_kvec + build_grid_ksqr
+// (filter_mpi/init.c:904-915, 318-336)
+static void axis_k2(long n, double dk, double ngrid_1, std::vector<double> &k)
+{
+  k.assign(n, 0.0);
+  long npos = (n % 2 == 0) ? n / 2 : (n - 1) / 2;
+  for (long j = 1; j <= npos; j++) {
+    double v = (double)j * dk * 1.0;
+    k[j] = v;
+    k[n - j] = -v;
+  }
+  for (long j = 1; j < n; j++) k[j] *= 0.5 * k[j] * ngrid_1;
+}
+
+template <typename D, typename S> static int upload(fbse_ctx *c, D **dst, const S *src, size_t n)
+{
+  std::vector<D> tmp(n);
+  for (size_t i = 0; i < n; i++) tmp[i] = (D)src[i];
+  FBSE_CUDA(c, cudaMalloc(dst, n * sizeof(D) + 16));
+  FBSE_CUDA(c, cudaMemcpy(*dst, tmp.data(), n * sizeof(D), cudaMemcpyHostToDevice));
+  return FBSE_OK;
+}
+
+static void def_LS(double *ls)
+{  // def_LS (filter_mpi/hamiltonian.c:312-442): L.S in the flattened (s, m) basis
+  const double h = std::sqrt(0.5);
+  const double Lre[3][3][3] = {{{0, h, 0}, {h, 0, h}, {0, h, 0}}, {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}},
+                               {{-1, 0, 0}, {0, 0, 0}, {0, 0, 1}}};
+  const double Lim[3][3][3] = {{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, {{0, h, 0}, {-h, 0, h}, {0, -h, 0}},
+                               {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}};
+  const double Sre[3][2][2] = {{{0, 0.5}, {0.5, 0}}, {{0, 0}, {0, 0}}, {{0.5, 0}, {0, -0.5}}};
+  const double Sim[3][2][2] = {{{0, 0}, {0, 0}}, {{0, -0.5}, {0.5, 0}}, {{0, 0}, {0, 0}}};
+  for (int jp = 0; jp < 6; jp++)
+    for (int j = 0; j < 6; j++) {
+      int sp = jp / 3, mp = jp % 3, s = j / 3, m = j % 3;
+      double re = 0, im = 0;
+      for (int k = 0; k < 3; k++) {
+        re += Lre[k][m][mp] * Sre[k][s][sp] - Lim[k][m][mp] * Sim[k][s][sp];
+        im += Lre[k][m][mp] * Sim[k][s][sp] + Lim[k][m][mp] * Sre[k][s][sp];
+      }
+      ls[2 * (jp * 6 + j)] = re;
+      ls[2 * (jp * 6 + j) + 1] = im;
+    }
+}
+
+static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const fbse_proj_desc *pj)
+{
+  if (g->nx < 1 || g->ny < 1 || g->nz < 1) return set_err(c, FBSE_ERR_ARG, "grid sizes must be positive");
+  if (g->nspin != 1 && g->nspin != 2) return set_err(c, FBSE_ERR_ARG, "nspin must be 1 or 2");
+  if (g->so && (g->nspin != 2 || !g->is_complex))
+    return set_err(c, FBSE_ERR_ARG, "spin-orbit requires complex spinors (read.c:927-936)");
+  if (g->nspin == 2 && !g->is_complex) return set_err(c, FBSE_ERR_ARG, "spinors must be complex");
+  if ((g->so || g->nl) && !pj) return set_err(c, FBSE_ERR_ARG, "projector table required when SO or NL is on");
+  if (!pot) return set_err(c, FBSE_ERR_ARG, "local potential required");
+  if ((double)g->nx * g->ny * g->nz > 2147483647.0) return set_err(c, FBSE_ERR_UNSUPPORTED, "grid too large");
+  c->nx = g->nx; c->ny = g->ny; c->nz = g->nz;
+  c->ngrid = g->nx * g->ny * g->nz;
+  c->nspin = g->nspin; c->is_complex = g->is_complex ? 1 : 0; c->so = g->so ? 1 : 0; c->nl = g->nl ? 1 : 0;
+  c->dx = g->dx; c->dy = g->dy; c->dz = g->dz;
+  c->dv = g->dx * g->dy * g->dz;
+  c->ke_max = g->ke_max;
+  const double nx_1 = 1.0 / (double)g->nx, ny_1 = 1.0 / (double)g->ny, nz_1 = 1.0 / (double)g->nz;
+  const double ng_1 = nx_1 * ny_1 * nz_1;
+  c->kemax_scaled = g->ke_max * (ny_1 * nx_1 * nz_1);
+  FBSE_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  int rc;
+  if ((rc = plan_axis(c, c->ax[0], (int)g->nx))) return rc;
+  if ((rc = plan_axis(c, c->ax[1], (int)g->ny))) return rc;
+  if ((rc = plan_axis(c, c->ax[2], (int)g->nz))) return rc;
+  // reciprocal spacing: box = n d (even n) or (n - 1) d (odd n)  (init.c:65-80)
+  const long ns[3] = {g->nx, g->ny, g->nz};
+  const double ds[3] = {g->dx, g->dy, g->dz};
+  double **dst[3] = {&c->k2x, &c->k2y, &c->k2z};
+  const double dkin[3] = {g->dkx, g->dky, g->dkz};
+  for (int a = 0; a < 3; a++) {
+    const double box = (ns[a] % 2 == 0) ? (double)ns[a] * ds[a] : (double)(ns[a] - 1) * ds[a];
+    const double dk = dkin[a] > 0 ? dkin[a] : 6.28318530717958647692 / box;
+    std::vector<double> k;
+    axis_k2(ns[a], dk, ng_1, k);
+    if ((rc = upload(c, dst[a], k.data(), k.size()))) return rc;
+  }
+  if ((rc = upload(c, &c->pot64, pot, c->ngrid))) return rc;
+  if ((rc = upload(c, &c->pot32, pot, c->ngrid))) return rc;
+  c->vpot_min = 1e300; c->vpot_max = -1e300;
+  for (long i = 0; i < c->ngrid; i++) {
+    c->vpot_min = std::fmin(c->vpot_min, pot[i]);
+    c->vpot_max = std::fmax(c->vpot_max, pot[i]);
+  }
+  if ((g->so || g->nl) && pj) {
+    ProjDev &p = c->proj;
+    if (pj->n_atoms < 0 || pj->npts < 1 || pj->nproj < 1 || pj->nproj > 5)
+      return set_err(c, FBSE_ERR_ARG, "projector table: n_atoms >= 0, npts >= 1, 1 <= nproj <= 5");
+    p.nat = pj->n_atoms; p.npts = pj->npts; p.nproj = pj->nproj; p.so = c->so; p.nl = c->nl;
+    const size_t ne = (size_t)p.nat * p.npts;
+    std::vector<int> cnt(p.nat > 0 ? p.nat : 1);
+    for (long a = 0; a < p.nat; a++) {
+      if (pj->nl[a] < 0 || pj->nl[a] > p.npts) return set_err(c, FBSE_ERR_ARG, "projector table: nl[a] > npts");
+      cnt[a] = (int)pj->nl[a];
+      for (long e = 0; e < pj->nl[a]; e++) {
+        const int j = pj->jxyz[a * p.npts + e];
+        if (j < 0 || j >= c->ngrid) return set_err(c, FBSE_ERR_ARG, "projector table: grid index out of range");
+      }
+    }
+    // entries beyond nl[a] are never read; zero-fill copies keep them finite
+    std::vector<int> jx(ne, 0);
+    std::vector<double> y1(ne * 6, 0.0), so(ne * p.nproj, 0.0), nlr(ne * p.nproj, 0.0);
+    for (long a = 0; a < p.nat; a++)
+      for (long e = 0; e < pj->nl[a]; e++) {
+        const size_t i = a * p.npts + e;
+        jx[i] = pj->jxyz[i];
+        for (int k = 0; k < 6; k++) y1[i * 6 + k] = pj->y1[i * 6 + k];
+        for (int k = 0; k < p.nproj; k++) {
+          so[i * p.nproj + k] = pj->so_proj ? pj->so_proj[i * p.nproj + k] : 0.0;
+          nlr[i * p.nproj + k] = pj->nl_proj ? pj->nl_proj[i * p.nproj + k] : 0.0;
+        }
+      }
+    std::vector<int> sg((size_t)(p.nat > 0 ? p.nat : 1) * p.nproj, 0);
+    if (pj->nl_sign)
+      for (size_t i = 0; i < (size_t)p.nat * p.nproj; i++) sg[i] = pj->nl_sign[i];
+    double ls[72];
+    if (pj->LS) std::memcpy(ls, pj->LS, sizeof(ls));
+    else def_LS(ls);
+    if ((rc = upload(c, &p.nl_cnt, cnt.data(), cnt.size()))) return rc;
+    if ((rc = upload(c, &p.jxyz, jx.data(), jx.size() ? jx.size() : 1))) return rc;
+    if ((rc = upload(c, &p.y1, y1.data(), y1.size()))) return rc;
+    if ((rc = upload(c, &p.sop, so.data(), so.size()))) return rc;
+    if ((rc = upload(c, &p.nlp, nlr.data(), nlr.size()))) return rc;
+    if ((rc = upload(c, &p.y1f, y1.data(), y1.size()))) return rc;
+    if ((rc = upload(c, &p.sopf, so.data(), so.size()))) return rc;
+    if ((rc = upload(c, &p.nlpf, nlr.data(), nlr.size()))) return rc;
+    if ((rc = upload(c, &p.sgn, sg.data(), sg.size()))) return rc;
+    FBSE_CUDA(c, cudaMalloc(&p.LS, 36 * sizeof(double2)));
+    FBSE_CUDA(c, cudaMemcpy(p.LS, ls, 36 * sizeof(double2), cudaMemcpyHostToDevice));
+  }
+  return FBSE_OK;
+}
+
+}  // namespace fbse
+
+using namespace fbse;
+
+extern "C" {
+
+int fbse_version(void) { return 1; }
+
+const char *fbse_last_error(const fbse_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int fbse_create(fbse_ctx **out, const fbse_grid_desc *grid, const double *pot_local, const fbse_proj_desc *proj,
+                int precision)
+{
+  if (!out || !grid) return FBSE_ERR_ARG;
+  *out = nullptr;
+  if (precision != FBSE_FP64 && precision != FBSE_MIXED) return FBSE_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return FBSE_ERR_CUDA;
+  }
+  fbse_ctx *c = new fbse_ctx();
+  c->precision = precision;
+  int rc = create(c, grid, pot_local, proj);
+  *out = c;  // returned even on failure so fbse_last_error can explain
+  return rc;
+}
+
+void fbse_destroy(fbse_ctx *c)
+{
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int a = 0; a < 3; a++) free_axis(c->ax[a]);
+  void *bufs[] = {c->k2x, c->k2y, c->k2z, c->pot64, c->pot32, c->wk, c->coef, c->tmp, c->red,
+                  c->proj.nl_cnt, c->proj.jxyz, c->proj.y1, c->proj.sop, c->proj.nlp, c->proj.sgn, c->proj.LS,
+                  c->proj.y1f, c->proj.sopf, c->proj.nlpf};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int fbse_alloc(fbse_ctx *c, void **dptr, size_t bytes)
+{
+  if (!c || !dptr) return FBSE_ERR_ARG;
+  if (cudaMalloc(dptr, bytes ? bytes : 1) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_OOM, "fbse_alloc of " + std::to_string(bytes) + " bytes failed");
+  }
+  return FBSE_OK;
+}
+
+int fbse_free(fbse_ctx *c, void *dptr)
+{
+  if (!c) return FBSE_ERR_ARG;
+  cudaStreamSynchronize(c->stream);
+  FBSE_CUDA(c, cudaFree(dptr));
+  return FBSE_OK;
+}
+
+int fbse_upload(fbse_ctx *c, void *dst, const void *src, size_t bytes)
+{
+  if (!c) return FBSE_ERR_ARG;
+  FBSE_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+  FBSE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FBSE_OK;
+}
+
+int fbse_download(fbse_ctx *c, void *dst, const void *src, size_t bytes)
+{
+  if (!c) return FBSE_ERR_ARG;
+  FBSE_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+  FBSE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FBSE_OK;
+}
+
+int fbse_sync(fbse_ctx *c)
+{
+  if (!c) return FBSE_ERR_ARG;
+  FBSE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FBSE_OK;
+}
+
+void *fbse_stream(fbse_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int fbse_hpsi(fbse_ctx *c, const void *in, void *out, long nstates)
+{
+  if (!c || !in || !out || nstates < 1) return c ? set_err(c, FBSE_ERR_ARG, "fbse_hpsi: bad arguments") : FBSE_ERR_ARG;
+  if (in == out) return set_err(c, FBSE_ERR_ARG, "fbse_hpsi: input and output must differ");
+  if (c->precision == FBSE_MIXED)
+    return hpsi_apply<float>(c, (const float2 *)in, (float2 *)out, nstates, 1.0, 0.0);
+  return hpsi_apply<double>(c, (const double2 *)in, (double2 *)out, nstates, 1.0, 0.0);
+}
+
+int fbse_hnorm(fbse_ctx *c, const void *in, void *out, long nstates, double vmin, double de, double zn)
+{
+  if (!c || !in || !out || nstates < 1 || !(de > 0))
+    return c ? set_err(c, FBSE_ERR_ARG, "fbse_hnorm: bad arguments") : FBSE_ERR_ARG;
+  if (in == out) return set_err(c, FBSE_ERR_ARG, "fbse_hnorm: input and output must differ");
+  const double de_1 = 4.0 / de;
+  const double b = -(2.0 + zn + vmin * de_1);
+  if (c->precision == FBSE_MIXED) return hpsi_apply<float>(c, (const float2 *)in, (float2 *)out, nstates, de_1, b);
+  return hpsi_apply<double>(c, (const double2 *)in, (double2 *)out, nstates, de_1, b);
+}
+
+int fbse_newton_filter(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin,
+                       double de, const double *psi0, long nstart, double *filtered)
+{
+  if (!c || !zn || !an || !psi0 || !filtered) return c ? set_err(c, FBSE_ERR_ARG, "fbse_newton_filter: null") : FBSE_ERR_ARG;
+  return newton_filter(c, zn, an, ncheby, m, vmin, de, psi0, nstart, filtered);
+}
+
+int fbse_energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *emax, long *iters)
+{
+  if (!c || !emin || !emax || max_iter < 1) return c ? set_err(c, FBSE_ERR_ARG, "fbse_energy_range: bad arguments") : FBSE_ERR_ARG;
+  return energy_range(c, seed, max_iter, emin, emax, iters);
+}
+
+int fbse_normalize_all(fbse_ctx *c, double *psitot, long n, double *norms)
+{
+  if (!c || !psitot) return c ? set_err(c, FBSE_ERR_ARG, "fbse_normalize_all: null") : FBSE_ERR_ARG;
+  return normalize_all(c, psitot, n, norms);
+}
+
+int fbse_energy_all(fbse_ctx *c, const double *psitot, long n, double *ene)
+{
+  if (!c || !psitot || !ene) return c ? set_err(c, FBSE_ERR_ARG, "fbse_energy_all: null") : FBSE_ERR_ARG;
+  return energy_all(c, psitot, n, ene);
+}
+
+int fbse_ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma)
+{
+  if (!c || !psitot || !n_kept || !eval || !sigma || n < 1)
+    return c ? set_err(c, FBSE_ERR_ARG, "fbse_ortho_diag_sigma: bad arguments") : FBSE_ERR_ARG;
+  return ortho_diag_sigma(c, psitot, n, n_kept, eval, sigma);
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+// Internal declarations shared by the CUDA translation units of libfbse_gpu.
+//
+// Layout in HBM (all device buffers are owned by an fbse_ctx):
+//   * a "state" is nspin blocks of ngrid complex values (spin-up block first),
+//     grid index jxyz = nx*(ny*jz + jy) + jx, interleaved (re, im) -- the same
+//     layout as the reference's zomplex arrays (filter_mpi/fd.h:333-337);
+//   * working states are complex in the context's precision (float2 for the
+//     mixed path, double2 for the plain FP64 path); real-valued jobs pack two
+//     real states into one complex state (re = state 2i, im = state 2i+1),
+//     which is exact because every operator on the filter path is real for
+//     real jobs (kinetic, local potential and the l = 1 nonlocal projector);
+//   * filtered-state accumulators and everything handed back to the caller
+//     use the reference's psi_rank / psitot layout in FP64: stlen doubles per
+//     state, 1 double per point for real jobs, (re, im) pairs otherwise.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/fbse.h"
+
+namespace fbse {
+
+// ---------------------------------------------------------------------------
+// complex helpers
+// ---------------------------------------------------------------------------
+template <typename T> struct cplx_t;
+template <> struct cplx_t<float> { using type = float2; };
+template <> struct cplx_t<double> { using type = double2; };
+template <typename T> using C = typename cplx_t<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ C<T> mk(T re, T im) { C<T> r; r.x = re; r.y = im; return r; }
+template <typename T> __host__ __device__ __forceinline__ C<T> cadd(C<T> a, C<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __host__ __device__ __forceinline__ C<T> csub(C<T> a, C<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __host__ __device__ __forceinline__ C<T> cmul(C<T> a, C<T> b)
+{
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b) when conjb, else a * b
+template <typename T> __host__ __device__ __forceinline__ C<T> cmulc(C<T> a, C<T> b, bool conjb)
+{
+  T by = conjb ? -b.y : b.y;
+  return mk<T>(a.x * b.x - a.y * by, a.x * by + a.y * b.x);
+}
+template <typename T> __host__ __device__ __forceinline__ C<T> cscale(C<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+
+// ---------------------------------------------------------------------------
+// FFT plan for one axis: mixed-radix Stockham stages + root table
+// ---------------------------------------------------------------------------
+constexpr int kMaxStages = 16;
+struct AxisPlan {
+  int n = 0;
+  int nst = 0;
+  int radix[kMaxStages] = {0};
+  double2 *tw64 = nullptr;  // device, n roots e^{-2 pi i t / n}
+  float2 *tw32 = nullptr;   // device, same roots rounded to FP32
+};
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct ProjDev {
+  long nat = 0, npts = 0;
+  int nproj = 0;
+  int so = 0, nl = 0;
+  int *nl_cnt = nullptr;      // [nat]
+  int *jxyz = nullptr;        // [nat*npts]
+  double *y1 = nullptr;       // [nat*npts*6]
+  double *sop = nullptr;      // [nat*npts*nproj]
+  double *nlp = nullptr;      // [nat*npts*nproj]
+  int *sgn = nullptr;         // [nat*nproj]
+  double2 *LS = nullptr;      // [36]
+  float *y1f = nullptr, *sopf = nullptr, *nlpf = nullptr;  // FP32 copies for the mixed path
+};
+
+}  // namespace fbse
+
+struct fbse_ctx {
+  int precision = FBSE_FP64;
+  long nx = 0, ny = 0, nz = 0, ngrid = 0;
+  int nspin = 1, is_complex = 0, so = 0, nl = 0;
+  double dx = 0, dy = 0, dz = 0, dv = 0, ke_max = 0;
+  double kemax_scaled = 0;                 // KE_max / N (init.c:338)
+  fbse::AxisPlan ax[3];                    // x, y, z
+  double *k2x = nullptr, *k2y = nullptr, *k2z = nullptr;  // per-axis 0.5 k^2 / N (device)
+  double *pot64 = nullptr;                 // [ngrid]
+  float *pot32 = nullptr;
+  double vpot_min = 0, vpot_max = 0;
+  fbse::ProjDev proj;
+  cudaStream_t stream = nullptr;
+  // scratch (grown on demand)
+  void *wk = nullptr; size_t wk_bytes = 0;       // FFT work states
+  void *coef = nullptr; size_t coef_bytes = 0;   // projector coefficients
+  void *tmp = nullptr; size_t tmp_bytes = 0;     // general
+  double *red = nullptr; size_t red_bytes = 0;   // reduction partials
+  std::string err;
+};
+
+namespace fbse {
+
+// error plumbing ------------------------------------------------------------
+int set_err(fbse_ctx *c, int code, const std::string &msg);
+#define FBSE_CUDA(ctx, call)                                                                  \
+  do {                                                                                        \
+    cudaError_t e__ = (call);                                                                 \
+    if (e__ != cudaSuccess)                                                                   \
+      return ::fbse::set_err((ctx), FBSE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
+  } while (0)
+#define FBSE_CHECK_LAUNCH(ctx) FBSE_CUDA(ctx, cudaGetLastError())
+
+int ensure(fbse_ctx *c, void **p, size_t *have, size_t need);
+
+// FFT (fft.cu) ----------------------------------------------------------------
+int plan_axis(fbse_ctx *c, AxisPlan &p, int n);
+void free_axis(AxisPlan &p);
+// kinetic part of H: out = a * (T in + V in) + b * in  (V from the context),
+// for nblk 3D blocks (states x spins).  work is a scratch of nblk*ngrid complex.
+template <typename T>
+int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b, int with_v);
+
+// projectors (hpsi.cu) --------------------------------------------------------
+template <typename T>
+int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scale);
+template <typename T>
+int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, double b);
+
+// reductions / vector ops (filter.cu) ------------------------------------------
+template <typename T>
+int state_dots(fbse_ctx *c, const C<T> *x, const C<T> *y, long nstates, long len, double *out_host, int mode);
+
+}  // namespace fbse

@@ -1,0 +1,489 @@
+// Newton filter, normalisation, energies and the spectrum range on the GPU
+// (Newton recursion, accumulation, normalisation, energies, spectrum range).
+//
+// Newton filter (replaces filter_cycle, filter_mpi/filter.c:187-371): all
+// random starts advance in lockstep as one batch.  The Newton vectors
+// phi_j = prod_{i<j}(H_s - z_i) psi_0 live in a ring of K slots: p_hnorm reads
+// slot (j-1) % K and writes slot j % K (no copies), and every K terms one
+// accumulation kernel forms F_t += sum_q a_{t,j0+q} phi_{j0+q} for all m
+// targets, so the m accumulators are read and written once per K terms
+// instead of once per term (filter.c:329-359 touches all m every term).
+// Accumulators are FP64 in the reference's psi_rank layout.
+#include <cmath>
+
+#include "fbse_internal.cuh"
+
+namespace fbse {
+
+constexpr int kMaxTargets = 32;
+
+// ---------------------------------------------------------------------------
+// psitot (FP64, stlen per state) <-> working complex states
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_pack(const double *__restrict__ src, C<T> *__restrict__ dst, long nsrc, long len, int cplx)
+{
+  // len = nspin*ngrid complex elements per working state
+  const long nw = cplx ? nsrc : (nsrc + 1) / 2;
+  const long total = nw * len;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const long w = i / len, k = i - w * len;
+    if (cplx) {
+      const double *s = src + w * 2 * len;
+      dst[i] = mk<T>((T)s[2 * k], (T)s[2 * k + 1]);
+    } else {
+      const double re = src[(2 * w) * len + k];
+      const double im = (2 * w + 1 < nsrc) ? src[(2 * w + 1) * len + k] : 0.0;
+      dst[i] = mk<T>((T)re, (T)im);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_unpack(const C<T> *__restrict__ src, double *__restrict__ dst, long ndst, long len, int cplx)
+{
+  const long nw = cplx ? ndst : (ndst + 1) / 2;
+  const long total = nw * len;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const long w = i / len, k = i - w * len;
+    const C<T> v = src[i];
+    if (cplx) {
+      dst[w * 2 * len + 2 * k] = (double)v.x;
+      dst[w * 2 * len + 2 * k + 1] = (double)v.y;
+    } else {
+      dst[(2 * w) * len + k] = (double)v.x;
+      if (2 * w + 1 < ndst) dst[(2 * w + 1) * len + k] = (double)v.y;
+    }
+  }
+}
+
+static unsigned grid_for(long n, int threads = 256)
+{
+  long g = (n + threads - 1) / threads;
+  if (g > 152L * 32) g = 152L * 32;  // a few waves over the 152 SMs, grid-stride beyond
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+template <typename T>
+int pack(fbse_ctx *c, const double *src, C<T> *dst, long nsrc)
+{
+  const long len = (long)c->nspin * c->ngrid;
+  const long nw = c->is_complex ? nsrc : (nsrc + 1) / 2;
+  k_pack<T><<<grid_for(nw * len), 256, 0, c->stream>>>(src, dst, nsrc, len, c->is_complex);
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+template <typename T>
+int unpack(fbse_ctx *c, const C<T> *src, double *dst, long ndst)
+{
+  const long len = (long)c->nspin * c->ngrid;
+  const long nw = c->is_complex ? ndst : (ndst + 1) / 2;
+  k_unpack<T><<<grid_for(nw * len), 256, 0, c->stream>>>(src, dst, ndst, len, c->is_complex);
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// K-blocked Newton accumulation into the psi_rank layout
+// F[start][t] (+)= sum_q a[t][j0+q] * ring[(j0+q) % K][w]
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_newton_acc(const C<T> *__restrict__ ring, long K, long j0, int nk,
+                                                   const double *__restrict__ a, long ncheby, int m,
+                                                   double *__restrict__ F, long nstart, long nw, long len, int cplx,
+                                                   int init)
+{
+  __shared__ double as[kMaxTargets * 64];
+  for (int i = threadIdx.x; i < m * nk; i += blockDim.x) {
+    const int t = i / nk, q = i % nk;
+    as[t * nk + q] = a[t * ncheby + j0 + q];
+  }
+  __syncthreads();
+  const long slot_stride = nw * len;
+  const long total = nw * len;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const long w = i / len, k = i - w * len;
+    double ar[kMaxTargets], ai[kMaxTargets];
+#pragma unroll
+    for (int t = 0; t < kMaxTargets; t++) { ar[t] = 0.0; ai[t] = 0.0; }
+    for (int q = 0; q < nk; q++) {
+      const long slot = (j0 + q) % K;
+      const C<T> v = ring[slot * slot_stride + i];
+      const double vr = (double)v.x, vi = (double)v.y;
+#pragma unroll
+      for (int t = 0; t < kMaxTargets; t++) {
+        if (t < m) {
+          const double co = as[t * nk + q];
+          ar[t] += co * vr;
+          ai[t] += co * vi;
+        }
+      }
+    }
+    // psi_rank layout: ns_block = jns*m*stlen, jstate = ns_block + t*stlen
+#pragma unroll
+    for (int t = 0; t < kMaxTargets; t++) {
+      if (t < m) {
+        if (cplx) {
+          double *d = F + ((w * m + t) * len + k) * 2;
+          if (init) { d[0] = ar[t]; d[1] = ai[t]; }
+          else { d[0] += ar[t]; d[1] += ai[t]; }
+        } else {
+          double *d0 = F + ((2 * w) * m + t) * len + k;
+          if (init) d0[0] = ar[t];
+          else d0[0] += ar[t];
+          if (2 * w + 1 < nstart) {
+            double *d1 = F + ((2 * w + 1) * m + t) * len + k;
+            if (init) d1[0] = ai[t];
+            else d1[0] += ai[t];
+          }
+        }
+      }
+    }
+  }
+}
+
+template <typename T>
+static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin,
+                           double de, const double *psi0, long nstart, double *filtered)
+{
+  const long len = (long)c->nspin * c->ngrid;
+  const long nw = c->is_complex ? nstart : (nstart + 1) / 2;
+  const long K = ncheby < 32 ? ncheby : 32;
+  // Newton coefficients: real parts only (gen_newton_coeff's are real)
+  std::vector<double> are((size_t)m * ncheby);
+  for (long t = 0; t < m; t++)
+    for (long j = 0; j < ncheby; j++) {
+      if (an[2 * (t * ncheby + j) + 1] != 0.0)
+        return set_err(c, FBSE_ERR_UNSUPPORTED, "complex Newton coefficients are not supported");
+      are[t * ncheby + j] = an[2 * (t * ncheby + j)];
+    }
+  double *a_dev = nullptr;
+  C<T> *ring = nullptr;
+  const size_t ring_bytes = (size_t)K * nw * len * sizeof(C<T>);
+  int rc = FBSE_OK;
+  if (cudaMalloc(&a_dev, are.size() * sizeof(double)) != cudaSuccess)
+    return set_err(c, FBSE_ERR_OOM, "newton coefficients");
+  if (cudaMalloc(&ring, ring_bytes) != cudaSuccess) {
+    cudaFree(a_dev);
+    return set_err(c, FBSE_ERR_OOM, "newton ring buffer");
+  }
+  const double de_1 = 4.0 / de;
+  do {
+    if (cudaMemcpyAsync(a_dev, are.data(), are.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream) !=
+        cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "coefficient upload"); break; }
+    if ((rc = pack<T>(c, psi0, ring, nstart))) break;
+    const long slot_stride = nw * len;
+    for (long jc = 0; jc < ncheby; jc++) {
+      if (jc > 0) {
+        const C<T> *src = ring + ((jc - 1) % K) * slot_stride;
+        C<T> *dst = ring + (jc % K) * slot_stride;
+        // p_hnorm: dE_1 * H psi - (2 + zn + Vmin * dE_1) psi   (filter.c:401-407)
+        if ((rc = hpsi_apply<T>(c, src, dst, nw, de_1, -(2.0 + zn[jc - 1] + vmin * de_1)))) break;
+      }
+      if ((jc % K) == K - 1 || jc == ncheby - 1) {
+        const long j0 = jc - (jc % K);
+        const int nk = (int)(jc - j0 + 1);
+        k_newton_acc<T><<<grid_for(nw * len), 256, 0, c->stream>>>(ring, K, j0, nk, a_dev, ncheby, (int)m, filtered,
+                                                                   nstart, nw, len, c->is_complex, j0 == 0);
+        if (cudaGetLastError() != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "newton accumulation launch"); break; }
+      }
+    }
+    if (rc) break;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "newton filter");
+  } while (0);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(ring);
+  cudaFree(a_dev);
+  return rc;
+}
+
+int newton_filter(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
+                  const double *psi0, long nstart, double *filtered)
+{
+  if (m < 1 || m > kMaxTargets) return set_err(c, FBSE_ERR_UNSUPPORTED, "mStatesPerFilter must be 1..32");
+  if (ncheby < 1 || nstart < 1) return set_err(c, FBSE_ERR_ARG, "ncheby and nstart must be positive");
+  if (!(de > 0)) return set_err(c, FBSE_ERR_ARG, "dE must be positive");
+  if (c->precision == FBSE_MIXED)
+    return newton_filter_t<float>(c, zn, an, ncheby, m, vmin, de, psi0, nstart, filtered);
+  return newton_filter_t<double>(c, zn, an, ncheby, m, vmin, de, psi0, nstart, filtered);
+}
+
+// ---------------------------------------------------------------------------
+// per-state reductions, FP64 accumulation, deterministic two-stage
+//   mode 0: sum |x|^2            (one output per state)
+//   mode 1: sum Re(conj(x) y)    (one output per state)
+//   mode 2: sum x.re*y.re and sum x.im*y.im   (two outputs per state:
+//           the two packed real states of a working state)
+// ---------------------------------------------------------------------------
+constexpr int kRedBlocks = 64;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dots(const C<T> *__restrict__ x, const C<T> *__restrict__ y, long len,
+                                              int mode, double *__restrict__ part)
+{
+  const long st = blockIdx.y;
+  const C<T> *xs = x + st * len;
+  const C<T> *ys = y ? y + st * len : nullptr;
+  double s0 = 0.0, s1 = 0.0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < len; k += (long)gridDim.x * blockDim.x) {
+    const C<T> a = xs[k];
+    if (mode == 0) {
+      s0 += (double)a.x * a.x + (double)a.y * a.y;
+    } else {
+      const C<T> b = ys[k];
+      if (mode == 1) s0 += (double)a.x * b.x + (double)a.y * b.y;
+      else { s0 += (double)a.x * b.x; s1 += (double)a.y * b.y; }
+    }
+  }
+  __shared__ double r0[8], r1[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+  }
+  if ((threadIdx.x & 31) == 0) { r0[threadIdx.x >> 5] = s0; r1[threadIdx.x >> 5] = s1; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a0 = 0, a1 = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a0 += r0[w]; a1 += r1[w]; }
+    part[(st * gridDim.x + blockIdx.x) * 2] = a0;
+    part[(st * gridDim.x + blockIdx.x) * 2 + 1] = a1;
+  }
+}
+
+__global__ void k_dots_final(const double *__restrict__ part, int nb, long nstates, double *__restrict__ out)
+{
+  for (long st = blockIdx.x * (long)blockDim.x + threadIdx.x; st < nstates; st += (long)gridDim.x * blockDim.x) {
+    double a0 = 0, a1 = 0;
+    for (int b = 0; b < nb; b++) { a0 += part[(st * nb + b) * 2]; a1 += part[(st * nb + b) * 2 + 1]; }
+    out[2 * st] = a0;
+    out[2 * st + 1] = a1;
+  }
+}
+
+// out_dev: 2 doubles per state (second used by mode 2)
+template <typename T>
+int state_dots_dev(fbse_ctx *c, const C<T> *x, const C<T> *y, long nstates, long len, int mode, double *out_dev)
+{
+  const size_t need = (size_t)nstates * kRedBlocks * 2 * sizeof(double);
+  int rc = ensure(c, (void **)&c->red, &c->red_bytes, need);
+  if (rc) return rc;
+  if (nstates > 65535) return set_err(c, FBSE_ERR_UNSUPPORTED, "too many states for one reduction");
+  dim3 g(kRedBlocks, (unsigned)nstates);
+  k_dots<T><<<g, 256, 0, c->stream>>>(x, y, len, mode, c->red);
+  FBSE_CHECK_LAUNCH(c);
+  k_dots_final<<<(unsigned)((nstates + 127) / 128), 128, 0, c->stream>>>(c->red, kRedBlocks, nstates, out_dev);
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+template <typename T>
+int state_dots(fbse_ctx *c, const C<T> *x, const C<T> *y, long nstates, long len, double *out_host, int mode)
+{
+  double *d = nullptr;
+  if (cudaMalloc(&d, nstates * 2 * sizeof(double)) != cudaSuccess) return set_err(c, FBSE_ERR_OOM, "dots");
+  int rc = state_dots_dev<T>(c, x, y, nstates, len, mode, d);
+  if (!rc && cudaMemcpyAsync(out_host, d, nstates * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+    rc = set_err(c, FBSE_ERR_CUDA, "dots download");
+  if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "dots sync");
+  cudaFree(d);
+  return rc;
+}
+template int state_dots<float>(fbse_ctx *, const C<float> *, const C<float> *, long, long, double *, int);
+template int state_dots<double>(fbse_ctx *, const C<double> *, const C<double> *, long, long, double *, int);
+
+// ---------------------------------------------------------------------------
+// psitot-level normalisation / energies
+// ---------------------------------------------------------------------------
+__global__ void k_sumsq(const double *__restrict__ x, long len, double *__restrict__ part)
+{
+  const long st = blockIdx.y;
+  const double *xs = x + st * len;
+  double s = 0.0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < len; k += (long)gridDim.x * blockDim.x)
+    s += xs[k] * xs[k];
+  __shared__ double r[8];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) r[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) a += r[w];
+    part[(st * gridDim.x + blockIdx.x) * 2] = a;
+    part[(st * gridDim.x + blockIdx.x) * 2 + 1] = 0.0;
+  }
+}
+
+__global__ void k_scale_states(double *__restrict__ x, long len, long n, const double *__restrict__ f)
+{
+  const long total = n * len;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x)
+    x[i] *= f[i / len];
+}
+
+int normalize_all(fbse_ctx *c, double *psitot, long n, double *norms)
+{
+  const long stlen = (long)(c->is_complex + 1) * c->nspin * c->ngrid;
+  if (n < 1) return FBSE_OK;
+  if (n > 65535) return set_err(c, FBSE_ERR_UNSUPPORTED, "too many states for one reduction");
+  int rc = ensure(c, (void **)&c->red, &c->red_bytes, (size_t)n * kRedBlocks * 2 * sizeof(double));
+  if (rc) return rc;
+  double *d = nullptr;
+  if (cudaMalloc(&d, n * 2 * sizeof(double)) != cudaSuccess) return set_err(c, FBSE_ERR_OOM, "norms");
+  std::vector<double> h(2 * n), f(n);
+  do {
+    k_sumsq<<<dim3(kRedBlocks, (unsigned)n), 256, 0, c->stream>>>(psitot, stlen, c->red);
+    k_dots_final<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(c->red, kRedBlocks, n, d);
+    if (cudaMemcpyAsync(h.data(), d, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "norm reduction"); break; }
+    for (long i = 0; i < n; i++) {
+      const double nr = h[2 * i] * c->dv;  // norm.c:138-140
+      if (norms) norms[i] = nr;
+      if (nr == 0.0) { rc = set_err(c, FBSE_ERR_NAN, "Norm is 0! exiting!"); break; }
+      if (std::isnan(nr)) { rc = set_err(c, FBSE_ERR_NAN, "Norm is NAN! exiting!"); break; }
+      f[i] = 1.0 / std::sqrt(nr);
+    }
+    if (rc) break;
+    if (cudaMemcpyAsync(d, f.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "norm upload");
+      break;
+    }
+    k_scale_states<<<grid_for(n * stlen), 256, 0, c->stream>>>(psitot, stlen, n, d);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "normalize");
+  } while (0);
+  cudaFree(d);
+  return rc;
+}
+
+template <typename T>
+static int energy_all_t(fbse_ctx *c, const double *psitot, long n, double *ene)
+{
+  const long len = (long)c->nspin * c->ngrid;
+  const long nw = c->is_complex ? n : (n + 1) / 2;
+  // process in chunks of working states to bound scratch
+  const long chunk = nw < 16 ? nw : 16;
+  C<T> *buf = nullptr;
+  if (cudaMalloc(&buf, 2 * chunk * len * sizeof(C<T>)) != cudaSuccess) return set_err(c, FBSE_ERR_OOM, "energy_all");
+  std::vector<double> h(2 * chunk);
+  int rc = FBSE_OK;
+  const long stlen = (long)(c->is_complex + 1) * len;
+  for (long w0 = 0; w0 < nw && !rc; w0 += chunk) {
+    const long cw = (nw - w0 < chunk) ? nw - w0 : chunk;
+    const long s0 = c->is_complex ? w0 : 2 * w0;
+    const long ns = c->is_complex ? cw : ((n - s0) < 2 * cw ? n - s0 : 2 * cw);
+    if ((rc = pack<T>(c, psitot + s0 * stlen, buf, ns))) break;
+    if ((rc = hpsi_apply<T>(c, buf, buf + chunk * len, cw, 1.0, 0.0))) break;
+    if ((rc = state_dots<T>(c, buf, buf + chunk * len, cw, len, h.data(), c->is_complex ? 1 : 2))) break;
+    for (long w = 0; w < cw; w++) {
+      if (c->is_complex) ene[s0 + w] = h[2 * w] * c->dv;
+      else {
+        ene[s0 + 2 * w] = h[2 * w] * c->dv;
+        if (s0 + 2 * w + 1 < n) ene[s0 + 2 * w + 1] = h[2 * w + 1] * c->dv;
+      }
+    }
+  }
+  cudaFree(buf);
+  return rc;
+}
+
+int energy_all(fbse_ctx *c, const double *psitot, long n, double *ene)
+{
+  if (n < 1) return FBSE_OK;
+  return c->precision == FBSE_MIXED ? energy_all_t<float>(c, psitot, n, ene) : energy_all_t<double>(c, psitot, n, ene);
+}
+
+// ---------------------------------------------------------------------------
+// spectrum range (energy.c:169-379, iterative branch)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_axpby(C<T> *__restrict__ y, const C<T> *__restrict__ x, long len, double a, double b)
+{  // y = a*y + b*x
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < len; i += (long)gridDim.x * blockDim.x) {
+    C<T> v = y[i], u = x[i];
+    y[i] = mk<T>((T)(a * v.x + b * u.x), (T)(a * v.y + b * u.y));
+  }
+}
+
+template <typename T>
+__global__ void k_cast_in(const double *__restrict__ s, C<T> *__restrict__ d, long len)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < len; i += (long)gridDim.x * blockDim.x)
+    d[i] = mk<T>((T)s[2 * i], (T)s[2 * i + 1]);
+}
+
+extern "C" long fbse_host_init_psi(double *psi, long seed, long ngrid, int is_complex, double dv);
+
+template <typename T>
+static int energy_range_t(fbse_ctx *c, long seed, long max_iter, double *emin_out, double *emax_out, long *iters)
+{
+  const long len = (long)c->nspin * c->ngrid;
+  C<T> *buf = nullptr;  // phi, h
+  double *hd = nullptr;
+  if (cudaMalloc(&buf, 2 * len * sizeof(C<T>)) != cudaSuccess) return set_err(c, FBSE_ERR_OOM, "energy range");
+  if (cudaMalloc(&hd, len * 2 * sizeof(double)) != cudaSuccess) { cudaFree(buf); return set_err(c, FBSE_ERR_OOM, "energy range"); }
+  C<T> *phi = buf, *h = buf + len;
+  std::vector<double> host(2 * len);
+  double dd[2];
+  int rc = FBSE_OK;
+  long it_total = 0;
+  auto draw = [&](void) -> int {
+    for (int s = 0; s < c->nspin; s++) seed = fbse_host_init_psi(host.data() + 2 * s * c->ngrid, seed, c->ngrid, c->is_complex, c->dv);
+    if (cudaMemcpyAsync(hd, host.data(), len * 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+      return set_err(c, FBSE_ERR_CUDA, "energy range upload");
+    k_cast_in<T><<<grid_for(len), 256, 0, c->stream>>>(hd, phi, len);
+    FBSE_CHECK_LAUNCH(c);
+    return FBSE_OK;
+  };
+  do {
+    // ---- E_min: phi <- normalize(phi - tau H phi)   (energy.c:221-271)
+    if ((rc = draw())) break;
+    double tau = 0.05, emin = 10.0, old = 0.0;
+    if ((rc = hpsi_apply<T>(c, phi, h, 1, 1.0, 0.0))) break;
+    for (long i = 0; std::fabs((emin - old) / emin) > 1.0e-6 && i < max_iter; i++) {
+      // h holds H phi_i
+      k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, h, len, 1.0, -tau);
+      if ((rc = state_dots<T>(c, phi, nullptr, 1, len, dd, 0))) break;
+      const double nrm = std::sqrt(dd[0] * c->dv);
+      k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, phi, len, 1.0 / nrm, 0.0);
+      if ((rc = hpsi_apply<T>(c, phi, h, 1, 1.0, 0.0))) break;
+      if ((rc = state_dots<T>(c, phi, h, 1, len, dd, 1))) break;
+      old = emin;
+      emin = dd[0] * c->dv;
+      if (i > 5 && (emin - old) > 0) tau -= 0.025;  // energy.c:262-269
+      it_total++;
+    }
+    if (rc) break;
+    // ---- E_max: power iteration psi <- normalize(H psi)   (energy.c:281-303)
+    if ((rc = draw())) break;
+    double emax = 0.1;
+    old = 0.0;
+    if ((rc = hpsi_apply<T>(c, phi, h, 1, 1.0, 0.0))) break;
+    for (long i = 0; std::fabs((emax - old) / emax) > 1.0e-6 && i < max_iter; i++) {
+      if ((rc = state_dots<T>(c, h, nullptr, 1, len, dd, 0))) break;
+      const double nrm = std::sqrt(dd[0] * c->dv);
+      k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, h, len, 0.0, 1.0 / nrm);
+      if ((rc = hpsi_apply<T>(c, phi, h, 1, 1.0, 0.0))) break;
+      if ((rc = state_dots<T>(c, phi, h, 1, len, dd, 1))) break;
+      old = emax;
+      emax = dd[0] * c->dv;
+      it_total++;
+    }
+    if (rc) break;
+    *emin_out = emin;
+    *emax_out = emax;
+    if (iters) *iters = it_total;
+  } while (0);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(buf);
+  cudaFree(hd);
+  return rc;
+}
+
+int energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *emax, long *iters)
+{
+  return c->precision == FBSE_MIXED ? energy_range_t<float>(c, seed, max_iter, emin, emax, iters)
+                                    : energy_range_t<double>(c, seed, max_iter, emin, emax, iters);
+}
+
+}  // namespace fbse

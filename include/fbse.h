@@ -1,0 +1,180 @@
+/*
+ * fbse.h -- C ABI of libfbse_gpu, the GB300 (sm_103a) implementation of
+ * FilterBSE's filter-diagonalization hot path.
+ *
+ * Plain C: pointers, sizes and POD descriptors only.  Every entry point
+ * returns FBSE_OK (0) or a negative FBSE_ERR_* code; the message of the last
+ * failure is available from fbse_last_error().  Callers that mirror the
+ * reference's error behaviour print that message to stderr and
+ * exit(EXIT_FAILURE) (as filter_mpi/norm.c:150-159 and read.c:875 do).
+ *
+ * Memory: a context owns all of its device scratch.  State arrays passed to
+ * the compute entry points are DEVICE pointers (allocate them with
+ * fbse_alloc or any CUDA allocator on the context's device); the host-side
+ * helpers at the end of this header work on host memory.  All work is
+ * ordered on the context's stream; entry points that return host values
+ * synchronise that stream.
+ *
+ * State layouts (the reference's, filter_mpi/fd.h:333-337):
+ *   "zomplex state": nspin blocks of ngrid complex values (spin-up first),
+ *     grid index jxyz = nx*(ny*jz + jy) + jx, interleaved (re, im), in the
+ *     context's working precision (double for FBSE_FP64, float for
+ *     FBSE_MIXED).  Used by fbse_hpsi / fbse_hnorm.
+ *   "psitot state": stlen = complex_idx * nspin * ngrid doubles, i.e. one
+ *     double per point for real jobs and (re, im) pairs for complex jobs --
+ *     the layout of psi_rank / psitot / psi.dat.  Always FP64.
+ */
+#ifndef FBSE_H
+#define FBSE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FBSE_OK 0
+#define FBSE_ERR_ARG (-1)         /* invalid argument or size */
+#define FBSE_ERR_CUDA (-2)        /* CUDA runtime error (message has details) */
+#define FBSE_ERR_OOM (-3)         /* device allocation failed */
+#define FBSE_ERR_NAN (-4)         /* zero or NaN norm (filter_mpi/norm.c:150-159) */
+#define FBSE_ERR_STATE (-5)       /* call out of order / missing setup */
+#define FBSE_ERR_UNSUPPORTED (-6) /* configuration not supported by this build */
+#define FBSE_ERR_NOCONV (-7)      /* an iterative solver hit its iteration limit */
+
+enum { FBSE_FP64 = 0, FBSE_MIXED = 1 };
+
+typedef struct fbse_ctx fbse_ctx;
+
+/* Grid and job switches: the fields of grid_st / index_st / flag_st that the
+ * hot path reads (filter_mpi/fd.h:30-91, 96-163, 257-299). */
+typedef struct fbse_grid_desc {
+  long nx, ny, nz;   /* grid points per axis (any sizes) */
+  double dx, dy, dz; /* spacing, bohr */
+  double ke_max;     /* KEmax, Ha: kinetic cap (filter_mpi/init.c:338-349) */
+  int nspin;         /* 1, or 2 for spinors */
+  int is_complex;    /* flag->isComplex (complex_idx - 1) */
+  int so;            /* flag->SO: spin-orbit projectors */
+  int nl;            /* flag->NL: nonlocal projectors */
+  double dkx, dky, dkz; /* reciprocal spacings; 0 = derived as init_grid_params does
+                           (2 pi / (n d) for even n, 2 pi / ((n - 1) d) for odd n,
+                           filter_mpi/init.c:65-80); set them to reproduce runs of
+                           older versions that used 2 pi / (n d) for every n */
+} fbse_grid_desc;
+
+/* Projector table: a structure-of-arrays copy of the reference's nlc_st
+ * array (filter_mpi/fd.h:382-398) as built by init_NL_projectors
+ * (filter_mpi/init.c, body lines 508-589).  Row stride npts = n_NL_gridpts. */
+typedef struct fbse_proj_desc {
+  long n_atoms;          /* n_NL_atoms (ligands excluded, filter_mpi/read.c:1102) */
+  long npts;             /* n_NL_gridpts: row stride */
+  int nproj;             /* ist->nproj (5) */
+  const long *nl;        /* [n_atoms] points used per atom */
+  const int *jxyz;       /* [n_atoms*npts] grid index of each point */
+  const double *y1;      /* [n_atoms*npts][3][2] Y_1m, m = 0..2, (re, im) */
+  const double *so_proj; /* [n_atoms*npts][nproj] SO radial (x sqrt(SO_par)) */
+  const double *nl_proj; /* [n_atoms*npts][nproj] NL radial */
+  const int *nl_sign;    /* [n_atoms][nproj] sign of each NL channel */
+  const double *LS;      /* [6][6][2] L.S, LS[(j'*6 + j)] (re, im); NULL: built as def_LS does */
+} fbse_proj_desc;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Replaces the setup of mod_mem_alloc / mod_pseudopot (filter_mpi/mod_mem.c:3,
+ * filter_mpi/mod_pseudopot.c:3): uploads the local potential (ngrid doubles;
+ * the reference stores it twice, filter_mpi/init.c:666 -- pass one copy) and
+ * the projector table, and plans the FFTs.  proj may be NULL when so = nl = 0.
+ * precision: FBSE_FP64 (plain) or FBSE_MIXED (FP32 recursion and FFTs). */
+int fbse_create(fbse_ctx **out, const fbse_grid_desc *grid, const double *pot_local,
+                const fbse_proj_desc *proj, int precision);
+void fbse_destroy(fbse_ctx *ctx);
+const char *fbse_last_error(const fbse_ctx *ctx);
+int fbse_version(void);
+
+/* ---- device memory helpers --------------------------------------------- */
+int fbse_alloc(fbse_ctx *ctx, void **dptr, size_t bytes);
+int fbse_free(fbse_ctx *ctx, void *dptr);
+int fbse_upload(fbse_ctx *ctx, void *dst_dev, const void *src_host, size_t bytes);
+int fbse_download(fbse_ctx *ctx, void *dst_host, const void *src_dev, size_t bytes);
+int fbse_sync(fbse_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t) so callers can order their own
+ * work and events with the context's kernels. */
+void *fbse_stream(fbse_ctx *ctx);
+
+/* ---- H psi ------------------------------------------------------------------
+ * Replaces p_hamiltonian (filter_mpi/phamiltonian.c:10-60) for a batch:
+ * psi_out[s] = H psi_in[s] for nstates zomplex states.  For real jobs the two
+ * channels are two independent real states (H is real), so a real state in
+ * .re with .im = 0 gives the reference's real-path result in .re. */
+int fbse_hpsi(fbse_ctx *ctx, const void *psi_in, void *psi_out, long nstates);
+
+/* Replaces p_hnorm (filter_mpi/filter.c:375-410): psi_out = (4/dE)(H psi_in)
+ * - (2 + zn + 4 Vmin/dE) psi_in, for nstates zomplex states. */
+int fbse_hnorm(fbse_ctx *ctx, const void *psi_in, void *psi_out, long nstates, double vmin, double de, double zn);
+
+/* ---- Newton filter -------------------------------------------------------
+ * Replaces filter_cycle (filter_mpi/filter.c:187-371) for nstart random starts
+ * at once.  zn: ncheby sample points (host); an: [m][ncheby] complex Newton
+ * coefficients (host, interleaved; imaginary parts must be 0, which
+ * gen_newton_coeff always produces); psi0: [nstart] psitot states (device);
+ * filtered: [nstart][m] psitot states (device) -- the psi_rank layout
+ * (ns_block = jns*m*stlen, filter_mpi/filter.c:231). */
+int fbse_newton_filter(fbse_ctx *ctx, const double *zn, const double *an, long ncheby, long m, double vmin,
+                       double de, const double *psi0, long nstart, double *filtered);
+
+/* ---- spectrum range ------------------------------------------------------
+ * Replaces the iterative branch of get_energy_range (filter_mpi/energy.c:
+ * 169-379): imaginary-time descent (tau = 0.05) for Emin and power iteration
+ * for Emax from random states drawn with the reference's generator starting
+ * at `seed` (the reference uses -874917403), stopping at a relative change
+ * below 1e-6 or max_iter iterations.  Returns the raw Emin / Emax; the
+ * range inflation is applied by fbse_inflate_range. */
+int fbse_energy_range(fbse_ctx *ctx, long seed, long max_iter, double *emin, double *emax, long *iters);
+
+/* ---- normalisation and energies ------------------------------------------
+ * normalize_all (filter_mpi/norm.c:82-179) and energy_all
+ * (filter_mpi/energy.c:61-165) over n psitot states (device).  norms / ene
+ * are host arrays of n doubles (may be NULL for norms).  A zero or NaN norm
+ * returns FBSE_ERR_NAN. */
+int fbse_normalize_all(fbse_ctx *ctx, double *psitot, long n, double *norms);
+int fbse_energy_all(fbse_ctx *ctx, const double *psitot, long n, double *ene);
+
+/* ---- orthogonalisation, subspace diagonalisation, sigma_E ----------------
+ * Replaces mod_ortho + mod_diag + mod_sigma (filter_mpi/mod_ortho.c:3-94,
+ * mod_diag.c:324-449, mod_sigma.c:6-63) for n psitot states (device, in
+ * place): the span is orthonormalised (overlap eigen-decomposition, rank
+ * cutoff s_i/s_0 < 1e-10 as SVDEPS in filter_mpi/fd.h), H is diagonalised in
+ * it in FP64 on the GPU, the first n_kept states are overwritten with the
+ * eigenvectors (ascending eigenvalue, normalised), and eval / sigma (host,
+ * n doubles each) receive E_i = <psi_i|H|psi_i> and
+ * sigma_i = ||(H - E_i) psi_i||, which equals the reference's
+ * sqrt|<H^2> - <H>^2| for normalised states. */
+int fbse_ortho_diag_sigma(fbse_ctx *ctx, double *psitot, long n, long *n_kept, double *eval, double *sigma);
+
+/* ---- host-side helpers (no device work) --------------------------------- */
+
+/* samp_points_ashkenazy on [-2, 2] (filter_mpi/coeff.c:227-293): writes
+ * ncheby Leja-type nodes to zn (host) and returns the capacity estimate. */
+double fbse_samp_points(long ncheby, double *zn);
+
+/* gen_newton_coeff (filter_mpi/coeff.c:8-118): an is [m][ncheby] complex
+ * (host, interleaved); dt = (ncheby / (2.5 dE))^2 as filter_mpi/mod_filter.c:114. */
+int fbse_newton_coeff(long ncheby, long m, const double *zn, const double *targets, double vmin, double de,
+                      double dt, double *an);
+
+/* ran_nrc (filter_mpi/rand.c:22-62): the reference's generator with its
+ * process-wide state.  Returns one U(0,1) draw and advances *seed. */
+double fbse_ran(long *seed);
+
+/* init_filter_states (filter_mpi/init.c:659-774) without file output:
+ * n_filters random starts into psitot states (host, nspin*ngrid*complex_idx
+ * doubles each), each spin block drawn and normalised on its own.  Returns the
+ * advanced seed; seeds_out (may be NULL) receives the n_filters*nspin seeds the
+ * reference prints to seed-<rank>.dat. */
+long fbse_init_filter_states(double *psitot, long n_filters, long ngrid, int nspin, int is_complex, double dv,
+                             long seed, long *seeds_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FBSE_H */

@@ -1,0 +1,543 @@
+"""FP64 CPU oracle for FilterBSE's filter hot path (TEST INFRASTRUCTURE ONLY).
+
+This module is the checker the CUDA path is compared against.  Only tests/,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import it;
+the product package ``filterbse_gb300`` never does.
+
+The loop-heavy pieces are a C restatement (``oracle/fbse_oracle.c``, built to
+``oracle/liboracle.so``); the 3D FFT of the kinetic term uses numpy's FFT with
+FFTW's conventions (forward e^{-i}, unnormalised backward), and the LAPACK
+steps (SVD, symmetric/Hermitian eigensolves) use numpy.linalg.  Every routine
+cites the reference function it restates (paths relative to the FilterBSE tree).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "liboracle.so")
+_lib = None
+
+PROJ_LEN = 1024  # filter_mpi/fd.h: PROJ_LEN
+NPROJ = 5  # filter_mpi/read.c: ist->nproj default
+
+_D = ctypes.POINTER(ctypes.c_double)
+_L = ctypes.POINTER(ctypes.c_long)
+_I = ctypes.POINTER(ctypes.c_int)
+
+
+def build(force: bool = False) -> str:
+    """Compile the C restatement to oracle/liboracle.so (gcc, -O2, no -ffast-math)."""
+    src = os.path.join(_HERE, "fbse_oracle.c")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu99", "-o", _LIB_PATH, src, "-lm"])
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(_LIB_PATH)
+        _lib.orc_ran.restype = ctypes.c_double
+        _lib.orc_ran_fill.restype = ctypes.c_long
+        _lib.orc_ran_fill.argtypes = [ctypes.c_long, ctypes.c_long, _D]
+        _lib.orc_init_psi.restype = ctypes.c_long
+        _lib.orc_init_psi.argtypes = [_D, ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_double]
+        _lib.orc_samp_points.restype = ctypes.c_double
+        _lib.orc_samp_points.argtypes = [ctypes.c_long, ctypes.c_double, ctypes.c_double, _D, _D]
+        _lib.orc_newton_coeff.argtypes = [ctypes.c_long, ctypes.c_long, _D, _D, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, _D]
+        _lib.orc_axis_ksqr.argtypes = [ctypes.c_long, ctypes.c_double, ctypes.c_double, _D]
+        _lib.orc_ksqr.argtypes = [ctypes.c_long] * 3 + [ctypes.c_double] * 4 + [_D]
+        _lib.orc_local_pot.argtypes = [ctypes.c_long] * 3 + [_D] * 3 + [ctypes.c_long, _D, _D, _D, _L,
+                                                                         _D, _D, _L, _L, _D, _D]
+        _lib.orc_proj_matrix.argtypes = [ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double, _D]
+        _lib.orc_proj_radial.argtypes = [ctypes.c_long, ctypes.c_double, ctypes.c_double, _D,
+                                         ctypes.c_double, _D]
+        _lib.orc_nlc_table.argtypes = ([ctypes.c_long] * 3 + [_D] * 3 + [ctypes.c_long, _D, _D, _D, _D,
+                                       ctypes.c_double, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D, _D,
+                                       _L, _I, _D, _D, _D])
+        _lib.orc_def_LS.argtypes = [_D]
+        _lib.orc_apply_so.argtypes = [_D, _D, ctypes.c_long, ctypes.c_long, _L, ctypes.c_long, ctypes.c_long,
+                                      _I, _D, _D, _D, ctypes.c_double]
+        _lib.orc_apply_nl.argtypes = [_D, _D, ctypes.c_long, ctypes.c_int, ctypes.c_long, _L, ctypes.c_long,
+                                      ctypes.c_long, _I, _D, _D, _I, ctypes.c_double]
+        _lib.orc_apply_vloc.argtypes = [_D, _D, _D, ctypes.c_long, ctypes.c_int, ctypes.c_int]
+        _lib.orc_hnorm_shift.argtypes = [_D, _D, ctypes.c_long] + [ctypes.c_double] * 3
+    return _lib
+
+
+def _p(a, t=_D):
+    return a.ctypes.data_as(t)
+
+
+# --------------------------------------------------------------------------
+# Random starts, Newton coefficients
+# --------------------------------------------------------------------------
+
+def ran_fill(seed: int, n: int, out: bool = True):
+    """n draws of ran_nrc (filter_mpi/rand.c:22-62); returns (values, new seed)."""
+    buf = np.empty(n) if out else None
+    s = lib().orc_ran_fill(seed, n, _p(buf) if out else None)
+    return buf, s
+
+
+def init_psi(seed: int, ngrid: int, is_complex: bool, dv: float):
+    """init_psi (filter_mpi/init.c:777-826): one normalised random block."""
+    psi = np.empty(2 * ngrid)
+    s = lib().orc_init_psi(_p(psi), seed, ngrid, int(is_complex), dv)
+    return psi.view(np.complex128), s
+
+
+def init_filter_states(seed: int, n_filters: int, ngrid: int, nspin: int, is_complex: bool, dv: float):
+    """init_filter_states (filter_mpi/init.c:659-774): n_filters random starts,
+    each spin block drawn and normalised separately; returns ([n][nspin*ngrid], seeds)."""
+    out = np.empty((n_filters, nspin * ngrid), np.complex128)
+    seeds = []
+    for j in range(n_filters):
+        for s in range(nspin):
+            seeds.append(seed)
+            blk, seed = init_psi(seed, ngrid, is_complex, dv)
+            out[j, s * ngrid:(s + 1) * ngrid] = blk
+    return out, seeds, seed
+
+
+def samp_points(ncheby: int):
+    """samp_points_ashkenazy on [-2, 2] (filter_mpi/coeff.c:227-293)."""
+    re = np.empty(ncheby)
+    im = np.empty(ncheby)
+    fk = lib().orc_samp_points(ncheby, -2.0, 2.0, _p(re), _p(im))
+    return re, im, fk
+
+
+def newton_coeff(zn, targets, vmin, de, dt):
+    """gen_newton_coeff (filter_mpi/coeff.c:8-118); returns complex [m][ncheby]."""
+    zn = np.ascontiguousarray(zn, np.float64)
+    targets = np.ascontiguousarray(targets, np.float64)
+    m, nc = len(targets), len(zn)
+    an = np.empty(2 * m * nc)
+    lib().orc_newton_coeff(nc, m, _p(zn), _p(targets), vmin, de, dt, _p(an))
+    return an.view(np.complex128).reshape(m, nc)
+
+
+def filter_dt(ncheby: int, de: float) -> float:
+    """dt = (ncheby / (2.5 dE))^2 (filter_mpi/mod_filter.c:114)."""
+    return (ncheby / (2.5 * de)) ** 2
+
+
+def ene_targets(vbmin, vbmax, cbmin, cbmax, n_vb, n_cb):
+    """set_ene_targets (filter_mpi/init.c:401-478)."""
+    t = np.empty(n_vb + n_cb)
+    d = (vbmax - vbmin) / n_vb
+    for jx in range(n_vb):
+        t[n_vb - jx - 1] = vbmax - jx * d
+    d = (cbmax - cbmin) / n_cb
+    for jx in range(n_vb, n_vb + n_cb):
+        t[jx] = cbmin + (jx - n_vb) * d
+    return t
+
+
+# --------------------------------------------------------------------------
+# Grid and system description
+# --------------------------------------------------------------------------
+
+@dataclass
+class Grid:
+    nx: int
+    ny: int
+    nz: int
+    dx: float
+    dy: float
+    dz: float
+    xmin: float
+    ymin: float
+    zmin: float
+    ke_max: float = 20.0
+    box_n: bool = False  # True: box = n d on every axis (older reference versions)
+
+    @property
+    def ngrid(self):
+        return self.nx * self.ny * self.nz
+
+    @property
+    def dv(self):
+        return self.dx * self.dy * self.dz
+
+    def axes(self):
+        """build_grid_ksqr's coordinates (filter_mpi/init.c:284-290): cumulative sums."""
+        out = []
+        for n, d, lo in ((self.nx, self.dx, self.xmin), (self.ny, self.dy, self.ymin), (self.nz, self.dz, self.zmin)):
+            a = np.empty(n)
+            v = lo
+            for j in range(n):
+                a[j] = v
+                v += d
+            out.append(a)
+        return out
+
+    def dk(self):
+        """reciprocal spacing 2 pi / box (filter_mpi/init.c:65-80): box = n d (even), (n-1) d (odd)."""
+        res = []
+        for n, d in ((self.nx, self.dx), (self.ny, self.dy), (self.nz, self.dz)):
+            box = n * d if (n % 2 == 0 or self.box_n) else (n - 1) * d
+            res.append(2.0 * np.pi / box)
+        return res
+
+    def ksqr(self):
+        k = np.empty(self.ngrid)
+        dkx, dky, dkz = self.dk()
+        lib().orc_ksqr(self.nx, self.ny, self.nz, dkx, dky, dkz, self.ke_max, _p(k))
+        return k
+
+    def axis_ksqr(self):
+        ng_1 = (1.0 / self.nx) * (1.0 / self.ny) * (1.0 / self.nz)
+        out = []
+        for n, dk in zip((self.nx, self.ny, self.nz), self.dk()):
+            a = np.empty(n)
+            lib().orc_axis_ksqr(n, dk, ng_1, _p(a))
+            out.append(a)
+        return out
+
+
+def reference_grid(coords: np.ndarray, d: float, n_in=(0, 0, 0), ke_max=20.0) -> Grid:
+    """init_grid_params (filter_mpi/init.c:5-255, non-periodic): grow each axis to
+    cover the dot plus 5 bohr each side, forced even when grown."""
+    dims = []
+    for ax in range(3):
+        c = coords[:, ax]
+        ext = np.sqrt(np.max((c[:, None] - c[None, :]) ** 2)) if len(c) > 1 else 0.0
+        xd = np.rint(0.5 * ext + 5.0)
+        lo, hi = -xd, xd - d
+        ntmp = int((hi - lo) / d)
+        n = n_in[ax]
+        if ntmp > n:
+            n = ntmp + (ntmp % 2)
+        box = n * d if n % 2 == 0 else (n - 1) * d
+        dims.append((n, -box / 2.0))
+    return Grid(dims[0][0], dims[1][0], dims[2][0], d, d, d, dims[0][1], dims[1][1], dims[2][1], ke_max)
+
+
+@dataclass
+class Projectors:
+    """Structure-of-arrays copy of the reference's nlc table (fd.h:382-398)."""
+    nl: np.ndarray          # [nat] points per atom
+    npts: int               # row stride (max points)
+    jxyz: np.ndarray        # int32 [nat*npts]
+    y1: np.ndarray          # [nat*npts*6] (re, im) x 3
+    proj: np.ndarray        # [nat*npts*nproj] SO radial (scaled by sqrt(SO_par))
+    nlp: np.ndarray         # [nat*npts*nproj] NL radial
+    sgn: np.ndarray         # int32 [nat*nproj]
+    nproj: int = NPROJ
+
+    @property
+    def nat(self):
+        return len(self.nl)
+
+
+@dataclass
+class System:
+    grid: Grid
+    pot: np.ndarray               # [ngrid] local potential
+    nspin: int = 1
+    is_complex: bool = False
+    so: bool = False
+    nlflag: bool = False
+    proj: Projectors | None = None
+    LS: np.ndarray = field(default_factory=lambda: def_LS())
+
+    @property
+    def ngrid(self):
+        return self.grid.ngrid
+
+
+def def_LS():
+    """def_LS (filter_mpi/hamiltonian.c:312-442) as complex [6][6] indexed [j'][j]."""
+    ls = np.zeros(72)
+    lib().orc_def_LS(_p(ls))
+    return ls.view(np.complex128).reshape(6, 6)
+
+
+def local_pot(grid: Grid, coords, atype, tables):
+    """build_local_pot (filter_mpi/init.c:481-703) for short-ranged tables.
+    tables: list per type of (r, v) arrays."""
+    gx, gy, gz = grid.axes()
+    rr = np.ascontiguousarray(coords[:, 0]), np.ascontiguousarray(coords[:, 1]), np.ascontiguousarray(coords[:, 2])
+    tr = np.concatenate([np.asarray(t[0], np.float64) for t in tables])
+    tv = np.concatenate([np.asarray(t[1], np.float64) for t in tables])
+    tlen = np.array([len(t[0]) for t in tables], np.int64)
+    toff = np.concatenate([[0], np.cumsum(tlen)[:-1]]).astype(np.int64)
+    tdr = np.array([t[0][1] - t[0][0] for t in tables], np.float64)
+    at = np.ascontiguousarray(atype, np.int64)
+    pot = np.empty(grid.ngrid)
+    lib().orc_local_pot(grid.nx, grid.ny, grid.nz, _p(gx), _p(gy), _p(gz), len(at), _p(rr[0]), _p(rr[1]),
+                        _p(rr[2]), _p(at, _L), _p(tr), _p(tv), _p(toff, _L), _p(tlen, _L), _p(tdr), _p(pot))
+    return pot
+
+
+def so_radial(dx: float, rcut: float, nproj: int = NPROJ):
+    """gen_SO_projectors (filter_mpi/projectors.c:12-84): the nproj leading
+    eigenvectors of the k-space integral matrix mapped back to r.  [nproj][N]."""
+    N = PROJ_LEN
+    A = np.empty(N * N)
+    lib().orc_proj_matrix(N, dx, rcut, 0, 0.0, 0.0, _p(A))
+    w, v = np.linalg.eigh(A.reshape(N, N))
+    out = np.empty((nproj, N))
+    for p in range(nproj):
+        vec = np.ascontiguousarray(v[:, N - p - 1])
+        lib().orc_proj_radial(N, dx, rcut, _p(vec), float(w[N - p - 1]), _p(out[p]))
+    return out
+
+
+def nl_radial(dx: float, rcut: float, lam1: float, lam2: float, nproj: int = NPROJ):
+    """gen_nlc_projectors (filter_mpi/projectors.c:87-228): the nproj eigenvectors
+    of largest |eigenvalue|, signs = sign of the eigenvalue.  ([nproj][N], sgn)."""
+    N = PROJ_LEN
+    if lam1 == 0 and lam2 == 0:
+        return np.zeros((nproj, N)), np.zeros(nproj, np.int32)
+    A = np.empty(N * N)
+    lib().orc_proj_matrix(N, dx, rcut, 1, lam1, lam2, _p(A))
+    w, v = np.linalg.eigh(A.reshape(N, N))
+    # insertion selection of the nproj largest |w| (projectors.c:166-186)
+    eigs = [0.0] * nproj
+    idx = [0] * nproj
+    for i in range(N):
+        if abs(w[i]) > eigs[nproj - 1]:
+            for j in range(nproj - 1, -1, -1):
+                if j == 0 or eigs[j - 1] > abs(w[i]):
+                    eigs[j] = abs(w[i])
+                    idx[j] = i
+                    break
+                eigs[j] = eigs[j - 1]
+                idx[j] = idx[j - 1]
+    out = np.empty((nproj, N))
+    sgn = np.empty(nproj, np.int32)
+    for p in range(nproj):
+        sgn[p] = -1 if w[idx[p]] < 0 else 1
+        vec = np.ascontiguousarray(v[:, idx[p]])
+        lib().orc_proj_radial(N, dx, rcut, _p(vec), float(abs(w[idx[p]])), _p(out[p]))
+    return out, sgn
+
+
+def r_nlcut2(dx: float) -> float:
+    """R_NLcut2 = 1.5 + 6 ln 10 + 3 dx (filter_mpi/read.c:908)."""
+    return 1.5 + 6.0 * np.log(10.0) + 3.0 * dx
+
+
+def nlc_table(grid: Grid, coords, so_par, so_tab, nl_tabs, nl_sgn, nproj=NPROJ) -> Projectors:
+    """init_NL_projectors (filter_mpi/init.c:848-1135 region, body 508-589) over the
+    projector atoms (coords rows), using the reference's EPSDX-shifted Y_1m."""
+    rc2 = r_nlcut2(grid.dx)
+    gx, gy, gz = grid.axes()
+    nat = len(coords)
+    # count the maximum points per atom (build_grid_ksqr, init.c:353-393)
+    npts = 0
+    for a in range(nat):
+        d2 = (gx[None, None, :] - coords[a, 0]) ** 2 + (gy[None, :, None] - coords[a, 1]) ** 2 + \
+             (gz[:, None, None] - coords[a, 2]) ** 2
+        npts = max(npts, int(np.count_nonzero(d2 < rc2)))
+    npts = max(npts, 1)
+    N = PROJ_LEN
+    so_tab = np.ascontiguousarray(so_tab, np.float64).reshape(nproj, N)
+    nl_tabs = np.ascontiguousarray(nl_tabs, np.float64).reshape(nat, nproj, N)
+    nl = np.zeros(nat, np.int64)
+    jxyz = np.zeros(nat * npts, np.int32)
+    y1 = np.zeros(nat * npts * 6)
+    proj = np.zeros(nat * npts * nproj)
+    nlp = np.zeros(nat * npts * nproj)
+    cx, cy, cz = (np.ascontiguousarray(coords[:, i]) for i in range(3))
+    sp = np.ascontiguousarray(so_par, np.float64)
+    lib().orc_nlc_table(grid.nx, grid.ny, grid.nz, _p(gx), _p(gy), _p(gz), nat, _p(cx), _p(cy), _p(cz), _p(sp),
+                        rc2, npts, nproj, N, _p(so_tab), _p(nl_tabs), _p(nl, _L), _p(jxyz, _I), _p(y1), _p(proj),
+                        _p(nlp))
+    return Projectors(nl, npts, jxyz, y1, proj, nlp, np.ascontiguousarray(nl_sgn, np.int32).reshape(-1), nproj)
+
+
+# --------------------------------------------------------------------------
+# H psi
+# --------------------------------------------------------------------------
+
+def kinetic(psi: np.ndarray, sysm: System) -> np.ndarray:
+    """kinetic (filter_mpi/hamiltonian.c:62-99) per spin block: FFTW forward,
+    times ksqr (which already holds 1/N), FFTW backward (unnormalised)."""
+    g = sysm.grid
+    k = g.ksqr().reshape(g.nz, g.ny, g.nx)
+    out = np.empty_like(psi)
+    n = g.ngrid
+    for s in range(sysm.nspin):
+        blk = psi[s * n:(s + 1) * n].reshape(g.nz, g.ny, g.nx)
+        f = np.fft.fftn(blk) * k
+        out[s * n:(s + 1) * n] = (np.fft.ifftn(f) * n).reshape(-1)
+    return out
+
+
+def potential_add(out: np.ndarray, psi: np.ndarray, sysm: System):
+    """p_potential (filter_mpi/phamiltonian.c:65-137): SO, then NL, then V_loc."""
+    L = lib()
+    o = out.view(np.float64)
+    p = np.ascontiguousarray(psi).view(np.float64)
+    n = sysm.ngrid
+    pr = sysm.proj
+    if sysm.so:
+        ls = np.ascontiguousarray(sysm.LS).view(np.float64)
+        L.orc_apply_so(_p(o), _p(p), n, pr.nat, _p(pr.nl, _L), pr.npts, pr.nproj, _p(pr.jxyz, _I), _p(pr.y1),
+                       _p(pr.proj), _p(ls), sysm.grid.dv)
+    if sysm.nlflag:
+        L.orc_apply_nl(_p(o), _p(p), n, sysm.nspin, pr.nat, _p(pr.nl, _L), pr.npts, pr.nproj, _p(pr.jxyz, _I),
+                       _p(pr.y1), _p(pr.nlp), _p(pr.sgn, _I), sysm.grid.dv)
+    pot = np.ascontiguousarray(sysm.pot, np.float64)
+    L.orc_apply_vloc(_p(o), _p(p), _p(pot), n, sysm.nspin, int(sysm.is_complex))
+
+
+def hamiltonian(psi: np.ndarray, sysm: System) -> np.ndarray:
+    """p_hamiltonian (filter_mpi/phamiltonian.c:10-60): H psi for one state
+    (complex [nspin*ngrid]).  For real states the imaginary channel is left to
+    the kinetic term only, exactly as the reference's real path does."""
+    psi = np.ascontiguousarray(psi, np.complex128)
+    out = kinetic(psi, sysm)
+    potential_add(out, psi, sysm)
+    return out
+
+
+def hnorm(psi: np.ndarray, sysm: System, de_1: float, vmin: float, zn: float) -> np.ndarray:
+    """p_hnorm (filter_mpi/filter.c:375-410)."""
+    h = hamiltonian(psi, sysm)
+    hv = h.view(np.float64)
+    lib().orc_hnorm_shift(_p(hv), _p(np.ascontiguousarray(psi).view(np.float64)), len(psi), de_1, vmin, zn)
+    return h
+
+
+def filter_cycle(psi0: np.ndarray, sysm: System, an: np.ndarray, zn: np.ndarray, vmin: float, de: float):
+    """filter_cycle (filter_mpi/filter.c:187-371): returns [m][nspin*ngrid] filtered
+    states F_t = sum_j a_{t,j} prod_{i<j}(H_s - z_i) psi0 (complex storage; for
+    real systems only the real part is meaningful, as in psi_rank)."""
+    de_1 = 4.0 / de
+    m, nc = an.shape
+    psi = np.array(psi0, np.complex128)
+    if not sysm.is_complex:
+        psi = psi.real.astype(np.complex128)
+    acc = an[:, 0:1] * psi[None, :]
+    for jc in range(1, nc):
+        psi = hnorm(psi, sysm, de_1, vmin, zn[jc - 1])
+        acc += an[:, jc:jc + 1] * psi[None, :]
+    if not sysm.is_complex:
+        acc = acc.real.astype(np.complex128)
+    return acc
+
+
+def energy(psi: np.ndarray, sysm: System) -> float:
+    """energy (filter_mpi/energy.c:6-57): dv sum Re(conj(psi) H psi)."""
+    h = hamiltonian(psi, sysm)
+    return float(np.sum(psi.real * h.real + psi.imag * h.imag) * sysm.grid.dv)
+
+
+def normalize(psi: np.ndarray, dv: float) -> np.ndarray:
+    """normalize (filter_mpi/norm.c:42-79)."""
+    return psi / np.sqrt(np.sum(np.abs(psi) ** 2) * dv)
+
+
+def energy_range(sysm: System, max_iter: int = 1500, seed: int = -874917403):
+    """get_energy_range (filter_mpi/energy.c:169-379) with approxEnergyRange = 0:
+    imaginary-time descent for E_min (tau = 0.05, halved-step on rises) and power
+    iteration for E_max, then the blanket inflation (x1.2 / -0.2|E_min|) used
+    when SO is on or no projectors are active.  Returns (Vmin, dE, Emin, Emax)."""
+    n = sysm.ngrid
+    dv = sysm.grid.dv
+    phi = np.empty(sysm.nspin * n, np.complex128)
+    for s in range(sysm.nspin):
+        blk, seed = init_psi(seed, n, sysm.is_complex, dv)
+        phi[s * n:(s + 1) * n] = blk
+    tau = 0.05
+    emin, old = 10.0, 0.0
+    i = 0
+    while abs((emin - old) / emin) > 1e-6 and i < max_iter:
+        psi = phi.copy()
+        h = hamiltonian(psi, sysm)
+        phi = normalize(psi - tau * h, dv)
+        old = emin
+        emin = energy(phi, sysm)
+        if i > 5 and (emin - old) > 0:
+            tau -= 0.025
+        i += 1
+    psi = np.empty(sysm.nspin * n, np.complex128)
+    for s in range(sysm.nspin):
+        blk, seed = init_psi(seed, n, sysm.is_complex, dv)
+        psi[s * n:(s + 1) * n] = blk
+    emax, old = 0.1, 0.0
+    i = 0
+    while abs((emax - old) / emax) > 1e-6 and i < max_iter:
+        psi = normalize(hamiltonian(psi, sysm), dv)
+        old = emax
+        emax = energy(psi, sysm)
+        i += 1
+    return inflate_range(sysm, emin, emax)
+
+
+def inflate_range(sysm: System, emin: float, emax: float, nl_lambda_min: float = 0.0):
+    """Range inflation of get_energy_range (filter_mpi/energy.c:338-369).
+    NL-only jobs with a negative NL bound get the trimmed rule."""
+    if sysm.nlflag and not sysm.so and nl_lambda_min < 0.0:
+        emax_i = emax * 1.05
+        emin_i = emin - 0.1 * abs(emin)
+        weyl = 1.05 * (float(np.min(sysm.pot)) + nl_lambda_min)
+        if emin_i > weyl:
+            emin_i = weyl
+    else:
+        emax_i = emax * 1.2
+        emin_i = emin - 0.2 * abs(emin)
+    return emin_i, emax_i - emin_i, emin, emax
+
+
+# --------------------------------------------------------------------------
+# Orthogonalisation, subspace diagonalisation, sigma_E
+# --------------------------------------------------------------------------
+
+def ortho(psis: np.ndarray, is_complex: bool, eps: float = 1e-10):
+    """ortho_real/ortho_cplx (filter_mpi/ortho.c:5-187) + normalize_all:
+    thin SVD of the (points x states) matrix, keep left vectors with
+    s_i/s_0 >= 1e-10.  psis: [n][npts]."""
+    A = psis.T if is_complex else psis.real.T
+    u, s, _ = np.linalg.svd(A, full_matrices=False)
+    keep = int(np.sum(s / s[0] >= eps))
+    return u[:, :keep].T.copy(), s
+
+
+def diag(psis: np.ndarray, sysm: System):
+    """diag_H (filter_mpi/Hmat.c:5-297): H_ij = dv <psi_i|H|psi_j>, eigh, rotate,
+    then normalize_all (mod_diag.c).  Returns (evals, vectors [n][npts])."""
+    dv = sysm.grid.dv
+    H = np.array([hamiltonian(p if sysm.is_complex else p.real.astype(np.complex128), sysm) for p in psis])
+    if not sysm.is_complex:
+        M = (psis.real @ H.real.T) * dv
+        M = 0.5 * (M + M.T)
+    else:
+        M = (psis.conj() @ H.T) * dv
+        M = 0.5 * (M + M.conj().T)
+    e, c = np.linalg.eigh(M)
+    vec = c.T @ psis
+    vec = np.array([normalize(v, dv) for v in vec])
+    return e, vec
+
+
+def sigma_e(psis: np.ndarray, sysm: System):
+    """calc_sigma_E (filter_mpi/energy.c:383-539): sigma = sqrt|<H^2> - <H>^2|,
+    computed here as the equal residual norm ||(H - E) psi|| for normalised psi
+    (the reference's two-application form loses digits to cancellation)."""
+    dv = sysm.grid.dv
+    ev, sg = [], []
+    for p in psis:
+        p = p if sysm.is_complex else p.real.astype(np.complex128)
+        h = hamiltonian(p, sysm)
+        e = float(np.sum(p.real * h.real + p.imag * h.imag) * dv)
+        r = h - e * p
+        if not sysm.is_complex:
+            r = r.real
+        ev.append(e)
+        sg.append(float(np.sqrt(np.sum(np.abs(r) ** 2) * dv)))
+    return np.array(ev), np.array(sg)

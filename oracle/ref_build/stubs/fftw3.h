@@ -1,0 +1,19 @@
+/* Type-only stand-in for <fftw3.h>, used only to compile the reference's
+ * pure-C hot-path files into the test-only oracle/_ref library.  The
+ * reference's FFT calls (fftw_execute etc.) are declared here but resolved
+ * by aborting stubs in ref_harness.c: no transform is ever run through them. */
+#pragma once
+typedef double fftw_complex[2];
+typedef struct fbse_ref_fftw_plan_s *fftw_plan;
+#define FFTW_FORWARD (-1)
+#define FFTW_BACKWARD (+1)
+#define FFTW_MEASURE (0U)
+#define FFTW_ESTIMATE (1U << 6)
+void fftw_execute(const fftw_plan p);
+fftw_plan fftw_plan_dft_3d(int n0, int n1, int n2, fftw_complex *in, fftw_complex *out, int sign, unsigned flags);
+void fftw_destroy_plan(fftw_plan p);
+void *fftw_malloc(unsigned long n);
+void fftw_free(void *p);
+int fftw_init_threads(void);
+void fftw_plan_with_nthreads(int n);
+void fftw_cleanup_threads(void);

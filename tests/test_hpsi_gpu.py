@@ -1,0 +1,121 @@
+"""H psi on the GPU against the FP64 oracle (kinetic FFT, local potential,
+spin-orbit and nonlocal projectors, p_hnorm), in FP64 and in the mixed (FP32)
+working precision, on grids whose axis lengths exercise every FFT radix path
+(2, 3, 4, odd primes 5, 7, 11, 13, 19 and a prime axis)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.systems import random_states, tiny_cluster
+
+pytestmark = pytest.mark.gpu
+
+TOL = {0: 1e-12, 1: 3e-6}  # relative max-norm error: FP64 path, mixed (FP32) path
+
+
+def _ctx(F, sysm, precision):
+    return F.Context(sysm.grid, sysm.pot, nspin=sysm.nspin, is_complex=sysm.is_complex, so=sysm.so, nl=sysm.nlflag,
+                     proj=sysm.proj, precision=precision)
+
+
+def _run_hpsi(F, ctx, psis, dev):
+    import torch
+    dt = ctx.working_dtype()
+    x = torch.tensor(psis, dtype=dt, device=dev).contiguous()
+    y = torch.empty_like(x)
+    ctx.hpsi(x, y)
+    return y.cpu().numpy().astype(np.complex128)
+
+
+def _relerr(a, b, real_only=False):
+    if real_only:
+        a, b = a.real, b.real
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 16), (24, 21, 22), (20, 26, 15), (19, 14, 33), (57, 52, 45), (13, 28, 17)])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kinetic_and_local(fbse, cuda, shape, precision):
+    nx, ny, nz = shape
+    sysm = tiny_cluster(nx, ny, nz, natoms=6, is_complex=True)
+    rng = np.random.default_rng(1)
+    psis = random_states(3, sysm, rng)
+    ctx = _ctx(fbse, sysm, precision)
+    got = _run_hpsi(fbse, ctx, psis, cuda)
+    want = np.array([O.hamiltonian(p, sysm) for p in psis])
+    assert _relerr(got, want) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kinetic_plane_wave(fbse, cuda, precision):
+    """A plane wave is an eigenvector of the kinetic operator with 0.5 k^2 (capped)."""
+    sysm = tiny_cluster(18, 20, 15, natoms=1, is_complex=True)
+    sysm.pot[:] = 0.0
+    g = sysm.grid
+    dkx, dky, dkz = g.dk()
+    x = np.arange(g.nx)[None, None, :]
+    y = np.arange(g.ny)[None, :, None]
+    z = np.arange(g.nz)[:, None, None]
+    kx, ky, kz = 3, -2, 5
+    pw = np.exp(2j * np.pi * (kx * x / g.nx + ky * y / g.ny + kz * z / g.nz)).reshape(1, -1)
+    ctx = _ctx(fbse, sysm, precision)
+    got = _run_hpsi(fbse, ctx, pw, cuda)
+    e = 0.5 * ((kx * dkx) ** 2 + (ky * dky) ** 2 + (kz * dkz) ** 2)
+    e = min(e, g.ke_max)
+    assert _relerr(got, e * pw) < TOL[precision] * 10
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_real_packing(fbse, cuda, precision):
+    """Real jobs: two real states packed as re/im give each real H psi."""
+    sysm = tiny_cluster(22, 18, 20, natoms=8, is_complex=False, nl=True)
+    rng = np.random.default_rng(2)
+    a = rng.uniform(-1, 1, (2, sysm.ngrid))
+    packed = (a[0] + 1j * a[1]).reshape(1, -1)
+    ctx = _ctx(fbse, sysm, precision)
+    got = _run_hpsi(fbse, ctx, packed, cuda)[0]
+    w0 = O.hamiltonian(a[0].astype(np.complex128), sysm).real
+    w1 = O.hamiltonian(a[1].astype(np.complex128), sysm).real
+    scale = max(np.abs(w0).max(), np.abs(w1).max())
+    assert np.max(np.abs(got.real - w0)) / scale < TOL[precision]
+    assert np.max(np.abs(got.imag - w1)) / scale < TOL[precision]
+
+
+@pytest.mark.parametrize("so,nl", [(True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_projectors_spinor(fbse, cuda, so, nl, precision):
+    sysm = tiny_cluster(24, 22, 20, natoms=10, nspin=2, is_complex=True, so=so, nl=nl)
+    rng = np.random.default_rng(3)
+    psis = random_states(2, sysm, rng)
+    ctx = _ctx(fbse, sysm, precision)
+    got = _run_hpsi(fbse, ctx, psis, cuda)
+    want = np.array([O.hamiltonian(p, sysm) for p in psis])
+    assert _relerr(got, want) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_hnorm(fbse, cuda, precision):
+    import torch
+    sysm = tiny_cluster(20, 20, 21, natoms=8, nspin=2, is_complex=True, so=True, nl=True)
+    rng = np.random.default_rng(4)
+    psis = random_states(2, sysm, rng)
+    vmin, de, zn = -1.3, 27.0, 0.37
+    ctx = _ctx(fbse, sysm, precision)
+    x = torch.tensor(psis, dtype=ctx.working_dtype(), device=cuda)
+    y = torch.empty_like(x)
+    ctx.hnorm(x, y, vmin, de, zn)
+    got = y.cpu().numpy()
+    want = np.array([O.hnorm(p, sysm, 4.0 / de, vmin, zn) for p in psis])
+    assert _relerr(got, want) < TOL[precision]
+
+
+def test_batch_independence(fbse, cuda):
+    """A state's H psi does not depend on the other states of its batch."""
+    import torch
+    sysm = tiny_cluster(16, 18, 20, natoms=8, nspin=2, is_complex=True, so=True, nl=True)
+    rng = np.random.default_rng(5)
+    psis = random_states(5, sysm, rng)
+    ctx = _ctx(fbse, sysm, 0)
+    full = _run_hpsi(fbse, ctx, psis, cuda)
+    one = _run_hpsi(fbse, ctx, psis[2:3], cuda)
+    assert np.max(np.abs(full[2] - one[0])) <= 1e-13 * np.max(np.abs(one[0]))

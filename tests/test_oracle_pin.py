@@ -1,0 +1,179 @@
+"""Pins the oracle: the C/numpy restatement against the reference's own
+compiled functions (oracle/_ref, built from the reference tree when it is
+present) and against the golden vectors of the reference's example runs
+(tests/golden/, always present)."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.systems import GOLD, cdse_tables, read_conf
+
+REF_SO = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "libfbse_ref.so")
+D = ctypes.POINTER(ctypes.c_double)
+
+
+def _p(a, t=D):
+    return a.ctypes.data_as(t)
+
+
+@pytest.fixture(scope="module")
+def ref():
+    if not os.path.exists(REF_SO):
+        pytest.skip("oracle/_ref not built (the reference tree is not mounted here)")
+    L = ctypes.CDLL(REF_SO)
+    L.ref_ran.restype = ctypes.c_double
+    L.ref_ran.argtypes = [ctypes.POINTER(ctypes.c_long)]
+    L.ref_samp_points.restype = ctypes.c_double
+    L.ref_samp_points.argtypes = [ctypes.c_long, D, D]
+    L.ref_newton_coeff.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                   D, D, D]
+    L.ref_def_LS.argtypes = [D]
+    L.ref_p_potential.argtypes = [D, D, D, D, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.POINTER(ctypes.c_long),
+                                  ctypes.POINTER(ctypes.c_int), D, D, D, ctypes.POINTER(ctypes.c_int), ctypes.c_double]
+    L.ref_normalize_all.argtypes = [D, ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+    return L
+
+
+# ---------------------------------------------------------------- golden vectors
+
+def test_rng_seed_sequence_golden():
+    """seed.dat of a reference run: each random start draws 57*52*45 values."""
+    rows = [l.split() for l in open(os.path.join(GOLD, "seed_2.2nm_CdSe.txt")).read().splitlines()[1:] if l.strip()]
+    seeds = [int(r[1]) for r in rows]
+    s = seeds[0]
+    for want in seeds[1:]:
+        _, s = O.ran_fill(s, 57 * 52 * 45, out=False)
+        assert s == want
+
+
+def test_leja_nodes_golden():
+    ref = np.loadtxt(os.path.join(GOLD, "zn_2048.txt"))
+    zn, _, _ = O.samp_points(2048)
+    # the file holds "%lg" (6 significant digits)
+    assert np.allclose(zn, ref[:, 1], rtol=6e-6, atol=1e-6)
+
+
+def test_ksqr_golden():
+    rows = np.loadtxt(os.path.join(GOLD, "ksqr_57x52x45.txt"), comments="#")
+    # grid of that run: 57 x 52 x 45 at dx = 0.8, KEmax = 10; the version that
+    # wrote it used box = n d on odd axes too (the current init.c uses (n-1) d)
+    g = O.Grid(57, 52, 45, 0.8, 0.8, 0.8, -22.8, -20.8, -18.0, 10.0, box_n=True)
+    k = g.ksqr()
+    idx = rows[:, 0].astype(int)
+    assert np.allclose(k[idx], rows[:, 1], rtol=6e-6, atol=1e-12)
+
+
+def test_local_potential_golden():
+    """build_local_pot on the 2.2 nm CdSe example vs the reference's localPot.cube."""
+    lines = open(os.path.join(GOLD, "cdse22", "localPot_sample.txt")).read().splitlines()
+    hdr = [l[1:].split() for l in lines if l.startswith("#")][2:6]
+    xmin, ymin, zmin = float(hdr[0][1]), float(hdr[0][2]), float(hdr[0][3])
+    nx, ny, nz = int(hdr[1][0]), int(hdr[2][0]), int(hdr[3][0])
+    d = float(hdr[1][1])
+    vals = np.array([l.split() for l in lines if not l.startswith("#")], float)
+    atyp, xyz = read_conf(os.path.join(GOLD, "cdse22", "conf.par"))
+    types = sorted(set(atyp), key=atyp.index)
+    g = O.Grid(nx, ny, nz, d, d, d, xmin, ymin, zmin, 10.0)
+    pot = O.local_pot(g, xyz, np.array([types.index(a) for a in atyp]), cdse_tables(types))
+    ci = vals[:, 0].astype(int)  # cube order: x outer, y, z inner
+    ix, rem = np.divmod(ci, ny * nz)
+    iy, iz = np.divmod(rem, nz)
+    got = pot[nx * (ny * iz + iy) + ix]
+    # "%.5g" in the cube file
+    assert np.allclose(got, vals[:, 1], rtol=1e-4, atol=6e-5)
+
+
+def test_def_LS_eigenvalues():
+    """L.S in the p shell has eigenvalues +1/2 (j = 3/2, x4) and -1 (j = 1/2, x2)."""
+    ls = O.def_LS()
+    ev = np.sort(np.linalg.eigvalsh(ls.T))
+    assert np.allclose(ev, [-1, -1, 0.5, 0.5, 0.5, 0.5], atol=1e-14)
+
+
+def test_eval_golden_files_parse():
+    for sub in ("cdse22", "cspbi3"):
+        ev = np.loadtxt(os.path.join(GOLD, sub, "eval.dat"))
+        assert ev.shape[1] == 3 and np.all(np.diff(ev[:, 1]) >= -1e-12)
+
+
+# ---------------------------------------------------------------- reference functions
+
+def test_rng_matches_reference(ref):
+    s_ref = ctypes.c_long(-987654)
+    s = -987654
+    for _ in range(3):
+        vals, s = O.ran_fill(s, 1000)
+        got = np.array([ref.ref_ran(ctypes.byref(s_ref)) for _ in range(1000)])
+        assert np.array_equal(vals, got)
+        assert s == s_ref.value
+        s = -s - 17  # re-initialise both
+        s_ref.value = s
+
+
+def test_samp_points_match_reference(ref):
+    for nc in (64, 257):
+        re = np.empty(nc)
+        im = np.empty(nc)
+        fk = ref.ref_samp_points(nc, _p(re), _p(im))
+        a, b, fk2 = O.samp_points(nc)
+        assert np.array_equal(a, re) and np.array_equal(b, im) and fk == fk2
+
+
+def test_newton_coeff_match_reference(ref, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)  # the reference writes zn.dat / coeff-*.dat / func.dat
+    nc, m = 200, 4
+    zn, _, _ = O.samp_points(nc)
+    targets = np.array([-0.31, -0.25, -0.14, -0.07])
+    vmin, de = -1.35, 14.2
+    dt = O.filter_dt(nc, de)
+    an_ref = np.empty(2 * m * nc)
+    ref.ref_newton_coeff(nc, m, vmin, de, dt, _p(zn), _p(targets), _p(an_ref))
+    an = O.newton_coeff(zn, targets, vmin, de, dt)
+    assert np.array_equal(an.view(np.float64).reshape(-1), an_ref)
+
+
+def test_def_LS_matches_reference(ref):
+    ls = np.empty(72)
+    ref.ref_def_LS(_p(ls))
+    assert np.array_equal(O.def_LS().reshape(-1).view(np.float64), ls)
+
+
+@pytest.mark.parametrize("so,nl,cplx", [(1, 1, 1), (1, 0, 1), (0, 1, 1), (0, 1, 0), (0, 0, 0)])
+def test_potential_matches_reference(ref, so, nl, cplx):
+    from tests.systems import tiny_cluster
+    nspin = 2 if so else 1
+    sysm = tiny_cluster(14, 15, 13, natoms=8, nspin=nspin, is_complex=bool(cplx), so=bool(so), nl=bool(nl))
+    rng = np.random.default_rng(11)
+    L = nspin * sysm.ngrid
+    psi = rng.uniform(-1, 1, L) + 1j * (rng.uniform(-1, 1, L) if cplx else 0)
+    base = rng.uniform(-1, 1, L) + 1j * rng.uniform(-1, 1, L)
+    mine = base.copy()
+    O.potential_add(mine, psi, sysm)
+    theirs = base.copy()
+    pr = sysm.proj
+    pot2 = np.concatenate([sysm.pot, sysm.pot])  # the reference stores V twice
+    ls = np.ascontiguousarray(sysm.LS).view(np.float64)
+    if pr is None:
+        pr = O.Projectors(np.zeros(1, np.int64), 1, np.zeros(1, np.int32), np.zeros(6), np.zeros(5), np.zeros(5),
+                          np.zeros(5, np.int32))
+    ref.ref_p_potential(_p(theirs.view(np.float64)), _p(psi.view(np.float64)), _p(pot2), _p(ls), sysm.ngrid, nspin,
+                        cplx, so, nl, pr.nat if (so or nl) else 0, pr.npts, pr.nproj,
+                        pr.nl.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                        pr.jxyz.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _p(pr.y1), _p(pr.proj), _p(pr.nlp),
+                        pr.sgn.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), sysm.grid.dv)
+    assert np.array_equal(mine, theirs)
+
+
+def test_normalize_all_matches_reference(ref):
+    rng = np.random.default_rng(3)
+    ngrid, n = 1000, 4
+    for cplx in (0, 1):
+        a = rng.uniform(-1, 1, (n, ngrid * (1 + cplx)))
+        b = a.copy()
+        ref.ref_normalize_all(_p(b), n, ngrid, 1, cplx, 0.37)
+        want = a / np.sqrt(np.sum(a ** 2, axis=1) * 0.37)[:, None]
+        assert np.allclose(b, want, rtol=1e-14, atol=0)
