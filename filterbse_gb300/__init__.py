@@ -27,7 +27,7 @@ EXPORTED = [
     "fbse_upload", "fbse_download", "fbse_sync", "fbse_stream", "fbse_hpsi", "fbse_hnorm",
     "fbse_newton_filter", "fbse_energy_range", "fbse_normalize_all", "fbse_energy_all",
     "fbse_ortho_diag_sigma", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
-    "fbse_init_filter_states",
+    "fbse_init_filter_states", "fbse_launch_count", "fbse_filter_job", "fbse_build_local_pot",
 ]
 
 
@@ -92,8 +92,16 @@ def load() -> ctypes.CDLL:
     L.fbse_init_filter_states.argtypes = [_D, ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_long, ctypes.POINTER(ctypes.c_long)]
     L.fbse_init_filter_states.restype = ctypes.c_long
+    L.fbse_launch_count.restype = ctypes.c_long
+    L.fbse_filter_job.argtypes = [_VP, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_double, ctypes.c_double, _D,
+                                  ctypes.c_long, ctypes.c_double, ctypes.POINTER(ctypes.c_long), _D, _D, _D]
     _lib = L
     return L
+
+
+def launch_count() -> int:
+    """Kernels launched by libfbse_gpu so far (all contexts)."""
+    return int(load().fbse_launch_count())
 
 
 def _dp(a: np.ndarray):
@@ -268,6 +276,27 @@ class Context:
         self._torch_sync()
         self._chk(self._L.fbse_energy_all(self._h, self._ptr(psitot), n, _dp(e)))
         return e
+
+    def filter_job(self, zn, an, vmin, de, psi0_host, sigma_cut=0.0, psi_out=None):
+        """Whole filter stage on host buffers (fbse_filter_job): returns
+        (n, eval, sigma); psi_out (host float64 [nstart*m, stlen], optional,
+        ideally pinned) receives the returned states."""
+        zn = np.ascontiguousarray(zn, np.float64)
+        an = np.ascontiguousarray(an, np.complex128)
+        m, nc = an.shape
+        p0 = np.ascontiguousarray(psi0_host, np.float64)
+        nstart = p0.shape[0]
+        ev = np.empty(nstart * m)
+        sg = np.empty(nstart * m)
+        nout = ctypes.c_long()
+        pp = None
+        if psi_out is not None:
+            pp = ctypes.cast(ctypes.c_void_p(psi_out.data_ptr() if hasattr(psi_out, "data_ptr")
+                                             else psi_out.ctypes.data), _D)
+        self._chk(self._L.fbse_filter_job(self._h, _dp(zn), _dp(an.view(np.float64).reshape(-1)), nc, m, vmin, de,
+                                          _dp(p0), nstart, sigma_cut, ctypes.byref(nout), _dp(ev), _dp(sg), pp))
+        k = nout.value
+        return k, ev[:k].copy(), sg[:k].copy()
 
     def ortho_diag_sigma(self, psitot):
         n = psitot.shape[0]

@@ -6,6 +6,8 @@
 
 namespace fbse {
 
+std::atomic<long> g_launches{0};
+
 int set_err(fbse_ctx *c, int code, const std::string &msg)
 {
   if (c) c->err = msg;
@@ -182,6 +184,8 @@ using namespace fbse;
 extern "C" {
 
 int fbse_version(void) { return 1; }
+
+long fbse_launch_count(void) { return g_launches.load(); }
 
 const char *fbse_last_error(const fbse_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 

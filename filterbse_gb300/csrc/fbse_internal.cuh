@@ -15,6 +15,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -107,7 +109,14 @@ int set_err(fbse_ctx *c, int code, const std::string &msg);
     if (e__ != cudaSuccess)                                                                   \
       return ::fbse::set_err((ctx), FBSE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
   } while (0)
-#define FBSE_CHECK_LAUNCH(ctx) FBSE_CUDA(ctx, cudaGetLastError())
+// every kernel launch of the library is counted (fbse_launch_count)
+extern std::atomic<long> g_launches;
+#define FBSE_COUNT(k) (::fbse::g_launches += (k))
+#define FBSE_CHECK_LAUNCH(ctx)              \
+  do {                                      \
+    FBSE_COUNT(1);                          \
+    FBSE_CUDA(ctx, cudaGetLastError());     \
+  } while (0)
 
 int ensure(fbse_ctx *c, void **p, size_t *have, size_t need);
 

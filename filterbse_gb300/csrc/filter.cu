@@ -85,6 +85,17 @@ int unpack(fbse_ctx *c, const C<T> *src, double *dst, long ndst)
   return FBSE_OK;
 }
 
+int pack_states(fbse_ctx *c, const double *src, void *dst, long nsrc)
+{
+  return c->precision == FBSE_MIXED ? pack<float>(c, src, (float2 *)dst, nsrc) : pack<double>(c, src, (double2 *)dst, nsrc);
+}
+
+int unpack_states(fbse_ctx *c, const void *src, double *dst, long ndst)
+{
+  return c->precision == FBSE_MIXED ? unpack<float>(c, (const float2 *)src, dst, ndst)
+                                    : unpack<double>(c, (const double2 *)src, dst, ndst);
+}
+
 // ---------------------------------------------------------------------------
 // K-blocked Newton accumulation into the psi_rank layout
 // F[start][t] (+)= sum_q a[t][j0+q] * ring[(j0+q) % K][w]
@@ -95,29 +106,31 @@ __global__ void __launch_bounds__(256) k_newton_acc(const C<T> *__restrict__ rin
                                                    double *__restrict__ F, long nstart, long nw, long len, int cplx,
                                                    int init)
 {
-  __shared__ double as[kMaxTargets * 64];
+  // The in-block sums run in the working precision T (FP32 on the mixed path:
+  // the FP64 pipe of this part is a small fraction of its FP32 rate), and
+  // each block's sum is added to the FP64 accumulator.
+  __shared__ T as[kMaxTargets * 64];
   for (int i = threadIdx.x; i < m * nk; i += blockDim.x) {
     const int t = i / nk, q = i % nk;
-    as[t * nk + q] = a[t * ncheby + j0 + q];
+    as[t * nk + q] = (T)a[t * ncheby + j0 + q];
   }
   __syncthreads();
   const long slot_stride = nw * len;
   const long total = nw * len;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     const long w = i / len, k = i - w * len;
-    double ar[kMaxTargets], ai[kMaxTargets];
+    T ar[kMaxTargets], ai[kMaxTargets];
 #pragma unroll
-    for (int t = 0; t < kMaxTargets; t++) { ar[t] = 0.0; ai[t] = 0.0; }
+    for (int t = 0; t < kMaxTargets; t++) { ar[t] = T(0); ai[t] = T(0); }
     for (int q = 0; q < nk; q++) {
       const long slot = (j0 + q) % K;
       const C<T> v = ring[slot * slot_stride + i];
-      const double vr = (double)v.x, vi = (double)v.y;
 #pragma unroll
       for (int t = 0; t < kMaxTargets; t++) {
         if (t < m) {
-          const double co = as[t * nk + q];
-          ar[t] += co * vr;
-          ai[t] += co * vi;
+          const T co = as[t * nk + q];
+          ar[t] += co * v.x;
+          ai[t] += co * v.y;
         }
       }
     }
@@ -185,7 +198,7 @@ static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long
       if ((jc % K) == K - 1 || jc == ncheby - 1) {
         const long j0 = jc - (jc % K);
         const int nk = (int)(jc - j0 + 1);
-        k_newton_acc<T><<<grid_for(nw * len), 256, 0, c->stream>>>(ring, K, j0, nk, a_dev, ncheby, (int)m, filtered,
+        FBSE_COUNT(1); k_newton_acc<T><<<grid_for(nw * len), 256, 0, c->stream>>>(ring, K, j0, nk, a_dev, ncheby, (int)m, filtered,
                                                                    nstart, nw, len, c->is_complex, j0 == 0);
         if (cudaGetLastError() != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "newton accumulation launch"); break; }
       }
@@ -333,7 +346,7 @@ int normalize_all(fbse_ctx *c, double *psitot, long n, double *norms)
   if (cudaMalloc(&d, n * 2 * sizeof(double)) != cudaSuccess) return set_err(c, FBSE_ERR_OOM, "norms");
   std::vector<double> h(2 * n), f(n);
   do {
-    k_sumsq<<<dim3(kRedBlocks, (unsigned)n), 256, 0, c->stream>>>(psitot, stlen, c->red);
+    FBSE_COUNT(2); k_sumsq<<<dim3(kRedBlocks, (unsigned)n), 256, 0, c->stream>>>(psitot, stlen, c->red);
     k_dots_final<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(c->red, kRedBlocks, n, d);
     if (cudaMemcpyAsync(h.data(), d, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "norm reduction"); break; }
@@ -349,7 +362,7 @@ int normalize_all(fbse_ctx *c, double *psitot, long n, double *norms)
       rc = set_err(c, FBSE_ERR_CUDA, "norm upload");
       break;
     }
-    k_scale_states<<<grid_for(n * stlen), 256, 0, c->stream>>>(psitot, stlen, n, d);
+    FBSE_COUNT(1); k_scale_states<<<grid_for(n * stlen), 256, 0, c->stream>>>(psitot, stlen, n, d);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "normalize");
   } while (0);
   cudaFree(d);
@@ -442,10 +455,10 @@ static int energy_range_t(fbse_ctx *c, long seed, long max_iter, double *emin_ou
     if ((rc = hpsi_apply<T>(c, phi, h, 1, 1.0, 0.0))) break;
     for (long i = 0; std::fabs((emin - old) / emin) > 1.0e-6 && i < max_iter; i++) {
       // h holds H phi_i
-      k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, h, len, 1.0, -tau);
+      FBSE_COUNT(1); k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, h, len, 1.0, -tau);
       if ((rc = state_dots<T>(c, phi, nullptr, 1, len, dd, 0))) break;
       const double nrm = std::sqrt(dd[0] * c->dv);
-      k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, phi, len, 1.0 / nrm, 0.0);
+      FBSE_COUNT(1); k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, phi, len, 1.0 / nrm, 0.0);
       if ((rc = hpsi_apply<T>(c, phi, h, 1, 1.0, 0.0))) break;
       if ((rc = state_dots<T>(c, phi, h, 1, len, dd, 1))) break;
       old = emin;
@@ -462,7 +475,7 @@ static int energy_range_t(fbse_ctx *c, long seed, long max_iter, double *emin_ou
     for (long i = 0; std::fabs((emax - old) / emax) > 1.0e-6 && i < max_iter; i++) {
       if ((rc = state_dots<T>(c, h, nullptr, 1, len, dd, 0))) break;
       const double nrm = std::sqrt(dd[0] * c->dv);
-      k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, h, len, 0.0, 1.0 / nrm);
+      FBSE_COUNT(1); k_axpby<T><<<grid_for(len), 256, 0, c->stream>>>(phi, h, len, 0.0, 1.0 / nrm);
       if ((rc = hpsi_apply<T>(c, phi, h, 1, 1.0, 0.0))) break;
       if ((rc = state_dots<T>(c, phi, h, 1, len, dd, 1))) break;
       old = emax;

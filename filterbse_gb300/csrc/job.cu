@@ -1,0 +1,62 @@
+// Host-buffer entry point for the whole filter stage: random starts in host
+// memory in, eigenvalues / sigma_E / eigenvectors in host memory out.  This is
+// the call a drop-in Filter executable makes after the setup: it covers
+// run_filter_cycles + mod_ortho + mod_diag + mod_sigma + the state selection
+// of mod_output (filter_mpi/filter.c:5-183, mod_ortho.c:3-94,
+// mod_diag.c:324-449, mod_sigma.c:6-63, mod_output.c:5-162).
+#include <cmath>
+#include <vector>
+
+#include "fbse_internal.cuh"
+
+namespace fbse {
+int newton_filter(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
+                  const double *psi0, long nstart, double *filtered);
+int ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma);
+}  // namespace fbse
+
+using namespace fbse;
+
+extern "C" int fbse_filter_job(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin,
+                               double de, const double *psi0_host, long nstart, double sigma_cut, long *n_out,
+                               double *eval_host, double *sigma_host, double *psi_host)
+{
+  if (!c || !zn || !an || !psi0_host || nstart < 1 || m < 1 || !n_out || !eval_host || !sigma_host)
+    return c ? set_err(c, FBSE_ERR_ARG, "fbse_filter_job: bad arguments") : FBSE_ERR_ARG;
+  const long stlen = (long)(c->is_complex + 1) * c->nspin * c->ngrid;
+  const long n = nstart * m;
+  double *d0 = nullptr, *df = nullptr;
+  int rc = FBSE_OK;
+  if (cudaMalloc(&d0, (size_t)nstart * stlen * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&df, (size_t)n * stlen * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    if (d0) cudaFree(d0);
+    return set_err(c, FBSE_ERR_OOM, "fbse_filter_job: state buffers");
+  }
+  std::vector<double> ev(n), sg(n);
+  long nk = 0;
+  do {
+    if (cudaMemcpyAsync(d0, psi0_host, (size_t)nstart * stlen * sizeof(double), cudaMemcpyHostToDevice, c->stream) !=
+        cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "fbse_filter_job: upload"); break; }
+    if ((rc = newton_filter(c, zn, an, ncheby, m, vmin, de, d0, nstart, df))) break;
+    if ((rc = ortho_diag_sigma(c, df, n, &nk, ev.data(), sg.data()))) break;
+    // mod_output: all states (sigma_cut <= 0, getAllStates = 1) or those with sigma <= cut
+    long w = 0;
+    for (long i = 0; i < nk; i++) {
+      if (sigma_cut > 0 && !(sg[i] <= sigma_cut)) continue;
+      eval_host[w] = ev[i];
+      sigma_host[w] = sg[i];
+      if (psi_host &&
+          cudaMemcpyAsync(psi_host + w * stlen, df + i * stlen, stlen * sizeof(double), cudaMemcpyDeviceToHost,
+                          c->stream) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "fbse_filter_job: download"); break; }
+      w++;
+    }
+    if (rc) break;
+    *n_out = w;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "fbse_filter_job");
+  } while (0);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(d0);
+  cudaFree(df);
+  return rc;
+}

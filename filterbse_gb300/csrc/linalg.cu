@@ -1,12 +1,633 @@
-// Orthogonalisation, subspace diagonalisation and sigma_E.
+// Orthogonalisation, subspace diagonalisation and sigma_E on the GPU.
+//
+// Replaces mod_ortho (thin SVD, filter_mpi/ortho.c:5-187), mod_diag
+// (diag_H: n H psi, H_ij = dv <psi_i|H|psi_j>, dsyev/zheev, rotation,
+// filter_mpi/Hmat.c:5-297) and mod_sigma (calc_sigma_E, two more H psi per
+// state, filter_mpi/energy.c:383-539) with one Rayleigh-Ritz pass:
+//
+//   1. HPsi = H Psi                       (batched H psi, all n states)
+//   2. G = dv Psi^H Psi, M = dv Psi^H HPsi (split-K GEMMs, FP64 partial sums)
+//   3. G = V diag(l) V^H                  (FP64 Jacobi on the GPU)
+//   4. keep l_i >= l_max * cut (the span of the left singular vectors with
+//      s_i / s_0 above the cutoff), X = V_k diag(l_k)^{-1/2}
+//   5. H' = X^H M X,  H' = U diag(E) U^H  (FP64 Jacobi on the GPU)
+//   6. C = X U;  Psi_f = Psi C and HPsi_f = HPsi C in one pass, whose epilogue
+//      forms the residual r_i = HPsi_f,i - E_i Psi_f,i and the norms
+//   7. sigma_i = ||r_i|| / ||Psi_f,i||, states normalised (normalize_all).
+// H is applied n times in total instead of the reference's 3n, and the Ritz
+// vectors' residuals come from the same two GEMMs that build the vectors.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
 #include "fbse_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace fbse {
 
+int pack_states(fbse_ctx *c, const double *src, void *dst, long nsrc);
+int unpack_states(fbse_ctx *c, const void *src, double *dst, long ndst);
+
+// ---------------------------------------------------------------------------
+// C[i][j] (+)= sum_l conj(A[i][l]) B[j][l]  over a K-chunk, i < n, j < n.
+// A, B: n vectors of length L (complex: interleaved FP64 pairs; real: FP64).
+// Tile 64 x 64 outputs per CTA, 256 threads x (4 x 4) outputs, K step 16.
+// Compute type T (float for the mixed path, double for the FP64 path);
+// partials are written in FP64: part[chunk][i][j].
+// ---------------------------------------------------------------------------
+template <typename T, bool CPLX>
+__global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, const double *__restrict__ B, int n,
+                                              long L, long kchunk, double2 *__restrict__ part)
+{
+  constexpr int TM = 64, TK = 16;
+  __shared__ T As[TK][TM][CPLX ? 2 : 1];
+  __shared__ T Bs[TK][TM][CPLX ? 2 : 1];
+  const int i0 = blockIdx.x * TM, j0 = blockIdx.y * TM;
+  const long k0 = blockIdx.z * kchunk;
+  const long k1 = min(L, k0 + kchunk);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  T accr[4][4], acci[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) { accr[a][b] = 0; acci[a][b] = 0; }
+  for (long kb = k0; kb < k1; kb += TK) {
+    // load: 64 rows x 16 k for A and B; thread t loads rows (t / 16) + 16 q, k = t % 16
+    for (int q = 0; q < 4; q++) {
+      const int r = ty + 16 * q, kk = tx;
+      const long k = kb + kk;
+      const bool okA = (i0 + r < n) && (k < k1);
+      const bool okB = (j0 + r < n) && (k < k1);
+      if (CPLX) {
+        As[kk][r][0] = okA ? (T)A[((long)(i0 + r) * L + k) * 2] : T(0);
+        As[kk][r][CPLX ? 1 : 0] = okA ? (T)A[((long)(i0 + r) * L + k) * 2 + 1] : T(0);
+        Bs[kk][r][0] = okB ? (T)B[((long)(j0 + r) * L + k) * 2] : T(0);
+        Bs[kk][r][CPLX ? 1 : 0] = okB ? (T)B[((long)(j0 + r) * L + k) * 2 + 1] : T(0);
+      } else {
+        As[kk][r][0] = okA ? (T)A[(long)(i0 + r) * L + k] : T(0);
+        Bs[kk][r][0] = okB ? (T)B[(long)(j0 + r) * L + k] : T(0);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; kk++) {
+      T ar[4], ai[4], br[4], bi[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        ar[a] = As[kk][ty + 16 * a][0];
+        ai[a] = CPLX ? As[kk][ty + 16 * a][CPLX ? 1 : 0] : T(0);
+        br[a] = Bs[kk][tx + 16 * a][0];
+        bi[a] = CPLX ? Bs[kk][tx + 16 * a][CPLX ? 1 : 0] : T(0);
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          // conj(a) * b
+          accr[a][b] += ar[a] * br[b] + (CPLX ? ai[a] * bi[b] : T(0));
+          if (CPLX) acci[a][b] += ar[a] * bi[b] - ai[a] * br[b];
+        }
+    }
+    __syncthreads();
+  }
+  double2 *P = part + (long)blockIdx.z * n * n;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+      if (i < n && j < n) P[(long)i * n + j] = make_double2((double)accr[a][b], (double)acci[a][b]);
+    }
+}
+
+__global__ void k_sum_partials(const double2 *__restrict__ part, int nchunk, long nn, double scale,
+                               double2 *__restrict__ out)
+{
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < nn; e += (long)gridDim.x * blockDim.x) {
+    double r = 0, im = 0;
+    for (int c = 0; c < nchunk; c++) { r += part[(long)c * nn + e].x; im += part[(long)c * nn + e].y; }
+    out[e] = make_double2(r * scale, im * scale);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// small dense FP64 complex GEMM: C[m][p] = op(A) op(B), row-major,
+// opA = 'N' (A is m x k) or 'H' (A is k x m, conjugate-transposed)
+// ---------------------------------------------------------------------------
+__global__ void k_zgemm(int m, int p, int k, const double2 *__restrict__ A, int lda, bool ah,
+                        const double2 *__restrict__ B, int ldb, bool bh, double2 *__restrict__ Cm, int ldc)
+{
+  const int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
+  if (i >= m || j >= p) return;
+  double r = 0, im = 0;
+  for (int l = 0; l < k; l++) {
+    double2 a = ah ? A[(long)l * lda + i] : A[(long)i * lda + l];
+    if (ah) a.y = -a.y;
+    double2 b = bh ? B[(long)j * ldb + l] : B[(long)l * ldb + j];
+    if (bh) b.y = -b.y;
+    r += a.x * b.x - a.y * b.y;
+    im += a.x * b.y + a.y * b.x;
+  }
+  Cm[(long)i * ldc + j] = make_double2(r, im);
+}
+
+static int zgemm(fbse_ctx *c, int m, int p, int k, const double2 *A, int lda, bool ah, const double2 *B, int ldb,
+                 bool bh, double2 *C, int ldc)
+{
+  dim3 b(16, 16), g((p + 15) / 16, (m + 15) / 16);
+  k_zgemm<<<g, b, 0, c->stream>>>(m, p, k, A, lda, ah, B, ldb, bh, C, ldc);
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Hermitian eigensolver: cyclic two-sided Jacobi with the round-robin pairing
+// (n/2 disjoint rotations per round, n-1 rounds per sweep), one cooperative
+// launch per sweep with grid-wide barriers between the phases.
+// A (n x n, row-major, Hermitian) is diagonalised in place; V accumulates the
+// unitary so that A_in = V diag(A_out) V^H.
+// ---------------------------------------------------------------------------
+struct Rot {
+  double cs, sn, pr, pi;  // U = D J:  U_pp = cs, U_pq = sn, U_qp = -sn e^{-i phi}, U_qq = cs e^{-i phi}
+  int p, q;
+};
+
+__device__ __forceinline__ void rr_pair(int r, int slot, int m, int &p, int &q)
+{  // round-robin tournament: player m-1 fixed, the others rotate
+  int a, b;
+  if (slot == 0) { a = m - 1; b = r % (m - 1); }
+  else { a = (r + slot) % (m - 1); b = (r - slot + (m - 1)) % (m - 1); }
+  p = min(a, b);
+  q = max(a, b);
+}
+
+__global__ void k_jacobi_sweep(double2 *__restrict__ A, double2 *__restrict__ V, int n, int m, Rot *__restrict__ rot,
+                               double *__restrict__ off)
+{
+  cg::grid_group grid = cg::this_grid();
+  const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long nth = (long)gridDim.x * blockDim.x;
+  const int half = m / 2;
+  for (int r = 0; r < m - 1; r++) {
+    // phase 1: rotation parameters for the n/2 pairs of this round
+    for (long s = tid; s < half; s += nth) {
+      int p, q;
+      rr_pair(r, (int)s, m, p, q);
+      Rot R{1.0, 0.0, 1.0, 0.0, p, q};
+      if (q < n) {
+        const double app = A[(long)p * n + p].x, aqq = A[(long)q * n + q].x;
+        const double2 apq = A[(long)p * n + q];
+        const double mag = hypot(apq.x, apq.y);
+        if (mag > 1e-300 && mag > 1e-18 * sqrt(fabs(app * aqq))) {
+          const double tau = (aqq - app) / (2.0 * mag);
+          const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+          R.cs = 1.0 / sqrt(1.0 + t * t);
+          R.sn = t * R.cs;
+          R.pr = apq.x / mag;  // e^{i phi}
+          R.pi = apq.y / mag;
+        }
+      }
+      rot[s] = R;
+    }
+    grid.sync();
+    // phase 2: rows p, q of A <- U^H rows   (new row p = cs a_p - sn e^{i phi} a_q,
+    //                                        new row q = sn a_p + cs e^{i phi} a_q)
+    for (long w = tid; w < (long)half * n; w += nth) {
+      const Rot R = rot[w / n];
+      const int col = (int)(w % n);
+      if (R.q >= n) continue;
+      const double2 ap = A[(long)R.p * n + col], aq = A[(long)R.q * n + col];
+      const double2 e = make_double2(R.pr, R.pi);
+      const double2 eaq = make_double2(e.x * aq.x - e.y * aq.y, e.x * aq.y + e.y * aq.x);
+      A[(long)R.p * n + col] = make_double2(R.cs * ap.x - R.sn * eaq.x, R.cs * ap.y - R.sn * eaq.y);
+      A[(long)R.q * n + col] = make_double2(R.sn * ap.x + R.cs * eaq.x, R.sn * ap.y + R.cs * eaq.y);
+    }
+    grid.sync();
+    // phase 3: columns p, q of A and V <- cols U  (new col p = cs a_p - sn e^{-i phi} a_q,
+    //                                             new col q = sn a_p + cs e^{-i phi} a_q)
+    for (long w = tid; w < (long)half * n * 2; w += nth) {
+      const long w2 = w % ((long)half * n);
+      const bool onV = w >= (long)half * n;
+      const Rot R = rot[w2 / n];
+      const int row = (int)(w2 % n);
+      if (R.q >= n) continue;
+      double2 *M = onV ? V : A;
+      const double2 ap = M[(long)row * n + R.p], aq = M[(long)row * n + R.q];
+      const double2 e = make_double2(R.pr, -R.pi);
+      const double2 eaq = make_double2(e.x * aq.x - e.y * aq.y, e.x * aq.y + e.y * aq.x);
+      M[(long)row * n + R.p] = make_double2(R.cs * ap.x - R.sn * eaq.x, R.cs * ap.y - R.sn * eaq.y);
+      M[(long)row * n + R.q] = make_double2(R.sn * ap.x + R.cs * eaq.x, R.sn * ap.y + R.cs * eaq.y);
+    }
+    grid.sync();
+    // the rotated pair is exactly diagonal in exact arithmetic: clean it
+    for (long s = tid; s < half; s += nth) {
+      const Rot R = rot[s];
+      if (R.q < n && !(R.cs == 1.0 && R.sn == 0.0)) {
+        A[(long)R.p * n + R.q] = make_double2(0, 0);
+        A[(long)R.q * n + R.p] = make_double2(0, 0);
+      }
+    }
+    grid.sync();
+  }
+  // off-diagonal Frobenius norm and diagonal norm
+  if (tid == 0) { off[0] = 0; off[1] = 0; }
+  grid.sync();
+  double so = 0, sd = 0;
+  for (long e = tid; e < (long)n * n; e += nth) {
+    const double2 a = A[e];
+    const double v = a.x * a.x + a.y * a.y;
+    if (e / n == e % n) sd += v;
+    else so += v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    so += __shfl_xor_sync(0xffffffffu, so, o);
+    sd += __shfl_xor_sync(0xffffffffu, sd, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&off[0], so);
+    atomicAdd(&off[1], sd);
+  }
+}
+
+__global__ void k_identity(double2 *V, int n)
+{
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)n * n; e += (long)gridDim.x * blockDim.x)
+    V[e] = make_double2(e / n == e % n ? 1.0 : 0.0, 0.0);
+}
+
+// eigen-decomposition of the Hermitian n x n matrix A (device, overwritten);
+// V (device, n x n) receives the eigenvectors as columns, w (host) the
+// eigenvalues in the order of V's columns
+static int jacobi_eig(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<double> &w)
+{
+  const int m = n + (n & 1);
+  Rot *rot = nullptr;
+  double *off = nullptr;
+  if (cudaMalloc(&rot, sizeof(Rot) * (m / 2 + 1)) != cudaSuccess) return set_err(c, FBSE_ERR_OOM, "jacobi");
+  if (cudaMalloc(&off, 2 * sizeof(double)) != cudaSuccess) { cudaFree(rot); return set_err(c, FBSE_ERR_OOM, "jacobi"); }
+  FBSE_COUNT(1); k_identity<<<256, 256, 0, c->stream>>>(V, n);
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_sweep, 256, 0);
+  long want = ((long)(m / 2) * n * 2 + 255) / 256;
+  int blocks = (int)std::min<long>(std::max<long>(1, want), (long)nsm * std::max(1, per_sm));
+  int rc = FBSE_OK;
+  double h[2] = {0, 0};
+  bool conv = (n < 2);
+  for (int sweep = 0; sweep < 60 && !conv; sweep++) {
+    void *args[] = {&A, &V, &n, (void *)&m, &rot, &off};
+    int mm = m;
+    args[3] = &mm;
+    FBSE_COUNT(1); if (cudaLaunchCooperativeKernel((void *)k_jacobi_sweep, blocks, 256, args, 0, c->stream) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, std::string("jacobi launch: ") + cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    if (cudaMemcpyAsync(h, off, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "jacobi sweep");
+      break;
+    }
+    if (!(h[0] == h[0])) { rc = set_err(c, FBSE_ERR_NAN, "jacobi: NaN in matrix"); break; }
+    if (h[0] <= 1e-30 * h[1] || h[0] < 1e-300) conv = true;
+  }
+  if (!rc && !conv) rc = set_err(c, FBSE_ERR_NOCONV, "jacobi eigensolver did not converge in 60 sweeps");
+  if (!rc) {
+    std::vector<double2> d((size_t)n * n);
+    // only the diagonal is needed on the host
+    w.resize(n);
+    for (int i = 0; i < n && !rc; i++) {
+      double2 v;
+      if (cudaMemcpyAsync(&v, A + (long)i * n + i, sizeof(double2), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+        rc = set_err(c, FBSE_ERR_CUDA, "jacobi download");
+      else d[i] = v;
+    }
+    if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "jacobi download");
+    for (int i = 0; i < n; i++) w[i] = d[i].x;
+  }
+  cudaFree(rot);
+  cudaFree(off);
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// rotation with residual epilogue
+//   P[i][l] = sum_j Psi[j][l] C[j][i],  Q[i][l] = sum_j HPsi[j][l] C[j][i]
+//   out[i][l] = P;  part[blk][i] += |Q - E_i P|^2, |P|^2, Re(conj(P) Q)
+// tile: 128 grid elements x 32 output states per CTA, 256 threads
+// ---------------------------------------------------------------------------
+template <typename T, bool CPLX>
+__global__ void __launch_bounds__(256) k_rotate(const double *__restrict__ Psi, const double *__restrict__ HPsi, int n,
+                                                long L, const double2 *__restrict__ Cm, int k,
+                                                const double *__restrict__ E, double *__restrict__ out,
+                                                double *__restrict__ part)
+{
+  constexpr int TL = 128, TS = 32, TJ = 8;
+  const long l0 = (long)blockIdx.x * TL;
+  const int s0 = blockIdx.y * TS;
+  __shared__ T Ps[TJ][TL][CPLX ? 2 : 1];
+  __shared__ T Hs[TJ][TL][CPLX ? 2 : 1];
+  __shared__ T Cs[TJ][TS][2];
+  __shared__ double red[TS][3];
+  const int tl = threadIdx.x % 32;  // 4 grid elements per thread: tl + 32 q
+  const int ts = threadIdx.x / 32;  // 4 output states per thread: ts + 8 r
+  T pr[4][4], pim[4][4], qr[4][4], qim[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) { pr[a][b] = pim[a][b] = qr[a][b] = qim[a][b] = 0; }
+  if (threadIdx.x < TS * 3) red[threadIdx.x / 3][threadIdx.x % 3] = 0;
+  for (int jb = 0; jb < n; jb += TJ) {
+    for (int t = threadIdx.x; t < TJ * TL; t += 256) {
+      const int jj = t / TL, ll = t % TL;
+      const int j = jb + jj;
+      const long l = l0 + ll;
+      const bool ok = (j < n) && (l < L);
+      if (CPLX) {
+        Ps[jj][ll][0] = ok ? (T)Psi[((long)j * L + l) * 2] : T(0);
+        Ps[jj][ll][CPLX ? 1 : 0] = ok ? (T)Psi[((long)j * L + l) * 2 + 1] : T(0);
+        Hs[jj][ll][0] = ok ? (T)HPsi[((long)j * L + l) * 2] : T(0);
+        Hs[jj][ll][CPLX ? 1 : 0] = ok ? (T)HPsi[((long)j * L + l) * 2 + 1] : T(0);
+      } else {
+        Ps[jj][ll][0] = ok ? (T)Psi[(long)j * L + l] : T(0);
+        Hs[jj][ll][0] = ok ? (T)HPsi[(long)j * L + l] : T(0);
+      }
+    }
+    for (int t = threadIdx.x; t < TJ * TS; t += 256) {
+      const int jj = t / TS, ss = t % TS;
+      const int j = jb + jj, s = s0 + ss;
+      const double2 v = (j < n && s < k) ? Cm[(long)j * k + s] : make_double2(0, 0);
+      Cs[jj][ss][0] = (T)v.x;
+      Cs[jj][ss][1] = (T)v.y;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int jj = 0; jj < TJ; jj++) {
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        const int ll = tl + 32 * a;
+        const T xr = Ps[jj][ll][0], xi = CPLX ? Ps[jj][ll][CPLX ? 1 : 0] : T(0);
+        const T yr = Hs[jj][ll][0], yi = CPLX ? Hs[jj][ll][CPLX ? 1 : 0] : T(0);
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          const int ss = ts + 8 * b;
+          const T cr = Cs[jj][ss][0], ci = Cs[jj][ss][1];
+          pr[a][b] += xr * cr - xi * ci;
+          pim[a][b] += xr * ci + xi * cr;
+          qr[a][b] += yr * cr - yi * ci;
+          qim[a][b] += yr * ci + yi * cr;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // epilogue
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    const int s = s0 + ts + 8 * b;
+    double rr = 0, pp = 0, pq = 0;
+    if (s < k) {
+      const double e = E[s];
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        const long l = l0 + tl + 32 * a;
+        if (l < L) {
+          const double Pr = pr[a][b], Pi = CPLX ? (double)pim[a][b] : 0.0;
+          const double Qr = qr[a][b], Qi = CPLX ? (double)qim[a][b] : 0.0;
+          if (CPLX) {
+            out[((long)s * L + l) * 2] = Pr;
+            out[((long)s * L + l) * 2 + 1] = Pi;
+          } else {
+            out[(long)s * L + l] = Pr;
+          }
+          const double dr = Qr - e * Pr, di = Qi - e * Pi;
+          rr += dr * dr + di * di;
+          pp += Pr * Pr + Pi * Pi;
+          pq += Pr * Qr + Pi * Qi;
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      rr += __shfl_xor_sync(0xffffffffu, rr, o);
+      pp += __shfl_xor_sync(0xffffffffu, pp, o);
+      pq += __shfl_xor_sync(0xffffffffu, pq, o);
+    }
+    if (tl == 0) {
+      red[ts + 8 * b][0] = rr;
+      red[ts + 8 * b][1] = pp;
+      red[ts + 8 * b][2] = pq;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < TS) {
+    const int s = s0 + threadIdx.x;
+    if (s < k) {
+      double *P = part + ((long)blockIdx.x * k + s) * 3;
+      P[0] = red[threadIdx.x][0];
+      P[1] = red[threadIdx.x][1];
+      P[2] = red[threadIdx.x][2];
+    }
+  }
+}
+
+__global__ void k_sum_rot(const double *__restrict__ part, int nblk, int k, double *__restrict__ out)
+{
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < k; s += gridDim.x * blockDim.x) {
+    double a = 0, b = 0, d = 0;
+    for (int q = 0; q < nblk; q++) {
+      a += part[((long)q * k + s) * 3];
+      b += part[((long)q * k + s) * 3 + 1];
+      d += part[((long)q * k + s) * 3 + 2];
+    }
+    out[3 * s] = a;
+    out[3 * s + 1] = b;
+    out[3 * s + 2] = d;
+  }
+}
+
+__global__ void k_scale_copy(const double *__restrict__ src, double *__restrict__ dst, long stlen, long k,
+                             const double *__restrict__ f)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < k * stlen; i += (long)gridDim.x * blockDim.x)
+    dst[i] = src[i] * f[i / stlen];
+}
+
+// X[j][s] = V[j][keep[s]] / sqrt(l[keep[s]])
+__global__ void k_build_x(const double2 *__restrict__ V, int n, const int *__restrict__ keep,
+                          const double *__restrict__ lam, int k, double2 *__restrict__ X)
+{
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)n * k; e += (long)gridDim.x * blockDim.x) {
+    const int j = (int)(e / k), s = (int)(e % k);
+    const double f = 1.0 / sqrt(lam[s]);
+    const double2 v = V[(long)j * n + keep[s]];
+    X[e] = make_double2(v.x * f, v.y * f);
+  }
+}
+
+__global__ void k_hermitize(double2 *A, int n)
+{
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)n * n; e += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    if (i > j) continue;
+    const double2 a = A[(long)i * n + j], b = A[(long)j * n + i];
+    const double2 h = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+    A[(long)i * n + j] = h;
+    A[(long)j * n + i] = make_double2(h.x, -h.y);
+  }
+}
+
+// permute the columns of U (k x k): U2[:, s] = U[:, perm[s]]
+__global__ void k_permute_cols(const double2 *__restrict__ U, const int *__restrict__ perm, int k,
+                               double2 *__restrict__ U2)
+{
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (long)k * k; e += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / k), s = (int)(e % k);
+    U2[e] = U[(long)i * k + perm[s]];
+  }
+}
+
+template <typename T>
+static int gram_t(fbse_ctx *c, const double *A, const double *B, int n, long L, double2 *out, double scale,
+                  double2 *part, int nchunk, long kchunk)
+{
+  dim3 g((n + 63) / 64, (n + 63) / 64, nchunk);
+  if (c->is_complex) k_gram<T, true><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
+  else k_gram<T, false><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
+  FBSE_CHECK_LAUNCH(c);
+  k_sum_partials<<<256, 256, 0, c->stream>>>(part, nchunk, (long)n * n, scale, out);
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+template <typename T>
+static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept, double *eval, double *sigma)
+{
+  const int n = (int)n_;
+  const long len = (long)c->nspin * c->ngrid;     // points per state
+  const long stlen = (long)(c->is_complex + 1) * len;
+  const long L = len;                              // vector length in (complex or real) elements
+  int rc = FBSE_OK;
+  // scratch: HPsi (n states FP64), rotated states (n states FP64), working states
+  double *hpsi = nullptr, *rot = nullptr;
+  void *work = nullptr;
+  double2 *G = nullptr, *M = nullptr, *V = nullptr, *X = nullptr, *Hp = nullptr, *Tm = nullptr, *U = nullptr,
+          *Cm = nullptr, *part = nullptr;
+  double *lam = nullptr, *Ed = nullptr, *rpart = nullptr, *rsum = nullptr, *fac = nullptr;
+  int *keepd = nullptr, *permd = nullptr;
+  const long chunk_states = 16;
+  const long nw_chunk = c->is_complex ? chunk_states : chunk_states / 2;
+  const int nchunk = (int)std::min<long>(std::max<long>(1, L / 4096), 1024);
+  const long kchunk = (L + nchunk - 1) / nchunk;
+  const int nrb = (int)((L + 127) / 128);
+  auto alloc = [&](void **p, size_t b) -> bool {
+    if (cudaMalloc(p, b) != cudaSuccess) { cudaGetLastError(); rc = set_err(c, FBSE_ERR_OOM, "ortho/diag scratch"); return false; }
+    return true;
+  };
+  do {
+    if (!alloc((void **)&hpsi, (size_t)n * stlen * sizeof(double))) break;
+    if (!alloc((void **)&rot, (size_t)n * stlen * sizeof(double))) break;
+    if (!alloc(&work, (size_t)2 * nw_chunk * len * sizeof(C<T>))) break;
+    const size_t nn = (size_t)n * n;
+    if (!alloc((void **)&G, nn * sizeof(double2)) || !alloc((void **)&M, nn * sizeof(double2)) ||
+        !alloc((void **)&V, nn * sizeof(double2)) || !alloc((void **)&X, nn * sizeof(double2)) ||
+        !alloc((void **)&Hp, nn * sizeof(double2)) || !alloc((void **)&Tm, nn * sizeof(double2)) ||
+        !alloc((void **)&U, nn * sizeof(double2)) || !alloc((void **)&Cm, nn * sizeof(double2)) ||
+        !alloc((void **)&part, (size_t)nchunk * nn * sizeof(double2)) || !alloc((void **)&lam, n * sizeof(double)) ||
+        !alloc((void **)&Ed, n * sizeof(double)) || !alloc((void **)&rpart, (size_t)nrb * n * 3 * sizeof(double)) ||
+        !alloc((void **)&rsum, (size_t)n * 3 * sizeof(double)) || !alloc((void **)&fac, n * sizeof(double)) ||
+        !alloc((void **)&keepd, n * sizeof(int)) || !alloc((void **)&permd, n * sizeof(int)))
+      break;
+    // 1. HPsi in chunks of working states
+    C<T> *w0 = reinterpret_cast<C<T> *>(work), *w1 = w0 + nw_chunk * len;
+    for (long s0 = 0; s0 < n && !rc; s0 += chunk_states) {
+      const long ns = std::min<long>(chunk_states, n - s0);
+      const long nw = c->is_complex ? ns : (ns + 1) / 2;
+      if ((rc = pack_states(c, psitot + s0 * stlen, w0, ns))) break;
+      if ((rc = hpsi_apply<T>(c, w0, w1, nw, 1.0, 0.0))) break;
+      if ((rc = unpack_states(c, w1, hpsi + s0 * stlen, ns))) break;
+    }
+    if (rc) break;
+    // 2. Gram and projected H (dv-weighted)
+    if ((rc = gram_t<T>(c, psitot, psitot, n, L, G, c->dv, part, nchunk, kchunk))) break;
+    if ((rc = gram_t<T>(c, psitot, hpsi, n, L, M, c->dv, part, nchunk, kchunk))) break;
+    FBSE_COUNT(2); k_hermitize<<<64, 256, 0, c->stream>>>(G, n);
+    k_hermitize<<<64, 256, 0, c->stream>>>(M, n);
+    // 3. overlap eigen-decomposition
+    std::vector<double> w;
+    if ((rc = jacobi_eig(c, G, V, n, w))) break;
+    // 4. rank cutoff (ortho.c:68-75 keeps s_i/s_0 >= 1e-10); the overlap
+    //    resolves l_i / l_max to the precision of its products
+    double lmax = 0;
+    for (double v : w) lmax = std::max(lmax, v);
+    const double cut = lmax * (c->precision == FBSE_MIXED ? 1e-6 : 1e-12);
+    std::vector<int> keep;
+    std::vector<int> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return w[a] > w[b]; });
+    for (int i : order)
+      if (w[i] > cut && w[i] >= lmax * 1e-20) keep.push_back(i);
+    const int k = (int)keep.size();
+    *n_kept = k;
+    if (k == 0) { rc = set_err(c, FBSE_ERR_NAN, "orthogonalisation kept no states"); break; }
+    std::vector<double> lk(k);
+    for (int s = 0; s < k; s++) lk[s] = w[keep[s]];
+    cudaMemcpyAsync(keepd, keep.data(), k * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(lam, lk.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    FBSE_COUNT(1); k_build_x<<<64, 256, 0, c->stream>>>(V, n, keepd, lam, k, X);
+    // 5. H' = X^H M X  (k x k), Hermitian eigen-decomposition
+    if ((rc = zgemm(c, n, k, n, M, n, false, X, k, false, Tm, k))) break;   // Tm = M X   (n x k)
+    if ((rc = zgemm(c, k, k, n, X, k, true, Tm, k, false, Hp, k))) break;  // Hp = X^H Tm (k x k)
+    FBSE_COUNT(1); k_hermitize<<<64, 256, 0, c->stream>>>(Hp, k);
+    std::vector<double> e;
+    if ((rc = jacobi_eig(c, Hp, U, k, e))) break;
+    std::vector<int> perm(k);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::sort(perm.begin(), perm.end(), [&](int a, int b) { return e[a] < e[b]; });
+    std::vector<double> es(k);
+    for (int s = 0; s < k; s++) es[s] = e[perm[s]];
+    cudaMemcpyAsync(permd, perm.data(), k * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(Ed, es.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    FBSE_COUNT(1); k_permute_cols<<<64, 256, 0, c->stream>>>(U, permd, k, Tm);
+    // 6. C = X U  (n x k); rotate Psi and HPsi with the residual epilogue
+    if ((rc = zgemm(c, n, k, k, X, k, false, Tm, k, false, Cm, k))) break;
+    dim3 gr(nrb, (k + 31) / 32);
+    if (c->is_complex) k_rotate<T, true><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+    else k_rotate<T, false><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+    FBSE_CHECK_LAUNCH(c);
+    FBSE_COUNT(1); k_sum_rot<<<(k + 127) / 128, 128, 0, c->stream>>>(rpart, nrb, k, rsum);
+    std::vector<double> hs(3 * k);
+    if (cudaMemcpyAsync(hs.data(), rsum, 3 * k * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "rotation"); break; }
+    // 7. normalise, report E (Ritz value) and sigma = ||(H - E) psi|| for the normalised state
+    std::vector<double> f(k);
+    for (int s = 0; s < k; s++) {
+      const double nrm = hs[3 * s + 1] * c->dv;
+      if (!(nrm > 0)) { rc = set_err(c, FBSE_ERR_NAN, "Norm is 0/NAN after diagonalisation"); break; }
+      f[s] = 1.0 / std::sqrt(nrm);
+      eval[s] = es[s];
+      sigma[s] = std::sqrt(std::fabs(hs[3 * s]) * c->dv) * f[s];
+    }
+    if (rc) break;
+    cudaMemcpyAsync(fac, f.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    k_scale_copy<<<4096, 256, 0, c->stream>>>(rot, psitot, stlen, k, fac);
+    FBSE_CHECK_LAUNCH(c);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "ortho/diag/sigma");
+  } while (0);
+  cudaStreamSynchronize(c->stream);
+  void *bufs[] = {hpsi, rot, work, G, M, V, X, Hp, Tm, U, Cm, part, lam, Ed, rpart, rsum, fac, keepd, permd};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  return rc;
+}
+
 int ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma)
 {
-  (void)psitot; (void)n; (void)n_kept; (void)eval; (void)sigma;
-  return set_err(c, FBSE_ERR_UNSUPPORTED, "ortho/diag/sigma not built yet");
+  if (n > 8192) return set_err(c, FBSE_ERR_UNSUPPORTED, "more than 8192 states in one subspace");
+  return c->precision == FBSE_MIXED ? ortho_diag_sigma_t<float>(c, psitot, n, n_kept, eval, sigma)
+                                    : ortho_diag_sigma_t<double>(c, psitot, n, n_kept, eval, sigma);
 }
 
 }  // namespace fbse

@@ -1,0 +1,297 @@
+"""Synthetic nanocrystal workloads in the reference's own input model.
+
+Builds what the reference reads from conf.par / pot*.par / SO_*.par and sets
+up in mod_init / mod_pseudopot: a passivated zincblende CdSe sphere, the
+grid of init_grid_params, the local potential of build_local_pot (on the GPU,
+fbse_build_local_pot), the spin-orbit radial projectors of gen_SO_projectors
+and the projector table of init_NL_projectors.  This is the input generator
+(the counterpart of the reference's example scripts), not part of the
+per-step hot path.
+
+Recorded choices (the reference does not fix them):
+  * lattice constant 6.08 A, zincblende, sphere centred on a Cd site; core
+    atoms with fewer than two core neighbours are dropped (repeatedly);
+  * one ligand per dangling bond along the bond: P1 at 0.55 of the bond from
+    Cd, P2 at 0.25 from Se (the 2.2 nm CdSe example places them at 2.74 and
+    1.24-1.49 bohr of a 4.97 bohr bond);
+  * local potentials: the reference's shipped II-VI tables (potCd, potSe,
+    potP1, potP2) -- the BASELINE form-factor parameters are not given, and
+    the shipped tables are the recorded alternative;
+  * spin-orbit: SO_par = 0.01 for Cd and Se, NL parameters 0 (no NL term).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+ANG = 1.889726125  # bohr per angstrom (filter_mpi/fd.h ANGTOBOHR)
+PROJ_LEN = 1024
+NPROJ = 5
+_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+POT_DIR = os.path.join(_ROOT, "tests", "golden", "cdse22")
+
+
+@dataclass
+class Grid:
+    nx: int
+    ny: int
+    nz: int
+    dx: float
+    dy: float
+    dz: float
+    xmin: float
+    ymin: float
+    zmin: float
+    ke_max: float = 20.0
+
+    @property
+    def ngrid(self):
+        return self.nx * self.ny * self.nz
+
+    @property
+    def dv(self):
+        return self.dx * self.dy * self.dz
+
+    def axes(self):
+        out = []
+        for n, d, lo in ((self.nx, self.dx, self.xmin), (self.ny, self.dy, self.ymin), (self.nz, self.dz, self.zmin)):
+            a = np.empty(n)
+            v = lo
+            for j in range(n):  # cumulative sums as build_grid_ksqr (init.c:284-290)
+                a[j] = v
+                v += d
+            out.append(a)
+        return out
+
+    def dk(self):
+        return tuple(2.0 * np.pi / (n * d if n % 2 == 0 else (n - 1) * d)
+                     for n, d in ((self.nx, self.dx), (self.ny, self.dy), (self.nz, self.dz)))
+
+
+@dataclass
+class ProjTable:
+    nl: np.ndarray
+    npts: int
+    jxyz: np.ndarray
+    y1: np.ndarray
+    proj: np.ndarray
+    nlp: np.ndarray
+    sgn: np.ndarray
+    nproj: int = NPROJ
+
+
+@dataclass
+class Dot:
+    types: list
+    coords: np.ndarray  # bohr, centred
+    grid: Grid
+    pot: np.ndarray
+    proj: ProjTable | None
+    nspin: int
+    is_complex: bool
+    so: bool
+    nl: bool
+
+    @property
+    def n_core(self):
+        return sum(1 for t in self.types if not t.startswith("P"))
+
+
+def zincblende_dot(radius_ang: float, a_ang: float = 6.08):
+    """Passivated zincblende CdSe sphere; returns (types, coords in bohr), core first."""
+    a = a_ang * ANG
+    R = radius_ang * ANG
+    n = int(np.ceil(R / a)) + 2
+    fcc = np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0]])
+    cells = np.array([[i, j, k] for i in range(-n, n + 1) for j in range(-n, n + 1) for k in range(-n, n + 1)], float)
+    cd = (cells[:, None, :] + fcc[None]).reshape(-1, 3) * a
+    se = cd + a * 0.25
+    pos = np.vstack([cd, se])
+    kind = np.array([0] * len(cd) + [1] * len(se))
+    keep = np.linalg.norm(pos, axis=1) <= R
+    pos, kind = pos[keep], kind[keep]
+    bonds = a / 4.0 * np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], float)
+    bl = np.linalg.norm(bonds[0])
+
+    def neighbour_mask(pos, kind):
+        from scipy.spatial import cKDTree
+        tree = cKDTree(pos)
+        has = np.zeros((len(pos), 4), bool)
+        for b in range(4):
+            sgn = np.where(kind == 0, 1.0, -1.0)[:, None]
+            d, _ = tree.query(pos + sgn * bonds[b], distance_upper_bound=0.1)
+            has[:, b] = np.isfinite(d)
+        return has
+
+    while True:
+        has = neighbour_mask(pos, kind)
+        ok = has.sum(axis=1) >= 2
+        if ok.all():
+            break
+        pos, kind = pos[ok], kind[ok]
+    has = neighbour_mask(pos, kind)
+    lig_pos, lig_typ = [], []
+    for i in range(len(pos)):
+        sgn = 1.0 if kind[i] == 0 else -1.0
+        for b in range(4):
+            if not has[i, b]:
+                frac = 0.55 if kind[i] == 0 else 0.25
+                lig_pos.append(pos[i] + sgn * bonds[b] * frac)
+                lig_typ.append("P1" if kind[i] == 0 else "P2")
+    order = np.argsort(kind, kind="stable")
+    types = ["Cd" if k == 0 else "Se" for k in kind[order]] + lig_typ
+    coords = np.vstack([pos[order], np.array(lig_pos).reshape(-1, 3)])
+    coords = coords - coords.mean(axis=0)  # centerConf (read.c)
+    return types, coords
+
+
+def reference_grid(coords, d, ke_max=20.0, n_in=(0, 0, 0)) -> Grid:
+    """init_grid_params (filter_mpi/init.c:5-255, non-periodic)."""
+    dims = []
+    for ax in range(3):
+        c = coords[:, ax]
+        ext = float(c.max() - c.min())
+        xd = np.rint(0.5 * ext + 5.0)
+        ntmp = int(((xd - d) - (-xd)) / d)
+        n = n_in[ax]
+        if ntmp > n:
+            n = ntmp + (ntmp % 2)
+        box = n * d if n % 2 == 0 else (n - 1) * d
+        dims.append((n, -box / 2.0))
+    return Grid(dims[0][0], dims[1][0], dims[2][0], d, d, d, dims[0][1], dims[1][1], dims[2][1], ke_max)
+
+
+def read_table(path):
+    t = np.loadtxt(path)
+    return t[:, 0].copy(), t[:, 1].copy()
+
+
+def local_pot(grid: Grid, types, coords, pot_dir=POT_DIR) -> np.ndarray:
+    """Local potential on the GPU (fbse_build_local_pot)."""
+    from . import load
+    uniq = sorted(set(types), key=types.index)
+    tabs = [read_table(os.path.join(pot_dir, f"pot{t}.par")) for t in uniq]
+    tr = np.concatenate([t[0] for t in tabs])
+    tv = np.concatenate([t[1] for t in tabs])
+    tlen = np.array([len(t[0]) for t in tabs], np.int64)
+    toff = np.concatenate([[0], np.cumsum(tlen)[:-1]]).astype(np.int64)
+    at = np.array([uniq.index(t) for t in types], np.int32)
+    gx, gy, gz = grid.axes()
+    xyz = np.ascontiguousarray(coords, np.float64)
+    pot = np.empty(grid.ngrid)
+    D = ctypes.POINTER(ctypes.c_double)
+    Lp = ctypes.POINTER(ctypes.c_long)
+    L = load()
+    L.fbse_build_local_pot.argtypes = [ctypes.c_long] * 3 + [D] * 3 + [ctypes.c_long, D,
+                                                                     ctypes.POINTER(ctypes.c_int), ctypes.c_int, D, D,
+                                                                     Lp, Lp, D]
+    rc = L.fbse_build_local_pot(grid.nx, grid.ny, grid.nz, gx.ctypes.data_as(D), gy.ctypes.data_as(D),
+                                gz.ctypes.data_as(D), len(at), xyz.ctypes.data_as(D),
+                                at.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(uniq), tr.ctypes.data_as(D),
+                                tv.ctypes.data_as(D), toff.ctypes.data_as(Lp), tlen.ctypes.data_as(Lp),
+                                pot.ctypes.data_as(D))
+    if rc:
+        raise RuntimeError(f"fbse_build_local_pot failed ({rc})")
+    return pot
+
+
+def r_nlcut2(dx):
+    return 1.5 + 6.0 * np.log(10.0) + 3.0 * dx  # read.c:908
+
+
+def so_radial(dx, rcut, nproj=NPROJ):
+    """gen_SO_projectors (filter_mpi/projectors.c:12-84) in numpy: the leading
+    eigenvectors of the k-space matrix of the Gaussian (width 0.7) radial SO
+    shape, transformed back to r on PROJ_LEN points."""
+    N = PROJ_LEN
+    dk = 1.5 * np.pi / dx / N
+    dr = rcut / N
+    k = np.arange(N) * dk
+    r = np.arange(N) * dr
+    kr = k[:, None] * r[None, :]
+    x1 = 1.0 / (kr + 1e-10)
+    J = np.where(kr < 1e-10, 0.0, np.sin(kr) * x1 * x1 - np.cos(kr) * x1)
+    w = np.exp(-(r / 0.7) ** 2) * r * r * dr
+    w[0] = 0.0
+    A = (J * w[None, :]) @ J.T
+    ev, vec = np.linalg.eigh(A)
+    out = np.empty((nproj, N))
+    for p in range(nproj):
+        lam = ev[N - p - 1]
+        out[p] = (2.0 / np.pi) * np.sqrt(lam) * ((k * k * dk)[None, :] * J.T * vec[:, N - p - 1][None, :]).sum(axis=1)
+    return out
+
+
+def nlc_table(grid: Grid, coords, so_par, so_tab, nproj=NPROJ) -> ProjTable:
+    """init_NL_projectors (filter_mpi/init.c, body 508-589) vectorised per atom:
+    grid points with r^2 < R_NLcut2 in jz, jy, jx order, Y_1m with the
+    reference's EPSDX shifts, SO radial interpolated and scaled by sqrt(SO_par)."""
+    rc2 = r_nlcut2(grid.dx)
+    rc = np.sqrt(rc2)
+    gx, gy, gz = grid.axes()
+    N = PROJ_LEN
+    drp = rc / N
+    vr = np.arange(N) * drp
+    tmp1 = 0.5 * np.sqrt(3.0 / np.pi)
+    tmp2 = 0.5 * np.sqrt(3.0 / (2.0 * np.pi))
+    eps = 1e-20
+    rows = []
+    for a in range(len(coords)):
+        sx = np.nonzero(np.abs(gx - coords[a, 0]) < rc + grid.dx)[0]
+        sy = np.nonzero(np.abs(gy - coords[a, 1]) < rc + grid.dy)[0]
+        sz = np.nonzero(np.abs(gz - coords[a, 2]) < rc + grid.dz)[0]
+        JZ, JY, JX = np.meshgrid(sz, sy, sx, indexing="ij")
+        dx = gx[JX] - coords[a, 0]
+        dy = gy[JY] - coords[a, 1]
+        dz = gz[JZ] - coords[a, 2]
+        d2 = dx * dx + dy * dy + dz * dz
+        m = d2 < rc2
+        dx, dy, dz, d2 = dx[m], dy[m], dz[m], d2[m]
+        jxyz = (grid.nx * (grid.ny * JZ[m] + JY[m]) + JX[m]).astype(np.int32)
+        y = np.zeros((len(d2), 6))
+        r1 = 1.0 / np.sqrt(dx * dx + dy * dy + (dz + eps) ** 2)
+        y[:, 2] = tmp1 * (dz + eps) * r1
+        r1 = 1.0 / np.sqrt((dx + eps) ** 2 + dy * dy + dz * dz)
+        y[:, 4] = -tmp2 * (dx + eps) * r1
+        y[:, 0] = tmp2 * (dx + eps) * r1
+        r1 = 1.0 / np.sqrt(dx * dx + (dy + eps) ** 2 + dz * dz)
+        y[:, 5] = -tmp2 * (dy + eps) * r1
+        y[:, 1] = -tmp2 * (dy + eps) * r1
+        r = np.sqrt(d2)
+        i = (r / drp).astype(np.int64)
+        ok = i <= N - 2
+        ic = np.minimum(i, N - 2)
+        pr = np.empty((len(r), nproj))
+        for p in range(nproj):
+            t = so_tab[p]
+            sl = (t[ic + 1] - t[ic]) / (vr[ic + 1] - vr[ic])
+            pr[:, p] = np.where(ok, sl * r + (t[ic] - vr[ic] * sl), 0.0) * np.sqrt(so_par[a])
+        rows.append((jxyz, y, pr))
+    npts = max(1, max(len(r[0]) for r in rows))
+    nat = len(rows)
+    nl = np.array([len(r[0]) for r in rows], np.int64)
+    jx = np.zeros(nat * npts, np.int32)
+    y1 = np.zeros(nat * npts * 6)
+    pj = np.zeros(nat * npts * nproj)
+    for a, (j, y, p) in enumerate(rows):
+        c = len(j)
+        jx[a * npts:a * npts + c] = j
+        y1[a * npts * 6:(a * npts + c) * 6] = y.reshape(-1)
+        pj[a * npts * nproj:(a * npts + c) * nproj] = p.reshape(-1)
+    return ProjTable(nl, npts, jx, y1, pj, np.zeros_like(pj), np.zeros(nat * nproj, np.int32), nproj)
+
+
+def cdse_dot(radius_ang: float, d: float = 0.5, ke_max: float = 20.0, spinor: bool = True, so_par: float = 0.01,
+             grid_n=(0, 0, 0)) -> Dot:
+    types, coords = zincblende_dot(radius_ang)
+    grid = reference_grid(coords, d, ke_max, grid_n)
+    pot = local_pot(grid, types, coords)
+    proj = None
+    if spinor:
+        core = [i for i, t in enumerate(types) if not t.startswith("P")]
+        tab = so_radial(d, np.sqrt(r_nlcut2(d)))
+        proj = nlc_table(grid, coords[core], np.full(len(core), so_par), tab)
+    return Dot(types, coords, grid, pot, proj, 2 if spinor else 1, spinor, spinor, False)

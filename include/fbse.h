@@ -90,6 +90,9 @@ int fbse_create(fbse_ctx **out, const fbse_grid_desc *grid, const double *pot_lo
 void fbse_destroy(fbse_ctx *ctx);
 const char *fbse_last_error(const fbse_ctx *ctx);
 int fbse_version(void);
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (all contexts), for launch accounting around a timed region. */
+long fbse_launch_count(void);
 
 /* ---- device memory helpers --------------------------------------------- */
 int fbse_alloc(fbse_ctx *ctx, void **dptr, size_t bytes);
@@ -150,6 +153,31 @@ int fbse_energy_all(fbse_ctx *ctx, const double *psitot, long n, double *ene);
  * sigma_i = ||(H - E_i) psi_i||, which equals the reference's
  * sqrt|<H^2> - <H>^2| for normalised states. */
 int fbse_ortho_diag_sigma(fbse_ctx *ctx, double *psitot, long n, long *n_kept, double *eval, double *sigma);
+
+/* ---- whole filter stage with host buffers ----------------------------------
+ * run_filter_cycles + mod_ortho + mod_diag + mod_sigma + mod_output's state
+ * selection (filter_mpi/filter.c:5-183, mod_ortho.c:3-94, mod_diag.c:324-449,
+ * mod_sigma.c:6-63, mod_output.c:5-162) in one call on HOST buffers:
+ * psi0_host [nstart] psitot states in; eval_host / sigma_host (nstart*m
+ * doubles each) and psi_host ([nstart*m] psitot states, may be NULL) out, in
+ * ascending eigenvalue order.  sigma_cut <= 0 keeps every state
+ * (getAllStates = 1); otherwise only states with sigma_E <= sigma_cut are
+ * returned (getAllStates = 0).  *n_out receives the number returned. */
+int fbse_filter_job(fbse_ctx *ctx, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
+                    const double *psi0_host, long nstart, double sigma_cut, long *n_out, double *eval_host,
+                    double *sigma_host, double *psi_host);
+
+/* ---- setup on the GPU -----------------------------------------------------
+ * build_local_pot (filter_mpi/init.c:481-703) for short-ranged tables
+ * (no strain, no cubic/ortho interpolation, no LSD, no long range):
+ * pot[jxyz] = sum_a v_{atype[a]}(|r - R_a|) with interpolate()'s linear rule
+ * (filter_mpi/interpolate.c:5-49).  gx/gy/gz: grid coordinates (host, nx/ny/nz
+ * each); coords: [natoms][3] (host); tables: type t occupies rows
+ * [tab_off[t], tab_off[t] + tab_len[t]) of tab_r / tab_v (host).  pot: host,
+ * ngrid doubles.  Uses the current CUDA device; no context needed. */
+int fbse_build_local_pot(long nx, long ny, long nz, const double *gx, const double *gy, const double *gz,
+                         long natoms, const double *coords, const int *atype, int ntypes, const double *tab_r,
+                         const double *tab_v, const long *tab_off, const long *tab_len, double *pot);
 
 /* ---- host-side helpers (no device work) --------------------------------- */
 

@@ -1,0 +1,105 @@
+"""End-to-end pins against the reference's own example runs (golden eval.dat).
+
+The whole filter path runs on the GPU in FP64 -- spectrum range, Newton
+coefficients, random starts, Newton filter, orthogonalisation, subspace
+diagonalisation, sigma_E -- on the reference's example inputs (conf.par,
+pot*.par, SO_*.par, input.par).  The reference's starts were clock-seeded,
+so the filtered subspaces differ; converged eigenvalues must agree."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.systems import GOLD, read_conf, read_pot
+
+pytestmark = pytest.mark.gpu
+
+
+def _targets(vbmin, vbmax, cbmin, cbmax, nvb, ncb):
+    return O.ene_targets(vbmin, vbmax, cbmin, cbmax, nvb, ncb)
+
+
+def _run(fbse, cuda, grid, pot, targets, ncheby, nstart, nspin, cplx, so=False, nl=False, proj=None, seed=-31415,
+         precision=0):
+    import torch
+    ctx = fbse.Context(grid, pot, nspin=nspin, is_complex=cplx, so=so, nl=nl, proj=proj, precision=precision)
+    e0, e1, it = ctx.energy_range()
+    emin = e0 - 0.2 * abs(e0)  # energy.c:360-363 (SO or no projectors)
+    emax = e1 * 1.2
+    de = emax - emin
+    zn, _ = fbse.samp_points(ncheby)
+    an = fbse.newton_coeff(zn, targets, emin, de, O.filter_dt(ncheby, de))
+    starts, _, _ = fbse.init_filter_states(nstart, grid.ngrid, nspin, cplx, grid.dv, seed)
+    filt = ctx.newton_filter(zn, an, emin, de, torch.tensor(starts, device=cuda))
+    m = len(targets)
+    psitot = filt.reshape(nstart * m, -1)
+    nk, ev, sg = ctx.ortho_diag_sigma(psitot)
+    return (emin, emax), ev, sg
+
+
+def _match(ref, ev, sg, ref_sig, my_sig, tol):
+    r = ref[ref[:, 2] < ref_sig]
+    mine = ev[sg < my_sig]
+    d = np.array([np.min(np.abs(mine - e)) if len(mine) else np.inf for e in r[:, 1]])
+    return r, d
+
+
+def test_cdse22_real_matches_reference_eval(fbse, cuda):
+    """2.2 nm CdSe, real, 57 x 52 x 45 at 0.8 bohr, 16 starts x 16 targets, nCheby 2048
+    (filter_mpi/EXAMPLES/2.2nm_CdSe/filter: input.par, eval.dat)."""
+    atyp, xyz = read_conf(os.path.join(GOLD, "cdse22", "conf.par"))
+    types = sorted(set(atyp), key=atyp.index)
+    # the grid of that run (localPot.cube header); its version used box = n d on odd axes
+    g = O.Grid(57, 52, 45, 0.8, 0.8, 0.8, -22.8, -20.8, -18.0, 10.0, box_n=True)
+    tabs = [read_pot(os.path.join(GOLD, "cdse22", f"pot{t}.par")) for t in types]
+    pot = O.local_pot(g, xyz, np.array([types.index(a) for a in atyp]), tabs)
+    targets = _targets(-0.31, -0.24, -0.15, -0.06, 10, 6)
+    (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 1, False)
+    # run.dat:140 of the reference run: Emin = -1.13271, Emax = 12.3281
+    assert abs(emin - (-1.13271)) < 2e-4 and abs(emax - 12.3281) < 2e-3
+    ref = np.loadtxt(os.path.join(GOLD, "cdse22", "eval.dat"))
+    r, d = _match(ref, ev, sg, 1e-5, 1e-4, 1e-5)
+    print(f"\n[cdse22] ours: {len(ev)} states, {np.sum(sg < 1e-4)} with sigma<1e-4; reference converged "
+          f"(sigma<1e-5): {len(r)}; matched within 1e-5: {np.sum(d < 1e-5)}; max |dE| of matched "
+          f"{np.max(d[d < 1e-5]) if np.any(d < 1e-5) else np.nan:.2e}")
+    assert np.mean(d < 1e-5) >= 0.8
+
+
+def _so_params(path):
+    vals = [float(l.split()[0]) for l in open(path).read().splitlines() if l.strip()]
+    return vals[0], vals[1], vals[2]
+
+
+def test_cspbi3_spinor_so_nl_matches_reference_eval(fbse, cuda):
+    """1x1x1 CsPbI3, spinor with spin-orbit and nonlocal projectors, 44^3 at 0.5 bohr
+    (filter_mpi/EXAMPLES/1x1x1_CsPbI3/filter: input.par, SO_*.par, reference_output/eval.dat)."""
+    d = os.path.join(GOLD, "cspbi3")
+    atyp, xyz = read_conf(os.path.join(d, "conf.par"))
+    types = sorted(set(atyp), key=atyp.index)
+    g = O.Grid(44, 44, 44, 0.5, 0.5, 0.5, -11.0, -11.0, -11.0, 20.0)
+    tabs = [read_pot(os.path.join(d, f"pot{t}.par")) for t in types]
+    pot = O.local_pot(g, xyz, np.array([types.index(a) for a in atyp]), tabs)
+    rc = np.sqrt(O.r_nlcut2(g.dx))
+    so_tab = O.so_radial(g.dx, rc)
+    params = {t: _so_params(os.path.join(d, f"SO_{t}.par")) for t in types}
+    cache = {}
+    nl_tabs, sgns = [], []
+    for a in atyp:
+        lam = params[a][1:]
+        if lam not in cache:
+            cache[lam] = O.nl_radial(g.dx, rc, *lam)
+        nl_tabs.append(cache[lam][0])
+        sgns.append(cache[lam][1])
+    proj = O.nlc_table(g, xyz, np.array([params[a][0] for a in atyp]), so_tab, np.array(nl_tabs), np.array(sgns))
+    assert int(proj.npts) == 2325  # n_NL_gridpts in the reference run's run.dat
+    targets = _targets(-0.50, -0.20, -0.167, -0.10, 10, 6)
+    (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 2, True, so=True, nl=True, proj=proj)
+    # run.dat:160 of the reference run: Emin = -0.756627, Emax = 25.2627
+    assert abs(emin - (-0.756627)) < 2e-4 and abs(emax - 25.2627) < 5e-3
+    ref = np.loadtxt(os.path.join(d, "eval.dat"))
+    r, dd = _match(ref, ev, sg, 1e-6, 1e-4, 1e-5)
+    print(f"\n[cspbi3] ours: {len(ev)} states, {np.sum(sg < 1e-4)} with sigma<1e-4; reference converged: {len(r)};"
+          f" matched within 1e-5: {np.sum(dd < 1e-5)}; max |dE| of matched "
+          f"{np.max(dd[dd < 1e-5]) if np.any(dd < 1e-5) else np.nan:.2e}")
+    assert np.mean(dd < 1e-5) >= 0.8
