@@ -4,21 +4,23 @@
 // fftw_plan_dft_3d(nz, ny, nx) forward transform, the ksqr multiply and the
 // unnormalised backward transform (plans made in filter_mpi/aux.c:259-270).
 //
-// Design: every axis is transformed by a self-sorting Stockham FFT held in
-// shared memory.  The grid sizes the reference's auto-grid produces are
-// arbitrary (e.g. 57 x 52 x 45 = 3*19 x 4*13 x 9*5), so each axis is factored
-// into radix-4/2/3 stages with hand-written butterflies plus generic odd-prime
-// stages; twiddles and butterfly roots come from one table of n roots
-// e^{-2 pi i t/n} per axis, computed on the host in extended precision.
-//   pass 1  x lines (contiguous): forward
-//   pass 2  y lines, tiles of TX consecutive x columns: forward
-//   pass 3  z lines, tiles of TX consecutive x columns: forward, multiply by
+// Every axis is transformed by a self-sorting Stockham FFT in shared memory.
+// The grid sizes the reference's auto-grid produces are arbitrary (e.g.
+// 57 x 52 x 45 = 3*19 x 4*13 x 9*5), so each axis is factored into radix-4/2/3
+// stages with hand-written butterflies plus generic odd-prime stages;
+// twiddles and butterfly roots come from one table of n roots e^{-2 pi i t/n}
+// per axis, computed on the host in extended precision.
+//
+// Plane path (an xy plane fits in shared memory, the usual case in FP32):
+//   pass 1  per (block, z): load the plane, x then y forward, store
+//   pass 2  z lines in tiles of 16 x-columns: forward, multiply by
 //           min(kx^2 + ky^2 + kz^2 terms, KE_max)/N computed from the indices
 //           exactly as filter_mpi/init.c:318-351 builds ksqr, inverse
-//   pass 4  y lines: inverse
-//   pass 5  x lines: inverse, fused epilogue out = a (T psi + V psi) + b psi
-// so the k^2 table costs no HBM traffic and the local potential and the
-// Newton scale-and-shift ride on the last pass.
+//   pass 3  per (block, z): y then x inverse, fused epilogue
+//           out = a (T psi + V psi) + b psi
+// Line path (larger planes, FP64): x, y, z-fused, y, x passes.
+// Blocks are processed in chunks sized so that a chunk's scratch stays in L2
+// between the passes.
 #include <cmath>
 
 #include "fbse_internal.cuh"
@@ -89,15 +91,21 @@ template <> const C<float> *roots<float>(const AxisPlan &p) { return p.tw32; }
 template <> const C<double> *roots<double>(const AxisPlan &p) { return p.tw64; }
 
 // ---------------------------------------------------------------------------
-// one Stockham stage in shared memory
-//   COLS = false: lines are contiguous (element stride 1, line stride n) and
-//                 consecutive threads walk along a line;
-//   COLS = true : element i of line c sits at i*L + c, consecutive threads
-//                 walk across lines (conflict-free for column tiles).
+// A view of L lines of length n in shared memory: element i of line c sits at
+// base[c * ls + i * es].
 // ---------------------------------------------------------------------------
-template <typename T, bool COLS>
-__device__ __forceinline__ void stage(C<T> *__restrict__ src, C<T> *__restrict__ dst, const C<T> *__restrict__ tw,
-                                      int n, int L, int p, int Ns, bool inv)
+template <typename T> struct Lines {
+  C<T> *base;
+  int es, ls;
+  __device__ __forceinline__ C<T> &at(int c, int i) const { return base[c * ls + i * es]; }
+};
+
+// One Stockham stage src -> dst over L lines.  ACROSS: consecutive threads
+// take consecutive lines (column tiles), otherwise consecutive butterflies of
+// one line.
+template <typename T, bool ACROSS>
+__device__ __forceinline__ void stage(Lines<T> src, Lines<T> dst, const C<T> *__restrict__ tw, int n, int L, int p,
+                                      int Ns, bool inv)
 {
   const int nb = n / p;
   const int total = nb * L;
@@ -106,78 +114,155 @@ __device__ __forceinline__ void stage(C<T> *__restrict__ src, C<T> *__restrict__
   const T sg = inv ? T(1) : T(-1);
   for (int w = threadIdx.x; w < total; w += blockDim.x) {
     int c, j;
-    if (COLS) { c = w % L; j = w / L; }
+    if (ACROSS) { c = w % L; j = w / L; }
     else { c = w / nb; j = w - c * nb; }
     const int k = j % Ns;
-    const int obase = (j / Ns) * Ns * p + k;
-    auto IN = [&](int i) -> C<T> & { return COLS ? src[i * L + c] : src[c * n + i]; };
-    auto OUT = [&](int i) -> C<T> & { return COLS ? dst[i * L + c] : dst[c * n + i]; };
+    const int ob = (j / Ns) * Ns * p + k;
     auto W = [&](int t) -> C<T> { C<T> r = tw[t]; if (inv) r.y = -r.y; return r; };
-    if (p == 2) {
-      C<T> v0 = IN(j), v1 = cmul<T>(IN(j + nb), W(k * twstep));
-      OUT(obase) = cadd<T>(v0, v1);
-      OUT(obase + Ns) = csub<T>(v0, v1);
-    } else if (p == 4) {
-      C<T> v0 = IN(j);
-      C<T> v1 = cmul<T>(IN(j + nb), W(k * twstep));
-      C<T> v2 = cmul<T>(IN(j + 2 * nb), W(2 * k * twstep));
-      C<T> v3 = cmul<T>(IN(j + 3 * nb), W(3 * k * twstep));
+    if (p == 4) {
+      C<T> v0 = src.at(c, j);
+      C<T> v1 = cmul<T>(src.at(c, j + nb), W(k * twstep));
+      C<T> v2 = cmul<T>(src.at(c, j + 2 * nb), W(2 * k * twstep));
+      C<T> v3 = cmul<T>(src.at(c, j + 3 * nb), W(3 * k * twstep));
       C<T> a = cadd<T>(v0, v2), b = csub<T>(v0, v2), cc = cadd<T>(v1, v3), d = csub<T>(v1, v3);
-      // s*i*d with s = -1 forward, +1 inverse
-      C<T> id = mk<T>(-sg * d.y, sg * d.x);
-      OUT(obase) = cadd<T>(a, cc);
-      OUT(obase + Ns) = cadd<T>(b, id);
-      OUT(obase + 2 * Ns) = csub<T>(a, cc);
-      OUT(obase + 3 * Ns) = csub<T>(b, id);
+      C<T> id = mk<T>(-sg * d.y, sg * d.x);  // s*i*d, s = -1 forward, +1 inverse
+      dst.at(c, ob) = cadd<T>(a, cc);
+      dst.at(c, ob + Ns) = cadd<T>(b, id);
+      dst.at(c, ob + 2 * Ns) = csub<T>(a, cc);
+      dst.at(c, ob + 3 * Ns) = csub<T>(b, id);
+    } else if (p == 2) {
+      C<T> v0 = src.at(c, j), v1 = cmul<T>(src.at(c, j + nb), W(k * twstep));
+      dst.at(c, ob) = cadd<T>(v0, v1);
+      dst.at(c, ob + Ns) = csub<T>(v0, v1);
     } else if (p == 3) {
-      C<T> v0 = IN(j);
-      C<T> v1 = cmul<T>(IN(j + nb), W(k * twstep));
-      C<T> v2 = cmul<T>(IN(j + 2 * nb), W(2 * k * twstep));
+      C<T> v0 = src.at(c, j);
+      C<T> v1 = cmul<T>(src.at(c, j + nb), W(k * twstep));
+      C<T> v2 = cmul<T>(src.at(c, j + 2 * nb), W(2 * k * twstep));
       const T h = T(0.86602540378443864676372317075293618);
       C<T> s12 = cadd<T>(v1, v2), d12 = csub<T>(v1, v2);
       C<T> t = mk<T>(v0.x - T(0.5) * s12.x, v0.y - T(0.5) * s12.y);
-      // u = s*(sqrt(3)/2)*(v1 - v2); i*u
-      C<T> iu = mk<T>(-sg * h * d12.y, sg * h * d12.x);
-      OUT(obase) = cadd<T>(v0, s12);
-      OUT(obase + Ns) = cadd<T>(t, iu);
-      OUT(obase + 2 * Ns) = csub<T>(t, iu);
+      C<T> iu = mk<T>(-sg * h * d12.y, sg * h * d12.x);  // i * s*(sqrt(3)/2)*(v1 - v2)
+      dst.at(c, ob) = cadd<T>(v0, s12);
+      dst.at(c, ob + Ns) = cadd<T>(t, iu);
+      dst.at(c, ob + 2 * Ns) = csub<T>(t, iu);
     } else {
       // generic radix: twiddle this butterfly's inputs in place (each input
       // element of a stage is read by exactly one butterfly), then a direct
       // length-p DFT with roots from the table.
-      for (int r = 1; r < p; r++) IN(j + r * nb) = cmul<T>(IN(j + r * nb), W(r * k * twstep));
+      for (int r = 1; r < p; r++) src.at(c, j + r * nb) = cmul<T>(src.at(c, j + r * nb), W(r * k * twstep));
       for (int q = 0; q < p; q++) {
-        C<T> acc = IN(j);
+        C<T> acc = src.at(c, j);
         int e = 0;
         for (int r = 1; r < p; r++) {
           e += q;
           if (e >= p) e -= p;
-          acc = cadd<T>(acc, cmul<T>(IN(j + r * nb), W(e * rstep)));
+          acc = cadd<T>(acc, cmul<T>(src.at(c, j + r * nb), W(e * rstep)));
         }
-        OUT(obase + q * Ns) = acc;
+        dst.at(c, ob + q * Ns) = acc;
       }
     }
   }
 }
 
-// full transform of L lines held in a; returns the buffer holding the result
-template <typename T, bool COLS>
-__device__ C<T> *fft_lines(C<T> *a, C<T> *b, const C<T> *tw, const Stages &st, int L, bool inv)
+// transform L lines held in a using b as the other Stockham buffer; returns
+// true when the result ended in b (odd number of stages)
+template <typename T, bool ACROSS>
+__device__ bool fft_lines(Lines<T> a, Lines<T> b, const C<T> *tw, const Stages &st, int L, bool inv)
 {
   int Ns = 1;
+  bool inb = false;
   for (int s = 0; s < st.nst; s++) {
-    stage<T, COLS>(a, b, tw, st.n, L, st.radix[s], Ns, inv);
+    if (!inb) stage<T, ACROSS>(a, b, tw, st.n, L, st.radix[s], Ns, inv);
+    else stage<T, ACROSS>(b, a, tw, st.n, L, st.radix[s], Ns, inv);
     __syncthreads();
     Ns *= st.radix[s];
-    C<T> *t = a;
-    a = b;
-    b = t;
+    inb = !inb;
   }
-  return a;
+  return inb;
 }
 
 // ---------------------------------------------------------------------------
-// x pass: L contiguous lines per CTA.  EPI = 0: store; EPI = 1: fused
+// plane pass: one (block, z) plane of ny x nx in shared memory.
+//   MODE 0: forward x then y, store to out
+//   MODE 1: inverse y then x, epilogue out = a (kin + V phi) + b phi
+// The rows / columns are transformed G at a time with a small scratch as the
+// second Stockham buffer, so the plane itself needs no second copy.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void plane_rows(C<T> *P, C<T> *S, const C<T> *tw, const Stages &st, int nx, int ny, int G, bool inv)
+{
+  for (int r0 = 0; r0 < ny; r0 += G) {
+    const int g = min(G, ny - r0);
+    Lines<T> a{P + r0 * nx, 1, nx}, b{S, 1, nx};
+    const bool inb = fft_lines<T, false>(a, b, tw, st, g, inv);
+    if (inb) {
+      for (int t = threadIdx.x; t < g * nx; t += blockDim.x) P[r0 * nx + t] = S[t];
+      __syncthreads();
+    }
+  }
+}
+
+template <typename T>
+__device__ void plane_cols(C<T> *P, C<T> *S, const C<T> *tw, const Stages &st, int nx, int ny, int G, bool inv)
+{
+  for (int c0 = 0; c0 < nx; c0 += G) {
+    const int g = min(G, nx - c0);
+    Lines<T> a{P + c0, nx, 1}, b{S, g, 1};
+    const bool inb = fft_lines<T, true>(a, b, tw, st, g, inv);
+    if (inb) {
+      for (int t = threadIdx.x; t < g * ny; t += blockDim.x) {
+        const int cc = t % g, i = t / g;
+        P[i * nx + c0 + cc] = S[i * g + cc];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(512) k_fft_plane(const C<T> *__restrict__ in, C<T> *__restrict__ out, Stages sx,
+                                                   Stages sy, const C<T> *__restrict__ twxg,
+                                                   const C<T> *__restrict__ twyg, int G,
+                                                   const C<T> *__restrict__ phi, const T *__restrict__ pot,
+                                                   long ngrid, T ca, T cb)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = sx.n, ny = sy.n;
+  const int npl = nx * ny;
+  C<T> *twx = reinterpret_cast<C<T> *>(smem_raw);
+  C<T> *twy = twx + nx;
+  C<T> *P = twy + ny;
+  C<T> *S = P + npl;
+  for (int t = threadIdx.x; t < nx; t += blockDim.x) twx[t] = twxg[t];
+  for (int t = threadIdx.x; t < ny; t += blockDim.x) twy[t] = twyg[t];
+  const long base = (long)blockIdx.x * npl;
+  for (int t = threadIdx.x; t < npl; t += blockDim.x) P[t] = in[base + t];
+  __syncthreads();
+  if (MODE == 0) {
+    plane_rows<T>(P, S, twx, sx, nx, ny, G, false);
+    plane_cols<T>(P, S, twy, sy, nx, ny, G, false);
+    for (int t = threadIdx.x; t < npl; t += blockDim.x) out[base + t] = P[t];
+  } else {
+    plane_cols<T>(P, S, twy, sy, nx, ny, G, true);
+    plane_rows<T>(P, S, twx, sx, nx, ny, G, true);
+    for (int t = threadIdx.x; t < npl; t += blockDim.x) {
+      const long g = base + t;
+      C<T> v = P[t];
+      const C<T> ph = phi[g];
+      if (pot) {
+        const T V = pot[g % ngrid];
+        v.x += V * ph.x;
+        v.y += V * ph.y;
+      }
+      v.x = ca * v.x + cb * ph.x;
+      v.y = ca * v.y + cb * ph.y;
+      out[g] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x line pass (line path): L contiguous lines per CTA.  EPI = 1: fused
 // out = a (kin + V phi) + b phi with V indexed by the spatial point.
 // ---------------------------------------------------------------------------
 template <typename T, int EPI>
@@ -197,7 +282,8 @@ __global__ void __launch_bounds__(256) k_fft_x(const C<T> *__restrict__ in, C<T>
   const long off = line0 * n;
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) A[t] = in[off + t];
   __syncthreads();
-  C<T> *r = fft_lines<T, false>(A, B, tw, st, nl, inv);
+  const bool inb = fft_lines<T, false>(Lines<T>{A, 1, n}, Lines<T>{B, 1, n}, tw, st, nl, inv);
+  const C<T> *r = inb ? B : A;
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     C<T> v = r[t];
     if (EPI == 1) {
@@ -224,7 +310,6 @@ __global__ void __launch_bounds__(256) k_fft_x(const C<T> *__restrict__ in, C<T>
 struct KinArgs {
   const double *k2x, *k2y, *k2z;
   double kemax;
-  int nx, ny;
 };
 
 template <typename T, bool KMUL>
@@ -248,8 +333,10 @@ __global__ void __launch_bounds__(256) k_fft_cols(C<T> *__restrict__ data, Stage
     A[i * L + cc] = data[base + (long)i * es + cc];
   }
   __syncthreads();
-  C<T> *r = fft_lines<T, true>(A, B, tw, st, L, KMUL ? false : inv);
+  Lines<T> la{A, L, 1}, lb{B, L, 1};
+  bool inb = fft_lines<T, true>(la, lb, tw, st, L, KMUL ? false : inv);
   if (KMUL) {
+    C<T> *r = inb ? B : A;
     const int jy = (int)(o % cnt);
     const double ky = ka.k2y[jy];
     for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
@@ -259,9 +346,10 @@ __global__ void __launch_bounds__(256) k_fft_cols(C<T> *__restrict__ data, Stage
       r[t] = cscale<T>(r[t], (T)kk);
     }
     __syncthreads();
-    C<T> *other = (r == A) ? B : A;
-    r = fft_lines<T, true>(r, other, tw, st, L, true);
+    const bool inb2 = inb ? fft_lines<T, true>(lb, la, tw, st, L, true) : fft_lines<T, true>(la, lb, tw, st, L, true);
+    inb = inb ? !inb2 : inb2;
   }
+  const C<T> *r = inb ? B : A;
   for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
     const int cc = t % L, i = t / L;
     data[base + (long)i * es + cc] = r[i * L + cc];
@@ -273,6 +361,16 @@ template <> const float *pot_of<float>(fbse_ctx *c) { return c->pot32; }
 template <> const double *pot_of<double>(fbse_ctx *c) { return c->pot64; }
 
 static int cols_tile(int nx) { return nx < 16 ? nx : 16; }
+static int max_smem()
+{
+  static int v = -1;
+  if (v < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) v = 48 * 1024;
+  }
+  return v;
+}
 
 template <typename T>
 static int launch_x(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, bool inv, int epi, const C<T> *phi,
@@ -322,7 +420,7 @@ static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, b
   }
   const size_t smem = (size_t)(n + 2L * TX * n) * sizeof(C<T>);
   const long grid = nouter * nxt;
-  KinArgs ka{c->k2x, c->k2y, c->k2z, c->kemax_scaled, (int)c->nx, (int)c->ny};
+  KinArgs ka{c->k2x, c->k2y, c->k2z, c->kemax_scaled};
   Stages st = stages_of(p);
   if (kmul) {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_cols<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -337,15 +435,71 @@ static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, b
   return FBSE_OK;
 }
 
+// rows / columns per scratch group and the plane kernel's shared memory
+template <typename T> static size_t plane_smem(fbse_ctx *c, int *G)
+{
+  const int nx = (int)c->nx, ny = (int)c->ny;
+  *G = 16;
+  const int mx = nx > ny ? nx : ny;
+  return (size_t)(nx + ny + (long)nx * ny + (long)(*G) * mx) * sizeof(C<T>);
+}
+
+template <typename T>
+static int launch_plane(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int mode, const C<T> *phi, const T *pot,
+                        T ca, T cb)
+{
+  int G;
+  const size_t smem = plane_smem<T>(c, &G);
+  const long grid = nblk * c->nz;
+  Stages sx = stages_of(c->ax[0]), sy = stages_of(c->ax[1]);
+  if (mode == 0) {
+    FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_plane<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_fft_plane<T, 0><<<grid, 512, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]), G,
+                                                       nullptr, nullptr, c->ngrid, T(1), T(0));
+  } else {
+    FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_plane<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_fft_plane<T, 1><<<grid, 512, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]), G,
+                                                       phi, pot, c->ngrid, ca, cb);
+  }
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+// blocks per chunk: keep a chunk's scratch (and its input) within L2
+template <typename T> static long chunk_blocks(fbse_ctx *c, long nblk)
+{
+  const char *e = getenv("FBSE_FFT_CHUNK_BLOCKS");
+  if (e && atol(e) > 0) return atol(e) < nblk ? atol(e) : nblk;
+  const double blk = (double)c->ngrid * sizeof(C<T>);
+  long cb = (long)(40.0e6 / blk);
+  if (cb < 1) cb = 1;
+  return cb < nblk ? cb : nblk;
+}
+
 template <typename T>
 int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b, int with_v)
 {
-  int rc;
-  if ((rc = launch_x<T>(c, in, work, nblk, false, 0, nullptr, nullptr, T(1), T(0)))) return rc;
-  if ((rc = launch_cols<T>(c, work, nblk, 1, false, false))) return rc;
-  if ((rc = launch_cols<T>(c, work, nblk, 2, false, true))) return rc;
-  if ((rc = launch_cols<T>(c, work, nblk, 1, true, false))) return rc;
-  return launch_x<T>(c, work, out, nblk, true, 1, in, with_v ? pot_of<T>(c) : nullptr, (T)a, (T)b);
+  int rc, G;
+  const bool plane = plane_smem<T>(c, &G) <= (size_t)max_smem() && getenv("FBSE_FFT_LINES") == nullptr;
+  const T *pot = with_v ? pot_of<T>(c) : nullptr;
+  const long cb = chunk_blocks<T>(c, nblk);
+  for (long b0 = 0; b0 < nblk; b0 += cb) {
+    const long nb = (nblk - b0 < cb) ? nblk - b0 : cb;
+    const C<T> *ci = in + b0 * c->ngrid;
+    C<T> *co = out + b0 * c->ngrid;
+    if (plane) {
+      if ((rc = launch_plane<T>(c, ci, work, nb, 0, nullptr, nullptr, T(1), T(0)))) return rc;
+      if ((rc = launch_cols<T>(c, work, nb, 2, false, true))) return rc;
+      if ((rc = launch_plane<T>(c, work, co, nb, 1, ci, pot, (T)a, (T)b))) return rc;
+    } else {
+      if ((rc = launch_x<T>(c, ci, work, nb, false, 0, nullptr, nullptr, T(1), T(0)))) return rc;
+      if ((rc = launch_cols<T>(c, work, nb, 1, false, false))) return rc;
+      if ((rc = launch_cols<T>(c, work, nb, 2, false, true))) return rc;
+      if ((rc = launch_cols<T>(c, work, nb, 1, true, false))) return rc;
+      if ((rc = launch_x<T>(c, work, co, nb, true, 1, ci, pot, (T)a, (T)b))) return rc;
+    }
+  }
+  return FBSE_OK;
 }
 
 template int kinetic_apply<float>(fbse_ctx *, const C<float> *, C<float> *, C<float> *, long, double, double, int);
