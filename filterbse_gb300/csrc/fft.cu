@@ -333,15 +333,18 @@ __global__ void __launch_bounds__(256) k_fft_plane(const C<T> *__restrict__ in, 
   for (int t = threadIdx.x; t < nx; t += blockDim.x) twx[t] = twxg[t];
   for (int t = threadIdx.x; t < ny; t += blockDim.x) twy[t] = twyg[t];
   const long base = (long)blockIdx.x * npl;
+#pragma unroll 8
   for (int t = threadIdx.x; t < npl; t += blockDim.x) P[(t / nx) * nxp + t % nx] = in[base + t];
   __syncthreads();
   if (MODE == 0) {
     fft_lines<T>(P, 1, nxp, ny, sx, twx, false, nullptr);  // rows
     fft_lines<T>(P, nxp, 1, nx, sy, twy, false, nullptr);  // columns
+#pragma unroll 8
     for (int t = threadIdx.x; t < npl; t += blockDim.x) out[base + t] = P[(t / nx) * nxp + t % nx];
   } else {
     fft_lines<T>(P, nxp, 1, nx, sy, twy, true, nullptr);
     fft_lines<T>(P, 1, nxp, ny, sx, twx, true, nullptr);
+#pragma unroll 8
     for (int t = threadIdx.x; t < npl; t += blockDim.x) {
       const long g = base + t;
       C<T> v = P[(t / nx) * nxp + t % nx];
@@ -377,9 +380,11 @@ __global__ void __launch_bounds__(256) k_fft_x(const C<T> *__restrict__ in, C<T>
   const long line0 = (long)blockIdx.x * L;
   const int nl = (int)min((long)L, nlines - line0);
   const long off = line0 * n;
+#pragma unroll 8
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) A[(t / n) * np + t % n] = in[off + t];
   __syncthreads();
   fft_lines<T>(A, 1, np, nl, st, tw, inv, st.big ? S : nullptr);
+#pragma unroll 8
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     C<T> v = A[(t / n) * np + t % n];
     if (EPI == 1) {
@@ -424,6 +429,7 @@ __global__ void __launch_bounds__(256) k_fft_cols(C<T> *__restrict__ data, Stage
   const int x0 = xt * TX;
   const int L = min(TX, nxc - x0);
   const long base = (o / cnt) * s1 + (o % cnt) * s2 + x0;
+#pragma unroll 8
   for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
     const int cc = t % L, i = t / L;
     A[i * L + cc] = data[base + (long)i * es + cc];
@@ -442,6 +448,7 @@ __global__ void __launch_bounds__(256) k_fft_cols(C<T> *__restrict__ data, Stage
     __syncthreads();
     fft_lines<T>(A, L, 1, L, st, tw, true, st.big ? S : nullptr);
   }
+#pragma unroll 8
   for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
     const int cc = t % L, i = t / L;
     data[base + (long)i * es + cc] = A[i * L + cc];
