@@ -28,6 +28,7 @@ EXPORTED = [
     "fbse_newton_filter", "fbse_energy_range", "fbse_normalize_all", "fbse_energy_all",
     "fbse_ortho_diag_sigma", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
     "fbse_init_filter_states", "fbse_launch_count", "fbse_filter_job", "fbse_build_local_pot",
+    "fbse_bse_potentials", "fbse_bse_kernel", "fbse_bse_solve", "fbse_bse_dipoles", "fbse_bse_optical",
 ]
 
 
@@ -95,6 +96,12 @@ def load() -> ctypes.CDLL:
     L.fbse_launch_count.restype = ctypes.c_long
     L.fbse_filter_job.argtypes = [_VP, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_double, ctypes.c_double, _D,
                                   ctypes.c_long, ctypes.c_double, ctypes.POINTER(ctypes.c_long), _D, _D, _D]
+    L.fbse_bse_potentials.argtypes = [_VP, _D, _D, _D] + [ctypes.c_double] * 6 + [_VP, _VP]
+    L.fbse_bse_kernel.argtypes = [_VP, _VP, ctypes.c_long, ctypes.c_long, ctypes.c_long, _VP, _VP, _VP, _VP]
+    L.fbse_bse_solve.argtypes = [_VP, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_long, _VP, _VP, _D,
+                                 _VP, _D, _D, _D, _D]
+    L.fbse_bse_dipoles.argtypes = [_VP, _VP, _D, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D]
+    L.fbse_bse_optical.argtypes = [_VP, _VP, _D, ctypes.c_long, ctypes.c_long, _D]
     _lib = L
     return L
 
@@ -307,3 +314,62 @@ class Context:
         self._chk(self._L.fbse_ortho_diag_sigma(self._h, self._ptr(psitot), n, ctypes.byref(nk), _dp(ev), _dp(sg)))
         k = nk.value
         return k, ev[:k].copy(), sg[:k].copy()
+
+    # -- Bethe-Salpeter stage -----------------------------------------------------
+    def bse_potentials(self, gx, gy, gz, xmin, ymin, zmin, eps=(6.0, 6.0, 6.0)):
+        """init_elec_hole_kernel: returns (pot_bare, pot_screened), [ngrid]
+        complex128 CUDA tensors."""
+        import torch
+        gx, gy, gz = (np.ascontiguousarray(a, np.float64) for a in (gx, gy, gz))
+        bare = torch.empty(self.ngrid, dtype=torch.complex128, device="cuda")
+        scr = torch.empty_like(bare)
+        self._torch_sync()
+        self._chk(self._L.fbse_bse_potentials(self._h, _dp(gx), _dp(gy), _dp(gz), xmin, ymin, zmin, eps[0], eps[1],
+                                              eps[2], self._ptr(bare), self._ptr(scr)))
+        return bare, scr
+
+    def bse_kernel(self, psi_qp, n_h, n_e, lumo_idx, pot_bare, pot_screened):
+        """calc_eh_kernel_cplx: psi_qp [n_qp, nspin*ngrid] complex128 CUDA;
+        returns (direct, exchange) [n_xton, n_xton] complex128, lower triangles."""
+        import torch
+        n = n_h * n_e
+        d = torch.zeros((n, n), dtype=torch.complex128, device=psi_qp.device)
+        x = torch.zeros_like(d)
+        self._torch_sync()
+        self._chk(self._L.fbse_bse_kernel(self._h, self._ptr(psi_qp), n_h, n_e, lumo_idx, self._ptr(pot_bare),
+                                          self._ptr(pot_screened), self._ptr(d), self._ptr(x)))
+        return d, x
+
+    def bse_solve(self, eval_qp, n_h, n_e, lumo_idx, direct, exchange):
+        """build_BSE_mat + bethe_salpeter: returns (xton_ene, coeff, <H>, <Kd>,
+        <Kx>, <h0>); coeff [n_xton, n_xton] complex128 CUDA, column j = exciton j.
+        direct/exchange are completed to Hermitian matrices in place."""
+        import torch
+        ev = np.ascontiguousarray(eval_qp, np.float64)
+        n = n_h * n_e
+        coeff = torch.empty((n, n), dtype=torch.complex128, device=direct.device)
+        e, h, dd, xx, h0 = (np.empty(n) for _ in range(5))
+        self._torch_sync()
+        self._chk(self._L.fbse_bse_solve(self._h, _dp(ev), len(ev), n_h, n_e, lumo_idx, self._ptr(direct),
+                                         self._ptr(exchange), _dp(e), self._ptr(coeff), _dp(h), _dp(dd), _dp(xx),
+                                         _dp(h0)))
+        return e, coeff, h, dd, xx, h0
+
+    def bse_dipoles(self, psi_qp, gx, gy, gz, n_h, n_e, lumo_idx):
+        """calc_elec_dipole: returns mu [n_h*n_e, 3] complex128 (numpy), row i*n_e+a."""
+        gx, gy, gz = (np.ascontiguousarray(a, np.float64) for a in (gx, gy, gz))
+        mu = np.empty(n_h * n_e * 3, np.complex128)
+        self._torch_sync()
+        self._chk(self._L.fbse_bse_dipoles(self._h, self._ptr(psi_qp), _dp(gx), _dp(gy), _dp(gz), n_h, n_e,
+                                           lumo_idx, _dp(mu.view(np.float64))))
+        return mu.reshape(-1, 3)
+
+    def bse_optical(self, coeff, mu_pairs, n_h, n_e):
+        """calc_optical_exc (electric part): exciton dipoles [n_xton, 3] complex128
+        and the oscillator-strength columns of OS.dat given xton energies later."""
+        mp = np.ascontiguousarray(mu_pairs, np.complex128)
+        out = np.empty(n_h * n_e * 3, np.complex128)
+        self._torch_sync()
+        self._chk(self._L.fbse_bse_optical(self._h, self._ptr(coeff), _dp(mp.reshape(-1).view(np.float64)), n_h, n_e,
+                                           _dp(out.view(np.float64))))
+        return out.reshape(-1, 3)

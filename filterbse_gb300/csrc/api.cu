@@ -203,6 +203,10 @@ int fbse_create(fbse_ctx **out, const fbse_grid_desc *grid, const double *pot_lo
   fbse_ctx *c = new fbse_ctx();
   c->precision = precision;
   int rc = create(c, grid, pot_local, proj);
+  // pageable uploads may still be in flight after cudaMemcpy returns; the
+  // context's non-blocking stream must not see them half done
+  if (rc == FBSE_OK && cudaDeviceSynchronize() != cudaSuccess)
+    rc = set_err(c, FBSE_ERR_CUDA, std::string("fbse_create: ") + cudaGetErrorString(cudaGetLastError()));
   *out = c;  // returned even on failure so fbse_last_error can explain
   return rc;
 }

@@ -120,6 +120,18 @@ extern std::atomic<long> g_launches;
 
 int ensure(fbse_ctx *c, void **p, size_t *have, size_t need);
 
+// host copies ordered on the context's (non-blocking) stream; d2h returns
+// after the data has arrived
+inline cudaError_t h2d(cudaStream_t s, void *dst, const void *src, size_t bytes)
+{
+  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+}
+inline cudaError_t d2h(cudaStream_t s, void *dst, const void *src, size_t bytes)
+{
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(s);
+}
+
 // FFT (fft.cu) ----------------------------------------------------------------
 int plan_axis(fbse_ctx *c, AxisPlan &p, int n);
 void free_axis(AxisPlan &p);
@@ -127,6 +139,11 @@ void free_axis(AxisPlan &p);
 // for nblk 3D blocks (states x spins).  work is a scratch of nblk*ngrid complex.
 template <typename T>
 int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b, int with_v);
+
+// out = F^-1 (kq . F in) per 3D block (the hartree convolution); kq holds the
+// k-space multiplier including 1/N
+template <typename T>
+int conv_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, const double2 *kq);
 
 // projectors (hpsi.cu) --------------------------------------------------------
 template <typename T>

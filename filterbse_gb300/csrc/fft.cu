@@ -197,7 +197,7 @@ template <typename T, int R>
 __device__ __forceinline__ void pass_reg(C<T> *buf, int es, int ls, int n, int L, int Ns, const C<T> *__restrict__ tw,
                                       bool inv)
 {
-  constexpr int kMaxE = sizeof(T) == 4 ? 16 : 8;        // complex values per thread
+  constexpr int kMaxE = R;                              // one butterfly per thread per round
   constexpr int BMAX = (kMaxE / R) > 0 ? kMaxE / R : 1;
   const int nb = n / R;
   const int twstep = n / (Ns * R);
@@ -318,7 +318,7 @@ __device__ void fft_lines(C<T> *buf, int es, int ls, int L, const Stages &st, co
 //   MODE 1: inverse y then x, epilogue out = a (kin + V phi) + b phi
 // ---------------------------------------------------------------------------
 template <typename T, int MODE>
-__global__ void __launch_bounds__(256) k_fft_plane(const C<T> *__restrict__ in, C<T> *__restrict__ out, Stages sx,
+__global__ void __launch_bounds__(1024, 1) k_fft_plane(const C<T> *__restrict__ in, C<T> *__restrict__ out, Stages sx,
                                                    Stages sy, const C<T> *__restrict__ twxg,
                                                    const C<T> *__restrict__ twyg, const C<T> *__restrict__ phi,
                                                    const T *__restrict__ pot, long ngrid, T ca, T cb)
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256) k_fft_plane(const C<T> *__restrict__ in, 
 // EPI = 1: fused out = a (kin + V phi) + b phi.
 // ---------------------------------------------------------------------------
 template <typename T, int EPI>
-__global__ void __launch_bounds__(256) k_fft_x(const C<T> *__restrict__ in, C<T> *__restrict__ out, Stages st,
+__global__ void __launch_bounds__(256, 4) k_fft_x(const C<T> *__restrict__ in, C<T> *__restrict__ out, Stages st,
                                                const C<T> *__restrict__ twg, long nlines, int L, bool inv,
                                                const C<T> *__restrict__ phi, const T *__restrict__ pot, long ngrid,
                                                T ca, T cb)
@@ -411,10 +411,12 @@ __global__ void __launch_bounds__(256) k_fft_x(const C<T> *__restrict__ in, C<T>
 struct KinArgs {
   const double *k2x, *k2y, *k2z;
   double kemax;
+  const double2 *kq;  // when set: multiply by this complex k-space array instead
+  long nx, nxy;
 };
 
 template <typename T, bool KMUL>
-__global__ void __launch_bounds__(256) k_fft_cols(C<T> *__restrict__ data, Stages st, const C<T> *__restrict__ twg,
+__global__ void __launch_bounds__(256, 4) k_fft_cols(C<T> *__restrict__ data, Stages st, const C<T> *__restrict__ twg,
                                                   long es, int nxc, int TX, int nxt, long cnt, long s1, long s2,
                                                   bool inv, KinArgs ka)
 {
@@ -438,12 +440,21 @@ __global__ void __launch_bounds__(256) k_fft_cols(C<T> *__restrict__ data, Stage
   fft_lines<T>(A, L, 1, L, st, tw, KMUL ? false : inv, st.big ? S : nullptr);
   if (KMUL) {
     const int jy = (int)(o % cnt);
-    const double ky = ka.k2y[jy];
-    for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
-      const int cc = t % L, i = t / L;
-      double kk = ka.k2x[x0 + cc] + ky + ka.k2z[i];
-      if (kk > ka.kemax) kk = ka.kemax;
-      A[t] = cscale<T>(A[t], (T)kk);
+    if (ka.kq) {
+      // convolution: multiply by the k-space array (hartree, bse_cplx/hartree.c:19-27)
+      for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
+        const int cc = t % L, i = t / L;
+        const double2 q = ka.kq[(long)i * ka.nxy + (long)jy * ka.nx + x0 + cc];
+        A[t] = cmul<T>(A[t], mk<T>((T)q.x, (T)q.y));
+      }
+    } else {
+      const double ky = ka.k2y[jy];
+      for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
+        const int cc = t % L, i = t / L;
+        double kk = ka.k2x[x0 + cc] + ky + ka.k2z[i];
+        if (kk > ka.kemax) kk = ka.kemax;
+        A[t] = cscale<T>(A[t], (T)kk);
+      }
     }
     __syncthreads();
     fft_lines<T>(A, L, 1, L, st, tw, true, st.big ? S : nullptr);
@@ -501,7 +512,8 @@ static int launch_x(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, bool inv,
 }
 
 template <typename T>
-static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, bool kmul)
+static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, bool kmul,
+                       const double2 *kq = nullptr)
 {
   const AxisPlan &p = c->ax[axis];
   const int n = p.n;
@@ -525,7 +537,7 @@ static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, b
   const size_t smem = (size_t)(n + (st.big ? 2L : 1L) * TX * n) * sizeof(C<T>);
   if (smem > (size_t)max_smem()) return set_err(c, FBSE_ERR_UNSUPPORTED, "FFT axis too long for shared memory");
   const long grid = nouter * nxt;
-  KinArgs ka{c->k2x, c->k2y, c->k2z, c->kemax_scaled};
+  KinArgs ka{c->k2x, c->k2y, c->k2z, c->kemax_scaled, kq, c->nx, c->nx * c->ny};
   if (kmul) {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_cols<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_fft_cols<T, true><<<grid, 256, smem, c->stream>>>(data, st, roots<T>(p), es, (int)c->nx, TX, nxt, cnt, s1, s2,
@@ -554,11 +566,11 @@ static int launch_plane(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int m
   Stages sx = stages_of(c->ax[0]), sy = stages_of(c->ax[1]);
   if (mode == 0) {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_plane<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_fft_plane<T, 0><<<grid, 256, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]),
+    k_fft_plane<T, 0><<<grid, 1024, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]),
                                                        nullptr, nullptr, c->ngrid, T(1), T(0));
   } else {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_plane<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_fft_plane<T, 1><<<grid, 256, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]), phi,
+    k_fft_plane<T, 1><<<grid, 1024, smem, c->stream>>>(in, out, sx, sy, roots<T>(c->ax[0]), roots<T>(c->ax[1]), phi,
                                                        pot, c->ngrid, ca, cb);
   }
   FBSE_CHECK_LAUNCH(c);
@@ -576,8 +588,11 @@ template <typename T> static long chunk_blocks(fbse_ctx *c, long nblk)
   return cb < nblk ? cb : nblk;
 }
 
+// out = a (F^-1 K F in + V in) + b in with K = the capped kinetic factor, or
+// the complex k-space array kq when given (then V is not applied)
 template <typename T>
-int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b, int with_v)
+static int fft_op_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b,
+                        int with_v, const double2 *kq)
 {
   int rc;
   const Stages sx = stages_of(c->ax[0]), sy = stages_of(c->ax[1]);
@@ -591,12 +606,12 @@ int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk,
     C<T> *co = out + b0 * c->ngrid;
     if (plane) {
       if ((rc = launch_plane<T>(c, ci, work, nb, 0, nullptr, nullptr, T(1), T(0)))) return rc;
-      if ((rc = launch_cols<T>(c, work, nb, 2, false, true))) return rc;
+      if ((rc = launch_cols<T>(c, work, nb, 2, false, true, kq))) return rc;
       if ((rc = launch_plane<T>(c, work, co, nb, 1, ci, pot, (T)a, (T)b))) return rc;
     } else {
       if ((rc = launch_x<T>(c, ci, work, nb, false, 0, nullptr, nullptr, T(1), T(0)))) return rc;
       if ((rc = launch_cols<T>(c, work, nb, 1, false, false))) return rc;
-      if ((rc = launch_cols<T>(c, work, nb, 2, false, true))) return rc;
+      if ((rc = launch_cols<T>(c, work, nb, 2, false, true, kq))) return rc;
       if ((rc = launch_cols<T>(c, work, nb, 1, true, false))) return rc;
       if ((rc = launch_x<T>(c, work, co, nb, true, 1, ci, pot, (T)a, (T)b))) return rc;
     }
@@ -604,6 +619,32 @@ int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk,
   return FBSE_OK;
 }
 
+template <typename T>
+int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b, int with_v)
+{
+  return fft_op_apply<T>(c, in, out, work, nblk, a, b, with_v, nullptr);
+}
+
+template <typename T>
+int conv_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, const double2 *kq)
+{
+  return fft_op_apply<T>(c, in, out, work, nblk, 1.0, 0.0, 0, kq);
+}
+
+// unnormalised forward 3D DFT of one FP64 block in place (FFTW_FORWARD of the
+// reference's fftw_plan_dft_3d); work: one block of scratch
+int forward_fft64(fbse_ctx *c, double2 *data, double2 *work)
+{
+  int rc;
+  if ((rc = launch_x<double>(c, data, work, 1, false, 0, nullptr, nullptr, 1.0, 0.0))) return rc;
+  if ((rc = launch_cols<double>(c, work, 1, 1, false, false))) return rc;
+  if ((rc = launch_cols<double>(c, work, 1, 2, false, false))) return rc;
+  FBSE_CUDA(c, cudaMemcpyAsync(data, work, c->ngrid * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
+  return FBSE_OK;
+}
+
+template int conv_apply<float>(fbse_ctx *, const C<float> *, C<float> *, C<float> *, long, const double2 *);
+template int conv_apply<double>(fbse_ctx *, const C<double> *, C<double> *, C<double> *, long, const double2 *);
 template int kinetic_apply<float>(fbse_ctx *, const C<float> *, C<float> *, C<float> *, long, double, double, int);
 template int kinetic_apply<double>(fbse_ctx *, const C<double> *, C<double> *, C<double> *, long, double, double, int);
 

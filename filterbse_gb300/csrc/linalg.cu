@@ -134,8 +134,8 @@ __global__ void k_zgemm(int m, int p, int k, const double2 *__restrict__ A, int 
   Cm[(long)i * ldc + j] = make_double2(r, im);
 }
 
-static int zgemm(fbse_ctx *c, int m, int p, int k, const double2 *A, int lda, bool ah, const double2 *B, int ldb,
-                 bool bh, double2 *C, int ldc)
+int zgemm_dev(fbse_ctx *c, int m, int p, int k, const double2 *A, int lda, bool ah, const double2 *B, int ldb, bool bh,
+              double2 *C, int ldc)
 {
   dim3 b(16, 16), g((p + 15) / 16, (m + 15) / 16);
   k_zgemm<<<g, b, 0, c->stream>>>(m, p, k, A, lda, ah, B, ldb, bh, C, ldc);
@@ -261,7 +261,7 @@ __global__ void k_identity(double2 *V, int n)
 // eigen-decomposition of the Hermitian n x n matrix A (device, overwritten);
 // V (device, n x n) receives the eigenvectors as columns, w (host) the
 // eigenvalues in the order of V's columns
-static int jacobi_eig(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<double> &w)
+int jacobi_eig_dev(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<double> &w)
 {
   const int m = n + (n & 1);
   Rot *rot = nullptr;
@@ -557,7 +557,7 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     k_hermitize<<<64, 256, 0, c->stream>>>(M, n);
     // 3. overlap eigen-decomposition
     std::vector<double> w;
-    if ((rc = jacobi_eig(c, G, V, n, w))) break;
+    if ((rc = jacobi_eig_dev(c, G, V, n, w))) break;
     // 4. rank cutoff (ortho.c:68-75 keeps s_i/s_0 >= 1e-10); the overlap
     //    resolves l_i / l_max to the precision of its products
     double lmax = 0;
@@ -578,11 +578,11 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     cudaMemcpyAsync(lam, lk.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);
     FBSE_COUNT(1); k_build_x<<<64, 256, 0, c->stream>>>(V, n, keepd, lam, k, X);
     // 5. H' = X^H M X  (k x k), Hermitian eigen-decomposition
-    if ((rc = zgemm(c, n, k, n, M, n, false, X, k, false, Tm, k))) break;   // Tm = M X   (n x k)
-    if ((rc = zgemm(c, k, k, n, X, k, true, Tm, k, false, Hp, k))) break;  // Hp = X^H Tm (k x k)
+    if ((rc = zgemm_dev(c, n, k, n, M, n, false, X, k, false, Tm, k))) break;   // Tm = M X   (n x k)
+    if ((rc = zgemm_dev(c, k, k, n, X, k, true, Tm, k, false, Hp, k))) break;  // Hp = X^H Tm (k x k)
     FBSE_COUNT(1); k_hermitize<<<64, 256, 0, c->stream>>>(Hp, k);
     std::vector<double> e;
-    if ((rc = jacobi_eig(c, Hp, U, k, e))) break;
+    if ((rc = jacobi_eig_dev(c, Hp, U, k, e))) break;
     std::vector<int> perm(k);
     std::iota(perm.begin(), perm.end(), 0);
     std::sort(perm.begin(), perm.end(), [&](int a, int b) { return e[a] < e[b]; });
@@ -592,7 +592,7 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     cudaMemcpyAsync(Ed, es.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);
     FBSE_COUNT(1); k_permute_cols<<<64, 256, 0, c->stream>>>(U, permd, k, Tm);
     // 6. C = X U  (n x k); rotate Psi and HPsi with the residual epilogue
-    if ((rc = zgemm(c, n, k, k, X, k, false, Tm, k, false, Cm, k))) break;
+    if ((rc = zgemm_dev(c, n, k, k, X, k, false, Tm, k, false, Cm, k))) break;
     dim3 gr(nrb, (k + 31) / 32);
     if (c->is_complex) k_rotate<T, true><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
     else k_rotate<T, false><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);

@@ -167,6 +167,50 @@ int fbse_filter_job(fbse_ctx *ctx, const double *zn, const double *an, long nche
                     const double *psi0_host, long nstart, double sigma_cut, long *n_out, double *eval_host,
                     double *sigma_host, double *psi_host);
 
+/* ---- Bethe-Salpeter stage (bse_cplx/) --------------------------------------
+ * States: psi_qp holds the quasiparticle basis as complex spinor states
+ * (nspin*ngrid complex doubles each, device): holes at indices 0..n_h-1, the
+ * electrons at lumo_idx..lumo_idx+n_e-1 (get_qp_basis, bse_cplx/basis.c:258).
+ * Pair index ibs = (a - lumo_idx) * n_h + i; n_xton = n_h * n_e. */
+
+/* init_elec_hole_kernel (bse_cplx/init.c:8-268): bare v(k) and screened W(k)
+ * on the context's grid (ngrid complex doubles each, device), including the
+ * 1/N of the FFT.  gx/gy/gz: grid coordinates (host); xmin..zmin: grid origin;
+ * eps_*: the dielectric constants (epsX/epsY/epsZ of bse input.par). */
+int fbse_bse_potentials(fbse_ctx *ctx, const double *gx, const double *gy, const double *gz, double xmin, double ymin,
+                        double zmin, double eps_x, double eps_y, double eps_z, double *pot_bare,
+                        double *pot_screened);
+
+/* calc_eh_kernel_cplx (bse_cplx/coulomb.c:20-738): direct and exchange kernels,
+ * n_xton x n_xton complex (device), lower triangle ibs >= jbs filled as the
+ * reference fills it (the rest is zero). */
+int fbse_bse_kernel(fbse_ctx *ctx, const double *psi_qp, long n_h, long n_e, long lumo_idx, const double *pot_bare,
+                    const double *pot_screened, double *direct, double *exchange);
+
+/* build_h0_mat + build_BSE_mat + bethe_salpeter (bse_cplx/mod_bse.c:54-148,
+ * bethe-salpeter.c:7-350): H = diag(e_a - e_i) - (K^d + K^x), FP64 Hermitian
+ * eigensolve on the GPU.  eval_qp_host: n_qp quasiparticle energies (host).
+ * direct/exchange (device) are completed to full Hermitian matrices; xton_ene
+ * (host, n_xton) ascending; coeff (device, n_xton x n_xton complex, row-major,
+ * column j = exciton j); h/d/x/h0_exp (host, may be NULL): <H>, <K^d>, <K^x>,
+ * <h0> per exciton -- the columns of exciton.dat. */
+int fbse_bse_solve(fbse_ctx *ctx, const double *eval_qp_host, long n_qp, long n_h, long n_e, long lumo_idx,
+                   double *direct, double *exchange, double *xton_ene, double *coeff, double *h_exp, double *d_exp,
+                   double *x_exp, double *h0_exp);
+
+/* calc_elec_dipole (bse_cplx/dipole.c:7-158): mu[(i * n_e + a)][3] complex
+ * (host) = dv sum_{r,sigma} conj(psi_i) r psi_a. */
+int fbse_bse_dipoles(fbse_ctx *ctx, const double *psi_qp, const double *gx, const double *gy, const double *gz,
+                     long n_h, long n_e, long lumo_idx, double *mu_host);
+
+/* calc_optical_exc (bse_cplx/optical.c:6-99), electric part: exciton transition
+ * dipoles mu_j = sum_ibs coeff[ibs][j] mu_(i(ibs), a(ibs)).  coeff: device, as
+ * fbse_bse_solve returns it; mu_pairs_host: fbse_bse_dipoles' output;
+ * mu_xton_host: [n_xton][3] complex (host).  OS.dat's columns follow from it:
+ * |mu_j|, E_j, (2/3) E_j |mu_j|^2. */
+int fbse_bse_optical(fbse_ctx *ctx, const double *coeff, const double *mu_pairs_host, long n_h, long n_e,
+                     double *mu_xton_host);
+
 /* ---- setup on the GPU -----------------------------------------------------
  * build_local_pot (filter_mpi/init.c:481-703) for short-ranged tables
  * (no strain, no cubic/ortho interpolation, no LSD, no long range):

@@ -541,3 +541,150 @@ def sigma_e(psis: np.ndarray, sysm: System):
         ev.append(e)
         sg.append(float(np.sqrt(np.sum(np.abs(r) ** 2) * dv)))
     return np.array(ev), np.array(sg)
+
+
+# --------------------------------------------------------------------------
+# Bethe-Salpeter stage (bse_cplx/)
+# --------------------------------------------------------------------------
+
+def bse_axes(grid: Grid):
+    """The BSE stage's coordinates, x_j = xmin + j dx (bse_cplx/read.c:398-409)."""
+    return [lo + np.arange(n) * d for n, d, lo in ((grid.nx, grid.dx, grid.xmin), (grid.ny, grid.dy, grid.ymin),
+                                                   (grid.nz, grid.dz, grid.zmin))]
+
+
+def bse_potentials(grid: Grid, eps=(6.0, 6.0, 6.0)):
+    """init_elec_hole_kernel (bse_cplx/init.c:8-268): bare v(k) and screened
+    W(k) on the grid, flat [ngrid] complex, including the 1/N."""
+    from scipy.special import erf
+    gx, gy, gz = bse_axes(grid)
+    nx, ny, nz, N = grid.nx, grid.ny, grid.nz, grid.ngrid
+    xm, ym, zm = abs(grid.xmin), abs(grid.ymin), abs(grid.zmin)
+    if xm < ym and xm < zm:
+        minr, boxl = xm, nx * grid.dx
+    elif ym < zm and ym < xm:
+        minr, boxl = ym, ny * grid.dy
+    else:
+        minr, boxl = zm, nz * grid.dz
+    gamma = 7.0 / (2.0 * minr)
+    ex, ey, ez = eps
+    sqe_1 = 1.0 / np.sqrt(ex * ey * ez)
+    sqrtaveps = np.sqrt((ex + ey + ez) / 3.0)
+    gammaeps = gamma * sqrtaveps
+    sqrk0 = gamma ** 2 * sqrtaveps ** 2
+
+    def coul(r, g):  # calc_coulomb (init.c:271-291)
+        out = np.empty_like(r)
+        small = r < 1e-10
+        out[small] = 2.0 * g / np.sqrt(np.pi)
+        out[~small] = erf(g * r[~small]) / r[~small]
+        return out
+
+    Z, Y, X = np.meshgrid(gz, gy, gx, indexing="ij")
+    x2, y2, z2 = X * X, Y * Y, Z * Z
+    r2 = x2 + y2 + z2
+    inside = r2 < boxl * boxl
+    potr = np.where(inside, coul(np.sqrt(x2 + y2 + z2), gamma), 0.0)
+    potrx = np.where(inside, sqe_1 * coul(np.sqrt(x2 / ex + y2 / ey + z2 / ez), gammaeps), 0.0)
+    fb = np.fft.fftn(potr.astype(np.complex128))
+    fs = np.fft.fftn(potrx.astype(np.complex128))
+    dk = [2 * np.pi / (n * d) for n, d in ((nx, grid.dx), (ny, grid.dy), (nz, grid.dz))]
+
+    def k2(n, d):
+        m = np.arange(n)
+        m = np.where(m <= n // 2, m, n - m)
+        return (m * d) ** 2
+
+    KZ, KY, KX = np.meshgrid(k2(nz, dk[2]), k2(ny, dk[1]), k2(nx, dk[0]), indexing="ij")
+    JZ, JY, JX = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    alpha = np.pi * (JX + JY + JZ + N // 2).astype(np.float64)
+    ph = np.cos(alpha) + 1j * np.sin(alpha)
+    bare = fb * ph * grid.dv + 4 * np.pi / (KX + KY + KZ + gamma ** 2)
+    ek = ex * KX + ey * KY + ez * KZ
+    scr = fs * ph * grid.dv + 4 * np.pi * (1.0 - np.exp(-0.25 * ek / sqrk0)) / (ek + 1e-10)
+    return (bare / N).reshape(-1), (scr / N).reshape(-1)
+
+
+def hartree(rho: np.ndarray, potq: np.ndarray, grid: Grid):
+    """hartree (bse_cplx/hartree.c:7-31): FFTW forward, times potq, backward."""
+    shp = (grid.nz, grid.ny, grid.nx)
+    f = np.fft.fftn(rho.reshape(shp)) * potq.reshape(shp)
+    return (np.fft.ifftn(f) * grid.ngrid).reshape(-1)
+
+
+def bse_kernels(psi_qp: np.ndarray, nh: int, ne: int, lumo: int, bare, scr, grid: Grid, nspin: int = 2):
+    """calc_eh_kernel_cplx (bse_cplx/coulomb.c:20-738): direct and exchange,
+    lower triangles ibs >= jbs as the reference fills them."""
+    N = grid.ngrid
+    dv = grid.dv
+
+    def rho(x, y):
+        return sum(np.conj(psi_qp[x, s * N:(s + 1) * N]) * psi_qp[y, s * N:(s + 1) * N] for s in range(nspin))
+
+    nx = ne * nh
+    D = np.zeros((nx, nx), np.complex128)
+    X = np.zeros((nx, nx), np.complex128)
+    for a in range(ne):
+        for b in range(ne):
+            h = hartree(rho(lumo + a, lumo + b), scr, grid)
+            for i in range(nh):
+                for j in range(nh):
+                    ibs, jbs = a * nh + i, b * nh + j
+                    if ibs < jbs:
+                        continue
+                    D[ibs, jbs] = np.sum(h * rho(j, i)) * dv
+    for a in range(ne):
+        for i in range(nh):
+            h = hartree(rho(lumo + a, i), bare, grid)
+            for b in range(ne):
+                for j in range(nh):
+                    ibs, jbs = a * nh + i, b * nh + j
+                    if ibs < jbs:
+                        continue
+                    X[ibs, jbs] = -np.sum(h * rho(j, lumo + b)) * dv
+    return D, X
+
+
+def bse_solve(eval_qp, nh, ne, lumo, D, X):
+    """build_h0_mat, build_BSE_mat, bethe_salpeter (bse_cplx/mod_bse.c:54-148,
+    bethe-salpeter.c:7-350): returns (E, C, <H>, <Kd>, <Kx>, <h0>)."""
+    n = nh * ne
+    Df = np.tril(D) + np.conj(np.tril(D, -1)).T
+    Xf = np.tril(X) + np.conj(np.tril(X, -1)).T
+    Df[np.diag_indices(n)] = Df.diagonal().real
+    Xf[np.diag_indices(n)] = Xf.diagonal().real
+    h0 = np.zeros((n, n))
+    for a in range(ne):
+        for i in range(nh):
+            h0[a * nh + i, a * nh + i] = eval_qp[lumo + a] - eval_qp[i]
+    H = h0 - (Df + Xf)
+    H[np.diag_indices(n)] = H.diagonal().real
+    e, C = np.linalg.eigh(H)
+    ex = lambda M: np.real(np.einsum("li,lk,ki->i", C.conj(), M, C))
+    return e, C, ex(H), ex(Df), ex(Xf), ex(h0)
+
+
+def bse_dipoles(psi_qp, nh, ne, lumo, grid: Grid, nspin=2):
+    """calc_elec_dipole (bse_cplx/dipole.c:7-158): [nh*ne][3] complex."""
+    gx, gy, gz = bse_axes(grid)
+    Z, Y, X = np.meshgrid(gz, gy, gx, indexing="ij")
+    coords = [X.reshape(-1), Y.reshape(-1), Z.reshape(-1)]
+    N = grid.ngrid
+    mu = np.zeros((nh * ne, 3), np.complex128)
+    for i in range(nh):
+        for a in range(ne):
+            t = sum(np.conj(psi_qp[i, s * N:(s + 1) * N]) * psi_qp[lumo + a, s * N:(s + 1) * N] for s in range(nspin))
+            for d in range(3):
+                mu[i * ne + a, d] = np.sum(t * coords[d]) * grid.dv
+    return mu
+
+
+def bse_optical(C, mu, nh, ne):
+    """calc_optical_exc (bse_cplx/optical.c:36-80), electric part: exciton
+    dipoles [n][3] and OS.dat's oscillator strengths need E: (2/3) E |mu|^2."""
+    n = nh * ne
+    out = np.zeros((n, 3), np.complex128)
+    for a in range(ne):
+        for i in range(nh):
+            out += np.outer(C[a * nh + i, :], mu[i * ne + a])
+    return out
