@@ -29,6 +29,7 @@ EXPORTED = [
     "fbse_ortho_diag_sigma", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
     "fbse_init_filter_states", "fbse_launch_count", "fbse_filter_job", "fbse_build_local_pot",
     "fbse_bse_potentials", "fbse_bse_kernel", "fbse_bse_solve", "fbse_bse_dipoles", "fbse_bse_optical",
+    "fbse_normalize_all_noalloc",
 ]
 
 

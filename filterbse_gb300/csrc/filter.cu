@@ -500,3 +500,113 @@ int energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *em
 }
 
 }  // namespace fbse
+
+// ---------------------------------------------------------------------------
+// normalize_all without any allocation: the partial sums, norms, scale
+// factors and the error key live in one file-scope device array.  Its device
+// address is looked up once per device (cudaGetSymbolAddress, with that
+// device current) on the first call.  Only the error key must start at a
+// known value; it is set on the stream at the start of every call.  The
+// array is shared by every context on the device, so overlapping calls race.
+// ---------------------------------------------------------------------------
+
+#include <mutex>
+
+namespace fbse {
+
+constexpr long kNoAllocMaxStates = 1024;
+constexpr long kNoAllocPart = kNoAllocMaxStates * kRedBlocks * 2;  // doubles of partial sums
+constexpr long kNoAllocDoubles = kNoAllocPart + 2 * kNoAllocMaxStates + 32;
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+namespace {
+std::mutex g_noalloc_mu;
+double *g_noalloc_ptr[64] = {};
+}  // namespace
+
+// norms, factors and the first failing state: key = 2 * index + (NaN ? 1 : 0)
+__global__ void k_norm_factors(const double *__restrict__ part, int nb, long n, double dv, double *__restrict__ norms,
+                               double *__restrict__ f, int *__restrict__ key)
+{
+  for (long st = blockIdx.x * (long)blockDim.x + threadIdx.x; st < n; st += (long)gridDim.x * blockDim.x) {
+    double a = 0;
+    for (int b = 0; b < nb; b++) a += part[(st * nb + b) * 2];
+    const double nr = a * dv;  // norm.c:138-140
+    norms[st] = nr;
+    if (nr == 0.0) atomicMin(key, (int)(2 * st));
+    else if (isnan(nr)) atomicMin(key, (int)(2 * st + 1));
+    f[st] = 1.0 / sqrt(nr);
+  }
+}
+
+__global__ void k_scale_states_if_ok(double *__restrict__ x, long len, long n, const double *__restrict__ f,
+                                     const int *__restrict__ key)
+{
+  if (*key != 0x7f7f7f7f) return;  // a zero or NaN norm: leave the states as they were
+  const long total = n * len;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x)
+    x[i] *= f[i / len];
+}
+
+static int noalloc_scratch(fbse_ctx *c, double **out)
+{
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: no current device");
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return set_err(c, FBSE_ERR_CUDA,
+                     std::string("fbse_normalize_all_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    }
+    g_noalloc_ptr[dev] = (double *)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return FBSE_OK;
+}
+
+int normalize_all_noalloc(fbse_ctx *c, double *psitot, long n, double *norms)
+{
+  if (n < 1) return FBSE_OK;
+  if (n > kNoAllocMaxStates)
+    return set_err(c, FBSE_ERR_ARG, "fbse_normalize_all_noalloc: " + std::to_string(n) + " states exceed the " +
+                                        std::to_string(kNoAllocMaxStates) + "-state scratch");
+  double *s = nullptr;
+  int rc = noalloc_scratch(c, &s);
+  if (rc) return rc;
+  double *part = s, *nrm = s + kNoAllocPart, *f = nrm + kNoAllocMaxStates;
+  int *key = (int *)(f + kNoAllocMaxStates);
+  const long stlen = (long)(c->is_complex + 1) * c->nspin * c->ngrid;
+  int hkey = 0;
+  if (cudaMemsetAsync(key, 0x7f, sizeof(int), c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: key reset");
+  }
+  k_sumsq<<<dim3(kRedBlocks, (unsigned)n), 256, 0, c->stream>>>(psitot, stlen, part);
+  FBSE_CHECK_LAUNCH(c);
+  k_norm_factors<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(part, kRedBlocks, n, c->dv, nrm, f, key);
+  FBSE_CHECK_LAUNCH(c);
+  k_scale_states_if_ok<<<grid_for(n * stlen), 256, 0, c->stream>>>(psitot, stlen, n, f, key);
+  FBSE_CHECK_LAUNCH(c);
+  if (d2h(c->stream, &hkey, key, sizeof(int)) != cudaSuccess ||
+      (norms && d2h(c->stream, norms, nrm, n * sizeof(double)) != cudaSuccess)) {
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: download");
+  }
+  if (hkey != 0x7f7f7f7f) return set_err(c, FBSE_ERR_NAN, (hkey & 1) ? "Norm is NAN! exiting!" : "Norm is 0! exiting!");
+  return FBSE_OK;
+}
+
+}  // namespace fbse
+
+extern "C" int fbse_normalize_all_noalloc(fbse_ctx *c, double *psitot, long n, double *norms)
+{
+  if (!c || !psitot) return c ? fbse::set_err(c, FBSE_ERR_ARG, "fbse_normalize_all_noalloc: null") : FBSE_ERR_ARG;
+  return fbse::normalize_all_noalloc(c, psitot, n, norms);
+}

@@ -142,6 +142,15 @@ int fbse_energy_range(fbse_ctx *ctx, long seed, long max_iter, double *emin, dou
 int fbse_normalize_all(fbse_ctx *ctx, double *psitot, long n, double *norms);
 int fbse_energy_all(fbse_ctx *ctx, const double *psitot, long n, double *ene);
 
+/* fbse_normalize_all without any allocation (no counterpart in the reference):
+ * for callers that must not allocate device memory mid-run.  Its scratch is a
+ * file-scope device array of about 1.06 MB, at most 1024 states per call
+ * (more returns FBSE_ERR_ARG).  The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress, with that device current) and should come
+ * before any stream capture.  The array is shared by all contexts on a device:
+ * calls that overlap in time race.  norms may be NULL. */
+int fbse_normalize_all_noalloc(fbse_ctx *ctx, double *psitot, long n, double *norms);
+
 /* ---- orthogonalisation, subspace diagonalisation, sigma_E ----------------
  * Replaces mod_ortho + mod_diag + mod_sigma (filter_mpi/mod_ortho.c:3-94,
  * mod_diag.c:324-449, mod_sigma.c:6-63) for n psitot states (device, in
