@@ -466,6 +466,12 @@ __global__ void __launch_bounds__(256, 4) k_fft_cols(C<T> *__restrict__ data, St
   }
 }
 
+}  // namespace fbse
+
+#include "fft_fast.cuh"
+
+namespace fbse {
+
 template <typename T> static const T *pot_of(fbse_ctx *c);
 template <> const float *pot_of<float>(fbse_ctx *c) { return c->pot32; }
 template <> const double *pot_of<double>(fbse_ctx *c) { return c->pot64; }
@@ -577,15 +583,143 @@ static int launch_plane(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int m
   return FBSE_OK;
 }
 
-// blocks per chunk: keep a chunk's scratch (and its input) within L2
+// blocks per launch: all of them by default (more CTAs in flight beat keeping
+// the scratch in L2 on measured 128^3 runs); FBSE_FFT_CHUNK_BLOCKS caps it
 template <typename T> static long chunk_blocks(fbse_ctx *c, long nblk)
 {
+  (void)c;
   const char *e = getenv("FBSE_FFT_CHUNK_BLOCKS");
   if (e && atol(e) > 0) return atol(e) < nblk ? atol(e) : nblk;
-  const double blk = (double)c->ngrid * sizeof(C<T>);
-  long cb = (long)(40.0e6 / blk);
-  if (cb < 1) cb = 1;
-  return cb < nblk ? cb : nblk;
+  return nblk;
+}
+
+// ---------------------------------------------------------------------------
+// register-resident kernels (fft_fast.cuh) for axes of 64, 128, 256 points;
+// FBSE_FFT_GENERIC=1 selects the mixed-radix kernels for every axis
+// ---------------------------------------------------------------------------
+static bool fast_generic_forced()
+{
+  static int v = -1;
+  if (v < 0) v = getenv("FBSE_FFT_GENERIC") != nullptr;
+  return v == 1;
+}
+static bool fast_axis_ok(long n) { return !fast_generic_forced() && (n == 64 || n == 128 || n == 256); }
+
+template <typename T> static bool fast_plane_ok(fbse_ctx *c)
+{
+  if (fast_generic_forced() || c->nx != c->ny || getenv("FBSE_FFT_LINES") != nullptr) return false;
+  if (c->nx == 64) return fast::PlaneCfg<T, 64>::smem() <= (size_t)max_smem();
+  if (c->nx == 128 && sizeof(C<T>) == 8) return fast::PlaneCfg<T, 128>::smem() <= (size_t)max_smem();
+  return false;
+}
+
+template <typename T, int N>
+static int launch_plane_fast_n(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int mode, const C<T> *phi,
+                               const T *pot, T ca, T cb)
+{
+  using Cfg = fast::PlaneCfg<T, N>;
+  const size_t smem = Cfg::smem();
+  const long grid = nblk * c->nz;
+  const C<T> *rt = roots<T>(c->ax[0]);
+  if (mode == 0) {
+    FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_plane_fast<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    fast::k_plane_fast<T, N, 0><<<grid, Cfg::THREADS, smem, c->stream>>>(in, out, rt, nullptr, nullptr, c->ngrid,
+                                                                          T(1), T(0));
+  } else {
+    FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_plane_fast<T, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    fast::k_plane_fast<T, N, 1><<<grid, Cfg::THREADS, smem, c->stream>>>(in, out, rt, phi, pot, c->ngrid, ca, cb);
+  }
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+template <typename T>
+static int launch_plane_fast(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int mode, const C<T> *phi,
+                             const T *pot, T ca, T cb)
+{
+  if (c->nx == 64) return launch_plane_fast_n<T, 64>(c, in, out, nblk, mode, phi, pot, ca, cb);
+  if constexpr (sizeof(C<T>) == 8) {
+    if (c->nx == 128) return launch_plane_fast_n<T, 128>(c, in, out, nblk, mode, phi, pot, ca, cb);
+  }
+  return set_err(c, FBSE_ERR_UNSUPPORTED, "no register-resident plane kernel for this size");
+}
+
+template <typename T, int N>
+static int launch_cols_fast_n(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, bool kmul, const double2 *kq)
+{
+  using Cfg = fast::ColsCfg<T, N>;
+  const int nxt = (int)((c->nx + 31) / 32);
+  long es, cnt, s1, s2, nouter;
+  if (axis == 1) {
+    es = c->nx; cnt = 1; s1 = c->nx * c->ny; s2 = 0; nouter = nblk * c->nz;
+  } else {
+    es = c->nx * c->ny; cnt = c->ny; s1 = c->ngrid; s2 = c->nx; nouter = nblk * c->ny;
+  }
+  const size_t smem = Cfg::smem();
+  const long grid = nouter * nxt;
+  const C<T> *rt = roots<T>(c->ax[axis]);
+  KinArgs ka{c->k2x, c->k2y, c->k2z, c->kemax_scaled, kq, c->nx, c->nx * c->ny};
+  if (kmul) {
+    FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_cols_fast<T, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    fast::k_cols_fast<T, N, true><<<grid, Cfg::THREADS, smem, c->stream>>>(data, rt, es, (int)c->nx, nxt, cnt, s1,
+                                                                            s2, inv, ka);
+  } else {
+    FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_cols_fast<T, N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    fast::k_cols_fast<T, N, false><<<grid, Cfg::THREADS, smem, c->stream>>>(data, rt, es, (int)c->nx, nxt, cnt, s1,
+                                                                             s2, inv, ka);
+  }
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+template <typename T>
+static int launch_cols_any(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, bool kmul,
+                           const double2 *kq = nullptr)
+{
+  switch (fast_axis_ok(c->ax[axis].n) ? c->ax[axis].n : 0) {
+    case 64: return launch_cols_fast_n<T, 64>(c, data, nblk, axis, inv, kmul, kq);
+    case 128: return launch_cols_fast_n<T, 128>(c, data, nblk, axis, inv, kmul, kq);
+    case 256: return launch_cols_fast_n<T, 256>(c, data, nblk, axis, inv, kmul, kq);
+    default: return launch_cols<T>(c, data, nblk, axis, inv, kmul, kq);
+  }
+}
+
+template <typename T, int N>
+static int launch_x_fast_n(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, bool inv, int epi, const C<T> *phi,
+                           const T *pot, T ca, T cb)
+{
+  using Cfg = fast::XCfg<T, N>;
+  const long nlines = nblk * c->ny * c->nz;
+  const size_t smem = Cfg::smem();
+  const long grid = (nlines + Cfg::LINES - 1) / Cfg::LINES;
+  const C<T> *rt = roots<T>(c->ax[0]);
+  if (epi) {
+    FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_x_fast<T, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fast::k_x_fast<T, N, 1><<<grid, Cfg::THREADS, smem, c->stream>>>(in, out, rt, nlines, inv, phi, pot, c->ngrid,
+                                                                      ca, cb);
+  } else {
+    FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_x_fast<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fast::k_x_fast<T, N, 0><<<grid, Cfg::THREADS, smem, c->stream>>>(in, out, rt, nlines, inv, nullptr, nullptr,
+                                                                      c->ngrid, T(1), T(0));
+  }
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+template <typename T>
+static int launch_x_any(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, bool inv, int epi, const C<T> *phi,
+                        const T *pot, T ca, T cb)
+{
+  switch (fast_axis_ok(c->nx) ? c->nx : 0) {
+    case 64: return launch_x_fast_n<T, 64>(c, in, out, nblk, inv, epi, phi, pot, ca, cb);
+    case 128: return launch_x_fast_n<T, 128>(c, in, out, nblk, inv, epi, phi, pot, ca, cb);
+    case 256: return launch_x_fast_n<T, 256>(c, in, out, nblk, inv, epi, phi, pot, ca, cb);
+    default: return launch_x<T>(c, in, out, nblk, inv, epi, phi, pot, ca, cb);
+  }
 }
 
 // out = a (F^-1 K F in + V in) + b in with K = the capped kinetic factor, or
@@ -599,21 +733,26 @@ static int fft_op_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long
   const bool plane = !sx.big && !sy.big && plane_smem<T>(c) <= (size_t)max_smem() &&
                      getenv("FBSE_FFT_LINES") == nullptr;
   const T *pot = with_v ? pot_of<T>(c) : nullptr;
+  const bool fplane = fast_plane_ok<T>(c);
   const long cb = chunk_blocks<T>(c, nblk);
   for (long b0 = 0; b0 < nblk; b0 += cb) {
     const long nb = (nblk - b0 < cb) ? nblk - b0 : cb;
     const C<T> *ci = in + b0 * c->ngrid;
     C<T> *co = out + b0 * c->ngrid;
-    if (plane) {
+    if (fplane) {
+      if ((rc = launch_plane_fast<T>(c, ci, work, nb, 0, nullptr, nullptr, T(1), T(0)))) return rc;
+      if ((rc = launch_cols_any<T>(c, work, nb, 2, false, true, kq))) return rc;
+      if ((rc = launch_plane_fast<T>(c, work, co, nb, 1, ci, pot, (T)a, (T)b))) return rc;
+    } else if (plane) {
       if ((rc = launch_plane<T>(c, ci, work, nb, 0, nullptr, nullptr, T(1), T(0)))) return rc;
       if ((rc = launch_cols<T>(c, work, nb, 2, false, true, kq))) return rc;
       if ((rc = launch_plane<T>(c, work, co, nb, 1, ci, pot, (T)a, (T)b))) return rc;
     } else {
-      if ((rc = launch_x<T>(c, ci, work, nb, false, 0, nullptr, nullptr, T(1), T(0)))) return rc;
-      if ((rc = launch_cols<T>(c, work, nb, 1, false, false))) return rc;
-      if ((rc = launch_cols<T>(c, work, nb, 2, false, true, kq))) return rc;
-      if ((rc = launch_cols<T>(c, work, nb, 1, true, false))) return rc;
-      if ((rc = launch_x<T>(c, work, co, nb, true, 1, ci, pot, (T)a, (T)b))) return rc;
+      if ((rc = launch_x_any<T>(c, ci, work, nb, false, 0, nullptr, nullptr, T(1), T(0)))) return rc;
+      if ((rc = launch_cols_any<T>(c, work, nb, 1, false, false))) return rc;
+      if ((rc = launch_cols_any<T>(c, work, nb, 2, false, true, kq))) return rc;
+      if ((rc = launch_cols_any<T>(c, work, nb, 1, true, false))) return rc;
+      if ((rc = launch_x_any<T>(c, work, co, nb, true, 1, ci, pot, (T)a, (T)b))) return rc;
     }
   }
   return FBSE_OK;

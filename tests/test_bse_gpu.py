@@ -17,6 +17,7 @@ GRIDS = {
     "cubic24": O.Grid(24, 24, 24, 0.7, 0.7, 0.7, -8.4, -8.4, -8.4),
     "odd21x20x18": O.Grid(21, 20, 18, 0.75, 0.8, 0.85, -7.5, -8.0, -7.65),
     "ymin_smallest": O.Grid(20, 18, 22, 0.8, 0.8, 0.8, -8.0, -7.2, -8.8),
+    "cubic64": O.Grid(64, 64, 64, 0.4, 0.4, 0.4, -12.8, -12.8, -12.8),
 }
 
 
@@ -69,7 +70,8 @@ def _setup(fbse, cuda, name, nh, ne, gap, precision=0, seed=7):
     return g, ctx, lumo, psi, psi_d, bare, scr
 
 
-@pytest.mark.parametrize("name,nh,ne,gap", [("cubic24", 3, 4, 1), ("odd21x20x18", 4, 2, 0), ("ymin_smallest", 2, 3, 2)])
+@pytest.mark.parametrize("name,nh,ne,gap", [("cubic24", 3, 4, 1), ("odd21x20x18", 4, 2, 0), ("ymin_smallest", 2, 3, 2),
+                                            ("cubic64", 2, 2, 0)])
 def test_bse_kernel_fp64_matches_oracle(fbse, cuda, name, nh, ne, gap):
     g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, name, nh, ne, gap)
     D, X = ctx.bse_kernel(psi_d, nh, ne, lumo, bare, scr)
@@ -81,8 +83,9 @@ def test_bse_kernel_fp64_matches_oracle(fbse, cuda, name, nh, ne, gap):
     assert np.all(D[iu] == 0) and np.all(X[iu] == 0)
 
 
-def test_bse_kernel_mixed_within_tolerance(fbse, cuda):
-    g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, "cubic24", 3, 4, 1, precision=1)
+@pytest.mark.parametrize("name", ["cubic24", "cubic64"])
+def test_bse_kernel_mixed_within_tolerance(fbse, cuda, name):
+    g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, name, 3, 4, 1, precision=1)
     D, X = ctx.bse_kernel(psi_d, 3, 4, lumo, bare, scr)
     rD, rX = O.bse_kernels(psi, 3, 4, lumo, bare.cpu().numpy(), scr.cpu().numpy(), g)
     assert _relmax(D.cpu().numpy(), rD) < 3e-5

@@ -33,7 +33,11 @@ def _relerr(a, b, real_only=False):
     return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
 
 
-@pytest.mark.parametrize("shape", [(16, 16, 16), (24, 21, 22), (20, 26, 15), (19, 14, 33), (57, 52, 45), (13, 28, 17)])
+# the last five shapes take the register-resident kernels (axes of 64, 128, 256):
+# square planes of 64 / 128, non-square planes (line path), a 256-point z axis
+# and a fast plane with a mixed-radix z axis
+@pytest.mark.parametrize("shape", [(16, 16, 16), (24, 21, 22), (20, 26, 15), (19, 14, 33), (57, 52, 45), (13, 28, 17),
+                                   (64, 64, 64), (128, 128, 64), (128, 64, 64), (64, 64, 256), (64, 64, 48)])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_kinetic_and_local(fbse, cuda, shape, precision):
     nx, ny, nz = shape
