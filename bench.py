@@ -170,6 +170,7 @@ def run_gpu(args):
     ext = torch.cuda.ExternalStream(cmx.stream_handle)
     for _ in range(args.warmup):
         step(cmx)
+    log(f"[launches] {F.launch_count()} library kernels launched before the timed steps")
     if dist:
         dist.barrier()
     torch.cuda.synchronize()

@@ -113,6 +113,7 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
   const long ns[3] = {g->nx, g->ny, g->nz};
   const double ds[3] = {g->dx, g->dy, g->dz};
   double **dst[3] = {&c->k2x, &c->k2y, &c->k2z};
+  float **dstf[3] = {&c->k2xf, &c->k2yf, &c->k2zf};
   const double dkin[3] = {g->dkx, g->dky, g->dkz};
   for (int a = 0; a < 3; a++) {
     const double box = (ns[a] % 2 == 0) ? (double)ns[a] * ds[a] : (double)(ns[a] - 1) * ds[a];
@@ -120,6 +121,7 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
     std::vector<double> k;
     axis_k2(ns[a], dk, ng_1, k);
     if ((rc = upload(c, dst[a], k.data(), k.size()))) return rc;
+    if ((rc = upload(c, dstf[a], k.data(), k.size()))) return rc;
   }
   if ((rc = upload(c, &c->pot64, pot, c->ngrid))) return rc;
   if ((rc = upload(c, &c->pot32, pot, c->ngrid))) return rc;
@@ -216,7 +218,7 @@ void fbse_destroy(fbse_ctx *c)
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (int a = 0; a < 3; a++) free_axis(c->ax[a]);
-  void *bufs[] = {c->k2x, c->k2y, c->k2z, c->pot64, c->pot32, c->wk, c->coef, c->tmp, c->red,
+  void *bufs[] = {c->k2x, c->k2y, c->k2z, c->k2xf, c->k2yf, c->k2zf, c->pot64, c->pot32, c->wk, c->coef, c->tmp, c->red,
                   c->proj.nl_cnt, c->proj.jxyz, c->proj.y1, c->proj.sop, c->proj.nlp, c->proj.sgn, c->proj.LS,
                   c->proj.y1f, c->proj.sopf, c->proj.nlpf};
   for (void *b : bufs)

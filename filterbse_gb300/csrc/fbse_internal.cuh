@@ -86,6 +86,7 @@ struct fbse_ctx {
   double kemax_scaled = 0;                 // KE_max / N (init.c:338)
   fbse::AxisPlan ax[3];                    // x, y, z
   double *k2x = nullptr, *k2y = nullptr, *k2z = nullptr;  // per-axis 0.5 k^2 / N (device)
+  float *k2xf = nullptr, *k2yf = nullptr, *k2zf = nullptr;  // the same rounded to FP32 (mixed path)
   double *pot64 = nullptr;                 // [ngrid]
   float *pot32 = nullptr;
   double vpot_min = 0, vpot_max = 0;

@@ -410,10 +410,25 @@ __global__ void __launch_bounds__(256, 4) k_fft_x(const C<T> *__restrict__ in, C
 // ---------------------------------------------------------------------------
 struct KinArgs {
   const double *k2x, *k2y, *k2z;
+  const float *k2xf, *k2yf, *k2zf;  // FP32 copies: the mixed path's factor is formed in FP32
   double kemax;
   const double2 *kq;  // when set: multiply by this complex k-space array instead
   long nx, nxy;
 };
+
+// min(0.5 k^2, KE_max) / N from the per-axis tables, in the working precision
+template <typename T> __device__ __forceinline__ T kin_factor(const KinArgs &ka, int x, int y, int z);
+template <> __device__ __forceinline__ double kin_factor<double>(const KinArgs &ka, int x, int y, int z)
+{
+  const double kk = ka.k2x[x] + ka.k2y[y] + ka.k2z[z];
+  return kk > ka.kemax ? ka.kemax : kk;
+}
+template <> __device__ __forceinline__ float kin_factor<float>(const KinArgs &ka, int x, int y, int z)
+{
+  const float kk = ka.k2xf[x] + ka.k2yf[y] + ka.k2zf[z];
+  const float cap = (float)ka.kemax;
+  return kk > cap ? cap : kk;
+}
 
 template <typename T, bool KMUL>
 __global__ void __launch_bounds__(256, 4) k_fft_cols(C<T> *__restrict__ data, Stages st, const C<T> *__restrict__ twg,
@@ -448,12 +463,9 @@ __global__ void __launch_bounds__(256, 4) k_fft_cols(C<T> *__restrict__ data, St
         A[t] = cmul<T>(A[t], mk<T>((T)q.x, (T)q.y));
       }
     } else {
-      const double ky = ka.k2y[jy];
       for (int t = threadIdx.x; t < n * L; t += blockDim.x) {
         const int cc = t % L, i = t / L;
-        double kk = ka.k2x[x0 + cc] + ky + ka.k2z[i];
-        if (kk > ka.kemax) kk = ka.kemax;
-        A[t] = cscale<T>(A[t], (T)kk);
+        A[t] = cscale<T>(A[t], kin_factor<T>(ka, x0 + cc, jy, i));
       }
     }
     __syncthreads();
@@ -543,7 +555,7 @@ static int launch_cols(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, b
   const size_t smem = (size_t)(n + (st.big ? 2L : 1L) * TX * n) * sizeof(C<T>);
   if (smem > (size_t)max_smem()) return set_err(c, FBSE_ERR_UNSUPPORTED, "FFT axis too long for shared memory");
   const long grid = nouter * nxt;
-  KinArgs ka{c->k2x, c->k2y, c->k2z, c->kemax_scaled, kq, c->nx, c->nx * c->ny};
+  KinArgs ka{c->k2x, c->k2y, c->k2z, c->k2xf, c->k2yf, c->k2zf, c->kemax_scaled, kq, c->nx, c->nx * c->ny};
   if (kmul) {
     FBSE_CUDA(c, cudaFuncSetAttribute(k_fft_cols<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_fft_cols<T, true><<<grid, 256, smem, c->stream>>>(data, st, roots<T>(p), es, (int)c->nx, TX, nxt, cnt, s1, s2,
@@ -660,7 +672,7 @@ static int launch_cols_fast_n(fbse_ctx *c, C<T> *data, long nblk, int axis, bool
   const size_t smem = Cfg::smem();
   const long grid = nouter * nxt;
   const C<T> *rt = roots<T>(c->ax[axis]);
-  KinArgs ka{c->k2x, c->k2y, c->k2z, c->kemax_scaled, kq, c->nx, c->nx * c->ny};
+  KinArgs ka{c->k2x, c->k2y, c->k2z, c->k2xf, c->k2yf, c->k2zf, c->kemax_scaled, kq, c->nx, c->nx * c->ny};
   if (kmul) {
     FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_cols_fast<T, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));

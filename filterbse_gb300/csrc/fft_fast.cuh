@@ -202,7 +202,9 @@ __global__ void __launch_bounds__(PlaneCfg<T, N>::THREADS, 1)
 #pragma unroll
       for (int k2 = 0; k2 < P; k2++) S[(ct + P * j + Q * k2) * PITCH + cc] = v[j * P + k2];
     __syncthreads();
-    // rows, inverse, with the epilogue
+    // rows, inverse, with the epilogue (a plane lies inside one block: one
+    // modulo gives its offset in the potential)
+    const long pbase = base % ngrid;
     C<T> *row = S + rr * PITCH;
 #pragma unroll
     for (int m = 0; m < Q; m++) v[m] = row[rt + P * m];
@@ -214,11 +216,12 @@ __global__ void __launch_bounds__(PlaneCfg<T, N>::THREADS, 1)
     for (int j = 0; j < Q / P; j++)
 #pragma unroll
       for (int k2 = 0; k2 < P; k2++) {
-        const long g = base + (long)rr * N + rt + P * j + Q * k2;
+        const long o = (long)rr * N + rt + P * j + Q * k2;
+        const long g = base + o;
         C<T> r = v[j * P + k2];
         const C<T> ph = phi[g];
         if (pot) {
-          const T V = pot[g % ngrid];
+          const T V = pot[pbase + o];
           r.x += V * ph.x;
           r.y += V * ph.y;
         }
@@ -284,9 +287,7 @@ __global__ void __launch_bounds__(ColsCfg<T, N>::THREADS)
           const double2 q = ka.kq[(long)k * ka.nxy + (long)jy * ka.nx + x];
           v[j * P + k2] = cmul<T>(v[j * P + k2], mk<T>((T)q.x, (T)q.y));
         } else {
-          double kk = ka.k2x[x] + ka.k2y[jy] + ka.k2z[k];
-          if (kk > ka.kemax) kk = ka.kemax;
-          v[j * P + k2] = cscale<T>(v[j * P + k2], (T)kk);
+          v[j * P + k2] = cscale<T>(v[j * P + k2], kin_factor<T>(ka, x, jy, k));
         }
       }
     tinner_p<T, N, true>(v, t, tw2);
@@ -338,6 +339,7 @@ __global__ void __launch_bounds__(256)
   const long line = (long)blockIdx.x * Cfg::LINES + li;
   const bool act = line < nlines;  // a tail line repeats line 0 and stores nothing
   const long off = (act ? line : 0) * N;
+  const long pbase = EPI == 1 ? off % ngrid : 0;  // a line lies inside one block
   C<T> v[Q];
 #pragma unroll
   for (int m = 0; m < Q; m++) v[m] = in[off + t + P * m];
@@ -355,13 +357,14 @@ __global__ void __launch_bounds__(256)
   for (int j = 0; j < Q / P; j++)
 #pragma unroll
     for (int k2 = 0; k2 < P; k2++) {
-      const long g = off + t + P * j + Q * k2;
+      const long o = t + P * j + Q * k2;
+      const long g = off + o;
       C<T> r = v[j * P + k2];
       if (!act) continue;
       if (EPI == 1) {
         const C<T> ph = phi[g];
         if (pot) {
-          const T V = pot[g % ngrid];
+          const T V = pot[pbase + o];
           r.x += V * ph.x;
           r.y += V * ph.y;
         }

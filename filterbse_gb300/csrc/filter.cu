@@ -99,62 +99,92 @@ int unpack_states(fbse_ctx *c, const void *src, double *dst, long ndst)
 // ---------------------------------------------------------------------------
 // K-blocked Newton accumulation into the psi_rank layout
 // F[start][t] (+)= sum_q a[t][j0+q] * ring[(j0+q) % K][w]
+// M: the number of targets rounded up to 4, 8, 16 or 32 (compile time).
+// The in-block sums run in the working precision T (FP32 on the mixed path)
+// and each block's sum is added to the FP64 accumulator, so a larger ring (K
+// up to 128 slots) means fewer FP64 read-modify-write passes over F.
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(256) k_newton_acc(const C<T> *__restrict__ ring, long K, long j0, int nk,
+constexpr int kMaxRing = 128;
+
+template <typename T, int M>
+__global__ void __launch_bounds__(256) k_newton_acc(const C<T> *__restrict__ ring, long j0, int nk,
                                                    const double *__restrict__ a, long ncheby, int m,
                                                    double *__restrict__ F, long nstart, long nw, long len, int cplx,
                                                    int init)
 {
-  // The in-block sums run in the working precision T (FP32 on the mixed path:
-  // the FP64 pipe of this part is a small fraction of its FP32 rate), and
-  // each block's sum is added to the FP64 accumulator.
-  __shared__ T as[kMaxTargets * 64];
-  for (int i = threadIdx.x; i < m * nk; i += blockDim.x) {
-    const int t = i / nk, q = i % nk;
-    as[t * nk + q] = (T)a[t * ncheby + j0 + q];
+  __shared__ T as[kMaxRing * M];  // as[q * M + t]
+  for (int i = threadIdx.x; i < nk * M; i += blockDim.x) {
+    const int q = i / M, t = i % M;
+    as[i] = t < m ? (T)a[t * ncheby + j0 + q] : T(0);
   }
   __syncthreads();
   const long slot_stride = nw * len;
-  const long total = nw * len;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const long w = i / len, k = i - w * len;
-    T ar[kMaxTargets], ai[kMaxTargets];
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < slot_stride; i += (long)gridDim.x * blockDim.x) {
+    T ar[M], ai[M];
 #pragma unroll
-    for (int t = 0; t < kMaxTargets; t++) { ar[t] = T(0); ai[t] = T(0); }
+    for (int t = 0; t < M; t++) { ar[t] = T(0); ai[t] = T(0); }
+    // j0 is a multiple of the ring length: term j0 + q sits in slot q
+#pragma unroll 4
     for (int q = 0; q < nk; q++) {
-      const long slot = (j0 + q) % K;
-      const C<T> v = ring[slot * slot_stride + i];
+      const C<T> v = ring[(long)q * slot_stride + i];
+      const T *cq = as + q * M;
 #pragma unroll
-      for (int t = 0; t < kMaxTargets; t++) {
-        if (t < m) {
-          const T co = as[t * nk + q];
-          ar[t] += co * v.x;
-          ai[t] += co * v.y;
-        }
+      for (int t = 0; t < M; t++) {
+        ar[t] += cq[t] * v.x;
+        ai[t] += cq[t] * v.y;
       }
     }
+    const long w = i / len, k = i - w * len;
     // psi_rank layout: ns_block = jns*m*stlen, jstate = ns_block + t*stlen
 #pragma unroll
-    for (int t = 0; t < kMaxTargets; t++) {
-      if (t < m) {
-        if (cplx) {
-          double *d = F + ((w * m + t) * len + k) * 2;
-          if (init) { d[0] = ar[t]; d[1] = ai[t]; }
-          else { d[0] += ar[t]; d[1] += ai[t]; }
-        } else {
-          double *d0 = F + ((2 * w) * m + t) * len + k;
-          if (init) d0[0] = ar[t];
-          else d0[0] += ar[t];
-          if (2 * w + 1 < nstart) {
-            double *d1 = F + ((2 * w + 1) * m + t) * len + k;
-            if (init) d1[0] = ai[t];
-            else d1[0] += ai[t];
-          }
+    for (int t = 0; t < M; t++) {
+      if (t >= m) break;
+      if (cplx) {
+        double2 *d = reinterpret_cast<double2 *>(F) + (w * m + t) * len + k;
+        double2 o = init ? make_double2(0.0, 0.0) : *d;
+        o.x += (double)ar[t];
+        o.y += (double)ai[t];
+        *d = o;
+      } else {
+        double *d0 = F + ((2 * w) * m + t) * len + k;
+        *d0 = (init ? 0.0 : *d0) + (double)ar[t];
+        if (2 * w + 1 < nstart) {
+          double *d1 = F + ((2 * w + 1) * m + t) * len + k;
+          *d1 = (init ? 0.0 : *d1) + (double)ai[t];
         }
       }
     }
   }
+}
+
+template <typename T>
+static int launch_newton_acc(fbse_ctx *c, const C<T> *ring, long j0, int nk, const double *a, long ncheby, int m,
+                             double *F, long nstart, long nw, long len)
+{
+  const unsigned g = grid_for(nw * len);
+  const int cp = c->is_complex, init = j0 == 0;
+  if (m <= 4) k_newton_acc<T, 4><<<g, 256, 0, c->stream>>>(ring, j0, nk, a, ncheby, m, F, nstart, nw, len, cp, init);
+  else if (m <= 8) k_newton_acc<T, 8><<<g, 256, 0, c->stream>>>(ring, j0, nk, a, ncheby, m, F, nstart, nw, len, cp, init);
+  else if (m <= 16) k_newton_acc<T, 16><<<g, 256, 0, c->stream>>>(ring, j0, nk, a, ncheby, m, F, nstart, nw, len, cp, init);
+  else k_newton_acc<T, 32><<<g, 256, 0, c->stream>>>(ring, j0, nk, a, ncheby, m, F, nstart, nw, len, cp, init);
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+// ring length: up to 128 slots within 40% of the free device memory
+// (FBSE_NEWTON_RING overrides), at most ncheby
+static long ring_slots(long ncheby, size_t slot_bytes)
+{
+  long K = kMaxRing;
+  const char *e = getenv("FBSE_NEWTON_RING");
+  if (e && atol(e) > 0) K = atol(e) < kMaxRing ? atol(e) : kMaxRing;
+  size_t free_b = 0, tot_b = 0;
+  if (cudaMemGetInfo(&free_b, &tot_b) != cudaSuccess) {
+    cudaGetLastError();
+    free_b = 0;
+  }
+  while (K > 8 && (double)K * slot_bytes > 0.4 * (double)free_b) K /= 2;
+  return ncheby < K ? ncheby : K;
 }
 
 template <typename T>
@@ -163,7 +193,7 @@ static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long
 {
   const long len = (long)c->nspin * c->ngrid;
   const long nw = c->is_complex ? nstart : (nstart + 1) / 2;
-  const long K = ncheby < 32 ? ncheby : 32;
+  const long K = ring_slots(ncheby, (size_t)nw * len * sizeof(C<T>));
   // Newton coefficients: real parts only (gen_newton_coeff's are real)
   std::vector<double> are((size_t)m * ncheby);
   for (long t = 0; t < m; t++)
@@ -198,9 +228,7 @@ static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long
       if ((jc % K) == K - 1 || jc == ncheby - 1) {
         const long j0 = jc - (jc % K);
         const int nk = (int)(jc - j0 + 1);
-        FBSE_COUNT(1); k_newton_acc<T><<<grid_for(nw * len), 256, 0, c->stream>>>(ring, K, j0, nk, a_dev, ncheby, (int)m, filtered,
-                                                                   nstart, nw, len, c->is_complex, j0 == 0);
-        if (cudaGetLastError() != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "newton accumulation launch"); break; }
+        if ((rc = launch_newton_acc<T>(c, ring, j0, nk, a_dev, ncheby, (int)m, filtered, nstart, nw, len))) break;
       }
     }
     if (rc) break;

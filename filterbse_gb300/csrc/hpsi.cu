@@ -7,13 +7,15 @@
 //   c[p][j'] = dv sum_pts b_p(r) conj(Y_m'(r)) psi_s'(r),   j' = 3 s' + m'
 // and scatters b_p(r) Y_m(r) sum_j' LS[j'][j] c[p][j'] into spin s of the
 // output (SO); the NL operator is the same with b^NL_p, a sign per channel and
-// no spin mixing.  Here one CTA per (atom, channel, group of 4 states) gathers
-// the 30 coefficients of each state in one warp (register accumulation, warp
-// reduction) -- the 4 warps share every table entry through L1, so the table
-// is read once per 4 states -- and applies L.S (or the NL sign).  The scatter
-// kernel has the same shape and adds the contribution with atomics
-// (overlapping spheres of neighbouring atoms make it a reduction; the
-// reference uses "omp atomic" for the same reason, phamiltonian.c:295-303).
+// no spin mixing.  Here one CTA per (atom, channel, group of states) gathers
+// the coefficients with one warp per (state, spin) (register accumulation,
+// warp reduction; the warps of a CTA share every table entry through L1) and
+// applies L.S (or the NL sign).  The scatter kernel runs one warp per state
+// and adds the contribution with atomics (overlapping spheres of neighbouring
+// atoms make it a reduction; the reference uses "omp atomic" for the same
+// reason, phamiltonian.c:295-303).
+#include <cstdlib>
+
 #include "fbse_internal.cuh"
 
 namespace fbse {
@@ -38,12 +40,16 @@ template <> ProjView<float> view<float>(fbse_ctx *c)
   return {p.nl_cnt, p.jxyz, p.sgn, p.y1f, p.sopf, p.nlpf, p.LS, p.npts, p.nproj};
 }
 
-constexpr int kSW = 4;              // states (warps) per CTA
+constexpr int kSW = 4;              // warps per CTA
 constexpr int kProjThreads = 32 * kSW;
 constexpr int kNC = 30;             // 5 radial channels x (2 spins x 3 m)
 
-// gather: coef[((st*nat + a)*2 + ch)*30 + p*6 + j]
-template <typename T>
+// gather: one warp per (state, spin s'); each lane accumulates the 15
+// coefficients b_p conj(Y_m) psi_s' of its points, kGU points per iteration so
+// that the dependent loads (grid index, then psi) of several points are in
+// flight together.  Then L.S (or the NL sign) per state:
+//   coef[((st*nat + a)*2 + ch)*30 + p*6 + j]
+template <typename T, int kGU>
 __global__ void __launch_bounds__(kProjThreads) k_proj_gather(const C<T> *__restrict__ psi, C<T> *__restrict__ coef,
                                                               ProjView<T> pv, long nat, long nstates, long ngrid,
                                                               int nspin, int ch0, double dv)
@@ -51,91 +57,100 @@ __global__ void __launch_bounds__(kProjThreads) k_proj_gather(const C<T> *__rest
   const long a = blockIdx.x;
   const int ch = ch0 + blockIdx.y;  // 0: SO, 1: NL
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const long st = (long)blockIdx.z * kSW + wid;
+  const int spc = kSW / nspin;  // states per CTA
+  const long st = (long)blockIdx.z * spc + wid / nspin;
+  const int sp = wid % nspin;
   const bool live = st < nstates;
   const int np = pv.cnt[a];
-  const C<T> *ps = psi + (live ? st : 0) * nspin * ngrid;
+  const C<T> *ps = psi + (live ? st : 0) * nspin * ngrid + (long)sp * ngrid;
   const T *rad = (ch == 0) ? pv.sop : pv.nlp;
-  T acc[2 * kNC];
+  const int npj = pv.nproj;
+  T acc[30];
 #pragma unroll
-  for (int i = 0; i < 2 * kNC; i++) acc[i] = T(0);
+  for (int i = 0; i < 30; i++) acc[i] = T(0);
   if (live) {
-    for (int g = lane; g < np; g += 32) {
-      const long e = a * pv.npts + g;
-      const int jx = pv.jxyz[e];
-      T yr[3], yi[3], b[5];
+    for (int g0 = lane; g0 < np; g0 += 32 * kGU) {
+      int jx[kGU];
+      long e[kGU];
 #pragma unroll
-      for (int m = 0; m < 3; m++) { yr[m] = pv.y1[e * 6 + 2 * m]; yi[m] = pv.y1[e * 6 + 2 * m + 1]; }
+      for (int u = 0; u < kGU; u++) {
+        const int g = g0 + 32 * u;
+        e[u] = a * pv.npts + (g < np ? g : 0);
+        jx[u] = g < np ? pv.jxyz[e[u]] : -1;
+      }
+      C<T> v[kGU];
 #pragma unroll
-      for (int p = 0; p < 5; p++) b[p] = (p < pv.nproj) ? rad[e * pv.nproj + p] : T(0);
+      for (int u = 0; u < kGU; u++) v[u] = jx[u] >= 0 ? ps[jx[u]] : mk<T>(T(0), T(0));
 #pragma unroll
-      for (int s = 0; s < 2; s++) {
-        if (s < nspin) {
-          const C<T> v = ps[s * ngrid + jx];
+      for (int u = 0; u < kGU; u++) {
+        if (jx[u] < 0) continue;
+        T b[5];
 #pragma unroll
-          for (int m = 0; m < 3; m++) {
-            // psi * conj(Y)
-            const T tr = v.x * yr[m] + v.y * yi[m];
-            const T ti = v.y * yr[m] - v.x * yi[m];
+        for (int p = 0; p < 5; p++) b[p] = (p < npj) ? rad[e[u] * npj + p] : T(0);
 #pragma unroll
-            for (int p = 0; p < 5; p++) {
-              acc[2 * (p * 6 + s * 3 + m)] += b[p] * tr;
-              acc[2 * (p * 6 + s * 3 + m) + 1] += b[p] * ti;
-            }
+        for (int m = 0; m < 3; m++) {
+          const T yr = pv.y1[e[u] * 6 + 2 * m], yi = pv.y1[e[u] * 6 + 2 * m + 1];
+          // psi * conj(Y)
+          const T tr = v[u].x * yr + v[u].y * yi;
+          const T ti = v[u].y * yr - v[u].x * yi;
+#pragma unroll
+          for (int p = 0; p < 5; p++) {
+            acc[2 * (p * 3 + m)] += b[p] * tr;
+            acc[2 * (p * 3 + m) + 1] += b[p] * ti;
           }
         }
       }
     }
   }
-  __shared__ C<T> cf[kSW][kNC];
 #pragma unroll
-  for (int i = 0; i < 2 * kNC; i++) {
-    T v = acc[i];
+  for (int i = 0; i < 30; i++) {
+    T x = acc[i];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    acc[i] = v;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    acc[i] = x;
   }
+  __shared__ C<T> cf[kSW][15];
   if (lane == 0) {
 #pragma unroll
-    for (int i = 0; i < kNC; i++) cf[wid][i] = mk<T>(acc[2 * i] * (T)dv, acc[2 * i + 1] * (T)dv);
+    for (int i = 0; i < 15; i++) cf[wid][i] = mk<T>(acc[2 * i] * (T)dv, acc[2 * i + 1] * (T)dv);
   }
-  __syncwarp();
-  if (live && lane < kNC) {
-    const int p = lane / 6, j = lane % 6;
+  __syncthreads();
+  for (int o = threadIdx.x; o < spc * kNC; o += blockDim.x) {
+    const int ls = o / kNC, q = o % kNC;
+    const long sg = (long)blockIdx.z * spc + ls;
+    if (sg >= nstates) continue;
+    const int p = q / 6, j = q % 6;
     C<T> d = mk<T>(0, 0);
     if (ch == 0) {
-      // d[p][j] = sum_j' LS[j'][j] c[p][j']   (phamiltonian.c:249-290)
-      for (int jp = 0; jp < 6; jp++) {
+      // d[p][j] = sum_j' LS[j'][j] c[p][j'], j' = 3 s' + m'   (phamiltonian.c:249-290)
+      for (int jp = 0; jp < 3 * nspin; jp++) {
         const double2 l = pv.LS[jp * 6 + j];
-        const C<T> cc = cf[wid][p * 6 + jp];
+        const C<T> cc = cf[ls * nspin + jp / 3][p * 3 + jp % 3];
         d.x += (T)l.x * cc.x - (T)l.y * cc.y;
         d.y += (T)l.x * cc.y + (T)l.y * cc.x;
       }
-    } else {
+    } else if (j / 3 < nspin) {
       // sign of the channel (phamiltonian.c:399-401), block diagonal in spin
-      const T sg = (p < pv.nproj) ? (T)pv.sgn[a * pv.nproj + p] : T(0);
-      d = cscale<T>(cf[wid][lane], sg);
+      const T sgn = (p < npj) ? (T)pv.sgn[a * npj + p] : T(0);
+      d = cscale<T>(cf[ls * nspin + j / 3][p * 3 + j % 3], sgn);
     }
-    coef[((st * nat + a) * 2 + ch) * kNC + lane] = d;
+    coef[((sg * nat + a) * 2 + ch) * kNC + q] = d;
   }
 }
 
-__device__ __forceinline__ void atomic_add_c(float2 *p, float2 v)
-{
-  atomicAdd(&p->x, v.x);
-  atomicAdd(&p->y, v.y);
-}
+__device__ __forceinline__ void atomic_add_c(float2 *p, float2 v) { atomicAdd(p, v); }
 __device__ __forceinline__ void atomic_add_c(double2 *p, double2 v)
 {
   atomicAdd(&p->x, v.x);
   atomicAdd(&p->y, v.y);
 }
 
-// scatter: out_s(r) += scale * sum_p b_p(r) sum_m Y_m(r) d[p][3 s + m] over the active channels
-template <typename T>
+// scatter: out_s(r) += scale * sum_m Y_m(r) sum_p b_p(r) d[p][3 s + m] over the
+// active channels; one warp per state, kSU points per lane per iteration
+template <typename T, bool SO, bool NL, int kSU>
 __global__ void __launch_bounds__(kProjThreads) k_proj_scatter(C<T> *__restrict__ out, const C<T> *__restrict__ coef,
                                                                ProjView<T> pv, long nat, long nstates, long ngrid,
-                                                               int nspin, int use_so, int use_nl, T scale)
+                                                               int nspin, T scale)
 {
   const long a = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -147,32 +162,52 @@ __global__ void __launch_bounds__(kProjThreads) k_proj_scatter(C<T> *__restrict_
   __syncwarp();
   if (st >= nstates) return;
   const int np = pv.cnt[a];
+  const int npj = pv.nproj;
   C<T> *po = out + st * nspin * ngrid;
-  for (int g = lane; g < np; g += 32) {
-    const long e = a * pv.npts + g;
-    const int jx = pv.jxyz[e];
-    T yr[3], yi[3];
+  for (int g0 = lane; g0 < np; g0 += 32 * kSU) {
+    int jx[kSU];
+    long e[kSU];
 #pragma unroll
-    for (int m = 0; m < 3; m++) { yr[m] = pv.y1[e * 6 + 2 * m]; yi[m] = pv.y1[e * 6 + 2 * m + 1]; }
-    for (int s = 0; s < nspin; s++) {
-      T vr = 0, vi = 0;
-      for (int ch = 0; ch < 2; ch++) {
-        if ((ch == 0 && !use_so) || (ch == 1 && !use_nl)) continue;
-        const T *rad = (ch == 0) ? pv.sop : pv.nlp;
-        for (int p = 0; p < pv.nproj; p++) {
-          const T b = rad[e * pv.nproj + p];
-          T sr = 0, si = 0;
+    for (int u = 0; u < kSU; u++) {
+      const int g = g0 + 32 * u;
+      e[u] = a * pv.npts + (g < np ? g : 0);
+      jx[u] = g < np ? pv.jxyz[e[u]] : -1;
+    }
 #pragma unroll
-          for (int m = 0; m < 3; m++) {
-            const C<T> q = d[wid][ch][p * 6 + s * 3 + m];
-            sr += yr[m] * q.x - yi[m] * q.y;
-            si += yr[m] * q.y + yi[m] * q.x;
-          }
-          vr += b * sr;
-          vi += b * si;
-        }
+    for (int u = 0; u < kSU; u++) {
+      if (jx[u] < 0) continue;
+      T yr[3], yi[3];
+#pragma unroll
+      for (int m = 0; m < 3; m++) { yr[m] = pv.y1[e[u] * 6 + 2 * m]; yi[m] = pv.y1[e[u] * 6 + 2 * m + 1]; }
+      T bs[5], bn[5];
+#pragma unroll
+      for (int p = 0; p < 5; p++) {
+        bs[p] = (SO && p < npj) ? pv.sop[e[u] * npj + p] : T(0);
+        bn[p] = (NL && p < npj) ? pv.nlp[e[u] * npj + p] : T(0);
       }
-      atomic_add_c(&po[s * ngrid + jx], mk<T>(scale * vr, scale * vi));
+      for (int s = 0; s < nspin; s++) {
+        T vr = 0, vi = 0;
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+          T qr = 0, qi = 0;  // sum_p b_p d[p][3 s + m]
+#pragma unroll
+          for (int p = 0; p < 5; p++) {
+            if (SO) {
+              const C<T> q = d[wid][0][p * 6 + s * 3 + m];
+              qr += bs[p] * q.x;
+              qi += bs[p] * q.y;
+            }
+            if (NL) {
+              const C<T> q = d[wid][1][p * 6 + s * 3 + m];
+              qr += bn[p] * q.x;
+              qi += bn[p] * q.y;
+            }
+          }
+          vr += yr[m] * qr - yi[m] * qi;
+          vi += yr[m] * qi + yi[m] * qr;
+        }
+        atomic_add_c(&po[s * ngrid + jx[u]], mk<T>(scale * vr, scale * vi));
+      }
     }
   }
 }
@@ -187,20 +222,40 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   if (rc) return rc;
   C<T> *coef = reinterpret_cast<C<T> *>(c->coef);
   const long ngroups = (nstates + kSW - 1) / kSW;
-  if (ngroups > 65535 || p.nat > 2147483647L) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector grid too large");
+  const long spc = kSW / c->nspin;
+  const long ggroups = (nstates + spc - 1) / spc;
+  if (ggroups > 65535 || p.nat > 2147483647L) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector grid too large");
   const int ch0 = c->so ? 0 : 1;
   const int nch = (c->so ? 1 : 0) + (c->nl ? 1 : 0);
-  if (!c->so || !c->nl) {
-    // zero the inactive channel so the scatter can skip it cheaply
-    FBSE_CUDA(c, cudaMemsetAsync(coef, 0, need, c->stream));
-  }
-  dim3 gg((unsigned)p.nat, (unsigned)nch, (unsigned)ngroups);
-  k_proj_gather<T><<<gg, kProjThreads, 0, c->stream>>>(in, coef, view<T>(c), p.nat, nstates, c->ngrid, c->nspin, ch0,
-                                                       c->dv);
+  // points per lane per iteration (memory-level parallelism of the dependent
+  // index -> psi loads): FBSE_PROJ_UNROLL=8 doubles both kernels' default
+  static const int wide = getenv("FBSE_PROJ_UNROLL") && atoi(getenv("FBSE_PROJ_UNROLL")) >= 8;
+  dim3 gg((unsigned)p.nat, (unsigned)nch, (unsigned)ggroups);
+  if (wide)
+    k_proj_gather<T, 8><<<gg, kProjThreads, 0, c->stream>>>(in, coef, view<T>(c), p.nat, nstates, c->ngrid, c->nspin,
+                                                            ch0, c->dv);
+  else
+    k_proj_gather<T, 4><<<gg, kProjThreads, 0, c->stream>>>(in, coef, view<T>(c), p.nat, nstates, c->ngrid, c->nspin,
+                                                            ch0, c->dv);
   FBSE_CHECK_LAUNCH(c);
   dim3 gs((unsigned)p.nat, (unsigned)ngroups);
-  k_proj_scatter<T><<<gs, kProjThreads, 0, c->stream>>>(out, coef, view<T>(c), p.nat, nstates, c->ngrid, c->nspin,
-                                                        c->so, c->nl, (T)scale);
+  const ProjView<T> pv = view<T>(c);
+  const T sc = (T)scale;
+  if (wide) {
+    if (c->so && c->nl)
+      k_proj_scatter<T, true, true, 4><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+    else if (c->so)
+      k_proj_scatter<T, true, false, 4><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+    else
+      k_proj_scatter<T, false, true, 4><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+  } else {
+    if (c->so && c->nl)
+      k_proj_scatter<T, true, true, 2><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+    else if (c->so)
+      k_proj_scatter<T, true, false, 2><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+    else
+      k_proj_scatter<T, false, true, 2><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+  }
   FBSE_CHECK_LAUNCH(c);
   return FBSE_OK;
 }
