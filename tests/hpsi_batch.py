@@ -1,0 +1,35 @@
+"""One batched H psi on the benchmark workload (3 nm CdSe spinor dot, 128^3,
+spin-orbit projectors, 16 seeded random starts), run three times.
+
+This is the program the per-kernel ncu captures under profiles/ profile
+(`python tests/hpsi_batch.py [mixed|fp64] [so|noso]`); pytest does not
+collect it.  It needs a GPU and the built library."""
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+
+def main():
+    import torch
+    import filterbse_gb300 as F
+    from filterbse_gb300 import workload as W
+    prec = F.FP64 if "fp64" in sys.argv[1:] else F.MIXED
+    so = "noso" not in sys.argv[1:]
+    dot = W.cdse_dot(15.0, d=0.5, ke_max=10.0, spinor=True)
+    g = dot.grid
+    c = F.Context(g, dot.pot, nspin=2, is_complex=True, so=so, nl=False, proj=dot.proj if so else None,
+                  precision=prec)
+    starts, _, _ = F.init_filter_states(16, g.ngrid, 2, True, g.dv, -777)
+    dt = torch.complex64 if prec == F.MIXED else torch.complex128
+    x = torch.tensor(starts.view(np.complex128), dtype=dt, device="cuda:0")
+    y = torch.empty_like(x)
+    for _ in range(3):
+        c.hpsi(x, y)
+    print("H psi batch done:", g.nx, g.ny, g.nz, "FP64" if prec == F.FP64 else "mixed", "SO" if so else "no SO")
+
+
+if __name__ == "__main__":
+    main()
