@@ -12,7 +12,7 @@ ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfbse_gpu.so")
 CU_SOURCES = ["fft.cu", "hpsi.cu", "filter.cu", "linalg.cu", "bse.cu", "setup.cu", "job.cu", "api.cu"]
-C_SOURCES = ["host/fbse_host.c"]
+C_SOURCES = ["host/fbse_host.c", "host/fbse_setup.c"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]

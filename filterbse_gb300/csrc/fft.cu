@@ -647,11 +647,42 @@ static int launch_plane_fast_n(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk
   return FBSE_OK;
 }
 
+// the two-CTA cluster variant (FBSE_FFT_CLUSTER=1) of the 128 x 128 FP32 plane
+template <typename T, int N>
+static int launch_plane_cl_n(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int mode, const C<T> *phi,
+                             const T *pot, T ca, T cb)
+{
+  using Cfg = fast::ClCfg<T, N>;
+  const size_t smem = Cfg::smem();
+  const long grid = 2 * nblk * c->nz;
+  const C<T> *rt = roots<T>(c->ax[0]);
+  if (mode == 0) {
+    FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_plane_cl<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fast::k_plane_cl<T, N, 0><<<grid, Cfg::THREADS, smem, c->stream>>>(in, out, rt, nullptr, nullptr, c->ngrid, T(1),
+                                                                        T(0));
+  } else {
+    FBSE_CUDA(c, cudaFuncSetAttribute(fast::k_plane_cl<T, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fast::k_plane_cl<T, N, 1><<<grid, Cfg::THREADS, smem, c->stream>>>(in, out, rt, phi, pot, c->ngrid, ca, cb);
+  }
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+static bool plane_cluster_on()
+{
+  static int v = -1;
+  if (v < 0) v = getenv("FBSE_FFT_CLUSTER") != nullptr && atoi(getenv("FBSE_FFT_CLUSTER")) == 1;
+  return v == 1;
+}
+
 template <typename T>
 static int launch_plane_fast(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int mode, const C<T> *phi,
                              const T *pot, T ca, T cb)
 {
   if (c->nx == 64) return launch_plane_fast_n<T, 64>(c, in, out, nblk, mode, phi, pot, ca, cb);
+  if constexpr (sizeof(C<T>) == 8) {
+    if (c->nx == 128 && plane_cluster_on()) return launch_plane_cl_n<T, 128>(c, in, out, nblk, mode, phi, pot, ca, cb);
+  }
   if constexpr (sizeof(C<T>) == 8) {
     if (c->nx == 128) return launch_plane_fast_n<T, 128>(c, in, out, nblk, mode, phi, pot, ca, cb);
   }

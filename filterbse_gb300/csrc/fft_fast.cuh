@@ -240,11 +240,14 @@ __global__ void __launch_bounds__(PlaneCfg<T, N>::THREADS, 1)
 template <typename T, int N> struct ColsCfg {
   static constexpr int P = Shape<N>::P, Q = Shape<N>::Q;
   static constexpr int THREADS = 32 * P;
+  // FP32 with 8 warps: ask for 3 CTAs per SM (24 warps) instead of the 2 that
+  // the unconstrained register count allows
+  static constexpr int MINB = (sizeof(T) == 4 && THREADS == 256) ? 3 : 1;
   static constexpr size_t smem() { return (size_t)(N + 32 * N) * sizeof(C<T>); }
 };
 
 template <typename T, int N, bool KMUL>
-__global__ void __launch_bounds__(ColsCfg<T, N>::THREADS)
+__global__ void __launch_bounds__(ColsCfg<T, N>::THREADS, ColsCfg<T, N>::MINB)
     k_cols_fast(C<T> *__restrict__ data, const C<T> *__restrict__ roots, long es, int nxc, int nxt, long cnt,
                 long s1, long s2, bool inv, KinArgs ka)
 {
@@ -372,6 +375,139 @@ __global__ void __launch_bounds__(256)
       }
       out[g] = r;
     }
+}
+
+}  // namespace fast
+}  // namespace fbse
+
+#include <cooperative_groups.h>
+
+namespace fbse {
+namespace fast {
+
+// ---------------------------------------------------------------------------
+// plane pass split over a cluster of two CTAs (two SMs), each holding half
+// of the plane's rows in its shared memory: half the footprint of the
+// one-CTA plane kernel, so two clusters share an SM and one's loads overlap
+// the other's arithmetic.  Rows are transformed where they live; the column
+// phase of CTA q covers columns [N/2 q, N/2 (q+1)) and reads the other half
+// of each column from the partner's shared memory.
+// ---------------------------------------------------------------------------
+template <typename T, int N> struct ClCfg {
+  static constexpr int P = Shape<N>::P, Q = Shape<N>::Q;
+  static constexpr int HR = N / 2;                 // rows per CTA
+  static constexpr int PITCH = N + 8;
+  static constexpr int THREADS = HR * P;           // row phase: P threads per row
+  static constexpr int CW = HR;                    // columns per CTA
+  static constexpr size_t smem() { return (size_t)(N + HR * PITCH) * sizeof(C<T>); }
+};
+
+template <typename T, int N, int MODE>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(ClCfg<T, N>::THREADS, 2)
+    k_plane_cl(const C<T> *__restrict__ in, C<T> *__restrict__ out, const C<T> *__restrict__ roots,
+               const C<T> *__restrict__ phi, const T *__restrict__ pot, long ngrid, T ca, T cb)
+{
+  using Cfg = ClCfg<T, N>;
+  constexpr int P = Cfg::P, Q = Cfg::Q, PITCH = Cfg::PITCH, HR = Cfg::HR, CW = Cfg::CW;
+  namespace cgr = cooperative_groups;
+  cgr::cluster_group cluster = cgr::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C<T> *tw2 = reinterpret_cast<C<T> *>(smem_raw);
+  C<T> *H = tw2 + N;  // HR rows x PITCH; reused as the column slots S2[slot * CW + c]
+  const unsigned q = cluster.block_rank();
+  C<T> *const Hp = cluster.map_shared_rank(H, 1 - q);
+  C<T> *const H0 = q == 0 ? H : Hp;  // rows [0, N/2)
+  C<T> *const H1 = q == 0 ? Hp : H;  // rows [N/2, N)
+  load_tw2<T, N>(tw2, roots);
+  const long base = (long)(blockIdx.x / 2) * N * N;
+  const int rr = threadIdx.x / P, rt = threadIdx.x % P;        // row phase: local row, thread in row
+  const int cw = threadIdx.x >> 5;
+  const int ct = cw % P, cl = (cw / P) * 32 + (threadIdx.x & 31);  // column phase: thread in column, local column
+  const int cgl = (int)q * CW + cl;                            // global column
+  C<T> v[Q];
+  __syncthreads();
+  if (MODE == 0) {
+    // rows N/2 q + rr, forward
+    const long rbase = base + (long)((int)q * HR + rr) * N;
+#pragma unroll
+    for (int m = 0; m < Q; m++) v[m] = in[rbase + rt + P * m];
+    inner_q<T, N, false>(v, rt, tw2);
+    C<T> *row = H + rr * PITCH;
+    row_exchange<T, N>(row, v, rt);
+    outer_p<T, N, false>(v);
+#pragma unroll
+    for (int j = 0; j < Q / P; j++)
+#pragma unroll
+      for (int k2 = 0; k2 < P; k2++) row[rt + P * j + Q * k2] = v[j * P + k2];
+    cluster.sync();
+    // columns, forward: rows R = ct + P m from the CTA that holds them
+#pragma unroll
+    for (int m = 0; m < Q; m++) {
+      const int R = ct + P * m;
+      v[m] = (R < HR ? H0 : H1)[(R % HR) * PITCH + cgl];
+    }
+    inner_q<T, N, false>(v, ct, tw2);
+    cluster.sync();  // the partner has read its half of every column
+#pragma unroll
+    for (int k1 = 0; k1 < Q; k1++) H[(k1 * P + ct) * CW + cl] = v[k1];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < Q / P; j++)
+#pragma unroll
+      for (int s = 0; s < P; s++) v[j * P + s] = H[((ct + P * j) * P + s) * CW + cl];
+    outer_p<T, N, false>(v);
+#pragma unroll
+    for (int j = 0; j < Q / P; j++)
+#pragma unroll
+      for (int k2 = 0; k2 < P; k2++) out[base + (long)(ct + P * j + Q * k2) * N + cgl] = v[j * P + k2];
+  } else {
+    // columns, inverse
+#pragma unroll
+    for (int m = 0; m < Q; m++) v[m] = in[base + (long)(ct + P * m) * N + cgl];
+    inner_q<T, N, true>(v, ct, tw2);
+#pragma unroll
+    for (int k1 = 0; k1 < Q; k1++) H[(k1 * P + ct) * CW + cl] = v[k1];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < Q / P; j++)
+#pragma unroll
+      for (int s = 0; s < P; s++) v[j * P + s] = H[((ct + P * j) * P + s) * CW + cl];
+    outer_p<T, N, true>(v);
+    cluster.sync();  // both CTAs are done with their column slots
+#pragma unroll
+    for (int j = 0; j < Q / P; j++)
+#pragma unroll
+      for (int k2 = 0; k2 < P; k2++) {
+        const int R = ct + P * j + Q * k2;
+        (R < HR ? H0 : H1)[(R % HR) * PITCH + cgl] = v[j * P + k2];
+      }
+    cluster.sync();
+    // rows N/2 q + rr, inverse, with the epilogue
+    const long o0 = (long)((int)q * HR + rr) * N;
+    const long pbase = base % ngrid;
+    C<T> *row = H + rr * PITCH;
+#pragma unroll
+    for (int m = 0; m < Q; m++) v[m] = row[rt + P * m];
+    __syncwarp();
+    inner_q<T, N, true>(v, rt, tw2);
+    row_exchange<T, N>(row, v, rt);
+    outer_p<T, N, true>(v);
+#pragma unroll
+    for (int j = 0; j < Q / P; j++)
+#pragma unroll
+      for (int k2 = 0; k2 < P; k2++) {
+        const long o = o0 + rt + P * j + Q * k2;
+        const long g = base + o;
+        C<T> r = v[j * P + k2];
+        const C<T> ph = phi[g];
+        if (pot) {
+          const T V = pot[pbase + o];
+          r.x += V * ph.x;
+          r.y += V * ph.y;
+        }
+        out[g] = mk<T>(ca * r.x + cb * ph.x, ca * r.y + cb * ph.y);
+      }
+  }
 }
 
 }  // namespace fast

@@ -1,0 +1,74 @@
+/* Host-side setup of the drop-in executables: the reference's input files
+ * (input.par, conf.par, pot<Atm>.par, SO_<Atm>.par), its grid rule, the
+ * spin-orbit / nonlocal projector table, and its output files (eval.dat,
+ * psi.dat, output.dat).  Plain C; the compute runs through libfbse_gpu. */
+#ifndef FBSE_DROPIN_H
+#define FBSE_DROPIN_H
+
+#include <stdio.h>
+
+#define FBSE_PROJ_LEN 1024 /* PROJ_LEN, filter_mpi/fd.h */
+#define FBSE_NPROJ 5       /* ist->nproj default, filter_mpi/read.c:75 */
+#define FBSE_MAX_TYPES 32
+
+/* the subset of filter_mpi/input.par this build runs (read.c:23-112 defaults) */
+typedef struct {
+  long nx, ny, nz;            /* requested minimum grid (0: from the atoms) */
+  double dx, dy, dz;
+  long m_states_per_filter, n_filter_cycles, ncheby;
+  double vbmin, vbmax, cbmin, cbmax;
+  double ke_max, fermi_e, sigma_e_cut;
+  int set_targets;
+  long n_targets_vb, n_targets_cb;
+  int set_seed;
+  long seed;
+  int use_spinors, so, nl, get_all_states, approx_energy_range, precision;
+} fbse_filter_params;
+
+/* the subset of bse_cplx/input.par (bse_cplx/read.c) */
+typedef struct {
+  long max_hole_states, max_elec_states;
+  double sigma_e_cut, eps_x, eps_y, eps_z, fermi_e, delta_e_hole, delta_e_elec;
+  int precision;
+} fbse_bse_params;
+
+/* input.par parsing: returns 0, or -1 with a message in err */
+int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, size_t errlen);
+int fbse_read_bse_params(const char *path, fbse_bse_params *p, char *err, size_t errlen);
+
+/* conf.par: natoms, then "Atm x y z" (bohr); centred (centerConf).  types[i]
+ * indexes names[]; returns 0 or -1. */
+int fbse_read_conf(const char *path, long *natoms, double **xyz, int **types, char names[][8], int *ntypes,
+                   char *err, size_t errlen);
+
+/* two-column table (r, V): returns the number of rows (or -1) */
+long fbse_read_table(const char *path, double **r, double **v);
+
+/* init_grid_params (filter_mpi/init.c:5-255, non-periodic) */
+void fbse_grid_rule(const double *xyz, long natoms, double d, long n_in, int axis, long *n, double *xmin);
+
+/* cumulative-sum coordinates of build_grid_ksqr (init.c:284-290) */
+void fbse_grid_axis(long n, double lo, double d, double *out);
+
+/* R_NLcut2 (read.c:908) */
+double fbse_r_nlcut2(double dx);
+
+/* radial projectors (filter_mpi/projectors.c): SO (kind 0) or NL (kind 1,
+ * lam1 exp(-r^2) + lam2 exp(-(r-1.5)^2)); out [nproj][PROJ_LEN]; sgn (NL)
+ * gets the eigenvalue signs.  Returns 0 or -1. */
+int fbse_radial_projectors(double dx, double rcut, int kind, double lam1, double lam2, int nproj, double *out,
+                           int *sgn);
+
+/* init_NL_projectors table (init.c:848-1135): projector atoms xyz[nat]; so
+ * radial [nproj][N] scaled per atom by sqrt(so_par[a]); nl radial
+ * [nat][nproj][N].  Allocates nl[nat], jxyz, y1, so_p, nl_p with row stride
+ * *npts.  Returns 0 or -1. */
+int fbse_build_nlc(long nx, long ny, long nz, const double *gx, const double *gy, const double *gz, long nat,
+                   const double *xyz, const double *so_par, const double *so_tab, const double *nl_tab, int nproj,
+                   double rcut2, long *npts, long **nl, int **jxyz, double **y1, double **so_p, double **nl_p);
+
+/* outputs (filter_mpi/write.c:263-299, save.c:446-503) */
+int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n);
+int fbse_write_psi(const char *path, const double *psi, long n_doubles);
+
+#endif

@@ -1,0 +1,605 @@
+/* Host-side setup for the drop-in executables (declared in fbse_dropin.h). */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "fbse_dropin.h"
+
+#define FBSE_PI 3.14159265358979323846
+#define FBSE_EPSDX 1.0e-20 /* EPSDX, filter_mpi/fd.h */
+
+static void seterr(char *err, size_t n, const char *msg, const char *what)
+{
+  if (err && n) snprintf(err, n, "%s%s%s", msg, what ? ": " : "", what ? what : "");
+}
+
+/* ---------------------------------------------------------------------------
+ * input.par: "key = value" pairs; a few keys take extra values on the same
+ * line (setTargets 1 nVB nCB, setSeed 1 seed, getAllStates 0 sigmaECut),
+ * read as the reference reads them (fscanf after the pair, read.c:405-439).
+ * ------------------------------------------------------------------------- */
+static int parse_long(const char *s, long *v)
+{
+  char *e;
+  *v = strtol(s, &e, 10);
+  return *e == '\0' ? 0 : -1;
+}
+static int parse_double(const char *s, double *v)
+{
+  char *e;
+  *v = strtod(s, &e);
+  return *e == '\0' ? 0 : -1;
+}
+
+/* keys that only steer threading, printing or checkpoints of the reference:
+ * accepted and ignored */
+static const char *k_ignored[] = {"nThreads", "hamThreads", "nestedOMP", "useFastHam", "useMPIOMP", "MPIOrtho",
+                                  "MPIDiag", "parallelSigma", "timeHamiltonian", "printNorm", "printCubes",
+                                  "printGaussCubes", "saveCheckpoints", "printPsiFilt", "printPsiOrtho",
+                                  "printPsiDiag", "fftWisdomDir", "saveOutput", "calcPotOverlap",
+                                  "calcSpinAngStat", "retryFilter", "centerConf", "noTimeRev", "psiZeroCut",
+                                  "coulombDone", "restartCoulomb", "calcDarkStates", "timingSpecs", NULL};
+/* keys whose non-zero value selects a path this build does not implement */
+static const char *k_unsupported[] = {"periodic", "useStrain", "longRange", "localStructureDependent",
+                                      "useGaussianBasis", "readProj", "readCoeffs", "inputPsiFilt",
+                                      "restartFromCheckpoint", "restartFromOrtho", "restartFromSigma",
+                                      "interpolatePot", "calcFilterOnly", NULL};
+
+static int in_list(const char *k, const char **l)
+{
+  for (int i = 0; l[i]; i++)
+    if (!strcmp(k, l[i])) return 1;
+  return 0;
+}
+
+int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, size_t errlen)
+{
+  memset(p, 0, sizeof(*p));
+  p->ke_max = 20.0;      /* read.c:32 */
+  p->fermi_e = -0.18;    /* read.c:87 */
+  p->sigma_e_cut = 0.01; /* read.c:89 */
+  p->get_all_states = 1; /* read.c:85 */
+  p->precision = 0;
+  FILE *f = fopen(path, "r");
+  if (!f) { seterr(err, errlen, "cannot open", path); return -1; }
+  char key[1000], val[1000];
+  int rc = 0, count = 0;
+  while (rc == 0 && count < 100 && fscanf(f, "%999s = %999s", key, val) == 2) {
+    long lv = 0;
+    double dv = 0;
+    count++;
+    if (!strcmp(key, "nx")) rc = parse_long(val, &p->nx);
+    else if (!strcmp(key, "ny")) rc = parse_long(val, &p->ny);
+    else if (!strcmp(key, "nz")) rc = parse_long(val, &p->nz);
+    else if (!strcmp(key, "dGrid")) { rc = parse_double(val, &p->dx); p->dy = p->dz = p->dx; }
+    else if (!strcmp(key, "dx")) rc = parse_double(val, &p->dx);
+    else if (!strcmp(key, "dy")) rc = parse_double(val, &p->dy);
+    else if (!strcmp(key, "dz")) rc = parse_double(val, &p->dz);
+    else if (!strcmp(key, "mStatesPerFilter")) rc = parse_long(val, &p->m_states_per_filter);
+    else if (!strcmp(key, "nFilterCycles")) rc = parse_long(val, &p->n_filter_cycles);
+    else if (!strcmp(key, "nCheby")) rc = parse_long(val, &p->ncheby);
+    else if (!strcmp(key, "VBmin")) rc = parse_double(val, &p->vbmin);
+    else if (!strcmp(key, "VBmax")) rc = parse_double(val, &p->vbmax);
+    else if (!strcmp(key, "CBmin")) rc = parse_double(val, &p->cbmin);
+    else if (!strcmp(key, "CBmax")) rc = parse_double(val, &p->cbmax);
+    else if (!strcmp(key, "KEmax")) rc = parse_double(val, &p->ke_max);
+    else if (!strcmp(key, "fermiEnergy")) rc = parse_double(val, &p->fermi_e);
+    else if (!strcmp(key, "sigmaECut")) rc = parse_double(val, &p->sigma_e_cut);
+    else if (!strcmp(key, "setTargets")) {
+      rc = parse_long(val, &lv);
+      p->set_targets = (int)lv;
+      if (!rc && lv == 1 && fscanf(f, "%ld %ld", &p->n_targets_vb, &p->n_targets_cb) != 2) rc = -1;
+    } else if (!strcmp(key, "setSeed")) {
+      rc = parse_long(val, &lv);
+      p->set_seed = (int)lv;
+      if (!rc && lv == 1 && fscanf(f, "%ld", &p->seed) != 1) rc = -1;
+    } else if (!strcmp(key, "getAllStates")) {
+      rc = parse_long(val, &lv);
+      p->get_all_states = (int)lv;
+      if (!rc && lv == 0 && fscanf(f, "%lg", &p->sigma_e_cut) != 1) rc = -1;
+    } else if (!strcmp(key, "useSpinors")) { rc = parse_long(val, &lv); p->use_spinors = (int)lv; }
+    else if (!strcmp(key, "spinOrbit")) { rc = parse_long(val, &lv); p->so = (int)lv; }
+    else if (!strcmp(key, "NonLocal")) { rc = parse_long(val, &lv); p->nl = (int)lv; }
+    else if (!strcmp(key, "approxEnergyRange")) { rc = parse_long(val, &lv); p->approx_energy_range = (int)lv; }
+    else if (!strcmp(key, "mixedPrecision")) { rc = parse_long(val, &lv); p->precision = lv ? 1 : 0; }
+    else if (in_list(key, k_unsupported)) {
+      if (parse_double(val, &dv) == 0 && dv != 0.0) {
+        seterr(err, errlen, "input.par key not supported by this build (set it to 0)", key);
+        fclose(f);
+        return -1;
+      }
+    } else if (in_list(key, k_ignored)) {
+      /* printCubes takes a second value in the reference's examples */
+      if (!strcmp(key, "printCubes") && parse_long(val, &lv) == 0 && lv == 1) {
+        long dummy;
+        if (fscanf(f, "%ld", &dummy) != 1) rc = -1;
+      }
+    } else {
+      seterr(err, errlen, "unknown input.par key", key);
+      fclose(f);
+      return -1;
+    }
+    if (rc) seterr(err, errlen, "cannot convert the value of", key);
+  }
+  fclose(f);
+  if (rc) return -1;
+  if (p->so) p->use_spinors = 1; /* read.c:897-900 */
+  if (p->dx <= 0 || p->dy <= 0 || p->dz <= 0) { seterr(err, errlen, "grid spacing missing", "dGrid"); return -1; }
+  if (p->m_states_per_filter < 2 || p->n_filter_cycles < 1 || p->ncheby < 2) {
+    seterr(err, errlen, "mStatesPerFilter, nFilterCycles and nCheby must be set", NULL);
+    return -1;
+  }
+  if (p->set_targets != 1) { /* set_ene_targets, init.c:420-424 */
+    p->n_targets_cb = p->m_states_per_filter / 2;
+    p->n_targets_vb = p->m_states_per_filter - p->n_targets_cb;
+  }
+  if (p->n_targets_vb + p->n_targets_cb != p->m_states_per_filter || p->n_targets_vb < 1 || p->n_targets_cb < 1) {
+    seterr(err, errlen, "n_targets_VB + n_targets_CB must equal mStatesPerFilter, at least one of each", NULL);
+    return -1;
+  }
+  return 0;
+}
+
+int fbse_read_bse_params(const char *path, fbse_bse_params *p, char *err, size_t errlen)
+{
+  memset(p, 0, sizeof(*p));
+  p->max_hole_states = -1;
+  p->max_elec_states = -1;
+  p->sigma_e_cut = 0.01;
+  p->eps_x = p->eps_y = p->eps_z = 1.0;
+  p->fermi_e = -0.18;
+  FILE *f = fopen(path, "r");
+  if (!f) { seterr(err, errlen, "cannot open", path); return -1; }
+  char key[1000], val[1000];
+  int rc = 0, count = 0;
+  while (rc == 0 && count < 100 && fscanf(f, "%999s = %999s", key, val) == 2) {
+    long lv = 0;
+    double dv = 0;
+    count++;
+    if (!strcmp(key, "maxHoleStates")) rc = parse_long(val, &p->max_hole_states);
+    else if (!strcmp(key, "maxElecStates")) rc = parse_long(val, &p->max_elec_states);
+    else if (!strcmp(key, "sigmaECut")) rc = parse_double(val, &p->sigma_e_cut);
+    else if (!strcmp(key, "epsX")) rc = parse_double(val, &p->eps_x);
+    else if (!strcmp(key, "epsY")) rc = parse_double(val, &p->eps_y);
+    else if (!strcmp(key, "epsZ")) rc = parse_double(val, &p->eps_z);
+    else if (!strcmp(key, "fermiEnergy")) rc = parse_double(val, &p->fermi_e);
+    else if (!strcmp(key, "deltaEhole")) rc = parse_double(val, &p->delta_e_hole);
+    else if (!strcmp(key, "deltaEelec")) rc = parse_double(val, &p->delta_e_elec);
+    else if (!strcmp(key, "mixedPrecision")) { rc = parse_long(val, &lv); p->precision = lv ? 1 : 0; }
+    else if (!strcmp(key, "spinOrbit") || !strcmp(key, "NonLocal") || !strcmp(key, "KEmax")) {
+      rc = parse_double(val, &dv); /* carried by output.dat; the value here is not used */
+    } else if (in_list(key, k_ignored)) {
+    } else {
+      seterr(err, errlen, "unknown input.par key", key);
+      fclose(f);
+      return -1;
+    }
+    if (rc) seterr(err, errlen, "cannot convert the value of", key);
+  }
+  fclose(f);
+  return rc ? -1 : 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * conf.par and tables
+ * ------------------------------------------------------------------------- */
+int fbse_read_conf(const char *path, long *natoms, double **xyz, int **types, char names[][8], int *ntypes,
+                   char *err, size_t errlen)
+{
+  FILE *f = fopen(path, "r");
+  if (!f) { seterr(err, errlen, "cannot open", path); return -1; }
+  long n = 0;
+  if (fscanf(f, "%ld", &n) != 1 || n < 1) { fclose(f); seterr(err, errlen, "bad atom count in", path); return -1; }
+  double *x = malloc(3 * n * sizeof(double));
+  int *t = malloc(n * sizeof(int));
+  *ntypes = 0;
+  double c[3] = {0, 0, 0};
+  for (long i = 0; i < n; i++) {
+    char nm[64];
+    if (fscanf(f, "%63s %lf %lf %lf", nm, &x[3 * i], &x[3 * i + 1], &x[3 * i + 2]) != 4 || strlen(nm) > 7) {
+      fclose(f);
+      free(x);
+      free(t);
+      seterr(err, errlen, "bad atom line in", path);
+      return -1;
+    }
+    int k;
+    for (k = 0; k < *ntypes; k++)
+      if (!strcmp(names[k], nm)) break;
+    if (k == *ntypes) {
+      if (*ntypes == FBSE_MAX_TYPES) { fclose(f); free(x); free(t); seterr(err, errlen, "too many atom types", NULL); return -1; }
+      strcpy(names[k], nm);
+      (*ntypes)++;
+    }
+    t[i] = k;
+    for (int a = 0; a < 3; a++) c[a] += x[3 * i + a];
+  }
+  fclose(f);
+  /* centerConf (read.c:1135-1148): shift the centre of the atoms to the origin */
+  for (int a = 0; a < 3; a++) c[a] /= (double)n;
+  for (long i = 0; i < n; i++)
+    for (int a = 0; a < 3; a++) x[3 * i + a] -= c[a];
+  *natoms = n;
+  *xyz = x;
+  *types = t;
+  return 0;
+}
+
+long fbse_read_table(const char *path, double **r, double **v)
+{
+  FILE *f = fopen(path, "r");
+  if (!f) return -1;
+  long cap = 1024, n = 0;
+  double *a = malloc(cap * sizeof(double)), *b = malloc(cap * sizeof(double));
+  double x, y;
+  while (fscanf(f, "%lf %lf", &x, &y) == 2) {
+    if (n == cap) {
+      cap *= 2;
+      a = realloc(a, cap * sizeof(double));
+      b = realloc(b, cap * sizeof(double));
+    }
+    a[n] = x;
+    b[n] = y;
+    n++;
+  }
+  fclose(f);
+  *r = a;
+  *v = b;
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * grid
+ * ------------------------------------------------------------------------- */
+void fbse_grid_rule(const double *xyz, long natoms, double d, long n_in, int axis, long *n, double *xmin)
+{
+  /* init_grid_params (init.c:5-255): the largest coordinate separation sets a
+   * half-width xd = nint(ext/2 + 5); the axis grows to cover [-xd, xd - d]
+   * (made even) when that exceeds the requested size; box = n d (even n) or
+   * (n - 1) d (odd n) centred on the origin */
+  double ext = 0.0;
+  for (long i = 0; i < natoms; i++)
+    for (long j = 0; j < natoms; j++) {
+      const double s = fabs(xyz[3 * i + axis] - xyz[3 * j + axis]);
+      if (s > ext) ext = s;
+    }
+  const double xd = rint(0.5 * ext + 5.0);
+  const long ntmp = (long)(((xd - d) - (-xd)) / d);
+  long nn = n_in;
+  if (ntmp > nn) nn = ntmp + (ntmp % 2);
+  const double box = (nn % 2 == 0) ? (double)nn * d : (double)(nn - 1) * d;
+  *n = nn;
+  *xmin = -box / 2.0;
+}
+
+void fbse_grid_axis(long n, double lo, double d, double *out)
+{
+  double v = lo;
+  for (long j = 0; j < n; j++) {
+    out[j] = v;
+    v += d;
+  }
+}
+
+double fbse_r_nlcut2(double dx) { return 1.5 + 6.0 * log(10.0) + 3.0 * dx; }
+
+/* ---------------------------------------------------------------------------
+ * radial projectors (filter_mpi/projectors.c:12-228).  The reference forms
+ * the PROJ_LEN x PROJ_LEN matrix
+ *   A[i][j] = sum_{r>0} r^2 j1(k_i r) w(r) j1(k_j r) dr
+ * (j1 the spherical Bessel function, w the SO Gaussian or the NL profile)
+ * and keeps the nproj eigenvectors of largest |eigenvalue|.  Here A is never
+ * formed: a block subspace iteration (block 12) with Rayleigh-Ritz steps
+ * (Jacobi on the small projected matrix) applies A as J diag(w r^2 dr) J^T.
+ * The kernel's spectrum falls off fast, so a handful of iterations reaches
+ * round-off.  Eigenvector signs are free; the projectors enter as products.
+ * ------------------------------------------------------------------------- */
+static double bessel1(double x, double x1) { return (x < 1e-10) ? 0.0 : (sin(x) * (x1 * x1) - cos(x) * x1); }
+
+/* cyclic Jacobi eigen-decomposition of a small symmetric matrix a[n][n]:
+ * eigenvalues in w, eigenvectors in the columns of v */
+static void jacobi_small(int n, double *a, double *w, double *v)
+{
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) v[i * n + j] = (i == j);
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0;
+    for (int p = 0; p < n; p++)
+      for (int q = p + 1; q < n; q++) off += a[p * n + q] * a[p * n + q];
+    if (off < 1e-300) break;
+    for (int p = 0; p < n; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double apq = a[p * n + q];
+        if (fabs(apq) < 1e-300) continue;
+        const double th = (a[q * n + q] - a[p * n + p]) / (2.0 * apq);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; k++) {
+          const double akp = a[k * n + p], akq = a[k * n + q];
+          a[k * n + p] = c * akp - s * akq;
+          a[k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; k++) {
+          const double apk = a[p * n + k], aqk = a[q * n + k];
+          a[p * n + k] = c * apk - s * aqk;
+          a[q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; k++) {
+          const double vkp = v[k * n + p], vkq = v[k * n + q];
+          v[k * n + p] = c * vkp - s * vkq;
+          v[k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < n; i++) w[i] = a[i * n + i];
+}
+
+int fbse_radial_projectors(double dx, double rcut, int kind, double lam1, double lam2, int nproj, double *out,
+                           int *sgn)
+{
+  const long N = FBSE_PROJ_LEN;
+  enum { B = 12 };
+  if (nproj < 1 || nproj > B / 2) return -1;
+  if (kind == 1 && lam1 == 0.0 && lam2 == 0.0) { /* gen_nlc_projectors: no NL term */
+    memset(out, 0, (size_t)nproj * N * sizeof(double));
+    for (int p = 0; p < nproj; p++) sgn[p] = 0;
+    return 0;
+  }
+  const double kmax = 1.5 * FBSE_PI / dx, dk = kmax / (double)N, dr = rcut / (double)N;
+  double *J = malloc((size_t)N * N * sizeof(double)); /* J[i * N + rp] = j1(k_i r_rp) */
+  double *wr = calloc(N, sizeof(double));
+  double *X = malloc((size_t)B * N * sizeof(double)), *Y = malloc((size_t)B * N * sizeof(double));
+  double *t = malloc(N * sizeof(double));
+  if (!J || !wr || !X || !Y || !t) { free(J); free(wr); free(X); free(Y); free(t); return -1; }
+  for (long i = 0; i < N; i++) {
+    const double ki = (double)i * dk;
+    J[i * N] = 0.0;
+    for (long rp = 1; rp < N; rp++) {
+      const double r = (double)rp * dr;
+      J[i * N + rp] = bessel1(ki * r, 1.0 / (ki * r + 1e-10));
+    }
+  }
+  for (long rp = 1; rp < N; rp++) {
+    const double r = (double)rp * dr;
+    const double w = (kind == 0) ? exp(-((r / 0.7) * (r / 0.7)))
+                                 : lam1 * exp(-(r * r)) + lam2 * exp(-((r - 1.5) * (r - 1.5)));
+    wr[rp] = r * r * w * dr;
+  }
+  /* start block: deterministic, well spread */
+  uint64_t s = 0x9E3779B97F4A7C15ull;
+  for (long i = 0; i < (long)B * N; i++) {
+    s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+    X[i] = (double)(s >> 11) / 9007199254740992.0 - 0.5;
+  }
+  double Hs[B * B], ev[B], V[B * B];
+  for (int it = 0; it < 60; it++) {
+    /* Y = A X */
+    for (int b = 0; b < B; b++) {
+      const double *x = X + (long)b * N;
+      for (long rp = 0; rp < N; rp++) t[rp] = 0.0;
+      for (long i = 0; i < N; i++) {
+        const double xi = x[i];
+        const double *Ji = J + i * N;
+        for (long rp = 1; rp < N; rp++) t[rp] += Ji[rp] * xi;
+      }
+      for (long rp = 0; rp < N; rp++) t[rp] *= wr[rp];
+      double *y = Y + (long)b * N;
+      for (long i = 0; i < N; i++) {
+        const double *Ji = J + i * N;
+        double acc = 0.0;
+        for (long rp = 1; rp < N; rp++) acc += Ji[rp] * t[rp];
+        y[i] = acc;
+      }
+    }
+    /* orthonormalise Y (modified Gram-Schmidt, twice) into X */
+    for (int pass = 0; pass < 2; pass++)
+      for (int b = 0; b < B; b++) {
+        double *y = Y + (long)b * N;
+        for (int c = 0; c < b; c++) {
+          const double *z = Y + (long)c * N;
+          double d = 0;
+          for (long i = 0; i < N; i++) d += z[i] * y[i];
+          for (long i = 0; i < N; i++) y[i] -= d * z[i];
+        }
+        double nrm = 0;
+        for (long i = 0; i < N; i++) nrm += y[i] * y[i];
+        nrm = sqrt(nrm);
+        if (nrm == 0) nrm = 1;
+        for (long i = 0; i < N; i++) y[i] /= nrm;
+      }
+    memcpy(X, Y, (size_t)B * N * sizeof(double));
+    /* Rayleigh-Ritz: Hs = X^T A X */
+    for (int b = 0; b < B; b++) {
+      const double *x = X + (long)b * N;
+      for (long rp = 0; rp < N; rp++) t[rp] = 0.0;
+      for (long i = 0; i < N; i++) {
+        const double *Ji = J + i * N;
+        for (long rp = 1; rp < N; rp++) t[rp] += Ji[rp] * x[i];
+      }
+      for (long rp = 0; rp < N; rp++) t[rp] *= wr[rp];
+      double *y = Y + (long)b * N;
+      for (long i = 0; i < N; i++) {
+        const double *Ji = J + i * N;
+        double acc = 0.0;
+        for (long rp = 1; rp < N; rp++) acc += Ji[rp] * t[rp];
+        y[i] = acc;
+      }
+    }
+    for (int a = 0; a < B; a++)
+      for (int b = 0; b < B; b++) {
+        double d = 0;
+        for (long i = 0; i < N; i++) d += X[(long)a * N + i] * Y[(long)b * N + i];
+        Hs[a * B + b] = d;
+      }
+    for (int a = 0; a < B; a++)
+      for (int b = a + 1; b < B; b++) Hs[a * B + b] = Hs[b * B + a] = 0.5 * (Hs[a * B + b] + Hs[b * B + a]);
+    jacobi_small(B, Hs, ev, V);
+    /* rotate X to the Ritz vectors, and Y (= A X) with it for the residuals */
+    double *Z = malloc((size_t)B * N * sizeof(double)), *AZ = malloc((size_t)B * N * sizeof(double));
+    for (int b = 0; b < B; b++)
+      for (long i = 0; i < N; i++) {
+        double z = 0, az = 0;
+        for (int a = 0; a < B; a++) {
+          z += X[(long)a * N + i] * V[a * B + b];
+          az += Y[(long)a * N + i] * V[a * B + b];
+        }
+        Z[(long)b * N + i] = z;
+        AZ[(long)b * N + i] = az;
+      }
+    memcpy(X, Z, (size_t)B * N * sizeof(double));
+    /* order by |eigenvalue| (the selection of projectors.c:166-186), check the
+     * residuals of the wanted ones */
+    int idx[B];
+    for (int b = 0; b < B; b++) idx[b] = b;
+    for (int a = 0; a < B; a++)
+      for (int b = a + 1; b < B; b++)
+        if (fabs(ev[idx[b]]) > fabs(ev[idx[a]])) { int tmp = idx[a]; idx[a] = idx[b]; idx[b] = tmp; }
+    double worst = 0, scale = fabs(ev[idx[0]]) > 0 ? fabs(ev[idx[0]]) : 1.0;
+    for (int p = 0; p < nproj; p++) {
+      const int b = idx[p];
+      double r2 = 0;
+      for (long i = 0; i < N; i++) {
+        const double rres = AZ[(long)b * N + i] - ev[b] * Z[(long)b * N + i];
+        r2 += rres * rres;
+      }
+      if (sqrt(r2) / scale > worst) worst = sqrt(r2) / scale;
+    }
+    if (worst < 1e-13 || it == 59) {
+      /* radial functions (projectors.c:62-78, 197-216) */
+      for (int p = 0; p < nproj; p++) {
+        const int b = idx[p];
+        const double *vec = X + (long)b * N;
+        const double pre = (2.00 / FBSE_PI) * sqrt(fabs(ev[b]));
+        if (sgn) sgn[p] = ev[b] < 0 ? -1 : 1;
+        for (long rp = 0; rp < N; rp++) {
+          const double r = (double)rp * dr;
+          double sum = 0.0;
+          for (long kp = 0; kp < N; kp++) {
+            const double k = (double)kp * dk;
+            sum += k * k * bessel1(k * r, 1 / (k * r + 1e-10)) * vec[kp] * dk;
+          }
+          out[(long)p * N + rp] = sum * pre;
+        }
+      }
+      free(Z);
+      free(AZ);
+      break;
+    }
+    free(Z);
+    free(AZ);
+  }
+  free(J);
+  free(wr);
+  free(X);
+  free(Y);
+  free(t);
+  return 0;
+}
+
+/* linear interpolation of a radial table (the reference's interpolate) */
+static double interp(double r, double dr, const double *tab, long n)
+{
+  const long i = (long)(r / dr);
+  if (i > n - 2) return 0.0;
+  const double x0 = (double)i * dr, x1 = (double)(i + 1) * dr;
+  const double a = (tab[i + 1] - tab[i]) / (x1 - x0);
+  return a * r + (tab[i] - x0 * a);
+}
+
+int fbse_build_nlc(long nx, long ny, long nz, const double *gx, const double *gy, const double *gz, long nat,
+                   const double *xyz, const double *so_par, const double *so_tab, const double *nl_tab, int nproj,
+                   double rcut2, long *npts_out, long **nl_out, int **jxyz_out, double **y1_out, double **so_out,
+                   double **nl_p_out)
+{
+  const long N = FBSE_PROJ_LEN;
+  const double tmp1 = 0.5 * sqrt(3.0 / FBSE_PI), tmp2 = 0.5 * sqrt(3.0 / (2.0 * FBSE_PI));
+  const double drp = sqrt(rcut2) / (double)N;
+  long *nl = calloc(nat > 0 ? nat : 1, sizeof(long));
+  /* count the points of each sphere first (the row stride is the largest) */
+  long npts = 1;
+  for (long a = 0; a < nat; a++) {
+    long cnt = 0;
+    for (long jz = 0; jz < nz; jz++) {
+      const double dz = gz[jz] - xyz[3 * a + 2];
+      if (dz * dz >= rcut2) continue;
+      for (long jy = 0; jy < ny; jy++) {
+        const double dy = gy[jy] - xyz[3 * a + 1];
+        if (dy * dy + dz * dz >= rcut2) continue;
+        for (long jx = 0; jx < nx; jx++) {
+          const double ddx = gx[jx] - xyz[3 * a];
+          if (ddx * ddx + dy * dy + dz * dz < rcut2) cnt++;
+        }
+      }
+    }
+    nl[a] = cnt;
+    if (cnt > npts) npts = cnt;
+  }
+  const size_t ne = (size_t)(nat > 0 ? nat : 1) * npts;
+  int *jxyz = calloc(ne, sizeof(int));
+  double *y1 = calloc(ne * 6, sizeof(double));
+  double *sop = calloc(ne * nproj, sizeof(double));
+  double *nlp = calloc(ne * nproj, sizeof(double));
+  if (!nl || !jxyz || !y1 || !sop || !nlp) return -1;
+  for (long a = 0; a < nat; a++) {
+    long cnt = 0;
+    const double sq = so_par ? sqrt(so_par[a]) : 0.0;
+    for (long jz = 0; jz < nz; jz++) {
+      const double dz = gz[jz] - xyz[3 * a + 2], dzeps = dz + FBSE_EPSDX;
+      for (long jy = 0; jy < ny; jy++) {
+        const double dy = gy[jy] - xyz[3 * a + 1], dyeps = dy + FBSE_EPSDX;
+        for (long jx = 0; jx < nx; jx++) {
+          const double ddx = gx[jx] - xyz[3 * a], dxeps = ddx + FBSE_EPSDX;
+          const double d2 = ddx * ddx + dy * dy + dz * dz;
+          if (!(d2 < rcut2)) continue;
+          const size_t e = (size_t)a * npts + cnt;
+          jxyz[e] = (int)(nx * (ny * jz + jy) + jx);
+          /* Y_1m with the reference's EPSDX shifts (init.c:540-560) */
+          double r_1 = 1.0 / sqrt(ddx * ddx + dy * dy + dzeps * dzeps);
+          y1[e * 6 + 2] = tmp1 * dzeps * r_1;
+          y1[e * 6 + 3] = 0.0;
+          r_1 = 1.0 / sqrt(dxeps * dxeps + dy * dy + dz * dz);
+          y1[e * 6 + 4] = -tmp2 * dxeps * r_1;
+          y1[e * 6 + 0] = tmp2 * dxeps * r_1;
+          r_1 = 1.0 / sqrt(ddx * ddx + dyeps * dyeps + dz * dz);
+          y1[e * 6 + 5] = -tmp2 * dyeps * r_1;
+          y1[e * 6 + 1] = -tmp2 * dyeps * r_1;
+          const double r = sqrt(d2);
+          for (int p = 0; p < nproj; p++) {
+            sop[e * nproj + p] = so_tab ? interp(r, drp, so_tab + (long)p * N, N) * sq : 0.0;
+            nlp[e * nproj + p] = nl_tab ? interp(r, drp, nl_tab + ((long)a * nproj + p) * N, N) : 0.0;
+          }
+          cnt++;
+        }
+      }
+    }
+  }
+  *npts_out = npts;
+  *nl_out = nl;
+  *jxyz_out = jxyz;
+  *y1_out = y1;
+  *so_out = sop;
+  *nl_p_out = nlp;
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * outputs
+ * ------------------------------------------------------------------------- */
+int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n)
+{
+  FILE *f = fopen(path, "w");
+  if (!f) return -1;
+  for (long i = 0; i < n; i++) fprintf(f, "%ld %.16g %g\n", i, eval[i], sigma[i]); /* write.c:279 */
+  fclose(f);
+  return 0;
+}
+
+int fbse_write_psi(const char *path, const double *psi, long n_doubles)
+{
+  FILE *f = fopen(path, "wb");
+  if (!f) return -1;
+  const size_t w = fwrite(psi, sizeof(double), (size_t)n_doubles, f);
+  fclose(f);
+  return w == (size_t)n_doubles ? 0 : -1;
+}
