@@ -13,6 +13,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfbse_gpu.so")
 CU_SOURCES = ["fft.cu", "hpsi.cu", "filter.cu", "linalg.cu", "bse.cu", "setup.cu", "job.cu", "api.cu"]
 C_SOURCES = ["host/fbse_host.c", "host/fbse_setup.c"]
+EXECUTABLES = {"fbse_filter": "host/fbse_filter_main.c", "fbse_bse": "host/fbse_bse_main.c"}
+BIN = os.path.join(HERE, "bin")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]
@@ -64,8 +66,18 @@ def build(force: bool = False, verbose: bool = False) -> str:
         for log in ex.map(_run, jobs):
             if verbose and log.strip():
                 print(log)
+    relinked = False
     if force or jobs or not os.path.exists(LIB):
         _run([NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+        relinked = True
+    # drop-in executables (filter_mpi's and bse_cplx's command-line stages)
+    os.makedirs(BIN, exist_ok=True)
+    for exe, src in EXECUTABLES.items():
+        out = os.path.join(BIN, exe)
+        srcp = os.path.join(HERE, src)
+        if force or relinked or _stale(out, [srcp, os.path.join(HERE, "host", "fbse_dropin.h"), LIB]):
+            _run(["gcc", "-O2", "-std=gnu99", "-I" + os.path.join(ROOT, "include"), "-o", out, srcp, "-L" + HERE,
+                  "-lfbse_gpu", "-Wl,-rpath,$ORIGIN/..", "-lm"])
     return LIB
 
 

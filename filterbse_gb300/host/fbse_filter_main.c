@@ -1,0 +1,305 @@
+/* fbse_filter: drop-in for the reference's filter executable (filter_mpi).
+ *
+ * Reads input.par, conf.par, pot<Atm>.par and SO_<Atm>.par from the working
+ * directory as the reference does (filter_mpi/read.c), runs the filter stage
+ * on one GPU through libfbse_gpu (energy range, Newton filter of every random
+ * start, orthogonalisation, subspace diagonalisation, sigma_E) and writes
+ * eval.dat, psi.dat and output.dat in the reference's layouts
+ * (filter_mpi/write.c:263-299, mod_output.c:5-162, save.c:446-503).
+ * Errors go to stderr and the process exits with EXIT_FAILURE, like the
+ * reference.  One non-reference key: "mixedPrecision = 1" selects the FP32
+ * recursion (default: the plain FP64 method). */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#include <unistd.h>
+
+#include "../../include/fbse.h"
+#include "fbse_dropin.h"
+
+static void die(const char *msg, const char *detail)
+{
+  fprintf(stderr, "ERROR: %s%s%s\n", msg, detail ? ": " : "", detail ? detail : "");
+  exit(EXIT_FAILURE);
+}
+
+static void check(fbse_ctx *c, int rc, const char *what)
+{
+  if (rc) {
+    fprintf(stderr, "ERROR: %s failed (%d): %s\n", what, rc, c ? fbse_last_error(c) : "");
+    exit(EXIT_FAILURE);
+  }
+}
+
+static int is_ligand(const char *t)
+{ /* is_ligand, filter_mpi/read.c:2425-2447 */
+  static const char *lig[] = {"P1", "P2", "P3", "P4", "PC5", "PC6", "PR1", "PR2", "PR3",
+                              "PA1", "PA2", "PA3", "C1", "C2", "C3", NULL};
+  for (int i = 0; lig[i]; i++)
+    if (!strcmp(t, lig[i])) return 1;
+  return 0;
+}
+
+static void save_output(const char *path, const fbse_filter_params *p, long natoms, const double *xyz,
+                        int ntypes, long nx, long ny, long nz, double dx, double dy, double dz, const double *gx,
+                        const double *gy, const double *gz, double xmin, double ymin, double zmin, int nspin,
+                        int cplx, long n, const double *eval, const double *sigma, const double *psi)
+{ /* save_output (filter_mpi/save.c:446-503) */
+  FILE *f = fopen(path, "wb");
+  if (!f) die("cannot write", path);
+  const long ngrid = nx * ny * nz;
+  const double dkx = 2.0 * M_PI / ((nx % 2 == 0) ? nx * dx : (nx - 1) * dx);
+  const double dky = 2.0 * M_PI / ((ny % 2 == 0) ? ny * dy : (ny - 1) * dy);
+  const double dkz = 2.0 * M_PI / ((nz % 2 == 0) ? nz * dz : (nz - 1) * dz);
+  fprintf(f, "%ld\n", (long)random());
+  fprintf(f, "%ld %ld\n", ngrid, nspin * ngrid);
+  fprintf(f, "%ld\n", n);
+  fprintf(f, "%ld %d\n", natoms, ntypes);
+  for (int j = 0; j < ntypes; j++) fprintf(f, "%d ", j);
+  fprintf(f, "%d\n", nspin);
+  fprintf(f, "%d\n", cplx + 1);
+  fprintf(f, "%g %g\n", p->ke_max, p->fermi_e);
+  fprintf(f, "%d %d %d %d %d\n", p->so, p->nl, 0, p->use_spinors, cplx);
+  for (long j = 0; j < natoms; j++) fprintf(f, "%g %g %g\n", xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2]);
+  fprintf(f, "%g %g %g %g %g %g %g %g\n", dx, dy, dz, sqrt(dx * dx + dy * dy + dz * dz), dx * dy * dz, dkx, dky, dkz);
+  fprintf(f, "%g %g %g %g %g %g\n", xmin, -xmin, ymin, -ymin, zmin, -zmin);
+  fprintf(f, "%ld %ld %ld\n", nx, ny, nz);
+  fprintf(f, "%g %g %g\n", 1.0 / nx, 1.0 / ny, 1.0 / nz);
+  fprintf(f, "%ld", ngrid);
+  fwrite(gx, sizeof(double), nx, f);
+  fwrite(gy, sizeof(double), ny, f);
+  fwrite(gz, sizeof(double), nz, f);
+  fwrite(eval, sizeof(double), n, f);
+  fwrite(sigma, sizeof(double), n, f);
+  fwrite(psi, sizeof(double), (size_t)(cplx + 1) * nspin * ngrid * n, f);
+  fprintf(f, "\n\nEOF\n");
+  fclose(f);
+}
+
+int main(void)
+{
+  char err[512];
+  fbse_filter_params p;
+  if (fbse_read_filter_params("input.par", &p, err, sizeof err)) die(err, NULL);
+  long natoms;
+  double *xyz;
+  int *atype, ntypes;
+  char names[FBSE_MAX_TYPES][8];
+  if (fbse_read_conf("conf.par", &natoms, &xyz, &atype, names, &ntypes, err, sizeof err)) die(err, NULL);
+  const int nspin = p.use_spinors ? 2 : 1, cplx = p.use_spinors ? 1 : 0;
+  printf("fbse_filter: %ld atoms, %d types, nspin %d, SO %d, NL %d, %s\n", natoms, ntypes, nspin, p.so, p.nl,
+         p.precision ? "mixed precision" : "FP64");
+
+  /* grid (init_grid_params) */
+  long nx, ny, nz;
+  double xmin, ymin, zmin;
+  fbse_grid_rule(xyz, natoms, p.dx, p.nx, 0, &nx, &xmin);
+  fbse_grid_rule(xyz, natoms, p.dy, p.ny, 1, &ny, &ymin);
+  fbse_grid_rule(xyz, natoms, p.dz, p.nz, 2, &nz, &zmin);
+  const long ngrid = nx * ny * nz;
+  double *gx = malloc(nx * sizeof(double)), *gy = malloc(ny * sizeof(double)), *gz = malloc(nz * sizeof(double));
+  fbse_grid_axis(nx, xmin, p.dx, gx);
+  fbse_grid_axis(ny, ymin, p.dy, gy);
+  fbse_grid_axis(nz, zmin, p.dz, gz);
+  printf("grid %ld x %ld x %ld, d = %g %g %g, origin %g %g %g\n", nx, ny, nz, p.dx, p.dy, p.dz, xmin, ymin, zmin);
+
+  /* local potential (build_local_pot on the GPU) */
+  double *tr = NULL, *tv = NULL;
+  long *toff = malloc(ntypes * sizeof(long)), *tlen = malloc(ntypes * sizeof(long)), tot = 0;
+  for (int t = 0; t < ntypes; t++) {
+    char path[64];
+    double *r, *v;
+    snprintf(path, sizeof path, "pot%s.par", names[t]);
+    const long n = fbse_read_table(path, &r, &v);
+    if (n < 2) die("cannot read potential table", path);
+    tr = realloc(tr, (tot + n) * sizeof(double));
+    tv = realloc(tv, (tot + n) * sizeof(double));
+    memcpy(tr + tot, r, n * sizeof(double));
+    memcpy(tv + tot, v, n * sizeof(double));
+    toff[t] = tot;
+    tlen[t] = n;
+    tot += n;
+    free(r);
+    free(v);
+  }
+  double *pot = malloc(ngrid * sizeof(double));
+  check(NULL, fbse_build_local_pot(nx, ny, nz, gx, gy, gz, natoms, xyz, atype, ntypes, tr, tv, toff, tlen, pot),
+        "build_local_pot");
+  double vmin_loc = pot[0], vmax_loc = pot[0];
+  for (long i = 1; i < ngrid; i++) {
+    if (pot[i] < vmin_loc) vmin_loc = pot[i];
+    if (pot[i] > vmax_loc) vmax_loc = pot[i];
+  }
+
+  /* projectors (gen_SO_projectors / gen_nlc_projectors, init_NL_projectors) */
+  fbse_proj_desc pd;
+  memset(&pd, 0, sizeof pd);
+  long *nl = NULL;
+  int *jx = NULL, *sgn = NULL;
+  double *y1 = NULL, *sop = NULL, *nlp = NULL, nl_lam_min = 0.0;
+  if (p.so || p.nl) {
+    const int np = FBSE_NPROJ;
+    const long N = FBSE_PROJ_LEN;
+    const double rc2 = fbse_r_nlcut2(p.dx), rc = sqrt(rc2);
+    double so_par[FBSE_MAX_TYPES], lam[FBSE_MAX_TYPES][2];
+    for (int t = 0; t < ntypes; t++) {
+      so_par[t] = lam[t][0] = lam[t][1] = 0.0;
+      if (is_ligand(names[t])) continue;
+      char path[64];
+      snprintf(path, sizeof path, "SO_%s.par", names[t]);
+      FILE *f = fopen(path, "r");
+      if (!f) die("No SO(+NL) pot found in", path);
+      if (fscanf(f, "%lg %*g", &so_par[t]) != 1 || fscanf(f, "%lg %*g", &lam[t][0]) != 1 ||
+          fscanf(f, "%lg %*g", &lam[t][1]) != 1)
+        die("cannot read", path);
+      fclose(f);
+    }
+    long nat = 0;
+    for (long a = 0; a < natoms; a++)
+      if (!is_ligand(names[atype[a]])) nat++;
+    double *pxyz = malloc(3 * (nat ? nat : 1) * sizeof(double)), *psp = malloc((nat ? nat : 1) * sizeof(double));
+    double *so_tab = calloc(np * N, sizeof(double));
+    double *nl_tab = calloc((size_t)(nat ? nat : 1) * np * N, sizeof(double));
+    double *type_nl = calloc((size_t)ntypes * np * N, sizeof(double));
+    int *type_sg = calloc((size_t)ntypes * np, sizeof(int));
+    sgn = calloc((size_t)(nat ? nat : 1) * np, sizeof(int));
+    if (p.so && fbse_radial_projectors(p.dx, rc, 0, 0.0, 0.0, np, so_tab, NULL)) die("SO projectors", NULL);
+    if (p.nl)
+      for (int t = 0; t < ntypes; t++)
+        if (!is_ligand(names[t]) &&
+            fbse_radial_projectors(p.dx, rc, 1, lam[t][0], lam[t][1], np, type_nl + (long)t * np * N,
+                                   type_sg + t * np))
+          die("NL projectors", names[t]);
+    long k = 0;
+    for (long a = 0; a < natoms; a++) {
+      const int t = atype[a];
+      if (is_ligand(names[t])) continue;
+      memcpy(pxyz + 3 * k, xyz + 3 * a, 3 * sizeof(double));
+      psp[k] = so_par[t];
+      if (p.nl) {
+        memcpy(nl_tab + (size_t)k * np * N, type_nl + (long)t * np * N, np * N * sizeof(double));
+        memcpy(sgn + k * np, type_sg + t * np, np * sizeof(int));
+      }
+      k++;
+    }
+    long npts;
+    if (fbse_build_nlc(nx, ny, nz, gx, gy, gz, nat, pxyz, psp, p.so ? so_tab : NULL, p.nl ? nl_tab : NULL, np, rc2,
+                       &npts, &nl, &jx, &y1, &sop, &nlp))
+      die("projector table", NULL);
+    printf("projectors: %ld atoms, %ld grid points per sphere\n", nat, npts);
+    if (p.nl) {
+      /* NL spectral bounds (filter_mpi/init.c:1095-1130) for the range rule */
+      const double dv = p.dx * p.dy * p.dz;
+      double lmin = 0.0;
+      for (long a = 0; a < nat; a++)
+        for (int q = 0; q < np; q++) {
+          double gm[3] = {0, 0, 0};
+          for (long g = 0; g < nl[a]; g++) {
+            const long e = a * npts + g;
+            const double b2 = nlp[e * np + q] * nlp[e * np + q];
+            for (int m = 0; m < 3; m++) gm[m] += b2 * (y1[e * 6 + 2 * m] * y1[e * 6 + 2 * m] +
+                                                       y1[e * 6 + 2 * m + 1] * y1[e * 6 + 2 * m + 1]);
+          }
+          for (int m = 0; m < 3; m++) {
+            const double l = (double)sgn[a * np + q] * dv * gm[m];
+            if (l < lmin) lmin = l;
+          }
+        }
+      nl_lam_min = lmin;
+    }
+    pd.n_atoms = nat;
+    pd.npts = npts;
+    pd.nproj = np;
+    pd.nl = nl;
+    pd.jxyz = jx;
+    pd.y1 = y1;
+    pd.so_proj = sop;
+    pd.nl_proj = nlp;
+    pd.nl_sign = sgn;
+    pd.LS = NULL;
+    free(pxyz);
+    free(psp);
+    free(so_tab);
+    free(nl_tab);
+    free(type_nl);
+    free(type_sg);
+  }
+
+  fbse_grid_desc gd;
+  memset(&gd, 0, sizeof gd);
+  gd.nx = nx; gd.ny = ny; gd.nz = nz;
+  gd.dx = p.dx; gd.dy = p.dy; gd.dz = p.dz;
+  gd.ke_max = p.ke_max;
+  gd.nspin = nspin;
+  gd.is_complex = cplx;
+  gd.so = p.so;
+  gd.nl = p.nl;
+  fbse_ctx *ctx = NULL;
+  int rc = fbse_create(&ctx, &gd, pot, (p.so || p.nl) ? &pd : NULL, p.precision ? FBSE_MIXED : FBSE_FP64);
+  check(ctx, rc, "fbse_create");
+
+  /* energy range (get_energy_range, filter_mpi/energy.c:169-379) */
+  double emin, emax;
+  if (p.approx_energy_range) {
+    emin = -0.8; /* energy.c:307-308 */
+    emax = vmax_loc + p.ke_max;
+    if (p.so) emax += 3.5;
+    if (p.nl && nl_lam_min < 0.0) emin += 1.15 * nl_lam_min;
+  } else {
+    long iters = 0;
+    check(ctx, fbse_energy_range(ctx, -874917403, 1500, &emin, &emax, &iters), "energy range");
+    printf("energy range: Emin %g, Emax %g (%ld iterations)\n", emin, emax, iters);
+  }
+  if (p.nl && !p.so && nl_lam_min < 0.0) { /* energy.c:350-362 */
+    emax *= 1.05;
+    emin -= 0.1 * fabs(emin);
+    const double weyl = 1.05 * (vmin_loc + nl_lam_min);
+    if (emin > weyl) emin = weyl;
+  } else {
+    emax *= 1.2;
+    emin -= 0.2 * fabs(emin);
+  }
+  const double de = emax - emin;
+  printf("Emin = %g, Emax = %g, dE = %g\n", emin, emax, de);
+
+  /* targets (set_ene_targets, init.c:401-478) and Newton coefficients */
+  const long m = p.m_states_per_filter, nc = p.ncheby, ns = p.n_filter_cycles;
+  double *targets = malloc(m * sizeof(double));
+  double del = (p.vbmax - p.vbmin) / (double)p.n_targets_vb;
+  for (long j = 0; j < p.n_targets_vb; j++) targets[p.n_targets_vb - j - 1] = p.vbmax - (double)j * del;
+  del = (p.cbmax - p.cbmin) / (double)p.n_targets_cb;
+  for (long j = p.n_targets_vb; j < m; j++) targets[j] = p.cbmin + (double)(j - p.n_targets_vb) * del;
+  double *zn = malloc(nc * sizeof(double)), *an = malloc(2 * m * nc * sizeof(double));
+  fbse_samp_points(nc, zn);
+  const double dt = ((double)nc / (2.5 * de)) * ((double)nc / (2.5 * de)); /* mod_filter.c:114 */
+  if (fbse_newton_coeff(nc, m, zn, targets, emin, de, dt, an)) die("Newton coefficients", NULL);
+
+  /* random starts (mod_filter.c:152-160, init_filter_states) */
+  long seed;
+  if (p.set_seed == 1) seed = -p.seed;
+  else {
+    srandom((unsigned)(time(NULL) ^ (getpid() << 8)));
+    seed = -random();
+  }
+  const long stlen = (long)(cplx + 1) * nspin * ngrid;
+  double *starts = malloc((size_t)ns * stlen * sizeof(double));
+  fbse_init_filter_states(starts, ns, ngrid, nspin, cplx, p.dx * p.dy * p.dz, seed, NULL);
+
+  /* filter + ortho + diag + sigma_E + mod_output's selection */
+  double *eval = malloc(ns * m * sizeof(double)), *sigma = malloc(ns * m * sizeof(double));
+  double *psi = malloc((size_t)ns * m * stlen * sizeof(double));
+  if (!starts || !eval || !sigma || !psi) die("host allocation", NULL);
+  long n_out = 0;
+  check(ctx, fbse_filter_job(ctx, zn, an, nc, m, emin, de, starts, ns, p.get_all_states ? 0.0 : p.sigma_e_cut, &n_out,
+                             eval, sigma, psi),
+        "filter job");
+  printf("%ld eigenstates written\n", n_out);
+  if (fbse_write_eval("eval.dat", eval, sigma, n_out)) die("cannot write", "eval.dat");
+  if (fbse_write_psi("psi.dat", psi, n_out * stlen)) die("cannot write", "psi.dat");
+  save_output("output.dat", &p, natoms, xyz, ntypes, nx, ny, nz, p.dx, p.dy, p.dz, gx, gy, gz, xmin, ymin, zmin,
+              nspin, cplx, n_out, eval, sigma, psi);
+  fbse_destroy(ctx);
+  return 0;
+}

@@ -1,0 +1,146 @@
+"""Host logic of the drop-in executables, on the CPU: input.par / conf.par
+parsing, the grid rule, the radial projectors and the projector table
+against the oracle, and the executables' refusal to run without a GPU."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.systems import GOLD, read_conf
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BIN = os.path.join(ROOT, "filterbse_gb300", "bin")
+D = ctypes.POINTER(ctypes.c_double)
+I = ctypes.POINTER(ctypes.c_int)
+Lp = ctypes.POINTER(ctypes.c_long)
+
+
+class FilterParams(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_long), ("ny", ctypes.c_long), ("nz", ctypes.c_long), ("dx", ctypes.c_double),
+                ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("m_states_per_filter", ctypes.c_long),
+                ("n_filter_cycles", ctypes.c_long), ("ncheby", ctypes.c_long), ("vbmin", ctypes.c_double),
+                ("vbmax", ctypes.c_double), ("cbmin", ctypes.c_double), ("cbmax", ctypes.c_double),
+                ("ke_max", ctypes.c_double), ("fermi_e", ctypes.c_double), ("sigma_e_cut", ctypes.c_double),
+                ("set_targets", ctypes.c_int), ("n_targets_vb", ctypes.c_long), ("n_targets_cb", ctypes.c_long),
+                ("set_seed", ctypes.c_int), ("seed", ctypes.c_long), ("use_spinors", ctypes.c_int),
+                ("so", ctypes.c_int), ("nl", ctypes.c_int), ("get_all_states", ctypes.c_int),
+                ("approx_energy_range", ctypes.c_int), ("precision", ctypes.c_int)]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import filterbse_gb300 as F
+    L = F.load()
+    L.fbse_read_filter_params.argtypes = [ctypes.c_char_p, ctypes.POINTER(FilterParams), ctypes.c_char_p,
+                                          ctypes.c_size_t]
+    L.fbse_grid_rule.argtypes = [D, ctypes.c_long, ctypes.c_double, ctypes.c_long, ctypes.c_int, Lp, D]
+    L.fbse_grid_rule.restype = None
+    L.fbse_radial_projectors.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_int, D, I]
+    L.fbse_build_nlc.argtypes = ([ctypes.c_long] * 3 + [D] * 3 + [ctypes.c_long, D, D, D, D, ctypes.c_int,
+                                                                 ctypes.c_double, Lp] +
+                                 [ctypes.POINTER(Lp), ctypes.POINTER(I), ctypes.POINTER(D), ctypes.POINTER(D),
+                                  ctypes.POINTER(D)])
+    return L
+
+
+def test_read_filter_params_example(lib):
+    p = FilterParams()
+    err = ctypes.create_string_buffer(512)
+    rc = lib.fbse_read_filter_params(os.path.join(GOLD, "cspbi3", "input.par").encode(), ctypes.byref(p), err, 512)
+    assert rc == 0, err.value
+    assert (p.nx, p.ny, p.nz, p.dx, p.dz) == (44, 44, 44, 0.5, 0.5)
+    assert (p.m_states_per_filter, p.n_filter_cycles, p.ncheby) == (16, 16, 2048)
+    assert (p.n_targets_vb, p.n_targets_cb, p.set_targets) == (10, 6, 1)
+    assert p.so == 1 and p.nl == 1 and p.use_spinors == 1 and p.get_all_states == 1
+    assert p.fermi_e == -0.19 and p.vbmin == -0.5 and p.cbmax == -0.1 and p.ke_max == 20.0
+
+
+def test_read_filter_params_rejects(lib, tmp_path):
+    err = ctypes.create_string_buffer(512)
+    p = FilterParams()
+    (tmp_path / "a.par").write_text("dGrid = 0.5\nmStatesPerFilter = 4\nnFilterCycles = 2\nnCheby = 16\nperiodic = 1\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "a.par").encode(), ctypes.byref(p), err, 512) != 0
+    assert b"periodic" in err.value
+    (tmp_path / "b.par").write_text("dGrid = 0.5\nmStatesPerFilter = 4\nnFilterCycles = 2\nnCheby = 16\nbogusKey = 3\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "b.par").encode(), ctypes.byref(p), err, 512) != 0
+    assert b"bogusKey" in err.value
+    (tmp_path / "c.par").write_text("dGrid = 0.5\nmStatesPerFilter = 4\nnFilterCycles = 2\nnCheby = 16\n"
+                                    "setTargets = 1 3 3\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "c.par").encode(), ctypes.byref(p), err, 512) != 0
+
+
+@pytest.mark.parametrize("name,n_in", [("cspbi3", 44), ("cdse22", 0)])
+def test_grid_rule_matches_oracle(lib, name, n_in):
+    _, xyz = read_conf(os.path.join(GOLD, name, "conf.par"))
+    xyz = np.ascontiguousarray(xyz)
+    ref = O.reference_grid(xyz, 0.8 if name == "cdse22" else 0.5, (n_in,) * 3)
+    for ax, (rn, rlo) in enumerate(((ref.nx, ref.xmin), (ref.ny, ref.ymin), (ref.nz, ref.zmin))):
+        n = ctypes.c_long()
+        lo = ctypes.c_double()
+        lib.fbse_grid_rule(xyz.reshape(-1).ctypes.data_as(D), len(xyz), 0.8 if name == "cdse22" else 0.5, n_in, ax,
+                           ctypes.byref(n), ctypes.byref(lo))
+        assert n.value == rn and lo.value == rlo
+
+
+@pytest.mark.parametrize("kind,lam", [(0, (0.0, 0.0)), (1, (0.5, -0.3)), (1, (-0.8, 0.2))])
+def test_radial_projectors_match_oracle(lib, kind, lam):
+    dx = 0.5
+    rc = np.sqrt(O.r_nlcut2(dx))
+    out = np.empty(5 * 1024)
+    sg = np.zeros(5, np.int32)
+    assert lib.fbse_radial_projectors(dx, rc, kind, lam[0], lam[1], 5, out.ctypes.data_as(D), sg.ctypes.data_as(I)) == 0
+    if kind == 0:
+        ref, rs = O.so_radial(dx, rc), np.ones(5, np.int32)
+    else:
+        ref, rs = O.nl_radial(dx, rc, *lam)
+    o = out.reshape(5, 1024)
+    for p in range(5):
+        s = np.sign(np.dot(o[p], ref[p]))  # eigenvector signs are free; the projectors enter squared
+        assert np.max(np.abs(s * o[p] - ref[p])) < 1e-10 * np.max(np.abs(ref[p]))
+    if kind == 1:
+        assert np.array_equal(sg, rs)
+
+
+def test_projector_table_matches_oracle(lib):
+    g = O.Grid(24, 22, 20, 0.5, 0.5, 0.5, -6.0, -5.5, -5.0)
+    rng = np.random.default_rng(4)
+    xyz = np.ascontiguousarray(rng.uniform(-3, 3, (3, 3)))
+    so_par = np.array([0.2, 0.5, 0.9])
+    rc2 = O.r_nlcut2(g.dx)
+    so_tab = np.ascontiguousarray(rng.normal(size=(5, 1024)))
+    nl_tab = np.ascontiguousarray(rng.normal(size=(3, 5, 1024)))
+    sgn = rng.choice([-1, 1], size=(3, 5)).astype(np.int32)
+    ref = O.nlc_table(g, xyz, so_par, so_tab, nl_tab, sgn)
+    gx, gy, gz = (np.ascontiguousarray(a) for a in g.axes())
+    npts = ctypes.c_long()
+    nl, jx, y1, sp, np_ = Lp(), I(), D(), D(), D()
+    assert lib.fbse_build_nlc(g.nx, g.ny, g.nz, gx.ctypes.data_as(D), gy.ctypes.data_as(D), gz.ctypes.data_as(D), 3,
+                              xyz.reshape(-1).ctypes.data_as(D), so_par.ctypes.data_as(D), so_tab.ctypes.data_as(D),
+                              nl_tab.ctypes.data_as(D), 5, rc2, ctypes.byref(npts), ctypes.byref(nl),
+                              ctypes.byref(jx), ctypes.byref(y1), ctypes.byref(sp), ctypes.byref(np_)) == 0
+    assert npts.value == ref.npts
+    n = 3 * ref.npts
+    assert np.array_equal(np.ctypeslib.as_array(nl, (3,)), ref.nl)
+    assert np.array_equal(np.ctypeslib.as_array(jx, (n,)), ref.jxyz)
+    assert np.array_equal(np.ctypeslib.as_array(y1, (n * 6,)), ref.y1)
+    assert np.allclose(np.ctypeslib.as_array(sp, (n * 5,)), ref.proj, rtol=1e-14, atol=1e-14)
+    assert np.allclose(np.ctypeslib.as_array(np_, (n * 5,)), ref.nlp, rtol=1e-14, atol=1e-14)
+
+
+def test_executables_fail_loudly_without_gpu(tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    exe = os.path.join(BIN, "fbse_filter")
+    assert os.path.exists(exe), "build() makes the drop-in executables"
+    for f in ("input.par", "conf.par", "potCs.par", "potPb.par", "potI.par", "SO_Cs.par", "SO_Pb.par", "SO_I.par"):
+        shutil.copy(os.path.join(GOLD, "cspbi3", f), tmp_path / f)
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert "ERROR" in r.stderr
+    assert not (tmp_path / "eval.dat").exists()
