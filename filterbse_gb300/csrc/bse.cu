@@ -22,6 +22,7 @@
 //               transition dipoles / oscillator strengths of calc_optical_exc
 //               (bse_cplx/optical.c:6-99).
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <vector>
 
@@ -185,9 +186,24 @@ __global__ void k_sum_parts(const double2 *__restrict__ part, int nchunk, long n
   }
 }
 
+// the mixed path's contraction runs on the tensor cores (tcgemm.cu, split-TF32
+// products, FP32 accumulation, FP64 split-K sums); FBSE_BSE_TC=0 keeps it on
+// the SIMT kernel below
+static bool bse_tensor_cores()
+{
+  static int v = -1;
+  if (v < 0) v = !(getenv("FBSE_BSE_TC") && atoi(getenv("FBSE_BSE_TC")) == 0);
+  return v == 1;
+}
+
 template <typename T>
 static int cgemm_nt(fbse_ctx *c, const C<T> *A, int ma, const C<T> *B, int nb, long L, double scale, double2 *out)
 {
+  if constexpr (sizeof(T) == 4) {
+    if (bse_tensor_cores())
+      return tc_complex_nt<float>(c, reinterpret_cast<const float *>(A), ma, reinterpret_cast<const float *>(B), nb,
+                                  L, false, scale, out);
+  }
   long nchunk = std::max<long>(1, std::min<long>(64, L / 8192));
   // keep the partials bounded (64 x ma x nb complex doubles)
   while (nchunk > 1 && (double)nchunk * ma * nb * 16.0 > 8.0e9) nchunk /= 2;

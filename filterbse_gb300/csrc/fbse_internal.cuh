@@ -152,6 +152,12 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
 template <typename T>
 int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, double b);
 
+// tensor-core complex products (tcgemm.cu):
+//   out[i][j] = scale * sum_r f(A[i][r]) B[j][r], f = conj when conj_a
+template <typename S>
+int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, bool conj_a, double scale,
+                  double2 *out);
+
 // reductions / vector ops (filter.cu) ------------------------------------------
 template <typename T>
 int state_dots(fbse_ctx *c, const C<T> *x, const C<T> *y, long nstates, long len, double *out_host, int mode);

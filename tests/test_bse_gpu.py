@@ -83,11 +83,13 @@ def test_bse_kernel_fp64_matches_oracle(fbse, cuda, name, nh, ne, gap):
     assert np.all(D[iu] == 0) and np.all(X[iu] == 0)
 
 
-@pytest.mark.parametrize("name", ["cubic24", "cubic64"])
-def test_bse_kernel_mixed_within_tolerance(fbse, cuda, name):
-    g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, name, 3, 4, 1, precision=1)
-    D, X = ctx.bse_kernel(psi_d, 3, 4, lumo, bare, scr)
-    rD, rX = O.bse_kernels(psi, 3, 4, lumo, bare.cpu().numpy(), scr.cpu().numpy(), g)
+# the mixed path contracts on the tensor cores (split-TF32, tcgemm.cu); 12 x 12
+# pairs span two 128-row tiles of the tensor-core GEMM
+@pytest.mark.parametrize("name,nh,ne", [("cubic24", 3, 4), ("cubic64", 3, 4), ("cubic24", 12, 12)])
+def test_bse_kernel_mixed_within_tolerance(fbse, cuda, name, nh, ne):
+    g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, name, nh, ne, 1, precision=1)
+    D, X = ctx.bse_kernel(psi_d, nh, ne, lumo, bare, scr)
+    rD, rX = O.bse_kernels(psi, nh, ne, lumo, bare.cpu().numpy(), scr.cpu().numpy(), g)
     assert _relmax(D.cpu().numpy(), rD) < 3e-5
     assert _relmax(X.cpu().numpy(), rX) < 3e-5
 
