@@ -14,6 +14,18 @@ int set_err(fbse_ctx *c, int code, const std::string &msg)
   return code;
 }
 
+int check_dev_status(fbse_ctx *c)
+{
+  int h[4] = {0, 0, 0, 0};
+  if (!c->dstatus) return FBSE_OK;
+  if (d2h(c->stream, h, c->dstatus, sizeof(h)) != cudaSuccess) return set_err(c, FBSE_ERR_CUDA, "status read");
+  if (h[0]) {
+    cudaMemsetAsync(c->dstatus, 0, sizeof(h), c->stream);
+    return set_err(c, FBSE_ERR_NOCONV, "a kernel's bounded wait for its staged data timed out");
+  }
+  return FBSE_OK;
+}
+
 int ensure(fbse_ctx *c, void **p, size_t *have, size_t need)
 {
   if (*have >= need && *p) return FBSE_OK;
@@ -105,6 +117,8 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
   const double ng_1 = nx_1 * ny_1 * nz_1;
   c->kemax_scaled = g->ke_max * (ny_1 * nx_1 * nz_1);
   FBSE_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  FBSE_CUDA(c, cudaMalloc(&c->dstatus, 4 * sizeof(int)));
+  FBSE_CUDA(c, cudaMemset(c->dstatus, 0, 4 * sizeof(int)));
   int rc;
   if ((rc = plan_axis(c, c->ax[0], (int)g->nx))) return rc;
   if ((rc = plan_axis(c, c->ax[1], (int)g->ny))) return rc;
@@ -218,10 +232,12 @@ void fbse_destroy(fbse_ctx *c)
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (int a = 0; a < 3; a++) free_axis(c->ax[a]);
-  void *bufs[] = {c->k2x, c->k2y, c->k2z, c->k2xf, c->k2yf, c->k2zf, c->pot64, c->pot32, c->wk, c->coef, c->tmp, c->red,
+  void *bufs[] = {c->dstatus, c->k2x, c->k2y, c->k2z, c->k2xf, c->k2yf, c->k2zf, c->pot64, c->pot32, c->wk, c->coef, c->tmp, c->red,
                   c->proj.nl_cnt, c->proj.jxyz, c->proj.y1, c->proj.sop, c->proj.nlp, c->proj.sgn, c->proj.LS,
                   c->proj.y1f, c->proj.sopf, c->proj.nlpf};
   for (void *b : bufs)
+    if (b) cudaFree(b);
+  for (void *b : c->cache)
     if (b) cudaFree(b);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -265,7 +281,7 @@ int fbse_sync(fbse_ctx *c)
 {
   if (!c) return FBSE_ERR_ARG;
   FBSE_CUDA(c, cudaStreamSynchronize(c->stream));
-  return FBSE_OK;
+  return check_dev_status(c);
 }
 
 void *fbse_stream(fbse_ctx *c) { return c ? (void *)c->stream : nullptr; }

@@ -191,9 +191,8 @@ __global__ void k_sum_parts(const double2 *__restrict__ part, int nchunk, long n
 // the SIMT kernel below
 static bool bse_tensor_cores()
 {
-  static int v = -1;
-  if (v < 0) v = !(getenv("FBSE_BSE_TC") && atoi(getenv("FBSE_BSE_TC")) == 0);
-  return v == 1;
+  const char *e = getenv("FBSE_BSE_TC");
+  return !(e && atoi(e) == 0);
 }
 
 template <typename T>

@@ -97,6 +97,12 @@ struct fbse_ctx {
   void *coef = nullptr; size_t coef_bytes = 0;   // projector coefficients
   void *tmp = nullptr; size_t tmp_bytes = 0;     // general
   double *red = nullptr; size_t red_bytes = 0;   // reduction partials
+  int *dstatus = nullptr;                        // device error flags of kernels with bounded waits
+  // large buffers kept between calls (grown on demand, freed by fbse_destroy):
+  // the Newton ring, the Rayleigh-Ritz H psi and rotated states, the
+  // filter job's device copies of the starts and filtered states
+  void *cache[8] = {};
+  size_t cache_bytes[8] = {};
   std::string err;
 };
 
@@ -120,6 +126,15 @@ extern std::atomic<long> g_launches;
   } while (0)
 
 int ensure(fbse_ctx *c, void **p, size_t *have, size_t need);
+enum CacheSlot { kSlotRing = 0, kSlotHpsi, kSlotRot, kSlotJobStarts, kSlotJobStates };
+inline int cached(fbse_ctx *c, int slot, size_t need, void **out)
+{
+  const int rc = ensure(c, &c->cache[slot], &c->cache_bytes[slot], need);
+  *out = c->cache[slot];
+  return rc;
+}
+// reads (and clears) the device error flags of the kernels with bounded waits
+int check_dev_status(fbse_ctx *c);
 
 // host copies ordered on the context's (non-blocking) stream; d2h returns
 // after the data has arrived

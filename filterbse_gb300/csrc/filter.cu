@@ -171,9 +171,10 @@ static int launch_newton_acc(fbse_ctx *c, const C<T> *ring, long j0, int nk, con
   return FBSE_OK;
 }
 
-// ring length: up to 128 slots within 40% of the free device memory
-// (FBSE_NEWTON_RING overrides), at most ncheby
-static long ring_slots(long ncheby, size_t slot_bytes)
+// ring length: up to 128 slots within 40% of the free device memory (the
+// ring the context already holds counts as free; FBSE_NEWTON_RING
+// overrides), at most ncheby
+static long ring_slots(fbse_ctx *c, long ncheby, size_t slot_bytes)
 {
   long K = kMaxRing;
   const char *e = getenv("FBSE_NEWTON_RING");
@@ -183,6 +184,7 @@ static long ring_slots(long ncheby, size_t slot_bytes)
     cudaGetLastError();
     free_b = 0;
   }
+  free_b += c->cache_bytes[kSlotRing];
   while (K > 8 && (double)K * slot_bytes > 0.4 * (double)free_b) K /= 2;
   return ncheby < K ? ncheby : K;
 }
@@ -193,7 +195,7 @@ static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long
 {
   const long len = (long)c->nspin * c->ngrid;
   const long nw = c->is_complex ? nstart : (nstart + 1) / 2;
-  const long K = ring_slots(ncheby, (size_t)nw * len * sizeof(C<T>));
+  const long K = ring_slots(c, ncheby, (size_t)nw * len * sizeof(C<T>));
   // Newton coefficients: real parts only (gen_newton_coeff's are real)
   std::vector<double> are((size_t)m * ncheby);
   for (long t = 0; t < m; t++)
@@ -208,9 +210,13 @@ static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long
   int rc = FBSE_OK;
   if (cudaMalloc(&a_dev, are.size() * sizeof(double)) != cudaSuccess)
     return set_err(c, FBSE_ERR_OOM, "newton coefficients");
-  if (cudaMalloc(&ring, ring_bytes) != cudaSuccess) {
-    cudaFree(a_dev);
-    return set_err(c, FBSE_ERR_OOM, "newton ring buffer");
+  {
+    void *r = nullptr;
+    if (cached(c, kSlotRing, ring_bytes, &r)) {
+      cudaFree(a_dev);
+      return set_err(c, FBSE_ERR_OOM, "newton ring buffer");
+    }
+    ring = reinterpret_cast<C<T> *>(r);
   }
   const double de_1 = 4.0 / de;
   do {
@@ -233,9 +239,9 @@ static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long
     }
     if (rc) break;
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "newton filter");
+    if (!rc) rc = check_dev_status(c);
   } while (0);
   cudaStreamSynchronize(c->stream);
-  cudaFree(ring);
   cudaFree(a_dev);
   return rc;
 }

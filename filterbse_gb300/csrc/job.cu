@@ -27,11 +27,13 @@ extern "C" int fbse_filter_job(fbse_ctx *c, const double *zn, const double *an, 
   const long n = nstart * m;
   double *d0 = nullptr, *df = nullptr;
   int rc = FBSE_OK;
-  if (cudaMalloc(&d0, (size_t)nstart * stlen * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&df, (size_t)n * stlen * sizeof(double)) != cudaSuccess) {
-    cudaGetLastError();
-    if (d0) cudaFree(d0);
-    return set_err(c, FBSE_ERR_OOM, "fbse_filter_job: state buffers");
+  {
+    void *a = nullptr, *b = nullptr;
+    if (cached(c, kSlotJobStarts, (size_t)nstart * stlen * sizeof(double), &a) ||
+        cached(c, kSlotJobStates, (size_t)n * stlen * sizeof(double), &b))
+      return set_err(c, FBSE_ERR_OOM, "fbse_filter_job: state buffers");
+    d0 = (double *)a;
+    df = (double *)b;
   }
   std::vector<double> ev(n), sg(n);
   long nk = 0;
@@ -56,7 +58,5 @@ extern "C" int fbse_filter_job(fbse_ctx *c, const double *zn, const double *an, 
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "fbse_filter_job");
   } while (0);
   cudaStreamSynchronize(c->stream);
-  cudaFree(d0);
-  cudaFree(df);
   return rc;
 }

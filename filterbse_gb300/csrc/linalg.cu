@@ -22,6 +22,8 @@
 #include <cmath>
 #include <numeric>
 
+#include <cstdlib>
+
 #include "fbse_internal.cuh"
 
 namespace cg = cooperative_groups;
@@ -527,8 +529,13 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     return true;
   };
   do {
-    if (!alloc((void **)&hpsi, (size_t)n * stlen * sizeof(double))) break;
-    if (!alloc((void **)&rot, (size_t)n * stlen * sizeof(double))) break;
+    {
+      void *a = nullptr, *b = nullptr;
+      if (cached(c, kSlotHpsi, (size_t)n * stlen * sizeof(double), &a) ||
+          cached(c, kSlotRot, (size_t)n * stlen * sizeof(double), &b)) { rc = FBSE_ERR_OOM; break; }
+      hpsi = (double *)a;
+      rot = (double *)b;
+    }
     if (!alloc(&work, (size_t)2 * nw_chunk * len * sizeof(C<T>))) break;
     const size_t nn = (size_t)n * n;
     if (!alloc((void **)&G, nn * sizeof(double2)) || !alloc((void **)&M, nn * sizeof(double2)) ||
@@ -617,7 +624,7 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "ortho/diag/sigma");
   } while (0);
   cudaStreamSynchronize(c->stream);
-  void *bufs[] = {hpsi, rot, work, G, M, V, X, Hp, Tm, U, Cm, part, lam, Ed, rpart, rsum, fac, keepd, permd};
+  void *bufs[] = {work, G, M, V, X, Hp, Tm, U, Cm, part, lam, Ed, rpart, rsum, fac, keepd, permd};
   for (void *b : bufs)
     if (b) cudaFree(b);
   return rc;

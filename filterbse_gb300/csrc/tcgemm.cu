@@ -20,59 +20,20 @@
 // wait is bounded: on a timeout the kernel records an error code, waits
 // (bounded) for its own copies and MMAs, frees its tensor memory and returns.
 #include <cstdint>
+#include <cstdlib>
 
 #include "fbse_internal.cuh"
+#include "fbse_async.cuh"
 
 namespace fbse {
 namespace tc {
+
+using namespace fbse::async;
 
 constexpr int kBM = 128, kBN = 256, kBK = 32;   // CTA tile: M x N, k block (FP32 elements)
 constexpr int kTileBytes = kBM * kBK * 4;        // one 128 x 32 image: 16 KB
 constexpr int kStageBytes = 6 * kTileBytes;      // Ah, Al (1 image each), Bh, Bl (2 each)
 constexpr int kStages = 2;
-constexpr long kSpinLimit = 1L << 26;            // bounded waits (~ seconds)
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-// bounded wait on the phase with the given parity; returns false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
-{
-  const uint32_t a = smem_u32(bar);
-  for (long it = 0; it < kSpinLimit; it++) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
-{
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
 // 1024 bytes apart (stride byte offset), leading byte offset unused (1)
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
@@ -118,7 +79,7 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar)
 __global__ void __launch_bounds__(128, 1)
     k_tc_gemm_nt(const float *__restrict__ Ah, const float *__restrict__ Al, const float *__restrict__ Bh,
                  const float *__restrict__ Bl, long nkb, long kb_per_split, float *__restrict__ part, long mp,
-                 long np, int *__restrict__ status)
+                 long np, int terms, int *__restrict__ status)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte alignment of the stage buffers (the swizzle atom)
@@ -188,8 +149,10 @@ __global__ void __launch_bounds__(128, 1)
         const uint32_t off = kk * 32;
         const uint32_t first = (it == 0 && kk == 0) ? 0u : 1u;
         mma_tf32(tmem, sw128_desc(a_hi + off), sw128_desc(b_hi + off), first);
-        mma_tf32(tmem, sw128_desc(a_hi + off), sw128_desc(b_lo + off), 1u);
-        mma_tf32(tmem, sw128_desc(a_lo + off), sw128_desc(b_hi + off), 1u);
+        if (terms > 1) {
+          mma_tf32(tmem, sw128_desc(a_hi + off), sw128_desc(b_lo + off), 1u);
+          mma_tf32(tmem, sw128_desc(a_lo + off), sw128_desc(b_hi + off), 1u);
+        }
       }
       mma_commit(&free_bar[s]);  // the stage is free once these MMAs have read it
     }
@@ -249,15 +212,18 @@ __global__ void __launch_bounds__(128, 1)
 // i.e. the row is multiplied into a real dot product with interleaved rows.
 // Images cover rows < mp (zero beyond nrows) and k < 32 nkb (zero beyond 2L).
 // ---------------------------------------------------------------------------
+// round to the nearest TF32 value (10 mantissa bits, ties away from zero) and
+// clear the 13 low bits, so that x - tf32(x) is exactly the part the tensor
+// core does not see
 __device__ __forceinline__ float tf32_round(float x)
 {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+  uint32_t u = __float_as_uint(x);
+  if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;
+  return __uint_as_float(u);
 }
 
 template <typename S>
-__global__ void k_tc_images(const S *__restrict__ src, long nrows, long L, int mode, long mp, long nkb,
+__global__ void k_tc_images(const S *__restrict__ src, long nrows, long L, int mode, long mp, long nkb, long k0,
                             float *__restrict__ hi, float *__restrict__ lo)
 {
   // one thread per (row, 4-element chunk) of the padded operand: 8 chunks per k block
@@ -270,7 +236,7 @@ __global__ void k_tc_images(const S *__restrict__ src, long nrows, long L, int m
     float h[4], l[4];
 #pragma unroll
     for (int e = 0; e < 4; e++) {
-      const long k = kb * kBK + c * 4 + e;  // real index
+      const long k = k0 + kb * kBK + c * 4 + e;  // real index
       float v = 0.0f;
       if (row < nrows && k < 2 * L) {
         const long p = k >> 1;
@@ -334,14 +300,27 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
   using namespace tc;
   const long mp = ((ma + kBM - 1) / kBM) * kBM;
   const long np = ((nb + kBN - 1) / kBN) * kBN;
-  const long nkb = (2 * L + kBK - 1) / kBK;
-  // splits: about two CTAs per SM, each split at least 64 k blocks
+  const long nkb_all = (2 * L + kBK - 1) / kBK;
+  // the images of a K chunk (A hi/lo, two B modes hi/lo) within 24 GB
+  // (FBSE_TC_IMAGE_BYTES overrides the budget)
+  const double budget = getenv("FBSE_TC_IMAGE_BYTES") ? atof(getenv("FBSE_TC_IMAGE_BYTES")) : 24.0e9;
+  long nkb_c = std::max<long>(1, (long)(budget / ((2.0 * mp + 4.0 * np) * kBK * 4.0)));
+  if (nkb_c > nkb_all) nkb_c = nkb_all;
+  const long nchunk = (nkb_all + nkb_c - 1) / nkb_c;
+  // splits per chunk: at most 64 k blocks (768 accumulating MMAs) per split --
+  // the tensor core's FP32 accumulation truncates, so its error grows with the
+  // number of MMAs summed into one accumulator -- with the FP32 partials of
+  // all chunks within 16 GB and at least two CTAs per SM
   const long tiles = (mp / kBM) * (np / kBN);
-  long nsplit = std::max<long>(1, std::min<long>((2 * 152) / std::max<long>(1, tiles), nkb / 64));
-  if (nsplit > 1024) nsplit = 1024;
-  const long kbs = (nkb + nsplit - 1) / nsplit;
-  nsplit = (nkb + kbs - 1) / kbs;
-  const size_t img_a = (size_t)mp * nkb * kBK, img_b = (size_t)np * nkb * kBK;  // floats
+  long sps = std::max<long>(1, (nkb_c + 63) / 64);
+  const long max_total = std::max<long>(nchunk, (long)(16.0e9 / (2.0 * 4.0 * mp * np)));
+  if (sps * nchunk > max_total) sps = std::max<long>(1, max_total / nchunk);
+  const long want = std::min<long>(nkb_c, (2 * 152 + tiles - 1) / tiles);
+  if (sps < want) sps = want;
+  const long kbs = (nkb_c + sps - 1) / sps;
+  sps = (nkb_c + kbs - 1) / kbs;
+  const long nsplit = sps * nchunk;
+  const size_t img_a = (size_t)mp * nkb_c * kBK, img_b = (size_t)np * nkb_c * kBK;  // floats
   const size_t part_n = (size_t)nsplit * mp * np;
   float *buf = nullptr;
   int *status = nullptr;
@@ -355,29 +334,41 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
   float *b0h = al + img_a, *b0l = b0h + img_b, *b1h = b0l + img_b, *b1l = b1h + img_b;
   float *p0 = b1l + img_b, *p1 = p0 + part_n;
   int rc = FBSE_OK;
+  // FBSE_TC_TERMS=1 keeps only the hi x hi product (for accuracy studies)
+  const int terms = (getenv("FBSE_TC_TERMS") && atoi(getenv("FBSE_TC_TERMS")) == 1) ? 1 : 3;
   do {
     if (cudaMemsetAsync(status, 0, sizeof(int), c->stream) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "memset"); break; }
+    const size_t smem = (size_t)kStages * kStageBytes + 1024;
+    if (cudaFuncSetAttribute(tc::k_tc_gemm_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "tensor-core GEMM attribute"); break; }
     // real dot products of interleaved rows:
     //   plain  re = A(re, im) . B(re, -im)   im = A(re, im) . B(im, re)
     //   conj_a re = A(re, im) . B(re, im)    im = A(re, -im) . B(im, re)
     const int mb0 = conj_a ? 0 : 1, mb1 = 2;
-    tc::k_tc_images<S><<<grid_of(mp * nkb * 8), 256, 0, c->stream>>>(A, ma, L, 0, mp, nkb, ah, al);
-    tc::k_tc_images<S><<<grid_of(np * nkb * 8), 256, 0, c->stream>>>(B, nb, L, mb0, np, nkb, b0h, b0l);
-    tc::k_tc_images<S><<<grid_of(np * nkb * 8), 256, 0, c->stream>>>(B, nb, L, mb1, np, nkb, b1h, b1l);
-    FBSE_COUNT(3);
-    const size_t smem = (size_t)kStages * kStageBytes + 1024;
-    if (cudaFuncSetAttribute(tc::k_tc_gemm_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "tensor-core GEMM attribute"); break; }
-    dim3 g((unsigned)(mp / kBM), (unsigned)(np / kBN), (unsigned)nsplit);
-    tc::k_tc_gemm_nt<<<g, 128, smem, c->stream>>>(ah, al, b0h, b0l, nkb, kbs, p0, mp, np, status);
-    FBSE_CHECK_LAUNCH(c);
-    if (conj_a) {
-      // imaginary part of <a|b>: sum re_a im_b - im_a re_b = A (re, -im) . B (im, re)
-      tc::k_tc_images<S><<<grid_of(mp * nkb * 8), 256, 0, c->stream>>>(A, ma, L, 1, mp, nkb, ah, al);
-      FBSE_COUNT(1);
+    for (long ch = 0; ch < nchunk && !rc; ch++) {
+      const long k0 = ch * nkb_c * kBK;
+      const long nkb = std::min<long>(nkb_c, nkb_all - ch * nkb_c);
+      const long nsp = (nkb + kbs - 1) / kbs;
+      float *q0 = p0 + (size_t)ch * sps * mp * np, *q1 = p1 + (size_t)ch * sps * mp * np;
+      if (nsp < sps) {  // a short last chunk: its unused partial slots must read as zero
+        cudaMemsetAsync(q0 + (size_t)nsp * mp * np, 0, (size_t)(sps - nsp) * mp * np * sizeof(float), c->stream);
+        cudaMemsetAsync(q1 + (size_t)nsp * mp * np, 0, (size_t)(sps - nsp) * mp * np * sizeof(float), c->stream);
+      }
+      tc::k_tc_images<S><<<grid_of(mp * nkb * 8), 256, 0, c->stream>>>(A, ma, L, 0, mp, nkb, k0, ah, al);
+      tc::k_tc_images<S><<<grid_of(np * nkb * 8), 256, 0, c->stream>>>(B, nb, L, mb0, np, nkb, k0, b0h, b0l);
+      tc::k_tc_images<S><<<grid_of(np * nkb * 8), 256, 0, c->stream>>>(B, nb, L, mb1, np, nkb, k0, b1h, b1l);
+      FBSE_COUNT(3);
+      dim3 g((unsigned)(mp / kBM), (unsigned)(np / kBN), (unsigned)nsp);
+      tc::k_tc_gemm_nt<<<g, 128, smem, c->stream>>>(ah, al, b0h, b0l, nkb, kbs, q0, mp, np, terms, status);
+      FBSE_CHECK_LAUNCH(c);
+      if (conj_a) {
+        tc::k_tc_images<S><<<grid_of(mp * nkb * 8), 256, 0, c->stream>>>(A, ma, L, 1, mp, nkb, k0, ah, al);
+        FBSE_COUNT(1);
+      }
+      tc::k_tc_gemm_nt<<<g, 128, smem, c->stream>>>(ah, al, b1h, b1l, nkb, kbs, q1, mp, np, terms, status);
+      FBSE_CHECK_LAUNCH(c);
     }
-    tc::k_tc_gemm_nt<<<g, 128, smem, c->stream>>>(ah, al, b1h, b1l, nkb, kbs, p1, mp, np, status);
-    FBSE_CHECK_LAUNCH(c);
+    if (rc) break;
     tc::k_tc_reduce<<<grid_of((long)ma * nb), 256, 0, c->stream>>>(p0, p1, (int)nsplit, mp, np, ma, nb, scale, out);
     FBSE_CHECK_LAUNCH(c);
     int hs = 0;
