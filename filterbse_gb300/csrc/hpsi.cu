@@ -49,8 +49,8 @@ constexpr int kNC = 30;             // 5 radial channels x (2 spins x 3 m)
 // that the dependent loads (grid index, then psi) of several points are in
 // flight together.  Then L.S (or the NL sign) per state:
 //   coef[((st*nat + a)*2 + ch)*30 + p*6 + j]
-template <typename T, int kGU>
-__global__ void __launch_bounds__(kProjThreads) k_proj_gather(const C<T> *__restrict__ psi, C<T> *__restrict__ coef,
+template <typename T, int kGU, int MINB>
+__global__ void __launch_bounds__(kProjThreads, MINB) k_proj_gather(const C<T> *__restrict__ psi, C<T> *__restrict__ coef,
                                                               ProjView<T> pv, long nat, long nstates, long ngrid,
                                                               int nspin, int ch0, double dv)
 {
@@ -147,8 +147,8 @@ __device__ __forceinline__ void atomic_add_c(double2 *p, double2 v)
 
 // scatter: out_s(r) += scale * sum_m Y_m(r) sum_p b_p(r) d[p][3 s + m] over the
 // active channels; one warp per state, kSU points per lane per iteration
-template <typename T, bool SO, bool NL, int kSU>
-__global__ void __launch_bounds__(kProjThreads) k_proj_scatter(C<T> *__restrict__ out, const C<T> *__restrict__ coef,
+template <typename T, bool SO, bool NL, int kSU, int MINB>
+__global__ void __launch_bounds__(kProjThreads, MINB) k_proj_scatter(C<T> *__restrict__ out, const C<T> *__restrict__ coef,
                                                                ProjView<T> pv, long nat, long nstates, long ngrid,
                                                                int nspin, T scale)
 {
@@ -227,35 +227,26 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   if (ggroups > 65535 || p.nat > 2147483647L) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector grid too large");
   const int ch0 = c->so ? 0 : 1;
   const int nch = (c->so ? 1 : 0) + (c->nl ? 1 : 0);
-  // points per lane per iteration (memory-level parallelism of the dependent
-  // index -> psi loads): FBSE_PROJ_UNROLL=8 doubles both kernels' default
-  static const int wide = getenv("FBSE_PROJ_UNROLL") && atoi(getenv("FBSE_PROJ_UNROLL")) >= 8;
+  // FP32 (mixed path): two points per lane per iteration with a register cap
+  // for 8 CTAs per SM (more warps in flight instead of more loads per warp;
+  // 0.52 -> 0.50 ms per 16-state spinor batch at 128^3).  FP64: four (gather)
+  // / two (scatter) points per lane, no cap (the cap spills there).
+  constexpr bool occ = sizeof(T) == 4;
+  constexpr int kGU = occ ? 2 : 4;
+  constexpr int kMinB = occ ? 8 : 1;
   dim3 gg((unsigned)p.nat, (unsigned)nch, (unsigned)ggroups);
-  if (wide)
-    k_proj_gather<T, 8><<<gg, kProjThreads, 0, c->stream>>>(in, coef, view<T>(c), p.nat, nstates, c->ngrid, c->nspin,
-                                                            ch0, c->dv);
-  else
-    k_proj_gather<T, 4><<<gg, kProjThreads, 0, c->stream>>>(in, coef, view<T>(c), p.nat, nstates, c->ngrid, c->nspin,
-                                                            ch0, c->dv);
+  const ProjView<T> pv = view<T>(c);
+  k_proj_gather<T, kGU, kMinB><<<gg, kProjThreads, 0, c->stream>>>(in, coef, pv, p.nat, nstates, c->ngrid, c->nspin,
+                                                                   ch0, c->dv);
   FBSE_CHECK_LAUNCH(c);
   dim3 gs((unsigned)p.nat, (unsigned)ngroups);
-  const ProjView<T> pv = view<T>(c);
   const T sc = (T)scale;
-  if (wide) {
-    if (c->so && c->nl)
-      k_proj_scatter<T, true, true, 4><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
-    else if (c->so)
-      k_proj_scatter<T, true, false, 4><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
-    else
-      k_proj_scatter<T, false, true, 4><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
-  } else {
-    if (c->so && c->nl)
-      k_proj_scatter<T, true, true, 2><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
-    else if (c->so)
-      k_proj_scatter<T, true, false, 2><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
-    else
-      k_proj_scatter<T, false, true, 2><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
-  }
+  if (c->so && c->nl)
+    k_proj_scatter<T, true, true, 2, kMinB><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+  else if (c->so)
+    k_proj_scatter<T, true, false, 2, kMinB><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+  else
+    k_proj_scatter<T, false, true, 2, kMinB><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
   FBSE_CHECK_LAUNCH(c);
   return FBSE_OK;
 }
