@@ -25,10 +25,11 @@ MIXED = 1
 EXPORTED = [
     "fbse_create", "fbse_destroy", "fbse_last_error", "fbse_version", "fbse_alloc", "fbse_free",
     "fbse_upload", "fbse_download", "fbse_sync", "fbse_stream", "fbse_hpsi", "fbse_hnorm",
-    "fbse_newton_filter", "fbse_energy_range", "fbse_normalize_all", "fbse_energy_all",
+    "fbse_newton_filter", "fbse_energy_range", "fbse_normalize_all", "fbse_energy_all", "fbse_sigma_e",
     "fbse_ortho_diag_sigma", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
     "fbse_init_filter_states", "fbse_launch_count", "fbse_filter_job", "fbse_build_local_pot",
-    "fbse_bse_potentials", "fbse_bse_kernel", "fbse_bse_solve", "fbse_bse_dipoles", "fbse_bse_optical",
+    "fbse_bse_potentials", "fbse_bse_kernel", "fbse_bse_kernel_real", "fbse_bse_solve", "fbse_bse_dipoles", "fbse_bse_mag_dipoles",
+    "fbse_bse_optical",
     "fbse_normalize_all_noalloc",
 ]
 
@@ -84,6 +85,7 @@ def load() -> ctypes.CDLL:
     L.fbse_energy_range.argtypes = [_VP, ctypes.c_long, ctypes.c_long, _D, _D, ctypes.POINTER(ctypes.c_long)]
     L.fbse_normalize_all.argtypes = [_VP, _VP, ctypes.c_long, _D]
     L.fbse_energy_all.argtypes = [_VP, _VP, ctypes.c_long, _D]
+    L.fbse_sigma_e.argtypes = [_VP, _VP, ctypes.c_long, _D, _D]
     L.fbse_ortho_diag_sigma.argtypes = [_VP, _VP, ctypes.c_long, ctypes.POINTER(ctypes.c_long), _D, _D]
     L.fbse_samp_points.argtypes = [ctypes.c_long, _D]
     L.fbse_samp_points.restype = ctypes.c_double
@@ -102,6 +104,8 @@ def load() -> ctypes.CDLL:
     L.fbse_bse_solve.argtypes = [_VP, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_long, _VP, _VP, _D,
                                  _VP, _D, _D, _D, _D]
     L.fbse_bse_dipoles.argtypes = [_VP, _VP, _D, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D]
+    L.fbse_bse_kernel_real.argtypes = [_VP, _VP, ctypes.c_long, ctypes.c_long, ctypes.c_long, _VP, _VP, _VP, _VP]
+    L.fbse_bse_mag_dipoles.argtypes = [_VP, _VP, _D, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D]
     L.fbse_bse_optical.argtypes = [_VP, _VP, _D, ctypes.c_long, ctypes.c_long, _D]
     _lib = L
     return L
@@ -285,6 +289,15 @@ class Context:
         self._chk(self._L.fbse_energy_all(self._h, self._ptr(psitot), n, _dp(e)))
         return e
 
+    def sigma_e(self, psitot):
+        """calc_sigma_E: (eval, sigma) of n psitot states (device)."""
+        n = psitot.shape[0]
+        e = np.empty(n)
+        sg = np.empty(n)
+        self._torch_sync()
+        self._chk(self._L.fbse_sigma_e(self._h, self._ptr(psitot), n, _dp(e), _dp(sg)))
+        return e, sg
+
     def filter_job(self, zn, an, vmin, de, psi0_host, sigma_cut=0.0, psi_out=None):
         """Whole filter stage on host buffers (fbse_filter_job): returns
         (n, eval, sigma); psi_out (host float64 [nstart*m, stlen], optional,
@@ -341,6 +354,19 @@ class Context:
                                           self._ptr(pot_screened), self._ptr(d), self._ptr(x)))
         return d, x
 
+    def bse_kernel_real(self, psi_qp, n_h, n_e, lumo_idx, pot_bare, pot_screened):
+        """calc_eh_kernel_cplx of bse_real: psi_qp [n_qp, ngrid] float64 CUDA
+        (real states, nspin = 1); returns (direct, exchange) [n_xton, n_xton]
+        float64, lower triangles, exchange with the singlet factor 2."""
+        import torch
+        n = n_h * n_e
+        d = torch.zeros((n, n), dtype=torch.float64, device=psi_qp.device)
+        x = torch.zeros_like(d)
+        self._torch_sync()
+        self._chk(self._L.fbse_bse_kernel_real(self._h, self._ptr(psi_qp), n_h, n_e, lumo_idx, self._ptr(pot_bare),
+                                               self._ptr(pot_screened), self._ptr(d), self._ptr(x)))
+        return d, x
+
     def bse_solve(self, eval_qp, n_h, n_e, lumo_idx, direct, exchange):
         """build_BSE_mat + bethe_salpeter: returns (xton_ene, coeff, <H>, <Kd>,
         <Kx>, <h0>); coeff [n_xton, n_xton] complex128 CUDA, column j = exciton j.
@@ -364,6 +390,15 @@ class Context:
         self._chk(self._L.fbse_bse_dipoles(self._h, self._ptr(psi_qp), _dp(gx), _dp(gy), _dp(gz), n_h, n_e,
                                            lumo_idx, _dp(mu.view(np.float64))))
         return mu.reshape(-1, 3)
+
+    def bse_mag_dipoles(self, psi_qp, gx, gy, gz, n_h, n_e, lumo_idx):
+        """calc_mag_dipole: returns m [n_h*n_e, 3] complex128 (numpy), row i*n_e+a."""
+        gx, gy, gz = (np.ascontiguousarray(a, np.float64) for a in (gx, gy, gz))
+        m = np.empty(n_h * n_e * 3, np.complex128)
+        self._torch_sync()
+        self._chk(self._L.fbse_bse_mag_dipoles(self._h, self._ptr(psi_qp), _dp(gx), _dp(gy), _dp(gz), n_h, n_e,
+                                               lumo_idx, _dp(m.view(np.float64))))
+        return m.reshape(-1, 3)
 
     def bse_optical(self, coeff, mu_pairs, n_h, n_e):
         """calc_optical_exc (electric part): exciton dipoles [n_xton, 3] complex128

@@ -48,7 +48,7 @@ int ensure(fbse_ctx *c, void **p, size_t *have, size_t need)
 int newton_filter(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
                   const double *psi0, long nstart, double *filtered);
 int normalize_all(fbse_ctx *c, double *psitot, long n, double *norms);
-int energy_all(fbse_ctx *c, const double *psitot, long n, double *ene);
+int energy_all(fbse_ctx *c, const double *psitot, long n, double *ene, double *sigma);
 int energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *emax, long *iters);
 int ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma);
 
@@ -159,17 +159,21 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
         if (j < 0 || j >= c->ngrid) return set_err(c, FBSE_ERR_ARG, "projector table: grid index out of range");
       }
     }
-    // entries beyond nl[a] are never read; zero-fill copies keep them finite
+    // entries beyond nl[a] are never read; zero-fill copies keep them finite.
+    // Device layout is structure-of-arrays so that a warp reading 32
+    // consecutive entries issues one coalesced load per quantity:
+    //   y1[(m*ne + i)*2 + {re, im}],  so/nl[p*ne + i]   (i = a*npts + e)
     std::vector<int> jx(ne, 0);
     std::vector<double> y1(ne * 6, 0.0), so(ne * p.nproj, 0.0), nlr(ne * p.nproj, 0.0);
     for (long a = 0; a < p.nat; a++)
       for (long e = 0; e < pj->nl[a]; e++) {
         const size_t i = a * p.npts + e;
         jx[i] = pj->jxyz[i];
-        for (int k = 0; k < 6; k++) y1[i * 6 + k] = pj->y1[i * 6 + k];
+        for (int m = 0; m < 3; m++)
+          for (int k = 0; k < 2; k++) y1[(m * ne + i) * 2 + k] = pj->y1[i * 6 + 2 * m + k];
         for (int k = 0; k < p.nproj; k++) {
-          so[i * p.nproj + k] = pj->so_proj ? pj->so_proj[i * p.nproj + k] : 0.0;
-          nlr[i * p.nproj + k] = pj->nl_proj ? pj->nl_proj[i * p.nproj + k] : 0.0;
+          so[k * ne + i] = pj->so_proj ? pj->so_proj[i * p.nproj + k] : 0.0;
+          nlr[k * ne + i] = pj->nl_proj ? pj->nl_proj[i * p.nproj + k] : 0.0;
         }
       }
     std::vector<int> sg((size_t)(p.nat > 0 ? p.nat : 1) * p.nproj, 0);
@@ -328,7 +332,13 @@ int fbse_normalize_all(fbse_ctx *c, double *psitot, long n, double *norms)
 int fbse_energy_all(fbse_ctx *c, const double *psitot, long n, double *ene)
 {
   if (!c || !psitot || !ene) return c ? set_err(c, FBSE_ERR_ARG, "fbse_energy_all: null") : FBSE_ERR_ARG;
-  return energy_all(c, psitot, n, ene);
+  return energy_all(c, psitot, n, ene, nullptr);
+}
+
+int fbse_sigma_e(fbse_ctx *c, const double *psitot, long n, double *eval, double *sigma)
+{
+  if (!c || !psitot || !eval || !sigma) return c ? set_err(c, FBSE_ERR_ARG, "fbse_sigma_e: null") : FBSE_ERR_ARG;
+  return energy_all(c, psitot, n, eval, sigma);
 }
 
 int fbse_ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma)

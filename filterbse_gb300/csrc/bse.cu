@@ -448,6 +448,81 @@ __global__ void k_xton_dipoles(const double2 *__restrict__ Cm, const double2 *__
   }
 }
 
+// ---------------------------------------------------------------------------
+// magnetic transition dipoles (calc_mag_dipole, bse_cplx/dipole.c:160-331):
+// p_d psi_a = IFFT(k_d FFT psi_a) per spin block (p_operator,
+// bse_cplx/ang_mom_operators.c:105-170, k_d from init_kvec with the 1/N of the
+// two unnormalised transforms), L psi = -(r x p psi) (l_operator, :6-52), and
+//   m[(i * ne + a) * 3 + d] = (dv / 2) sum_{r,sigma} conj(psi_i) (L psi_a)_d
+// One CTA per hole i for the electron a whose p psi_a is in P[3][nspin][N].
+// ---------------------------------------------------------------------------
+__global__ void k_mag_dots(const double2 *__restrict__ psi, long nsg, long ngrid, int nspin, int nx, int ny,
+                           const double *__restrict__ gx, const double *__restrict__ gy, const double *__restrict__ gz,
+                           const double2 *__restrict__ P, int ne, int a, double dv, double2 *__restrict__ m)
+{
+  const int i = blockIdx.x;
+  const double2 *pi = psi + (long)i * nsg;
+  const double2 *Px = P, *Py = P + nsg, *Pz = P + 2 * nsg;
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (long g = threadIdx.x; g < ngrid; g += blockDim.x) {
+    const double x = gx[g % nx], y = gy[(g / nx) % ny], z = gz[g / ((long)nx * ny)];
+    for (int sp = 0; sp < nspin; sp++) {
+      const long q = sp * ngrid + g;
+      const double2 u = pi[q], px = Px[q], py = Py[q], pz = Pz[q];
+      const double2 l[3] = {make_double2(-(y * pz.x - z * py.x), -(y * pz.y - z * py.y)),
+                            make_double2(-(z * px.x - x * pz.x), -(z * px.y - x * pz.y)),
+                            make_double2(-(x * py.x - y * px.x), -(x * py.y - y * px.y))};
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        s[2 * d] += u.x * l[d].x + u.y * l[d].y;  // conj(u) l
+        s[2 * d + 1] += u.x * l[d].y - u.y * l[d].x;
+      }
+    }
+  }
+  __shared__ double red[32][6];
+  for (int k = 0; k < 6; k++) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[w][threadIdx.x];
+    red[0][threadIdx.x] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3)
+    m[(long)(i * ne + a) * 3 + threadIdx.x] =
+        make_double2(0.5 * dv * red[0][2 * threadIdx.x], 0.5 * dv * red[0][2 * threadIdx.x + 1]);
+}
+
+// real quasiparticle states as complex ones (imaginary part 0), and the real
+// parts of complex kernels back, scaled
+__global__ void k_real_to_cplx(const double *__restrict__ src, double2 *__restrict__ dst, long n)
+{
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    dst[e] = make_double2(src[e], 0.0);
+}
+
+__global__ void k_real_part(const double2 *__restrict__ src, double *__restrict__ dst, long n, double scale)
+{
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    dst[e] = scale * src[e].x;
+}
+
+// init_kvec (ang_mom_operators.c:90-103): k[j] = j dk norm, k[n-j] = -j dk norm
+// for j = 1..n/2 in that order (for even n the second write leaves k[n/2] < 0)
+static void init_kvec(std::vector<double> &k, long n, double dk, double norm)
+{
+  k.assign(n, 0.0);
+  const long npos = (n % 2 == 0) ? n / 2 : (n - 1) / 2;
+  for (long j = 1; j <= npos; j++) {
+    k[j] = j * dk * norm;
+    k[n - j] = -(j * dk * norm);
+  }
+}
+
 }  // namespace fbse
 
 using namespace fbse;
@@ -516,6 +591,48 @@ int fbse_bse_kernel(fbse_ctx *c, const double *psi_qp, long n_h, long n_e, long 
   if (c->precision == FBSE_MIXED)
     return eh_kernels_t<float>(c, psi_qp, n_h, n_e, lumo_idx, pot_bare, pot_screened, direct, exchange);
   return eh_kernels_t<double>(c, psi_qp, n_h, n_e, lumo_idx, pot_bare, pot_screened, direct, exchange);
+}
+
+int fbse_bse_kernel_real(fbse_ctx *c, const double *psi_qp, long n_h, long n_e, long lumo_idx, const double *pot_bare,
+                         const double *pot_screened, double *direct, double *exchange)
+{
+  if (!c || !psi_qp || !pot_bare || !pot_screened || !direct || !exchange || n_h < 1 || n_e < 1 || lumo_idx < n_h)
+    return c ? set_err(c, FBSE_ERR_ARG, "fbse_bse_kernel_real: bad arguments") : FBSE_ERR_ARG;
+  if (c->nspin != 1) return set_err(c, FBSE_ERR_UNSUPPORTED, "fbse_bse_kernel_real: one spin component per state");
+  const long N = c->ngrid, nq = lumo_idx + n_e, nx = n_h * n_e;
+  double2 *pc = nullptr, *dc = nullptr, *xc = nullptr;
+  if (cudaMalloc(&pc, nq * N * sizeof(double2)) != cudaSuccess || cudaMalloc(&dc, nx * nx * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&xc, nx * nx * sizeof(double2)) != cudaSuccess) {
+    cudaGetLastError();
+    if (pc) cudaFree(pc);
+    if (dc) cudaFree(dc);
+    return set_err(c, FBSE_ERR_OOM, "fbse_bse_kernel_real");
+  }
+  int rc = FBSE_OK;
+  k_real_to_cplx<<<gridn(nq * N), 256, 0, c->stream>>>(psi_qp, pc, nq * N);
+  FBSE_COUNT(1);
+  if (cudaGetLastError() != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "fbse_bse_kernel_real");
+  if (!rc)
+    rc = c->precision == FBSE_MIXED
+             ? eh_kernels_t<float>(c, (const double *)pc, n_h, n_e, lumo_idx, pot_bare, pot_screened, (double *)dc,
+                                   (double *)xc)
+             : eh_kernels_t<double>(c, (const double *)pc, n_h, n_e, lumo_idx, pot_bare, pot_screened, (double *)dc,
+                                    (double *)xc);
+  if (!rc) {
+    // bse_real/coulomb.c: K^d = dv sum Re(W * rho_ab) psi_j psi_i; K^x carries the
+    // singlet factor 2 (exchange = -2 sum, coulomb.c:568; hartree keeps the real
+    // part of the convolution, hartree.c:31)
+    k_real_part<<<gridn(nx * nx), 256, 0, c->stream>>>(dc, direct, nx * nx, 1.0);
+    k_real_part<<<gridn(nx * nx), 256, 0, c->stream>>>(xc, exchange, nx * nx, 2.0);
+    FBSE_COUNT(2);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
+      rc = set_err(c, FBSE_ERR_CUDA, "fbse_bse_kernel_real");
+  }
+  cudaStreamSynchronize(c->stream);
+  cudaFree(pc);
+  cudaFree(dc);
+  cudaFree(xc);
+  return rc;
 }
 
 int fbse_bse_solve(fbse_ctx *c, const double *eval_qp_host, long n_qp, long n_h, long n_e, long lumo_idx,
@@ -620,6 +737,66 @@ int fbse_bse_dipoles(fbse_ctx *c, const double *psi_qp, const double *gx, const 
     rc = set_err(c, FBSE_ERR_CUDA, "fbse_bse_dipoles");
   cudaFree(dg);
   cudaFree(mu);
+  return rc;
+}
+
+int fbse_bse_mag_dipoles(fbse_ctx *c, const double *psi_qp, const double *gx, const double *gy, const double *gz,
+                         long n_h, long n_e, long lumo_idx, double *m_host)
+{
+  if (!c || !psi_qp || !gx || !gy || !gz || !m_host || n_h < 1 || n_e < 1 || lumo_idx < n_h)
+    return c ? set_err(c, FBSE_ERR_ARG, "fbse_bse_mag_dipoles: bad arguments") : FBSE_ERR_ARG;
+  if (!c->is_complex) return set_err(c, FBSE_ERR_UNSUPPORTED, "fbse_bse_mag_dipoles: complex states required");
+  const long N = c->ngrid, nsg = (long)c->nspin * N;
+  // k_d multipliers in the transform's (z, y, x) order, with 1/N
+  std::vector<double> kx, ky, kz;
+  const double norm = 1.0 / (double)N;
+  auto dk = [](long n, double d) { return 2.0 * M_PI / (n * d); };  // bse_cplx/read.c:347-349
+  init_kvec(kx, c->nx, dk(c->nx, c->dx), norm);
+  init_kvec(ky, c->ny, dk(c->ny, c->dy), norm);
+  init_kvec(kz, c->nz, dk(c->nz, c->dz), norm);
+  std::vector<double2> kq((size_t)3 * N);
+  for (long g = 0; g < N; g++) {
+    kq[g] = make_double2(kx[g % c->nx], 0.0);
+    kq[N + g] = make_double2(ky[(g / c->nx) % c->ny], 0.0);
+    kq[2 * N + g] = make_double2(kz[g / (c->nx * c->ny)], 0.0);
+  }
+  double2 *dk3 = nullptr, *P = nullptr, *work = nullptr, *m = nullptr;
+  double *dg = nullptr;
+  int rc = FBSE_OK;
+  if (cudaMalloc(&dk3, 3 * N * sizeof(double2)) != cudaSuccess || cudaMalloc(&P, 3 * nsg * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&work, nsg * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&m, n_h * n_e * 3 * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&dg, (c->nx + c->ny + c->nz) * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    rc = set_err(c, FBSE_ERR_OOM, "fbse_bse_mag_dipoles");
+  }
+  do {
+    if (rc) break;
+    if (h2d(c->stream, dk3, kq.data(), 3 * N * sizeof(double2)) != cudaSuccess ||
+        h2d(c->stream, dg, gx, c->nx * sizeof(double)) != cudaSuccess ||
+        h2d(c->stream, dg + c->nx, gy, c->ny * sizeof(double)) != cudaSuccess ||
+        h2d(c->stream, dg + c->nx + c->ny, gz, c->nz * sizeof(double)) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "fbse_bse_mag_dipoles upload");
+      break;
+    }
+    for (long a = 0; a < n_e && !rc; a++) {
+      const double2 *pa = (const double2 *)psi_qp + (lumo_idx + a) * nsg;
+      for (int d = 0; d < 3 && !rc; d++) rc = conv_apply<double>(c, pa, P + d * nsg, work, c->nspin, dk3 + d * N);
+      if (rc) break;
+      k_mag_dots<<<(unsigned)n_h, 256, 0, c->stream>>>((const double2 *)psi_qp, nsg, N, c->nspin, (int)c->nx,
+                                                        (int)c->ny, dg, dg + c->nx, dg + c->nx + c->ny, P, (int)n_e,
+                                                        (int)a, c->dv, m);
+      FBSE_COUNT(1);
+      if (cudaGetLastError() != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "fbse_bse_mag_dipoles launch");
+    }
+    if (rc) break;
+    if (d2h(c->stream, m_host, m, n_h * n_e * 3 * sizeof(double2)) != cudaSuccess)
+      rc = set_err(c, FBSE_ERR_CUDA, "fbse_bse_mag_dipoles download");
+  } while (0);
+  cudaStreamSynchronize(c->stream);
+  void *bufs[] = {dk3, P, work, m, dg};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
   return rc;
 }
 

@@ -68,9 +68,9 @@ struct ProjDev {
   int so = 0, nl = 0;
   int *nl_cnt = nullptr;      // [nat]
   int *jxyz = nullptr;        // [nat*npts]
-  double *y1 = nullptr;       // [nat*npts*6]
-  double *sop = nullptr;      // [nat*npts*nproj]
-  double *nlp = nullptr;      // [nat*npts*nproj]
+  double *y1 = nullptr;       // [3][nat*npts] complex Y_1m (structure of arrays)
+  double *sop = nullptr;      // [nproj][nat*npts]
+  double *nlp = nullptr;      // [nproj][nat*npts]
   int *sgn = nullptr;         // [nat*nproj]
   double2 *LS = nullptr;      // [36]
   float *y1f = nullptr, *sopf = nullptr, *nlpf = nullptr;  // FP32 copies for the mixed path

@@ -404,7 +404,7 @@ int normalize_all(fbse_ctx *c, double *psitot, long n, double *norms)
 }
 
 template <typename T>
-static int energy_all_t(fbse_ctx *c, const double *psitot, long n, double *ene)
+static int energy_all_t(fbse_ctx *c, const double *psitot, long n, double *ene, double *sigma)
 {
   const long len = (long)c->nspin * c->ngrid;
   const long nw = c->is_complex ? n : (n + 1) / 2;
@@ -412,21 +412,33 @@ static int energy_all_t(fbse_ctx *c, const double *psitot, long n, double *ene)
   const long chunk = nw < 16 ? nw : 16;
   C<T> *buf = nullptr;
   if (cudaMalloc(&buf, 2 * chunk * len * sizeof(C<T>)) != cudaSuccess) return set_err(c, FBSE_ERR_OOM, "energy_all");
-  std::vector<double> h(2 * chunk);
+  std::vector<double> h(2 * chunk), h2(2 * chunk);
   int rc = FBSE_OK;
   const long stlen = (long)(c->is_complex + 1) * len;
+  // sigma_E = sqrt|<H^2> - <H>^2| with <H^2> = dv <H psi|H psi> (calc_sigma_E,
+  // energy.c:383-539, applies H twice and takes <psi|H H psi>; the same for
+  // Hermitian H)
+  auto sig = [&](double e2, double e) { return std::sqrt(std::fabs(e2 * c->dv - e * e)); };
   for (long w0 = 0; w0 < nw && !rc; w0 += chunk) {
     const long cw = (nw - w0 < chunk) ? nw - w0 : chunk;
     const long s0 = c->is_complex ? w0 : 2 * w0;
     const long ns = c->is_complex ? cw : ((n - s0) < 2 * cw ? n - s0 : 2 * cw);
+    C<T> *hb = buf + chunk * len;
     if ((rc = pack<T>(c, psitot + s0 * stlen, buf, ns))) break;
-    if ((rc = hpsi_apply<T>(c, buf, buf + chunk * len, cw, 1.0, 0.0))) break;
-    if ((rc = state_dots<T>(c, buf, buf + chunk * len, cw, len, h.data(), c->is_complex ? 1 : 2))) break;
+    if ((rc = hpsi_apply<T>(c, buf, hb, cw, 1.0, 0.0))) break;
+    if ((rc = state_dots<T>(c, buf, hb, cw, len, h.data(), c->is_complex ? 1 : 2))) break;
+    if (sigma && (rc = state_dots<T>(c, hb, hb, cw, len, h2.data(), c->is_complex ? 0 : 2))) break;
     for (long w = 0; w < cw; w++) {
-      if (c->is_complex) ene[s0 + w] = h[2 * w] * c->dv;
-      else {
+      if (c->is_complex) {
+        ene[s0 + w] = h[2 * w] * c->dv;
+        if (sigma) sigma[s0 + w] = sig(h2[2 * w], ene[s0 + w]);
+      } else {
         ene[s0 + 2 * w] = h[2 * w] * c->dv;
-        if (s0 + 2 * w + 1 < n) ene[s0 + 2 * w + 1] = h[2 * w + 1] * c->dv;
+        if (sigma) sigma[s0 + 2 * w] = sig(h2[2 * w], ene[s0 + 2 * w]);
+        if (s0 + 2 * w + 1 < n) {
+          ene[s0 + 2 * w + 1] = h[2 * w + 1] * c->dv;
+          if (sigma) sigma[s0 + 2 * w + 1] = sig(h2[2 * w + 1], ene[s0 + 2 * w + 1]);
+        }
       }
     }
   }
@@ -434,10 +446,11 @@ static int energy_all_t(fbse_ctx *c, const double *psitot, long n, double *ene)
   return rc;
 }
 
-int energy_all(fbse_ctx *c, const double *psitot, long n, double *ene)
+int energy_all(fbse_ctx *c, const double *psitot, long n, double *ene, double *sigma)
 {
   if (n < 1) return FBSE_OK;
-  return c->precision == FBSE_MIXED ? energy_all_t<float>(c, psitot, n, ene) : energy_all_t<double>(c, psitot, n, ene);
+  return c->precision == FBSE_MIXED ? energy_all_t<float>(c, psitot, n, ene, sigma)
+                                    : energy_all_t<double>(c, psitot, n, ene, sigma);
 }
 
 // ---------------------------------------------------------------------------

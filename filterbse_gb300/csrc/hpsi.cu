@@ -20,11 +20,15 @@
 
 namespace fbse {
 
+// Table entries i = a*npts + e in structure-of-arrays form (one coalesced
+// load per quantity for 32 consecutive entries): y1[m*ne + i] = Y_1m as a
+// complex, sop/nlp[p*ne + i] = radial value of channel p.
 template <typename T> struct ProjView {
   const int *cnt, *jxyz, *sgn;
-  const T *y1, *sop, *nlp;
+  const C<T> *y1;
+  const T *sop, *nlp;
   const double2 *LS;
-  long npts;
+  long npts, ne;
   int nproj;
 };
 
@@ -32,12 +36,14 @@ template <typename T> static ProjView<T> view(fbse_ctx *c);
 template <> ProjView<double> view<double>(fbse_ctx *c)
 {
   const ProjDev &p = c->proj;
-  return {p.nl_cnt, p.jxyz, p.sgn, p.y1, p.sop, p.nlp, p.LS, p.npts, p.nproj};
+  return {p.nl_cnt, p.jxyz, p.sgn, reinterpret_cast<const double2 *>(p.y1), p.sop, p.nlp, p.LS, p.npts,
+          p.nat * p.npts, p.nproj};
 }
 template <> ProjView<float> view<float>(fbse_ctx *c)
 {
   const ProjDev &p = c->proj;
-  return {p.nl_cnt, p.jxyz, p.sgn, p.y1f, p.sopf, p.nlpf, p.LS, p.npts, p.nproj};
+  return {p.nl_cnt, p.jxyz, p.sgn, reinterpret_cast<const float2 *>(p.y1f), p.sopf, p.nlpf, p.LS, p.npts,
+          p.nat * p.npts, p.nproj};
 }
 
 constexpr int kSW = 4;              // warps per CTA
@@ -47,17 +53,20 @@ constexpr int kNC = 30;             // 5 radial channels x (2 spins x 3 m)
 // gather: one warp per (state, spin s'); each lane accumulates the 15
 // coefficients b_p conj(Y_m) psi_s' of its points, kGU points per iteration so
 // that the dependent loads (grid index, then psi) of several points are in
-// flight together.  Then L.S (or the NL sign) per state:
+// flight together; the grid indices of the next iteration are loaded before
+// the current iteration's arithmetic, so only the psi load is on the critical
+// path.  W warps per CTA (W / nspin states) share every table entry through
+// L1.  Then L.S (or the NL sign) per state:
 //   coef[((st*nat + a)*2 + ch)*30 + p*6 + j]
-template <typename T, int kGU, int MINB>
-__global__ void __launch_bounds__(kProjThreads, MINB) k_proj_gather(const C<T> *__restrict__ psi, C<T> *__restrict__ coef,
+template <typename T, int kGU, int MINB, int W>
+__global__ void __launch_bounds__(32 * W, MINB) k_proj_gather(const C<T> *__restrict__ psi, C<T> *__restrict__ coef,
                                                               ProjView<T> pv, long nat, long nstates, long ngrid,
                                                               int nspin, int ch0, double dv)
 {
   const long a = blockIdx.x;
   const int ch = ch0 + blockIdx.y;  // 0: SO, 1: NL
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int spc = kSW / nspin;  // states per CTA
+  const int spc = W / nspin;  // states per CTA
   const long st = (long)blockIdx.z * spc + wid / nspin;
   const int sp = wid % nspin;
   const bool live = st < nstates;
@@ -65,34 +74,43 @@ __global__ void __launch_bounds__(kProjThreads, MINB) k_proj_gather(const C<T> *
   const C<T> *ps = psi + (live ? st : 0) * nspin * ngrid + (long)sp * ngrid;
   const T *rad = (ch == 0) ? pv.sop : pv.nlp;
   const int npj = pv.nproj;
+  const long ebase = a * pv.npts;
   T acc[30];
 #pragma unroll
   for (int i = 0; i < 30; i++) acc[i] = T(0);
   if (live) {
+    int jn[kGU];
+#pragma unroll
+    for (int u = 0; u < kGU; u++) {
+      const int g = lane + 32 * u;
+      jn[u] = g < np ? pv.jxyz[ebase + g] : -1;
+    }
     for (int g0 = lane; g0 < np; g0 += 32 * kGU) {
       int jx[kGU];
-      long e[kGU];
-#pragma unroll
-      for (int u = 0; u < kGU; u++) {
-        const int g = g0 + 32 * u;
-        e[u] = a * pv.npts + (g < np ? g : 0);
-        jx[u] = g < np ? pv.jxyz[e[u]] : -1;
-      }
       C<T> v[kGU];
 #pragma unroll
-      for (int u = 0; u < kGU; u++) v[u] = jx[u] >= 0 ? ps[jx[u]] : mk<T>(T(0), T(0));
+      for (int u = 0; u < kGU; u++) {
+        jx[u] = jn[u];
+        v[u] = jx[u] >= 0 ? ps[jx[u]] : mk<T>(T(0), T(0));
+      }
+#pragma unroll
+      for (int u = 0; u < kGU; u++) {
+        const int g = g0 + 32 * (kGU + u);
+        jn[u] = g < np ? pv.jxyz[ebase + g] : -1;
+      }
 #pragma unroll
       for (int u = 0; u < kGU; u++) {
         if (jx[u] < 0) continue;
+        const long e = ebase + g0 + 32 * u;
         T b[5];
 #pragma unroll
-        for (int p = 0; p < 5; p++) b[p] = (p < npj) ? rad[e[u] * npj + p] : T(0);
+        for (int p = 0; p < 5; p++) b[p] = (p < npj) ? rad[p * pv.ne + e] : T(0);
 #pragma unroll
         for (int m = 0; m < 3; m++) {
-          const T yr = pv.y1[e[u] * 6 + 2 * m], yi = pv.y1[e[u] * 6 + 2 * m + 1];
+          const C<T> y = pv.y1[m * pv.ne + e];
           // psi * conj(Y)
-          const T tr = v[u].x * yr + v[u].y * yi;
-          const T ti = v[u].y * yr - v[u].x * yi;
+          const T tr = v[u].x * y.x + v[u].y * y.y;
+          const T ti = v[u].y * y.x - v[u].x * y.y;
 #pragma unroll
           for (int p = 0; p < 5; p++) {
             acc[2 * (p * 3 + m)] += b[p] * tr;
@@ -109,7 +127,7 @@ __global__ void __launch_bounds__(kProjThreads, MINB) k_proj_gather(const C<T> *
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     acc[i] = x;
   }
-  __shared__ C<T> cf[kSW][15];
+  __shared__ C<T> cf[W][15];
   if (lane == 0) {
 #pragma unroll
     for (int i = 0; i < 15; i++) cf[wid][i] = mk<T>(acc[2 * i] * (T)dv, acc[2 * i + 1] * (T)dv);
@@ -164,26 +182,39 @@ __global__ void __launch_bounds__(kProjThreads, MINB) k_proj_scatter(C<T> *__res
   const int np = pv.cnt[a];
   const int npj = pv.nproj;
   C<T> *po = out + st * nspin * ngrid;
+  const long ebase = a * pv.npts;
+  // grid indices one iteration ahead (see the gather)
+  int jn[kSU];
+#pragma unroll
+  for (int u = 0; u < kSU; u++) {
+    const int g = lane + 32 * u;
+    jn[u] = g < np ? pv.jxyz[ebase + g] : -1;
+  }
   for (int g0 = lane; g0 < np; g0 += 32 * kSU) {
     int jx[kSU];
     long e[kSU];
 #pragma unroll
     for (int u = 0; u < kSU; u++) {
-      const int g = g0 + 32 * u;
-      e[u] = a * pv.npts + (g < np ? g : 0);
-      jx[u] = g < np ? pv.jxyz[e[u]] : -1;
+      jx[u] = jn[u];
+      e[u] = ebase + g0 + 32 * u;
+      const int g = g0 + 32 * (kSU + u);
+      jn[u] = g < np ? pv.jxyz[ebase + g] : -1;
     }
 #pragma unroll
     for (int u = 0; u < kSU; u++) {
       if (jx[u] < 0) continue;
       T yr[3], yi[3];
 #pragma unroll
-      for (int m = 0; m < 3; m++) { yr[m] = pv.y1[e[u] * 6 + 2 * m]; yi[m] = pv.y1[e[u] * 6 + 2 * m + 1]; }
+      for (int m = 0; m < 3; m++) {
+        const C<T> y = pv.y1[m * pv.ne + e[u]];
+        yr[m] = y.x;
+        yi[m] = y.y;
+      }
       T bs[5], bn[5];
 #pragma unroll
       for (int p = 0; p < 5; p++) {
-        bs[p] = (SO && p < npj) ? pv.sop[e[u] * npj + p] : T(0);
-        bn[p] = (NL && p < npj) ? pv.nlp[e[u] * npj + p] : T(0);
+        bs[p] = (SO && p < npj) ? pv.sop[p * pv.ne + e[u]] : T(0);
+        bn[p] = (NL && p < npj) ? pv.nlp[p * pv.ne + e[u]] : T(0);
       }
       for (int s = 0; s < nspin; s++) {
         T vr = 0, vi = 0;
@@ -229,15 +260,17 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   const int nch = (c->so ? 1 : 0) + (c->nl ? 1 : 0);
   // FP32 (mixed path): two points per lane per iteration with a register cap
   // for 8 CTAs per SM (more warps in flight instead of more loads per warp;
-  // 0.52 -> 0.50 ms per 16-state spinor batch at 128^3).  FP64: four (gather)
-  // / two (scatter) points per lane, no cap (the cap spills there).
+  // gather + scatter 0.52 -> 0.50 ms per 16-state spinor batch at 128^3, and
+  // 0.47 ms with the index prefetch).  FP64: four (gather) / two (scatter)
+  // points per lane, no cap (the cap spills there).
   constexpr bool occ = sizeof(T) == 4;
   constexpr int kGU = occ ? 2 : 4;
   constexpr int kMinB = occ ? 8 : 1;
   dim3 gg((unsigned)p.nat, (unsigned)nch, (unsigned)ggroups);
   const ProjView<T> pv = view<T>(c);
-  k_proj_gather<T, kGU, kMinB><<<gg, kProjThreads, 0, c->stream>>>(in, coef, pv, p.nat, nstates, c->ngrid, c->nspin,
-                                                                   ch0, c->dv);
+  // (8 warps per CTA measured 4% slower than 4: 0.49 vs 0.47 ms)
+  k_proj_gather<T, kGU, kMinB, kSW><<<gg, kProjThreads, 0, c->stream>>>(in, coef, pv, p.nat, nstates, c->ngrid,
+                                                                       c->nspin, ch0, c->dv);
   FBSE_CHECK_LAUNCH(c);
   dim3 gs((unsigned)p.nat, (unsigned)ngroups);
   const T sc = (T)scale;

@@ -608,14 +608,23 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     std::vector<double> hs(3 * k);
     if (cudaMemcpyAsync(hs.data(), rsum, 3 * k * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "rotation"); break; }
-    // 7. normalise, report E (Ritz value) and sigma = ||(H - E) psi|| for the normalised state
+    // 7. normalise; report the Rayleigh quotient rho = <psi|H psi>/<psi|psi> of
+    //    the returned state and sigma = ||(H - rho) psi|| / ||psi||.  rho differs
+    //    from the Ritz value E by the basis' departure from orthonormality
+    //    (X^H G X = I up to eps * cond(G)); for the reference's SVD basis the
+    //    two agree, so rho is the closer match to its eig_vals and is what
+    //    calc_sigma_E reports for the state.  With r = ||(H - E) psi||^2:
+    //    ||(H - rho) psi||^2 = r - (rho - E)^2 ||psi||^2.
     std::vector<double> f(k);
     for (int s = 0; s < k; s++) {
-      const double nrm = hs[3 * s + 1] * c->dv;
+      const double pp = hs[3 * s + 1];
+      const double nrm = pp * c->dv;
       if (!(nrm > 0)) { rc = set_err(c, FBSE_ERR_NAN, "Norm is 0/NAN after diagonalisation"); break; }
       f[s] = 1.0 / std::sqrt(nrm);
-      eval[s] = es[s];
-      sigma[s] = std::sqrt(std::fabs(hs[3 * s]) * c->dv) * f[s];
+      const double rho = hs[3 * s + 2] / pp;
+      const double d = rho - es[s];
+      eval[s] = rho;
+      sigma[s] = std::sqrt(std::fabs(hs[3 * s] / pp - d * d));
     }
     if (rc) break;
     cudaMemcpyAsync(fac, f.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);

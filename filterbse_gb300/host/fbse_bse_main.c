@@ -1,4 +1,6 @@
-/* fbse_bse: drop-in for the reference's bse executable (bse_cplx).
+/* fbse_bse: drop-in for the reference's bse executables: bse_cplx for
+ * spinor filter output, bse_real for real one-component states (the singlet
+ * exchange factor 2, real kernel files and optical files).
  *
  * Reads input.par and the filter's output.dat from the working directory
  * (bse_cplx/read.c, save.c), picks the quasiparticle basis as
@@ -6,8 +8,12 @@
  * on one GPU through libfbse_gpu: Coulomb potentials (init.c), direct and
  * exchange kernels (coulomb.c), the BSE eigensolve with its expectation
  * values (mod_bse.c, bethe-salpeter.c), pair and exciton transition dipoles
- * (dipole.c, optical.c).  Writes BSEeval.par, exciton.dat, OS0.dat and OS.dat
- * in the reference's formats.  Errors go to stderr with EXIT_FAILURE. */
+ * (dipole.c, optical.c), magnetic dipoles and rotational strengths.  Writes
+ * BSEeval.par, direct-0.dat, exchange-0.dat, h0.dat, bsRE/IM.dat,
+ * HBSmatRE/IM.dat, BSEcoeffRE/IM.dat, exciton.dat, OS0.dat, OS.dat, M0.dat,
+ * M.dat, rs0.dat, rs.dat and bs-coeff-<j>.dat in the reference's formats; coulombDone = 1 reads the kernels back from direct.dat /
+ * exchange.dat instead of computing them, calcCoulombOnly stops after the
+ * kernels.  Errors go to stderr with EXIT_FAILURE. */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -90,6 +96,136 @@ static void read_output(const char *path, output_dat *o)
   fclose(f);
 }
 
+/* one part (0: re, 1: im) of an n x n complex row-major matrix as text rows */
+static void write_part(const char *path, const double *m, long n, int part, const char *fmt, int prec)
+{
+  FILE *f = fopen(path, "w");
+  if (!f) die("cannot write", path);
+  for (long i = 0; i < n; i++, fputc('\n', f))
+    for (long j = 0; j < n; j++) fprintf(f, fmt, prec, m[2 * (i * n + j) + part]);
+  fclose(f);
+}
+
+/* the matrix files of build_h0_mat, build_BSE_mat and bethe_salpeter:
+ * h0.dat (mod_bse.c:73-84, "%.6g "), bsRE/bsIM.dat = K^d + K^x
+ * (mod_bse.c:126-144), HBSmatRE/IM.dat = h0 - K (bethe-salpeter.c:71-95) and
+ * BSEcoeffRE/IM.dat, column j = exciton j (bethe-salpeter.c:115-133), all with
+ * PR_LEN = 6 significant digits (bse_cplx/fd.h:131) */
+static void write_matrices(fbse_ctx *ctx, void *d_dir, void *d_exc, void *d_coef, const double *eqp, long nh,
+                           long ne, long lumo, int real)
+{
+  const long n = nh * ne;
+  const size_t bytes = (size_t)n * n * 2 * sizeof(double);
+  double *dm = malloc(bytes), *xm = malloc(bytes), *cm = malloc(bytes);
+  if (!dm || !xm || !cm) die("host allocation", NULL);
+  check(ctx, fbse_download(ctx, dm, d_dir, bytes), "download");
+  check(ctx, fbse_download(ctx, xm, d_exc, bytes), "download");
+  check(ctx, fbse_download(ctx, cm, d_coef, bytes), "download");
+  FILE *f = fopen("h0.dat", "w");
+  if (!f) die("cannot write", "h0.dat");
+  for (long i = 0; i < n; i++, fputc('\n', f))
+    for (long j = 0; j < n; j++) fprintf(f, "%.6g ", i == j ? eqp[lumo + i / nh] - eqp[i % nh] : 0.0);
+  fclose(f);
+  for (size_t k = 0; k < (size_t)n * n * 2; k++) dm[k] += xm[k]; /* K = K^d + K^x */
+  if (real) {
+    /* bse_real: bs.dat, HBSmat.dat, BSEcoeff.dat with row j = exciton j
+     * (bse_real/mod_bse.c:124-131, bethe-salpeter.c:78-114) */
+    write_part("bs.dat", dm, n, 0, "%.*g ", 6);
+  } else {
+    write_part("bsRE.dat", dm, n, 0, "%.*g ", 6);
+    write_part("bsIM.dat", dm, n, 1, "%.*g ", 6);
+  }
+  for (size_t k = 0; k < (size_t)n * n * 2; k++) dm[k] = -dm[k];
+  for (long i = 0; i < n; i++) dm[2 * (i * n + i)] += eqp[lumo + i / nh] - eqp[i % nh];
+  if (real) {
+    write_part("HBSmat.dat", dm, n, 0, "%.*g \t", 6);
+    for (long i = 0; i < n; i++) /* transpose */
+      for (long j = 0; j < n; j++) xm[2 * (i * n + j)] = cm[2 * (j * n + i)];
+    write_part("BSEcoeff.dat", xm, n, 0, "%.*g\t", 6);
+  } else {
+    write_part("HBSmatRE.dat", dm, n, 0, "%.*g \t", 6);
+    write_part("HBSmatIM.dat", dm, n, 1, "%.*g \t", 6);
+    write_part("BSEcoeffRE.dat", cm, n, 0, "%.*g\t", 6);
+    write_part("BSEcoeffIM.dat", cm, n, 1, "%.*g\t", 6);
+  }
+  free(dm);
+  free(xm);
+  free(cm);
+}
+
+/* Im(mu . conj(m)) of two complex 3-vectors stored (re, im) x 3 */
+static double im_dot_conj(const double *mu, const double *m)
+{
+  double r = 0.0;
+  for (int d = 0; d < 3; d++) r += mu[2 * d + 1] * m[2 * d] - mu[2 * d] * m[2 * d + 1];
+  return r;
+}
+
+/* direct-<rank>.dat / exchange-<rank>.dat (bse_cplx/coulomb.c:289-371,
+ * 534-602; one rank): "a b i j ibs jbs re im" per element.  direct: every
+ * (a, b, i, j) in a, b, i, j order, zero above the diagonal (coulomb.c:360-371);
+ * exchange: (a, i, b, j) order, lower triangle only (coulomb.c:586-600). */
+static void kline(FILE *f, long a, long b, long i, long j, long ibs, long jbs, const double *v, int real)
+{
+  if (real) /* bse_real/coulomb.c:355, 580: one value */
+    fprintf(f, "%03ld %03ld %03ld %03ld %ld %ld %.12f\n", a, b, i, j, ibs, jbs, v[0]);
+  else
+    fprintf(f, "%03ld %03ld %03ld %03ld %ld %ld %.12f %.12f\n", a, b, i, j, ibs, jbs, v[0], v[1]);
+}
+
+static void write_kernel_files(const double *dir, const double *exc, long nh, long ne, long lumo, int real)
+{
+  const long nx = nh * ne;
+  FILE *f = fopen("direct-0.dat", "w");
+  if (!f) die("cannot write", "direct-0.dat");
+  for (long a = lumo; a < lumo + ne; a++)
+    for (long b = lumo; b < lumo + ne; b++)
+      for (long i = 0; i < nh; i++)
+        for (long j = 0; j < nh; j++) {
+          const long ibs = (a - lumo) * nh + i, jbs = (b - lumo) * nh + j;
+          kline(f, a, b, i, j, ibs, jbs, dir + 2 * (ibs * nx + jbs), real);
+        }
+  fclose(f);
+  f = fopen("exchange-0.dat", "w");
+  if (!f) die("cannot write", "exchange-0.dat");
+  for (long a = lumo; a < lumo + ne; a++)
+    for (long i = 0; i < nh; i++)
+      for (long b = lumo; b < lumo + ne; b++)
+        for (long j = 0; j < nh; j++) {
+          const long ibs = (a - lumo) * nh + i, jbs = (b - lumo) * nh + j;
+          if (ibs < jbs) continue;
+          kline(f, a, b, i, j, ibs, jbs, exc + 2 * (ibs * nx + jbs), real);
+        }
+  fclose(f);
+}
+
+/* load_coulomb_mat (bse_cplx/coulomb.c:742-817): fills mat[ibs][jbs] from the
+ * lines of path; the file is complete when the largest a, b reach the last
+ * electron and the largest i, j the last hole (mod_kernel.c:56-80) */
+static void load_kernel_file(const char *path, double *mat, long nh, long ne, long lumo, int real)
+{
+  const long nx = nh * ne;
+  FILE *f = fopen(path, "r");
+  if (!f) die("could not open file", path);
+  long a, b, i, j, ibs, jbs, amax = 0, bmax = 0, imax = 0, jmax = 0, cnt = 0;
+  double re, im = 0.0;
+  while (cnt < nx * nx && (real ? fscanf(f, "%ld %ld %ld %ld %ld %ld %lg", &a, &b, &i, &j, &ibs, &jbs, &re) == 7
+                                : fscanf(f, "%ld %ld %ld %ld %ld %ld %lg %lg", &a, &b, &i, &j, &ibs, &jbs, &re, &im) == 8)) {
+    if (ibs < 0 || ibs >= nx || jbs < 0 || jbs >= nx) die("pair index out of range in", path);
+    mat[2 * (ibs * nx + jbs)] = re;
+    mat[2 * (ibs * nx + jbs) + 1] = im;
+    if (a > amax) amax = a;
+    if (b > bmax) bmax = b;
+    if (i > imax) imax = i;
+    if (j > jmax) jmax = j;
+    cnt++;
+  }
+  fclose(f);
+  const long el_max = lumo + ne - 1, ho_max = nh - 1;
+  if (!(amax == el_max && bmax == el_max && imax == ho_max && jmax == ho_max))
+    die("matrix elements not done in", path);
+}
+
 int main(void)
 {
   char err[512];
@@ -97,7 +233,10 @@ int main(void)
   if (fbse_read_bse_params("input.par", &p, err, sizeof err)) die(err, NULL);
   output_dat o;
   read_output("output.dat", &o);
-  if (o.complex_idx != 2 || o.nspin != 2) die("the complex BSE needs spinor filter output (bse_cplx)", NULL);
+  /* complex spinors: bse_cplx; real one-component states: bse_real */
+  const int real = (o.complex_idx == 1 && o.nspin == 1);
+  if (!real && !(o.complex_idx == 2 && o.nspin == 2))
+    die("output.dat holds neither complex spinors (bse_cplx) nor real one-component states (bse_real)", NULL);
 
   /* get_qp_basis_indices (bse_cplx/basis.c:7-254) */
   long *hole = malloc(o.mn * sizeof(long)), *elec = malloc(o.mn * sizeof(long)), nh = 0, ne = 0;
@@ -125,17 +264,24 @@ int main(void)
   if (fe) fclose(fe);
   printf("fbse_bse: %ld holes, %ld electrons, %ld excitons; gap %.6g Ha\n", nh, ne, nx, eqp[lumo] - eqp[lumo - 1]);
 
-  /* the basis states (get_qp_basis, basis.c:258-300) */
-  const long stlen = 2 * o.nspinngrid; /* doubles per complex spinor state */
-  double *psi_host = malloc((size_t)nqp * stlen * sizeof(double));
+  /* the basis states (get_qp_basis, basis.c:258-300): as stored (flen
+   * doubles each), and as complex states (stlen doubles) for the dipoles */
+  const long flen = o.complex_idx * o.nspinngrid, stlen = 2 * o.nspinngrid;
+  double *file_psi = malloc((size_t)nqp * flen * sizeof(double));
   FILE *f = fopen("output.dat", "rb");
-  if (!f || !psi_host) die("cannot read states from", "output.dat");
+  if (!f || !file_psi) die("cannot read states from", "output.dat");
   for (long i = 0; i < nqp; i++) {
-    if (fseek(f, o.psi_pos + sel[i] * stlen * (long)sizeof(double), SEEK_SET) ||
-        fread(psi_host + i * stlen, sizeof(double), stlen, f) != (size_t)stlen)
+    if (fseek(f, o.psi_pos + sel[i] * flen * (long)sizeof(double), SEEK_SET) ||
+        fread(file_psi + i * flen, sizeof(double), flen, f) != (size_t)flen)
       die("truncated states in", "output.dat");
   }
   fclose(f);
+  double *psi_host = file_psi;
+  if (real) {
+    psi_host = calloc((size_t)nqp * stlen, sizeof(double));
+    if (!psi_host) die("host allocation", NULL);
+    for (size_t k = 0; k < (size_t)nqp * flen; k++) psi_host[2 * k] = file_psi[k];
+  }
 
   /* context: the grid only (no potential / projectors are used by the BSE) */
   fbse_grid_desc gd;
@@ -143,7 +289,7 @@ int main(void)
   gd.nx = o.nx; gd.ny = o.ny; gd.nz = o.nz;
   gd.dx = o.dx; gd.dy = o.dy; gd.dz = o.dz;
   gd.ke_max = o.ke_max;
-  gd.nspin = 2;
+  gd.nspin = o.nspin;
   gd.is_complex = 1;
   double *zero = calloc(o.ngrid, sizeof(double));
   fbse_ctx *ctx = NULL;
@@ -167,10 +313,59 @@ int main(void)
 
   check(ctx, fbse_bse_potentials(ctx, gx, gy, gz, o.xmin, o.ymin, o.zmin, p.eps_x, p.eps_y, p.eps_z, d_bare, d_scr),
         "Coulomb potentials");
-  check(ctx, fbse_bse_kernel(ctx, d_psi, nh, ne, lumo, d_bare, d_scr, d_dir, d_exc), "BSE kernels");
+  {
+    const size_t mbytes = (size_t)nx * nx * 2 * sizeof(double);
+    double *hd = calloc((size_t)nx * nx * 2, sizeof(double)), *hx = calloc((size_t)nx * nx * 2, sizeof(double));
+    if (!hd || !hx) die("host allocation", NULL);
+    if (p.coulomb_done) {
+      /* coulombDone = 1: the kernels from direct.dat / exchange.dat (mod_kernel.c:56-80) */
+      load_kernel_file("direct.dat", hd, nh, ne, lumo, real);
+      load_kernel_file("exchange.dat", hx, nh, ne, lumo, real);
+      check(ctx, fbse_upload(ctx, d_dir, hd, mbytes), "upload");
+      check(ctx, fbse_upload(ctx, d_exc, hx, mbytes), "upload");
+      printf("kernels loaded from direct.dat and exchange.dat\n");
+    } else if (real) {
+      /* bse_real: real kernels from the real states, as complex matrices for the solve */
+      void *d_pr, *d_dr, *d_xr;
+      const size_t rb = (size_t)nx * nx * sizeof(double);
+      check(ctx, fbse_alloc(ctx, &d_pr, (size_t)nqp * flen * sizeof(double)), "alloc");
+      check(ctx, fbse_alloc(ctx, &d_dr, rb), "alloc");
+      check(ctx, fbse_alloc(ctx, &d_xr, rb), "alloc");
+      check(ctx, fbse_upload(ctx, d_pr, file_psi, (size_t)nqp * flen * sizeof(double)), "upload");
+      check(ctx, fbse_bse_kernel_real(ctx, d_pr, nh, ne, lumo, d_bare, d_scr, d_dr, d_xr), "BSE kernels");
+      double *rr = malloc(rb);
+      if (!rr) die("host allocation", NULL);
+      check(ctx, fbse_download(ctx, rr, d_dr, rb), "download");
+      for (long k = 0; k < nx * nx; k++) hd[2 * k] = rr[k];
+      check(ctx, fbse_download(ctx, rr, d_xr, rb), "download");
+      for (long k = 0; k < nx * nx; k++) hx[2 * k] = rr[k];
+      free(rr);
+      fbse_free(ctx, d_pr);
+      fbse_free(ctx, d_dr);
+      fbse_free(ctx, d_xr);
+      check(ctx, fbse_upload(ctx, d_dir, hd, mbytes), "upload");
+      check(ctx, fbse_upload(ctx, d_exc, hx, mbytes), "upload");
+      write_kernel_files(hd, hx, nh, ne, lumo, 1);
+    } else {
+      /* restartCoulomb = 1 continues an interrupted CPU run in the reference;
+       * here the whole kernel is recomputed, which gives the same matrices */
+      check(ctx, fbse_bse_kernel(ctx, d_psi, nh, ne, lumo, d_bare, d_scr, d_dir, d_exc), "BSE kernels");
+      check(ctx, fbse_download(ctx, hd, d_dir, mbytes), "download");
+      check(ctx, fbse_download(ctx, hx, d_exc, mbytes), "download");
+      write_kernel_files(hd, hx, nh, ne, lumo, 0);
+    }
+    free(hd);
+    free(hx);
+    if (p.calc_coulomb_only) { /* mod_kernel.c:84-93 */
+      printf("calcCoulombOnly: stopping after the kernels\n");
+      fbse_destroy(ctx);
+      return 0;
+    }
+  }
   double *ene = malloc(nx * sizeof(double)), *hx = malloc(nx * sizeof(double)), *dx = malloc(nx * sizeof(double));
   double *xx = malloc(nx * sizeof(double)), *h0x = malloc(nx * sizeof(double));
   check(ctx, fbse_bse_solve(ctx, eqp, nqp, nh, ne, lumo, d_dir, d_exc, ene, d_coef, hx, dx, xx, h0x), "BSE solve");
+  write_matrices(ctx, d_dir, d_exc, d_coef, eqp, nh, ne, lumo, real);
 
   FILE *px = fopen("exciton.dat", "w"); /* bethe-salpeter.c:337-346 */
   if (!px) die("cannot write", "exciton.dat");
@@ -184,26 +379,93 @@ int main(void)
   check(ctx, fbse_bse_dipoles(ctx, d_psi, gx, gy, gz, nh, ne, lumo, mu), "transition dipoles");
   FILE *p0 = fopen("OS0.dat", "w"); /* dipole.c:61, 137-152 */
   if (!p0) die("cannot write", "OS0.dat");
-  fprintf(p0, "i  a   sqrt(mu2)     Ea-Ei \t  f_osc       mu_x.re     mu_x.im     mu_y.re     mu_y.im     mu_z.re     mu_z.im\n");
+  if (real) /* bse_real/dipole.c:61, 142-144: real components */
+    fprintf(p0, "i  a   sqrt(mu2)     Ea-Ei \t  f_osc       mu_x        mu_y       mu_z\n");
+  else
+    fprintf(p0, "i  a   sqrt(mu2)     Ea-Ei \t  f_osc       mu_x.re     mu_x.im     mu_y.re     mu_y.im     mu_z.re     mu_z.im\n");
   for (long i = 0; i < nh; i++)
     for (long a = lumo; a < lumo + ne; a++) {
       const double *m = mu + (i * ne + (a - lumo)) * 6;
       const double e = eqp[a] - eqp[i];
       const double m2 = m[0] * m[0] + m[1] * m[1] + m[2] * m[2] + m[3] * m[3] + m[4] * m[4] + m[5] * m[5];
-      fprintf(p0, "%ld % ld  %.8f %.12f % .8f % .8f % .8f % .8f % .8f % .8f % .8f\n", i, a, sqrt(m2), e,
-              (2.0 / 3.0) * e * m2, m[0], m[1], m[2], m[3], m[4], m[5]);
+      if (real)
+        fprintf(p0, "%ld % ld  %.8f %.12f % .8f % .8f % .8f % .8f\n", i, a, sqrt(m2), e, (2.0 / 3.0) * e * m2, m[0],
+                m[2], m[4]);
+      else
+        fprintf(p0, "%ld % ld  %.8f %.12f % .8f % .8f % .8f % .8f % .8f % .8f % .8f\n", i, a, sqrt(m2), e,
+                (2.0 / 3.0) * e * m2, m[0], m[1], m[2], m[3], m[4], m[5]);
     }
   fclose(p0);
+  /* magnetic transition dipoles and rotational strengths of the pairs
+   * (calc_mag_dipole, dipole.c:297-311, a-major; calc_rotational_strength,
+   * dipole.c:333-370, i-major) */
+  double *mg = malloc((size_t)nx * 6 * sizeof(double)), *mgx = malloc((size_t)nx * 6 * sizeof(double));
+  check(ctx, fbse_bse_mag_dipoles(ctx, d_psi, gx, gy, gz, nh, ne, lumo, mg), "magnetic dipoles");
+  FILE *pm0 = fopen("M0.dat", "w");
+  if (!pm0) die("cannot write", "M0.dat");
+  for (long a = lumo; a < lumo + ne; a++)
+    for (long i = 0; i < nh; i++) {
+      const double *m = mg + (i * ne + (a - lumo)) * 6;
+      const double e = eqp[a] - eqp[i];
+      const double ms = m[0] * m[0] + m[1] * m[1] + m[2] * m[2] + m[3] * m[3] + m[4] * m[4] + m[5] * m[5];
+      fprintf(pm0, "%3ld %3ld  %+.8f %+.12f %+.8f %+.8f %+.8f %+.8f %+.8f %+.8f %+.8f\n", i, a, sqrt(ms), e,
+              (4.0 / 3.0) * e * ms, m[0], m[1], m[2], m[3], m[4], m[5]);
+    }
+  fclose(pm0);
+  FILE *pr0 = fopen("rs0.dat", "w");
+  if (!pr0) die("cannot write", "rs0.dat");
+  for (long i = 0; i < nh; i++)
+    for (long a = lumo; a < lumo + ne; a++) {
+      const long q = (i * ne + (a - lumo)) * 6;
+      fprintf(pr0, "%ld %ld %.12f %.12g\n", i, a, eqp[a] - eqp[i], im_dot_conj(mu + q, mg + q));
+    }
+  fclose(pr0);
   check(ctx, fbse_bse_optical(ctx, d_coef, mu, nh, ne, mx), "exciton dipoles");
+  check(ctx, fbse_bse_optical(ctx, d_coef, mg, nh, ne, mgx), "exciton magnetic dipoles");
   FILE *po = fopen("OS.dat", "w"); /* optical.c:72-75 */
   if (!po) die("cannot write", "OS.dat");
   for (long j = 0; j < nx; j++) {
     const double *m = mx + j * 6;
     const double os = m[0] * m[0] + m[1] * m[1] + m[2] * m[2] + m[3] * m[3] + m[4] * m[4] + m[5] * m[5];
-    fprintf(po, "%ld % .8f % .8f % .8f % .12f % .12f % .12f % .12f % .12f % .12f\n", j, sqrt(os), ene[j],
-            (2.0 / 3.0) * ene[j] * os, m[0], m[1], m[2], m[3], m[4], m[5]);
+    if (real) /* bse_real/optical.c:72-75: real parts */
+      fprintf(po, "%ld % .8f % .8f % .8f % .12f % .12f % .12f\n", j, sqrt(os), ene[j], (2.0 / 3.0) * ene[j] * os, m[0],
+              m[2], m[4]);
+    else
+      fprintf(po, "%ld % .8f % .8f % .8f % .12f % .12f % .12f % .12f % .12f % .12f\n", j, sqrt(os), ene[j],
+              (2.0 / 3.0) * ene[j] * os, m[0], m[1], m[2], m[3], m[4], m[5]);
   }
   fclose(po);
+  /* M.dat, rs.dat and bs-coeff-<j>.dat for j < 10 (optical.c:29-95) */
+  FILE *pm = fopen("M.dat", "w"), *prs = fopen("rs.dat", "w");
+  if (!pm || !prs) die("cannot write", "M.dat / rs.dat");
+  for (long j = 0; j < nx; j++) {
+    const double *m = mgx + j * 6;
+    const double mos = m[0] * m[0] + m[1] * m[1] + m[2] * m[2] + m[3] * m[3] + m[4] * m[4] + m[5] * m[5];
+    fprintf(pm, "%ld % .8f % .8f % .8f % .12f % .12f % .12f % .12f % .12f % .12f\n", j, sqrt(mos), ene[j],
+            (4.0 / 3.0) * ene[j] * mos, m[0], m[1], m[2], m[3], m[4], m[5]);
+    fprintf(prs, "%ld %.8f % .16f\n", j, ene[j], im_dot_conj(mx + j * 6, m));
+  }
+  fclose(pm);
+  fclose(prs);
+  {
+    const long ncoef = nx < 10 ? nx : 10;
+    double *cf = malloc((size_t)nx * nx * 2 * sizeof(double));
+    if (!cf) die("host allocation", NULL);
+    check(ctx, fbse_download(ctx, cf, d_coef, (size_t)nx * nx * 2 * sizeof(double)), "download");
+    for (long j = 0; j < ncoef; j++) {
+      char path[64];
+      snprintf(path, sizeof path, "bs-coeff-%ld.dat", j);
+      FILE *pc = fopen(path, "w");
+      if (!pc) die("cannot write", path);
+      for (long a = lumo, ibs = 0; a < lumo + ne; a++)
+        for (long i = 0; i < nh; i++, ibs++) {
+          const double *c = cf + 2 * (ibs * nx + j);
+          fprintf(pc, "%ld %ld %.12lg %lg\n", i, a, eqp[a] - eqp[i], c[0] * c[0] + c[1] * c[1]);
+        }
+      fclose(pc);
+    }
+    free(cf);
+  }
   printf("lowest exciton %.12f Ha, binding %.6f eV\n", ene[0], (ene[0] - h0x[0]) * AUTOEV);
   fbse_destroy(ctx);
   return 0;

@@ -23,6 +23,9 @@ typedef struct {
   int set_seed;
   long seed;
   int use_spinors, so, nl, get_all_states, approx_energy_range, precision;
+  /* restart / state files (read.c:34-35, 87-93, 762-787, 954-967) */
+  int print_psi_filt, print_psi_diag, calc_filter_only, restart_from_ortho, restart_from_sigma;
+  long n_states_for_ortho, n_states_for_sigma;
 } fbse_filter_params;
 
 /* the subset of bse_cplx/input.par (bse_cplx/read.c) */
@@ -30,6 +33,8 @@ typedef struct {
   long max_hole_states, max_elec_states;
   double sigma_e_cut, eps_x, eps_y, eps_z, fermi_e, delta_e_hole, delta_e_elec;
   int precision;
+  /* kernel files (bse_cplx/read.c:58-60, 127-129; mod_kernel.c:31-96) */
+  int coulomb_done, restart_coulomb, calc_coulomb_only;
 } fbse_bse_params;
 
 /* input.par parsing: returns 0, or -1 with a message in err */

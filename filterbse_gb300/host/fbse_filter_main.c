@@ -6,6 +6,12 @@
  * start, orthogonalisation, subspace diagonalisation, sigma_E) and writes
  * eval.dat, psi.dat and output.dat in the reference's layouts
  * (filter_mpi/write.c:263-299, mod_output.c:5-162, save.c:446-503).
+ * Also eval_aux.dat (calc_sigma_E), the per-start psi-filt-<start>-0.dat
+ * files (printPsiFilt, on by default as in the reference) and psi-diag.dat
+ * (printPsiDiag), and the restarts from them: "restartFromOrtho = 1 <n>"
+ * reads psi-filt.dat and starts at the orthogonalisation, "restartFromSigma
+ * = 1 <n>" reads psi-diag.dat and only computes energies and sigma_E
+ * (main.c:128-305, read.c:954-967); calcFilterOnly stops after the filter.
  * Errors go to stderr and the process exits with EXIT_FAILURE, like the
  * reference.  One non-reference key: "mixedPrecision = 1" selects the FP32
  * recursion (default: the plain FP64 method). */
@@ -75,6 +81,25 @@ static void save_output(const char *path, const fbse_filter_params *p, long nato
   fwrite(sigma, sizeof(double), n, f);
   fwrite(psi, sizeof(double), (size_t)(cplx + 1) * nspin * ngrid * n, f);
   fprintf(f, "\n\nEOF\n");
+  fclose(f);
+}
+
+/* n states of stlen doubles from a raw state file (psi-filt.dat, psi-diag.dat) */
+static double *read_states(const char *path, long n, long stlen)
+{
+  FILE *f = fopen(path, "rb");
+  if (!f) die("could not open", path);
+  double *buf = malloc((size_t)n * stlen * sizeof(double));
+  if (!buf) die("host allocation", path);
+  if (fread(buf, sizeof(double), (size_t)n * stlen, f) != (size_t)n * stlen) die("fewer states than requested in", path);
+  fclose(f);
+  return buf;
+}
+
+static void write_states(const char *path, const double *x, long count)
+{
+  FILE *f = fopen(path, "wb");
+  if (!f || fwrite(x, sizeof(double), (size_t)count, f) != (size_t)count) die("cannot write", path);
   fclose(f);
 }
 
@@ -240,66 +265,152 @@ int main(void)
   int rc = fbse_create(&ctx, &gd, pot, (p.so || p.nl) ? &pd : NULL, p.precision ? FBSE_MIXED : FBSE_FP64);
   check(ctx, rc, "fbse_create");
 
-  /* energy range (get_energy_range, filter_mpi/energy.c:169-379) */
-  double emin, emax;
-  if (p.approx_energy_range) {
-    emin = -0.8; /* energy.c:307-308 */
-    emax = vmax_loc + p.ke_max;
-    if (p.so) emax += 3.5;
-    if (p.nl && nl_lam_min < 0.0) emin += 1.15 * nl_lam_min;
-  } else {
-    long iters = 0;
-    check(ctx, fbse_energy_range(ctx, -874917403, 1500, &emin, &emax, &iters), "energy range");
-    printf("energy range: Emin %g, Emax %g (%ld iterations)\n", emin, emax, iters);
-  }
-  if (p.nl && !p.so && nl_lam_min < 0.0) { /* energy.c:350-362 */
-    emax *= 1.05;
-    emin -= 0.1 * fabs(emin);
-    const double weyl = 1.05 * (vmin_loc + nl_lam_min);
-    if (emin > weyl) emin = weyl;
-  } else {
-    emax *= 1.2;
-    emin -= 0.2 * fabs(emin);
-  }
-  const double de = emax - emin;
-  printf("Emin = %g, Emax = %g, dE = %g\n", emin, emax, de);
-
-  /* targets (set_ene_targets, init.c:401-478) and Newton coefficients */
-  const long m = p.m_states_per_filter, nc = p.ncheby, ns = p.n_filter_cycles;
-  double *targets = malloc(m * sizeof(double));
-  double del = (p.vbmax - p.vbmin) / (double)p.n_targets_vb;
-  for (long j = 0; j < p.n_targets_vb; j++) targets[p.n_targets_vb - j - 1] = p.vbmax - (double)j * del;
-  del = (p.cbmax - p.cbmin) / (double)p.n_targets_cb;
-  for (long j = p.n_targets_vb; j < m; j++) targets[j] = p.cbmin + (double)(j - p.n_targets_vb) * del;
-  double *zn = malloc(nc * sizeof(double)), *an = malloc(2 * m * nc * sizeof(double));
-  fbse_samp_points(nc, zn);
-  const double dt = ((double)nc / (2.5 * de)) * ((double)nc / (2.5 * de)); /* mod_filter.c:114 */
-  if (fbse_newton_coeff(nc, m, zn, targets, emin, de, dt, an)) die("Newton coefficients", NULL);
-
-  /* random starts (mod_filter.c:152-160, init_filter_states) */
-  long seed;
-  if (p.set_seed == 1) seed = -p.seed;
-  else {
-    srandom((unsigned)(time(NULL) ^ (getpid() << 8)));
-    seed = -random();
-  }
   const long stlen = (long)(cplx + 1) * nspin * ngrid;
-  double *starts = malloc((size_t)ns * stlen * sizeof(double));
-  fbse_init_filter_states(starts, ns, ngrid, nspin, cplx, p.dx * p.dy * p.dz, seed, NULL);
+  const size_t sbytes = (size_t)stlen * sizeof(double);
+  long n = 0;         /* states entering ortho (or sigma) */
+  void *d_psi = NULL; /* psitot on the device */
+  double *host_psi = NULL;
+  if (p.restart_from_sigma) {
+    /* restart_from_sigma (mod_sigma.c:67-124): psi-diag.dat holds the
+     * diagonalised states, stlen doubles each */
+    n = p.n_states_for_sigma;
+    host_psi = read_states("psi-diag.dat", n, stlen);
+    check(ctx, fbse_alloc(ctx, &d_psi, n * sbytes), "state buffer");
+    check(ctx, fbse_upload(ctx, d_psi, host_psi, n * sbytes), "upload psi-diag.dat");
+  } else if (p.restart_from_ortho) {
+    /* restart_from_ortho (ortho.c:189-240): psi-filt.dat holds the filtered
+     * states (the psi-filt-<start>-<rank>.dat files one after the other) */
+    n = p.n_states_for_ortho;
+    host_psi = read_states("psi-filt.dat", n, stlen);
+    check(ctx, fbse_alloc(ctx, &d_psi, n * sbytes), "state buffer");
+    check(ctx, fbse_upload(ctx, d_psi, host_psi, n * sbytes), "upload psi-filt.dat");
+    free(host_psi);
+    host_psi = NULL;
+  } else {
+    /* energy range (get_energy_range, filter_mpi/energy.c:169-379) */
+    double emin, emax;
+    if (p.approx_energy_range) {
+      emin = -0.8; /* energy.c:307-308 */
+      emax = vmax_loc + p.ke_max;
+      if (p.so) emax += 3.5;
+      if (p.nl && nl_lam_min < 0.0) emin += 1.15 * nl_lam_min;
+    } else {
+      long iters = 0;
+      check(ctx, fbse_energy_range(ctx, -874917403, 1500, &emin, &emax, &iters), "energy range");
+      printf("energy range: Emin %g, Emax %g (%ld iterations)\n", emin, emax, iters);
+    }
+    if (p.nl && !p.so && nl_lam_min < 0.0) { /* energy.c:350-362 */
+      emax *= 1.05;
+      emin -= 0.1 * fabs(emin);
+      const double weyl = 1.05 * (vmin_loc + nl_lam_min);
+      if (emin > weyl) emin = weyl;
+    } else {
+      emax *= 1.2;
+      emin -= 0.2 * fabs(emin);
+    }
+    const double de = emax - emin;
+    printf("Emin = %g, Emax = %g, dE = %g\n", emin, emax, de);
 
-  /* filter + ortho + diag + sigma_E + mod_output's selection */
-  double *eval = malloc(ns * m * sizeof(double)), *sigma = malloc(ns * m * sizeof(double));
-  double *psi = malloc((size_t)ns * m * stlen * sizeof(double));
-  if (!starts || !eval || !sigma || !psi) die("host allocation", NULL);
+    /* targets (set_ene_targets, init.c:401-478) and Newton coefficients */
+    const long m = p.m_states_per_filter, nc = p.ncheby, ns = p.n_filter_cycles;
+    double *targets = malloc(m * sizeof(double));
+    double del = (p.vbmax - p.vbmin) / (double)p.n_targets_vb;
+    for (long j = 0; j < p.n_targets_vb; j++) targets[p.n_targets_vb - j - 1] = p.vbmax - (double)j * del;
+    del = (p.cbmax - p.cbmin) / (double)p.n_targets_cb;
+    for (long j = p.n_targets_vb; j < m; j++) targets[j] = p.cbmin + (double)(j - p.n_targets_vb) * del;
+    double *zn = malloc(nc * sizeof(double)), *an = malloc(2 * m * nc * sizeof(double));
+    fbse_samp_points(nc, zn);
+    const double dt = ((double)nc / (2.5 * de)) * ((double)nc / (2.5 * de)); /* mod_filter.c:114 */
+    if (fbse_newton_coeff(nc, m, zn, targets, emin, de, dt, an)) die("Newton coefficients", NULL);
+
+    /* random starts (mod_filter.c:152-160, init_filter_states) */
+    long seed;
+    if (p.set_seed == 1) seed = -p.seed;
+    else {
+      srandom((unsigned)(time(NULL) ^ (getpid() << 8)));
+      seed = -random();
+    }
+    double *starts = malloc((size_t)ns * sbytes);
+    if (!starts) die("host allocation", NULL);
+    fbse_init_filter_states(starts, ns, ngrid, nspin, cplx, p.dx * p.dy * p.dz, seed, NULL);
+
+    /* the filter cycles of every start at once (run_filter_cycles) */
+    void *d_starts = NULL;
+    n = ns * m;
+    check(ctx, fbse_alloc(ctx, &d_starts, ns * sbytes), "start buffer");
+    check(ctx, fbse_alloc(ctx, &d_psi, n * sbytes), "state buffer");
+    check(ctx, fbse_upload(ctx, d_starts, starts, ns * sbytes), "upload starts");
+    check(ctx, fbse_newton_filter(ctx, zn, an, nc, m, emin, de, d_starts, ns, d_psi), "Newton filter");
+    check(ctx, fbse_free(ctx, d_starts), "free");
+    free(starts);
+    free(targets);
+    free(zn);
+    free(an);
+    if (p.print_psi_filt) {
+      /* printPsiFilt (filter.c:118-138): the m filtered states of start jns,
+       * before normalisation, in psi-filt-<jns>-<rank>.dat */
+      double *blk = malloc(m * sbytes);
+      if (!blk) die("host allocation", NULL);
+      for (long j = 0; j < ns; j++) {
+        char path[64];
+        snprintf(path, sizeof path, "psi-filt-%ld-0.dat", j);
+        check(ctx, fbse_download(ctx, blk, (char *)d_psi + (size_t)j * m * sbytes, m * sbytes), "download");
+        write_states(path, blk, m * stlen);
+      }
+      free(blk);
+    }
+    if (p.calc_filter_only) { /* main.c:160-163 */
+      printf("calcFilterOnly: %ld filtered states, stopping after the filter\n", n);
+      fbse_destroy(ctx);
+      return 0;
+    }
+  }
+
+  double *eval = malloc(n * sizeof(double)), *sigma = malloc(n * sizeof(double));
+  if (!eval || !sigma) die("host allocation", NULL);
+  long nk = n;
+  if (p.restart_from_sigma) {
+    /* mod_sigma -> calc_sigma_E (energy.c:383-539) */
+    check(ctx, fbse_sigma_e(ctx, d_psi, n, eval, sigma), "sigma_E");
+  } else {
+    /* normalize_all after the filter (filter.c:152) or on restart
+     * (ortho.c:242), then ortho + diag + sigma_E */
+    check(ctx, fbse_normalize_all(ctx, d_psi, n, NULL), "normalize_all");
+    check(ctx, fbse_ortho_diag_sigma(ctx, d_psi, n, &nk, eval, sigma), "ortho/diag/sigma");
+    printf("%ld states after orthogonalisation\n", nk);
+  }
+  FILE *fa = fopen("eval_aux.dat", "w"); /* calc_sigma_E (energy.c:528) */
+  if (!fa) die("cannot write", "eval_aux.dat");
+  for (long i = 0; i < nk; i++) fprintf(fa, "%ld %.16lg %.16lg\n", i, eval[i], sigma[i]);
+  fclose(fa);
+  if (p.print_psi_diag && !p.restart_from_sigma) {
+    /* printPsiDiag (mod_diag.c:439-444): every diagonalised state */
+    double *all = malloc(nk * sbytes);
+    if (!all) die("host allocation", NULL);
+    check(ctx, fbse_download(ctx, all, d_psi, nk * sbytes), "download");
+    write_states("psi-diag.dat", all, nk * stlen);
+    free(all);
+  }
+
+  /* mod_output's selection (mod_output.c:63-120): every state, or those with
+   * sigma_E <= sigmaECut */
+  double *psi = malloc((size_t)(nk ? nk : 1) * sbytes);
+  if (!psi) die("host allocation", NULL);
   long n_out = 0;
-  check(ctx, fbse_filter_job(ctx, zn, an, nc, m, emin, de, starts, ns, p.get_all_states ? 0.0 : p.sigma_e_cut, &n_out,
-                             eval, sigma, psi),
-        "filter job");
+  for (long i = 0; i < nk; i++) {
+    if (!p.get_all_states && !(sigma[i] <= p.sigma_e_cut)) continue;
+    eval[n_out] = eval[i];
+    sigma[n_out] = sigma[i];
+    if (host_psi) memcpy(psi + n_out * stlen, host_psi + i * stlen, sbytes);
+    else check(ctx, fbse_download(ctx, psi + n_out * stlen, (char *)d_psi + i * sbytes, sbytes), "download");
+    n_out++;
+  }
   printf("%ld eigenstates written\n", n_out);
   if (fbse_write_eval("eval.dat", eval, sigma, n_out)) die("cannot write", "eval.dat");
   if (fbse_write_psi("psi.dat", psi, n_out * stlen)) die("cannot write", "psi.dat");
   save_output("output.dat", &p, natoms, xyz, ntypes, nx, ny, nz, p.dx, p.dy, p.dz, gx, gy, gz, xmin, ymin, zmin,
               nspin, cplx, n_out, eval, sigma, psi);
+  check(ctx, fbse_free(ctx, d_psi), "free");
   fbse_destroy(ctx);
   return 0;
 }

@@ -33,18 +33,21 @@ static int parse_double(const char *s, double *v)
 }
 
 /* keys that only steer threading, printing or checkpoints of the reference:
- * accepted and ignored */
+ * accepted and ignored.  saveCheckpoints among them: the reference's
+ * checkpoint_<id>.dat reader (filter_mpi/save.c:389) takes three of the
+ * five flags its writer puts on that line (save.c:283), so its checkpoints do
+ * not restart; the file-level restarts (restartFromOrtho from psi-filt.dat,
+ * restartFromSigma from psi-diag.dat) are implemented instead. */
 static const char *k_ignored[] = {"nThreads", "hamThreads", "nestedOMP", "useFastHam", "useMPIOMP", "MPIOrtho",
                                   "MPIDiag", "parallelSigma", "timeHamiltonian", "printNorm", "printCubes",
-                                  "printGaussCubes", "saveCheckpoints", "printPsiFilt", "printPsiOrtho",
-                                  "printPsiDiag", "fftWisdomDir", "saveOutput", "calcPotOverlap",
+                                  "printGaussCubes", "saveCheckpoints", "printPsiOrtho",
+                                  "fftWisdomDir", "saveOutput", "calcPotOverlap",
                                   "calcSpinAngStat", "retryFilter", "centerConf", "noTimeRev", "psiZeroCut",
-                                  "coulombDone", "restartCoulomb", "calcDarkStates", "timingSpecs", NULL};
+                                  "calcDarkStates", "timingSpecs", "crystalStructure", "outmostMaterial", NULL};
 /* keys whose non-zero value selects a path this build does not implement */
 static const char *k_unsupported[] = {"periodic", "useStrain", "longRange", "localStructureDependent",
                                       "useGaussianBasis", "readProj", "readCoeffs", "inputPsiFilt",
-                                      "restartFromCheckpoint", "restartFromOrtho", "restartFromSigma",
-                                      "interpolatePot", "calcFilterOnly", NULL};
+                                      "restartFromCheckpoint", "interpolatePot", NULL};
 
 static int in_list(const char *k, const char **l)
 {
@@ -60,6 +63,7 @@ int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, 
   p->fermi_e = -0.18;    /* read.c:87 */
   p->sigma_e_cut = 0.01; /* read.c:89 */
   p->get_all_states = 1; /* read.c:85 */
+  p->print_psi_filt = 1; /* read.c:34 */
   p->precision = 0;
   FILE *f = fopen(path, "r");
   if (!f) { seterr(err, errlen, "cannot open", path); return -1; }
@@ -103,7 +107,20 @@ int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, 
     else if (!strcmp(key, "NonLocal")) { rc = parse_long(val, &lv); p->nl = (int)lv; }
     else if (!strcmp(key, "approxEnergyRange")) { rc = parse_long(val, &lv); p->approx_energy_range = (int)lv; }
     else if (!strcmp(key, "mixedPrecision")) { rc = parse_long(val, &lv); p->precision = lv ? 1 : 0; }
-    else if (in_list(key, k_unsupported)) {
+    else if (!strcmp(key, "printPsiFilt")) { rc = parse_long(val, &lv); p->print_psi_filt = (int)lv; }
+    else if (!strcmp(key, "printPsiDiag")) { rc = parse_long(val, &lv); p->print_psi_diag = (int)lv; }
+    else if (!strcmp(key, "calcFilterOnly")) { rc = parse_long(val, &lv); p->calc_filter_only = (int)lv; }
+    else if (!strcmp(key, "restartFromOrtho")) {
+      /* "restartFromOrtho = 1 <states in psi-filt.dat>" (read.c:762-773) */
+      rc = parse_long(val, &lv);
+      p->restart_from_ortho = (int)lv;
+      if (!rc && lv == 1 && (fscanf(f, "%ld", &p->n_states_for_ortho) != 1 || p->n_states_for_ortho < 1)) rc = -1;
+    } else if (!strcmp(key, "restartFromSigma")) {
+      /* "restartFromSigma = 1 <states in psi-diag.dat>" (read.c:775-786) */
+      rc = parse_long(val, &lv);
+      p->restart_from_sigma = (int)lv;
+      if (!rc && lv == 1 && (fscanf(f, "%ld", &p->n_states_for_sigma) != 1 || p->n_states_for_sigma < 1)) rc = -1;
+    } else if (in_list(key, k_unsupported)) {
       if (parse_double(val, &dv) == 0 && dv != 0.0) {
         seterr(err, errlen, "input.par key not supported by this build (set it to 0)", key);
         fclose(f);
@@ -167,6 +184,9 @@ int fbse_read_bse_params(const char *path, fbse_bse_params *p, char *err, size_t
     else if (!strcmp(key, "deltaEhole")) rc = parse_double(val, &p->delta_e_hole);
     else if (!strcmp(key, "deltaEelec")) rc = parse_double(val, &p->delta_e_elec);
     else if (!strcmp(key, "mixedPrecision")) { rc = parse_long(val, &lv); p->precision = lv ? 1 : 0; }
+    else if (!strcmp(key, "coulombDone")) { rc = parse_long(val, &lv); p->coulomb_done = (int)lv; }
+    else if (!strcmp(key, "restartCoulomb")) { rc = parse_long(val, &lv); p->restart_coulomb = (int)lv; }
+    else if (!strcmp(key, "calcCoulombOnly")) { rc = parse_long(val, &lv); p->calc_coulomb_only = (int)lv; }
     else if (!strcmp(key, "spinOrbit") || !strcmp(key, "NonLocal") || !strcmp(key, "KEmax")) {
       rc = parse_double(val, &dv); /* carried by output.dat; the value here is not used */
     } else if (in_list(key, k_ignored)) {

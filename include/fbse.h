@@ -142,6 +142,13 @@ int fbse_energy_range(fbse_ctx *ctx, long seed, long max_iter, double *emin, dou
 int fbse_normalize_all(fbse_ctx *ctx, double *psitot, long n, double *norms);
 int fbse_energy_all(fbse_ctx *ctx, const double *psitot, long n, double *ene);
 
+/* calc_sigma_E (filter_mpi/energy.c:383-539) over n psitot states (device):
+ * eval_i = dv Re<psi_i|H psi_i> and sigma_i = sqrt|dv <H psi_i|H psi_i> -
+ * eval_i^2| (host arrays of n doubles).  The reference forms <psi|H (H psi)>,
+ * equal for Hermitian H; the states are not normalised here (the reference
+ * expects normalised states, as after diag_H or restart_from_sigma). */
+int fbse_sigma_e(fbse_ctx *ctx, const double *psitot, long n, double *eval, double *sigma);
+
 /* fbse_normalize_all without any allocation (no counterpart in the reference):
  * for callers that must not allocate device memory mid-run.  Its scratch is a
  * file-scope device array of about 1.06 MB, at most 1024 states per call
@@ -212,10 +219,28 @@ int fbse_bse_solve(fbse_ctx *ctx, const double *eval_qp_host, long n_qp, long n_
 int fbse_bse_dipoles(fbse_ctx *ctx, const double *psi_qp, const double *gx, const double *gy, const double *gz,
                      long n_h, long n_e, long lumo_idx, double *mu_host);
 
+/* calc_eh_kernel_cplx of the real-valued BSE (bse_real/coulomb.c:20-705):
+ * psi_qp holds real one-component states (ngrid doubles each, device; the
+ * context has nspin = 1), direct / exchange are n_xton x n_xton doubles
+ * (device), lower triangles as fbse_bse_kernel; K^d uses the real part of the
+ * convolution (bse_real/hartree.c:31) and K^x the singlet factor 2
+ * (exchange = -2 dv sum, bse_real/coulomb.c:568). */
+int fbse_bse_kernel_real(fbse_ctx *ctx, const double *psi_qp, long n_h, long n_e, long lumo_idx,
+                         const double *pot_bare, const double *pot_screened, double *direct, double *exchange);
+
+/* calc_mag_dipole (bse_cplx/dipole.c:160-331): magnetic transition dipoles
+ * m_ia = -(1/2) <i|L|a>, L = r x p with p = -i grad by FFT (l_operator,
+ * p_operator, bse_cplx/ang_mom_operators.c:6-170), for the same basis and
+ * coordinates as fbse_bse_dipoles.  m_host: [n_h][n_e][3] complex (host,
+ * interleaved), pair index i * n_e + (a - lumo_idx). */
+int fbse_bse_mag_dipoles(fbse_ctx *ctx, const double *psi_qp, const double *gx, const double *gy, const double *gz,
+                         long n_h, long n_e, long lumo_idx, double *m_host);
+
 /* calc_optical_exc (bse_cplx/optical.c:6-99), electric part: exciton transition
  * dipoles mu_j = sum_ibs coeff[ibs][j] mu_(i(ibs), a(ibs)).  coeff: device, as
  * fbse_bse_solve returns it; mu_pairs_host: fbse_bse_dipoles' output;
- * mu_xton_host: [n_xton][3] complex (host).  OS.dat's columns follow from it:
+ * mu_xton_host: [n_xton][3] complex (host); the same sum of the magnetic pair
+ * dipoles (fbse_bse_mag_dipoles) gives M.dat.  OS.dat's columns follow from it:
  * |mu_j|, E_j, (2/3) E_j |mu_j|^2. */
 int fbse_bse_optical(fbse_ctx *ctx, const double *coeff, const double *mu_pairs_host, long n_h, long n_e,
                      double *mu_xton_host);

@@ -645,6 +645,35 @@ def bse_kernels(psi_qp: np.ndarray, nh: int, ne: int, lumo: int, bare, scr, grid
     return D, X
 
 
+def bse_kernels_real(psi_qp: np.ndarray, nh: int, ne: int, lumo: int, bare, scr, grid: Grid):
+    """calc_eh_kernel_cplx of the real-valued BSE (bse_real/coulomb.c:20-705) for
+    real one-component states [n_qp][ngrid]: rho products without conjugation,
+    the real part of each convolution (bse_real/hartree.c:31), and the singlet
+    factor 2 on the exchange (coulomb.c:568)."""
+    N = grid.ngrid
+    dv = grid.dv
+    nx = ne * nh
+    D = np.zeros((nx, nx))
+    X = np.zeros((nx, nx))
+    for a in range(ne):
+        for b in range(ne):
+            h = hartree(psi_qp[lumo + a] * psi_qp[lumo + b], scr, grid).real
+            for i in range(nh):
+                for j in range(nh):
+                    ibs, jbs = a * nh + i, b * nh + j
+                    if ibs >= jbs:
+                        D[ibs, jbs] = np.sum(h * psi_qp[j] * psi_qp[i]) * dv
+    for a in range(ne):
+        for i in range(nh):
+            h = hartree(psi_qp[lumo + a] * psi_qp[i], bare, grid).real
+            for b in range(ne):
+                for j in range(nh):
+                    ibs, jbs = a * nh + i, b * nh + j
+                    if ibs >= jbs:
+                        X[ibs, jbs] = -2.0 * np.sum(h * psi_qp[j] * psi_qp[lumo + b]) * dv
+    return D, X
+
+
 def bse_solve(eval_qp, nh, ne, lumo, D, X):
     """build_h0_mat, build_BSE_mat, bethe_salpeter (bse_cplx/mod_bse.c:54-148,
     bethe-salpeter.c:7-350): returns (E, C, <H>, <Kd>, <Kx>, <h0>)."""
@@ -677,6 +706,42 @@ def bse_dipoles(psi_qp, nh, ne, lumo, grid: Grid, nspin=2):
             for d in range(3):
                 mu[i * ne + a, d] = np.sum(t * coords[d]) * grid.dv
     return mu
+
+
+def init_kvec(n, dk):
+    """init_kvec (bse_cplx/ang_mom_operators.c:90-103) without the 1/N norm:
+    k[j] = j dk, k[n-j] = -j dk for j = 1..n/2 in that order."""
+    k = np.zeros(n)
+    for j in range(1, n // 2 + 1):
+        k[j] = j * dk
+        k[n - j] = -j * dk
+    return k
+
+
+def bse_mag_dipoles(psi_qp, nh, ne, lumo, grid: Grid, nspin=2):
+    """calc_mag_dipole (bse_cplx/dipole.c:160-331): m_ia = (dv/2) sum
+    conj(psi_i) L'psi_a with L'psi = -(r x p psi), p_d psi = IFFT(k_d FFT psi)
+    (l_operator / p_operator, ang_mom_operators.c:6-170; the two unnormalised
+    FFTW transforms and the 1/N in k_d make numpy's fftn / ifftn pair)."""
+    gx, gy, gz = bse_axes(grid)
+    shp = (grid.nz, grid.ny, grid.nx)
+    Z, Y, X = np.meshgrid(gz, gy, gx, indexing="ij")
+    KZ, KY, KX = np.meshgrid(init_kvec(grid.nz, 2 * np.pi / (grid.nz * grid.dz)),
+                             init_kvec(grid.ny, 2 * np.pi / (grid.ny * grid.dy)),
+                             init_kvec(grid.nx, 2 * np.pi / (grid.nx * grid.dx)), indexing="ij")
+    N = grid.ngrid
+    m = np.zeros((nh * ne, 3), np.complex128)
+    for a in range(ne):
+        L = []
+        for s in range(nspin):
+            f = np.fft.fftn(psi_qp[lumo + a, s * N:(s + 1) * N].reshape(shp))
+            px, py, pz = (np.fft.ifftn(k * f) for k in (KX, KY, KZ))
+            L.append([-(Y * pz - Z * py), -(Z * px - X * pz), -(X * py - Y * px)])
+        for i in range(nh):
+            for d in range(3):
+                m[i * ne + a, d] = 0.5 * grid.dv * sum(
+                    np.sum(np.conj(psi_qp[i, s * N:(s + 1) * N].reshape(shp)) * L[s][d]) for s in range(nspin))
+    return m
 
 
 def bse_optical(C, mu, nh, ne):

@@ -16,7 +16,10 @@ Fixtures (all data outputs or inputs of the reference's own example runs):
                          value of its localPot.cube (build_local_pot output,
                          "%.5g") with the grid header
   cspbi3/                1x1x1 CsPbI3 spinor SO+NL example: input.par,
-                         conf.par, pot*.par, SO_*.par and reference eval.dat
+                         conf.par, pot*.par, SO_*.par and reference eval.dat;
+                         its BSE run (bse_cplx/EXAMPLES/1x1x1_CsPbI3/bse):
+                         bse_input.par and the reference's exciton.dat,
+                         OS.dat, OS0.dat, M0.dat, M.dat, rs0.dat, rs.dat
 """
 import os
 import shutil
@@ -64,6 +67,10 @@ def main():
     for fn in ("input.par", "conf.par", "potCs.par", "potI.par", "potPb.par", "SO_Cs.par", "SO_I.par", "SO_Pb.par"):
         shutil.copy(os.path.join(src, fn), d)
     shutil.copy(os.path.join(src, "reference_output", "eval.dat"), d)
+    bse = os.path.join(REF, "bse_cplx", "EXAMPLES", "1x1x1_CsPbI3", "bse")
+    shutil.copy(os.path.join(bse, "input.par"), os.path.join(d, "bse_input.par"))
+    for fn in ("exciton.dat", "OS.dat", "OS0.dat", "M0.dat", "M.dat", "rs0.dat", "rs.dat"):
+        shutil.copy(os.path.join(bse, "reference_output", fn), d)
 
 
 if __name__ == "__main__":

@@ -126,6 +126,39 @@ def test_bse_dipoles_match_oracle(fbse, cuda):
     assert _relmax(mu, ref) < 1e-12
 
 
+@pytest.mark.parametrize("name,precision,tol", [("odd21x20x18", 0, 1e-12), ("cubic24", 0, 1e-12), ("cubic24", 1, 3e-5)])
+def test_bse_kernel_real_matches_oracle(fbse, cuda, name, precision, tol):
+    """bse_real: real one-component states, real kernels, exchange x 2."""
+    import torch
+    nh, ne, gap = 3, 3, 1
+    g = GRIDS[name]
+    ctx = _ctx(fbse, g, precision, nspin=1, cplx=False)
+    lumo = nh + gap
+    psi = qp_states(g, lumo + ne, 11, nspin=1).real.copy()
+    psi /= np.sqrt(np.sum(psi ** 2, axis=1) * g.dv)[:, None]
+    bare, scr = ctx.bse_potentials(*O.bse_axes(g), g.xmin, g.ymin, g.zmin, (5.0, 5.0, 5.0))
+    D, X = ctx.bse_kernel_real(torch.tensor(psi, device=cuda), nh, ne, lumo, bare, scr)
+    rD, rX = O.bse_kernels_real(psi, nh, ne, lumo, bare.cpu().numpy(), scr.cpu().numpy(), g)
+    assert _relmax(D.cpu().numpy(), rD) < tol
+    assert _relmax(X.cpu().numpy(), rX) < tol
+    # the complex kernel on the same states as complex spinless states: same
+    # direct, half the exchange (no singlet factor)
+    if precision == 0:
+        cctx = _ctx(fbse, g, 0, nspin=1, cplx=True)
+        Dc, Xc = cctx.bse_kernel(torch.tensor(psi.astype(np.complex128), device=cuda), nh, ne, lumo, bare, scr)
+        assert _relmax(Dc.cpu().numpy().real, rD) < 1e-12 and _relmax(2 * Xc.cpu().numpy().real, rX) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["odd21x20x18", "cubic24"])
+def test_bse_mag_dipoles_match_oracle(fbse, cuda, name):
+    """calc_mag_dipole: p by FFT (init_kvec's k, Nyquist negative), L = -(r x p)."""
+    nh, ne, gap = 3, 4, 1
+    g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, name, nh, ne, gap)
+    m = ctx.bse_mag_dipoles(psi_d, *O.bse_axes(g), nh, ne, lumo)
+    ref = O.bse_mag_dipoles(psi, nh, ne, lumo, g)
+    assert _relmax(m, ref) < 1e-12
+
+
 def test_bse_optical_matches_oracle(fbse, cuda):
     nh, ne, gap = 3, 4, 1
     g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, "cubic24", nh, ne, gap)

@@ -28,7 +28,11 @@ class FilterParams(ctypes.Structure):
                 ("set_targets", ctypes.c_int), ("n_targets_vb", ctypes.c_long), ("n_targets_cb", ctypes.c_long),
                 ("set_seed", ctypes.c_int), ("seed", ctypes.c_long), ("use_spinors", ctypes.c_int),
                 ("so", ctypes.c_int), ("nl", ctypes.c_int), ("get_all_states", ctypes.c_int),
-                ("approx_energy_range", ctypes.c_int), ("precision", ctypes.c_int)]
+                ("approx_energy_range", ctypes.c_int), ("precision", ctypes.c_int),
+                ("print_psi_filt", ctypes.c_int), ("print_psi_diag", ctypes.c_int),
+                ("calc_filter_only", ctypes.c_int), ("restart_from_ortho", ctypes.c_int),
+                ("restart_from_sigma", ctypes.c_int), ("n_states_for_ortho", ctypes.c_long),
+                ("n_states_for_sigma", ctypes.c_long)]
 
 
 @pytest.fixture(scope="module")
@@ -58,6 +62,38 @@ def test_read_filter_params_example(lib):
     assert (p.n_targets_vb, p.n_targets_cb, p.set_targets) == (10, 6, 1)
     assert p.so == 1 and p.nl == 1 and p.use_spinors == 1 and p.get_all_states == 1
     assert p.fermi_e == -0.19 and p.vbmin == -0.5 and p.cbmax == -0.1 and p.ke_max == 20.0
+    # printPsiFilt is on unless input.par says otherwise (read.c:34)
+    assert p.print_psi_filt == 1 and p.restart_from_ortho == 0 and p.restart_from_sigma == 0
+
+
+def test_read_filter_params_restarts(lib, tmp_path):
+    base = "dGrid = 0.5\nmStatesPerFilter = 4\nnFilterCycles = 2\nnCheby = 16\n"
+    err = ctypes.create_string_buffer(512)
+    p = FilterParams()
+    (tmp_path / "a.par").write_text(base + "restartFromOrtho = 1 8\nprintPsiFilt = 0\nprintPsiDiag = 1\n"
+                                    "calcFilterOnly = 0\nsaveCheckpoints = 1\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "a.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
+    assert (p.restart_from_ortho, p.n_states_for_ortho, p.print_psi_filt, p.print_psi_diag) == (1, 8, 0, 1)
+    (tmp_path / "b.par").write_text(base + "restartFromSigma = 1 12\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "b.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
+    assert (p.restart_from_sigma, p.n_states_for_sigma) == (1, 12)
+    # the state count must follow (read.c:770-773)
+    (tmp_path / "c.par").write_text(base + "restartFromOrtho = 1\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "c.par").encode(), ctypes.byref(p), err, 512) != 0
+    # checkpoint_<id>.dat restarts are refused with the key named
+    (tmp_path / "d.par").write_text(base + "restartFromCheckpoint = 2\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "d.par").encode(), ctypes.byref(p), err, 512) != 0
+    assert b"restartFromCheckpoint" in err.value
+
+
+def test_read_filter_params_cdse_example(lib):
+    # the 2.2 nm CdSe example's keys (crystalStructure, outmostMaterial,
+    # useStrain = 0, printCubes with its second value) are accepted
+    p = FilterParams()
+    err = ctypes.create_string_buffer(512)
+    rc = lib.fbse_read_filter_params(os.path.join(GOLD, "cdse22", "input.par").encode(), ctypes.byref(p), err, 512)
+    assert rc == 0, err.value
+    assert (p.dx, p.so, p.use_spinors, p.m_states_per_filter) == (0.8, 0, 0, 16)
 
 
 def test_read_filter_params_rejects(lib, tmp_path):

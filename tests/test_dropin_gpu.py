@@ -79,3 +79,132 @@ def test_dropin_bse_matches_reference_exciton(cuda, tmp_path):
     osr = np.loadtxt(os.path.join(GOLD, "cspbi3", "OS.dat"))
     assert osd[0, 1] < 1e-3  # the lowest exciton is dark
     assert abs(np.sum(osd[1:4, 1] ** 2) - np.sum(osr[1:4, 1] ** 2)) < 1e-2 * np.sum(osr[1:4, 1] ** 2)
+
+    # magnetic outputs: the files and their pair / exciton counts
+    assert np.loadtxt(tmp_path / "M0.dat").shape == (64, 11) and np.loadtxt(tmp_path / "rs0.dat").shape == (64, 4)
+    assert np.loadtxt(tmp_path / "M.dat").shape == (64, 10) and np.loadtxt(tmp_path / "rs.dat").shape == (64, 3)
+    bc = np.loadtxt(tmp_path / "bs-coeff-0.dat")
+    assert bc.shape == (64, 4) and abs(bc[:, 3].sum() - 1.0) < 1e-4  # |C_j|^2 ("%lg") sums to 1
+    assert (tmp_path / "bs-coeff-9.dat").exists() and not (tmp_path / "bs-coeff-10.dat").exists()
+
+    # the kernel files (coulomb.c:289-371, 534-602) and the coulombDone restart
+    dl = np.loadtxt(tmp_path / "direct-0.dat")
+    xl = np.loadtxt(tmp_path / "exchange-0.dat")
+    assert dl.shape == (64 * 64, 8) and xl.shape == (64 * 65 // 2, 8)
+    assert np.all(xl[:, 4] >= xl[:, 5]) and np.all(dl[dl[:, 4] < dl[:, 5]][:, 6:] == 0)
+    assert dl[0, :4].tolist() == [8, 8, 0, 0] and dl[-1, :4].tolist() == [15, 15, 7, 7]
+    shutil.copy(tmp_path / "direct-0.dat", tmp_path / "direct.dat")
+    shutil.copy(tmp_path / "exchange-0.dat", tmp_path / "exchange.dat")
+    with open(tmp_path / "input.par", "w") as f:
+        f.write(bse + "coulombDone = 1\n")
+    _run("fbse_bse", tmp_path)
+    ex2 = np.loadtxt(tmp_path / "exciton.dat")
+    # the files carry 12 decimals
+    assert np.max(np.abs(ex2[:, 1] - ex[:, 1])) < 1e-9
+
+
+def _small(extra=""):
+    text = open(os.path.join(GOLD, "cspbi3", "input.par")).read()
+    text = text.replace("mStatesPerFilter = 16", "mStatesPerFilter = 8").replace("nFilterCycles = 16", "nFilterCycles = 3")
+    text = text.replace("nCheby = 2048", "nCheby = 512").replace("setTargets = 1 10 6", "setTargets = 1 4 4")
+    return text.replace("setSeed = 0", "setSeed = 1 2718") + extra
+
+
+def test_dropin_restarts_reproduce_the_full_run(cuda, tmp_path):
+    """printPsiFilt / printPsiDiag files and the restarts from them
+    (restartFromOrtho, restartFromSigma), and calcFilterOnly."""
+    full = tmp_path / "full"
+    full.mkdir()
+    _stage(full, _small("printPsiDiag = 1\n"))
+    _run("fbse_filter", full)
+    ev = np.loadtxt(full / "eval.dat")
+    aux = np.loadtxt(full / "eval_aux.dat")
+    assert np.array_equal(aux[:, 1], ev[:, 1]) and len(aux) == len(ev)  # getAllStates = 1
+    stlen = 2 * 2 * 44 ** 3
+    parts = [full / f"psi-filt-{j}-0.dat" for j in range(3)]
+    assert all(os.path.getsize(f) == 8 * stlen * 8 for f in parts)
+    assert os.path.getsize(full / "psi-diag.dat") == len(ev) * stlen * 8
+
+    # restartFromOrtho: psi-filt.dat = the per-start files one after the other
+    ro = tmp_path / "ortho"
+    ro.mkdir()
+    _stage(ro, _small("restartFromOrtho = 1 24\n"))
+    with open(ro / "psi-filt.dat", "wb") as out:
+        for f in parts:
+            out.write(open(f, "rb").read())
+    _run("fbse_filter", ro)
+    ev_o = np.loadtxt(ro / "eval.dat")
+    assert ev_o.shape == ev.shape
+    assert np.max(np.abs(ev_o[:, 1] - ev[:, 1])) < 1e-10
+    assert not (ro / "psi-filt-0-0.dat").exists()  # no filter ran
+
+    # restartFromSigma on psi-diag.dat: the same energies, sigma_E as <H^2> - <H>^2
+    rs = tmp_path / "sigma"
+    rs.mkdir()
+    _stage(rs, _small(f"restartFromSigma = 1 {len(ev)}\n"))
+    shutil.copy(full / "psi-diag.dat", rs / "psi-diag.dat")
+    _run("fbse_filter", rs)
+    ev_s = np.loadtxt(rs / "eval.dat")
+    assert np.max(np.abs(ev_s[:, 1] - ev[:, 1])) < 1e-10
+    assert np.max(np.abs(ev_s[:, 2] - ev[:, 2])) < 1e-6
+    assert os.path.getsize(rs / "psi.dat") == os.path.getsize(full / "psi.dat")
+
+    # calcFilterOnly: the psi-filt files and nothing after the filter
+    fo = tmp_path / "only"
+    fo.mkdir()
+    _stage(fo, _small("calcFilterOnly = 1\n"))
+    _run("fbse_filter", fo)
+    assert (fo / "psi-filt-2-0.dat").exists() and not (fo / "eval.dat").exists()
+    # the same filter (the projector scatter's atomics may reorder the last bits)
+    a, b = np.fromfile(fo / "psi-filt-0-0.dat"), np.fromfile(parts[0])
+    assert np.max(np.abs(a - b)) < 1e-9 * np.max(np.abs(b))
+
+
+def test_dropin_bse_real_on_cdse_filter_output(cuda, tmp_path):
+    """bse_real through fbse_bse: the real 2.2 nm CdSe filter output (one
+    component, complex_idx = 1) gives real kernel files and the real optical
+    formats, and the exciton energies of the oracle's real BSE on the same
+    basis states (read back from output.dat)."""
+    from oracle import oracle as O
+    for f in ("conf.par", "potCd.par", "potSe.par", "potP1.par", "potP2.par"):
+        shutil.copy(os.path.join(GOLD, "cdse22", f), tmp_path / f)
+    text = open(os.path.join(GOLD, "cdse22", "input.par")).read()
+    text = text.replace("nCheby = 2048", "nCheby = 1024").replace("nFilterCycles = 16", "nFilterCycles = 4")
+    text = text.replace("setSeed = 0", "setSeed = 1 4242")
+    with open(tmp_path / "input.par", "w") as f:
+        f.write(text + "printPsiFilt = 0\n")
+    out = _run("fbse_filter", tmp_path)
+    ev = np.loadtxt(tmp_path / "eval.dat")
+    with open(tmp_path / "input.par", "w") as f:
+        f.write("maxHoleStates = 4\nmaxElecStates = 3\nsigmaECut = 0.01\nepsX = 5.0\nepsY = 5.0\nepsZ = 5.0\n"
+                "fermiEnergy = -0.18\n")
+    bout = _run("fbse_bse", tmp_path)
+    import re
+    nh, ne = (int(v) for v in re.search(r"fbse_bse: (\d+) holes, (\d+) electrons", bout).groups())
+    assert 1 <= nh <= 4 and 1 <= ne <= 3
+    nx = nh * ne
+    ex = np.loadtxt(tmp_path / "exciton.dat")
+    assert ex.shape == (nx, 7)
+    dl = np.loadtxt(tmp_path / "direct-0.dat")
+    assert dl.shape == (nx * nx, 7)  # one value per element (bse_real/coulomb.c:355)
+    assert np.loadtxt(tmp_path / "OS0.dat", skiprows=1).shape == (nx, 8)
+    assert np.loadtxt(tmp_path / "OS.dat").shape == (nx, 7)
+    assert (tmp_path / "bs.dat").exists() and (tmp_path / "BSEcoeff.dat").exists()
+
+    # the oracle on the basis that get_qp_basis_indices picks from eval.dat
+    m = re.search(r"grid (\d+) x (\d+) x (\d+), d = (\S+) (\S+) (\S+), origin (\S+) (\S+) (\S+)", out)
+    nx, ny, nz = (int(m.group(k)) for k in (1, 2, 3))
+    dx, dy, dz, x0, y0, z0 = (float(m.group(k)) for k in range(4, 10))
+    g = O.Grid(nx, ny, nz, dx, dy, dz, x0, y0, z0)
+    conv = [i for i in range(len(ev)) if ev[i, 2] < 0.01]
+    holes = [i for i in conv if ev[i, 1] < -0.18][-4:]
+    elecs = [i for i in conv if ev[i, 1] > -0.18][:3]
+    assert (len(holes), len(elecs)) == (nh, ne)
+    psi_all = np.fromfile(tmp_path / "psi.dat").reshape(len(ev), g.ngrid)
+    qp = psi_all[holes + elecs]
+    bare, scr = O.bse_potentials(g, (5.0, 5.0, 5.0))
+    D, X = O.bse_kernels_real(qp, nh, ne, nh, bare, scr, g)
+    evq = ev[holes + elecs, 1]
+    e, *_ = O.bse_solve(evq, nh, ne, nh, D.astype(np.complex128), X.astype(np.complex128))
+    print(f"\n[fbse_bse real] lowest exciton {ex[0, 1]:.10f} (oracle {e[0]:.10f})\n" + bout[-200:])
+    assert np.max(np.abs(ex[:, 1] - e)) < 1e-8

@@ -100,6 +100,11 @@ def test_normalize_and_energy(fbse, cuda, cplx):
     st = got.view(np.complex128) if cplx else got.astype(np.complex128)
     wantE = [O.energy(s if cplx else s.real.astype(np.complex128), sysm) for s in st]
     assert np.allclose(ene, wantE, rtol=1e-11, atol=1e-12)
+    # calc_sigma_E on the same normalised states (n = 5: an odd tail of packed real pairs)
+    ev, sg = ctx.sigma_e(t)
+    wev, wsg = O.sigma_e(st, sysm)
+    assert np.allclose(ev, wev, rtol=1e-11, atol=1e-12)
+    assert np.allclose(sg, wsg, rtol=1e-9)
 
 
 def test_normalize_zero_norm_errors(fbse, cuda):

@@ -187,6 +187,12 @@ def test_cspbi3_bse_matches_reference_exciton(fbse, cuda):
         mu = bctx.bse_dipoles(qp, gx, gy, gz, 8, 8, 8)
         mx = bctx.bse_optical(C, mu, 8, 8)
         samples.append((e, dd, xx, h0, np.sum(np.abs(mx) ** 2, axis=1)))
+        if smp == 0:
+            # magnetic dipoles and rotational strengths (calc_mag_dipole,
+            # calc_rotational_strength, calc_optical_exc) of the same basis
+            mm = bctx.bse_mag_dipoles(qp, gx, gy, gz, 8, 8, 8)
+            mmx = bctx.bse_optical(C, mm, 8, 8)
+            mag0 = (mu, mm, mx, mmx)
     E = np.array([s[0] for s in samples])
     ref = np.loadtxt(os.path.join(d, "exciton.dat"))
     osr = np.loadtxt(os.path.join(d, "OS.dat"))
@@ -209,3 +215,45 @@ def test_cspbi3_bse_matches_reference_exciton(fbse, cuda):
         assert abs(np.sum(x0[cl]) - np.sum(ref[cl, 4])) < 1e-6
         assert abs(np.sum(h00[cl]) - np.sum(ref[cl, 5])) < 1e-6
         assert abs(np.sum(m0[cl]) - np.sum(osr[cl, 1] ** 2)) < 1e-5 * max(1.0, np.sum(osr[cl, 1] ** 2))
+    # M.dat / rs.dat: |m_j|^2 and Im(mu_j . conj m_j) summed over the same clusters
+    mu, mm, mx, mmx = mag0
+    Mr = np.loadtxt(os.path.join(d, "M.dat"))
+    rsr = np.loadtxt(os.path.join(d, "rs.dat"))
+    m2 = np.sum(np.abs(mmx) ** 2, axis=1)
+    rsx = np.sum(np.imag(mx * np.conj(mmx)), axis=1)
+    worst_m = worst_rs = 0.0
+    for cl in _clusters(ref[:, 1]):
+        if not np.all(fixed[cl]):
+            continue
+        worst_m = max(worst_m, abs(np.sum(m2[cl]) - np.sum(Mr[cl, 1] ** 2)))
+        worst_rs = max(worst_rs, abs(np.sum(rsx[cl]) - np.sum(rsr[cl, 2])))
+    # pair level (M0.dat, rs0.dat): sums over Kramers-degenerate hole and electron
+    # levels, leaving out the two holes of the partly included quartet
+    M0r = np.loadtxt(os.path.join(d, "M0.dat"))
+    rs0r = np.loadtxt(os.path.join(d, "rs0.dat"))
+    lv = lambda idx: [[idx[k] for k in cl] for cl in _clusters(evq[idx])]
+    holes_lv, elec_lv = lv(list(range(2, 8))), lv(list(range(8, 16)))
+    worst_m0 = worst_rs0 = 0.0
+    scale_m0 = np.max(M0r[:, 2] ** 2)
+    # the files list (i, a) in different orders (M0.dat a-major, rs0.dat i-major)
+    row_m0 = {(int(r[0]), int(r[1])): k for k, r in enumerate(M0r)}
+    row_rs0 = {(int(r[0]), int(r[1])): k for k, r in enumerate(rs0r)}
+    for H in holes_lv:
+        for A in elec_lv:
+            pairs = [(i, a) for i in H for a in A]
+            mine_rows = [i * 8 + (a - 8) for i, a in pairs]  # this library: i * n_e + (a - lumo)
+            mine = np.sum(np.abs(mm[mine_rows]) ** 2)
+            ref_m = np.sum(M0r[[row_m0[p] for p in pairs], 2] ** 2)
+            worst_m0 = max(worst_m0, abs(mine - ref_m) / scale_m0)
+            mine_rs = np.sum(np.imag(np.sum(mu[mine_rows] * np.conj(mm[mine_rows]), axis=1)))
+            ref_rs = np.sum(rs0r[[row_rs0[p] for p in pairs], 3])
+            # the cube is centrosymmetric: rotational strengths vanish up to the
+            # grid's asymmetry and the states' convergence, so they can only
+            # agree on the scale |mu| |m| of the block
+            rs_scale = np.sqrt(np.sum(np.abs(mu[mine_rows]) ** 2) * mine)
+            worst_rs0 = max(worst_rs0, abs(mine_rs - ref_rs) / rs_scale)
+    print(f"[cspbi3 bse] magnetic: exciton |m|^2 max dev {worst_m:.2e} (max {Mr[:, 1].max() ** 2:.2e}), rs {worst_rs:.2e}; "
+          f"pairs |m|^2 rel {worst_m0:.2e}, rs0 rel to |mu||m| {worst_rs0:.2e}")
+    assert worst_m0 < 1e-4 and worst_rs0 < 3e-3
+    assert worst_m < 1e-4 * Mr[:, 1].max() ** 2
+    assert worst_rs < 1e-4 * np.sqrt(np.max(np.sum(np.abs(mx) ** 2, axis=1)) * Mr[:, 1].max() ** 2)
