@@ -176,6 +176,9 @@ def run_gpu(args):
     torch.cuda.synchronize()
     times, counts = [], []
     l0 = F.launch_count()
+    # the timed steps sit in an NVTX range so that a profiler can select them
+    # (ncu --nvtx --nvtx-include "fbse_timed_steps/")
+    torch.cuda.nvtx.range_push("fbse_timed_steps")
     with Clocks(local) as clk:
         for _ in range(args.steps):
             a = torch.cuda.Event(enable_timing=True)
@@ -188,6 +191,7 @@ def run_gpu(args):
             times.append(a.elapsed_time(b) / 1e3)
             counts.append(count_converged(ev, sg, ev64, sg64))
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     launches = (F.launch_count() - l0) / max(1, args.steps)
     t_step = float(np.mean(times))
     n_conv = int(np.median(counts))

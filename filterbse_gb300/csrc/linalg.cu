@@ -24,6 +24,8 @@
 
 #include <cstdlib>
 
+#include <type_traits>
+
 #include "fbse_internal.cuh"
 
 namespace cg = cooperative_groups;
@@ -38,16 +40,28 @@ int unpack_states(fbse_ctx *c, const void *src, double *dst, long ndst);
 // A, B: n vectors of length L (complex: interleaved FP64 pairs; real: FP64).
 // Tile 64 x 64 outputs per CTA, 256 threads x (4 x 4) outputs, K step 16.
 // Compute type T (float for the mixed path, double for the FP64 path);
-// partials are written in FP64: part[chunk][i][j].
+// partials are written in FP64: part[chunk][i][j].  Both products this file
+// forms (Psi^H Psi and Psi^H H Psi) are Hermitian, so only tiles with
+// ti <= tj are computed (blockIdx.x enumerates them) and an off-diagonal
+// tile is also stored conjugate-transposed.  Shared tiles hold complex values
+// as C<T> with one element of padding per K row, so the transposing stores
+// (consecutive threads: consecutive k) and the float2 / double2 reads of the
+// product loop are free of bank conflicts.
 // ---------------------------------------------------------------------------
 template <typename T, bool CPLX>
 __global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, const double *__restrict__ B, int n,
                                               long L, long kchunk, double2 *__restrict__ part)
 {
   constexpr int TM = 64, TK = 16;
-  __shared__ T As[TK][TM][CPLX ? 2 : 1];
-  __shared__ T Bs[TK][TM][CPLX ? 2 : 1];
-  const int i0 = blockIdx.x * TM, j0 = blockIdx.y * TM;
+  using E = typename std::conditional<CPLX, C<T>, T>::type;
+  __shared__ E As[TK][TM + 1];
+  __shared__ E Bs[TK][TM + 1];
+  // tile pair (ti, tj), ti <= tj, from the linear index
+  const int nt = (n + TM - 1) / TM;
+  int ti = 0, rem = blockIdx.x;
+  while (rem >= nt - ti) { rem -= nt - ti; ti++; }
+  const int tj = ti + rem;
+  const int i0 = ti * TM, j0 = tj * TM;
   const long k0 = blockIdx.z * kchunk;
   const long k1 = min(L, k0 + kchunk);
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -58,19 +72,20 @@ __global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, cons
     for (int b = 0; b < 4; b++) { accr[a][b] = 0; acci[a][b] = 0; }
   for (long kb = k0; kb < k1; kb += TK) {
     // load: 64 rows x 16 k for A and B; thread t loads rows (t / 16) + 16 q, k = t % 16
+#pragma unroll
     for (int q = 0; q < 4; q++) {
       const int r = ty + 16 * q, kk = tx;
       const long k = kb + kk;
       const bool okA = (i0 + r < n) && (k < k1);
       const bool okB = (j0 + r < n) && (k < k1);
-      if (CPLX) {
-        As[kk][r][0] = okA ? (T)A[((long)(i0 + r) * L + k) * 2] : T(0);
-        As[kk][r][CPLX ? 1 : 0] = okA ? (T)A[((long)(i0 + r) * L + k) * 2 + 1] : T(0);
-        Bs[kk][r][0] = okB ? (T)B[((long)(j0 + r) * L + k) * 2] : T(0);
-        Bs[kk][r][CPLX ? 1 : 0] = okB ? (T)B[((long)(j0 + r) * L + k) * 2 + 1] : T(0);
+      if constexpr (CPLX) {
+        const double2 va = okA ? reinterpret_cast<const double2 *>(A)[(long)(i0 + r) * L + k] : make_double2(0, 0);
+        const double2 vb = okB ? reinterpret_cast<const double2 *>(B)[(long)(j0 + r) * L + k] : make_double2(0, 0);
+        As[kk][r] = mk<T>((T)va.x, (T)va.y);
+        Bs[kk][r] = mk<T>((T)vb.x, (T)vb.y);
       } else {
-        As[kk][r][0] = okA ? (T)A[(long)(i0 + r) * L + k] : T(0);
-        Bs[kk][r][0] = okB ? (T)B[(long)(j0 + r) * L + k] : T(0);
+        As[kk][r] = okA ? (T)A[(long)(i0 + r) * L + k] : T(0);
+        Bs[kk][r] = okB ? (T)B[(long)(j0 + r) * L + k] : T(0);
       }
     }
     __syncthreads();
@@ -79,10 +94,13 @@ __global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, cons
       T ar[4], ai[4], br[4], bi[4];
 #pragma unroll
       for (int a = 0; a < 4; a++) {
-        ar[a] = As[kk][ty + 16 * a][0];
-        ai[a] = CPLX ? As[kk][ty + 16 * a][CPLX ? 1 : 0] : T(0);
-        br[a] = Bs[kk][tx + 16 * a][0];
-        bi[a] = CPLX ? Bs[kk][tx + 16 * a][CPLX ? 1 : 0] : T(0);
+        if constexpr (CPLX) {
+          const C<T> u = As[kk][ty + 16 * a], v = Bs[kk][tx + 16 * a];
+          ar[a] = u.x; ai[a] = u.y; br[a] = v.x; bi[a] = v.y;
+        } else {
+          ar[a] = As[kk][ty + 16 * a]; br[a] = Bs[kk][tx + 16 * a];
+          ai[a] = bi[a] = T(0);
+        }
       }
 #pragma unroll
       for (int a = 0; a < 4; a++)
@@ -101,7 +119,10 @@ __global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, cons
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
-      if (i < n && j < n) P[(long)i * n + j] = make_double2((double)accr[a][b], (double)acci[a][b]);
+      if (i < n && j < n) {
+        P[(long)i * n + j] = make_double2((double)accr[a][b], (double)acci[a][b]);
+        if (ti != tj) P[(long)j * n + i] = make_double2((double)accr[a][b], -(double)acci[a][b]);
+      }
     }
 }
 
@@ -321,8 +342,12 @@ int jacobi_eig_dev(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<doubl
 //   out[i][l] = P;  part[blk][i] += |Q - E_i P|^2, |P|^2, Re(conj(P) Q)
 // tile: 128 grid elements x 32 output states per CTA, 256 threads
 // ---------------------------------------------------------------------------
-template <typename T, bool CPLX>
-__global__ void __launch_bounds__(256) k_rotate(const double *__restrict__ Psi, const double *__restrict__ HPsi, int n,
+// PART 2: rotate Psi and H Psi together; PART 0: Psi only (writes out);
+// PART 1: H Psi only, reading the rotated Psi back from out for the residual
+// sums (two launches of half the accumulators each: two CTAs per SM instead
+// of one for the FP32 path).
+template <typename T, bool CPLX, int PART>
+__global__ void __launch_bounds__(256, PART == 2 ? 1 : 2) k_rotate(const double *__restrict__ Psi, const double *__restrict__ HPsi, int n,
                                                 long L, const double2 *__restrict__ Cm, int k,
                                                 const double *__restrict__ E, double *__restrict__ out,
                                                 double *__restrict__ part)
@@ -330,9 +355,11 @@ __global__ void __launch_bounds__(256) k_rotate(const double *__restrict__ Psi, 
   constexpr int TL = 128, TS = 32, TJ = 8;
   const long l0 = (long)blockIdx.x * TL;
   const int s0 = blockIdx.y * TS;
-  __shared__ T Ps[TJ][TL][CPLX ? 2 : 1];
-  __shared__ T Hs[TJ][TL][CPLX ? 2 : 1];
-  __shared__ T Cs[TJ][TS][2];
+  // complex values as C<T>: one float2 / double2 access per value
+  using Elt = typename std::conditional<CPLX, C<T>, T>::type;
+  __shared__ Elt Ps[TJ][TL];
+  __shared__ Elt Hs[TJ][TL];
+  __shared__ C<T> Cs[TJ][TS];
   __shared__ double red[TS][3];
   const int tl = threadIdx.x % 32;  // 4 grid elements per thread: tl + 32 q
   const int ts = threadIdx.x / 32;  // 4 output states per thread: ts + 8 r
@@ -348,22 +375,25 @@ __global__ void __launch_bounds__(256) k_rotate(const double *__restrict__ Psi, 
       const int j = jb + jj;
       const long l = l0 + ll;
       const bool ok = (j < n) && (l < L);
-      if (CPLX) {
-        Ps[jj][ll][0] = ok ? (T)Psi[((long)j * L + l) * 2] : T(0);
-        Ps[jj][ll][CPLX ? 1 : 0] = ok ? (T)Psi[((long)j * L + l) * 2 + 1] : T(0);
-        Hs[jj][ll][0] = ok ? (T)HPsi[((long)j * L + l) * 2] : T(0);
-        Hs[jj][ll][CPLX ? 1 : 0] = ok ? (T)HPsi[((long)j * L + l) * 2 + 1] : T(0);
+      if constexpr (CPLX) {
+        if constexpr (PART != 1) {
+          const double2 u = ok ? reinterpret_cast<const double2 *>(Psi)[(long)j * L + l] : make_double2(0, 0);
+          Ps[jj][ll] = mk<T>((T)u.x, (T)u.y);
+        }
+        if constexpr (PART != 0) {
+          const double2 w = ok ? reinterpret_cast<const double2 *>(HPsi)[(long)j * L + l] : make_double2(0, 0);
+          Hs[jj][ll] = mk<T>((T)w.x, (T)w.y);
+        }
       } else {
-        Ps[jj][ll][0] = ok ? (T)Psi[(long)j * L + l] : T(0);
-        Hs[jj][ll][0] = ok ? (T)HPsi[(long)j * L + l] : T(0);
+        if constexpr (PART != 1) Ps[jj][ll] = ok ? (T)Psi[(long)j * L + l] : T(0);
+        if constexpr (PART != 0) Hs[jj][ll] = ok ? (T)HPsi[(long)j * L + l] : T(0);
       }
     }
     for (int t = threadIdx.x; t < TJ * TS; t += 256) {
       const int jj = t / TS, ss = t % TS;
       const int j = jb + jj, s = s0 + ss;
       const double2 v = (j < n && s < k) ? Cm[(long)j * k + s] : make_double2(0, 0);
-      Cs[jj][ss][0] = (T)v.x;
-      Cs[jj][ss][1] = (T)v.y;
+      Cs[jj][ss] = mk<T>((T)v.x, (T)v.y);
     }
     __syncthreads();
 #pragma unroll
@@ -371,16 +401,27 @@ __global__ void __launch_bounds__(256) k_rotate(const double *__restrict__ Psi, 
 #pragma unroll
       for (int a = 0; a < 4; a++) {
         const int ll = tl + 32 * a;
-        const T xr = Ps[jj][ll][0], xi = CPLX ? Ps[jj][ll][CPLX ? 1 : 0] : T(0);
-        const T yr = Hs[jj][ll][0], yi = CPLX ? Hs[jj][ll][CPLX ? 1 : 0] : T(0);
+        T xr = T(0), xi = T(0), yr = T(0), yi = T(0);
+        if constexpr (CPLX) {
+          if constexpr (PART != 1) { const C<T> x = Ps[jj][ll]; xr = x.x; xi = x.y; }
+          if constexpr (PART != 0) { const C<T> y = Hs[jj][ll]; yr = y.x; yi = y.y; }
+        } else {
+          if constexpr (PART != 1) xr = Ps[jj][ll];
+          if constexpr (PART != 0) yr = Hs[jj][ll];
+        }
 #pragma unroll
         for (int b = 0; b < 4; b++) {
           const int ss = ts + 8 * b;
-          const T cr = Cs[jj][ss][0], ci = Cs[jj][ss][1];
-          pr[a][b] += xr * cr - xi * ci;
-          pim[a][b] += xr * ci + xi * cr;
-          qr[a][b] += yr * cr - yi * ci;
-          qim[a][b] += yr * ci + yi * cr;
+          const C<T> cv = Cs[jj][ss];
+          const T cr = cv.x, ci = cv.y;
+          if constexpr (PART != 1) {
+            pr[a][b] += xr * cr - xi * ci;
+            pim[a][b] += xr * ci + xi * cr;
+          }
+          if constexpr (PART != 0) {
+            qr[a][b] += yr * cr - yi * ci;
+            qim[a][b] += yr * ci + yi * cr;
+          }
         }
       }
     }
@@ -397,14 +438,22 @@ __global__ void __launch_bounds__(256) k_rotate(const double *__restrict__ Psi, 
       for (int a = 0; a < 4; a++) {
         const long l = l0 + tl + 32 * a;
         if (l < L) {
-          const double Pr = pr[a][b], Pi = CPLX ? (double)pim[a][b] : 0.0;
-          const double Qr = qr[a][b], Qi = CPLX ? (double)qim[a][b] : 0.0;
-          if (CPLX) {
-            out[((long)s * L + l) * 2] = Pr;
-            out[((long)s * L + l) * 2 + 1] = Pi;
+          double Pr, Pi;
+          if constexpr (PART != 1) {
+            Pr = pr[a][b];
+            Pi = CPLX ? (double)pim[a][b] : 0.0;
+            if (CPLX) {
+              out[((long)s * L + l) * 2] = Pr;
+              out[((long)s * L + l) * 2 + 1] = Pi;
+            } else {
+              out[(long)s * L + l] = Pr;
+            }
+            if constexpr (PART == 0) continue;
           } else {
-            out[(long)s * L + l] = Pr;
+            Pr = CPLX ? out[((long)s * L + l) * 2] : out[(long)s * L + l];
+            Pi = CPLX ? out[((long)s * L + l) * 2 + 1] : 0.0;
           }
+          const double Qr = qr[a][b], Qi = CPLX ? (double)qim[a][b] : 0.0;
           const double dr = Qr - e * Pr, di = Qi - e * Pi;
           rr += dr * dr + di * di;
           pp += Pr * Pr + Pi * Pi;
@@ -424,7 +473,7 @@ __global__ void __launch_bounds__(256) k_rotate(const double *__restrict__ Psi, 
     }
   }
   __syncthreads();
-  if (threadIdx.x < TS) {
+  if (PART != 0 && threadIdx.x < TS) {
     const int s = s0 + threadIdx.x;
     if (s < k) {
       double *P = part + ((long)blockIdx.x * k + s) * 3;
@@ -495,7 +544,8 @@ template <typename T>
 static int gram_t(fbse_ctx *c, const double *A, const double *B, int n, long L, double2 *out, double scale,
                   double2 *part, int nchunk, long kchunk)
 {
-  dim3 g((n + 63) / 64, (n + 63) / 64, nchunk);
+  const int nt = (n + 63) / 64;
+  dim3 g(nt * (nt + 1) / 2, 1, nchunk);
   if (c->is_complex) k_gram<T, true><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
   else k_gram<T, false><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
   FBSE_CHECK_LAUNCH(c);
@@ -601,8 +651,19 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     // 6. C = X U  (n x k); rotate Psi and HPsi with the residual epilogue
     if ((rc = zgemm_dev(c, n, k, k, X, k, false, Tm, k, false, Cm, k))) break;
     dim3 gr(nrb, (k + 31) / 32);
-    if (c->is_complex) k_rotate<T, true><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
-    else k_rotate<T, false><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+    if constexpr (sizeof(T) == 4) {  // FP32: two half-register launches (Psi, then H Psi + residuals)
+      if (c->is_complex) {
+        k_rotate<T, true, 0><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+        k_rotate<T, true, 1><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+      } else {
+        k_rotate<T, false, 0><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+        k_rotate<T, false, 1><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+      }
+      FBSE_COUNT(1);
+    } else {
+      if (c->is_complex) k_rotate<T, true, 2><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+      else k_rotate<T, false, 2><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
+    }
     FBSE_CHECK_LAUNCH(c);
     FBSE_COUNT(1); k_sum_rot<<<(k + 127) / 128, 128, 0, c->stream>>>(rpart, nrb, k, rsum);
     std::vector<double> hs(3 * k);

@@ -26,6 +26,8 @@ typedef struct {
   /* restart / state files (read.c:34-35, 87-93, 762-787, 954-967) */
   int print_psi_filt, print_psi_diag, calc_filter_only, restart_from_ortho, restart_from_sigma;
   long n_states_for_ortho, n_states_for_sigma;
+  int print_cubes; /* printCubes = 1 <ncubes> (read.c:691-715) */
+  long ncubes;
 } fbse_filter_params;
 
 /* the subset of bse_cplx/input.par (bse_cplx/read.c) */
@@ -75,5 +77,11 @@ int fbse_build_nlc(long nx, long ny, long nz, const double *gx, const double *gy
 /* outputs (filter_mpi/write.c:263-299, save.c:446-503) */
 int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n);
 int fbse_write_psi(const char *path, const double *psi, long n_doubles);
+
+/* write_cube_file (filter_mpi/write.c:65-139): rho [ngrid] in grid order,
+ * atoms as 8-byte symbol slots (sym8) and xyz (bohr); returns 0 or -1 (an
+ * atom symbol the reference's cube table does not know) */
+int fbse_write_cube(const char *path, const double *rho, long nx, long ny, long nz, double dx, double dy, double dz,
+                    double xmin, double ymin, double zmin, long natoms, const char *sym8, const double *xyz);
 
 #endif

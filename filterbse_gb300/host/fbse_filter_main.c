@@ -12,6 +12,8 @@
  * reads psi-filt.dat and starts at the orthogonalisation, "restartFromSigma
  * = 1 <n>" reads psi-diag.dat and only computes energies and sigma_E
  * (main.c:128-305, read.c:954-967); calcFilterOnly stops after the filter.
+ * conf.dat and, with "printCubes = 1 <n>", the homo-i / lumo+i cube files of
+ * mod_optional_output.
  * Errors go to stderr and the process exits with EXIT_FAILURE, like the
  * reference.  One non-reference key: "mixedPrecision = 1" selects the FP32
  * recursion (default: the plain FP64 method). */
@@ -84,6 +86,51 @@ static void save_output(const char *path, const fbse_filter_params *p, long nato
   fclose(f);
 }
 
+/* print_eigstate_densities (mod_optional_output.c:74-240): homo is the last
+ * converged state below fermiEnergy, lumo the next converged one; the cubes of
+ * homo-i and lumo+i (i < ncubes) hold |psi|^2 signed by the dominant component
+ * (density_phase_sign, write.c:52-60), per spin block.  The states are the
+ * ones written to psi.dat, in eval.dat's order. */
+static void write_cubes(const fbse_filter_params *p, const double *psi, const double *eval, const double *sigma,
+                        long n, long nx, long ny, long nz, double xmin, double ymin, double zmin, int nspin, int cplx,
+                        long natoms, const double *xyz, const int *atype, char names[][8])
+{
+  long homo = 0, lumo = 0;
+  for (long i = 0; i < n; i++)
+    if (eval[i] < p->fermi_e && sigma[i] < p->sigma_e_cut) homo = i;
+  for (long i = homo + 1; i < n; i++)
+    if (sigma[i] < p->sigma_e_cut) { lumo = i; break; }
+  printf("homo_idx = %ld; lumo_idx = %ld\n", homo, lumo);
+  if (homo == 0 || lumo == 0) {
+    printf("Did not converge enough electron or hole states to visualize cube files.\n");
+    return;
+  }
+  const long ngrid = nx * ny * nz, stlen = (long)(cplx + 1) * nspin * ngrid;
+  const long total_homo = homo, total_lumo = n - homo;
+  double *rho = malloc(ngrid * sizeof(double));
+  char *sym8 = calloc((size_t)natoms * 8, 1);
+  if (!rho || !sym8) die("host allocation", NULL);
+  for (long a = 0; a < natoms; a++) memcpy(sym8 + 8 * a, names[atype[a]], 7);
+  for (int side = 0; side < 2; side++)
+    for (long i = 0; i < (side ? total_lumo : total_homo) && i < p->ncubes; i++) {
+      const long st = side ? lumo + i : homo - i;
+      for (int s = 0; s < nspin; s++) {
+        const double *q = psi + st * stlen + (long)(cplx + 1) * s * ngrid;
+        for (long g = 0; g < ngrid; g++) {
+          const double re = q[(cplx + 1) * g], im = cplx ? q[2 * g + 1] : 0.0;
+          const double dom = fabs(re) >= fabs(im) ? re : im;
+          rho[g] = (re * re + im * im) * (dom > 0.0 ? 1.0 : (dom < 0.0 ? -1.0 : 0.0));
+        }
+        char path[64];
+        snprintf(path, sizeof path, side ? "lumo+%ld-%s.cube" : "homo-%ld-%s.cube", i, s ? "Dn" : "Up");
+        if (fbse_write_cube(path, rho, nx, ny, nz, p->dx, p->dy, p->dz, xmin, ymin, zmin, natoms, sym8, xyz))
+          die("cannot write cube file (unknown atom symbol?)", path);
+      }
+    }
+  free(rho);
+  free(sym8);
+}
+
 /* n states of stlen doubles from a raw state file (psi-filt.dat, psi-diag.dat) */
 static double *read_states(const char *path, long n, long stlen)
 {
@@ -114,6 +161,13 @@ int main(void)
   char names[FBSE_MAX_TYPES][8];
   if (fbse_read_conf("conf.par", &natoms, &xyz, &atype, names, &ntypes, err, sizeof err)) die(err, NULL);
   const int nspin = p.use_spinors ? 2 : 1, cplx = p.use_spinors ? 1 : 0;
+  /* conf.dat: the centred configuration the run uses (read.c:1150-1157) */
+  FILE *fc = fopen("conf.dat", "w");
+  if (!fc) die("cannot write", "conf.dat");
+  fprintf(fc, "%ld\n", natoms);
+  for (long a = 0; a < natoms; a++)
+    fprintf(fc, "%3s % .16g % .16g % .16g\n", names[atype[a]], xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]);
+  fclose(fc);
   printf("fbse_filter: %ld atoms, %d types, nspin %d, SO %d, NL %d, %s\n", natoms, ntypes, nspin, p.so, p.nl,
          p.precision ? "mixed precision" : "FP64");
 
@@ -411,6 +465,8 @@ int main(void)
   save_output("output.dat", &p, natoms, xyz, ntypes, nx, ny, nz, p.dx, p.dy, p.dz, gx, gy, gz, xmin, ymin, zmin,
               nspin, cplx, n_out, eval, sigma, psi);
   check(ctx, fbse_free(ctx, d_psi), "free");
+  if (p.print_cubes == 1)
+    write_cubes(&p, psi, eval, sigma, n_out, nx, ny, nz, xmin, ymin, zmin, nspin, cplx, natoms, xyz, atype, names);
   fbse_destroy(ctx);
   return 0;
 }

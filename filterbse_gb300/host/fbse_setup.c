@@ -39,7 +39,7 @@ static int parse_double(const char *s, double *v)
  * not restart; the file-level restarts (restartFromOrtho from psi-filt.dat,
  * restartFromSigma from psi-diag.dat) are implemented instead. */
 static const char *k_ignored[] = {"nThreads", "hamThreads", "nestedOMP", "useFastHam", "useMPIOMP", "MPIOrtho",
-                                  "MPIDiag", "parallelSigma", "timeHamiltonian", "printNorm", "printCubes",
+                                  "MPIDiag", "parallelSigma", "timeHamiltonian", "printNorm",
                                   "printGaussCubes", "saveCheckpoints", "printPsiOrtho",
                                   "fftWisdomDir", "saveOutput", "calcPotOverlap",
                                   "calcSpinAngStat", "retryFilter", "centerConf", "noTimeRev", "psiZeroCut",
@@ -126,12 +126,12 @@ int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, 
         fclose(f);
         return -1;
       }
+    } else if (!strcmp(key, "printCubes")) {
+      /* "printCubes = 1 <states per side>" (read.c:691-715) */
+      rc = parse_long(val, &lv);
+      p->print_cubes = (int)lv;
+      if (!rc && lv == 1 && (fscanf(f, "%ld", &p->ncubes) != 1 || p->ncubes < 0)) rc = -1;
     } else if (in_list(key, k_ignored)) {
-      /* printCubes takes a second value in the reference's examples */
-      if (!strcmp(key, "printCubes") && parse_long(val, &lv) == 0 && lv == 1) {
-        long dummy;
-        if (fscanf(f, "%ld", &dummy) != 1) rc = -1;
-      }
     } else {
       seterr(err, errlen, "unknown input.par key", key);
       fclose(f);
@@ -611,6 +611,53 @@ int fbse_write_eval(const char *path, const double *eval, const double *sigma, l
   FILE *f = fopen(path, "w");
   if (!f) return -1;
   for (long i = 0; i < n; i++) fprintf(f, "%ld %.16g %g\n", i, eval[i], sigma[i]); /* write.c:279 */
+  fclose(f);
+  return 0;
+}
+
+/* atomic numbers of the cube files: cube_atom_number's ligand entries
+ * (filter_mpi/write.c:7-50), then the element list of assign_atom_number
+ * (read.c:2452-2545) */
+static long cube_z(const char *s)
+{
+  static const struct { const char *sym; long z; } tab[] = {
+      {"C1", 2},  {"C2", 3},  {"C3", 4},   {"P1", 84},  {"P2", 85},  {"P3", 86},  {"PC5", 87}, {"PC6", 88},
+      {"PA1", 3}, {"PA2", 4}, {"I0", 53},  {"I1", 53},  {"Br0", 35}, {"Br1", 35}, {"PA3", 1},  {"PR1", 1},
+      {"PR2", 1}, {"PR3", 1}, {"H", 1},    {"C", 6},    {"Si", 14},  {"P", 15},   {"S", 16},   {"Cl", 17},
+      {"Zn", 30}, {"Ga", 31}, {"As", 33},  {"Se", 34},  {"Br", 35},  {"Cd", 48},  {"In", 49},  {"Te", 52},
+      {"I", 53},  {"Cs", 55}, {"Pb", 82},  {NULL, 0}};
+  for (int i = 0; tab[i].sym; i++)
+    if (!strcmp(s, tab[i].sym)) return tab[i].z;
+  return -1;
+}
+
+int fbse_write_cube(const char *path, const double *rho, long nx, long ny, long nz, double dx, double dy, double dz,
+                    double xmin, double ymin, double zmin, long natoms, const char *sym8, const double *xyz)
+{ /* write_cube_file (filter_mpi/write.c:65-139): x outer, z inner, 6 per line */
+  FILE *f = fopen(path, "w");
+  if (!f) return -1;
+  fprintf(f, "CUBE FILE\n");
+  fprintf(f, "OUTER LOOP: X, MIDDLE LOOP: Y, INNER LOOP: Z\n");
+  fprintf(f, "%5li%12.6f%12.6f%12.6f\n", natoms, xmin, ymin, zmin);
+  fprintf(f, "%5li%12.6f%12.6f%12.6f\n", nx, dx, 0.0, 0.0);
+  fprintf(f, "%5li%12.6f%12.6f%12.6f\n", ny, 0.0, dy, 0.0);
+  fprintf(f, "%5li%12.6f%12.6f%12.6f\n", nz, 0.0, 0.0, dz);
+  for (long a = 0; a < natoms; a++) {
+    char s[8];
+    memcpy(s, sym8 + 8 * a, 7);
+    s[7] = '\0';
+    const long z = cube_z(s);
+    if (z < 0) { fclose(f); return -1; }
+    fprintf(f, "%5li%12.6f%12.6f%12.6f%12.6f\n", z, 0.0, xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]);
+  }
+  for (long ix = 0; ix < nx; ix++)
+    for (long iy = 0; iy < ny; iy++) {
+      for (long iz = 0; iz < nz; iz++) {
+        fprintf(f, "%.5g ", rho[nx * (ny * iz + iy) + ix]);
+        if (iz % 6 == 5) fputc('\n', f);
+      }
+      fputc('\n', f);
+    }
   fclose(f);
   return 0;
 }

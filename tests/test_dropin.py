@@ -32,7 +32,7 @@ class FilterParams(ctypes.Structure):
                 ("print_psi_filt", ctypes.c_int), ("print_psi_diag", ctypes.c_int),
                 ("calc_filter_only", ctypes.c_int), ("restart_from_ortho", ctypes.c_int),
                 ("restart_from_sigma", ctypes.c_int), ("n_states_for_ortho", ctypes.c_long),
-                ("n_states_for_sigma", ctypes.c_long)]
+                ("n_states_for_sigma", ctypes.c_long), ("print_cubes", ctypes.c_int), ("ncubes", ctypes.c_long)]
 
 
 @pytest.fixture(scope="module")
@@ -166,6 +166,45 @@ def test_projector_table_matches_oracle(lib):
     assert np.array_equal(np.ctypeslib.as_array(y1, (n * 6,)), ref.y1)
     assert np.allclose(np.ctypeslib.as_array(sp, (n * 5,)), ref.proj, rtol=1e-14, atol=1e-14)
     assert np.allclose(np.ctypeslib.as_array(np_, (n * 5,)), ref.nlp, rtol=1e-14, atol=1e-14)
+
+
+def _cube_text(rho, n, d, lo, atoms):
+    """write_cube_file's layout (filter_mpi/write.c:65-139), restated."""
+    nx, ny, nz = n
+    out = ["CUBE FILE", "OUTER LOOP: X, MIDDLE LOOP: Y, INNER LOOP: Z",
+           "%5li%12.6f%12.6f%12.6f" % (len(atoms), *lo), "%5li%12.6f%12.6f%12.6f" % (nx, d[0], 0.0, 0.0),
+           "%5li%12.6f%12.6f%12.6f" % (ny, 0.0, d[1], 0.0), "%5li%12.6f%12.6f%12.6f" % (nz, 0.0, 0.0, d[2])]
+    out += ["%5li%12.6f%12.6f%12.6f%12.6f" % (z, 0.0, *xyz) for z, xyz in atoms]
+    body = []
+    r = rho.reshape(nz, ny, nx)
+    for ix in range(nx):
+        for iy in range(ny):
+            line = ""
+            for iz in range(nz):
+                line += "%.5g " % r[iz, iy, ix]
+                if iz % 6 == 5:
+                    line += "\n"
+            body.append(line + "\n")
+    return "\n".join(out) + "\n" + "".join(body)
+
+
+def test_cube_file_matches_reference_layout(lib, tmp_path):
+    lib.fbse_write_cube.argtypes = ([ctypes.c_char_p, D] + [ctypes.c_long] * 3 + [ctypes.c_double] * 6 +
+                                    [ctypes.c_long, ctypes.c_char_p, D])
+    rng = np.random.default_rng(3)
+    n, d, lo = (5, 4, 13), (0.5, 0.6, 0.7), (-1.25, -1.2, -4.55)
+    rho = rng.normal(size=n[0] * n[1] * n[2]) * 1e-3
+    syms = ["Cd", "Se", "P1", "I", "Cs"]
+    xyz = rng.uniform(-2, 2, (5, 3))
+    sym8 = b"".join(s.encode().ljust(8, b"\0") for s in syms)
+    path = tmp_path / "x.cube"
+    assert lib.fbse_write_cube(str(path).encode(), rho.ctypes.data_as(D), *n, *d, *lo, 5, sym8,
+                               np.ascontiguousarray(xyz).ctypes.data_as(D)) == 0
+    want = _cube_text(rho, n, d, lo, list(zip([48, 34, 84, 53, 55], xyz)))
+    assert path.read_text() == want
+    # an atom the reference's table does not know is an error
+    assert lib.fbse_write_cube(str(path).encode(), rho.ctypes.data_as(D), *n, *d, *lo, 1, b"Xx\0\0\0\0\0\0",
+                               np.ascontiguousarray(xyz).ctypes.data_as(D)) != 0
 
 
 def test_executables_fail_loudly_without_gpu(tmp_path):

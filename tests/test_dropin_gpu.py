@@ -49,6 +49,16 @@ def test_dropin_filter_matches_reference_eval(cuda, tmp_path):
     # psi.dat holds the states of eval.dat, stlen doubles each (2 x 2 x 44^3)
     assert os.path.getsize(tmp_path / "psi.dat") == len(ev) * 2 * 2 * 44 ** 3 * 8
     assert (tmp_path / "output.dat").exists()
+    # conf.dat and the cube files of "printCubes = 1 3" (mod_optional_output):
+    # the signed densities of both spin blocks integrate to 1
+    assert int(open(tmp_path / "conf.dat").readline()) == 15
+    for name in ("homo-0", "homo-2", "lumo+0", "lumo+2"):
+        lines = open(tmp_path / f"{name}-Up.cube").read().split("\n")
+        assert lines[0] == "CUBE FILE" and int(lines[2].split()[0]) == 15
+        up = np.array(" ".join(lines[6 + 15:]).split(), float)
+        dn = np.array(" ".join(open(tmp_path / f"{name}-Dn.cube").read().split("\n")[6 + 15:]).split(), float)
+        assert up.size == dn.size == 44 ** 3
+        assert abs((np.abs(up).sum() + np.abs(dn).sum()) * 0.125 - 1.0) < 1e-3
 
 
 def test_dropin_bse_matches_reference_exciton(cuda, tmp_path):
