@@ -106,7 +106,9 @@ int unpack_states(fbse_ctx *c, const void *src, double *dst, long ndst)
 // ---------------------------------------------------------------------------
 constexpr int kMaxRing = 128;
 
-template <typename T, int M>
+// ring slots unrolled by 16: more slot loads in flight per thread (2.98 ->
+// 2.94 s for the 16 x 16 x 2048 spinor filter at 128^3 against 4)
+template <typename T, int M, int U = 16>
 __global__ void __launch_bounds__(256) k_newton_acc(const C<T> *__restrict__ ring, long j0, int nk,
                                                    const double *__restrict__ a, long ncheby, int m,
                                                    double *__restrict__ F, long nstart, long nw, long len, int cplx,
@@ -124,7 +126,7 @@ __global__ void __launch_bounds__(256) k_newton_acc(const C<T> *__restrict__ rin
 #pragma unroll
     for (int t = 0; t < M; t++) { ar[t] = T(0); ai[t] = T(0); }
     // j0 is a multiple of the ring length: term j0 + q sits in slot q
-#pragma unroll 4
+#pragma unroll U
     for (int q = 0; q < nk; q++) {
       const C<T> v = ring[(long)q * slot_stride + i];
       const T *cq = as + q * M;
