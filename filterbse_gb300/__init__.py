@@ -29,6 +29,7 @@ EXPORTED = [
     "fbse_ortho_diag_sigma", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
     "fbse_init_filter_states", "fbse_launch_count", "fbse_filter_job", "fbse_build_local_pot",
     "fbse_bse_potentials", "fbse_bse_kernel", "fbse_bse_kernel_real", "fbse_bse_solve", "fbse_bse_dipoles", "fbse_bse_mag_dipoles",
+    "fbse_bse_qp_ang_mom",
     "fbse_bse_optical",
     "fbse_normalize_all_noalloc",
 ]
@@ -106,6 +107,8 @@ def load() -> ctypes.CDLL:
     L.fbse_bse_dipoles.argtypes = [_VP, _VP, _D, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D]
     L.fbse_bse_kernel_real.argtypes = [_VP, _VP, ctypes.c_long, ctypes.c_long, ctypes.c_long, _VP, _VP, _VP, _VP]
     L.fbse_bse_mag_dipoles.argtypes = [_VP, _VP, _D, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D]
+    L.fbse_bse_qp_ang_mom.argtypes = [_VP, _VP, _D, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D, _D, _D,
+                                      _D]
     L.fbse_bse_optical.argtypes = [_VP, _VP, _D, ctypes.c_long, ctypes.c_long, _D]
     _lib = L
     return L
@@ -399,6 +402,21 @@ class Context:
         self._chk(self._L.fbse_bse_mag_dipoles(self._h, self._ptr(psi_qp), _dp(gx), _dp(gy), _dp(gz), n_h, n_e,
                                                lumo_idx, _dp(m.view(np.float64))))
         return m.reshape(-1, 3)
+
+    def bse_qp_ang_mom(self, psi_qp, gx, gy, gz, n_h, n_e, lumo_idx):
+        """calc_qp_spin_mtrx + calc_qp_ang_mom_mtrx: (s [n,3], l [n,3], l2 [n],
+        ls [n]) complex128 with n = n_h^2 + n_e^2 (holes first)."""
+        gx, gy, gz = (np.ascontiguousarray(a, np.float64) for a in (gx, gy, gz))
+        n = n_h * n_h + n_e * n_e
+        s = np.empty(n * 3, np.complex128)
+        l = np.empty(n * 3, np.complex128)
+        l2 = np.empty(n, np.complex128)
+        ls = np.empty(n, np.complex128)
+        self._torch_sync()
+        self._chk(self._L.fbse_bse_qp_ang_mom(self._h, self._ptr(psi_qp), _dp(gx), _dp(gy), _dp(gz), n_h, n_e,
+                                              lumo_idx, _dp(s.view(np.float64)), _dp(l.view(np.float64)),
+                                              _dp(l2.view(np.float64)), _dp(ls.view(np.float64))))
+        return s.reshape(-1, 3), l.reshape(-1, 3), l2, ls
 
     def bse_optical(self, coeff, mu_pairs, n_h, n_e):
         """calc_optical_exc (electric part): exciton dipoles [n_xton, 3] complex128

@@ -12,7 +12,7 @@ ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfbse_gpu.so")
 CU_SOURCES = ["fft.cu", "hpsi.cu", "filter.cu", "linalg.cu", "bse.cu", "tcgemm.cu", "setup.cu", "job.cu", "api.cu"]
-C_SOURCES = ["host/fbse_host.c", "host/fbse_setup.c"]
+C_SOURCES = ["host/fbse_host.c", "host/fbse_setup.c", "host/fbse_bse_stats.c"]
 EXECUTABLES = {"fbse_filter": "host/fbse_filter_main.c", "fbse_bse": "host/fbse_bse_main.c"}
 BIN = os.path.join(HERE, "bin")
 NVCC = os.environ.get("NVCC", "nvcc")

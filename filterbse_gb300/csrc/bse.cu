@@ -511,6 +511,99 @@ __global__ void k_real_part(const double2 *__restrict__ src, double *__restrict_
     dst[e] = scale * src[e].x;
 }
 
+// ---------------------------------------------------------------------------
+// quasiparticle spin and angular-momentum matrices (calc_qp_spin_mtrx,
+// calc_qp_ang_mom_mtrx, bse_cplx/angular.c:7-690) for spinor states.
+// l_operator's L'psi = -(r x p psi) (ang_mom_operators.c:6-52) per spin block:
+// k_cross forms component d (or all three) of L' from P = (p_x, p_y, p_z) psi.
+// ---------------------------------------------------------------------------
+__global__ void k_cross(const double2 *__restrict__ P, long nsg, long ngrid, int nx, int ny,
+                        const double *__restrict__ gx, const double *__restrict__ gy, const double *__restrict__ gz,
+                        int only, double2 *__restrict__ out, int accumulate)
+{
+  // out[d][q] (d = 0..2, or only component `only` into out[0] when only >= 0)
+  const double2 *Px = P, *Py = P + nsg, *Pz = P + 2 * nsg;
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nsg; q += (long)gridDim.x * blockDim.x) {
+    const long g = q % ngrid;
+    const double x = gx[g % nx], y = gy[(g / nx) % ny], z = gz[g / ((long)nx * ny)];
+    const double2 px = Px[q], py = Py[q], pz = Pz[q];
+    const double2 l[3] = {make_double2(-(y * pz.x - z * py.x), -(y * pz.y - z * py.y)),
+                          make_double2(-(z * px.x - x * pz.x), -(z * px.y - x * pz.y)),
+                          make_double2(-(x * py.x - y * px.x), -(x * py.y - y * px.y))};
+    if (only < 0) {
+      out[q] = l[0];
+      out[nsg + q] = l[1];
+      out[2 * nsg + q] = l[2];
+    } else {
+      const double2 v = l[only];
+      out[q] = accumulate ? make_double2(out[q].x + v.x, out[q].y + v.y) : v;
+    }
+  }
+}
+
+// for the state i whose L'_d psi_i (Lp[3]) and sum_d L'_d L'_d psi_i (L2) are
+// given, and every partner j of its block (CTA j, ncols partners from j0):
+//   r[0..2] = sum conj(psi_j) L'_d psi_i, r[3] = sum conj(psi_j) L2,
+//   r[4]    = sum [conj(psi_j,dn) L'x_up + conj(psi_j,up) L'x_dn
+//                  + i conj(psi_j,dn) L'y_up - i conj(psi_j,up) L'y_dn
+//                  + conj(psi_j,up) L'z_up - conj(psi_j,dn) L'z_dn]     (the L.S sum)
+//   r[5..7] = the sx, sy, sz sums of calc_qp_spin_mtrx on psi_j, psi_i
+// (complex, unscaled) into out[(j - j0) * 8 + k]
+__global__ void k_ang_dots(const double2 *__restrict__ psi, long nsg, long ngrid, long i, long j0,
+                           const double2 *__restrict__ Lp, const double2 *__restrict__ L2,
+                           double2 *__restrict__ out)
+{
+  const long j = j0 + blockIdx.x;
+  const double2 *pj = psi + j * nsg, *pi = psi + i * nsg;
+  double s[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) s[k] = 0.0;
+  auto acc = [&](int k, double2 a, double2 b, double sr, double si) {
+    // s[k] += (sr + i si) conj(a) b
+    const double tr = a.x * b.x + a.y * b.y, ti = a.x * b.y - a.y * b.x;
+    s[2 * k] += sr * tr - si * ti;
+    s[2 * k + 1] += sr * ti + si * tr;
+  };
+  for (long g = threadIdx.x; g < ngrid; g += blockDim.x) {
+    const double2 ju = pj[g], jd = pj[ngrid + g], iu = pi[g], id = pi[ngrid + g];
+    for (int sp = 0; sp < 2; sp++) {
+      const double2 jv = sp ? jd : ju;
+      const long q = sp * ngrid + g;
+      acc(0, jv, Lp[q], 1, 0);
+      acc(1, jv, Lp[nsg + q], 1, 0);
+      acc(2, jv, Lp[2 * nsg + q], 1, 0);
+      acc(3, jv, L2[q], 1, 0);
+    }
+    acc(4, jd, Lp[g], 1, 0);
+    acc(4, ju, Lp[ngrid + g], 1, 0);
+    acc(4, jd, Lp[nsg + g], 0, 1);
+    acc(4, ju, Lp[nsg + ngrid + g], 0, -1);
+    acc(4, ju, Lp[2 * nsg + g], 1, 0);
+    acc(4, jd, Lp[2 * nsg + ngrid + g], -1, 0);
+    acc(5, jd, iu, 1, 0);
+    acc(5, ju, id, 1, 0);
+    acc(6, jd, iu, 0, 1);
+    acc(6, ju, id, 0, -1);
+    acc(7, ju, iu, 1, 0);
+    acc(7, jd, id, -1, 0);
+  }
+  __shared__ double red[32][16];
+  for (int k = 0; k < 16; k++) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 16) {
+    double v = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[w][threadIdx.x];
+    red[0][threadIdx.x] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 8)
+    out[(long)blockIdx.x * 8 + threadIdx.x] = make_double2(red[0][2 * threadIdx.x], red[0][2 * threadIdx.x + 1]);
+}
+
 // init_kvec (ang_mom_operators.c:90-103): k[j] = j dk norm, k[n-j] = -j dk norm
 // for j = 1..n/2 in that order (for even n the second write leaves k[n/2] < 0)
 static void init_kvec(std::vector<double> &k, long n, double dk, double norm)
@@ -795,6 +888,115 @@ int fbse_bse_mag_dipoles(fbse_ctx *c, const double *psi_qp, const double *gx, co
   } while (0);
   cudaStreamSynchronize(c->stream);
   void *bufs[] = {dk3, P, work, m, dg};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  return rc;
+}
+
+int fbse_bse_qp_ang_mom(fbse_ctx *c, const double *psi_qp, const double *gx, const double *gy, const double *gz,
+                        long n_h, long n_e, long lumo_idx, double *s_mom, double *l_mom, double *l2_mom,
+                        double *ldots)
+{
+  if (!c || !psi_qp || !gx || !gy || !gz || !s_mom || !l_mom || !l2_mom || !ldots || n_h < 1 || n_e < 1 ||
+      lumo_idx < n_h)
+    return c ? set_err(c, FBSE_ERR_ARG, "fbse_bse_qp_ang_mom: bad arguments") : FBSE_ERR_ARG;
+  if (!c->is_complex || c->nspin != 2)
+    return set_err(c, FBSE_ERR_UNSUPPORTED, "fbse_bse_qp_ang_mom: complex spinor states required");
+  const long N = c->ngrid, nsg = 2 * N;
+  std::vector<double> kx, ky, kz;
+  const double norm = 1.0 / (double)N;
+  auto dk = [](long n, double d) { return 2.0 * M_PI / (n * d); };  // bse_cplx/read.c:347-349
+  init_kvec(kx, c->nx, dk(c->nx, c->dx), norm);
+  init_kvec(ky, c->ny, dk(c->ny, c->dy), norm);
+  init_kvec(kz, c->nz, dk(c->nz, c->dz), norm);
+  std::vector<double2> kq((size_t)3 * N);
+  for (long g = 0; g < N; g++) {
+    kq[g] = make_double2(kx[g % c->nx], 0.0);
+    kq[N + g] = make_double2(ky[(g / c->nx) % c->ny], 0.0);
+    kq[2 * N + g] = make_double2(kz[g / (c->nx * c->ny)], 0.0);
+  }
+  const long nmax = n_h > n_e ? n_h : n_e;
+  double2 *dk3 = nullptr, *P = nullptr, *Lp = nullptr, *L2 = nullptr, *work = nullptr, *dots = nullptr;
+  double *dg = nullptr;
+  int rc = FBSE_OK;
+  if (cudaMalloc(&dk3, 3 * N * sizeof(double2)) != cudaSuccess || cudaMalloc(&P, 3 * nsg * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&Lp, 3 * nsg * sizeof(double2)) != cudaSuccess || cudaMalloc(&L2, nsg * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&work, nsg * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&dots, nmax * 8 * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&dg, (c->nx + c->ny + c->nz) * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    rc = set_err(c, FBSE_ERR_OOM, "fbse_bse_qp_ang_mom");
+  }
+  const double dv = c->dv;
+  const unsigned gblk = (unsigned)std::min<long>((nsg + 255) / 256, 4096);
+  std::vector<double2> hd((size_t)nmax * 8);
+  double2 *S = reinterpret_cast<double2 *>(s_mom), *Lm = reinterpret_cast<double2 *>(l_mom);
+  double2 *L2m = reinterpret_cast<double2 *>(l2_mom), *LS = reinterpret_cast<double2 *>(ldots);
+  auto conjd = [](double2 v) { return make_double2(v.x, -v.y); };
+  auto sc = [](double2 v, double f) { return make_double2(f * v.x, f * v.y); };
+  do {
+    if (rc) break;
+    if (h2d(c->stream, dk3, kq.data(), 3 * N * sizeof(double2)) != cudaSuccess ||
+        h2d(c->stream, dg, gx, c->nx * sizeof(double)) != cudaSuccess ||
+        h2d(c->stream, dg + c->nx, gy, c->ny * sizeof(double)) != cudaSuccess ||
+        h2d(c->stream, dg + c->nx + c->ny, gz, c->nz * sizeof(double)) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "fbse_bse_qp_ang_mom upload");
+      break;
+    }
+    // blocks: holes (states 0..n_h-1, matrix offset 0), electrons (lumo_idx.., offset n_h^2)
+    for (int blk = 0; blk < 2 && !rc; blk++) {
+      const long n = blk ? n_e : n_h, s0 = blk ? lumo_idx : 0, off = blk ? n_h * n_h : 0;
+      for (long i = 0; i < n && !rc; i++) {
+        const double2 *pi = (const double2 *)psi_qp + (s0 + i) * nsg;
+        // L' psi_i (three components), then sum_d L'_d (L'_d psi_i)
+        for (int d = 0; d < 3 && !rc; d++) rc = conv_apply<double>(c, pi, P + d * nsg, work, 2, dk3 + d * N);
+        if (rc) break;
+        k_cross<<<gblk, 256, 0, c->stream>>>(P, nsg, N, (int)c->nx, (int)c->ny, dg, dg + c->nx, dg + c->nx + c->ny,
+                                             -1, Lp, 0);
+        FBSE_COUNT(1);
+        for (int d = 0; d < 3 && !rc; d++) {
+          for (int e = 0; e < 3 && !rc; e++) rc = conv_apply<double>(c, Lp + d * nsg, P + e * nsg, work, 2, dk3 + e * N);
+          if (rc) break;
+          k_cross<<<gblk, 256, 0, c->stream>>>(P, nsg, N, (int)c->nx, (int)c->ny, dg, dg + c->nx,
+                                               dg + c->nx + c->ny, d, L2, d > 0);
+          FBSE_COUNT(1);
+        }
+        if (rc) break;
+        // partners: all j for the spins, j >= i for the L quantities (the
+        // reference fills the rest by Hermitian conjugation)
+        k_ang_dots<<<(unsigned)n, 256, 0, c->stream>>>((const double2 *)psi_qp, nsg, N, s0 + i, s0, Lp, L2, dots);
+        FBSE_COUNT(1);
+        if (cudaGetLastError() != cudaSuccess || d2h(c->stream, hd.data(), dots, n * 8 * sizeof(double2)) != cudaSuccess) {
+          rc = set_err(c, FBSE_ERR_CUDA, "fbse_bse_qp_ang_mom");
+          break;
+        }
+        for (long j = 0; j < n; j++) {
+          const double2 *r = hd.data() + j * 8;
+          // spins (angular.c:89-103 holes: -1/2 conj(s) dv; :172-183 electrons: 1/2 s dv), all pairs
+          for (int d = 0; d < 3; d++)
+            S[(off + i * n + j) * 3 + d] = blk ? sc(r[5 + d], 0.5 * dv) : sc(conjd(r[5 + d]), -0.5 * dv);
+          if (j < i) continue;
+          // L' sums: holes accumulate -conj(psi_j) L' psi_i and store conj (angular.c:404-434),
+          // electrons store the sums as they are (:530-558)
+          double2 l[3], l2, ls;
+          for (int d = 0; d < 3; d++) l[d] = blk ? sc(r[d], dv) : sc(conjd(r[d]), -dv);
+          l2 = blk ? sc(r[3], dv) : sc(conjd(r[3]), dv);
+          ls = blk ? sc(r[4], 0.5 * dv) : sc(conjd(r[4]), 0.5 * dv);
+          const long ut = off + i * n + j, lt = off + j * n + i;
+          for (int d = 0; d < 3; d++) {
+            Lm[ut * 3 + d] = l[d];
+            Lm[lt * 3 + d] = conjd(l[d]);
+          }
+          L2m[ut] = l2;
+          L2m[lt] = conjd(l2);
+          LS[ut] = ls;
+          LS[lt] = conjd(ls);
+        }
+      }
+    }
+  } while (0);
+  cudaStreamSynchronize(c->stream);
+  void *bufs[] = {dk3, P, Lp, L2, work, dots, dg};
   for (void *b : bufs)
     if (b) cudaFree(b);
   return rc;

@@ -153,6 +153,85 @@ static void write_matrices(fbse_ctx *ctx, void *d_dir, void *d_exc, void *d_coef
   free(cm);
 }
 
+/* qp_spin_frac (bse_cplx/spin.c:3-60): the norm of each spin block of every
+ * quasiparticle spinor, qp_spins.dat */
+static void write_qp_spins(const double *psi, const double *eqp, long nqp, long ngrid, double dv)
+{
+  FILE *f = fopen("qp_spins.dat", "w");
+  if (!f) die("cannot write", "qp_spins.dat");
+  for (long i = 0; i < nqp; i++) {
+    fprintf(f, "\nStats on state%lu: (E=%lg)\n", (unsigned long)i, eqp[i]);
+    for (int s = 0; s < 2; s++) {
+      const double *q = psi + (i * 2 + s) * 2 * ngrid;
+      double pct = 0.0;
+      for (long g = 0; g < ngrid; g++) pct += q[2 * g] * q[2 * g] + q[2 * g + 1] * q[2 * g + 1];
+      fprintf(f, " Spin %d fraction: %f\n", s, pct * dv);
+    }
+  }
+  fclose(f);
+}
+
+/* calcSpinAngStat (bse_cplx/main.c:160-195): the quasiparticle spin and
+ * angular-momentum matrices (sx/sy/sz.dat, lx/ly/lz/lsqr/ls.dat,
+ * angular.c:116-129, 200-211, 436-460, 562-586) and the exciton statistics
+ * (spins.dat, orbital.dat, couple.dat, angular.c:789-791, 949-950, 1034) */
+static void write_ang_stats(fbse_ctx *ctx, void *d_psi, const double *gx, const double *gy, const double *gz,
+                            long nh, long ne, long lumo, const double *coeff)
+{
+  const long n = nh * nh + ne * ne, nx = nh * ne;
+  double *sm = malloc(n * 6 * sizeof(double)), *lm = malloc(n * 6 * sizeof(double));
+  double *l2 = malloc(n * 2 * sizeof(double)), *ls = malloc(n * 2 * sizeof(double));
+  double *sp = malloc(nx * 6 * sizeof(double)), *st = malloc(nx * 2 * sizeof(double));
+  double *orb = malloc(nx * 6 * sizeof(double)), *ot = malloc(nx * 2 * sizeof(double));
+  double *lst = malloc(nx * 2 * sizeof(double));
+  if (!sm || !lm || !l2 || !ls || !sp || !st || !orb || !ot || !lst) die("host allocation", NULL);
+  check(ctx, fbse_bse_qp_ang_mom(ctx, d_psi, gx, gy, gz, nh, ne, lumo, sm, lm, l2, ls), "angular momenta");
+  const char *sn[3] = {"sx.dat", "sy.dat", "sz.dat"}, *ln[3] = {"lx.dat", "ly.dat", "lz.dat"};
+  for (int d = 0; d < 3; d++) {
+    FILE *fs = fopen(sn[d], "w"), *fl = fopen(ln[d], "w");
+    if (!fs || !fl) die("cannot write", sn[d]);
+    for (int blk = 0; blk < 2; blk++) {
+      const long cnt = blk ? ne : nh, off = blk ? nh * nh : 0, base = blk ? lumo : 0;
+      for (long i = 0; i < cnt; i++)
+        for (long j = 0; j < cnt; j++) {
+          const long k = off + i * cnt + j;
+          fprintf(fs, "%ld %ld % .10g % .10g\n", base + i, base + j, sm[6 * k + 2 * d], sm[6 * k + 2 * d + 1]);
+          fprintf(fl, "%ld\t%ld\t%lf\t%lf\n", base + i, base + j, lm[6 * k + 2 * d], lm[6 * k + 2 * d + 1]);
+        }
+    }
+    fclose(fs);
+    fclose(fl);
+  }
+  FILE *fq = fopen("lsqr.dat", "w"), *fls = fopen("ls.dat", "w");
+  if (!fq || !fls) die("cannot write", "lsqr.dat / ls.dat");
+  for (int blk = 0; blk < 2; blk++) {
+    const long cnt = blk ? ne : nh, off = blk ? nh * nh : 0, base = blk ? lumo : 0;
+    for (long i = 0; i < cnt; i++)
+      for (long j = 0; j < cnt; j++) {
+        const long k = off + i * cnt + j;
+        fprintf(fq, "%ld\t%ld\t%lf\t%lf\n", base + i, base + j, l2[2 * k], l2[2 * k + 1]);
+        fprintf(fls, "%ld\t%ld\t%lf\t%lf\n", base + i, base + j, ls[2 * k], ls[2 * k + 1]);
+      }
+  }
+  fclose(fq);
+  fclose(fls);
+  if (fbse_xton_ang_stats(nh, ne, coeff, sm, lm, l2, ls, sp, st, orb, ot, lst)) die("host allocation", NULL);
+  FILE *fsp = fopen("spins.dat", "w"), *fo = fopen("orbital.dat", "w"), *fc = fopen("couple.dat", "w");
+  if (!fsp || !fo || !fc) die("cannot write", "spins.dat / orbital.dat / couple.dat");
+  for (long j = 0; j < nx; j++) {
+    fprintf(fsp, "%ld\t%-10.5lg\t%-10.5lg\t%-10.5lg\t%-10.5lg\t%-10.5lg\t%-10.5lg\t", j, sp[6 * j], sp[6 * j + 1],
+            sp[6 * j + 2], sp[6 * j + 3], sp[6 * j + 4], sp[6 * j + 5]);
+    fprintf(fsp, "%-10.5lg\t (%-10.5lg)\n", 1.5 + 2.0 * st[2 * j], 2.0 * st[2 * j + 1]);
+    fprintf(fo, "%ld\t%-10.5lf\t%-10.5lf\t%-10.5lf\t", j, orb[6 * j], orb[6 * j + 2], orb[6 * j + 4]);
+    fprintf(fo, "%-10.5lf\t (%-10.5lf)\n", ot[2 * j], ot[2 * j + 1]);
+    fprintf(fc, "%ld\t%-10.5lf\t (%-10.5lf)\n", j, lst[2 * j], lst[2 * j + 1]);
+  }
+  fclose(fsp);
+  fclose(fo);
+  fclose(fc);
+  free(sm); free(lm); free(l2); free(ls); free(sp); free(st); free(orb); free(ot); free(lst);
+}
+
 /* Im(mu . conj(m)) of two complex 3-vectors stored (re, im) x 3 */
 static double im_dot_conj(const double *mu, const double *m)
 {
@@ -435,6 +514,7 @@ int main(void)
               (2.0 / 3.0) * ene[j] * os, m[0], m[1], m[2], m[3], m[4], m[5]);
   }
   fclose(po);
+  if (!real) write_qp_spins(psi_host, eqp, nqp, o.ngrid, o.dx * o.dy * o.dz);
   /* M.dat, rs.dat and bs-coeff-<j>.dat for j < 10 (optical.c:29-95) */
   FILE *pm = fopen("M.dat", "w"), *prs = fopen("rs.dat", "w");
   if (!pm || !prs) die("cannot write", "M.dat / rs.dat");
@@ -463,6 +543,12 @@ int main(void)
           fprintf(pc, "%ld %ld %.12lg %lg\n", i, a, eqp[a] - eqp[i], c[0] * c[0] + c[1] * c[1]);
         }
       fclose(pc);
+    }
+    if (p.calc_spin_ang_stat) {
+      if (real)
+        printf("calcSpinAngStat: the spin / angular statistics need spinor states; skipped\n");
+      else
+        write_ang_stats(ctx, d_psi, gx, gy, gz, nh, ne, lumo, cf);
     }
     free(cf);
   }

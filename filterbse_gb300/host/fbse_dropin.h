@@ -37,6 +37,7 @@ typedef struct {
   int precision;
   /* kernel files (bse_cplx/read.c:58-60, 127-129; mod_kernel.c:31-96) */
   int coulomb_done, restart_coulomb, calc_coulomb_only;
+  int calc_spin_ang_stat; /* main.c:160-195 */
 } fbse_bse_params;
 
 /* input.par parsing: returns 0, or -1 with a message in err */
@@ -77,6 +78,16 @@ int fbse_build_nlc(long nx, long ny, long nz, const double *gx, const double *gy
 /* outputs (filter_mpi/write.c:263-299, save.c:446-503) */
 int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n);
 int fbse_write_psi(const char *path, const double *psi, long n_doubles);
+
+/* calc_xton_spin_mtrx + calc_xton_ang_mom_mtrx (bse_cplx/angular.c:692-1043):
+ * per exciton n (complex, interleaved) <S> spin[n][3], the two-body spin sum
+ * spintot[n] (spins.dat prints 1.5 + 2 Re), <L> orbit[n][3], the <L^2> sum
+ * orbittot[n] (orbital.dat) and the <L.S> sum lstot[n] (couple.dat), from the
+ * coefficients coeff[ibs][n] (ibs = a * n_h + i) and fbse_bse_qp_ang_mom's
+ * matrices.  Returns 0 or -1 (allocation). */
+int fbse_xton_ang_stats(long nh, long ne, const double *coeff, const double *s_mom, const double *l_mom,
+                        const double *l2_mom, const double *ldots, double *spin, double *spintot, double *orbit,
+                        double *orbittot, double *lstot);
 
 /* write_cube_file (filter_mpi/write.c:65-139): rho [ngrid] in grid order,
  * atoms as 8-byte symbol slots (sym8) and xyz (bohr); returns 0 or -1 (an

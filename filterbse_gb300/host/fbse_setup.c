@@ -42,12 +42,12 @@ static const char *k_ignored[] = {"nThreads", "hamThreads", "nestedOMP", "useFas
                                   "MPIDiag", "parallelSigma", "timeHamiltonian", "printNorm",
                                   "printGaussCubes", "saveCheckpoints", "printPsiOrtho",
                                   "fftWisdomDir", "saveOutput", "calcPotOverlap",
-                                  "calcSpinAngStat", "retryFilter", "centerConf", "noTimeRev", "psiZeroCut",
+                                  "retryFilter", "centerConf", "noTimeRev", "psiZeroCut",
                                   "calcDarkStates", "timingSpecs", "crystalStructure", "outmostMaterial", NULL};
 /* keys whose non-zero value selects a path this build does not implement */
 static const char *k_unsupported[] = {"periodic", "useStrain", "longRange", "localStructureDependent",
                                       "useGaussianBasis", "readProj", "readCoeffs", "inputPsiFilt",
-                                      "restartFromCheckpoint", "interpolatePot", NULL};
+                                      "restartFromCheckpoint", "interpolatePot", "calcSpinAngStat", NULL};
 
 static int in_list(const char *k, const char **l)
 {
@@ -187,6 +187,7 @@ int fbse_read_bse_params(const char *path, fbse_bse_params *p, char *err, size_t
     else if (!strcmp(key, "coulombDone")) { rc = parse_long(val, &lv); p->coulomb_done = (int)lv; }
     else if (!strcmp(key, "restartCoulomb")) { rc = parse_long(val, &lv); p->restart_coulomb = (int)lv; }
     else if (!strcmp(key, "calcCoulombOnly")) { rc = parse_long(val, &lv); p->calc_coulomb_only = (int)lv; }
+    else if (!strcmp(key, "calcSpinAngStat")) { rc = parse_long(val, &lv); p->calc_spin_ang_stat = (int)lv; }
     else if (!strcmp(key, "spinOrbit") || !strcmp(key, "NonLocal") || !strcmp(key, "KEmax")) {
       rc = parse_double(val, &dv); /* carried by output.dat; the value here is not used */
     } else if (in_list(key, k_ignored)) {

@@ -236,6 +236,18 @@ int fbse_bse_kernel_real(fbse_ctx *ctx, const double *psi_qp, long n_h, long n_e
 int fbse_bse_mag_dipoles(fbse_ctx *ctx, const double *psi_qp, const double *gx, const double *gy, const double *gz,
                          long n_h, long n_e, long lumo_idx, double *m_host);
 
+/* calc_qp_spin_mtrx + calc_qp_ang_mom_mtrx (bse_cplx/angular.c:7-690) for
+ * complex spinor states, with the reference's conventions per block: holes
+ * i, j < n_h at pair index i * n_h + j, electrons a, b at n_h^2 + (a - lumo)
+ * * n_e + (b - lumo).  s_mom, l_mom: [n_h^2 + n_e^2][3] complex; l2_mom
+ * (<L^2>) and ldots (<L.S>): [n_h^2 + n_e^2] complex (host, interleaved).
+ * L is l_operator's -(r x p) with p by FFT (as fbse_bse_mag_dipoles), L^2 is
+ * sum_d L_d L_d; the L quantities are computed for j >= i and the rest filled
+ * by Hermitian conjugation, as the reference does. */
+int fbse_bse_qp_ang_mom(fbse_ctx *ctx, const double *psi_qp, const double *gx, const double *gy, const double *gz,
+                        long n_h, long n_e, long lumo_idx, double *s_mom, double *l_mom, double *l2_mom,
+                        double *ldots);
+
 /* calc_optical_exc (bse_cplx/optical.c:6-99), electric part: exciton transition
  * dipoles mu_j = sum_ibs coeff[ibs][j] mu_(i(ibs), a(ibs)).  coeff: device, as
  * fbse_bse_solve returns it; mu_pairs_host: fbse_bse_dipoles' output;

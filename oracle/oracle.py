@@ -744,6 +744,105 @@ def bse_mag_dipoles(psi_qp, nh, ne, lumo, grid: Grid, nspin=2):
     return m
 
 
+def _l_prime(f, grid):
+    """l_operator (bse_cplx/ang_mom_operators.c:6-52) on one spin block:
+    L' f = -(r x p f), p_d f = IFFT(k_d FFT f) (p_operator, init_kvec)."""
+    gx, gy, gz = bse_axes(grid)
+    shp = (grid.nz, grid.ny, grid.nx)
+    Z, Y, X = np.meshgrid(gz, gy, gx, indexing="ij")
+    KZ, KY, KX = np.meshgrid(init_kvec(grid.nz, 2 * np.pi / (grid.nz * grid.dz)),
+                             init_kvec(grid.ny, 2 * np.pi / (grid.ny * grid.dy)),
+                             init_kvec(grid.nx, 2 * np.pi / (grid.nx * grid.dx)), indexing="ij")
+    F = np.fft.fftn(f.reshape(shp))
+    px, py, pz = (np.fft.ifftn(k * F) for k in (KX, KY, KZ))
+    return [(-(Y * pz - Z * py)).reshape(-1), (-(Z * px - X * pz)).reshape(-1), (-(X * py - Y * px)).reshape(-1)]
+
+
+def bse_qp_ang_mom(psi_qp, nh, ne, lumo, grid: Grid):
+    """calc_qp_spin_mtrx and calc_qp_ang_mom_mtrx (bse_cplx/angular.c:7-690)
+    for spinor states: s, l [nh^2 + ne^2][3], l2, ls [nh^2 + ne^2] with the
+    reference's per-block conventions (holes: -1/2 conj for spins, conj of the
+    negated L' sums; electrons: the sums as they are)."""
+    N, dv = grid.ngrid, grid.dv
+    n = nh * nh + ne * ne
+    S = np.zeros((n, 3), np.complex128)
+    Lm = np.zeros((n, 3), np.complex128)
+    L2 = np.zeros(n, np.complex128)
+    LS = np.zeros(n, np.complex128)
+    for blk, (cnt, s0, off) in enumerate(((nh, 0, 0), (ne, lumo, nh * nh))):
+        for i in range(cnt):
+            pi = psi_qp[s0 + i]
+            iu, idn = pi[:N], pi[N:]
+            lp = [_l_prime(iu, grid), _l_prime(idn, grid)]  # [spin][d]
+            l2 = [sum(_l_prime(lp[sp][d], grid)[d] for d in range(3)) for sp in range(2)]
+            for j in range(cnt):
+                pj = psi_qp[s0 + j]
+                ju, jd = pj[:N], pj[N:]
+                c = np.conj
+                sx = np.sum(c(jd) * iu) + np.sum(c(ju) * idn)
+                sy = 1j * np.sum(c(jd) * iu) - 1j * np.sum(c(ju) * idn)
+                sz = np.sum(c(ju) * iu) - np.sum(c(jd) * idn)
+                sv = np.array([sx, sy, sz])
+                k = off + i * cnt + j
+                S[k] = 0.5 * sv * dv if blk else -0.5 * np.conj(sv) * dv
+                if j < i:
+                    continue
+                r = np.array([np.sum(c(ju) * lp[0][d]) + np.sum(c(jd) * lp[1][d]) for d in range(3)])
+                rl2 = np.sum(c(ju) * l2[0]) + np.sum(c(jd) * l2[1])
+                rls = (np.sum(c(jd) * lp[0][0]) + np.sum(c(ju) * lp[1][0]) + 1j * np.sum(c(jd) * lp[0][1])
+                       - 1j * np.sum(c(ju) * lp[1][1]) + np.sum(c(ju) * lp[0][2]) - np.sum(c(jd) * lp[1][2]))
+                lv = r * dv if blk else -np.conj(r) * dv
+                l2v = rl2 * dv if blk else np.conj(rl2) * dv
+                lsv = 0.5 * rls * dv if blk else 0.5 * np.conj(rls) * dv
+                kt = off + j * cnt + i
+                Lm[k], Lm[kt] = lv, np.conj(lv)
+                L2[k], L2[kt] = l2v, np.conj(l2v)
+                LS[k], LS[kt] = lsv, np.conj(lsv)
+    return S, Lm, L2, LS
+
+
+def xton_ang_stats(C, S, Lm, L2, LS, nh, ne):
+    """calc_xton_spin_mtrx and calc_xton_ang_mom_mtrx (bse_cplx/angular.c:692-1043):
+    per exciton n: <S> (3), the spin sum of spins.dat, <L> (3), the orbital sum
+    of orbital.dat and the L.S sum of couple.dat.  C[ibs][n], ibs = a*nh + i."""
+    nx = nh * ne
+    he = lambda i, j: i * nh + j            # hole pair index
+    el = lambda a, b: nh * nh + a * ne + b  # electron pair index
+    spin = np.zeros((nx, 3), np.complex128)
+    stot = np.zeros(nx, np.complex128)
+    orb = np.zeros((nx, 3), np.complex128)
+    otot = np.zeros(nx, np.complex128)
+    lstot = np.zeros(nx, np.complex128)
+    for n in range(nx):
+        c = C[:, n]
+        for a in range(ne):
+            for i in range(nh):
+                ibs = a * nh + i
+                st = sum(np.conj(c[b * nh + i]) * S[el(a, b)] for b in range(ne)) + \
+                    sum(np.conj(c[a * nh + j]) * S[he(i, j)] for j in range(nh))
+                lt = sum(np.conj(c[b * nh + i]) * Lm[el(a, b)] for b in range(ne)) + \
+                    sum(np.conj(c[a * nh + j]) * Lm[he(i, j)] for j in range(nh))
+                spin[n] += c[ibs] * st
+                orb[n] += c[ibs] * lt
+                for b in range(ne):
+                    for j in range(nh):
+                        ct = np.conj(c[b * nh + j]) * c[ibs]
+                        stot[n] += ct * np.sum(S[el(a, b)] * S[he(i, j)])
+                        o = 2.0 * np.sum(Lm[el(a, b)] * Lm[he(i, j)])
+                        if i == j:
+                            o += L2[el(a, b)]
+                        if a == b:
+                            o += L2[he(i, j)]
+                        otot[n] += ct * o
+                        x = np.sum(Lm[el(a, b)] * S[he(i, j)]) + np.sum(S[el(a, b)] * Lm[he(i, j)])
+                        if i == j:
+                            x += LS[el(a, b)]
+                        if a == b:
+                            x += LS[he(i, j)]
+                        lstot[n] += ct * x
+    return spin, stot, orb, otot, lstot
+
+
 def bse_optical(C, mu, nh, ne):
     """calc_optical_exc (bse_cplx/optical.c:36-80), electric part: exciton
     dipoles [n][3] and OS.dat's oscillator strengths need E: (2/3) E |mu|^2."""

@@ -19,7 +19,9 @@ Fixtures (all data outputs or inputs of the reference's own example runs):
                          conf.par, pot*.par, SO_*.par and reference eval.dat;
                          its BSE run (bse_cplx/EXAMPLES/1x1x1_CsPbI3/bse):
                          bse_input.par and the reference's exciton.dat,
-                         OS.dat, OS0.dat, M0.dat, M.dat, rs0.dat, rs.dat
+                         OS.dat, OS0.dat, M0.dat, M.dat, rs0.dat, rs.dat and
+                         the calcSpinAngStat files lsqr.dat, ls.dat,
+                         spins.dat, orbital.dat, couple.dat, qp_spins.dat
 """
 import os
 import shutil
@@ -69,7 +71,8 @@ def main():
     shutil.copy(os.path.join(src, "reference_output", "eval.dat"), d)
     bse = os.path.join(REF, "bse_cplx", "EXAMPLES", "1x1x1_CsPbI3", "bse")
     shutil.copy(os.path.join(bse, "input.par"), os.path.join(d, "bse_input.par"))
-    for fn in ("exciton.dat", "OS.dat", "OS0.dat", "M0.dat", "M.dat", "rs0.dat", "rs.dat"):
+    for fn in ("exciton.dat", "OS.dat", "OS0.dat", "M0.dat", "M.dat", "rs0.dat", "rs.dat", "lsqr.dat", "ls.dat",
+               "spins.dat", "orbital.dat", "couple.dat", "qp_spins.dat"):
         shutil.copy(os.path.join(bse, "reference_output", fn), d)
 
 

@@ -159,6 +159,22 @@ def test_bse_mag_dipoles_match_oracle(fbse, cuda, name):
     assert _relmax(m, ref) < 1e-12
 
 
+def test_bse_qp_ang_mom_matches_oracle(fbse, cuda):
+    """calc_qp_spin_mtrx / calc_qp_ang_mom_mtrx: spin, L, L^2 and L.S matrices
+    of both blocks with the reference's per-block conventions."""
+    nh, ne, gap = 3, 2, 1
+    g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, "odd21x20x18", nh, ne, gap)
+    got = ctx.bse_qp_ang_mom(psi_d, *O.bse_axes(g), nh, ne, lumo)
+    want = O.bse_qp_ang_mom(psi, nh, ne, lumo, g)
+    for a, b in zip(got, want):
+        assert _relmax(a, b) < 1e-11
+    # Hermitian blocks (spins, L, L^2, L.S)
+    for m in (got[0][:, 0], got[1][:, 2], got[2], got[3]):
+        for off, n in ((0, nh), (nh * nh, ne)):
+            M = m[off:off + n * n].reshape(n, n)
+            assert np.max(np.abs(M - M.conj().T)) < 1e-10 * max(1.0, np.max(np.abs(M)))
+
+
 def test_bse_optical_matches_oracle(fbse, cuda):
     nh, ne, gap = 3, 4, 1
     g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, "cubic24", nh, ne, gap)

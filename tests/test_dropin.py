@@ -219,3 +219,36 @@ def test_executables_fail_loudly_without_gpu(tmp_path):
     assert r.returncode != 0
     assert "ERROR" in r.stderr
     assert not (tmp_path / "eval.dat").exists()
+
+
+def test_xton_ang_stats_match_oracle(lib):
+    """calc_xton_spin_mtrx / calc_xton_ang_mom_mtrx on random Hermitian pair
+    matrices and a random unitary coefficient matrix (host code)."""
+    rng = np.random.default_rng(12)
+    nh, ne = 3, 4
+    nx, n = nh * ne, nh * nh + ne * ne
+
+    def herm_blocks(k):
+        out = np.zeros((n, k), np.complex128) if k else np.zeros(n, np.complex128)
+        for off, m in ((0, nh), (nh * nh, ne)):
+            for d in range(max(k, 1)):
+                A = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+                A = A + A.conj().T
+                if k:
+                    out[off:off + m * m, d] = A.reshape(-1)
+                else:
+                    out[off:off + m * m] = A.reshape(-1)
+        return out
+
+    S, Lm, L2, LS = herm_blocks(3), herm_blocks(3), herm_blocks(0), herm_blocks(0)
+    C, _ = np.linalg.qr(rng.normal(size=(nx, nx)) + 1j * rng.normal(size=(nx, nx)))
+    C = np.ascontiguousarray(C)
+    out = [np.empty(nx * 3, np.complex128), np.empty(nx, np.complex128), np.empty(nx * 3, np.complex128),
+           np.empty(nx, np.complex128), np.empty(nx, np.complex128)]
+    lib.fbse_xton_ang_stats.argtypes = [ctypes.c_long, ctypes.c_long] + [D] * 10
+    v = lambda a: np.ascontiguousarray(a).view(np.float64).ctypes.data_as(D)
+    assert lib.fbse_xton_ang_stats(nh, ne, v(C), v(S), v(Lm), v(L2), v(LS), *[v(o) for o in out]) == 0
+    want = O.xton_ang_stats(C, S, Lm, L2, LS, nh, ne)
+    got = [out[0].reshape(nx, 3), out[1], out[2].reshape(nx, 3), out[3], out[4]]
+    for g_, w in zip(got, want):
+        assert np.max(np.abs(g_ - w)) < 1e-12 * max(1.0, np.max(np.abs(w)))

@@ -72,6 +72,7 @@ def test_dropin_bse_matches_reference_exciton(cuda, tmp_path):
     _run("fbse_filter", tmp_path)
     bse = open(os.path.join(GOLD, "cspbi3", "bse_input.par")).read()
     bse = bse.replace("maxHoleStates = 10", "maxHoleStates = 8").replace("maxElecStates = 10", "maxElecStates = 8")
+    bse = bse.replace("calcSpinAngStat = 0", "calcSpinAngStat = 1")
     with open(tmp_path / "input.par", "w") as f:
         f.write(bse)
     out = _run("fbse_bse", tmp_path)
@@ -89,6 +90,8 @@ def test_dropin_bse_matches_reference_exciton(cuda, tmp_path):
     osr = np.loadtxt(os.path.join(GOLD, "cspbi3", "OS.dat"))
     assert osd[0, 1] < 1e-3  # the lowest exciton is dark
     assert abs(np.sum(osd[1:4, 1] ** 2) - np.sum(osr[1:4, 1] ** 2)) < 1e-2 * np.sum(osr[1:4, 1] ** 2)
+
+    _check_ang_stats(tmp_path, ex, ref)
 
     # magnetic outputs: the files and their pair / exciton counts
     assert np.loadtxt(tmp_path / "M0.dat").shape == (64, 11) and np.loadtxt(tmp_path / "rs0.dat").shape == (64, 4)
@@ -111,6 +114,76 @@ def test_dropin_bse_matches_reference_exciton(cuda, tmp_path):
     ex2 = np.loadtxt(tmp_path / "exciton.dat")
     # the files carry 12 decimals
     assert np.max(np.abs(ex2[:, 1] - ex[:, 1])) < 1e-9
+
+
+def _groups(e, tol=1e-6):
+    out, cur = [], [0]
+    for i in range(1, len(e)):
+        if abs(e[i] - e[i - 1]) < tol:
+            cur.append(i)
+        else:
+            out.append(cur)
+            cur = [i]
+    out.append(cur)
+    return out
+
+
+def _check_ang_stats(tmp, ex, ref):
+    """calcSpinAngStat files against the reference's run on the same basis:
+    traces over degenerate levels (basis-invariant) of the spin fractions
+    (qp_spins.dat), <L^2> and <L.S> (lsqr.dat, ls.dat), and the exciton sums
+    of spins.dat / orbital.dat over degenerate exciton clusters whose energies
+    match.  Holes 0 and 1 are half of a four-fold level and depend on which
+    half each run picked; they are left out.  The reference's electron <L.S>
+    loop (bse_cplx/angular.c:582-604) never advances its spin-down index, so
+    its electron ls.dat entries and couple.dat are not the L.S sums; those are
+    checked against the oracle instead (test_bse_gpu, test_dropin)."""
+    g = os.path.join(GOLD, "cspbi3")
+
+    def qp_frac(path):
+        t = open(path).read().split("Stats on state")[1:]
+        return np.array([[float(x.split("fraction:")[1]) for x in b.splitlines()[1:3]] for b in t]), \
+            np.array([float(b.split("E=")[1].split(")")[0]) for b in t])
+
+    mf, me = qp_frac(tmp / "qp_spins.dat")
+    rf, _ = qp_frac(os.path.join(g, "qp_spins.dat"))
+    assert mf.shape == rf.shape == (16, 2)
+    levels = [[2 + k for k in cl] for cl in _groups(me[2:], 1e-5)]
+    worst = 0.0
+    for name in ("lsqr.dat", "ls.dat"):
+        mine = np.loadtxt(tmp / name)
+        refm = np.loadtxt(os.path.join(g, name))
+        dm = {(int(r[0]), int(r[1])): r[2] for r in mine}
+        dr = {(int(r[0]), int(r[1])): r[2] for r in refm}
+        for lv in levels:
+            if name == "ls.dat" and lv[0] >= 8:
+                continue  # electrons: see above
+            a = sum(dm[(k, k)] for k in lv)
+            b = sum(dr[(k, k)] for k in lv)
+            worst = max(worst, abs(a - b) / max(1.0, abs(b)))
+    for lv in levels:
+        worst = max(worst, np.max(np.abs(mf[lv].sum(0) - rf[lv].sum(0))))
+    def totals(path):
+        # the value before "(imaginary part)"; the example's spins.dat has the
+        # three real spin components where angular.c:789-790 writes six
+        out = []
+        for line in open(path):
+            t = line.split()
+            out.append(float(t[next(k for k, x in enumerate(t) if x.startswith("(")) - 1]))
+        return np.array(out)
+
+    names = ("spins.dat", "orbital.dat")
+    mine_x = [totals(tmp / f) for f in names]
+    ref_x = [totals(os.path.join(g, f)) for f in names]
+    nmatch = 0
+    for cl in _groups(ref[:, 1]):
+        if np.all(np.abs(ex[cl, 1] - ref[cl, 1]) < 1e-6):
+            nmatch += 1
+            for m_, r_ in zip(mine_x, ref_x):
+                worst = max(worst, abs(m_[cl].sum() - r_[cl].sum()) / max(1.0, abs(r_[cl].sum())))
+    print(f"[fbse_bse cspbi3] angular statistics: {len(levels)} qp levels, {nmatch} exciton clusters, "
+          f"max rel dev {worst:.2e}")
+    assert nmatch >= 10 and worst < 1e-3
 
 
 def _small(extra=""):
