@@ -115,3 +115,54 @@ def test_normalize_zero_norm_errors(fbse, cuda):
     with pytest.raises(fbse.FbseError) as ei:
         ctx.normalize_all(t)
     assert ei.value.code == -4
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_filter_job_matches_device_path(fbse, cuda, pinned):
+    """fbse_filter_job on host buffers = newton_filter + ortho_diag_sigma on
+    device buffers, with mod_output's sigma cut; pinned output buffers are
+    filled by the device directly, pageable ones by copies."""
+    import torch
+    sysm = tiny_cluster(16, 18, 15, natoms=8, nspin=2, is_complex=True, so=True, nl=True)
+    emin, emax = _range(sysm)
+    de = emax - emin
+    ncheby, m, nstart = 60, 3, 3
+    zn, _, _ = O.samp_points(ncheby)
+    targets = np.linspace(emin + 0.1 * de, emin + 0.3 * de, m)
+    an = O.newton_coeff(zn, targets, emin, de, O.filter_dt(ncheby, de))
+    starts, _, _ = O.init_filter_states(-777, nstart, sysm.ngrid, sysm.nspin, sysm.is_complex, sysm.grid.dv)
+    p0 = np.ascontiguousarray(starts.view(np.float64).reshape(nstart, -1))
+    ctx = _ctx(fbse, sysm, 0)
+    filt = ctx.newton_filter(zn, an, emin, de, torch.tensor(p0, device=cuda))
+    nk, ev, sg = ctx.ortho_diag_sigma(filt.reshape(nstart * m, -1))
+    ref_states = filt.reshape(nstart * m, -1)[:nk].cpu().numpy()
+    stlen = p0.shape[1]
+    dv = sysm.grid.dv
+
+    def run(cut):
+        out = torch.zeros((nstart * m, stlen), dtype=torch.float64)
+        if pinned:
+            out = out.pin_memory()
+        k, e, s_ = ctx.filter_job(zn, an, emin, de, p0, sigma_cut=cut, psi_out=out)
+        return k, e, s_, out.numpy()
+
+    # every state (getAllStates): the same Ritz values and the same span (the
+    # spin-orbit levels are Kramers pairs, so compare subspaces, not vectors)
+    k, ev_j, sg_j, got = run(0.0)
+    assert k == nk and np.max(np.abs(ev_j - ev)) < 1e-10
+    a = got[:k].view(np.complex128)
+    b = ref_states.view(np.complex128)
+    sv = np.linalg.svd(a @ b.conj().T * dv, compute_uv=False)
+    assert np.max(np.abs(sv - 1.0)) < 1e-8
+    assert not np.any(got[k:])
+    # the sigma cut of mod_output
+    srt = np.sort(sg_j)
+    gaps = [(srt[i + 1] - srt[i], i) for i in range(len(srt) - 1) if srt[i + 1] - srt[i] > 1e-9 * srt[i + 1]]
+    assert gaps
+    i_cut = min(gaps, key=lambda t: abs(t[1] - len(srt) // 2))[1]
+    cut = float(0.5 * (srt[i_cut] + srt[i_cut + 1]))  # between two separated values
+    k2, ev2, sg2, got2 = run(cut)
+    assert k2 == int(np.sum(sg_j <= cut)) and np.all(sg2 <= cut)
+    assert np.max(np.abs(ev2 - ev_j[sg_j <= cut])) < 1e-10
+    nrm = np.sum(got2[:k2] ** 2, axis=1) * dv
+    assert np.max(np.abs(nrm - 1.0)) < 1e-10 and not np.any(got2[k2:])
