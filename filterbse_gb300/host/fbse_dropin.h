@@ -28,6 +28,9 @@ typedef struct {
   long n_states_for_ortho, n_states_for_sigma;
   int print_cubes; /* printCubes = 1 <ncubes> (read.c:691-715) */
   long ncubes;
+  int read_coeffs; /* readCoeffs = 1: zn.dat and coeff-<t>.dat are read (mod_filter.c:116-126) */
+  int input_psi_filt; /* inputPsiFilt = 1 <start> <end>: starts from psi-init.dat (init.c:1166-1203) */
+  long init_psi_start, init_psi_end;
 } fbse_filter_params;
 
 /* the subset of bse_cplx/input.par (bse_cplx/read.c) */

@@ -12,8 +12,10 @@
  * reads psi-filt.dat and starts at the orthogonalisation, "restartFromSigma
  * = 1 <n>" reads psi-diag.dat and only computes energies and sigma_E
  * (main.c:128-305, read.c:954-967); calcFilterOnly stops after the filter.
- * conf.dat and, with "printCubes = 1 <n>", the homo-i / lumo+i cube files of
- * mod_optional_output.
+ * The starts come from psi-init.dat with "inputPsiFilt = 1 <start> <end>".
+ * Also written: conf.dat, seed-0.dat, zn.dat / coeff-<t>.dat (read back
+ * instead of computed with readCoeffs = 1) and, with "printCubes = 1 <n>",
+ * the homo-i / lumo+i cube files of mod_optional_output.
  * Errors go to stderr and the process exits with EXIT_FAILURE, like the
  * reference.  One non-reference key: "mixedPrecision = 1" selects the FP32
  * recursion (default: the plain FP64 method). */
@@ -129,6 +131,45 @@ static void write_cubes(const fbse_filter_params *p, const double *psi, const do
     }
   free(rho);
   free(sym8);
+}
+
+/* zn.dat and coeff-<t>.dat as gen_newton_coeff writes them (coeff.c:66-108):
+ * "%ld %lg" nodes, "%ld %g %g" coefficients */
+static void write_coeff_files(const double *zn, const double *an, long nc, long m)
+{
+  FILE *f = fopen("zn.dat", "w");
+  if (!f) die("cannot write", "zn.dat");
+  for (long j = 0; j < nc; j++) fprintf(f, "%ld %lg\n", j, zn[j]);
+  fclose(f);
+  for (long t = 0; t < m; t++) {
+    char path[64];
+    snprintf(path, sizeof path, "coeff-%ld.dat", t);
+    f = fopen(path, "w");
+    if (!f) die("cannot write", path);
+    for (long j = 0; j < nc; j++) fprintf(f, "%ld %g %g\n", j, an[2 * (t * nc + j)], an[2 * (t * nc + j) + 1]);
+    fclose(f);
+  }
+}
+
+/* read_newton_coeff (coeff.c:176-212): the same files back */
+static void read_coeff_files(double *zn, double *an, long nc, long m)
+{
+  FILE *f = fopen("zn.dat", "r");
+  if (!f) die("could not open", "zn.dat");
+  long idx;
+  for (long j = 0; j < nc; j++)
+    if (fscanf(f, "%ld %lg", &idx, &zn[j]) != 2) die("fewer nodes than nCheby in", "zn.dat");
+  fclose(f);
+  for (long t = 0; t < m; t++) {
+    char path[64];
+    snprintf(path, sizeof path, "coeff-%ld.dat", t);
+    f = fopen(path, "r");
+    if (!f) die("could not open", path);
+    for (long j = 0; j < nc; j++)
+      if (fscanf(f, "%ld %lg %lg", &idx, &an[2 * (t * nc + j)], &an[2 * (t * nc + j) + 1]) != 3)
+        die("fewer coefficients than nCheby in", path);
+    fclose(f);
+  }
 }
 
 /* n states of stlen doubles from a raw state file (psi-filt.dat, psi-diag.dat) */
@@ -373,9 +414,14 @@ int main(void)
     del = (p.cbmax - p.cbmin) / (double)p.n_targets_cb;
     for (long j = p.n_targets_vb; j < m; j++) targets[j] = p.cbmin + (double)(j - p.n_targets_vb) * del;
     double *zn = malloc(nc * sizeof(double)), *an = malloc(2 * m * nc * sizeof(double));
-    fbse_samp_points(nc, zn);
-    const double dt = ((double)nc / (2.5 * de)) * ((double)nc / (2.5 * de)); /* mod_filter.c:114 */
-    if (fbse_newton_coeff(nc, m, zn, targets, emin, de, dt, an)) die("Newton coefficients", NULL);
+    if (p.read_coeffs == 1) {
+      read_coeff_files(zn, an, nc, m);
+    } else {
+      fbse_samp_points(nc, zn);
+      const double dt = ((double)nc / (2.5 * de)) * ((double)nc / (2.5 * de)); /* mod_filter.c:114 */
+      if (fbse_newton_coeff(nc, m, zn, targets, emin, de, dt, an)) die("Newton coefficients", NULL);
+      write_coeff_files(zn, an, nc, m);
+    }
 
     /* random starts (mod_filter.c:152-160, init_filter_states) */
     long seed;
@@ -386,7 +432,34 @@ int main(void)
     }
     double *starts = malloc((size_t)ns * sbytes);
     if (!starts) die("host allocation", NULL);
-    fbse_init_filter_states(starts, ns, ngrid, nspin, cplx, p.dx * p.dy * p.dz, seed, NULL);
+    if (p.input_psi_filt == 1) {
+      /* read_psi_dat (aux.c:131-156): from state `start`, every second state
+       * for spinors (Kramers partners skipped), the one after each skip; the
+       * read states fill psi_rank contiguously and cycle jns starts from the
+       * first state of its block, jns * m (filter.c:253-275) */
+      const long every = nspin == 2 ? 2 : 1;
+      const long nread = (p.init_psi_end - p.init_psi_start + every - 1) / every;
+      if ((ns - 1) * m >= nread) die("psi-init.dat range holds fewer states than nFilterCycles x mStatesPerFilter", NULL);
+      FILE *fi = fopen("psi-init.dat", "rb");
+      if (!fi) die("could not open", "psi-init.dat");
+      for (long j = 0; j < ns; j++) {
+        const long q = j * m; /* read index of this start */
+        const long state = p.init_psi_start + q * every + (every - 1);
+        if (fseek(fi, (long)(state * sbytes), SEEK_SET) || fread(starts + j * stlen, sizeof(double), stlen, fi) != (size_t)stlen)
+          die("truncated", "psi-init.dat");
+      }
+      fclose(fi);
+    } else {
+      long *seeds = malloc((size_t)ns * nspin * sizeof(long));
+      if (!seeds) die("host allocation", NULL);
+      fbse_init_filter_states(starts, ns, ngrid, nspin, cplx, p.dx * p.dy * p.dz, seed, seeds);
+      FILE *fsd = fopen("seed-0.dat", "w"); /* init.c:1204-1212 */
+      if (!fsd) die("cannot write", "seed-0.dat");
+      fprintf(fsd, "idx  seed\n");
+      for (long k = 0; k < ns * nspin; k++) fprintf(fsd, "%ld %ld\n", k, seeds[k]);
+      fclose(fsd);
+      free(seeds);
+    }
 
     /* the filter cycles of every start at once (run_filter_cycles) */
     void *d_starts = NULL;

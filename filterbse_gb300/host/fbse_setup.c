@@ -46,7 +46,7 @@ static const char *k_ignored[] = {"nThreads", "hamThreads", "nestedOMP", "useFas
                                   "calcDarkStates", "timingSpecs", "crystalStructure", "outmostMaterial", NULL};
 /* keys whose non-zero value selects a path this build does not implement */
 static const char *k_unsupported[] = {"periodic", "useStrain", "longRange", "localStructureDependent",
-                                      "useGaussianBasis", "readProj", "readCoeffs", "inputPsiFilt",
+                                      "useGaussianBasis", "readProj",
                                       "restartFromCheckpoint", "interpolatePot", "calcSpinAngStat", NULL};
 
 static int in_list(const char *k, const char **l)
@@ -108,6 +108,15 @@ int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, 
     else if (!strcmp(key, "approxEnergyRange")) { rc = parse_long(val, &lv); p->approx_energy_range = (int)lv; }
     else if (!strcmp(key, "mixedPrecision")) { rc = parse_long(val, &lv); p->precision = lv ? 1 : 0; }
     else if (!strcmp(key, "printPsiFilt")) { rc = parse_long(val, &lv); p->print_psi_filt = (int)lv; }
+    else if (!strcmp(key, "readCoeffs")) { rc = parse_long(val, &lv); p->read_coeffs = (int)lv; }
+    else if (!strcmp(key, "inputPsiFilt")) {
+      /* "inputPsiFilt = 1 <start> <end>" (read.c:440-451) */
+      rc = parse_long(val, &lv);
+      p->input_psi_filt = (int)lv;
+      if (!rc && lv == 1 && (fscanf(f, "%ld %ld", &p->init_psi_start, &p->init_psi_end) != 2 ||
+                             p->init_psi_start < 0 || p->init_psi_end <= p->init_psi_start))
+        rc = -1;
+    }
     else if (!strcmp(key, "printPsiDiag")) { rc = parse_long(val, &lv); p->print_psi_diag = (int)lv; }
     else if (!strcmp(key, "calcFilterOnly")) { rc = parse_long(val, &lv); p->calc_filter_only = (int)lv; }
     else if (!strcmp(key, "restartFromOrtho")) {

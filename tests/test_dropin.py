@@ -32,7 +32,9 @@ class FilterParams(ctypes.Structure):
                 ("print_psi_filt", ctypes.c_int), ("print_psi_diag", ctypes.c_int),
                 ("calc_filter_only", ctypes.c_int), ("restart_from_ortho", ctypes.c_int),
                 ("restart_from_sigma", ctypes.c_int), ("n_states_for_ortho", ctypes.c_long),
-                ("n_states_for_sigma", ctypes.c_long), ("print_cubes", ctypes.c_int), ("ncubes", ctypes.c_long)]
+                ("n_states_for_sigma", ctypes.c_long), ("print_cubes", ctypes.c_int), ("ncubes", ctypes.c_long),
+                ("read_coeffs", ctypes.c_int), ("input_psi_filt", ctypes.c_int), ("init_psi_start", ctypes.c_long),
+                ("init_psi_end", ctypes.c_long)]
 
 
 @pytest.fixture(scope="module")
@@ -74,6 +76,12 @@ def test_read_filter_params_restarts(lib, tmp_path):
                                     "calcFilterOnly = 0\nsaveCheckpoints = 1\n")
     assert lib.fbse_read_filter_params(str(tmp_path / "a.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
     assert (p.restart_from_ortho, p.n_states_for_ortho, p.print_psi_filt, p.print_psi_diag) == (1, 8, 0, 1)
+    (tmp_path / "e.par").write_text(base + "readCoeffs = 1\nprintCubes = 1 2\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "e.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
+    assert (p.read_coeffs, p.print_cubes, p.ncubes) == (1, 1, 2)
+    (tmp_path / "f.par").write_text(base + "inputPsiFilt = 1 4 20\n")
+    assert lib.fbse_read_filter_params(str(tmp_path / "f.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
+    assert (p.input_psi_filt, p.init_psi_start, p.init_psi_end) == (1, 4, 20)
     (tmp_path / "b.par").write_text(base + "restartFromSigma = 1 12\n")
     assert lib.fbse_read_filter_params(str(tmp_path / "b.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
     assert (p.restart_from_sigma, p.n_states_for_sigma) == (1, 12)

@@ -49,6 +49,13 @@ def test_dropin_filter_matches_reference_eval(cuda, tmp_path):
     # psi.dat holds the states of eval.dat, stlen doubles each (2 x 2 x 44^3)
     assert os.path.getsize(tmp_path / "psi.dat") == len(ev) * 2 * 2 * 44 ** 3 * 8
     assert (tmp_path / "output.dat").exists()
+    # seed-0.dat (init.c:1204-1212): the seed before each spin block of each start
+    sd = open(tmp_path / "seed-0.dat").read().splitlines()
+    assert sd[0] == "idx  seed" and len(sd) == 1 + 16 * 2 and sd[1] == "0 -31415"
+    # zn.dat and coeff-<t>.dat (coeff.c:66-108)
+    zn = np.loadtxt(tmp_path / "zn.dat")
+    assert zn.shape == (2048, 2) and np.array_equal(zn[:, 0], np.arange(2048))
+    assert all(np.loadtxt(tmp_path / f"coeff-{t}.dat").shape == (2048, 3) for t in range(16))
     # conf.dat and the cube files of "printCubes = 1 3" (mod_optional_output):
     # the signed densities of both spin blocks integrate to 1
     assert int(open(tmp_path / "conf.dat").readline()) == 15
@@ -231,6 +238,37 @@ def test_dropin_restarts_reproduce_the_full_run(cuda, tmp_path):
     assert np.max(np.abs(ev_s[:, 1] - ev[:, 1])) < 1e-10
     assert np.max(np.abs(ev_s[:, 2] - ev[:, 2])) < 1e-6
     assert os.path.getsize(rs / "psi.dat") == os.path.getsize(full / "psi.dat")
+
+    # readCoeffs: zn.dat / coeff-<t>.dat of the full run read back (6 digits,
+    # as the reference writes them): the converged levels stay put
+    rc_ = tmp_path / "coeffs"
+    rc_.mkdir()
+    _stage(rc_, _small("readCoeffs = 1\nprintPsiFilt = 0\n"))
+    for f in ["zn.dat"] + [f"coeff-{t}.dat" for t in range(8)]:
+        shutil.copy(full / f, rc_ / f)
+    _run("fbse_filter", rc_)
+    ev_c = np.loadtxt(rc_ / "eval.dat")
+    good = ev[ev[:, 2] < 1e-3, 1]
+    assert len(good) >= 2
+    assert all(np.min(np.abs(ev_c[:, 1] - e)) < 1e-5 for e in good)
+
+    # inputPsiFilt = 1 <start> <end>: starts from psi-init.dat (every second
+    # state for spinors, the first of each start's block of m); converged
+    # states are eigenstates of the same Hamiltonian
+    pi = tmp_path / "psiinit"
+    pi.mkdir()
+    _stage(pi, _small("inputPsiFilt = 1 2 40\nprintPsiFilt = 0\n"))
+    rng = np.random.default_rng(5)
+    states = rng.uniform(-1, 1, (40, stlen))
+    states /= np.sqrt(np.sum(states ** 2, axis=1) * 0.125)[:, None]
+    states.tofile(pi / "psi-init.dat")
+    _run("fbse_filter", pi)
+    assert not (pi / "seed-0.dat").exists()
+    ev_i = np.loadtxt(pi / "eval.dat")
+    refe = np.loadtxt(os.path.join(GOLD, "cspbi3", "eval.dat"))
+    refe = refe[refe[:, 2] < 1e-6, 1]
+    conv = ev_i[ev_i[:, 2] < 1e-3, 1]
+    assert len(conv) >= 1 and all(np.min(np.abs(refe - e)) < 1e-5 for e in conv)
 
     # calcFilterOnly: the psi-filt files and nothing after the filter
     fo = tmp_path / "only"
