@@ -126,7 +126,7 @@ extern std::atomic<long> g_launches;
   } while (0)
 
 int ensure(fbse_ctx *c, void **p, size_t *have, size_t need);
-enum CacheSlot { kSlotRing = 0, kSlotHpsi, kSlotRot, kSlotJobStarts, kSlotJobStates };
+enum CacheSlot { kSlotRing = 0, kSlotHpsi, kSlotRot, kSlotJobStarts, kSlotJobStates, kSlotJacobi };
 inline int cached(fbse_ctx *c, int slot, size_t need, void **out)
 {
   const int rc = ensure(c, &c->cache[slot], &c->cache_bytes[slot], need);

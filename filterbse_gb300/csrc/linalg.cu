@@ -169,7 +169,8 @@ int zgemm_dev(fbse_ctx *c, int m, int p, int k, const double2 *A, int lda, bool 
 // ---------------------------------------------------------------------------
 // Hermitian eigensolver: cyclic two-sided Jacobi with the round-robin pairing
 // (n/2 disjoint rotations per round, n-1 rounds per sweep), one cooperative
-// launch per sweep with grid-wide barriers between the phases.
+// launch per sweep with two grid-wide barriers per round (rotation
+// parameters, then the two-sided update of A and V).
 // A (n x n, row-major, Hermitian) is diagonalised in place; V accumulates the
 // unitary so that A_in = V diag(A_out) V^H.
 // ---------------------------------------------------------------------------
@@ -194,6 +195,7 @@ __global__ void k_jacobi_sweep(double2 *__restrict__ A, double2 *__restrict__ V,
   const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const long nth = (long)gridDim.x * blockDim.x;
   const int half = m / 2;
+  const long nblk = (long)half * half;  // 2 x 2 blocks of A, one per (row pair, column pair)
   for (int r = 0; r < m - 1; r++) {
     // phase 1: rotation parameters for the n/2 pairs of this round
     for (long s = tid; s < half; s += nth) {
@@ -216,41 +218,57 @@ __global__ void k_jacobi_sweep(double2 *__restrict__ A, double2 *__restrict__ V,
       rot[s] = R;
     }
     grid.sync();
-    // phase 2: rows p, q of A <- U^H rows   (new row p = cs a_p - sn e^{i phi} a_q,
-    //                                        new row q = sn a_p + cs e^{i phi} a_q)
-    for (long w = tid; w < (long)half * n; w += nth) {
-      const Rot R = rot[w / n];
-      const int col = (int)(w % n);
-      if (R.q >= n) continue;
-      const double2 ap = A[(long)R.p * n + col], aq = A[(long)R.q * n + col];
-      const double2 e = make_double2(R.pr, R.pi);
-      const double2 eaq = make_double2(e.x * aq.x - e.y * aq.y, e.x * aq.y + e.y * aq.x);
-      A[(long)R.p * n + col] = make_double2(R.cs * ap.x - R.sn * eaq.x, R.cs * ap.y - R.sn * eaq.y);
-      A[(long)R.q * n + col] = make_double2(R.sn * ap.x + R.cs * eaq.x, R.sn * ap.y + R.cs * eaq.y);
-    }
-    grid.sync();
-    // phase 3: columns p, q of A and V <- cols U  (new col p = cs a_p - sn e^{-i phi} a_q,
-    //                                             new col q = sn a_p + cs e^{-i phi} a_q)
-    for (long w = tid; w < (long)half * n * 2; w += nth) {
-      const long w2 = w % ((long)half * n);
-      const bool onV = w >= (long)half * n;
-      const Rot R = rot[w2 / n];
-      const int row = (int)(w2 % n);
-      if (R.q >= n) continue;
-      double2 *M = onV ? V : A;
-      const double2 ap = M[(long)row * n + R.p], aq = M[(long)row * n + R.q];
-      const double2 e = make_double2(R.pr, -R.pi);
-      const double2 eaq = make_double2(e.x * aq.x - e.y * aq.y, e.x * aq.y + e.y * aq.x);
-      M[(long)row * n + R.p] = make_double2(R.cs * ap.x - R.sn * eaq.x, R.cs * ap.y - R.sn * eaq.y);
-      M[(long)row * n + R.q] = make_double2(R.sn * ap.x + R.cs * eaq.x, R.sn * ap.y + R.cs * eaq.y);
-    }
-    grid.sync();
-    // the rotated pair is exactly diagonal in exact arithmetic: clean it
-    for (long s = tid; s < half; s += nth) {
-      const Rot R = rot[s];
-      if (R.q < n && !(R.cs == 1.0 && R.sn == 0.0)) {
-        A[(long)R.p * n + R.q] = make_double2(0, 0);
-        A[(long)R.q * n + R.p] = make_double2(0, 0);
+    // phase 2: the pairs of a round cover every index once, so every element
+    // of A lies in one 2 x 2 block (row pair a, column pair b) and every
+    // element of V in one 1 x 2 block (row i, column pair b).  A block is
+    // rotated from both sides at once, A_blk <- U_a^H A_blk U_b:
+    //   rows:    new p = cs a_p - sn e^{i phi} a_q,   new q = sn a_p + cs e^{i phi} a_q
+    //   columns: new p = cs a_p - sn e^{-i phi} a_q,  new q = sn a_p + cs e^{-i phi} a_q
+    // and the rotated pair's off-diagonal element, zero in exact arithmetic,
+    // is set to zero.  A dummy index (q = n for odd n) carries the identity.
+    for (long w = tid; w < nblk + (long)n * half; w += nth) {
+      if (w < nblk) {
+        const Rot Ra = rot[w / half], Rb = rot[w % half];
+        const bool qa = Ra.q < n, qb = Rb.q < n;
+        double2 x[2][2];
+        x[0][0] = A[(long)Ra.p * n + Rb.p];
+        x[0][1] = qb ? A[(long)Ra.p * n + Rb.q] : make_double2(0, 0);
+        x[1][0] = qa ? A[(long)Ra.q * n + Rb.p] : make_double2(0, 0);
+        x[1][1] = qa && qb ? A[(long)Ra.q * n + Rb.q] : make_double2(0, 0);
+        const double2 ea = make_double2(Ra.pr, Ra.pi);
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+          const double2 ap = x[0][c], aq = x[1][c];
+          const double2 eaq = make_double2(ea.x * aq.x - ea.y * aq.y, ea.x * aq.y + ea.y * aq.x);
+          x[0][c] = make_double2(Ra.cs * ap.x - Ra.sn * eaq.x, Ra.cs * ap.y - Ra.sn * eaq.y);
+          x[1][c] = make_double2(Ra.sn * ap.x + Ra.cs * eaq.x, Ra.sn * ap.y + Ra.cs * eaq.y);
+        }
+        const double2 eb = make_double2(Rb.pr, -Rb.pi);
+#pragma unroll
+        for (int rw = 0; rw < 2; rw++) {
+          const double2 ap = x[rw][0], aq = x[rw][1];
+          const double2 eaq = make_double2(eb.x * aq.x - eb.y * aq.y, eb.x * aq.y + eb.y * aq.x);
+          x[rw][0] = make_double2(Rb.cs * ap.x - Rb.sn * eaq.x, Rb.cs * ap.y - Rb.sn * eaq.y);
+          x[rw][1] = make_double2(Rb.sn * ap.x + Rb.cs * eaq.x, Rb.sn * ap.y + Rb.cs * eaq.y);
+        }
+        if (w / half == w % half && !(Ra.cs == 1.0 && Ra.sn == 0.0)) {
+          x[0][1] = make_double2(0, 0);
+          x[1][0] = make_double2(0, 0);
+        }
+        A[(long)Ra.p * n + Rb.p] = x[0][0];
+        if (qb) A[(long)Ra.p * n + Rb.q] = x[0][1];
+        if (qa) A[(long)Ra.q * n + Rb.p] = x[1][0];
+        if (qa && qb) A[(long)Ra.q * n + Rb.q] = x[1][1];
+      } else {
+        const long w2 = w - nblk;
+        const Rot R = rot[w2 / n];
+        const int row = (int)(w2 % n);
+        if (R.q >= n) continue;
+        const double2 ap = V[(long)row * n + R.p], aq = V[(long)row * n + R.q];
+        const double2 e = make_double2(R.pr, -R.pi);
+        const double2 eaq = make_double2(e.x * aq.x - e.y * aq.y, e.x * aq.y + e.y * aq.x);
+        V[(long)row * n + R.p] = make_double2(R.cs * ap.x - R.sn * eaq.x, R.cs * ap.y - R.sn * eaq.y);
+        V[(long)row * n + R.q] = make_double2(R.sn * ap.x + R.cs * eaq.x, R.sn * ap.y + R.cs * eaq.y);
       }
     }
     grid.sync();
@@ -287,18 +305,21 @@ __global__ void k_identity(double2 *V, int n)
 int jacobi_eig_dev(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<double> &w)
 {
   const int m = n + (n & 1);
-  Rot *rot = nullptr;
-  double *off = nullptr;
-  if (cudaMalloc(&rot, sizeof(Rot) * (m / 2 + 1)) != cudaSuccess) return set_err(c, FBSE_ERR_OOM, "jacobi");
-  if (cudaMalloc(&off, 2 * sizeof(double)) != cudaSuccess) { cudaFree(rot); return set_err(c, FBSE_ERR_OOM, "jacobi"); }
+  // rotation table and the two norms, kept in the context between calls
+  const size_t rot_bytes = (sizeof(Rot) * (m / 2 + 1) + 15) / 16 * 16;
+  void *scratch = nullptr;
+  int rc = cached(c, kSlotJacobi, rot_bytes + 2 * sizeof(double), &scratch);
+  if (rc) return rc;
+  Rot *rot = static_cast<Rot *>(scratch);
+  double *off = reinterpret_cast<double *>(static_cast<char *>(scratch) + rot_bytes);
   FBSE_COUNT(1); k_identity<<<256, 256, 0, c->stream>>>(V, n);
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_sweep, 256, 0);
-  long want = ((long)(m / 2) * n * 2 + 255) / 256;
+  const long work = (long)(m / 2) * (m / 2) + (long)n * (m / 2);
+  long want = (work + 255) / 256;
   int blocks = (int)std::min<long>(std::max<long>(1, want), (long)nsm * std::max(1, per_sm));
-  int rc = FBSE_OK;
   double h[2] = {0, 0};
   bool conv = (n < 2);
   for (int sweep = 0; sweep < 60 && !conv; sweep++) {
@@ -319,20 +340,15 @@ int jacobi_eig_dev(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<doubl
   }
   if (!rc && !conv) rc = set_err(c, FBSE_ERR_NOCONV, "jacobi eigensolver did not converge in 60 sweeps");
   if (!rc) {
-    std::vector<double2> d((size_t)n * n);
-    // only the diagonal is needed on the host
+    // only the diagonal is needed on the host: one strided copy (pitch n + 1)
+    std::vector<double2> d((size_t)n);
+    if (cudaMemcpy2DAsync(d.data(), sizeof(double2), A, (size_t)(n + 1) * sizeof(double2), sizeof(double2), (size_t)n,
+                          cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+      rc = set_err(c, FBSE_ERR_CUDA, "jacobi download");
     w.resize(n);
-    for (int i = 0; i < n && !rc; i++) {
-      double2 v;
-      if (cudaMemcpyAsync(&v, A + (long)i * n + i, sizeof(double2), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
-        rc = set_err(c, FBSE_ERR_CUDA, "jacobi download");
-      else d[i] = v;
-    }
-    if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "jacobi download");
-    for (int i = 0; i < n; i++) w[i] = d[i].x;
+    for (int i = 0; i < n && !rc; i++) w[i] = d[i].x;
   }
-  cudaFree(rot);
-  cudaFree(off);
   return rc;
 }
 
