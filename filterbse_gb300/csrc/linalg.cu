@@ -356,7 +356,10 @@ int jacobi_eig_dev(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<doubl
 // rotation with residual epilogue
 //   P[i][l] = sum_j Psi[j][l] C[j][i],  Q[i][l] = sum_j HPsi[j][l] C[j][i]
 //   out[i][l] = P;  part[blk][i] += |Q - E_i P|^2, |P|^2, Re(conj(P) Q)
-// tile: 128 grid elements x 32 output states per CTA, 256 threads
+// tile: 128 grid elements x 32 output states per CTA, 256 threads; the state
+// tiles of one grid tile are consecutive blocks (they share the grid tile's
+// Psi / H Psi through L2, so the states stream from DRAM once), and the next
+// j block is loaded into registers while the current one is multiplied
 // ---------------------------------------------------------------------------
 // PART 2: rotate Psi and H Psi together; PART 0: Psi only (writes out);
 // PART 1: H Psi only, reading the rotated Psi back from out for the residual
@@ -369,10 +372,15 @@ __global__ void __launch_bounds__(256, PART == 2 ? 1 : 2) k_rotate(const double 
                                                 double *__restrict__ part)
 {
   constexpr int TL = 128, TS = 32, TJ = 8;
-  const long l0 = (long)blockIdx.x * TL;
-  const int s0 = blockIdx.y * TS;
+  constexpr int NU = TJ * TL / 256;  // Psi / H Psi tile values per thread
+  static_assert(TJ * TS == 256, "one coefficient per thread and j block");
+  const int nsb = (k + TS - 1) / TS;
+  const long bx = blockIdx.x / nsb;
+  const long l0 = bx * TL;
+  const int s0 = (int)(blockIdx.x % nsb) * TS;
   // complex values as C<T>: one float2 / double2 access per value
   using Elt = typename std::conditional<CPLX, C<T>, T>::type;
+  using Raw = typename std::conditional<CPLX, double2, double>::type;
   __shared__ Elt Ps[TJ][TL];
   __shared__ Elt Hs[TJ][TL];
   __shared__ C<T> Cs[TJ][TS];
@@ -385,33 +393,43 @@ __global__ void __launch_bounds__(256, PART == 2 ? 1 : 2) k_rotate(const double 
 #pragma unroll
     for (int b = 0; b < 4; b++) { pr[a][b] = pim[a][b] = qr[a][b] = qim[a][b] = 0; }
   if (threadIdx.x < TS * 3) red[threadIdx.x / 3][threadIdx.x % 3] = 0;
-  for (int jb = 0; jb < n; jb += TJ) {
-    for (int t = threadIdx.x; t < TJ * TL; t += 256) {
-      const int jj = t / TL, ll = t % TL;
-      const int j = jb + jj;
-      const long l = l0 + ll;
+  Raw rp[NU], rh[NU];
+  double2 rc;
+  auto fetch = [&](int jb) {
+#pragma unroll
+    for (int u = 0; u < NU; u++) {
+      const int t = threadIdx.x + 256 * u;
+      const int j = jb + t / TL;
+      const long l = l0 + t % TL;
       const bool ok = (j < n) && (l < L);
       if constexpr (CPLX) {
-        if constexpr (PART != 1) {
-          const double2 u = ok ? reinterpret_cast<const double2 *>(Psi)[(long)j * L + l] : make_double2(0, 0);
-          Ps[jj][ll] = mk<T>((T)u.x, (T)u.y);
-        }
-        if constexpr (PART != 0) {
-          const double2 w = ok ? reinterpret_cast<const double2 *>(HPsi)[(long)j * L + l] : make_double2(0, 0);
-          Hs[jj][ll] = mk<T>((T)w.x, (T)w.y);
-        }
+        if constexpr (PART != 1) rp[u] = ok ? reinterpret_cast<const double2 *>(Psi)[(long)j * L + l] : make_double2(0, 0);
+        if constexpr (PART != 0) rh[u] = ok ? reinterpret_cast<const double2 *>(HPsi)[(long)j * L + l] : make_double2(0, 0);
       } else {
-        if constexpr (PART != 1) Ps[jj][ll] = ok ? (T)Psi[(long)j * L + l] : T(0);
-        if constexpr (PART != 0) Hs[jj][ll] = ok ? (T)HPsi[(long)j * L + l] : T(0);
+        if constexpr (PART != 1) rp[u] = ok ? Psi[(long)j * L + l] : 0.0;
+        if constexpr (PART != 0) rh[u] = ok ? HPsi[(long)j * L + l] : 0.0;
       }
     }
-    for (int t = threadIdx.x; t < TJ * TS; t += 256) {
-      const int jj = t / TS, ss = t % TS;
-      const int j = jb + jj, s = s0 + ss;
-      const double2 v = (j < n && s < k) ? Cm[(long)j * k + s] : make_double2(0, 0);
-      Cs[jj][ss] = mk<T>((T)v.x, (T)v.y);
+    const int j = jb + threadIdx.x / TS, sc = s0 + threadIdx.x % TS;
+    rc = (j < n && sc < k) ? Cm[(long)j * k + sc] : make_double2(0, 0);
+  };
+  fetch(0);
+  for (int jb = 0; jb < n; jb += TJ) {
+#pragma unroll
+    for (int u = 0; u < NU; u++) {
+      const int t = threadIdx.x + 256 * u;
+      const int jj = t / TL, ll = t % TL;
+      if constexpr (CPLX) {
+        if constexpr (PART != 1) Ps[jj][ll] = mk<T>((T)rp[u].x, (T)rp[u].y);
+        if constexpr (PART != 0) Hs[jj][ll] = mk<T>((T)rh[u].x, (T)rh[u].y);
+      } else {
+        if constexpr (PART != 1) Ps[jj][ll] = (T)rp[u];
+        if constexpr (PART != 0) Hs[jj][ll] = (T)rh[u];
+      }
     }
+    Cs[threadIdx.x / TS][threadIdx.x % TS] = mk<T>((T)rc.x, (T)rc.y);
     __syncthreads();
+    if (jb + TJ < n) fetch(jb + TJ);
 #pragma unroll
     for (int jj = 0; jj < TJ; jj++) {
 #pragma unroll
@@ -492,7 +510,7 @@ __global__ void __launch_bounds__(256, PART == 2 ? 1 : 2) k_rotate(const double 
   if (PART != 0 && threadIdx.x < TS) {
     const int s = s0 + threadIdx.x;
     if (s < k) {
-      double *P = part + ((long)blockIdx.x * k + s) * 3;
+      double *P = part + (bx * k + s) * 3;
       P[0] = red[threadIdx.x][0];
       P[1] = red[threadIdx.x][1];
       P[2] = red[threadIdx.x][2];
@@ -666,7 +684,7 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     FBSE_COUNT(1); k_permute_cols<<<64, 256, 0, c->stream>>>(U, permd, k, Tm);
     // 6. C = X U  (n x k); rotate Psi and HPsi with the residual epilogue
     if ((rc = zgemm_dev(c, n, k, k, X, k, false, Tm, k, false, Cm, k))) break;
-    dim3 gr(nrb, (k + 31) / 32);
+    const dim3 gr((unsigned)(nrb * ((k + 31) / 32)));
     if constexpr (sizeof(T) == 4) {  // FP32: two half-register launches (Psi, then H Psi + residuals)
       if (c->is_complex) {
         k_rotate<T, true, 0><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
