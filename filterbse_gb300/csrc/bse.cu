@@ -303,7 +303,7 @@ static int eh_kernels_t(fbse_ctx *c, const double *psi_qp, long nh, long ne, lon
     if ((rc = conv_batches<T>(c, psi_qp, pr, Q, wk, batch, dpairs, nullptr))) break;
     if ((rc = cgemm_nt<T>(c, P, (int)(ne * ne), Q, (int)(nh * nh), N, c->dv, G))) break;
     k_scatter_direct<<<gridn(nx * nx), 256, 0, c->stream>>>(G, (int)ne, (int)nh, (double2 *)direct);
-    FBSE_CHECK_LAUNCH(c);
+    FBSE_LAUNCH_OR_BREAK(c, rc);
     // ---- exchange: P[(a,i)] = v * rho_ai (ibs order), Q[(b,j)] = rho_jb (jbs order)
     pr.clear();
     for (long a = 0; a < ne; a++)
@@ -315,7 +315,7 @@ static int eh_kernels_t(fbse_ctx *c, const double *psi_qp, long nh, long ne, lon
     if ((rc = conv_batches<T>(c, psi_qp, pr, Q, wk, batch, dpairs, nullptr))) break;
     if ((rc = cgemm_nt<T>(c, P, (int)nx, Q, (int)nx, N, -c->dv, (double2 *)exchange))) break;
     k_lower_only<<<gridn(nx * nx), 256, 0, c->stream>>>((double2 *)exchange, nx);
-    FBSE_CHECK_LAUNCH(c);
+    FBSE_LAUNCH_OR_BREAK(c, rc);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "bse kernels");
   } while (0);
   cudaStreamSynchronize(c->stream);

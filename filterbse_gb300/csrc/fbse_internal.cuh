@@ -124,8 +124,18 @@ extern std::atomic<long> g_launches;
     FBSE_COUNT(1);                          \
     FBSE_CUDA(ctx, cudaGetLastError());     \
   } while (0)
+// the same inside a do { } while (0) block whose exit frees the caller's
+// scratch: records the error in rc and leaves the block with break
+#define FBSE_LAUNCH_OR_BREAK(ctx, rc)                                                                      \
+  if (FBSE_COUNT(1), (rc = ::fbse::launch_status(ctx)) != FBSE_OK) break
 
 int ensure(fbse_ctx *c, void **p, size_t *have, size_t need);
+// FBSE_OK, or the last launch's error recorded in the context
+inline int launch_status(fbse_ctx *c)
+{
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FBSE_OK : set_err(c, FBSE_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+}
 enum CacheSlot { kSlotRing = 0, kSlotHpsi, kSlotRot, kSlotJobStarts, kSlotJobStates, kSlotJacobi };
 inline int cached(fbse_ctx *c, int slot, size_t need, void **out)
 {

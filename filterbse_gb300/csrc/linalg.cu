@@ -665,8 +665,11 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     if (k == 0) { rc = set_err(c, FBSE_ERR_NAN, "orthogonalisation kept no states"); break; }
     std::vector<double> lk(k);
     for (int s = 0; s < k; s++) lk[s] = w[keep[s]];
-    cudaMemcpyAsync(keepd, keep.data(), k * sizeof(int), cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(lam, lk.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (h2d(c->stream, keepd, keep.data(), k * sizeof(int)) != cudaSuccess ||
+        h2d(c->stream, lam, lk.data(), k * sizeof(double)) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "orthogonalisation: basis upload");
+      break;
+    }
     FBSE_COUNT(1); k_build_x<<<64, 256, 0, c->stream>>>(V, n, keepd, lam, k, X);
     // 5. H' = X^H M X  (k x k), Hermitian eigen-decomposition
     if ((rc = zgemm_dev(c, n, k, n, M, n, false, X, k, false, Tm, k))) break;   // Tm = M X   (n x k)
@@ -679,8 +682,11 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     std::sort(perm.begin(), perm.end(), [&](int a, int b) { return e[a] < e[b]; });
     std::vector<double> es(k);
     for (int s = 0; s < k; s++) es[s] = e[perm[s]];
-    cudaMemcpyAsync(permd, perm.data(), k * sizeof(int), cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(Ed, es.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (h2d(c->stream, permd, perm.data(), k * sizeof(int)) != cudaSuccess ||
+        h2d(c->stream, Ed, es.data(), k * sizeof(double)) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "diagonalisation: eigenvalue upload");
+      break;
+    }
     FBSE_COUNT(1); k_permute_cols<<<64, 256, 0, c->stream>>>(U, permd, k, Tm);
     // 6. C = X U  (n x k); rotate Psi and HPsi with the residual epilogue
     if ((rc = zgemm_dev(c, n, k, k, X, k, false, Tm, k, false, Cm, k))) break;
@@ -698,7 +704,7 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
       if (c->is_complex) k_rotate<T, true, 2><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
       else k_rotate<T, false, 2><<<gr, 256, 0, c->stream>>>(psitot, hpsi, n, L, Cm, k, Ed, rot, rpart);
     }
-    FBSE_CHECK_LAUNCH(c);
+    FBSE_LAUNCH_OR_BREAK(c, rc);
     FBSE_COUNT(1); k_sum_rot<<<(k + 127) / 128, 128, 0, c->stream>>>(rpart, nrb, k, rsum);
     std::vector<double> hs(3 * k);
     if (cudaMemcpyAsync(hs.data(), rsum, 3 * k * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
@@ -722,9 +728,12 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
       sigma[s] = std::sqrt(std::fabs(hs[3 * s] / pp - d * d));
     }
     if (rc) break;
-    cudaMemcpyAsync(fac, f.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (h2d(c->stream, fac, f.data(), k * sizeof(double)) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "normalisation: factor upload");
+      break;
+    }
     k_scale_copy<<<4096, 256, 0, c->stream>>>(rot, psitot, stlen, k, fac);
-    FBSE_CHECK_LAUNCH(c);
+    FBSE_LAUNCH_OR_BREAK(c, rc);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "ortho/diag/sigma");
   } while (0);
   cudaStreamSynchronize(c->stream);

@@ -334,6 +334,13 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
   float *b0h = al + img_a, *b0l = b0h + img_b, *b1h = b0l + img_b, *b1l = b1h + img_b;
   float *p0 = b1l + img_b, *p1 = p0 + part_n;
   int rc = FBSE_OK;
+  // launch errors end the call through the cleanup below (no early return)
+  auto launched = [&](int nk) {
+    FBSE_COUNT(nk);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, std::string("tensor-core launch: ") + cudaGetErrorString(e));
+    return e == cudaSuccess;
+  };
   // FBSE_TC_TERMS=1 keeps only the hi x hi product (for accuracy studies)
   const int terms = (getenv("FBSE_TC_TERMS") && atoi(getenv("FBSE_TC_TERMS")) == 1) ? 1 : 3;
   do {
@@ -351,26 +358,30 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
       const long nsp = (nkb + kbs - 1) / kbs;
       float *q0 = p0 + (size_t)ch * sps * mp * np, *q1 = p1 + (size_t)ch * sps * mp * np;
       if (nsp < sps) {  // a short last chunk: its unused partial slots must read as zero
-        cudaMemsetAsync(q0 + (size_t)nsp * mp * np, 0, (size_t)(sps - nsp) * mp * np * sizeof(float), c->stream);
-        cudaMemsetAsync(q1 + (size_t)nsp * mp * np, 0, (size_t)(sps - nsp) * mp * np * sizeof(float), c->stream);
+        const size_t tail = (size_t)(sps - nsp) * mp * np * sizeof(float);
+        if (cudaMemsetAsync(q0 + (size_t)nsp * mp * np, 0, tail, c->stream) != cudaSuccess ||
+            cudaMemsetAsync(q1 + (size_t)nsp * mp * np, 0, tail, c->stream) != cudaSuccess) {
+          rc = set_err(c, FBSE_ERR_CUDA, "tensor-core product: partial clear");
+          break;
+        }
       }
       tc::k_tc_images<S><<<grid_of(mp * nkb * 8), 256, 0, c->stream>>>(A, ma, L, 0, mp, nkb, k0, ah, al);
       tc::k_tc_images<S><<<grid_of(np * nkb * 8), 256, 0, c->stream>>>(B, nb, L, mb0, np, nkb, k0, b0h, b0l);
       tc::k_tc_images<S><<<grid_of(np * nkb * 8), 256, 0, c->stream>>>(B, nb, L, mb1, np, nkb, k0, b1h, b1l);
-      FBSE_COUNT(3);
+      if (!launched(3)) break;
       dim3 g((unsigned)(mp / kBM), (unsigned)(np / kBN), (unsigned)nsp);
       tc::k_tc_gemm_nt<<<g, 128, smem, c->stream>>>(ah, al, b0h, b0l, nkb, kbs, q0, mp, np, terms, status);
-      FBSE_CHECK_LAUNCH(c);
+      if (!launched(1)) break;
       if (conj_a) {
         tc::k_tc_images<S><<<grid_of(mp * nkb * 8), 256, 0, c->stream>>>(A, ma, L, 1, mp, nkb, k0, ah, al);
-        FBSE_COUNT(1);
+        if (!launched(1)) break;
       }
       tc::k_tc_gemm_nt<<<g, 128, smem, c->stream>>>(ah, al, b1h, b1l, nkb, kbs, q1, mp, np, terms, status);
-      FBSE_CHECK_LAUNCH(c);
+      if (!launched(1)) break;
     }
     if (rc) break;
     tc::k_tc_reduce<<<grid_of((long)ma * nb), 256, 0, c->stream>>>(p0, p1, (int)nsplit, mp, np, ma, nb, scale, out);
-    FBSE_CHECK_LAUNCH(c);
+    if (!launched(1)) break;
     int hs = 0;
     if (d2h(c->stream, &hs, status, sizeof(int)) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "tensor-core GEMM"); break; }
     if (hs) rc = set_err(c, FBSE_ERR_NOCONV, "tensor-core GEMM: a wait timed out");
