@@ -53,7 +53,7 @@ int energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *em
 int ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma);
 
 // per-axis 0.5 k^2 / N exactly as init_kvec + build_grid_ksqr
-// (filter_mpi/init.c:904-915, 318-336)
+// (filter_mpi/init.c:1383-1394, 318-336)
 static void axis_k2(long n, double dk, double ngrid_1, std::vector<double> &k)
 {
   k.assign(n, 0.0);
@@ -102,7 +102,7 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
   if (g->nx < 1 || g->ny < 1 || g->nz < 1) return set_err(c, FBSE_ERR_ARG, "grid sizes must be positive");
   if (g->nspin != 1 && g->nspin != 2) return set_err(c, FBSE_ERR_ARG, "nspin must be 1 or 2");
   if (g->so && (g->nspin != 2 || !g->is_complex))
-    return set_err(c, FBSE_ERR_ARG, "spin-orbit requires complex spinors (read.c:927-936)");
+    return set_err(c, FBSE_ERR_ARG, "spin-orbit requires complex spinors (read.c:914-921)");
   if (g->nspin == 2 && !g->is_complex) return set_err(c, FBSE_ERR_ARG, "spinors must be complex");
   if ((g->so || g->nl) && !pj) return set_err(c, FBSE_ERR_ARG, "projector table required when SO or NL is on");
   if (!pot) return set_err(c, FBSE_ERR_ARG, "local potential required");

@@ -246,7 +246,7 @@ static double im_dot_conj(const double *mu, const double *m)
  * exchange: (a, i, b, j) order, lower triangle only (coulomb.c:586-600). */
 static void kline(FILE *f, long a, long b, long i, long j, long ibs, long jbs, const double *v, int real)
 {
-  if (real) /* bse_real/coulomb.c:355, 580: one value */
+  if (real) /* bse_real/coulomb.c:352, 583: one value */
     fprintf(f, "%03ld %03ld %03ld %03ld %ld %ld %.12f\n", a, b, i, j, ibs, jbs, v[0]);
   else
     fprintf(f, "%03ld %03ld %03ld %03ld %ld %ld %.12f %.12f\n", a, b, i, j, ibs, jbs, v[0], v[1]);

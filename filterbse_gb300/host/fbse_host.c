@@ -49,7 +49,7 @@ double fbse_ran(long *seed)
   return (u > 1.0 - 1.2e-7) ? 1.0 - 1.2e-7 : u;
 }
 
-/* init_psi (filter_mpi/init.c:777-826): one spin block of U[-1, 1] values in
+/* init_psi (filter_mpi/init.c:1256-1307): one spin block of U[-1, 1] values in
  * grid order (re then im per point for complex jobs), normalised to 1 with dv
  * (normalize, filter_mpi/norm.c:42-79).  psi is interleaved complex.
  * Returns the advanced seed. */

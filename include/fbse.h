@@ -121,7 +121,7 @@ int fbse_hnorm(fbse_ctx *ctx, const void *psi_in, void *psi_out, long nstates, d
  * coefficients (host, interleaved; imaginary parts must be 0, which
  * gen_newton_coeff always produces); psi0: [nstart] psitot states (device);
  * filtered: [nstart][m] psitot states (device) -- the psi_rank layout
- * (ns_block = jns*m*stlen, filter_mpi/filter.c:231). */
+ * (ns_block = jns*m*stlen, filter_mpi/filter.c:253). */
 int fbse_newton_filter(fbse_ctx *ctx, const double *zn, const double *an, long ncheby, long m, double vmin,
                        double de, const double *psi0, long nstart, double *filtered);
 
@@ -284,7 +284,7 @@ int fbse_newton_coeff(long ncheby, long m, const double *zn, const double *targe
  * process-wide state.  Returns one U(0,1) draw and advances *seed. */
 double fbse_ran(long *seed);
 
-/* init_filter_states (filter_mpi/init.c:659-774) without file output:
+/* init_filter_states (filter_mpi/init.c:1138-1255) without file output:
  * n_filters random starts into psitot states (host, nspin*ngrid*complex_idx
  * doubles each), each spin block drawn and normalised on its own.  Returns the
  * advanced seed; seeds_out (may be NULL) receives the n_filters*nspin seeds the

@@ -81,7 +81,7 @@ long orc_ran_fill(long seed, long n, double *out)
   return seed;
 }
 
-/* init_psi (filter_mpi/init.c:777-826): values U[-1,1] over the grid in
+/* init_psi (filter_mpi/init.c:1256-1307): values U[-1,1] over the grid in
  * jz, jy, jx order (two draws per point when complex), then normalise the
  * block to 1 with dv (norm.c:10-35, 42-79).  psi is interleaved complex.
  * Returns the updated seed. */
@@ -179,7 +179,7 @@ void orc_newton_coeff(long ncheby, long m, const double *samp, const double *tar
 /* Grid, k^2 table, energy targets                                          */
 /* ------------------------------------------------------------------------- */
 
-/* init_kvec (filter_mpi/init.c:904-915) followed by the per-axis 0.5 k^2/N
+/* init_kvec (filter_mpi/init.c:1383-1394) followed by the per-axis 0.5 k^2/N
  * scaling of build_grid_ksqr (init.c:318-336). */
 void orc_axis_ksqr(long n, double dk, double ngrid_1, double *k2)
 {

@@ -90,14 +90,14 @@ def ran_fill(seed: int, n: int, out: bool = True):
 
 
 def init_psi(seed: int, ngrid: int, is_complex: bool, dv: float):
-    """init_psi (filter_mpi/init.c:777-826): one normalised random block."""
+    """init_psi (filter_mpi/init.c:1256-1307): one normalised random block."""
     psi = np.empty(2 * ngrid)
     s = lib().orc_init_psi(_p(psi), seed, ngrid, int(is_complex), dv)
     return psi.view(np.complex128), s
 
 
 def init_filter_states(seed: int, n_filters: int, ngrid: int, nspin: int, is_complex: bool, dv: float):
-    """init_filter_states (filter_mpi/init.c:659-774): n_filters random starts,
+    """init_filter_states (filter_mpi/init.c:1138-1255): n_filters random starts,
     each spin block drawn and normalised separately; returns ([n][nspin*ngrid], seeds)."""
     out = np.empty((n_filters, nspin * ngrid), np.complex128)
     seeds = []

@@ -318,7 +318,7 @@ def test_dropin_bse_real_on_cdse_filter_output(cuda, tmp_path):
     ex = np.loadtxt(tmp_path / "exciton.dat")
     assert ex.shape == (nx, 7)
     dl = np.loadtxt(tmp_path / "direct-0.dat")
-    assert dl.shape == (nx * nx, 7)  # one value per element (bse_real/coulomb.c:355)
+    assert dl.shape == (nx * nx, 7)  # one value per element (bse_real/coulomb.c:352)
     assert np.loadtxt(tmp_path / "OS0.dat", skiprows=1).shape == (nx, 8)
     assert np.loadtxt(tmp_path / "OS.dat").shape == (nx, 7)
     assert (tmp_path / "bs.dat").exists() and (tmp_path / "BSEcoeff.dat").exists()

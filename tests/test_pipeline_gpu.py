@@ -57,8 +57,8 @@ def test_cdse22_real_matches_reference_eval(fbse, cuda):
     targets = _targets(-0.31, -0.24, -0.15, -0.06, 10, 6)
     (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 1, False)
     # run.dat:140 of the reference run: Emin = -1.13271, Emax = 12.3281.  Both
-    # iterations stop at a relative change below 1e-6 per step (energy.c:229,
-    # 285), not at the extremum, so the stopping values agree only to ~1e-3.
+    # iterations stop at a relative change below 1e-6 per step (energy.c:239,
+    # 282), not at the extremum, so the stopping values agree only to ~1e-3.
     assert abs(emin - (-1.13271)) < 3e-3 and abs(emax - 12.3281) < 1e-3 * 12.3281
     ref = np.loadtxt(os.path.join(GOLD, "cdse22", "eval.dat"))
     r, d = _match(ref, ev, sg, 1e-5, 1e-4, 1e-5)
