@@ -203,7 +203,7 @@ using namespace fbse;
 
 extern "C" {
 
-int fbse_version(void) { return 1; }
+int fbse_version(void) { return FBSE_ABI_VERSION; }
 
 long fbse_launch_count(void) { return g_launches.load(); }
 

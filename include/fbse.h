@@ -33,6 +33,9 @@
 extern "C" {
 #endif
 
+/* ABI version: fbse_version() returns the value the library was built with */
+#define FBSE_ABI_VERSION 1
+
 #define FBSE_OK 0
 #define FBSE_ERR_ARG (-1)         /* invalid argument or size */
 #define FBSE_ERR_CUDA (-2)        /* CUDA runtime error (message has details) */

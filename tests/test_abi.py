@@ -28,7 +28,9 @@ def test_exports_every_declared_symbol(fbse):
 
 
 def test_version(fbse):
-    assert fbse.load().fbse_version() >= 1
+    src = open(os.path.join(ROOT, "include", "fbse.h")).read()
+    want = int(re.search(r"#define FBSE_ABI_VERSION (\d+)", src).group(1))
+    assert fbse.load().fbse_version() == want
 
 
 def test_context_without_gpu_fails_cleanly(fbse):
