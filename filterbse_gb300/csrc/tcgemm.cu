@@ -341,8 +341,7 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
     if (e != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, std::string("tensor-core launch: ") + cudaGetErrorString(e));
     return e == cudaSuccess;
   };
-  // FBSE_TC_TERMS=1 keeps only the hi x hi product (for accuracy studies)
-  const int terms = (getenv("FBSE_TC_TERMS") && atoi(getenv("FBSE_TC_TERMS")) == 1) ? 1 : 3;
+  const int terms = 3;  // hi x hi + hi x lo + lo x hi
   do {
     if (cudaMemsetAsync(status, 0, sizeof(int), c->stream) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "memset"); break; }
     const size_t smem = (size_t)kStages * kStageBytes + 1024;
