@@ -182,15 +182,20 @@ def _check_ang_stats(tmp, ex, ref):
     names = ("spins.dat", "orbital.dat")
     mine_x = [totals(tmp / f) for f in names]
     ref_x = [totals(os.path.join(g, f)) for f in names]
-    nmatch = 0
-    for cl in _groups(ref[:, 1]):
+    # clusters of excitons within 1e-4 Ha of each other: a sum over a cluster
+    # does not depend on how the runs mix its members, and members up to
+    # ~1e-4 Ha apart mix differently (angles up to ~1e-3) under last-bit
+    # changes of the states (the projector scatter accumulates with float
+    # atomics); the remaining gaps of the spectrum are above 1.1e-4 Ha
+    nmatch, worst_x = 0, 0.0
+    for cl in _groups(ref[:, 1], 1e-4):
         if np.all(np.abs(ex[cl, 1] - ref[cl, 1]) < 1e-6):
             nmatch += 1
             for m_, r_ in zip(mine_x, ref_x):
-                worst = max(worst, abs(m_[cl].sum() - r_[cl].sum()) / max(1.0, abs(r_[cl].sum())))
-    print(f"[fbse_bse cspbi3] angular statistics: {len(levels)} qp levels, {nmatch} exciton clusters, "
-          f"max rel dev {worst:.2e}")
-    assert nmatch >= 10 and worst < 1e-3
+                worst_x = max(worst_x, abs(m_[cl].sum() - r_[cl].sum()) / max(1.0, abs(r_[cl].sum())))
+    print(f"[fbse_bse cspbi3] angular statistics: {len(levels)} qp levels (max dev {worst:.2e}), "
+          f"{nmatch} exciton clusters (max rel dev {worst_x:.2e})")
+    assert nmatch >= 10 and worst < 1e-3 and worst_x < 1e-3
 
 
 def _small(extra=""):
