@@ -273,7 +273,10 @@ def run_gpu(args):
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "H psi (5 FFT passes + projector gather/scatter), 16 spinor states",
+                     "traffic": HPSI_DRAM_BYTES if (args.radius, args.nstart) == (15.0, 16) else None,
+                     "traffic_source": "ncu capture of the five H psi kernels on this workload "
+                                       "(profiles/hpsi_kernels_cdse3nm_128cubed_mixed_16spinor.md)",
+                     "kernel": "H psi (5 FFT passes + projector gather/scatter), 16 spinor states",
                      "ms_per_launch": t_h * 1e3, "algorithmic_bytes": bytes_h, "peak_kind": peak_kind},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
@@ -368,6 +371,12 @@ def run_reference(args):
                                       f"{n_conv} as produced by the FP64 pipeline on this workload"},
            "e2e": {"value": val, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+# DRAM bytes read + written by one batched H psi of the 16 spinor starts of the
+# 3 nm CdSe dot (the five kernels of one H psi, one ncu capture with cold
+# caches: planes 1024 + 1038 + 1627 MB, projector gather 582 MB, scatter 761 MB)
+HPSI_DRAM_BYTES = 5.032e9
 
 
 def main():
