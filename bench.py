@@ -192,7 +192,7 @@ def run_gpu(args):
             counts.append(count_converged(ev, sg, ev64, sg64))
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    launches = (F.launch_count() - l0) / max(1, args.steps)
+    launches = F.launch_count() - l0  # all kernels of the K timed steps
     t_step = float(np.mean(times))
     n_conv = int(np.median(counts))
     log(f"[mixed] step {t_step * 1e3:.1f} ms, converged {counts}, Ritz pairs {nk}, fp64-run {t_fp64:.1f}s")
@@ -273,6 +273,7 @@ def run_gpu(args):
         "e2e": {"value": tot_e2e / t_e2e_max, "unit": "eigenpairs/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
+        "gpu_launches_per_step": int(round(launches / max(1, args.steps))),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": HPSI_DRAM_BYTES if (args.radius, args.nstart) == (15.0, 16) else None,
                      "traffic_source": "ncu capture of the five H psi kernels on this workload "
