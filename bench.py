@@ -250,7 +250,8 @@ def run_gpu(args):
             dist.destroy_process_group()
         return
     # the CPU port is FP64: it converges what the FP64 pipeline converges
-    cpu = cpu_baseline(dot, args, int(np.sum(sg64 <= SIGMA_CUT)), nk64, sample_states=1)
+    n64 = int(np.sum(sg64 <= SIGMA_CUT))
+    cpu = cpu_baseline(dot, args, n64, nk64, sample_states=1)
     out = {
         "metric": METRIC,
         "value": tot_conv / t_max,
@@ -268,6 +269,8 @@ def run_gpu(args):
                                f"grid {g.nx}x{g.ny}x{g.nz} @0.5 bohr, {ns} starts x {m} targets, nCheby {nc}",
                    "grid": [g.nx, g.ny, g.nz], "n_states": ns * m, "ncheby": nc,
                    "converged_per_step": n_conv, "ritz_pairs": int(nk), "fp64_run_s": t_fp64,
+                   "fp64_converged": n64, "fp64_eigenpairs_per_s": n64 / t_fp64,
+                   "mixed_over_fp64": (n_conv / t_step) / (n64 / t_fp64) if n64 else None,
                    "energy_range_s": t_range, "l2": "working set >> L2 (no flush needed)",
                    "parallelism": f"replicas x{world} (independent starts per GPU)"},
         "e2e": {"value": tot_e2e / t_e2e_max, "unit": "eigenpairs/s", "h2d_bytes_per_step": h2d,
