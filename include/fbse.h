@@ -108,6 +108,14 @@ int fbse_sync(fbse_ctx *ctx);
 void *fbse_stream(fbse_ctx *ctx);
 
 /* ---- H psi ------------------------------------------------------------------
+ * fbse_hpsi and fbse_hnorm only enqueue kernels on the context's stream (no
+ * host synchronisation); the first call sizes their scratch and sets kernel
+ * attributes.  The composite calls below (filter, energy range, orthogonal-
+ * isation / diagonalisation / sigma, the BSE stages) synchronise with the host
+ * between phases (eigensolver sweeps, convergence checks, small host-side
+ * steps) and return with their results on the host or complete on the device.
+ * Capturing fbse_hpsi into a CUDA graph is not exercised by this build's tests.
+ *
  * Replaces p_hamiltonian (filter_mpi/phamiltonian.c:10-60) for a batch:
  * psi_out[s] = H psi_in[s] for nstates zomplex states.  For real jobs the two
  * channels are two independent real states (H is real), so a real state in
