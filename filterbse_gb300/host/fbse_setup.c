@@ -584,7 +584,7 @@ int fbse_build_nlc(long nx, long ny, long nz, const double *gx, const double *gy
           if (!(d2 < rcut2)) continue;
           const size_t e = (size_t)a * npts + cnt;
           jxyz[e] = (int)(nx * (ny * jz + jy) + jx);
-          /* Y_1m with the reference's EPSDX shifts (init.c:540-560) */
+          /* Y_1m with the reference's EPSDX shifts (init.c:1002-1040) */
           double r_1 = 1.0 / sqrt(ddx * ddx + dy * dy + dzeps * dzeps);
           y1[e * 6 + 2] = tmp1 * dzeps * r_1;
           y1[e * 6 + 3] = 0.0;
