@@ -15,8 +15,8 @@ Recorded choices (the reference does not fix them):
     Cd, P2 at 0.25 from Se (the 2.2 nm CdSe example places them at 2.74 and
     1.24-1.49 bohr of a 4.97 bohr bond);
   * local potentials: the reference's shipped II-VI tables (potCd, potSe,
-    potP1, potP2) -- the BASELINE form-factor parameters are not given, and
-    the shipped tables are the recorded alternative;
+    potP1, potP2) -- the workload's form-factor parameters are not published,
+    and the shipped tables stand in for them;
   * spin-orbit: SO_par = 0.01 for Cd and Se, NL parameters 0 (no NL term).
 """
 from __future__ import annotations
