@@ -11,7 +11,7 @@
 #define FBSE_NPROJ 5       /* ist->nproj default, filter_mpi/read.c:75 */
 #define FBSE_MAX_TYPES 32
 
-/* the subset of filter_mpi/input.par this build runs (read.c:23-112 defaults) */
+/* the subset of filter_mpi/input.par this library runs (read.c:23-112 defaults) */
 typedef struct {
   long nx, ny, nz;            /* requested minimum grid (0: from the atoms) */
   double dx, dy, dz;

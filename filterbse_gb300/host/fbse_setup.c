@@ -44,7 +44,7 @@ static const char *k_ignored[] = {"nThreads", "hamThreads", "nestedOMP", "useFas
                                   "fftWisdomDir", "saveOutput", "calcPotOverlap",
                                   "retryFilter", "centerConf", "noTimeRev", "psiZeroCut",
                                   "calcDarkStates", "timingSpecs", "crystalStructure", "outmostMaterial", NULL};
-/* keys whose non-zero value selects a path this build does not implement */
+/* keys whose non-zero value selects a path this library does not implement */
 static const char *k_unsupported[] = {"periodic", "useStrain", "longRange", "localStructureDependent",
                                       "useGaussianBasis", "readProj",
                                       "restartFromCheckpoint", "interpolatePot", "calcSpinAngStat", NULL};
@@ -131,7 +131,7 @@ int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, 
       if (!rc && lv == 1 && (fscanf(f, "%ld", &p->n_states_for_sigma) != 1 || p->n_states_for_sigma < 1)) rc = -1;
     } else if (in_list(key, k_unsupported)) {
       if (parse_double(val, &dv) == 0 && dv != 0.0) {
-        seterr(err, errlen, "input.par key not supported by this build (set it to 0)", key);
+        seterr(err, errlen, "input.par key not supported by this library (set it to 0)", key);
         fclose(f);
         return -1;
       }

@@ -18,7 +18,7 @@ its own starts).  This module is the host-side exchange of that step:
 Every collective first checks in through the process group's store, with a
 deadline: a rank that died or never arrived is reported by number
 (``ShardError``) instead of hanging the others.  Tested with gloo ranks on
-the CPU; the GPU machines of this build hold one GPU each, so the benchmark runs
+the CPU; it has not run on more than one GPU, and the benchmark runs
 independent replicas.
 """
 from __future__ import annotations

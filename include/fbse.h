@@ -42,7 +42,7 @@ extern "C" {
 #define FBSE_ERR_OOM (-3)         /* device allocation failed */
 #define FBSE_ERR_NAN (-4)         /* zero or NaN norm (filter_mpi/norm.c:150-159) */
 #define FBSE_ERR_STATE (-5)       /* call out of order / missing setup */
-#define FBSE_ERR_UNSUPPORTED (-6) /* configuration not supported by this build */
+#define FBSE_ERR_UNSUPPORTED (-6) /* configuration not supported by this library */
 #define FBSE_ERR_NOCONV (-7)      /* an iterative solver hit its iteration limit */
 
 enum { FBSE_FP64 = 0, FBSE_MIXED = 1 };
@@ -114,7 +114,7 @@ void *fbse_stream(fbse_ctx *ctx);
  * isation / diagonalisation / sigma, the BSE stages) synchronise with the host
  * between phases (eigensolver sweeps, convergence checks, small host-side
  * steps) and return with their results on the host or complete on the device.
- * Capturing fbse_hpsi into a CUDA graph is not exercised by this build's tests.
+ * Capturing fbse_hpsi into a CUDA graph is not exercised by the tests.
  *
  * Replaces p_hamiltonian (filter_mpi/phamiltonian.c:10-60) for a batch:
  * psi_out[s] = H psi_in[s] for nstates zomplex states.  For real jobs the two

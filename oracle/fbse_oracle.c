@@ -1,8 +1,8 @@
 /*
  * fbse_oracle.c -- CPU restatement of FilterBSE's filter hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA path is
- * compared against; only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * TEST INFRASTRUCTURE ONLY.  This file is the reference restatement that the
+ * CUDA path is compared against; only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline leg may load it.  Nothing in filterbse_gb300/ links or calls it.
  *
  * Every function restates one reference function in plain FP64 C, in the

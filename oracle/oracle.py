@@ -1,6 +1,6 @@
 """FP64 CPU oracle for FilterBSE's filter hot path (TEST INFRASTRUCTURE ONLY).
 
-This module is the checker the CUDA path is compared against.  Only tests/,
+This module is the reference restatement the CUDA path is compared against.  Only tests/,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import it;
 the product package ``filterbse_gb300`` never does.
 
