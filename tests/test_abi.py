@@ -27,6 +27,40 @@ def test_exports_every_declared_symbol(fbse):
     assert set(names) <= set(fbse.EXPORTED) | set(names)
 
 
+def test_null_context_is_an_argument_error(fbse):
+    """Every entry point that takes a context returns FBSE_ERR_ARG for a NULL
+    context (and NULL buffers, zero sizes) without touching a device; argument
+    types come from the header's declarations."""
+    import ctypes
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "fbse.h")).read(), flags=re.S)
+    decls = re.findall(r"\b(?:int|long|double|void|const char)\s*\*?\s*(fbse_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src)
+    assert len(decls) == len(_declared())
+    L = ctypes.CDLL(fbse.load()._name)
+    checked = 0
+    for name, params in decls:
+        ps = [p.strip() for p in params.split(",") if p.strip() and p.strip() != "void"]
+        if not ps or not ps[0].startswith("fbse_ctx") or name in ("fbse_destroy", "fbse_last_error", "fbse_stream"):
+            continue
+        types, args = [], []
+        for p in ps:
+            if "*" in p:
+                types.append(ctypes.c_void_p); args.append(None)
+            elif "double" in p:
+                types.append(ctypes.c_double); args.append(0.0)
+            elif "size_t" in p:
+                types.append(ctypes.c_size_t); args.append(0)
+            elif "long" in p:
+                types.append(ctypes.c_long); args.append(0)
+            else:
+                assert "int" in p, (name, p)
+                types.append(ctypes.c_int); args.append(0)
+        fn = getattr(L, name)
+        fn.argtypes, fn.restype = types, ctypes.c_int
+        assert fn(*args) == -1, name  # FBSE_ERR_ARG
+        checked += 1
+    assert checked >= 20
+
+
 def test_version(fbse):
     src = open(os.path.join(ROOT, "include", "fbse.h")).read()
     want = int(re.search(r"#define FBSE_ABI_VERSION (\d+)", src).group(1))
