@@ -98,6 +98,13 @@ def load() -> ctypes.CDLL:
                                           ctypes.c_double, ctypes.c_long, ctypes.POINTER(ctypes.c_long)]
     L.fbse_init_filter_states.restype = ctypes.c_long
     L.fbse_launch_count.restype = ctypes.c_long
+    L.fbse_launch_count.argtypes = []
+    L.fbse_version.argtypes = []
+    L.fbse_alloc.argtypes = [_VP, ctypes.POINTER(_VP), ctypes.c_size_t]
+    L.fbse_free.argtypes = [_VP, _VP]
+    L.fbse_upload.argtypes = [_VP, _VP, _VP, ctypes.c_size_t]
+    L.fbse_download.argtypes = [_VP, _VP, _VP, ctypes.c_size_t]
+    L.fbse_normalize_all_noalloc.argtypes = [_VP, _VP, ctypes.c_long, _VP]
     L.fbse_filter_job.argtypes = [_VP, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_double, ctypes.c_double, _D,
                                   ctypes.c_long, ctypes.c_double, ctypes.POINTER(ctypes.c_long), _D, _D, _D]
     L.fbse_bse_potentials.argtypes = [_VP, _D, _D, _D] + [ctypes.c_double] * 6 + [_VP, _VP]
