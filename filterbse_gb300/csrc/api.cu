@@ -191,6 +191,49 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
     if ((rc = upload(c, &p.sopf, so.data(), so.size()))) return rc;
     if ((rc = upload(c, &p.nlpf, nlr.data(), nlr.size()))) return rc;
     if ((rc = upload(c, &p.sgn, sg.data(), sg.size()))) return rc;
+    // point-major copy (counting sort by grid index; entries of one point in
+    // increasing atom order because atoms are visited in order)
+    {
+      size_t nent = 0;
+      for (long a = 0; a < p.nat; a++) nent += (size_t)pj->nl[a];
+      if (nent > 2147483647u) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector table too large");
+      std::vector<int> start((size_t)c->ngrid + 1, 0);
+      for (long a = 0; a < p.nat; a++)
+        for (long e = 0; e < pj->nl[a]; e++) start[(size_t)pj->jxyz[a * p.npts + e] + 1]++;
+      std::vector<int> cj, cb;
+      for (long j = 0; j < c->ngrid; j++)
+        if (start[j + 1]) cj.push_back((int)j);
+      for (long j = 0; j < c->ngrid; j++) start[j + 1] += start[j];  // start[j] = first entry of point j
+      for (size_t k = 0; k < cj.size(); k++) cb.push_back(start[cj[k]]);
+      cb.push_back((int)nent);
+      std::vector<int> pa(nent ? nent : 1, 0);
+      std::vector<double> py((nent ? nent : 1) * 6, 0.0), ps((nent ? nent : 1) * p.nproj, 0.0),
+          pn((nent ? nent : 1) * p.nproj, 0.0);
+      for (long a = 0; a < p.nat; a++)
+        for (long e = 0; e < pj->nl[a]; e++) {
+          const size_t i = a * p.npts + e;
+          const size_t k = (size_t)start[pj->jxyz[i]]++;
+          pa[k] = (int)a;
+          for (int m = 0; m < 3; m++)
+            for (int q = 0; q < 2; q++) py[(m * nent + k) * 2 + q] = y1[(m * ne + i) * 2 + q];
+          for (int q = 0; q < p.nproj; q++) {
+            ps[q * nent + k] = so[q * ne + i];
+            pn[q * nent + k] = nlr[q * ne + i];
+          }
+        }
+      p.ncov = (long)cj.size();
+      p.nent = (long)nent;
+      if (cj.empty()) cj.push_back(0);
+      if ((rc = upload(c, &p.cov_j, cj.data(), cj.size()))) return rc;
+      if ((rc = upload(c, &p.cov_beg, cb.data(), cb.size()))) return rc;
+      if ((rc = upload(c, &p.pe_atom, pa.data(), pa.size()))) return rc;
+      if ((rc = upload(c, &p.pe_y1, py.data(), py.size()))) return rc;
+      if ((rc = upload(c, &p.pe_sop, ps.data(), ps.size()))) return rc;
+      if ((rc = upload(c, &p.pe_nlp, pn.data(), pn.size()))) return rc;
+      if ((rc = upload(c, &p.pe_y1f, py.data(), py.size()))) return rc;
+      if ((rc = upload(c, &p.pe_sopf, ps.data(), ps.size()))) return rc;
+      if ((rc = upload(c, &p.pe_nlpf, pn.data(), pn.size()))) return rc;
+    }
     FBSE_CUDA(c, cudaMalloc(&p.LS, 36 * sizeof(double2)));
     FBSE_CUDA(c, cudaMemcpy(p.LS, ls, 36 * sizeof(double2), cudaMemcpyHostToDevice));
   }
@@ -238,7 +281,8 @@ void fbse_destroy(fbse_ctx *c)
   for (int a = 0; a < 3; a++) free_axis(c->ax[a]);
   void *bufs[] = {c->dstatus, c->k2x, c->k2y, c->k2z, c->k2xf, c->k2yf, c->k2zf, c->pot64, c->pot32, c->wk, c->coef, c->tmp, c->red,
                   c->proj.nl_cnt, c->proj.jxyz, c->proj.y1, c->proj.sop, c->proj.nlp, c->proj.sgn, c->proj.LS,
-                  c->proj.y1f, c->proj.sopf, c->proj.nlpf};
+                  c->proj.y1f, c->proj.sopf, c->proj.nlpf, c->proj.cov_j, c->proj.cov_beg, c->proj.pe_atom,
+                  c->proj.pe_y1, c->proj.pe_sop, c->proj.pe_nlp, c->proj.pe_y1f, c->proj.pe_sopf, c->proj.pe_nlpf};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : c->cache)

@@ -74,6 +74,16 @@ struct ProjDev {
   int *sgn = nullptr;         // [nat*nproj]
   double2 *LS = nullptr;      // [36]
   float *y1f = nullptr, *sopf = nullptr, *nlpf = nullptr;  // FP32 copies for the mixed path
+  // point-major copy of the table for the scatter: the ncov grid points that
+  // lie in at least one sphere in increasing grid index (cov_j), each with its
+  // entries cov_beg[k] .. cov_beg[k+1]-1 in increasing atom order; per entry
+  // the atom (pe_atom), Y_1m and the radial values in the same structure-of-
+  // arrays form as above.  One thread owns each covered point, so the scatter
+  // adds in a fixed order and needs no atomics.
+  long ncov = 0, nent = 0;
+  int *cov_j = nullptr, *cov_beg = nullptr, *pe_atom = nullptr;
+  double *pe_y1 = nullptr, *pe_sop = nullptr, *pe_nlp = nullptr;
+  float *pe_y1f = nullptr, *pe_sopf = nullptr, *pe_nlpf = nullptr;
 };
 
 }  // namespace fbse
@@ -98,6 +108,7 @@ struct fbse_ctx {
   void *tmp = nullptr; size_t tmp_bytes = 0;     // general
   double *red = nullptr; size_t red_bytes = 0;   // reduction partials
   int *dstatus = nullptr;                        // device error flags of kernels with bounded waits
+  int tc_poisoned = 0;  // a tensor-core wait timed out: MMAs may still be in flight, the path is refused
   // large buffers kept between calls (grown on demand, freed by fbse_destroy):
   // the Newton ring, the Rayleigh-Ritz H psi and rotated states, the
   // filter job's device copies of the starts and filtered states

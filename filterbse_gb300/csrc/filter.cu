@@ -553,11 +553,16 @@ int energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *em
 // ---------------------------------------------------------------------------
 // normalize_all without any allocation: the partial sums, norms, scale
 // factors and the error key live in one file-scope device array.  Its device
-// address is looked up once per device (cudaGetSymbolAddress, with that
-// device current) on the first call.  Only the error key must start at a
-// known value; it is set on the stream at the start of every call.  The
-// array is shared by every context on the device, so overlapping calls race.
+// address is looked up (cudaGetSymbolAddress, with the caller's device
+// current) on the first call in each CUDA context -- the device's primary
+// context for runtime-API callers -- and kept per context id, so a device
+// reset or another context gets its own lookup.  Only the error key must start
+// at a known value; it is set on the stream at the start of every call.  The
+// array is shared by every fbse context on the device, so overlapping calls
+// race.
 // ---------------------------------------------------------------------------
+
+#include <cuda.h>  // CUcontext / CUresult types only; the driver is reached through the runtime
 
 #include <mutex>
 
@@ -571,7 +576,15 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 
 namespace {
 std::mutex g_noalloc_mu;
-double *g_noalloc_ptr[64] = {};
+struct NoAllocEntry {
+  unsigned long long ctx_id;
+  double *ptr;
+};
+std::vector<NoAllocEntry> g_noalloc_cache;
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext *);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long *);
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
 }  // namespace
 
 // norms, factors and the first failing state: key = 2 * index + (NaN ? 1 : 0)
@@ -598,25 +611,53 @@ __global__ void k_scale_states_if_ok(double *__restrict__ x, long len, long n, c
     x[i] *= f[i / len];
 }
 
+// id of the caller's current CUDA context (after the runtime has made the
+// device's primary context current), through driver entry points obtained
+// from the runtime, so the library does not link the driver library itself
+static int current_ctx_id(fbse_ctx *c, unsigned long long *id)
+{
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+      cudaGetLastError();
+      return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: driver entry points unavailable");
+    }
+    g_ctx_get_current = (PfnCtxGetCurrent)f1;
+    g_ctx_get_id = (PfnCtxGetId)f2;
+  }
+  if (cudaFree(nullptr) != cudaSuccess) {  // makes the device's primary context current
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: no usable device");
+  }
+  CUcontext cu = nullptr;
+  if (g_ctx_get_current(&cu) != CUDA_SUCCESS || !cu || g_ctx_get_id(cu, id) != CUDA_SUCCESS)
+    return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: no current context");
+  return FBSE_OK;
+}
+
 static int noalloc_scratch(fbse_ctx *c, double **out)
 {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-    cudaGetLastError();
-    return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: no current device");
-  }
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      cudaGetLastError();
-      return set_err(c, FBSE_ERR_CUDA,
-                     std::string("fbse_normalize_all_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  unsigned long long id = 0;
+  int rc = current_ctx_id(c, &id);
+  if (rc) return rc;
+  for (const NoAllocEntry &e : g_noalloc_cache)
+    if (e.ctx_id == id) {
+      *out = e.ptr;
+      return FBSE_OK;
     }
-    g_noalloc_ptr[dev] = (double *)p;
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_CUDA,
+                   std::string("fbse_normalize_all_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
   }
-  *out = g_noalloc_ptr[dev];
+  g_noalloc_cache.push_back({id, (double *)p});
+  *out = (double *)p;
   return FBSE_OK;
 }
 
@@ -643,8 +684,14 @@ int normalize_all_noalloc(fbse_ctx *c, double *psitot, long n, double *norms)
   FBSE_CHECK_LAUNCH(c);
   k_scale_states_if_ok<<<grid_for(n * stlen), 256, 0, c->stream>>>(psitot, stlen, n, f, key);
   FBSE_CHECK_LAUNCH(c);
-  if (d2h(c->stream, &hkey, key, sizeof(int)) != cudaSuccess ||
-      (norms && d2h(c->stream, norms, nrm, n * sizeof(double)) != cudaSuccess)) {
+  // norms as fbse_normalize_all leaves them: up to and including the first
+  // state with a zero or NaN norm when there is one, all n otherwise
+  if (d2h(c->stream, &hkey, key, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: download");
+  }
+  const long nout = hkey != 0x7f7f7f7f ? std::min<long>(n, hkey / 2 + 1) : n;
+  if (norms && d2h(c->stream, norms, nrm, nout * sizeof(double)) != cudaSuccess) {
     cudaGetLastError();
     return set_err(c, FBSE_ERR_CUDA, "fbse_normalize_all_noalloc: download");
   }

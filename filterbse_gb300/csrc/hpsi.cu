@@ -10,10 +10,11 @@
 // no spin mixing.  Here one CTA per (atom, channel, group of states) gathers
 // the coefficients with one warp per (state, spin) (register accumulation,
 // warp reduction; the warps of a CTA share every table entry through L1) and
-// applies L.S (or the NL sign).  The scatter kernel runs one warp per state
-// and adds the contribution with atomics (overlapping spheres of neighbouring
-// atoms make it a reduction; the reference uses "omp atomic" for the same
-// reason, phamiltonian.c:295-303).
+// applies L.S (or the NL sign).  The scatter runs one thread per grid point
+// covered by any sphere (overlapping spheres of neighbouring atoms make it a
+// reduction, which the reference does with "omp atomic",
+// phamiltonian.c:295-303): each point's entries are summed in a fixed order,
+// so H psi is bit-identical from run to run.
 #include <cstdlib>
 
 #include "fbse_internal.cuh"
@@ -156,80 +157,89 @@ __global__ void __launch_bounds__(32 * W, MINB) k_proj_gather(const C<T> *__rest
   }
 }
 
-__device__ __forceinline__ void atomic_add_c(float2 *p, float2 v) { atomicAdd(p, v); }
-__device__ __forceinline__ void atomic_add_c(double2 *p, double2 v)
+// point-major view of the table for the scatter (ProjDev::cov_j ...)
+template <typename T> struct PtView {
+  const int *cov_j, *cov_beg, *atom;
+  const C<T> *y1;
+  const T *sop, *nlp;
+  long ncov, nent;
+  int nproj;
+};
+
+template <typename T> static PtView<T> ptview(fbse_ctx *c);
+template <> PtView<double> ptview<double>(fbse_ctx *c)
 {
-  atomicAdd(&p->x, v.x);
-  atomicAdd(&p->y, v.y);
+  const ProjDev &p = c->proj;
+  return {p.cov_j, p.cov_beg, p.pe_atom, reinterpret_cast<const double2 *>(p.pe_y1), p.pe_sop, p.pe_nlp, p.ncov,
+          p.nent, p.nproj};
+}
+template <> PtView<float> ptview<float>(fbse_ctx *c)
+{
+  const ProjDev &p = c->proj;
+  return {p.cov_j, p.cov_beg, p.pe_atom, reinterpret_cast<const float2 *>(p.pe_y1f), p.pe_sopf, p.pe_nlpf, p.ncov,
+          p.nent, p.nproj};
 }
 
-// scatter: out_s(r) += scale * sum_m Y_m(r) sum_p b_p(r) d[p][3 s + m] over the
-// active channels; one warp per state, kSU points per lane per iteration
-template <typename T, bool SO, bool NL, int kSU, int MINB>
-__global__ void __launch_bounds__(kProjThreads, MINB) k_proj_scatter(C<T> *__restrict__ out, const C<T> *__restrict__ coef,
-                                                               ProjView<T> pv, long nat, long nstates, long ngrid,
-                                                               int nspin, T scale)
+// scatter: out_s(r) += scale * sum_(a covering r) sum_m Y_m(r) sum_p b_p(r) d_a[p][3 s + m]
+// over the active channels.  One thread owns one covered point for kG states:
+// it sums the point's entries in increasing atom order and writes the point
+// once, so the result is the same on every run and for every batch size (the
+// reference adds with "omp atomic", phamiltonian.c:295-303, whose order
+// varies).  The lanes of a warp mostly share their atom, so the coefficient
+// loads are broadcasts.
+template <typename T, bool SO, bool NL, int kG>
+__global__ void __launch_bounds__(256) k_proj_scatter(C<T> *__restrict__ out, const C<T> *__restrict__ coef,
+                                                      PtView<T> pv, long nat, long nstates, long ngrid, int nspin,
+                                                      T scale)
 {
-  const long a = blockIdx.x;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const long st = (long)blockIdx.y * kSW + wid;
-  __shared__ C<T> d[kSW][2][kNC];
-  if (st < nstates) {
-    for (int i = lane; i < 2 * kNC; i += 32) d[wid][i / kNC][i % kNC] = coef[((st * nat + a) * 2) * kNC + i];
-  }
-  __syncwarp();
-  if (st >= nstates) return;
-  const int np = pv.cnt[a];
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= pv.ncov) return;
+  const long s0 = (long)blockIdx.y * kG;
+  const int ng = (int)(nstates - s0 < kG ? nstates - s0 : kG);
+  const long j = pv.cov_j[k];
+  const int e0 = pv.cov_beg[k], e1 = pv.cov_beg[k + 1];
   const int npj = pv.nproj;
-  C<T> *po = out + st * nspin * ngrid;
-  const long ebase = a * pv.npts;
-  // grid indices one iteration ahead (see the gather)
-  int jn[kSU];
+  T ar[kG][2], ai[kG][2];
 #pragma unroll
-  for (int u = 0; u < kSU; u++) {
-    const int g = lane + 32 * u;
-    jn[u] = g < np ? pv.jxyz[ebase + g] : -1;
+  for (int g = 0; g < kG; g++) {
+    ar[g][0] = ar[g][1] = T(0);
+    ai[g][0] = ai[g][1] = T(0);
   }
-  for (int g0 = lane; g0 < np; g0 += 32 * kSU) {
-    int jx[kSU];
-    long e[kSU];
+  for (int e = e0; e < e1; e++) {
+    const long a = pv.atom[e];
+    T yr[3], yi[3];
 #pragma unroll
-    for (int u = 0; u < kSU; u++) {
-      jx[u] = jn[u];
-      e[u] = ebase + g0 + 32 * u;
-      const int g = g0 + 32 * (kSU + u);
-      jn[u] = g < np ? pv.jxyz[ebase + g] : -1;
+    for (int m = 0; m < 3; m++) {
+      const C<T> y = pv.y1[m * pv.nent + e];
+      yr[m] = y.x;
+      yi[m] = y.y;
+    }
+    T bs[5], bn[5];
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+      bs[p] = (SO && p < npj) ? pv.sop[p * pv.nent + e] : T(0);
+      bn[p] = (NL && p < npj) ? pv.nlp[p * pv.nent + e] : T(0);
     }
 #pragma unroll
-    for (int u = 0; u < kSU; u++) {
-      if (jx[u] < 0) continue;
-      T yr[3], yi[3];
+    for (int g = 0; g < kG; g++) {
+      const C<T> *d = coef + (((s0 + (g < ng ? g : 0)) * nat + a) * 2) * kNC;
 #pragma unroll
-      for (int m = 0; m < 3; m++) {
-        const C<T> y = pv.y1[m * pv.ne + e[u]];
-        yr[m] = y.x;
-        yi[m] = y.y;
-      }
-      T bs[5], bn[5];
-#pragma unroll
-      for (int p = 0; p < 5; p++) {
-        bs[p] = (SO && p < npj) ? pv.sop[p * pv.ne + e[u]] : T(0);
-        bn[p] = (NL && p < npj) ? pv.nlp[p * pv.ne + e[u]] : T(0);
-      }
-      for (int s = 0; s < nspin; s++) {
+      for (int s = 0; s < 2; s++) {
+        if (g >= ng || s >= nspin) continue;
         T vr = 0, vi = 0;
 #pragma unroll
         for (int m = 0; m < 3; m++) {
           T qr = 0, qi = 0;  // sum_p b_p d[p][3 s + m]
 #pragma unroll
           for (int p = 0; p < 5; p++) {
+            if (p >= npj) continue;
             if (SO) {
-              const C<T> q = d[wid][0][p * 6 + s * 3 + m];
+              const C<T> q = __ldg(d + p * 6 + s * 3 + m);
               qr += bs[p] * q.x;
               qi += bs[p] * q.y;
             }
             if (NL) {
-              const C<T> q = d[wid][1][p * 6 + s * 3 + m];
+              const C<T> q = __ldg(d + kNC + p * 6 + s * 3 + m);
               qr += bn[p] * q.x;
               qi += bn[p] * q.y;
             }
@@ -237,8 +247,21 @@ __global__ void __launch_bounds__(kProjThreads, MINB) k_proj_scatter(C<T> *__res
           vr += yr[m] * qr - yi[m] * qi;
           vi += yr[m] * qi + yi[m] * qr;
         }
-        atomic_add_c(&po[s * ngrid + jx[u]], mk<T>(scale * vr, scale * vi));
+        ar[g][s] += vr;
+        ai[g][s] += vi;
       }
+    }
+  }
+#pragma unroll
+  for (int g = 0; g < kG; g++) {
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      if (g >= ng || s >= nspin) continue;
+      C<T> *o = out + ((s0 + g) * nspin + s) * ngrid + j;
+      C<T> v = *o;
+      v.x += scale * ar[g][s];
+      v.y += scale * ai[g][s];
+      *o = v;
     }
   }
 }
@@ -252,7 +275,6 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   int rc = ensure(c, &c->coef, &c->coef_bytes, need);
   if (rc) return rc;
   C<T> *coef = reinterpret_cast<C<T> *>(c->coef);
-  const long ngroups = (nstates + kSW - 1) / kSW;
   const long spc = kSW / c->nspin;
   const long ggroups = (nstates + spc - 1) / spc;
   if (ggroups > 65535 || p.nat > 2147483647L) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector grid too large");
@@ -272,14 +294,19 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   k_proj_gather<T, kGU, kMinB, kSW><<<gg, kProjThreads, 0, c->stream>>>(in, coef, pv, p.nat, nstates, c->ngrid,
                                                                        c->nspin, ch0, c->dv);
   FBSE_CHECK_LAUNCH(c);
-  dim3 gs((unsigned)p.nat, (unsigned)ngroups);
+  if (p.ncov == 0) return FBSE_OK;
+  constexpr int kG = occ ? 8 : 4;  // states per scatter thread
+  const long sgroups = (nstates + kG - 1) / kG;
+  if (sgroups > 65535) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector grid too large");
+  dim3 gs((unsigned)((p.ncov + 255) / 256), (unsigned)sgroups);
+  const PtView<T> pt = ptview<T>(c);
   const T sc = (T)scale;
   if (c->so && c->nl)
-    k_proj_scatter<T, true, true, 2, kMinB><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+    k_proj_scatter<T, true, true, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
   else if (c->so)
-    k_proj_scatter<T, true, false, 2, kMinB><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+    k_proj_scatter<T, true, false, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
   else
-    k_proj_scatter<T, false, true, 2, kMinB><<<gs, kProjThreads, 0, c->stream>>>(out, coef, pv, p.nat, nstates, c->ngrid, c->nspin, sc);
+    k_proj_scatter<T, false, true, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
   FBSE_CHECK_LAUNCH(c);
   return FBSE_OK;
 }

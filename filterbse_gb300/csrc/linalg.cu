@@ -273,9 +273,9 @@ __global__ void k_jacobi_sweep(double2 *__restrict__ A, double2 *__restrict__ V,
     }
     grid.sync();
   }
-  // off-diagonal Frobenius norm and diagonal norm
-  if (tid == 0) { off[0] = 0; off[1] = 0; }
-  grid.sync();
+  // off-diagonal Frobenius norm and diagonal norm: per-warp partials
+  // (off[2 + 2 w], off[3 + 2 w]) summed by warp 0 of block 0 in a fixed order,
+  // so that the sweep count is the same on every run
   double so = 0, sd = 0;
   for (long e = tid; e < (long)n * n; e += nth) {
     const double2 a = A[e];
@@ -287,9 +287,26 @@ __global__ void k_jacobi_sweep(double2 *__restrict__ A, double2 *__restrict__ V,
     so += __shfl_xor_sync(0xffffffffu, so, o);
     sd += __shfl_xor_sync(0xffffffffu, sd, o);
   }
+  const long nw = nth / 32, w = tid / 32;
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&off[0], so);
-    atomicAdd(&off[1], sd);
+    off[2 + 2 * w] = so;
+    off[3 + 2 * w] = sd;
+  }
+  grid.sync();
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    double to = 0, td = 0;
+    for (long i = threadIdx.x; i < nw; i += 32) {
+      to += off[2 + 2 * i];
+      td += off[3 + 2 * i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      to += __shfl_xor_sync(0xffffffffu, to, o);
+      td += __shfl_xor_sync(0xffffffffu, td, o);
+    }
+    if (threadIdx.x == 0) {
+      off[0] = to;
+      off[1] = td;
+    }
   }
 }
 
@@ -305,14 +322,6 @@ __global__ void k_identity(double2 *V, int n)
 int jacobi_eig_dev(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<double> &w)
 {
   const int m = n + (n & 1);
-  // rotation table and the two norms, kept in the context between calls
-  const size_t rot_bytes = (sizeof(Rot) * (m / 2 + 1) + 15) / 16 * 16;
-  void *scratch = nullptr;
-  int rc = cached(c, kSlotJacobi, rot_bytes + 2 * sizeof(double), &scratch);
-  if (rc) return rc;
-  Rot *rot = static_cast<Rot *>(scratch);
-  double *off = reinterpret_cast<double *>(static_cast<char *>(scratch) + rot_bytes);
-  FBSE_COUNT(1); k_identity<<<256, 256, 0, c->stream>>>(V, n);
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -320,6 +329,15 @@ int jacobi_eig_dev(fbse_ctx *c, double2 *A, double2 *V, int n, std::vector<doubl
   const long work = (long)(m / 2) * (m / 2) + (long)n * (m / 2);
   long want = (work + 255) / 256;
   int blocks = (int)std::min<long>(std::max<long>(1, want), (long)nsm * std::max(1, per_sm));
+  // rotation table, the two norms and their per-warp partials, kept in the
+  // context between calls
+  const size_t rot_bytes = (sizeof(Rot) * (m / 2 + 1) + 15) / 16 * 16;
+  void *scratch = nullptr;
+  int rc = cached(c, kSlotJacobi, rot_bytes + (2 + 2 * (size_t)blocks * 8) * sizeof(double), &scratch);
+  if (rc) return rc;
+  Rot *rot = static_cast<Rot *>(scratch);
+  double *off = reinterpret_cast<double *>(static_cast<char *>(scratch) + rot_bytes);
+  FBSE_COUNT(1); k_identity<<<256, 256, 0, c->stream>>>(V, n);
   double h[2] = {0, 0};
   bool conv = (n < 2);
   for (int sweep = 0; sweep < 60 && !conv; sweep++) {

@@ -200,6 +200,11 @@ __global__ void __launch_bounds__(128, 1)
                         __uint_as_float(r[j + 3]));
     }
   }
+  // after a timed-out wait, MMAs this CTA issued may still write the
+  // accumulator: the issuing thread waits once more (bounded) before the
+  // tensor memory is released; the host treats status = 1 as fatal for the
+  // context's tensor-core path
+  if (!done && nk > 0 && threadIdx.x == 32) mbar_wait(&done_bar, 0u);
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
@@ -298,6 +303,8 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
                   double2 *out)
 {
   using namespace tc;
+  if (c->tc_poisoned)
+    return set_err(c, FBSE_ERR_CUDA, "tensor-core path disabled: an earlier tensor-core wait timed out in this context");
   const long mp = ((ma + kBM - 1) / kBM) * kBM;
   const long np = ((nb + kBN - 1) / kBN) * kBN;
   const long nkb_all = (2 * L + kBK - 1) / kBK;
@@ -383,7 +390,10 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
     if (!launched(1)) break;
     int hs = 0;
     if (d2h(c->stream, &hs, status, sizeof(int)) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "tensor-core GEMM"); break; }
-    if (hs) rc = set_err(c, FBSE_ERR_NOCONV, "tensor-core GEMM: a wait timed out");
+    if (hs) {
+      c->tc_poisoned = 1;
+      rc = set_err(c, FBSE_ERR_NOCONV, "tensor-core GEMM: a wait timed out");
+    }
   } while (0);
   cudaStreamSynchronize(c->stream);
   cudaFree(buf);

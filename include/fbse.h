@@ -163,10 +163,14 @@ int fbse_sigma_e(fbse_ctx *ctx, const double *psitot, long n, double *eval, doub
 /* fbse_normalize_all without any allocation (no counterpart in the reference):
  * for callers that must not allocate device memory mid-run.  Its scratch is a
  * file-scope device array of about 1.06 MB, at most 1024 states per call
- * (more returns FBSE_ERR_ARG).  The first call on a device looks the array's
- * address up (cudaGetSymbolAddress, with that device current) and should come
- * before any stream capture.  The array is shared by all contexts on a device:
- * calls that overlap in time race.  norms may be NULL. */
+ * (more returns FBSE_ERR_ARG).  The first call in each CUDA context (the
+ * device's primary context for runtime-API callers; a device reset makes a new
+ * one) looks the array's address up (cudaGetSymbolAddress, with that device
+ * current) and should come before any stream capture.  The array is shared by
+ * all fbse contexts on a device: calls that overlap in time race.  norms may
+ * be NULL; on a zero or NaN norm it holds the norms up to and including the
+ * first failing state, as fbse_normalize_all leaves it, and the states are
+ * left unscaled. */
 int fbse_normalize_all_noalloc(fbse_ctx *ctx, double *psitot, long n, double *norms);
 
 /* ---- orthogonalisation, subspace diagonalisation, sigma_E ----------------

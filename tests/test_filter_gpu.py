@@ -166,3 +166,35 @@ def test_filter_job_matches_device_path(fbse, cuda, pinned):
     assert np.max(np.abs(ev2 - ev_j[sg_j <= cut])) < 1e-10
     nrm = np.sum(got2[:k2] ** 2, axis=1) * dv
     assert np.max(np.abs(nrm - 1.0)) < 1e-10 and not np.any(got2[k2:])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_filter_and_ritz_determinism(fbse, cuda, precision):
+    """The same starts give bit-identical filtered states whether they are
+    filtered together or in two batches and on a second run, and the
+    Rayleigh-Ritz step (Gram products, Jacobi eigensolver, rotation) gives
+    bit-identical Ritz values, residuals and vectors on a second run."""
+    import torch
+    sysm = tiny_cluster(16, 18, 15, natoms=10, nspin=2, is_complex=True, so=True, nl=True)
+    emin, emax = _range(sysm)
+    de = emax - emin
+    ncheby, m, nstart = 40, 3, 4
+    zn, _, _ = O.samp_points(ncheby)
+    targets = np.linspace(emin + 0.1 * de, emin + 0.3 * de, m)
+    an = O.newton_coeff(zn, targets, emin, de, O.filter_dt(ncheby, de))
+    starts, _, _ = O.init_filter_states(-4242, nstart, sysm.ngrid, sysm.nspin, sysm.is_complex, sysm.grid.dv)
+    p0 = torch.tensor(np.ascontiguousarray(starts.view(np.float64).reshape(nstart, -1)), device=cuda)
+    ctx = _ctx(fbse, sysm, precision)
+    a = ctx.newton_filter(zn, an, emin, de, p0).cpu().numpy()
+    b = ctx.newton_filter(zn, an, emin, de, p0).cpu().numpy()
+    c = np.concatenate([ctx.newton_filter(zn, an, emin, de, p0[:1]).cpu().numpy(),
+                        ctx.newton_filter(zn, an, emin, de, p0[1:]).cpu().numpy()])
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+    res = []
+    for _ in range(2):
+        t = torch.tensor(a.reshape(nstart * m, -1), device=cuda)
+        nk, ev, sg = ctx.ortho_diag_sigma(t)
+        res.append((nk, ev, sg, t[:nk].cpu().numpy()))
+    assert res[0][0] == res[1][0]
+    for x, y in zip(res[0][1:], res[1][1:]):
+        assert np.array_equal(x, y)

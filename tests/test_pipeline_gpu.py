@@ -1,10 +1,13 @@
 """End-to-end pins against the reference's own example runs (golden eval.dat).
 
-The whole filter path runs on the GPU in FP64 -- spectrum range, Newton
+The whole filter path runs on the GPU -- spectrum range, Newton
 coefficients, random starts, Newton filter, orthogonalisation, subspace
 diagonalisation, sigma_E -- on the reference's example inputs (conf.par,
-pot*.par, SO_*.par, input.par).  The reference's starts were clock-seeded,
-so the filtered subspaces differ; converged eigenvalues must agree."""
+pot*.par, SO_*.par, input.par), in FP64 and in the mixed path (FP32 recursion
+and FFTs, FP64 accumulators and eigensolves).  The reference's starts were
+clock-seeded, so the filtered subspaces differ; converged eigenvalues must
+agree to 1e-5 Ha.  The mixed path's converged eigenvectors must span the FP64
+path's degenerate eigenspaces on the same starts."""
 import os
 
 import numpy as np
@@ -21,7 +24,7 @@ def _targets(vbmin, vbmax, cbmin, cbmax, nvb, ncb):
 
 
 def _run(fbse, cuda, grid, pot, targets, ncheby, nstart, nspin, cplx, so=False, nl=False, proj=None, seed=-31415,
-         precision=0):
+         precision=0, states=False):
     import torch
     ctx = fbse.Context(grid, pot, nspin=nspin, is_complex=cplx, so=so, nl=nl, proj=proj, precision=precision)
     e0, e1, it = ctx.energy_range()
@@ -35,6 +38,8 @@ def _run(fbse, cuda, grid, pot, targets, ncheby, nstart, nspin, cplx, so=False, 
     m = len(targets)
     psitot = filt.reshape(nstart * m, -1)
     nk, ev, sg = ctx.ortho_diag_sigma(psitot)
+    if states:
+        return (emin, emax), ev, sg, psitot[:nk].cpu().numpy()
     return (emin, emax), ev, sg
 
 
@@ -45,7 +50,8 @@ def _match(ref, ev, sg, ref_sig, my_sig, tol):
     return r, d
 
 
-def test_cdse22_real_matches_reference_eval(fbse, cuda):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cdse22_real_matches_reference_eval(fbse, cuda, precision):
     """2.2 nm CdSe, real, 57 x 52 x 45 at 0.8 bohr, 16 starts x 16 targets, nCheby 2048
     (filter_mpi/EXAMPLES/2.2nm_CdSe/filter: input.par, eval.dat)."""
     atyp, xyz = read_conf(os.path.join(GOLD, "cdse22", "conf.par"))
@@ -55,14 +61,14 @@ def test_cdse22_real_matches_reference_eval(fbse, cuda):
     tabs = [read_pot(os.path.join(GOLD, "cdse22", f"pot{t}.par")) for t in types]
     pot = O.local_pot(g, xyz, np.array([types.index(a) for a in atyp]), tabs)
     targets = _targets(-0.31, -0.24, -0.15, -0.06, 10, 6)
-    (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 1, False)
+    (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 1, False, precision=precision)
     # run.dat:140 of the reference run: Emin = -1.13271, Emax = 12.3281.  Both
     # iterations stop at a relative change below 1e-6 per step (energy.c:239,
     # 282), not at the extremum, so the stopping values agree only to ~1e-3.
     assert abs(emin - (-1.13271)) < 3e-3 and abs(emax - 12.3281) < 1e-3 * 12.3281
     ref = np.loadtxt(os.path.join(GOLD, "cdse22", "eval.dat"))
     r, d = _match(ref, ev, sg, 1e-5, 1e-4, 1e-5)
-    print(f"\n[cdse22] ours: {len(ev)} states, {np.sum(sg < 1e-4)} with sigma<1e-4; reference converged "
+    print(f"\n[cdse22 precision={precision}] ours: {len(ev)} states, {np.sum(sg < 1e-4)} with sigma<1e-4; reference converged "
           f"(sigma<1e-5): {len(r)}; matched within 1e-5: {np.sum(d < 1e-5)}; max |dE| of matched "
           f"{np.max(d[d < 1e-5]) if np.any(d < 1e-5) else np.nan:.2e}")
     assert np.mean(d < 1e-5) >= 0.8
@@ -73,9 +79,7 @@ def _so_params(path):
     return vals[0], vals[1], vals[2]
 
 
-def test_cspbi3_spinor_so_nl_matches_reference_eval(fbse, cuda):
-    """1x1x1 CsPbI3, spinor with spin-orbit and nonlocal projectors, 44^3 at 0.5 bohr
-    (filter_mpi/EXAMPLES/1x1x1_CsPbI3/filter: input.par, SO_*.par, reference_output/eval.dat)."""
+def _cspbi3_system():
     d = os.path.join(GOLD, "cspbi3")
     atyp, xyz = read_conf(os.path.join(d, "conf.par"))
     types = sorted(set(atyp), key=atyp.index)
@@ -95,16 +99,60 @@ def test_cspbi3_spinor_so_nl_matches_reference_eval(fbse, cuda):
         sgns.append(cache[lam][1])
     proj = O.nlc_table(g, xyz, np.array([params[a][0] for a in atyp]), so_tab, np.array(nl_tabs), np.array(sgns))
     assert int(proj.npts) == 2325  # n_NL_gridpts in the reference run's run.dat
+    return g, pot, proj
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cspbi3_spinor_so_nl_matches_reference_eval(fbse, cuda, precision):
+    """1x1x1 CsPbI3, spinor with spin-orbit and nonlocal projectors, 44^3 at 0.5 bohr
+    (filter_mpi/EXAMPLES/1x1x1_CsPbI3/filter: input.par, SO_*.par, reference_output/eval.dat)."""
+    d = os.path.join(GOLD, "cspbi3")
+    g, pot, proj = _cspbi3_system()
     targets = _targets(-0.50, -0.20, -0.167, -0.10, 10, 6)
-    (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 2, True, so=True, nl=True, proj=proj)
+    (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 2, True, so=True, nl=True, proj=proj,
+                                precision=precision)
     # run.dat:160 of the reference run: Emin = -0.756627, Emax = 25.2627
     assert abs(emin - (-0.756627)) < 3e-3 and abs(emax - 25.2627) < 1e-3 * 25.2627
     ref = np.loadtxt(os.path.join(d, "eval.dat"))
     r, dd = _match(ref, ev, sg, 1e-6, 1e-4, 1e-5)
-    print(f"\n[cspbi3] ours: {len(ev)} states, {np.sum(sg < 1e-4)} with sigma<1e-4; reference converged: {len(r)};"
+    print(f"\n[cspbi3 precision={precision}] ours: {len(ev)} states, {np.sum(sg < 1e-4)} with sigma<1e-4; reference converged: {len(r)};"
           f" matched within 1e-5: {np.sum(dd < 1e-5)}; max |dE| of matched "
           f"{np.max(dd[dd < 1e-5]) if np.any(dd < 1e-5) else np.nan:.2e}")
     assert np.mean(dd < 1e-5) >= 0.8
+
+
+def test_mixed_subspace_overlap_matches_fp64(fbse, cuda):
+    """The mixed path's converged eigenvectors span the plain FP64 path's: on
+    the same starts (CsPbI3, spinor, SO + NL), for every degenerate FP64
+    cluster (levels within 1e-6 Ha) converged to sigma_E < 1e-6 in both runs,
+    1 - s_min(V_mixed^H V_fp64 dv) <= 1e-6, s_min the smallest singular value
+    of the overlap of the two orthonormal cluster bases."""
+    g, pot, proj = _cspbi3_system()
+    targets = _targets(-0.50, -0.20, -0.167, -0.10, 10, 6)
+    out = {}
+    for prec in (0, 1):
+        _, ev, sg, v = _run(fbse, cuda, g, pot, targets, 2048, 16, 2, True, so=True, nl=True, proj=proj,
+                            precision=prec, states=True)
+        out[prec] = (ev, sg, v.view(np.complex128))
+    (e64, s64, v64), (emx, smx, vmx) = out[0], out[1]
+    good64 = np.where(s64 < 1e-6)[0]
+    order = good64[np.argsort(e64[good64])]
+    worst, nclus = 0.0, 0
+    for cl in _clusters(e64[order], 1e-6):
+        idx = order[cl]
+        e = e64[idx].mean()
+        # the cluster must be isolated among the FP64 levels (no partner left out)
+        if np.sum(np.abs(e64 - e) < 1e-5) != len(idx):
+            continue
+        mine = np.where((np.abs(emx - e) < 1e-5) & (smx < 1e-6))[0]
+        if len(mine) != len(idx):
+            continue
+        ov = vmx[mine].conj() @ v64[idx].T * g.dv
+        smin = np.linalg.svd(ov, compute_uv=False).min()
+        worst = max(worst, 1.0 - smin)
+        nclus += 1
+    print(f"\n[cspbi3 mixed vs fp64] {nclus} converged clusters compared, max 1 - s_min = {worst:.2e}")
+    assert nclus >= 10 and worst <= 1e-6
 
 
 def _clusters(e, tol=1e-6):

@@ -63,9 +63,16 @@ def test_noalloc_rejects_oversize_and_zero_norm(fbse, cuda):
     x = torch.ones((3, sysm.ngrid), dtype=torch.float64, device=cuda)
     x[1] = 0
     before = x.clone()
-    with pytest.raises(fbse.FbseError, match="Norm is 0"):
-        _run_noalloc(fbse, ctx, x)
+    f = _bind(fbse.load())
+    norms = np.full(3, -7.0)
+    ctx._torch_sync()
+    rc = f(ctx._h, ctypes.c_void_p(x.data_ptr()), 3, norms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc != 0 and "Norm is 0" in fbse.load().fbse_last_error(ctx._h).decode()
     assert torch.equal(x, before)
+    # norms as fbse_normalize_all leaves them: written up to the failing state
+    assert np.allclose(norms[:2], [sysm.ngrid * sysm.grid.dv, 0.0]) and norms[2] == -7.0
+    with pytest.raises(fbse.FbseError, match="Norm is 0"):
+        ctx.normalize_all(before.clone())
     # the key is reset per call: a good call right after the failing one succeeds
     y = torch.ones((3, sysm.ngrid), dtype=torch.float64, device=cuda)
     n = _run_noalloc(fbse, ctx, y)
