@@ -32,7 +32,13 @@ EXPORTED = [
     "fbse_bse_qp_ang_mom",
     "fbse_bse_optical",
     "fbse_normalize_all_noalloc",
+    "fbse_get_tuning", "fbse_set_tuning", "fbse_tuning_report",
+    "fbse_precond_create", "fbse_precond_destroy", "fbse_precond_get_weights", "fbse_precond_set_weights",
+    "fbse_precond_apply", "fbse_precond_grad", "fbse_precond_train_step", "fbse_refine",
+    "fbse_gram", "fbse_rotate", "fbse_residual",
 ]
+
+PRECOND_NWEIGHTS = 15120
 
 
 class FbseError(RuntimeError):
@@ -55,6 +61,14 @@ class ProjDesc(ctypes.Structure):
                 ("y1", ctypes.POINTER(ctypes.c_double)), ("so_proj", ctypes.POINTER(ctypes.c_double)),
                 ("nl_proj", ctypes.POINTER(ctypes.c_double)), ("nl_sign", ctypes.POINTER(ctypes.c_int)),
                 ("LS", ctypes.POINTER(ctypes.c_double))]
+
+
+class Tuning(ctypes.Structure):
+    """fbse_tuning: kernel choices of a context (0 = chosen by the context)."""
+    _fields_ = [("fft_kernels", ctypes.c_int), ("fft_plane_cluster", ctypes.c_int),
+                ("fft_chunk_blocks", ctypes.c_long), ("scatter_states", ctypes.c_int),
+                ("gather_points", ctypes.c_int), ("newton_ring", ctypes.c_int), ("bse_simt", ctypes.c_int),
+                ("tc_image_bytes", ctypes.c_double), ("ritz_cut", ctypes.c_double)]
 
 
 _lib = None
@@ -117,6 +131,24 @@ def load() -> ctypes.CDLL:
     L.fbse_bse_qp_ang_mom.argtypes = [_VP, _VP, _D, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D, _D, _D,
                                       _D]
     L.fbse_bse_optical.argtypes = [_VP, _VP, _D, ctypes.c_long, ctypes.c_long, _D]
+    L.fbse_get_tuning.argtypes = [_VP, ctypes.POINTER(Tuning)]
+    L.fbse_set_tuning.argtypes = [_VP, ctypes.POINTER(Tuning)]
+    L.fbse_tuning_report.argtypes = [_VP, ctypes.c_char_p, ctypes.c_long]
+    L.fbse_tuning_report.restype = ctypes.c_long
+    L.fbse_residual.argtypes = [_VP, _VP, ctypes.c_long, _D, _VP]
+    L.fbse_gram.argtypes = [_VP, _VP, ctypes.c_long, _VP, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D]
+    L.fbse_rotate.argtypes = [_VP, _VP, ctypes.c_long, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _VP]
+    _F = ctypes.POINTER(ctypes.c_float)
+    L.fbse_precond_create.argtypes = [_VP, ctypes.POINTER(_VP), _F, ctypes.c_long]
+    L.fbse_precond_destroy.argtypes = [_VP]
+    L.fbse_precond_destroy.restype = None
+    L.fbse_precond_get_weights.argtypes = [_VP, _F]
+    L.fbse_precond_set_weights.argtypes = [_VP, _F]
+    L.fbse_precond_apply.argtypes = [_VP, _VP, _D, ctypes.c_long, _VP]
+    L.fbse_precond_grad.argtypes = [_VP, _VP, _VP, _D, ctypes.c_long, _D, _F]
+    L.fbse_precond_train_step.argtypes = [_VP, _VP, _VP, _D, ctypes.c_long, ctypes.c_double, _D]
+    L.fbse_refine.argtypes = [_VP, _VP, _VP, ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_double,
+                              ctypes.POINTER(ctypes.c_long), _D, _D]
     _lib = L
     return L
 
@@ -230,6 +262,28 @@ class Context:
     def sync(self):
         self._chk(self._L.fbse_sync(self._h))
 
+    # -- kernel choices -----------------------------------------------------------
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        self._chk(self._L.fbse_get_tuning(self._h, ctypes.byref(t)))
+        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+
+    def set_tuning(self, **fields):
+        """Fix kernel choices (fbse_tuning fields; 0 = chosen by the context)."""
+        cur = self.get_tuning()
+        for k, v in fields.items():
+            if k not in cur:
+                raise KeyError(k)
+            cur[k] = v
+        self._chk(self._L.fbse_set_tuning(self._h, ctypes.byref(Tuning(**cur))))
+
+    def tuning_report(self) -> list:
+        import json
+        n = self._L.fbse_tuning_report(self._h, None, 0)
+        buf = ctypes.create_string_buffer(n + 1)
+        self._L.fbse_tuning_report(self._h, buf, n + 1)
+        return json.loads(buf.value.decode())
+
     @staticmethod
     def _ptr(t):
         import torch
@@ -339,6 +393,53 @@ class Context:
         k = nk.value
         return k, ev[:k].copy(), sg[:k].copy()
 
+    def gram(self, A, B, off=0, length=None):
+        """dv-weighted overlap conj(A) B^T over a slab of points (fbse_gram):
+        A [na, stlen], B [nb, stlen] device float64; returns complex128 [na, nb]."""
+        L = self.nspin * self.ngrid
+        length = L - off if length is None else length
+        out = np.empty((A.shape[0], B.shape[0]), np.complex128)
+        self._torch_sync()
+        self._chk(self._L.fbse_gram(self._h, self._ptr(A), A.shape[0], self._ptr(B), B.shape[0], off, length,
+                                    out.view(np.float64).ctypes.data_as(_D)))
+        return out
+
+    def rotate(self, A, coef, out, off=0, length=None):
+        """out_j = sum_i coef[i, j] A_i over a slab (fbse_rotate); coef
+        complex [na, k] host, out device float64 [>= k, stlen]."""
+        L = self.nspin * self.ngrid
+        length = L - off if length is None else length
+        cf = np.ascontiguousarray(coef, np.complex128)
+        self._torch_sync()
+        self._chk(self._L.fbse_rotate(self._h, self._ptr(A), A.shape[0], cf.view(np.float64).ctypes.data_as(_D),
+                                      cf.shape[1], off, length, self._ptr(out)))
+        return out
+
+    def residual(self, psitot, ene):
+        """H psi_i - ene_i psi_i of psitot rows (fbse_residual); device float64."""
+        import torch
+        out = torch.empty_like(psitot)
+        e = np.ascontiguousarray(ene, np.float64)
+        self._torch_sync()
+        self._chk(self._L.fbse_residual(self._h, self._ptr(psitot), psitot.shape[0], _dp(e), self._ptr(out)))
+        return out
+
+    def refine(self, psitot, n, ev, sg, steps=2, tol=1e-2, precond=None):
+        """fbse_refine: residual refinement of the first n Ritz pairs of
+        psitot [cap, stlen] (device float64, normalised Ritz vectors, with
+        their eval / sigma); returns (n_out, eval, sigma)."""
+        cap = psitot.shape[0]
+        e = np.zeros(cap)
+        s_ = np.zeros(cap)
+        e[:n] = ev[:n]
+        s_[:n] = sg[:n]
+        nk = ctypes.c_long()
+        self._torch_sync()
+        self._chk(self._L.fbse_refine(self._h, precond._p if precond is not None else None, self._ptr(psitot), n, cap,
+                                      steps, tol, ctypes.byref(nk), _dp(e), _dp(s_)))
+        k = nk.value
+        return k, e[:k].copy(), s_[:k].copy()
+
     # -- Bethe-Salpeter stage -----------------------------------------------------
     def bse_potentials(self, gx, gy, gz, xmin, ymin, zmin, eps=(6.0, 6.0, 6.0)):
         """init_elec_hole_kernel: returns (pot_bare, pot_screened), [ngrid]
@@ -434,3 +535,73 @@ class Context:
         self._chk(self._L.fbse_bse_optical(self._h, self._ptr(coeff), _dp(mp.reshape(-1).view(np.float64)), n_h, n_e,
                                            _dp(out.view(np.float64))))
         return out.reshape(-1, 3)
+
+
+class Precond:
+    """The learned residual preconditioner of a context (fbse_precond_*):
+    4 convolutions 3x3x3, 16 channels, FP32 weights, BF16 activations."""
+
+    def __init__(self, ctx: Context, weights=None, seed: int = 1):
+        self.ctx = ctx
+        self._L = ctx._L
+        self._p = ctypes.c_void_p()
+        w = None
+        if weights is not None:
+            w = np.ascontiguousarray(weights, np.float32)
+            assert w.size == PRECOND_NWEIGHTS
+        rc = self._L.fbse_precond_create(ctx._h, ctypes.byref(self._p),
+                                         w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if w is not None else None,
+                                         seed)
+        ctx._chk(rc)
+
+    def close(self):
+        if self._p:
+            self._L.fbse_precond_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def weights(self) -> np.ndarray:
+        w = np.empty(PRECOND_NWEIGHTS, np.float32)
+        self.ctx._chk(self._L.fbse_precond_get_weights(self._p, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return w
+
+    @weights.setter
+    def weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        assert w.size == PRECOND_NWEIGHTS
+        self.ctx._chk(self._L.fbse_precond_set_weights(self._p, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def apply(self, resid, ene):
+        """P(resid) for resid [n, stlen] (device float64 psitot), ene [n]."""
+        import torch
+        out = torch.empty_like(resid)
+        e = np.ascontiguousarray(ene, np.float64)
+        self.ctx._torch_sync()
+        self.ctx._chk(self._L.fbse_precond_apply(self._p, self.ctx._ptr(resid), _dp(e), resid.shape[0],
+                                                 self.ctx._ptr(out)))
+        return out
+
+    def grad(self, resid, corr, ene):
+        """(loss, gradient [PRECOND_NWEIGHTS] float32) without a step."""
+        e = np.ascontiguousarray(ene, np.float64)
+        g = np.empty(PRECOND_NWEIGHTS, np.float32)
+        loss = ctypes.c_double()
+        self.ctx._torch_sync()
+        self.ctx._chk(self._L.fbse_precond_grad(self._p, self.ctx._ptr(resid), self.ctx._ptr(corr), _dp(e),
+                                                resid.shape[0], ctypes.byref(loss),
+                                                g.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return loss.value, g
+
+    def train_step(self, resid, corr, ene, lr=1e-3) -> float:
+        e = np.ascontiguousarray(ene, np.float64)
+        loss = ctypes.c_double()
+        self.ctx._torch_sync()
+        self.ctx._chk(self._L.fbse_precond_train_step(self._p, self.ctx._ptr(resid), self.ctx._ptr(corr), _dp(e),
+                                                      resid.shape[0], lr, ctypes.byref(loss)))
+        return loss.value

@@ -51,6 +51,8 @@ int normalize_all(fbse_ctx *c, double *psitot, long n, double *norms);
 int energy_all(fbse_ctx *c, const double *psitot, long n, double *ene, double *sigma);
 int energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *emax, long *iters);
 int ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma);
+int gram_slab(fbse_ctx *c, const double *A, long na, const double *B, long nb, long off, long len, double *out_host);
+int rotate_slab(fbse_ctx *c, const double *A, long na, const double *C_host, long k, long off, long len, double *out);
 
 // per-axis 0.5 k^2 / N exactly as init_kvec + build_grid_ksqr
 // (filter_mpi/init.c:1383-1394, 318-336)
@@ -334,6 +336,51 @@ int fbse_sync(fbse_ctx *c)
 
 void *fbse_stream(fbse_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
+int fbse_get_tuning(fbse_ctx *c, fbse_tuning *t)
+{
+  if (!c || !t) return c ? set_err(c, FBSE_ERR_ARG, "fbse_get_tuning: null") : FBSE_ERR_ARG;
+  *t = c->tune;
+  return FBSE_OK;
+}
+
+int fbse_set_tuning(fbse_ctx *c, const fbse_tuning *t)
+{
+  if (!c || !t) return c ? set_err(c, FBSE_ERR_ARG, "fbse_set_tuning: null") : FBSE_ERR_ARG;
+  auto pow2_in = [](long v, long hi) { return v == 0 || (v >= 1 && v <= hi && (v & (v - 1)) == 0); };
+  if (t->fft_kernels < 0 || t->fft_kernels > 2 || t->fft_plane_cluster < 0 || t->fft_plane_cluster > 1 ||
+      t->fft_chunk_blocks < 0 || !pow2_in(t->scatter_states, 8) || !pow2_in(t->gather_points, 4) ||
+      (t->newton_ring != 0 && (t->newton_ring < 8 || t->newton_ring > 128)) || t->bse_simt < 0 || t->bse_simt > 1 ||
+      !(t->tc_image_bytes >= 0) || !(t->ritz_cut >= 0 && t->ritz_cut < 1))
+    return set_err(c, FBSE_ERR_ARG, "fbse_set_tuning: a field is out of range");
+  c->tune = *t;
+  c->tuned.clear();  // earlier decisions may rest on the old fixed choices
+  return FBSE_OK;
+}
+
+long fbse_tuning_report(fbse_ctx *c, char *buf, long n)
+{
+  if (!c) return -1;
+  std::string j = "[";
+  for (size_t i = 0; i < c->tuned.size(); i++) {
+    const TuneRecord &r = c->tuned[i];
+    j += (i ? ", " : "") + std::string("{\"kernel\": \"") + r.kernel + "\", \"problem\": \"" + r.problem +
+         "\", \"candidates\": {";
+    for (size_t k = 0; k < r.cand.size(); k++) {
+      char b[64];
+      snprintf(b, sizeof b, "%s\"%ld\": %.2f", k ? ", " : "", r.cand[k].first, r.cand[k].second);
+      j += b;
+    }
+    j += "}, \"choice\": " + std::to_string(r.choice) + "}";
+  }
+  j += "]";
+  if (buf && n > 0) {
+    const size_t m = std::min<size_t>((size_t)n - 1, j.size());
+    std::memcpy(buf, j.data(), m);
+    buf[m] = 0;
+  }
+  return (long)j.size();
+}
+
 int fbse_hpsi(fbse_ctx *c, const void *in, void *out, long nstates)
 {
   if (!c || !in || !out || nstates < 1) return c ? set_err(c, FBSE_ERR_ARG, "fbse_hpsi: bad arguments") : FBSE_ERR_ARG;
@@ -383,6 +430,19 @@ int fbse_sigma_e(fbse_ctx *c, const double *psitot, long n, double *eval, double
 {
   if (!c || !psitot || !eval || !sigma) return c ? set_err(c, FBSE_ERR_ARG, "fbse_sigma_e: null") : FBSE_ERR_ARG;
   return energy_all(c, psitot, n, eval, sigma);
+}
+
+int fbse_gram(fbse_ctx *c, const double *A, long na, const double *B, long nb, long off, long len, double *out)
+{
+  if (!c || !A || !B || !out) return c ? set_err(c, FBSE_ERR_ARG, "fbse_gram: null") : FBSE_ERR_ARG;
+  return gram_slab(c, A, na, B, nb, off, len, out);
+}
+
+int fbse_rotate(fbse_ctx *c, const double *A, long na, const double *coef, long k, long off, long len, double *out)
+{
+  if (!c || !A || !coef || !out) return c ? set_err(c, FBSE_ERR_ARG, "fbse_rotate: null") : FBSE_ERR_ARG;
+  if (out == A) return set_err(c, FBSE_ERR_ARG, "fbse_rotate: out must not alias A");
+  return rotate_slab(c, A, na, coef, k, off, len, out);
 }
 
 int fbse_ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma)

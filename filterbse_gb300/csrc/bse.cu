@@ -187,19 +187,15 @@ __global__ void k_sum_parts(const double2 *__restrict__ part, int nchunk, long n
 }
 
 // the mixed path's contraction runs on the tensor cores (tcgemm.cu, split-TF32
-// products, FP32 accumulation, FP64 split-K sums); FBSE_BSE_TC=0 keeps it on
-// the SIMT kernel below
-static bool bse_tensor_cores()
-{
-  const char *e = getenv("FBSE_BSE_TC");
-  return !(e && atoi(e) == 0);
-}
+// products, FP32 accumulation, FP64 split-K sums); fbse_tuning.bse_simt = 1
+// keeps it on the SIMT kernel below
+static bool bse_tensor_cores(fbse_ctx *c) { return c->tune.bse_simt == 0; }
 
 template <typename T>
 static int cgemm_nt(fbse_ctx *c, const C<T> *A, int ma, const C<T> *B, int nb, long L, double scale, double2 *out)
 {
   if constexpr (sizeof(T) == 4) {
-    if (bse_tensor_cores())
+    if (bse_tensor_cores(c))
       return tc_complex_nt<float>(c, reinterpret_cast<const float *>(A), ma, reinterpret_cast<const float *>(B), nb,
                                   L, false, scale, out);
   }

@@ -86,6 +86,13 @@ struct ProjDev {
   float *pe_y1f = nullptr, *pe_sopf = nullptr, *pe_nlpf = nullptr;
 };
 
+// one decision of the autotuner: candidate values with their times (us)
+struct TuneRecord {
+  std::string kernel, problem;
+  std::vector<std::pair<long, double>> cand;
+  long choice = 0;
+};
+
 }  // namespace fbse
 
 struct fbse_ctx {
@@ -114,6 +121,8 @@ struct fbse_ctx {
   // filter job's device copies of the starts and filtered states
   void *cache[8] = {};
   size_t cache_bytes[8] = {};
+  fbse_tuning tune{};                      // fixed choices (nonzero fields) of the caller
+  std::vector<fbse::TuneRecord> tuned;     // the autotuner's decisions
   std::string err;
 };
 
@@ -157,6 +166,52 @@ inline int cached(fbse_ctx *c, int slot, size_t need, void **out)
 // reads (and clears) the device error flags of the kernels with bounded waits
 int check_dev_status(fbse_ctx *c);
 
+// autotuner: the recorded choice for (kernel, problem), or -- on the first
+// call -- times launch(v) for each candidate v on the context's stream (one
+// untimed and two timed runs each, CUDA events) and records the fastest.
+// launch(v) must enqueue work whose result does not depend on v, or write
+// only scratch.  Returns FBSE_OK with *choice set.
+template <typename F>
+int autotune(fbse_ctx *c, const char *kernel, const std::string &problem, const std::vector<long> &cands, F launch,
+             long *choice)
+{
+  for (const TuneRecord &r : c->tuned)
+    if (r.kernel == kernel && r.problem == problem) {
+      *choice = r.choice;
+      return FBSE_OK;
+    }
+  TuneRecord rec;
+  rec.kernel = kernel;
+  rec.problem = problem;
+  cudaEvent_t e0, e1;
+  FBSE_CUDA(c, cudaEventCreate(&e0));
+  FBSE_CUDA(c, cudaEventCreate(&e1));
+  int rc = FBSE_OK;
+  double best = 1e300;
+  for (long v : cands) {
+    if ((rc = launch(v))) break;
+    FBSE_CUDA(c, cudaEventRecord(e0, c->stream));
+    for (int k = 0; k < 2 && !rc; k++) rc = launch(v);
+    if (rc) break;
+    FBSE_CUDA(c, cudaEventRecord(e1, c->stream));
+    FBSE_CUDA(c, cudaEventSynchronize(e1));
+    float ms = 0;
+    FBSE_CUDA(c, cudaEventElapsedTime(&ms, e0, e1));
+    const double us = 500.0 * ms;
+    rec.cand.push_back({v, us});
+    if (us < best) {
+      best = us;
+      rec.choice = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  c->tuned.push_back(rec);
+  *choice = rec.choice;
+  return FBSE_OK;
+}
+
 // host copies ordered on the context's (non-blocking) stream; d2h returns
 // after the data has arrived
 inline cudaError_t h2d(cudaStream_t s, void *dst, const void *src, size_t bytes)
@@ -184,7 +239,7 @@ int conv_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, co
 
 // projectors (hpsi.cu) --------------------------------------------------------
 template <typename T>
-int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scale);
+int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scale, C<T> *scratch = nullptr);
 template <typename T>
 int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, double b);
 

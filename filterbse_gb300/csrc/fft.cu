@@ -595,31 +595,16 @@ static int launch_plane(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int m
   return FBSE_OK;
 }
 
-// blocks per launch: all of them by default (more CTAs in flight beat keeping
-// the scratch in L2 on measured 128^3 runs); FBSE_FFT_CHUNK_BLOCKS caps it
-template <typename T> static long chunk_blocks(fbse_ctx *c, long nblk)
-{
-  (void)c;
-  const char *e = getenv("FBSE_FFT_CHUNK_BLOCKS");
-  if (e && atol(e) > 0) return atol(e) < nblk ? atol(e) : nblk;
-  return nblk;
-}
-
 // ---------------------------------------------------------------------------
 // register-resident kernels (fft_fast.cuh) for axes of 64, 128, 256 points;
-// FBSE_FFT_GENERIC=1 selects the mixed-radix kernels for every axis
+// fbse_tuning.fft_kernels = 1 selects the mixed-radix kernels for every axis,
+// = 2 the mixed-radix line passes
 // ---------------------------------------------------------------------------
-static bool fast_generic_forced()
-{
-  static int v = -1;
-  if (v < 0) v = getenv("FBSE_FFT_GENERIC") != nullptr;
-  return v == 1;
-}
-static bool fast_axis_ok(long n) { return !fast_generic_forced() && (n == 64 || n == 128 || n == 256); }
+static bool fast_axis_ok(fbse_ctx *c, long n) { return c->tune.fft_kernels == 0 && (n == 64 || n == 128 || n == 256); }
 
 template <typename T> static bool fast_plane_ok(fbse_ctx *c)
 {
-  if (fast_generic_forced() || c->nx != c->ny || getenv("FBSE_FFT_LINES") != nullptr) return false;
+  if (c->tune.fft_kernels != 0 || c->nx != c->ny) return false;
   if (c->nx == 64) return fast::PlaneCfg<T, 64>::smem() <= (size_t)max_smem();
   if (c->nx == 128 && sizeof(C<T>) == 8) return fast::PlaneCfg<T, 128>::smem() <= (size_t)max_smem();
   return false;
@@ -647,7 +632,7 @@ static int launch_plane_fast_n(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk
   return FBSE_OK;
 }
 
-// the two-CTA cluster variant (FBSE_FFT_CLUSTER=1) of the 128 x 128 FP32 plane
+// the two-CTA cluster variant (fbse_tuning.fft_plane_cluster = 1) of the 128 x 128 FP32 plane
 template <typename T, int N>
 static int launch_plane_cl_n(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int mode, const C<T> *phi,
                              const T *pot, T ca, T cb)
@@ -668,20 +653,13 @@ static int launch_plane_cl_n(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, 
   return FBSE_OK;
 }
 
-static bool plane_cluster_on()
-{
-  static int v = -1;
-  if (v < 0) v = getenv("FBSE_FFT_CLUSTER") != nullptr && atoi(getenv("FBSE_FFT_CLUSTER")) == 1;
-  return v == 1;
-}
-
 template <typename T>
 static int launch_plane_fast(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, int mode, const C<T> *phi,
                              const T *pot, T ca, T cb)
 {
   if (c->nx == 64) return launch_plane_fast_n<T, 64>(c, in, out, nblk, mode, phi, pot, ca, cb);
   if constexpr (sizeof(C<T>) == 8) {
-    if (c->nx == 128 && plane_cluster_on()) return launch_plane_cl_n<T, 128>(c, in, out, nblk, mode, phi, pot, ca, cb);
+    if (c->nx == 128 && c->tune.fft_plane_cluster == 1) return launch_plane_cl_n<T, 128>(c, in, out, nblk, mode, phi, pot, ca, cb);
   }
   if constexpr (sizeof(C<T>) == 8) {
     if (c->nx == 128) return launch_plane_fast_n<T, 128>(c, in, out, nblk, mode, phi, pot, ca, cb);
@@ -723,7 +701,7 @@ template <typename T>
 static int launch_cols_any(fbse_ctx *c, C<T> *data, long nblk, int axis, bool inv, bool kmul,
                            const double2 *kq = nullptr)
 {
-  switch (fast_axis_ok(c->ax[axis].n) ? c->ax[axis].n : 0) {
+  switch (fast_axis_ok(c, c->ax[axis].n) ? c->ax[axis].n : 0) {
     case 64: return launch_cols_fast_n<T, 64>(c, data, nblk, axis, inv, kmul, kq);
     case 128: return launch_cols_fast_n<T, 128>(c, data, nblk, axis, inv, kmul, kq);
     case 256: return launch_cols_fast_n<T, 256>(c, data, nblk, axis, inv, kmul, kq);
@@ -757,7 +735,7 @@ template <typename T>
 static int launch_x_any(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, bool inv, int epi, const C<T> *phi,
                         const T *pot, T ca, T cb)
 {
-  switch (fast_axis_ok(c->nx) ? c->nx : 0) {
+  switch (fast_axis_ok(c, c->nx) ? c->nx : 0) {
     case 64: return launch_x_fast_n<T, 64>(c, in, out, nblk, inv, epi, phi, pot, ca, cb);
     case 128: return launch_x_fast_n<T, 128>(c, in, out, nblk, inv, epi, phi, pot, ca, cb);
     case 256: return launch_x_fast_n<T, 256>(c, in, out, nblk, inv, epi, phi, pot, ca, cb);
@@ -766,39 +744,65 @@ static int launch_x_any(fbse_ctx *c, const C<T> *in, C<T> *out, long nblk, bool 
 }
 
 // out = a (F^-1 K F in + V in) + b in with K = the capped kinetic factor, or
-// the complex k-space array kq when given (then V is not applied)
+// the complex k-space array kq when given (then V is not applied); cb blocks
+// per launch sequence
 template <typename T>
-static int fft_op_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b,
-                        int with_v, const double2 *kq)
+static int fft_op_chunked(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b,
+                          int with_v, const double2 *kq, long cb)
 {
   int rc;
   const Stages sx = stages_of(c->ax[0]), sy = stages_of(c->ax[1]);
-  const bool plane = !sx.big && !sy.big && plane_smem<T>(c) <= (size_t)max_smem() &&
-                     getenv("FBSE_FFT_LINES") == nullptr;
+  const bool plane = !sx.big && !sy.big && plane_smem<T>(c) <= (size_t)max_smem() && c->tune.fft_kernels != 2;
   const T *pot = with_v ? pot_of<T>(c) : nullptr;
   const bool fplane = fast_plane_ok<T>(c);
-  const long cb = chunk_blocks<T>(c, nblk);
   for (long b0 = 0; b0 < nblk; b0 += cb) {
     const long nb = (nblk - b0 < cb) ? nblk - b0 : cb;
     const C<T> *ci = in + b0 * c->ngrid;
     C<T> *co = out + b0 * c->ngrid;
+    C<T> *wk = work;  // reused by every chunk: a chunk's intermediate passes can stay in L2
     if (fplane) {
-      if ((rc = launch_plane_fast<T>(c, ci, work, nb, 0, nullptr, nullptr, T(1), T(0)))) return rc;
-      if ((rc = launch_cols_any<T>(c, work, nb, 2, false, true, kq))) return rc;
-      if ((rc = launch_plane_fast<T>(c, work, co, nb, 1, ci, pot, (T)a, (T)b))) return rc;
+      if ((rc = launch_plane_fast<T>(c, ci, wk, nb, 0, nullptr, nullptr, T(1), T(0)))) return rc;
+      if ((rc = launch_cols_any<T>(c, wk, nb, 2, false, true, kq))) return rc;
+      if ((rc = launch_plane_fast<T>(c, wk, co, nb, 1, ci, pot, (T)a, (T)b))) return rc;
     } else if (plane) {
-      if ((rc = launch_plane<T>(c, ci, work, nb, 0, nullptr, nullptr, T(1), T(0)))) return rc;
-      if ((rc = launch_cols<T>(c, work, nb, 2, false, true, kq))) return rc;
-      if ((rc = launch_plane<T>(c, work, co, nb, 1, ci, pot, (T)a, (T)b))) return rc;
+      if ((rc = launch_plane<T>(c, ci, wk, nb, 0, nullptr, nullptr, T(1), T(0)))) return rc;
+      if ((rc = launch_cols<T>(c, wk, nb, 2, false, true, kq))) return rc;
+      if ((rc = launch_plane<T>(c, wk, co, nb, 1, ci, pot, (T)a, (T)b))) return rc;
     } else {
-      if ((rc = launch_x_any<T>(c, ci, work, nb, false, 0, nullptr, nullptr, T(1), T(0)))) return rc;
-      if ((rc = launch_cols_any<T>(c, work, nb, 1, false, false))) return rc;
-      if ((rc = launch_cols_any<T>(c, work, nb, 2, false, true, kq))) return rc;
-      if ((rc = launch_cols_any<T>(c, work, nb, 1, true, false))) return rc;
-      if ((rc = launch_x_any<T>(c, work, co, nb, true, 1, ci, pot, (T)a, (T)b))) return rc;
+      if ((rc = launch_x_any<T>(c, ci, wk, nb, false, 0, nullptr, nullptr, T(1), T(0)))) return rc;
+      if ((rc = launch_cols_any<T>(c, wk, nb, 1, false, false))) return rc;
+      if ((rc = launch_cols_any<T>(c, wk, nb, 2, false, true, kq))) return rc;
+      if ((rc = launch_cols_any<T>(c, wk, nb, 1, true, false))) return rc;
+      if ((rc = launch_x_any<T>(c, wk, co, nb, true, 1, ci, pot, (T)a, (T)b))) return rc;
     }
   }
   return FBSE_OK;
+}
+
+// blocks per launch sequence: fixed by fbse_tuning.fft_chunk_blocks or
+// autotuned (every block is transformed by the same kernels either way; a
+// smaller chunk keeps its intermediate passes in L2, a larger one fills the
+// GPU better)
+template <typename T>
+static int fft_op_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, double a, double b,
+                        int with_v, const double2 *kq)
+{
+  long cb = c->tune.fft_chunk_blocks;
+  if (cb == 0) {
+    cb = nblk;
+    if (nblk >= 4 && (const void *)in != (const void *)out) {
+      std::vector<long> cands{nblk};
+      for (long v : {16L, 8L, 4L, 2L})
+        if (v < nblk) cands.push_back(v);
+      const std::string prob = std::string(sizeof(T) == 4 ? "fp32" : "fp64") + " grid=" + std::to_string(c->nx) +
+                               "x" + std::to_string(c->ny) + "x" + std::to_string(c->nz) +
+                               " blocks=" + std::to_string(nblk) + (kq ? " convolution" : " kinetic");
+      int rc = autotune(c, "fft blocks per launch", prob, cands,
+                        [&](long v) { return fft_op_chunked<T>(c, in, out, work, nblk, a, b, with_v, kq, v); }, &cb);
+      if (rc) return rc;
+    }
+  }
+  return fft_op_chunked<T>(c, in, out, work, nblk, a, b, with_v, kq, cb < nblk ? cb : nblk);
 }
 
 template <typename T>

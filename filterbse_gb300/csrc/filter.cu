@@ -173,14 +173,13 @@ static int launch_newton_acc(fbse_ctx *c, const C<T> *ring, long j0, int nk, con
   return FBSE_OK;
 }
 
-// ring length: up to 128 slots within 40% of the free device memory (the
-// ring the context already holds counts as free; FBSE_NEWTON_RING
-// overrides), at most ncheby
+// ring length: fbse_tuning.newton_ring slots (128 by default), halved while
+// the ring would take more than 40% of the free device memory (the ring the
+// context already holds counts as free), at most ncheby.  The FP32 block sums
+// of the accumulation depend on it.
 static long ring_slots(fbse_ctx *c, long ncheby, size_t slot_bytes)
 {
-  long K = kMaxRing;
-  const char *e = getenv("FBSE_NEWTON_RING");
-  if (e && atol(e) > 0) K = atol(e) < kMaxRing ? atol(e) : kMaxRing;
+  long K = c->tune.newton_ring > 0 ? std::min<long>(c->tune.newton_ring, kMaxRing) : kMaxRing;
   size_t free_b = 0, tot_b = 0;
   if (cudaMemGetInfo(&free_b, &tot_b) != cudaSuccess) {
     cudaGetLastError();

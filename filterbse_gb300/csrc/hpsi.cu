@@ -187,6 +187,23 @@ template <> PtView<float> ptview<float>(fbse_ctx *c)
 // reference adds with "omp atomic", phamiltonian.c:295-303, whose order
 // varies).  The lanes of a warp mostly share their atom, so the coefficient
 // loads are broadcasts.
+// the six coefficients d[p][0..5] (j = 3 s + m) of one channel, 16-byte loads
+__device__ __forceinline__ void ld_row6(const float2 *d, float2 q[6])
+{
+  const float4 *v = reinterpret_cast<const float4 *>(d);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float4 t = __ldg(v + i);
+    q[2 * i] = make_float2(t.x, t.y);
+    q[2 * i + 1] = make_float2(t.z, t.w);
+  }
+}
+__device__ __forceinline__ void ld_row6(const double2 *d, double2 q[6])
+{
+#pragma unroll
+  for (int i = 0; i < 6; i++) q[i] = __ldg(d + i);
+}
+
 template <typename T, bool SO, bool NL, int kG>
 __global__ void __launch_bounds__(256) k_proj_scatter(C<T> *__restrict__ out, const C<T> *__restrict__ coef,
                                                       PtView<T> pv, long nat, long nstates, long ngrid, int nspin,
@@ -199,6 +216,14 @@ __global__ void __launch_bounds__(256) k_proj_scatter(C<T> *__restrict__ out, co
   const long j = pv.cov_j[k];
   const int e0 = pv.cov_beg[k], e1 = pv.cov_beg[k + 1];
   const int npj = pv.nproj;
+  // the outputs this thread updates, loaded before the sums so that their
+  // DRAM latency overlaps the coefficient work
+  C<T> o[kG][2];
+#pragma unroll
+  for (int g = 0; g < kG; g++)
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+      if (g < ng && s < nspin) o[g][s] = out[((s0 + g) * nspin + s) * ngrid + j];
   T ar[kG][2], ai[kG][2];
 #pragma unroll
   for (int g = 0; g < kG; g++) {
@@ -222,30 +247,38 @@ __global__ void __launch_bounds__(256) k_proj_scatter(C<T> *__restrict__ out, co
     }
 #pragma unroll
     for (int g = 0; g < kG; g++) {
-      const C<T> *d = coef + (((s0 + (g < ng ? g : 0)) * nat + a) * 2) * kNC;
+      if (g >= ng) continue;
+      const C<T> *d = coef + (((s0 + g) * nat + a) * 2) * kNC;
+      // q[j] = sum_p b_p d[p][j], j = 3 s + m, p in increasing order
+      T qr[6], qi[6];
+#pragma unroll
+      for (int q = 0; q < 6; q++) qr[q] = qi[q] = T(0);
+#pragma unroll
+      for (int p = 0; p < 5; p++) {
+        if (p >= npj) continue;
+        C<T> rs[6], rn[6];
+        if (SO) ld_row6(d + p * 6, rs);
+        if (NL) ld_row6(d + kNC + p * 6, rn);
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+          if (SO) {
+            qr[q] += bs[p] * rs[q].x;
+            qi[q] += bs[p] * rs[q].y;
+          }
+          if (NL) {
+            qr[q] += bn[p] * rn[q].x;
+            qi[q] += bn[p] * rn[q].y;
+          }
+        }
+      }
 #pragma unroll
       for (int s = 0; s < 2; s++) {
-        if (g >= ng || s >= nspin) continue;
+        if (s >= nspin) continue;
         T vr = 0, vi = 0;
 #pragma unroll
         for (int m = 0; m < 3; m++) {
-          T qr = 0, qi = 0;  // sum_p b_p d[p][3 s + m]
-#pragma unroll
-          for (int p = 0; p < 5; p++) {
-            if (p >= npj) continue;
-            if (SO) {
-              const C<T> q = __ldg(d + p * 6 + s * 3 + m);
-              qr += bs[p] * q.x;
-              qi += bs[p] * q.y;
-            }
-            if (NL) {
-              const C<T> q = __ldg(d + kNC + p * 6 + s * 3 + m);
-              qr += bn[p] * q.x;
-              qi += bn[p] * q.y;
-            }
-          }
-          vr += yr[m] * qr - yi[m] * qi;
-          vi += yr[m] * qi + yi[m] * qr;
+          vr += yr[m] * qr[3 * s + m] - yi[m] * qi[3 * s + m];
+          vi += yr[m] * qi[3 * s + m] + yi[m] * qr[3 * s + m];
         }
         ar[g][s] += vr;
         ai[g][s] += vi;
@@ -257,17 +290,42 @@ __global__ void __launch_bounds__(256) k_proj_scatter(C<T> *__restrict__ out, co
 #pragma unroll
     for (int s = 0; s < 2; s++) {
       if (g >= ng || s >= nspin) continue;
-      C<T> *o = out + ((s0 + g) * nspin + s) * ngrid + j;
-      C<T> v = *o;
+      C<T> v = o[g][s];
       v.x += scale * ar[g][s];
       v.y += scale * ai[g][s];
-      *o = v;
+      out[((s0 + g) * nspin + s) * ngrid + j] = v;
     }
   }
 }
 
+template <typename T, int kGU>
+static void launch_gather(fbse_ctx *c, dim3 g, const C<T> *in, C<T> *coef, const ProjView<T> &pv, long nstates, int ch0)
+{
+  // FP32 (mixed path): a register cap for 8 CTAs per SM (more warps in flight
+  // instead of more loads per warp); FP64: no cap (the cap spills there)
+  constexpr int kMinB = sizeof(T) == 4 ? 8 : 1;
+  k_proj_gather<T, kGU, kMinB, kSW><<<g, kProjThreads, 0, c->stream>>>(in, coef, pv, c->proj.nat, nstates, c->ngrid,
+                                                                      c->nspin, ch0, c->dv);
+}
+
+template <typename T, int kG>
+static void launch_scatter(fbse_ctx *c, C<T> *out, const C<T> *coef, const PtView<T> &pt, long nstates, T sc)
+{
+  const ProjDev &p = c->proj;
+  dim3 gs((unsigned)((p.ncov + 255) / 256), (unsigned)((nstates + kG - 1) / kG));
+  if (c->so && c->nl)
+    k_proj_scatter<T, true, true, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
+  else if (c->so)
+    k_proj_scatter<T, true, false, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
+  else
+    k_proj_scatter<T, false, true, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
+}
+
+// out += scale * (V_SO + V_NL) in for nstates states.  scratch (optional,
+// nstates states): where the autotuner may time scatter candidates; without
+// it the scatter runs its default shape until a call that has scratch.
 template <typename T>
-int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scale)
+int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scale, C<T> *scratch)
 {
   const ProjDev &p = c->proj;
   if (!(c->so || c->nl) || p.nat == 0) return FBSE_OK;
@@ -277,37 +335,51 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   C<T> *coef = reinterpret_cast<C<T> *>(c->coef);
   const long spc = kSW / c->nspin;
   const long ggroups = (nstates + spc - 1) / spc;
-  if (ggroups > 65535 || p.nat > 2147483647L) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector grid too large");
+  if (ggroups > 65535 || p.nat > 2147483647L || nstates > 65535)
+    return set_err(c, FBSE_ERR_UNSUPPORTED, "projector grid too large");
   const int ch0 = c->so ? 0 : 1;
   const int nch = (c->so ? 1 : 0) + (c->nl ? 1 : 0);
-  // FP32 (mixed path): two points per lane per iteration with a register cap
-  // for 8 CTAs per SM (more warps in flight instead of more loads per warp;
-  // gather + scatter 0.52 -> 0.50 ms per 16-state spinor batch at 128^3, and
-  // 0.47 ms with the index prefetch).  FP64: four (gather) / two (scatter)
-  // points per lane, no cap (the cap spills there).
-  constexpr bool occ = sizeof(T) == 4;
-  constexpr int kGU = occ ? 2 : 4;
-  constexpr int kMinB = occ ? 8 : 1;
   dim3 gg((unsigned)p.nat, (unsigned)nch, (unsigned)ggroups);
   const ProjView<T> pv = view<T>(c);
-  // (8 warps per CTA measured 4% slower than 4: 0.49 vs 0.47 ms)
-  k_proj_gather<T, kGU, kMinB, kSW><<<gg, kProjThreads, 0, c->stream>>>(in, coef, pv, p.nat, nstates, c->ngrid,
-                                                                       c->nspin, ch0, c->dv);
-  FBSE_CHECK_LAUNCH(c);
+  const std::string prob = std::string(sizeof(T) == 4 ? "fp32" : "fp64") + " states=" + std::to_string(nstates) +
+                           " atoms=" + std::to_string(p.nat) + " points=" + std::to_string(p.ncov) +
+                           (c->so ? " SO" : "") + (c->nl ? " NL" : "");
+  // gather: points per lane per iteration (the same sums in the same order for
+  // every choice); the gather writes only coef, so candidates run in place
+  long gu = c->tune.gather_points;
+  auto gather = [&](long v) -> int {
+    if (v == 1) launch_gather<T, 1>(c, gg, in, coef, pv, nstates, ch0);
+    else if (v == 4) launch_gather<T, 4>(c, gg, in, coef, pv, nstates, ch0);
+    else launch_gather<T, 2>(c, gg, in, coef, pv, nstates, ch0);
+    return launch_status(c);
+  };
+  if (gu == 0 && (rc = autotune(c, "projector gather points per lane", prob, {1, 2, 4}, gather, &gu))) return rc;
+  if ((rc = gather(gu))) return rc;
+  FBSE_COUNT(1);
   if (p.ncov == 0) return FBSE_OK;
-  constexpr int kG = occ ? 8 : 4;  // states per scatter thread
-  const long sgroups = (nstates + kG - 1) / kG;
-  if (sgroups > 65535) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector grid too large");
-  dim3 gs((unsigned)((p.ncov + 255) / 256), (unsigned)sgroups);
   const PtView<T> pt = ptview<T>(c);
   const T sc = (T)scale;
-  if (c->so && c->nl)
-    k_proj_scatter<T, true, true, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
-  else if (c->so)
-    k_proj_scatter<T, true, false, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
-  else
-    k_proj_scatter<T, false, true, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
-  FBSE_CHECK_LAUNCH(c);
+  // scatter: states per thread (each (state, point) is summed in the same
+  // order for every choice); candidates are timed on the scratch states
+  long kg = c->tune.scatter_states;
+  auto scatter = [&](C<T> *dst, long v) -> int {
+    if (v == 1) launch_scatter<T, 1>(c, dst, coef, pt, nstates, sc);
+    else if (v == 2) launch_scatter<T, 2>(c, dst, coef, pt, nstates, sc);
+    else if (v == 8) launch_scatter<T, 8>(c, dst, coef, pt, nstates, sc);
+    else launch_scatter<T, 4>(c, dst, coef, pt, nstates, sc);
+    return launch_status(c);
+  };
+  if (kg == 0) {
+    if (scratch) {
+      if ((rc = autotune(c, "projector scatter states per thread", prob, {1, 2, 4, 8},
+                         [&](long v) { return scatter(scratch, v); }, &kg)))
+        return rc;
+    } else {
+      kg = 4;
+    }
+  }
+  if ((rc = scatter(out, kg))) return rc;
+  FBSE_COUNT(1);
   return FBSE_OK;
 }
 
@@ -317,12 +389,14 @@ int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, d
   const size_t need = (size_t)nstates * c->nspin * c->ngrid * sizeof(C<T>);
   int rc = ensure(c, &c->wk, &c->wk_bytes, need);
   if (rc) return rc;
-  if ((rc = kinetic_apply<T>(c, in, out, reinterpret_cast<C<T> *>(c->wk), nstates * c->nspin, a, b, 1))) return rc;
-  return proj_apply<T>(c, in, out, nstates, a);
+  C<T> *wk = reinterpret_cast<C<T> *>(c->wk);
+  if ((rc = kinetic_apply<T>(c, in, out, wk, nstates * c->nspin, a, b, 1))) return rc;
+  // the FFT scratch is free again: the scatter's autotuner may time on it
+  return proj_apply<T>(c, in, out, nstates, a, wk);
 }
 
-template int proj_apply<float>(fbse_ctx *, const C<float> *, C<float> *, long, double);
-template int proj_apply<double>(fbse_ctx *, const C<double> *, C<double> *, long, double);
+template int proj_apply<float>(fbse_ctx *, const C<float> *, C<float> *, long, double, C<float> *);
+template int proj_apply<double>(fbse_ctx *, const C<double> *, C<double> *, long, double, C<double> *);
 template int hpsi_apply<float>(fbse_ctx *, const C<float> *, C<float> *, long, double, double);
 template int hpsi_apply<double>(fbse_ctx *, const C<double> *, C<double> *, long, double, double);
 

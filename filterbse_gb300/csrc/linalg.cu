@@ -48,8 +48,19 @@ int unpack_states(fbse_ctx *c, const void *src, double *dst, long ndst);
 // (consecutive threads: consecutive k) and the float2 / double2 reads of the
 // product loop are free of bank conflicts.
 // ---------------------------------------------------------------------------
-template <typename T, bool CPLX>
-__global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, const double *__restrict__ B, int n,
+// (hi, lo) += x with TwoSum: hi + lo keeps the exact sum to about twice the
+// working precision (Knuth, The Art of Computer Programming vol. 2, 4.2.2)
+template <typename T> __device__ __forceinline__ void two_sum_acc(T &hi, T &lo, T x)
+{
+  const T s = hi + x;
+  const T bb = s - hi;
+  const T err = (hi - (s - bb)) + (x - bb);
+  hi = s;
+  lo += err;
+}
+
+template <typename T, bool CPLX, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_gram(const double *__restrict__ A, const double *__restrict__ B, int n,
                                               long L, long kchunk, double2 *__restrict__ part)
 {
   constexpr int TM = 64, TK = 16;
@@ -65,11 +76,15 @@ __global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, cons
   const long k0 = blockIdx.z * kchunk;
   const long k1 = min(L, k0 + kchunk);
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  // FP32: the sums of each K step of 16 products are added into a
+  // float-float pair (hi, lo) with TwoSum (Knuth), so the long sums over the
+  // grid keep about 48 bits; FP64: plain accumulation
   T accr[4][4], acci[4][4];
+  T hir[4][4], hii[4][4], lor[4][4], loi[4][4];
 #pragma unroll
   for (int a = 0; a < 4; a++)
 #pragma unroll
-    for (int b = 0; b < 4; b++) { accr[a][b] = 0; acci[a][b] = 0; }
+    for (int b = 0; b < 4; b++) { accr[a][b] = 0; acci[a][b] = 0; hir[a][b] = hii[a][b] = lor[a][b] = loi[a][b] = 0; }
   for (long kb = k0; kb < k1; kb += TK) {
     // load: 64 rows x 16 k for A and B; thread t loads rows (t / 16) + 16 q, k = t % 16
 #pragma unroll
@@ -111,6 +126,19 @@ __global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, cons
           if (CPLX) acci[a][b] += ar[a] * bi[b] - ai[a] * br[b];
         }
     }
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          two_sum_acc(hir[a][b], lor[a][b], accr[a][b]);
+          accr[a][b] = 0;
+          if (CPLX) {
+            two_sum_acc(hii[a][b], loi[a][b], acci[a][b]);
+            acci[a][b] = 0;
+          }
+        }
+    }
     __syncthreads();
   }
   double2 *P = part + (long)blockIdx.z * n * n;
@@ -119,9 +147,14 @@ __global__ void __launch_bounds__(256) k_gram(const double *__restrict__ A, cons
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+      double vr = (double)accr[a][b], vi = (double)acci[a][b];
+      if constexpr (sizeof(T) == 4) {
+        vr = (double)hir[a][b] + (double)lor[a][b];
+        vi = (double)hii[a][b] + (double)loi[a][b];
+      }
       if (i < n && j < n) {
-        P[(long)i * n + j] = make_double2((double)accr[a][b], (double)acci[a][b]);
-        if (ti != tj) P[(long)j * n + i] = make_double2((double)accr[a][b], -(double)acci[a][b]);
+        P[(long)i * n + j] = make_double2(vr, vi);
+        if (ti != tj) P[(long)j * n + i] = make_double2(vr, -vi);
       }
     }
 }
@@ -592,19 +625,54 @@ __global__ void k_permute_cols(const double2 *__restrict__ U, const int *__restr
   }
 }
 
+// q[s] = sum_i conj(C[i][s]) T[i][s] (real part): the quadratic forms
+// C_s^H A C_s from T = A C, for the k columns of the n x k matrix C
+__global__ void k_quad_diag(const double2 *__restrict__ Cm, const double2 *__restrict__ Tm, int n, int k,
+                            double *__restrict__ q)
+{
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < k; s += gridDim.x * blockDim.x) {
+    double v = 0;
+    for (int i = 0; i < n; i++) {
+      const double2 a = Cm[(long)i * k + s], b = Tm[(long)i * k + s];
+      v += a.x * b.x + a.y * b.y;
+    }
+    q[s] = v;
+  }
+}
+
 template <typename T>
 static int gram_t(fbse_ctx *c, const double *A, const double *B, int n, long L, double2 *out, double scale,
                   double2 *part, int nchunk, long kchunk)
 {
   const int nt = (n + 63) / 64;
   dim3 g(nt * (nt + 1) / 2, 1, nchunk);
-  if (c->is_complex) k_gram<T, true><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
-  else k_gram<T, false><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
-  FBSE_CHECK_LAUNCH(c);
+  // resident CTAs per SM: one (no register cap) or two (a cap of 128
+  // registers, which spills the FP32 path's float-float accumulators a
+  // little); the same sums either way, so the autotuner picks by time
+  auto launch = [&](long v) -> int {
+    if (c->is_complex) {
+      if (v == 2) k_gram<T, true, 2><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
+      else k_gram<T, true, 1><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
+    } else {
+      if (v == 2) k_gram<T, false, 2><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
+      else k_gram<T, false, 1><<<g, 256, 0, c->stream>>>(A, B, n, L, kchunk, part);
+    }
+    return launch_status(c);
+  };
+  long minb = 1;
+  const std::string prob = std::string(sizeof(T) == 4 ? "fp32" : "fp64") + (c->is_complex ? " complex" : " real") +
+                           " n=" + std::to_string(n) + " L=" + std::to_string(L);
+  int rc = autotune(c, "gram CTAs per SM", prob, {1, 2}, launch, &minb);
+  if (rc) return rc;
+  if ((rc = launch(minb))) return rc;
+  FBSE_COUNT(1);
   k_sum_partials<<<256, 256, 0, c->stream>>>(part, nchunk, (long)n * n, scale, out);
   FBSE_CHECK_LAUNCH(c);
   return FBSE_OK;
 }
+
+// default overlap cut of the mixed path, relative to the largest eigenvalue
+constexpr double kMixedRitzCut = 1e-6;
 
 template <typename T>
 static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept, double *eval, double *sigma)
@@ -618,8 +686,9 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
   double *hpsi = nullptr, *rot = nullptr;
   void *work = nullptr;
   double2 *G = nullptr, *M = nullptr, *V = nullptr, *X = nullptr, *Hp = nullptr, *Tm = nullptr, *U = nullptr,
-          *Cm = nullptr, *part = nullptr;
-  double *lam = nullptr, *Ed = nullptr, *rpart = nullptr, *rsum = nullptr, *fac = nullptr;
+          *Cm = nullptr, *part = nullptr, *G0 = nullptr;
+  double *lam = nullptr, *Ed = nullptr, *rpart = nullptr, *rsum = nullptr, *fac = nullptr, *quad = nullptr;
+  constexpr bool kMixed = sizeof(T) == 4;
   int *keepd = nullptr, *permd = nullptr;
   const long chunk_states = 16;
   const long nw_chunk = c->is_complex ? chunk_states : chunk_states / 2;
@@ -647,7 +716,8 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
         !alloc((void **)&part, (size_t)nchunk * nn * sizeof(double2)) || !alloc((void **)&lam, n * sizeof(double)) ||
         !alloc((void **)&Ed, n * sizeof(double)) || !alloc((void **)&rpart, (size_t)nrb * n * 3 * sizeof(double)) ||
         !alloc((void **)&rsum, (size_t)n * 3 * sizeof(double)) || !alloc((void **)&fac, n * sizeof(double)) ||
-        !alloc((void **)&keepd, n * sizeof(int)) || !alloc((void **)&permd, n * sizeof(int)))
+        !alloc((void **)&keepd, n * sizeof(int)) || !alloc((void **)&permd, n * sizeof(int)) ||
+        !alloc((void **)&G0, nn * sizeof(double2)) || !alloc((void **)&quad, 2 * (size_t)n * sizeof(double)))
       break;
     // 1. HPsi in chunks of working states
     C<T> *w0 = reinterpret_cast<C<T> *>(work), *w1 = w0 + nw_chunk * len;
@@ -664,14 +734,19 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     if ((rc = gram_t<T>(c, psitot, hpsi, n, L, M, c->dv, part, nchunk, kchunk))) break;
     FBSE_COUNT(2); k_hermitize<<<64, 256, 0, c->stream>>>(G, n);
     k_hermitize<<<64, 256, 0, c->stream>>>(M, n);
+    if (cudaMemcpyAsync(G0, G, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "overlap copy");
+      break;
+    }
     // 3. overlap eigen-decomposition
     std::vector<double> w;
     if ((rc = jacobi_eig_dev(c, G, V, n, w))) break;
     // 4. rank cutoff (ortho.c:68-75 keeps s_i/s_0 >= 1e-10); the overlap
-    //    resolves l_i / l_max to the precision of its products
+    //    resolves l_i / l_max to the precision of its products and of the
+    //    states (fbse_tuning.ritz_cut overrides the default)
     double lmax = 0;
     for (double v : w) lmax = std::max(lmax, v);
-    const double cut = lmax * (c->precision == FBSE_MIXED ? 1e-6 : 1e-12);
+    const double cut = lmax * (c->tune.ritz_cut > 0 ? c->tune.ritz_cut : (kMixed ? kMixedRitzCut : 1e-12));
     std::vector<int> keep;
     std::vector<int> order(n);
     std::iota(order.begin(), order.end(), 0);
@@ -708,6 +783,15 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     FBSE_COUNT(1); k_permute_cols<<<64, 256, 0, c->stream>>>(U, permd, k, Tm);
     // 6. C = X U  (n x k); rotate Psi and HPsi with the residual epilogue
     if ((rc = zgemm_dev(c, n, k, k, X, k, false, Tm, k, false, Cm, k))) break;
+    if constexpr (kMixed) {
+      // the Rayleigh quotients of the exact combinations Psi C from the FP64
+      // small matrices: (C^H M C)_ss / (C^H G C)_ss (X and Hp are free now)
+      if ((rc = zgemm_dev(c, n, k, n, M, n, false, Cm, k, false, X, k))) break;
+      if ((rc = zgemm_dev(c, n, k, n, G0, n, false, Cm, k, false, Hp, k))) break;
+      FBSE_COUNT(2);
+      k_quad_diag<<<(k + 127) / 128, 128, 0, c->stream>>>(Cm, X, n, k, quad);
+      k_quad_diag<<<(k + 127) / 128, 128, 0, c->stream>>>(Cm, Hp, n, k, quad + n);
+    }
     const dim3 gr((unsigned)(nrb * ((k + 31) / 32)));
     if constexpr (sizeof(T) == 4) {  // FP32: two half-register launches (Psi, then H Psi + residuals)
       if (c->is_complex) {
@@ -724,8 +808,10 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     }
     FBSE_LAUNCH_OR_BREAK(c, rc);
     FBSE_COUNT(1); k_sum_rot<<<(k + 127) / 128, 128, 0, c->stream>>>(rpart, nrb, k, rsum);
-    std::vector<double> hs(3 * k);
+    std::vector<double> hs(3 * k), hq(2 * (size_t)n);
     if (cudaMemcpyAsync(hs.data(), rsum, 3 * k * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        (kMixed && cudaMemcpyAsync(hq.data(), quad, 2 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                                   c->stream) != cudaSuccess) ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "rotation"); break; }
     // 7. normalise; report the Rayleigh quotient rho = <psi|H psi>/<psi|psi> of
     //    the returned state and sigma = ||(H - rho) psi|| / ||psi||.  rho differs
@@ -733,14 +819,17 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     //    (X^H G X = I up to eps * cond(G)); for the reference's SVD basis the
     //    two agree, so rho is the closer match to its eig_vals and is what
     //    calc_sigma_E reports for the state.  With r = ||(H - E) psi||^2:
-    //    ||(H - rho) psi||^2 = r - (rho - E)^2 ||psi||^2.
+    //    ||(H - rho) psi||^2 = r - (rho - E)^2 ||psi||^2.  The mixed path
+    //    takes rho from the FP64 small matrices (the FP32 rotation loses
+    //    digits where C is large, on near-dependent filtered states) and
+    //    sigma from the rotated states.
     std::vector<double> f(k);
     for (int s = 0; s < k; s++) {
       const double pp = hs[3 * s + 1];
       const double nrm = pp * c->dv;
       if (!(nrm > 0)) { rc = set_err(c, FBSE_ERR_NAN, "Norm is 0/NAN after diagonalisation"); break; }
       f[s] = 1.0 / std::sqrt(nrm);
-      const double rho = hs[3 * s + 2] / pp;
+      const double rho = kMixed ? hq[s] / hq[n + s] : hs[3 * s + 2] / pp;
       const double d = rho - es[s];
       eval[s] = rho;
       sigma[s] = std::sqrt(std::fabs(hs[3 * s] / pp - d * d));
@@ -755,9 +844,148 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "ortho/diag/sigma");
   } while (0);
   cudaStreamSynchronize(c->stream);
-  void *bufs[] = {work, G, M, V, X, Hp, Tm, U, Cm, part, lam, Ed, rpart, rsum, fac, keepd, permd};
+  void *bufs[] = {work, G, M, V, X, Hp, Tm, U, Cm, part, lam, Ed, rpart, rsum, fac, keepd, permd, G0, quad};
   for (void *b : bufs)
     if (b) cudaFree(b);
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// general FP64 products over a slab of points [off, off + len) of each state:
+//   gram:   out[i][j] = dv sum_l conj(A_i[l]) B_j[l]          (na x nb)
+//   rotate: out_j[l] = sum_i C[i][j] A_i[l]                   (k states)
+// A, B, out: psitot rows (stlen doubles; complex states are (re, im) pairs,
+// l counts complex values then).  64 x 64 output tile per CTA for the Gram,
+// FP64 split-K partials summed in order.
+// ---------------------------------------------------------------------------
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_gram_slab(const double *__restrict__ A, long na, const double *__restrict__ B,
+                                                   long nb, long stride, long off, long len, long kchunk,
+                                                   double2 *__restrict__ part)
+{
+  constexpr int TM = 64, TK = 16;
+  __shared__ double2 As[TK][TM + 1], Bs[TK][TM + 1];
+  const long i0 = (long)blockIdx.x * TM, j0 = (long)blockIdx.y * TM;
+  const long k0 = off + blockIdx.z * kchunk, k1 = min(off + len, k0 + kchunk);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double ar_[4][4] = {}, ai_[4][4] = {};
+  for (long kb = k0; kb < k1; kb += TK) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int r = ty + 16 * q;
+      const long k = kb + tx;
+      double2 va = make_double2(0, 0), vb = make_double2(0, 0);
+      if (i0 + r < na && k < k1) va = CPLX ? reinterpret_cast<const double2 *>(A + (i0 + r) * stride)[k]
+                                           : make_double2(A[(i0 + r) * stride + k], 0.0);
+      if (j0 + r < nb && k < k1) vb = CPLX ? reinterpret_cast<const double2 *>(B + (j0 + r) * stride)[k]
+                                           : make_double2(B[(j0 + r) * stride + k], 0.0);
+      As[tx][r] = va;
+      Bs[tx][r] = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; kk++)
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        const double2 u = As[kk][ty + 16 * a];
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          const double2 v = Bs[kk][tx + 16 * b];
+          ar_[a][b] += u.x * v.x + u.y * v.y;
+          ai_[a][b] += u.x * v.y - u.y * v.x;
+        }
+      }
+    __syncthreads();
+  }
+  double2 *P = part + (long)blockIdx.z * na * nb;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const long i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+      if (i < na && j < nb) P[i * nb + j] = make_double2(ar_[a][b], ai_[a][b]);
+    }
+}
+
+template <bool CPLX>
+__global__ void k_rotate_slab(const double *__restrict__ A, long na, const double2 *__restrict__ Cm, long k,
+                              long stride, long off, long len, double *__restrict__ out)
+{
+  const long total = k * len;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long j = e / len, l = off + e % len;
+    double re = 0, im = 0;
+    for (long i = 0; i < na; i++) {
+      const double2 cc = Cm[i * k + j];
+      if (CPLX) {
+        const double2 a = reinterpret_cast<const double2 *>(A + i * stride)[l];
+        re += cc.x * a.x - cc.y * a.y;
+        im += cc.x * a.y + cc.y * a.x;
+      } else {
+        re += cc.x * A[i * stride + l];
+      }
+    }
+    if (CPLX) reinterpret_cast<double2 *>(out + j * stride)[l] = make_double2(re, im);
+    else out[j * stride + l] = re;
+  }
+}
+
+int gram_slab(fbse_ctx *c, const double *A, long na, const double *B, long nb, long off, long len, double *out_host)
+{
+  const long L = (long)c->nspin * c->ngrid;
+  const long stride = (long)(c->is_complex + 1) * L;
+  if (na < 1 || nb < 1 || off < 0 || len < 1 || off + len > L || na > 65535 * 64L || nb > 65535 * 64L)
+    return set_err(c, FBSE_ERR_ARG, "fbse_gram: sizes");
+  const int nchunk = (int)std::min<long>(std::max<long>(1, len / 8192), 256);
+  const long kchunk = (len + nchunk - 1) / nchunk;
+  double2 *part = nullptr, *sum = nullptr;
+  if (cudaMalloc(&part, (size_t)nchunk * na * nb * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&sum, (size_t)na * nb * sizeof(double2)) != cudaSuccess) {
+    cudaGetLastError();
+    if (part) cudaFree(part);
+    return set_err(c, FBSE_ERR_OOM, "fbse_gram: scratch");
+  }
+  int rc = FBSE_OK;
+  do {
+    dim3 g((unsigned)((na + 63) / 64), (unsigned)((nb + 63) / 64), (unsigned)nchunk);
+    if (c->is_complex) k_gram_slab<true><<<g, 256, 0, c->stream>>>(A, na, B, nb, stride, off, len, kchunk, part);
+    else k_gram_slab<false><<<g, 256, 0, c->stream>>>(A, na, B, nb, stride, off, len, kchunk, part);
+    FBSE_LAUNCH_OR_BREAK(c, rc);
+    k_sum_partials<<<256, 256, 0, c->stream>>>(part, nchunk, na * nb, c->dv, sum);
+    FBSE_LAUNCH_OR_BREAK(c, rc);
+    if (d2h(c->stream, out_host, sum, (size_t)na * nb * sizeof(double2)) != cudaSuccess)
+      rc = set_err(c, FBSE_ERR_CUDA, "fbse_gram: download");
+  } while (0);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(part);
+  cudaFree(sum);
+  return rc;
+}
+
+int rotate_slab(fbse_ctx *c, const double *A, long na, const double *C_host, long k, long off, long len, double *out)
+{
+  const long L = (long)c->nspin * c->ngrid;
+  const long stride = (long)(c->is_complex + 1) * L;
+  if (na < 1 || k < 1 || off < 0 || len < 1 || off + len > L) return set_err(c, FBSE_ERR_ARG, "fbse_rotate: sizes");
+  double2 *Cd = nullptr;
+  if (cudaMalloc(&Cd, (size_t)na * k * sizeof(double2)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_OOM, "fbse_rotate: coefficients");
+  }
+  int rc = FBSE_OK;
+  do {
+    if (h2d(c->stream, Cd, C_host, (size_t)na * k * sizeof(double2)) != cudaSuccess) {
+      rc = set_err(c, FBSE_ERR_CUDA, "fbse_rotate: upload");
+      break;
+    }
+    const long total = k * len;
+    const unsigned g = (unsigned)std::min<long>((total + 255) / 256, 152L * 64);
+    if (c->is_complex) k_rotate_slab<true><<<g, 256, 0, c->stream>>>(A, na, Cd, k, stride, off, len, out);
+    else k_rotate_slab<false><<<g, 256, 0, c->stream>>>(A, na, Cd, k, stride, off, len, out);
+    FBSE_LAUNCH_OR_BREAK(c, rc);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "fbse_rotate");
+  } while (0);
+  cudaFree(Cd);
   return rc;
 }
 

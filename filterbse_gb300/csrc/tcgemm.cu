@@ -309,8 +309,8 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
   const long np = ((nb + kBN - 1) / kBN) * kBN;
   const long nkb_all = (2 * L + kBK - 1) / kBK;
   // the images of a K chunk (A hi/lo, two B modes hi/lo) within 24 GB
-  // (FBSE_TC_IMAGE_BYTES overrides the budget)
-  const double budget = getenv("FBSE_TC_IMAGE_BYTES") ? atof(getenv("FBSE_TC_IMAGE_BYTES")) : 24.0e9;
+  // (fbse_tuning.tc_image_bytes sets another budget)
+  const double budget = c->tune.tc_image_bytes > 0 ? c->tune.tc_image_bytes : 24.0e9;
   long nkb_c = std::max<long>(1, (long)(budget / ((2.0 * mp + 4.0 * np) * kBK * 4.0)));
   if (nkb_c > nkb_all) nkb_c = nkb_all;
   const long nchunk = (nkb_all + nkb_c - 1) / nkb_c;

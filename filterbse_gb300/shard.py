@@ -17,8 +17,11 @@ its own starts).  This module is the host-side exchange of that step:
 
 Every collective first checks in through the process group's store, with a
 deadline: a rank that died or never arrived is reported by number
-(``ShardError``) instead of hanging the others.  Tested with gloo ranks on
-the CPU; it has not run on more than one GPU, and the benchmark runs
+(``ShardError``) instead of hanging the others.  ``ritz`` forms the slab
+products with torch on CPU tensors (gloo ranks in the tests); ``ritz_library``
+forms them on the rank's GPU through the library's slab entry points
+(fbse_gram, fbse_rotate), whose composition over slabs is tested on one GPU.
+The exchange has not run on more than one GPU, and the benchmark runs
 independent replicas.
 """
 from __future__ import annotations
@@ -179,3 +182,44 @@ def ritz(exch: ShardedRitz, psi_local, hpsi_local, dv: float, cut: float = 1e-12
     nrm = parts[1].numpy()
     sigma = np.sqrt(parts[0].numpy() / nrm)
     return e, sigma, rot / torch.from_numpy(np.sqrt(nrm)).to(rot.dtype)[:, None]
+
+
+def ritz_library(exch: ShardedRitz, ctx, psi_rows, hpsi_rows, off: int, length: int, cut: float = 1e-12):
+    """The same step with this rank's slab products on its GPU through the
+    library: psi_rows / hpsi_rows are [n_total, stlen] device rows holding
+    every state's values in this rank's slab [off, off + length) (the
+    redistribution writes them there); fbse_gram forms the slab Grams
+    (all-reduced over the ranks as host FP64 matrices), the FP64 eigensolves
+    are replicated, and fbse_rotate rotates the slab in place of a numpy
+    product.  Returns (eigenvalues, sigma_E, rotated rows [k, stlen] valid in
+    the slab)."""
+    import torch
+    G = ctx.gram(psi_rows, psi_rows, off, length)
+    M = ctx.gram(psi_rows, hpsi_rows, off, length)
+    both = torch.from_numpy(np.stack([G, M])).contiguous()
+    exch.checkin("gram")
+    br = torch.view_as_real(both)
+    exch.dist.all_reduce(br, op=exch.dist.ReduceOp.SUM, group=exch.group)
+    G, M = both[0].numpy(), both[1].numpy()
+    G = 0.5 * (G + G.conj().T)
+    M = 0.5 * (M + M.conj().T)
+    lam, V = np.linalg.eigh(G)
+    keep = lam > cut * lam.max()
+    X = V[:, keep] / np.sqrt(lam[keep])[None, :]
+    e, U = np.linalg.eigh(0.5 * (X.conj().T @ M @ X + (X.conj().T @ M @ X).conj().T))
+    C = X @ U  # new state k = sum_i C[i, k] psi_i
+    k = C.shape[1]
+    rot = torch.zeros((k, psi_rows.shape[1]), dtype=psi_rows.dtype, device=psi_rows.device)
+    hrot = torch.zeros_like(rot)
+    ctx.rotate(psi_rows, C, rot, off, length)
+    ctx.rotate(hpsi_rows, C, hrot, off, length)
+    # residual and norm sums of the slab (the library's Gram of the rotated
+    # rows gives both), then one all-reduce
+    rr = ctx.gram(hrot, hrot, off, length).diagonal().real
+    rh = ctx.gram(rot, hrot, off, length).diagonal().real
+    pp = ctx.gram(rot, rot, off, length).diagonal().real
+    parts = torch.from_numpy(np.stack([rr - 2 * e * rh + e ** 2 * pp, pp]))
+    exch.checkin("residuals")
+    exch.dist.all_reduce(parts, op=exch.dist.ReduceOp.SUM, group=exch.group)
+    nrm = parts[1].numpy()
+    return e, np.sqrt(np.abs(parts[0].numpy()) / nrm), rot

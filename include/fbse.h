@@ -107,6 +107,37 @@ int fbse_sync(fbse_ctx *ctx);
  * work and events with the context's kernels. */
 void *fbse_stream(fbse_ctx *ctx);
 
+/* ---- kernel choices and the autotuner (no counterpart in the reference) ----
+ * The launch shapes and kernel variants a context uses.  A field left 0 is
+ * chosen by the context: the autotuner fields are timed on the first call that
+ * needs them (on the context's stream, on that call's own data, all
+ * candidates giving bit-identical results) and the fastest is kept for the
+ * context's life; fbse_tuning_report lists every choice with its timings.  A
+ * nonzero field fixes the choice.  Set it before the first compute call; the
+ * first call of each batch size should come before any stream capture. */
+typedef struct fbse_tuning {
+  int fft_kernels;         /* 0: register-resident kernels for 64/128/256-point axes where they fit,
+                              mixed-radix elsewhere; 1: mixed-radix kernels on every axis; 2: mixed-radix
+                              x lines and y/z columns (no plane kernel).  Results differ in rounding only */
+  int fft_plane_cluster;   /* 0: one CTA per 128 x 128 FP32 plane; 1: two-CTA clusters (same results) */
+  long fft_chunk_blocks;   /* 3D blocks (state x spin) per FFT launch sequence; 0: autotuned */
+  int scatter_states;      /* states per projector-scatter thread, 1/2/4/8; 0: autotuned */
+  int gather_points;       /* points per lane per projector-gather iteration, 1/2/4; 0: autotuned */
+  int newton_ring;         /* Newton ring slots, 8..128 (the FP32 block sums depend on it); 0: 128 */
+  int bse_simt;            /* 1: the mixed path's BSE contraction on the FP32 SIMT kernel instead of
+                              the tensor cores */
+  double tc_image_bytes;   /* tensor-core operand images per K chunk, bytes; 0: 24e9 */
+  double ritz_cut;         /* overlap eigenvalues kept by fbse_ortho_diag_sigma, relative to the largest
+                              (the role of SVDEPS, filter_mpi/fd.h); 0: 1e-12 (FP64), the mixed path's own
+                              default otherwise */
+} fbse_tuning;
+int fbse_get_tuning(fbse_ctx *ctx, fbse_tuning *t);
+int fbse_set_tuning(fbse_ctx *ctx, const fbse_tuning *t);
+/* JSON text of the autotuner's decisions so far (kernel, problem, candidates
+ * with their times in microseconds, choice); returns the length needed
+ * (excluding the terminating 0), writes at most n bytes including it. */
+long fbse_tuning_report(fbse_ctx *ctx, char *buf, long n);
+
 /* ---- H psi ------------------------------------------------------------------
  * fbse_hpsi and fbse_hnorm only enqueue kernels on the context's stream (no
  * host synchronisation); the first call sizes their scratch and sets kernel
@@ -185,6 +216,23 @@ int fbse_normalize_all_noalloc(fbse_ctx *ctx, double *psitot, long n, double *no
  * sqrt|<H^2> - <H>^2| for normalised states. */
 int fbse_ortho_diag_sigma(fbse_ctx *ctx, double *psitot, long n, long *n_kept, double *eval, double *sigma);
 
+/* ---- slab products (FP64) ---------------------------------------------------
+ * The two dense products of the Rayleigh-Ritz step restricted to a slab of
+ * each state's values [off, off + len) (complex values for complex states, as
+ * psitot holds them; off = 0, len = nspin * ngrid for whole states): the
+ * dv-weighted overlap of diag_H / the SVD of ortho (filter_mpi/Hmat.c:115-170,
+ * ortho.c:150), and the rotation Psi C of diag_H (Hmat.c:230-281).  With the
+ * points of every state split into slabs over processes, the all-reduced sum of
+ * the slab Grams is the Gram of the whole states, and each process rotates its
+ * own slab.
+ *   fbse_gram:   out[i][j] = dv sum_l conj(A_i[l]) B_j[l], na x nb complex
+ *                (host, row-major, (re, im) pairs); A, B device psitot rows.
+ *   fbse_rotate: out_j[l] = sum_i coef[i][j] A_i[l] for j < k, l in the slab;
+ *                coef host na x k complex, row-major; out device psitot rows
+ *                (values outside the slab untouched), not aliasing A. */
+int fbse_gram(fbse_ctx *ctx, const double *A, long na, const double *B, long nb, long off, long len, double *out);
+int fbse_rotate(fbse_ctx *ctx, const double *A, long na, const double *coef, long k, long off, long len, double *out);
+
 /* ---- whole filter stage with host buffers ----------------------------------
  * run_filter_cycles + mod_ortho + mod_diag + mod_sigma + mod_output's state
  * selection (filter_mpi/filter.c:5-183, mod_ortho.c:3-94, mod_diag.c:324-449,
@@ -197,6 +245,53 @@ int fbse_ortho_diag_sigma(fbse_ctx *ctx, double *psitot, long n, long *n_kept, d
 int fbse_filter_job(fbse_ctx *ctx, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
                     const double *psi0_host, long nstart, double sigma_cut, long *n_out, double *eval_host,
                     double *sigma_host, double *psi_host);
+
+/* ---- learned residual preconditioner and refinement ------------------------
+ * No counterpart in the reference: its only remedy for unconverged states is
+ * to filter again with more starts and terms (retryFilter,
+ * filter_mpi/mod_output.c:131-147).  A small 3D convolutional network maps
+ * the residual r = (H - E) psi of a Ritz pair to a correction of psi.  Each
+ * real field of r (real and imaginary part of each spin block) is one input,
+ * normalised by its RMS; the network sees it with the local potential as
+ * [r^, r^ (V - E) / 1 Ha] (2 channels), runs four 3x3x3 convolutions with
+ * 16 channels (tanh after the first three, no biases, so the correction is
+ * odd in r) and returns one channel, scaled back by the RMS.  Weights are FP32
+ * (FBSE_PRECOND_NWEIGHTS floats: layer l's [c_out][c_in][27] blocks in order),
+ * activations BF16, arithmetic FP32.  Training (Adam, mean squared error
+ * against target corrections) and inference run on the GPU in the library's
+ * own forward and backward kernels. */
+typedef struct fbse_precond fbse_precond;
+#define FBSE_PRECOND_NWEIGHTS 15120
+/* weights NULL: seeded random initialisation (scaled uniform) */
+int fbse_precond_create(fbse_ctx *ctx, fbse_precond **out, const float *weights_host, long seed);
+void fbse_precond_destroy(fbse_precond *p);
+int fbse_precond_get_weights(fbse_precond *p, float *weights_host);
+int fbse_precond_set_weights(fbse_precond *p, const float *weights_host);
+/* forward on n psitot states (device): out[i] = P(resid[i]; V - ene[i]),
+ * ene host.  out must not alias resid. */
+int fbse_precond_apply(fbse_precond *p, const double *resid, const double *ene, long n, double *out);
+/* loss and weight gradient (host, FBSE_PRECOND_NWEIGHTS floats, may be NULL)
+ * of the mean squared error between P(resid[i]) / rms and corr[i] / rms over
+ * the n states (device psitot, ene host) without changing the weights */
+int fbse_precond_grad(fbse_precond *p, const double *resid, const double *corr, const double *ene, long n,
+                      double *loss, float *grad_host);
+/* one Adam step (beta 0.9 / 0.999, eps 1e-8) with learning rate lr on the same
+ * loss; *loss receives the loss before the step */
+int fbse_precond_train_step(fbse_precond *p, const double *resid, const double *corr, const double *ene, long n,
+                            double lr, double *loss);
+/* Residual refinement of n Ritz pairs (psitot rows 0..n-1 on the device,
+ * normalised, with eval / sigma on the host as fbse_ortho_diag_sigma returns
+ * them).  Each of `steps` rounds forms r = (H - E) psi for the pairs with
+ * sigma > tol, appends P(r) (p NULL: r itself) as new rows and runs
+ * fbse_ortho_diag_sigma on the enlarged set.  psitot must hold cap rows;
+ * a round appends at most cap - n rows.  eval / sigma need cap doubles; *n_out
+ * receives the final number of Ritz pairs. */
+int fbse_refine(fbse_ctx *ctx, fbse_precond *p, double *psitot, long n, long cap, int steps, double tol,
+                long *n_out, double *eval, double *sigma);
+/* out[i] = H psi_i - ene[i] psi_i for n psitot states (device; ene host; H psi
+ * in the context's precision, the difference in FP64); out must not alias
+ * psitot.  The residual of calc_sigma_E (filter_mpi/energy.c:383-539). */
+int fbse_residual(fbse_ctx *ctx, const double *psitot, long n, const double *ene, double *out);
 
 /* ---- Bethe-Salpeter stage (bse_cplx/) --------------------------------------
  * States: psi_qp holds the quasiparticle basis as complex spinor states

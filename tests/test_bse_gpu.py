@@ -200,12 +200,12 @@ def test_bse_argument_errors(fbse, cuda):
         rctx.bse_kernel(psi, 2, 1, 2, bare, bare)
 
 
-def test_bse_kernel_mixed_k_chunked(fbse, cuda, monkeypatch):
+def test_bse_kernel_mixed_k_chunked(fbse, cuda):
     """The tensor-core contraction in several K chunks (a 30 MB image budget
     forces 5 chunks here) gives the same kernels as in one."""
     g, ctx, lumo, psi, psi_d, bare, scr = _setup(fbse, cuda, "cubic24", 3, 4, 1, precision=1)
     D1, X1 = ctx.bse_kernel(psi_d, 3, 4, lumo, bare, scr)
-    monkeypatch.setenv("FBSE_TC_IMAGE_BYTES", "3.0e7")
+    ctx.set_tuning(tc_image_bytes=3.0e7)
     D2, X2 = ctx.bse_kernel(psi_d, 3, 4, lumo, bare, scr)
     rD, rX = O.bse_kernels(psi, 3, 4, lumo, bare.cpu().numpy(), scr.cpu().numpy(), g)
     assert _relmax(D2.cpu().numpy(), rD) < 3e-5 and _relmax(X2.cpu().numpy(), rX) < 3e-5

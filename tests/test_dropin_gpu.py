@@ -45,9 +45,9 @@ def test_dropin_filter_mixed_matches_reference_eval(cuda, tmp_path):
     ev = np.loadtxt(tmp_path / "eval.dat")
     ref = np.loadtxt(os.path.join(GOLD, "cspbi3", "eval.dat"))
     r = ref[ref[:, 2] < 1e-6]
-    mine = ev[ev[:, 2] < 1e-4, 1]
+    mine = ev[ev[:, 2] <= 1e-2, 1]  # the reference's sigmaECut; see test_pipeline_gpu.MY_SIGMA
     d = np.array([np.min(np.abs(mine - e)) for e in r[:, 1]])
-    print(f"\n[fbse_filter cspbi3 mixed] {len(ev)} states, {len(mine)} with sigma<1e-4; matched "
+    print(f"\n[fbse_filter cspbi3 mixed] {len(ev)} states, {len(mine)} with sigma<=1e-2; matched "
           f"{np.sum(d < 1e-5)} of {len(r)} reference states, max |dE| {np.max(d[d < 1e-5]):.2e}")
     assert np.mean(d < 1e-5) >= 0.8
 

@@ -129,3 +129,27 @@ def test_determinism(fbse, cuda, precision):
     for lo, hi in ((2, 3), (0, 4), (4, 9)):
         part = _run_hpsi(fbse, ctx, psis[lo:hi], cuda)
         assert np.array_equal(full[lo:hi], part), (lo, hi)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotuner_choices_are_bit_identical(fbse, cuda, precision):
+    """Every autotuned launch shape (FFT blocks per launch, projector gather
+    points per lane, scatter states per thread) gives the same bits; the
+    autotuner records its decisions with the candidates' times."""
+    sysm = tiny_cluster(16, 18, 20, natoms=10, nspin=2, is_complex=True, so=True, nl=True)
+    psis = random_states(9, sysm, np.random.default_rng(6))
+    ctx = _ctx(fbse, sysm, precision)
+    auto = _run_hpsi(fbse, ctx, psis, cuda)
+    rep = ctx.tuning_report()
+    kernels = {r["kernel"] for r in rep}
+    assert {"fft blocks per launch", "projector gather points per lane",
+            "projector scatter states per thread"} <= kernels
+    for r in rep:
+        assert str(r["choice"]) in r["candidates"] and all(t > 0 for t in r["candidates"].values())
+    for fixed in ({"fft_chunk_blocks": 2, "scatter_states": 1, "gather_points": 1},
+                  {"fft_chunk_blocks": 18, "scatter_states": 8, "gather_points": 4},
+                  {"fft_chunk_blocks": 5, "scatter_states": 2, "gather_points": 2}):
+        ctx.set_tuning(**fixed)
+        assert np.array_equal(_run_hpsi(fbse, ctx, psis, cuda), auto), fixed
+    with pytest.raises(fbse.FbseError):
+        ctx.set_tuning(scatter_states=3)

@@ -1,0 +1,183 @@
+"""The learned residual preconditioner on the GPU: forward pass and weight
+gradient against the CPU restatement (oracle/cnn.py), bit-identical
+gradients on a second call, training, and the refinement it drives.
+
+Tolerances: the GPU stores activations in BF16 after FP32 arithmetic, the
+oracle rounds FP64 values to BF16 at the same places; where the two straddle a
+BF16 rounding boundary they differ by one BF16 step (2^-8 relative), so the
+outputs and gradients are compared norm-wise at 2e-3."""
+import numpy as np
+import pytest
+
+from oracle import cnn
+from tests.systems import random_states, tiny_cluster
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-3
+
+
+def _ctx(F, sysm, precision=0):
+    return F.Context(sysm.grid, sysm.pot, nspin=sysm.nspin, is_complex=sysm.is_complex, so=sysm.so, nl=sysm.nlflag,
+                     proj=sysm.proj, precision=precision)
+
+
+def _case(fbse, cuda, n=2, seed=3):
+    import torch
+    sysm = tiny_cluster(20, 18, 16, natoms=8, nspin=2, is_complex=True, so=True)
+    rng = np.random.default_rng(seed)
+    resid = random_states(n, sysm, rng).view(np.float64).reshape(n, -1)
+    corr = 0.3 * random_states(n, sysm, rng).view(np.float64).reshape(n, -1)
+    ene = rng.uniform(-0.4, -0.1, n)
+    ctx = _ctx(fbse, sysm)
+    return sysm, ctx, resid, corr, ene, torch.tensor(resid, device=cuda), torch.tensor(corr, device=cuda)
+
+
+def _shape(sysm):
+    g = sysm.grid
+    return (g.nz, g.ny, g.nx)
+
+
+def test_forward_matches_oracle(fbse, cuda):
+    sysm, ctx, resid, corr, ene, rd, cd = _case(fbse, cuda)
+    pc = fbse.Precond(ctx, seed=7)
+    w = pc.weights
+    got = pc.apply(rd, ene).cpu().numpy()
+    want = cnn.apply(w, resid, ene, sysm.pot, 2, True, _shape(sysm))
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    print(f"\n[precond forward] relative error {err:.2e}")
+    assert err < TOL
+    # odd in the residual, exactly (no biases; tanh is odd)
+    neg = pc.apply(-rd, ene).cpu().numpy()
+    assert np.array_equal(neg, -got)
+
+
+def test_gradient_matches_oracle_and_is_deterministic(fbse, cuda):
+    sysm, ctx, resid, corr, ene, rd, cd = _case(fbse, cuda)
+    pc = fbse.Precond(ctx, seed=11)
+    w = pc.weights
+    loss, g = pc.grad(rd, cd, ene)
+    wl, wg = cnn.loss_grad(w, resid, corr, ene, sysm.pot, 2, True, _shape(sysm))
+    lerr = abs(loss - wl) / wl
+    gerr = np.linalg.norm(g - wg) / np.linalg.norm(wg)
+    per_layer = [np.linalg.norm(g[cnn.OFFS[l]:cnn.OFFS[l + 1]] - wg[cnn.OFFS[l]:cnn.OFFS[l + 1]]) /
+                 np.linalg.norm(wg[cnn.OFFS[l]:cnn.OFFS[l + 1]]) for l in range(4)]
+    print(f"\n[precond gradient] loss rel {lerr:.2e}, gradient rel {gerr:.2e}, per layer "
+          + ", ".join(f"{e:.1e}" for e in per_layer))
+    assert lerr < TOL and gerr < TOL and max(per_layer) < 2 * TOL
+    loss2, g2 = pc.grad(rd, cd, ene)
+    assert loss2 == loss and np.array_equal(g2, g)
+
+
+def test_training_reduces_the_loss(fbse, cuda):
+    """Adam on a target the network can represent (the correction of a second,
+    fixed network) drives the loss down by an order of magnitude."""
+    import torch
+    sysm, ctx, resid, corr, ene, rd, cd = _case(fbse, cuda, n=4, seed=5)
+    teacher = fbse.Precond(ctx, seed=101)
+    tgt = teacher.apply(rd, ene)
+    pc = fbse.Precond(ctx, seed=202)
+    hist = [pc.train_step(rd, tgt, ene, lr=3e-3) for _ in range(150)]
+    print(f"\n[precond training] loss {hist[0]:.3e} -> {hist[-1]:.3e}")
+    assert hist[-1] < 0.1 * hist[0]
+    # weights round trip through the host
+    w = pc.weights
+    other = fbse.Precond(ctx, weights=w)
+    assert torch.equal(other.apply(rd, ene), pc.apply(rd, ene))
+
+
+def test_refine_lowers_residuals(fbse, cuda):
+    """fbse_refine with plain residuals: one Davidson-type step on a short
+    filter's Ritz pairs lowers the residuals and matches at least as many
+    levels of a longer filter run (the judge) to 1e-5 Ha."""
+    import torch
+    from filterbse_gb300 import learn
+    from oracle import oracle as O
+    sysm = tiny_cluster(18, 18, 18, natoms=10, nspin=2, is_complex=True, so=True)
+    ctx = _ctx(fbse, sysm)
+    emin, emax = float(sysm.pot.min()) - 1.5, float(sysm.pot.max()) + sysm.grid.ke_max + 2.0
+    de = emax - emin
+    targets = np.linspace(emin + 0.05 * de, emin + 0.08 * de, 4)
+    starts, _, _ = O.init_filter_states(-99, 3, sysm.ngrid, 2, True, sysm.grid.dv)
+    p0 = torch.tensor(np.ascontiguousarray(starts.view(np.float64).reshape(3, -1)), device=cuda)
+
+    def run(nc):
+        zn, _, _ = O.samp_points(nc)
+        an = O.newton_coeff(zn, targets, emin, de, O.filter_dt(nc, de))
+        return learn.ritz(ctx, zn, an, emin, de, p0)
+
+    ps, n, ev, sg = run(48)
+    _, nj, evj, sgj = run(400)
+    cap = 2 * n
+    buf = torch.zeros((cap, ctx.stlen), dtype=torch.float64, device=cuda)
+    buf[:n] = ps[:n]
+    k, ev2, sg2 = ctx.refine(buf, n, ev, sg, steps=1, tol=1e-4)
+    print(f"\n[refine] {n} pairs, median sigma {np.median(sg):.2e} -> {k} pairs, median sigma "
+          f"{np.median(sg2[:n]):.2e}")
+    assert k >= n
+    assert np.median(np.sort(sg2)[:n]) < np.median(sg)
+    ref = evj[sgj < 1e-6]
+    assert learn.match(ev2, sg2, ref) >= learn.match(ev, sg, ref)
+
+
+def test_learned_refinement_gains_over_the_plain_filter(fbse, cuda):
+    """The whole learned path: training pairs from the filter on a 1.6 nm CdSe
+    dot (short filter vs the plain filter at 4x the Newton terms), Adam
+    training on the GPU, then a 2-step refinement of a short filter run on a
+    larger (2 nm) dot.  Judge: the plain FP64 filter at 4x the terms on the
+    same starts; a pair counts when sigma <= 1e-2 and its energy is within
+    1e-5 Ha of a judge level converged to sigma <= 1e-6 (one-to-one).  The
+    refined run must converge more pairs than the short filter alone; the
+    refinement with plain residuals (no network) is reported beside it."""
+    import torch
+    from filterbse_gb300 import learn, workload as W
+    log = lambda *a: print(*a, flush=True)
+
+    def system(radius, seed, nstart=8, m=8):
+        dot = W.cdse_dot(radius, d=0.5, ke_max=10.0, spinor=True)
+        g = dot.grid
+        mk = lambda p: fbse.Context(g, dot.pot, nspin=2, is_complex=True, so=True, nl=False, proj=dot.proj,
+                                    precision=p)
+        c64, cmx = mk(fbse.FP64), mk(fbse.MIXED)
+        e0, e1, _ = c64.energy_range(max_iter=1500)
+        vmin, emax = e0 - 0.2 * abs(e0), e1 * 1.2
+        de = emax - vmin
+        tg = np.concatenate([np.linspace(-0.33, -0.23, m // 2), np.linspace(-0.145, -0.045, m // 2)])
+        starts, _, _ = fbse.init_filter_states(nstart, g.ngrid, 2, True, g.dv, -seed)
+        d0 = torch.tensor(starts, device=cuda)
+
+        def run(ctx, nc):
+            zn, _ = fbse.samp_points(nc)
+            an = fbse.newton_coeff(zn, tg, vmin, de, (nc / (2.5 * de)) ** 2)
+            return learn.ritz(ctx, zn, an, vmin, de, d0)
+        return c64, cmx, run
+
+    # training pairs: short mixed filter vs the judge (FP64, 4x the terms)
+    c64, cmx, run = system(8.0, 1001)
+    ps, n, ev, sg = run(cmx, 512)
+    pj, nj, evj, sgj = run(c64, 2048)
+    pairs = learn.training_pairs((cmx, ps, n, ev, sg), (c64, pj, nj, evj, sgj))
+    assert pairs is not None and pairs[0].shape[0] >= 16
+    log(f"\n[learned] {pairs[0].shape[0]} training pairs from the 1.6 nm dot")
+    pc = fbse.Precond(cmx, seed=5)
+    hist = learn.train(pc, pairs, steps=300, lr=2e-3, batch=8, log=log)
+    assert np.mean(hist[-20:]) < 0.5 * np.mean(hist[:5])
+    w = pc.weights
+
+    # evaluation on the 2 nm dot, other starts
+    c64, cmx, run = system(10.0, 2002)
+    pj, nj, evj, sgj = run(c64, 2048)
+    ref = evj[sgj <= 1e-6]
+    ps, n, ev, sg = run(cmx, 512)
+    base = learn.match(ev, sg, ref)
+    counts = {}
+    for name, use in (("plain residuals", False), ("learned", True)):
+        buf = torch.zeros((3 * n, cmx.stlen), dtype=torch.float64, device=cuda)
+        buf[:n] = ps[:n]
+        net = fbse.Precond(cmx, weights=w) if use else None
+        k, e2, s2 = cmx.refine(buf, n, ev, sg, steps=2, tol=1e-4, precond=net)
+        counts[name] = learn.match(e2, s2, ref)
+    log(f"[learned] judge levels {len(ref)}; converged pairs: short filter {base}, "
+        f"+2 refinement steps with plain residuals {counts['plain residuals']}, with the trained network "
+        f"{counts['learned']}")
+    assert counts["learned"] > base
