@@ -36,6 +36,8 @@ EXPORTED = [
     "fbse_precond_create", "fbse_precond_destroy", "fbse_precond_get_weights", "fbse_precond_set_weights",
     "fbse_precond_apply", "fbse_precond_grad", "fbse_precond_train_step", "fbse_refine",
     "fbse_gram", "fbse_rotate", "fbse_residual",
+    "fbse_batch_create", "fbse_batch_run", "fbse_batch_run_sequential", "fbse_batch_graph_nodes",
+    "fbse_batch_last_error", "fbse_batch_destroy",
 ]
 
 PRECOND_NWEIGHTS = 15120
@@ -63,12 +65,19 @@ class ProjDesc(ctypes.Structure):
                 ("LS", ctypes.POINTER(ctypes.c_double))]
 
 
+class BatchDot(ctypes.Structure):
+    _fields_ = [("ctx", ctypes.c_void_p), ("zn", ctypes.POINTER(ctypes.c_double)),
+                ("an", ctypes.POINTER(ctypes.c_double)), ("ncheby", ctypes.c_long), ("m", ctypes.c_long),
+                ("vmin", ctypes.c_double), ("de", ctypes.c_double), ("psi0", ctypes.c_void_p),
+                ("nstart", ctypes.c_long), ("filtered", ctypes.c_void_p)]
+
+
 class Tuning(ctypes.Structure):
     """fbse_tuning: kernel choices of a context (0 = chosen by the context)."""
     _fields_ = [("fft_kernels", ctypes.c_int), ("fft_plane_cluster", ctypes.c_int),
                 ("fft_chunk_blocks", ctypes.c_long), ("scatter_states", ctypes.c_int),
                 ("gather_points", ctypes.c_int), ("newton_ring", ctypes.c_int), ("bse_simt", ctypes.c_int),
-                ("tc_image_bytes", ctypes.c_double), ("ritz_cut", ctypes.c_double)]
+                ("tc_image_bytes", ctypes.c_double), ("ritz_cut", ctypes.c_double), ("ritz_hpsi", ctypes.c_int)]
 
 
 _lib = None
@@ -136,6 +145,15 @@ def load() -> ctypes.CDLL:
     L.fbse_tuning_report.argtypes = [_VP, ctypes.c_char_p, ctypes.c_long]
     L.fbse_tuning_report.restype = ctypes.c_long
     L.fbse_residual.argtypes = [_VP, _VP, ctypes.c_long, _D, _VP]
+    L.fbse_batch_create.argtypes = [ctypes.POINTER(_VP), ctypes.POINTER(BatchDot), ctypes.c_int]
+    L.fbse_batch_run.argtypes = [_VP]
+    L.fbse_batch_run_sequential.argtypes = [_VP]
+    L.fbse_batch_graph_nodes.argtypes = [_VP]
+    L.fbse_batch_graph_nodes.restype = ctypes.c_long
+    L.fbse_batch_last_error.argtypes = [_VP]
+    L.fbse_batch_last_error.restype = ctypes.c_char_p
+    L.fbse_batch_destroy.argtypes = [_VP]
+    L.fbse_batch_destroy.restype = None
     L.fbse_gram.argtypes = [_VP, _VP, ctypes.c_long, _VP, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D]
     L.fbse_rotate.argtypes = [_VP, _VP, ctypes.c_long, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _VP]
     _F = ctypes.POINTER(ctypes.c_float)
@@ -605,3 +623,56 @@ class Precond:
         self.ctx._chk(self._L.fbse_precond_train_step(self._p, self.ctx._ptr(resid), self.ctx._ptr(corr), _dp(e),
                                                       resid.shape[0], lr, ctypes.byref(loss)))
         return loss.value
+
+
+class Batch:
+    """Multi-dot filter in one CUDA graph (fbse_batch_*).  dots: list of
+    (ctx, zn, an, vmin, de, psi0 device [nstart, stlen]); filtered outputs are
+    allocated here ([nstart, m, stlen] float64 CUDA tensors, ``self.out``)."""
+
+    def __init__(self, dots):
+        import torch
+        self._L = load()
+        self._keep = []
+        arr = (BatchDot * len(dots))()
+        self.out = []
+        for i, (ctx, zn, an, vmin, de, psi0) in enumerate(dots):
+            zn = np.ascontiguousarray(zn, np.float64)
+            an = np.ascontiguousarray(an, np.complex128)
+            m, nc = an.shape
+            anv = an.view(np.float64).reshape(-1)
+            out = torch.empty((psi0.shape[0], m, ctx.stlen), dtype=torch.float64, device=psi0.device)
+            self._keep += [zn, anv, psi0, out]
+            self.out.append(out)
+            arr[i] = BatchDot(ctx._h, _dp(zn), _dp(anv), nc, m, vmin, de, psi0.data_ptr(), psi0.shape[0],
+                              out.data_ptr())
+        torch.cuda.current_stream().synchronize()
+        self._b = ctypes.c_void_p()
+        rc = self._L.fbse_batch_create(ctypes.byref(self._b), arr, len(dots))
+        if rc:
+            msg = self._L.fbse_batch_last_error(self._b).decode() if self._b else ""
+            if self._b:
+                self._L.fbse_batch_destroy(self._b)
+                self._b = ctypes.c_void_p()
+            raise FbseError(rc, msg)
+
+    @property
+    def nodes(self) -> int:
+        return int(self._L.fbse_batch_graph_nodes(self._b))
+
+    def run(self, sequential=False):
+        f = self._L.fbse_batch_run_sequential if sequential else self._L.fbse_batch_run
+        rc = f(self._b)
+        if rc:
+            raise FbseError(rc, self._L.fbse_batch_last_error(self._b).decode())
+
+    def close(self):
+        if self._b:
+            self._L.fbse_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

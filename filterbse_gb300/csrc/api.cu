@@ -1,4 +1,5 @@
 // C-ABI entry points of libfbse_gpu (declared in include/fbse.h).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -225,6 +226,40 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
         }
       p.ncov = (long)cj.size();
       p.nent = (long)nent;
+      // chunks of consecutive covered points for the scatter: at most
+      // kScatterChunkPoints points and kScatterChunkAtoms distinct atoms each;
+      // per chunk its atoms, per entry the atom's slot in its chunk
+      std::vector<int> chb, cha;
+      std::vector<unsigned char> slot(nent ? nent : 1, 0);
+      {
+        long k = 0;
+        while (k < p.ncov) {
+          std::vector<int> atoms;
+          const long k0 = k;
+          while (k < p.ncov && k - k0 < kScatterChunkPoints) {
+            std::vector<int> add;
+            for (int e = cb[k]; e < cb[k + 1]; e++)
+              if (std::find(atoms.begin(), atoms.end(), pa[e]) == atoms.end() &&
+                  std::find(add.begin(), add.end(), pa[e]) == add.end())
+                add.push_back(pa[e]);
+            if ((long)(atoms.size() + add.size()) > kScatterChunkAtoms) break;
+            atoms.insert(atoms.end(), add.begin(), add.end());
+            for (int e = cb[k]; e < cb[k + 1]; e++)
+              slot[e] = (unsigned char)(std::find(atoms.begin(), atoms.end(), pa[e]) - atoms.begin());
+            k++;
+          }
+          if (k == k0) return set_err(c, FBSE_ERR_UNSUPPORTED, "projector table: a point lies in too many spheres");
+          chb.push_back((int)k0);
+          atoms.resize(kScatterChunkAtoms, -1);
+          cha.insert(cha.end(), atoms.begin(), atoms.end());
+        }
+        chb.push_back((int)p.ncov);
+      }
+      p.nchunk = (long)chb.size() - 1;
+      if (cha.empty()) cha.assign(kScatterChunkAtoms, -1);
+      if ((rc = upload(c, &p.chunk_beg, chb.data(), chb.size()))) return rc;
+      if ((rc = upload(c, &p.chunk_atoms, cha.data(), cha.size()))) return rc;
+      if ((rc = upload(c, &p.pe_slot, slot.data(), slot.size()))) return rc;
       if (cj.empty()) cj.push_back(0);
       if ((rc = upload(c, &p.cov_j, cj.data(), cj.size()))) return rc;
       if ((rc = upload(c, &p.cov_beg, cb.data(), cb.size()))) return rc;
@@ -284,7 +319,8 @@ void fbse_destroy(fbse_ctx *c)
   void *bufs[] = {c->dstatus, c->k2x, c->k2y, c->k2z, c->k2xf, c->k2yf, c->k2zf, c->pot64, c->pot32, c->wk, c->coef, c->tmp, c->red,
                   c->proj.nl_cnt, c->proj.jxyz, c->proj.y1, c->proj.sop, c->proj.nlp, c->proj.sgn, c->proj.LS,
                   c->proj.y1f, c->proj.sopf, c->proj.nlpf, c->proj.cov_j, c->proj.cov_beg, c->proj.pe_atom,
-                  c->proj.pe_y1, c->proj.pe_sop, c->proj.pe_nlp, c->proj.pe_y1f, c->proj.pe_sopf, c->proj.pe_nlpf};
+                  c->proj.pe_y1, c->proj.pe_sop, c->proj.pe_nlp, c->proj.pe_y1f, c->proj.pe_sopf, c->proj.pe_nlpf,
+                  c->proj.chunk_beg, c->proj.chunk_atoms, c->proj.pe_slot};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : c->cache)
@@ -348,9 +384,11 @@ int fbse_set_tuning(fbse_ctx *c, const fbse_tuning *t)
   if (!c || !t) return c ? set_err(c, FBSE_ERR_ARG, "fbse_set_tuning: null") : FBSE_ERR_ARG;
   auto pow2_in = [](long v, long hi) { return v == 0 || (v >= 1 && v <= hi && (v & (v - 1)) == 0); };
   if (t->fft_kernels < 0 || t->fft_kernels > 2 || t->fft_plane_cluster < 0 || t->fft_plane_cluster > 1 ||
-      t->fft_chunk_blocks < 0 || !pow2_in(t->scatter_states, 8) || !pow2_in(t->gather_points, 4) ||
+      t->fft_chunk_blocks < 0 || !(pow2_in(t->scatter_states, 8) || t->scatter_states == 18 || t->scatter_states == 20) ||
+      !pow2_in(t->gather_points, 4) ||
       (t->newton_ring != 0 && (t->newton_ring < 8 || t->newton_ring > 128)) || t->bse_simt < 0 || t->bse_simt > 1 ||
-      !(t->tc_image_bytes >= 0) || !(t->ritz_cut >= 0 && t->ritz_cut < 1))
+      !(t->tc_image_bytes >= 0) || !(t->ritz_cut >= 0 && t->ritz_cut < 1) || t->ritz_hpsi < 0 ||
+      t->ritz_hpsi > 2)
     return set_err(c, FBSE_ERR_ARG, "fbse_set_tuning: a field is out of range");
   c->tune = *t;
   c->tuned.clear();  // earlier decisions may rest on the old fixed choices

@@ -82,9 +82,19 @@ struct ProjDev {
   // adds in a fixed order and needs no atomics.
   long ncov = 0, nent = 0;
   int *cov_j = nullptr, *cov_beg = nullptr, *pe_atom = nullptr;
+  // the covered points in chunks (consecutive points, at most
+  // kScatterChunkPoints of them and kScatterChunkAtoms distinct atoms): chunk
+  // c holds points chunk_beg[c] .. chunk_beg[c+1]-1, its atoms
+  // chunk_atoms[c * kScatterChunkAtoms + s] (-1 unused), and pe_slot[e] is the
+  // slot of entry e's atom in its chunk
+  long nchunk = 0;
+  int *chunk_beg = nullptr, *chunk_atoms = nullptr;
+  unsigned char *pe_slot = nullptr;
   double *pe_y1 = nullptr, *pe_sop = nullptr, *pe_nlp = nullptr;
   float *pe_y1f = nullptr, *pe_sopf = nullptr, *pe_nlpf = nullptr;
 };
+
+constexpr int kScatterChunkPoints = 128, kScatterChunkAtoms = 32;
 
 // one decision of the autotuner: candidate values with their times (us)
 struct TuneRecord {
@@ -236,6 +246,10 @@ int kinetic_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk,
 // k-space multiplier including 1/N
 template <typename T>
 int conv_apply(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *work, long nblk, const double2 *kq);
+
+// psitot rows (FP64) <-> working states in precision T (filter.cu)
+template <typename T> int pack(fbse_ctx *c, const double *src, C<T> *dst, long nsrc);
+template <typename T> int unpack(fbse_ctx *c, const C<T> *src, double *dst, long ndst);
 
 // projectors (hpsi.cu) --------------------------------------------------------
 template <typename T>

@@ -85,6 +85,11 @@ int unpack(fbse_ctx *c, const C<T> *src, double *dst, long ndst)
   return FBSE_OK;
 }
 
+template int pack<float>(fbse_ctx *, const double *, C<float> *, long);
+template int pack<double>(fbse_ctx *, const double *, C<double> *, long);
+template int unpack<float>(fbse_ctx *, const C<float> *, double *, long);
+template int unpack<double>(fbse_ctx *, const C<double> *, double *, long);
+
 int pack_states(fbse_ctx *c, const double *src, void *dst, long nsrc)
 {
   return c->precision == FBSE_MIXED ? pack<float>(c, src, (float2 *)dst, nsrc) : pack<double>(c, src, (double2 *)dst, nsrc);
@@ -190,55 +195,83 @@ static long ring_slots(fbse_ctx *c, long ncheby, size_t slot_bytes)
   return ncheby < K ? ncheby : K;
 }
 
-template <typename T>
-static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin,
-                           double de, const double *psi0, long nstart, double *filtered)
+// the real parts of the Newton coefficients (gen_newton_coeff's are real)
+static int real_coeffs(fbse_ctx *c, const double *an, long ncheby, long m, std::vector<double> &are)
 {
-  const long len = (long)c->nspin * c->ngrid;
-  const long nw = c->is_complex ? nstart : (nstart + 1) / 2;
-  const long K = ring_slots(c, ncheby, (size_t)nw * len * sizeof(C<T>));
-  // Newton coefficients: real parts only (gen_newton_coeff's are real)
-  std::vector<double> are((size_t)m * ncheby);
+  are.assign((size_t)m * ncheby, 0.0);
   for (long t = 0; t < m; t++)
     for (long j = 0; j < ncheby; j++) {
       if (an[2 * (t * ncheby + j) + 1] != 0.0)
         return set_err(c, FBSE_ERR_UNSUPPORTED, "complex Newton coefficients are not supported");
       are[t * ncheby + j] = an[2 * (t * ncheby + j)];
     }
-  double *a_dev = nullptr;
-  C<T> *ring = nullptr;
-  const size_t ring_bytes = (size_t)K * nw * len * sizeof(C<T>);
-  int rc = FBSE_OK;
-  if (cudaMalloc(&a_dev, are.size() * sizeof(double)) != cudaSuccess)
-    return set_err(c, FBSE_ERR_OOM, "newton coefficients");
-  {
-    void *r = nullptr;
-    if (cached(c, kSlotRing, ring_bytes, &r)) {
-      cudaFree(a_dev);
-      return set_err(c, FBSE_ERR_OOM, "newton ring buffer");
-    }
-    ring = reinterpret_cast<C<T> *>(r);
-  }
+  return FBSE_OK;
+}
+
+// the kernel sequence of filter_cycle for every start on the context's
+// stream: no allocation and no host synchronisation, so it can be captured
+// into a CUDA graph.  ring: K slots of the working states; a_dev: the real
+// coefficients [m][ncheby] on the device.
+template <typename T>
+static int newton_enqueue_t(fbse_ctx *c, const double *zn, long ncheby, long m, double vmin, double de,
+                            const double *psi0, long nstart, double *filtered, C<T> *ring, long K,
+                            const double *a_dev)
+{
+  const long len = (long)c->nspin * c->ngrid;
+  const long nw = c->is_complex ? nstart : (nstart + 1) / 2;
   const double de_1 = 4.0 / de;
+  int rc;
+  if ((rc = pack<T>(c, psi0, ring, nstart))) return rc;
+  const long slot_stride = nw * len;
+  for (long jc = 0; jc < ncheby; jc++) {
+    if (jc > 0) {
+      const C<T> *src = ring + ((jc - 1) % K) * slot_stride;
+      C<T> *dst = ring + (jc % K) * slot_stride;
+      // p_hnorm: dE_1 * H psi - (2 + zn + Vmin * dE_1) psi   (filter.c:401-407)
+      if ((rc = hpsi_apply<T>(c, src, dst, nw, de_1, -(2.0 + zn[jc - 1] + vmin * de_1)))) return rc;
+    }
+    if ((jc % K) == K - 1 || jc == ncheby - 1) {
+      const long j0 = jc - (jc % K);
+      const int nk = (int)(jc - j0 + 1);
+      if ((rc = launch_newton_acc<T>(c, ring, j0, nk, a_dev, ncheby, (int)m, filtered, nstart, nw, len))) return rc;
+    }
+  }
+  return FBSE_OK;
+}
+
+// ring slots and the ring buffer (kept in the context) for nstart starts
+template <typename T>
+static int newton_ring_t(fbse_ctx *c, long ncheby, long nstart, long *K_out, void **ring)
+{
+  const long len = (long)c->nspin * c->ngrid;
+  const long nw = c->is_complex ? nstart : (nstart + 1) / 2;
+  const long K = ring_slots(c, ncheby, (size_t)nw * len * sizeof(C<T>));
+  if (cached(c, kSlotRing, (size_t)K * nw * len * sizeof(C<T>), ring)) return set_err(c, FBSE_ERR_OOM, "newton ring");
+  *K_out = K;
+  return FBSE_OK;
+}
+
+template <typename T>
+static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin,
+                           double de, const double *psi0, long nstart, double *filtered)
+{
+  std::vector<double> are;
+  int rc = real_coeffs(c, an, ncheby, m, are);
+  if (rc) return rc;
+  long K = 0;
+  void *ring = nullptr;
+  if ((rc = newton_ring_t<T>(c, ncheby, nstart, &K, &ring))) return rc;
+  double *a_dev = nullptr;
+  if (cudaMalloc(&a_dev, are.size() * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, FBSE_ERR_OOM, "newton coefficients");
+  }
   do {
     if (cudaMemcpyAsync(a_dev, are.data(), are.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream) !=
         cudaSuccess) { rc = set_err(c, FBSE_ERR_CUDA, "coefficient upload"); break; }
-    if ((rc = pack<T>(c, psi0, ring, nstart))) break;
-    const long slot_stride = nw * len;
-    for (long jc = 0; jc < ncheby; jc++) {
-      if (jc > 0) {
-        const C<T> *src = ring + ((jc - 1) % K) * slot_stride;
-        C<T> *dst = ring + (jc % K) * slot_stride;
-        // p_hnorm: dE_1 * H psi - (2 + zn + Vmin * dE_1) psi   (filter.c:401-407)
-        if ((rc = hpsi_apply<T>(c, src, dst, nw, de_1, -(2.0 + zn[jc - 1] + vmin * de_1)))) break;
-      }
-      if ((jc % K) == K - 1 || jc == ncheby - 1) {
-        const long j0 = jc - (jc % K);
-        const int nk = (int)(jc - j0 + 1);
-        if ((rc = launch_newton_acc<T>(c, ring, j0, nk, a_dev, ncheby, (int)m, filtered, nstart, nw, len))) break;
-      }
-    }
-    if (rc) break;
+    if ((rc = newton_enqueue_t<T>(c, zn, ncheby, m, vmin, de, psi0, nstart, filtered, static_cast<C<T> *>(ring), K,
+                                  a_dev)))
+      break;
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = set_err(c, FBSE_ERR_CUDA, "newton filter");
     if (!rc) rc = check_dev_status(c);
   } while (0);
@@ -247,15 +280,52 @@ static int newton_filter_t(fbse_ctx *c, const double *zn, const double *an, long
   return rc;
 }
 
-int newton_filter(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
-                  const double *psi0, long nstart, double *filtered)
+static int newton_args(fbse_ctx *c, long ncheby, long m, long nstart, double de)
 {
   if (m < 1 || m > kMaxTargets) return set_err(c, FBSE_ERR_UNSUPPORTED, "mStatesPerFilter must be 1..32");
   if (ncheby < 1 || nstart < 1) return set_err(c, FBSE_ERR_ARG, "ncheby and nstart must be positive");
   if (!(de > 0)) return set_err(c, FBSE_ERR_ARG, "dE must be positive");
+  return FBSE_OK;
+}
+
+int newton_filter(fbse_ctx *c, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
+                  const double *psi0, long nstart, double *filtered)
+{
+  int rc = newton_args(c, ncheby, m, nstart, de);
+  if (rc) return rc;
   if (c->precision == FBSE_MIXED)
     return newton_filter_t<float>(c, zn, an, ncheby, m, vmin, de, psi0, nstart, filtered);
   return newton_filter_t<double>(c, zn, an, ncheby, m, vmin, de, psi0, nstart, filtered);
+}
+
+// for the multi-dot batch: validate and upload the coefficients into a_dev
+// (m * ncheby doubles, owned by the caller) and size the ring; then
+// newton_filter_enqueue only enqueues kernels (capturable)
+int newton_filter_prepare(fbse_ctx *c, const double *an, long ncheby, long m, long nstart, double de,
+                          double *a_dev, long *K)
+{
+  int rc = newton_args(c, ncheby, m, nstart, de);
+  if (rc) return rc;
+  std::vector<double> are;
+  if ((rc = real_coeffs(c, an, ncheby, m, are))) return rc;
+  if (h2d(c->stream, a_dev, are.data(), are.size() * sizeof(double)) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return set_err(c, FBSE_ERR_CUDA, "coefficient upload");
+  void *ring = nullptr;
+  return c->precision == FBSE_MIXED ? newton_ring_t<float>(c, ncheby, nstart, K, &ring)
+                                    : newton_ring_t<double>(c, ncheby, nstart, K, &ring);
+}
+
+int newton_filter_enqueue(fbse_ctx *c, const double *zn, long ncheby, long m, double vmin, double de,
+                          const double *psi0, long nstart, double *filtered, const double *a_dev, long K)
+{
+  void *ring = c->cache[kSlotRing];
+  if (!ring) return set_err(c, FBSE_ERR_STATE, "newton ring not prepared");
+  if (c->precision == FBSE_MIXED)
+    return newton_enqueue_t<float>(c, zn, ncheby, m, vmin, de, psi0, nstart, filtered, static_cast<float2 *>(ring), K,
+                                   a_dev);
+  return newton_enqueue_t<double>(c, zn, ncheby, m, vmin, de, psi0, nstart, filtered, static_cast<double2 *>(ring), K,
+                                  a_dev);
 }
 
 // ---------------------------------------------------------------------------

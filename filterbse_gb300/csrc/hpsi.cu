@@ -298,6 +298,122 @@ __global__ void __launch_bounds__(256) k_proj_scatter(C<T> *__restrict__ out, co
   }
 }
 
+// scatter over chunks of covered points (ProjDev::chunk_beg ...): one CTA
+// per chunk (at most kScatterChunkPoints points, kScatterChunkAtoms atoms),
+// one thread per point, all states in groups of kG.  The coefficients of the
+// chunk's atoms for a group's states are staged in shared memory once and
+// shared by every point, and the table entries of the chunk stay in L1 across
+// the groups, so the table is read from L2 once per H psi.  The arithmetic of
+// each (state, point) is that of k_proj_scatter, in the same order.
+template <typename T, bool SO, bool NL, int kG>
+__global__ void __launch_bounds__(kScatterChunkPoints) k_proj_scatter_chunk(
+    C<T> *__restrict__ out, const C<T> *__restrict__ coef, PtView<T> pv, const int *__restrict__ chunk_beg,
+    const int *__restrict__ chunk_atoms, const unsigned char *__restrict__ slot, long nat, long nstates, long ngrid,
+    int nspin, T scale)
+{
+  constexpr int NCH = (SO ? 1 : 0) + (NL ? 1 : 0);
+  constexpr int ROW = NCH * kNC;  // coefficients per (state, atom)
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C<T> *dsm = reinterpret_cast<C<T> *>(smem_raw);  // [kG][kScatterChunkAtoms][ROW]
+  const int c = blockIdx.x;
+  const int p0 = chunk_beg[c], np = chunk_beg[c + 1] - p0;
+  const int t = threadIdx.x;
+  const bool live = t < np;
+  const long k = p0 + (live ? t : 0);
+  const long j = pv.cov_j[k];
+  const int e0 = pv.cov_beg[k], e1 = live ? pv.cov_beg[k + 1] : e0;
+  const int npj = pv.nproj;
+  const int ch0 = SO ? 0 : 1;
+  for (long s0 = 0; s0 < nstates; s0 += kG) {
+    const int ng = (int)(nstates - s0 < kG ? nstates - s0 : kG);
+    __syncthreads();
+    for (int i = t; i < kG * kScatterChunkAtoms * ROW; i += blockDim.x) {
+      const int g = i / (kScatterChunkAtoms * ROW), sa = (i / ROW) % kScatterChunkAtoms, q = i % ROW;
+      const int a = chunk_atoms[c * kScatterChunkAtoms + sa];
+      C<T> v = mk<T>(T(0), T(0));
+      if (g < ng && a >= 0) v = coef[(((s0 + g) * nat + a) * 2 + ch0) * kNC + q];
+      dsm[i] = v;
+    }
+    __syncthreads();
+    if (!live) continue;
+    C<T> o[kG][2];
+#pragma unroll
+    for (int g = 0; g < kG; g++)
+#pragma unroll
+      for (int s = 0; s < 2; s++)
+        if (g < ng && s < nspin) o[g][s] = out[((s0 + g) * nspin + s) * ngrid + j];
+    T ar[kG][2], ai[kG][2];
+#pragma unroll
+    for (int g = 0; g < kG; g++) {
+      ar[g][0] = ar[g][1] = T(0);
+      ai[g][0] = ai[g][1] = T(0);
+    }
+    for (int e = e0; e < e1; e++) {
+      const int sl = slot[e];
+      T yr[3], yi[3];
+#pragma unroll
+      for (int m = 0; m < 3; m++) {
+        const C<T> y = pv.y1[m * pv.nent + e];
+        yr[m] = y.x;
+        yi[m] = y.y;
+      }
+      T bs[5], bn[5];
+#pragma unroll
+      for (int p = 0; p < 5; p++) {
+        bs[p] = (SO && p < npj) ? pv.sop[p * pv.nent + e] : T(0);
+        bn[p] = (NL && p < npj) ? pv.nlp[p * pv.nent + e] : T(0);
+      }
+#pragma unroll
+      for (int g = 0; g < kG; g++) {
+        if (g >= ng) continue;
+        const C<T> *d = dsm + (g * kScatterChunkAtoms + sl) * ROW;
+        T qr[6], qi[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) qr[q] = qi[q] = T(0);
+#pragma unroll
+        for (int p = 0; p < 5; p++) {
+          if (p >= npj) continue;
+#pragma unroll
+          for (int q = 0; q < 6; q++) {
+            if (SO) {
+              const C<T> r = d[p * 6 + q];
+              qr[q] += bs[p] * r.x;
+              qi[q] += bs[p] * r.y;
+            }
+            if (NL) {
+              const C<T> r = d[(SO ? kNC : 0) + p * 6 + q];
+              qr[q] += bn[p] * r.x;
+              qi[q] += bn[p] * r.y;
+            }
+          }
+        }
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+          if (s >= nspin) continue;
+          T vr = 0, vi = 0;
+#pragma unroll
+          for (int m = 0; m < 3; m++) {
+            vr += yr[m] * qr[3 * s + m] - yi[m] * qi[3 * s + m];
+            vi += yr[m] * qi[3 * s + m] + yi[m] * qr[3 * s + m];
+          }
+          ar[g][s] += vr;
+          ai[g][s] += vi;
+        }
+      }
+    }
+#pragma unroll
+    for (int g = 0; g < kG; g++)
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        if (g >= ng || s >= nspin) continue;
+        C<T> v = o[g][s];
+        v.x += scale * ar[g][s];
+        v.y += scale * ai[g][s];
+        out[((s0 + g) * nspin + s) * ngrid + j] = v;
+      }
+  }
+}
+
 template <typename T, int kGU>
 static void launch_gather(fbse_ctx *c, dim3 g, const C<T> *in, C<T> *coef, const ProjView<T> &pv, long nstates, int ch0)
 {
@@ -306,6 +422,27 @@ static void launch_gather(fbse_ctx *c, dim3 g, const C<T> *in, C<T> *coef, const
   constexpr int kMinB = sizeof(T) == 4 ? 8 : 1;
   k_proj_gather<T, kGU, kMinB, kSW><<<g, kProjThreads, 0, c->stream>>>(in, coef, pv, c->proj.nat, nstates, c->ngrid,
                                                                       c->nspin, ch0, c->dv);
+}
+
+template <typename T, bool SO, bool NL, int kG>
+static int launch_scatter_chunk1(fbse_ctx *c, C<T> *out, const C<T> *coef, const PtView<T> &pt, long nstates, T sc)
+{
+  const ProjDev &p = c->proj;
+  constexpr int NCH = (SO ? 1 : 0) + (NL ? 1 : 0);
+  const size_t smem = (size_t)kG * kScatterChunkAtoms * NCH * kNC * sizeof(C<T>);
+  FBSE_CUDA(c, cudaFuncSetAttribute(k_proj_scatter_chunk<T, SO, NL, kG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+  k_proj_scatter_chunk<T, SO, NL, kG><<<(unsigned)p.nchunk, kScatterChunkPoints, smem, c->stream>>>(
+      out, coef, pt, p.chunk_beg, p.chunk_atoms, p.pe_slot, p.nat, nstates, c->ngrid, c->nspin, sc);
+  return FBSE_OK;
+}
+
+template <typename T, int kG>
+static int launch_scatter_chunk(fbse_ctx *c, C<T> *out, const C<T> *coef, const PtView<T> &pt, long nstates, T sc)
+{
+  if (c->so && c->nl) return launch_scatter_chunk1<T, true, true, kG>(c, out, coef, pt, nstates, sc);
+  if (c->so) return launch_scatter_chunk1<T, true, false, kG>(c, out, coef, pt, nstates, sc);
+  return launch_scatter_chunk1<T, false, true, kG>(c, out, coef, pt, nstates, sc);
 }
 
 template <typename T, int kG>
@@ -359,20 +496,25 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   if (p.ncov == 0) return FBSE_OK;
   const PtView<T> pt = ptview<T>(c);
   const T sc = (T)scale;
-  // scatter: states per thread (each (state, point) is summed in the same
-  // order for every choice); candidates are timed on the scratch states
+  // scatter: v = 1, 2, 4, 8: one thread per point and v states; v = 16 + g:
+  // one CTA per chunk of points, all states in groups of g with the chunk's
+  // coefficients in shared memory.  Each (state, point) is summed in the same
+  // order for every choice; candidates are timed on the scratch states
   long kg = c->tune.scatter_states;
   auto scatter = [&](C<T> *dst, long v) -> int {
+    int r = FBSE_OK;
     if (v == 1) launch_scatter<T, 1>(c, dst, coef, pt, nstates, sc);
     else if (v == 2) launch_scatter<T, 2>(c, dst, coef, pt, nstates, sc);
     else if (v == 8) launch_scatter<T, 8>(c, dst, coef, pt, nstates, sc);
+    else if (v == 18) r = launch_scatter_chunk<T, 2>(c, dst, coef, pt, nstates, sc);
+    else if (v == 20) r = launch_scatter_chunk<T, 4>(c, dst, coef, pt, nstates, sc);
     else launch_scatter<T, 4>(c, dst, coef, pt, nstates, sc);
-    return launch_status(c);
+    return r ? r : launch_status(c);
   };
   if (kg == 0) {
     if (scratch) {
-      if ((rc = autotune(c, "projector scatter states per thread", prob, {1, 2, 4, 8},
-                         [&](long v) { return scatter(scratch, v); }, &kg)))
+      if ((rc = autotune(c, "projector scatter states per thread (16 + g: chunked, g per group)", prob,
+                         {1, 2, 4, 8, 18, 20}, [&](long v) { return scatter(scratch, v); }, &kg)))
         return rc;
     } else {
       kg = 4;

@@ -671,8 +671,12 @@ static int gram_t(fbse_ctx *c, const double *A, const double *B, int n, long L, 
   return FBSE_OK;
 }
 
-// default overlap cut of the mixed path, relative to the largest eigenvalue
-constexpr double kMixedRitzCut = 1e-6;
+// default overlap cut of the mixed path, relative to the largest eigenvalue:
+// with the compensated Gram sums and the Rayleigh quotients from the FP64
+// small matrices, a lower cut keeps more of the filtered span; measured on
+// the 3 nm CdSe spinor dot (256 filtered states), 1e-10 keeps 250 pairs and
+// matches 148 to the FP64 pipeline's levels, against 228 and 142 at 1e-6
+constexpr double kMixedRitzCut = 1e-10;
 
 template <typename T>
 static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept, double *eval, double *sigma)
@@ -707,7 +711,11 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
       hpsi = (double *)a;
       rot = (double *)b;
     }
-    if (!alloc(&work, (size_t)2 * nw_chunk * len * sizeof(C<T>))) break;
+    // the mixed path applies H in FP32 here unless told otherwise (FP64 H psi
+    // measured no better on the 3 nm dot: the FP32 recursion's noise in the
+    // filtered states, not the operator, limits the projected problem)
+    const bool h64 = kMixed && c->tune.ritz_hpsi == 2;
+    if (!alloc(&work, (size_t)2 * nw_chunk * len * (h64 ? sizeof(double2) : sizeof(C<T>)))) break;
     const size_t nn = (size_t)n * n;
     if (!alloc((void **)&G, nn * sizeof(double2)) || !alloc((void **)&M, nn * sizeof(double2)) ||
         !alloc((void **)&V, nn * sizeof(double2)) || !alloc((void **)&X, nn * sizeof(double2)) ||
@@ -720,13 +728,20 @@ static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept
         !alloc((void **)&G0, nn * sizeof(double2)) || !alloc((void **)&quad, 2 * (size_t)n * sizeof(double)))
       break;
     // 1. HPsi in chunks of working states
-    C<T> *w0 = reinterpret_cast<C<T> *>(work), *w1 = w0 + nw_chunk * len;
     for (long s0 = 0; s0 < n && !rc; s0 += chunk_states) {
       const long ns = std::min<long>(chunk_states, n - s0);
       const long nw = c->is_complex ? ns : (ns + 1) / 2;
-      if ((rc = pack_states(c, psitot + s0 * stlen, w0, ns))) break;
-      if ((rc = hpsi_apply<T>(c, w0, w1, nw, 1.0, 0.0))) break;
-      if ((rc = unpack_states(c, w1, hpsi + s0 * stlen, ns))) break;
+      if (h64) {
+        double2 *w0 = reinterpret_cast<double2 *>(work), *w1 = w0 + nw_chunk * len;
+        if ((rc = pack<double>(c, psitot + s0 * stlen, w0, ns))) break;
+        if ((rc = hpsi_apply<double>(c, w0, w1, nw, 1.0, 0.0))) break;
+        if ((rc = unpack<double>(c, w1, hpsi + s0 * stlen, ns))) break;
+      } else {
+        C<T> *w0 = reinterpret_cast<C<T> *>(work), *w1 = w0 + nw_chunk * len;
+        if ((rc = pack<T>(c, psitot + s0 * stlen, w0, ns))) break;
+        if ((rc = hpsi_apply<T>(c, w0, w1, nw, 1.0, 0.0))) break;
+        if ((rc = unpack<T>(c, w1, hpsi + s0 * stlen, ns))) break;
+      }
     }
     if (rc) break;
     // 2. Gram and projected H (dv-weighted)

@@ -8,9 +8,9 @@ training pairs: a short filter run gives Ritz pairs (psi, E) with residuals
 r = (H - E) psi; a longer run on the same starts -- the plain method with more
 Newton terms, which is also the judge of the refined energies -- gives
 converged eigenvectors.  The target correction of psi is the step to its
-component in the converged eigenspace it belongs to:
+projection on the longer run's Ritz vectors near its energy:
     c = Q Q^H psi / |Q^H psi| - psi,
-Q the converged eigenvectors of the cluster that holds most of psi's weight.
+Q those Ritz vectors (energies within a window of E, small residuals).
 Every product runs in the library on the GPU (fbse_gram, fbse_rotate,
 fbse_hpsi); this module only moves pointers and picks clusters.
 """
@@ -20,7 +20,7 @@ import numpy as np
 
 from . import Context, Precond
 
-SIGMA_CONVERGED = 1e-6  # judge pairs that define the eigenspaces
+SIGMA_CONVERGED = 1e-5  # judge pairs that define the eigenspaces
 
 
 def clusters(e, tol=1e-6):
@@ -51,38 +51,29 @@ def residuals(ctx: Context, psitot, ev):
     return ctx.residual(psitot.contiguous(), np.asarray(ev, np.float64)[:psitot.shape[0]])
 
 
-def training_pairs(short, judge, tol_lo=1e-5, tol_hi=0.1, min_weight=0.5):
+def training_pairs(short, judge, tol_lo=1e-5, tol_hi=0.1, window=0.02, judge_sigma=1e-3, min_weight=0.5):
     """(resid, corr, ene) of the short run's Ritz pairs with tol_lo < sigma <=
-    tol_hi whose weight in one converged cluster of the judge run exceeds
-    min_weight.  short, judge: (ctx, psitot, n, ev, sg) with the judge's ctx
-    FP64."""
+    tol_hi.  The target of pair (psi, E) is the step to its projection on the
+    judge's Ritz vectors with energies within `window` of E and sigma <=
+    judge_sigma, normalised: c = Q Q^H psi / |Q^H psi| - psi; pairs with less
+    than min_weight of their norm in that span are left out.  short, judge:
+    (ctx, psitot, n, ev, sg); the judge's ctx is FP64."""
     import torch
     ctx, ps, n, ev, sg = short
     jctx, pj, nj, evj, sgj = judge
-    good = np.where(sgj[:nj] <= SIGMA_CONVERGED)[0]
-    if len(good) == 0:
-        return None
-    cl = [good[c] for c in clusters(evj[good])]
+    good = np.where(sgj[:nj] <= judge_sigma)[0]
     sel = [i for i in range(n) if tol_lo < sg[i] <= tol_hi]
-    if not sel:
+    if len(good) == 0 or not sel:
         return None
-    psel = ps[sel].contiguous()
-    # overlaps with every converged judge state, one FP64 product on the GPU
     Q = pj[good].contiguous()
-    ov = jctx.gram(Q, psel)  # [ngood, nsel]
-    pos = {g: k for k, g in enumerate(good)}
+    ov = jctx.gram(Q, ps[sel].contiguous())  # [ngood, nsel], one FP64 product on the GPU
     keep, coef = [], []
     for col, i in enumerate(sel):
-        best, bw = None, 0.0
-        for c in cl:
-            w = float(np.sum(np.abs(ov[[pos[g] for g in c], col]) ** 2))
-            if w > bw:
-                best, bw = c, w
-        if best is None or bw < min_weight:
+        near = np.abs(evj[good] - ev[i]) <= window
+        w = float(np.sum(np.abs(ov[near, col]) ** 2))
+        if w < min_weight:
             continue
-        cf = np.zeros(len(good), np.complex128)
-        idx = [pos[g] for g in best]
-        cf[idx] = ov[idx, col] / np.sqrt(bw)
+        cf = np.where(near, ov[:, col], 0.0) / np.sqrt(w)
         keep.append(i)
         coef.append(cf)
     if not keep:

@@ -100,8 +100,18 @@ class Dot:
         return sum(1 for t in self.types if not t.startswith("P"))
 
 
-def zincblende_dot(radius_ang: float, a_ang: float = 6.08):
-    """Passivated zincblende CdSe sphere; returns (types, coords in bohr), core first."""
+MATERIALS = {
+    # cation, anion, lattice constant (A), directory of the local-potential tables
+    "CdSe": ("Cd", "Se", 6.08, os.path.join(_ROOT, "tests", "golden", "cdse22")),
+    "InP": ("In", "P", 5.87, os.path.join(_ROOT, "tests", "golden", "inp")),
+}
+
+
+def zincblende_dot(radius_ang: float, a_ang: float = 6.08, cation: str = "Cd", anion: str = "Se"):
+    """Passivated zincblende sphere (CdSe by default); returns (types, coords
+    in bohr), core first.  Ligands: P1 on the cation's dangling bonds, P2 on
+    the anion's (the passivation model of the reference's CdSe and InP
+    examples)."""
     a = a_ang * ANG
     R = radius_ang * ANG
     n = int(np.ceil(R / a)) + 2
@@ -142,7 +152,7 @@ def zincblende_dot(radius_ang: float, a_ang: float = 6.08):
                 lig_pos.append(pos[i] + sgn * bonds[b] * frac)
                 lig_typ.append("P1" if kind[i] == 0 else "P2")
     order = np.argsort(kind, kind="stable")
-    types = ["Cd" if k == 0 else "Se" for k in kind[order]] + lig_typ
+    types = [cation if k == 0 else anion for k in kind[order]] + lig_typ
     coords = np.vstack([pos[order], np.array(lig_pos).reshape(-1, 3)])
     coords = coords - coords.mean(axis=0)  # centerConf (read.c)
     return types, coords
@@ -170,10 +180,11 @@ def read_table(path):
 
 
 def local_pot(grid: Grid, types, coords, pot_dir=POT_DIR) -> np.ndarray:
-    """Local potential on the GPU (fbse_build_local_pot)."""
+    """Local potential on the GPU (fbse_build_local_pot).  Ligand tables
+    (potP1 / potP2) come from the II-VI directory for every material."""
     from . import load
     uniq = sorted(set(types), key=types.index)
-    tabs = [read_table(os.path.join(pot_dir, f"pot{t}.par")) for t in uniq]
+    tabs = [read_table(os.path.join(POT_DIR if t in ("P1", "P2") else pot_dir, f"pot{t}.par")) for t in uniq]
     tr = np.concatenate([t[0] for t in tabs])
     tv = np.concatenate([t[1] for t in tabs])
     tlen = np.array([len(t[0]) for t in tabs], np.int64)
@@ -285,13 +296,41 @@ def nlc_table(grid: Grid, coords, so_par, so_tab, nproj=NPROJ) -> ProjTable:
 
 
 def cdse_dot(radius_ang: float, d: float = 0.5, ke_max: float = 20.0, spinor: bool = True, so_par: float = 0.01,
-             grid_n=(0, 0, 0)) -> Dot:
-    types, coords = zincblende_dot(radius_ang)
+             grid_n=(0, 0, 0), material: str = "CdSe") -> Dot:
+    cat, an, a_ang, pdir = MATERIALS[material]
+    types, coords = zincblende_dot(radius_ang, a_ang, cat, an)
     grid = reference_grid(coords, d, ke_max, grid_n)
-    pot = local_pot(grid, types, coords)
+    pot = local_pot(grid, types, coords, pdir)
     proj = None
     if spinor:
         core = [i for i, t in enumerate(types) if not t.startswith("P")]
         tab = so_radial(d, np.sqrt(r_nlcut2(d)))
         proj = nlc_table(grid, coords[core], np.full(len(core), so_par), tab)
     return Dot(types, coords, grid, pot, proj, 2 if spinor else 1, spinor, spinor, False)
+
+
+def uneven_dots(n: int = 24, seed: int = 20261206, d_min_nm: float = 2.0, d_max_nm: float = 4.0, d: float = 0.5,
+                ke_max: float = 10.0, max_grid: int = 160):
+    """The multi-dot workload: n passivated zincblende dots, CdSe and InP
+    alternating, diameters uniform in [d_min_nm, d_max_nm] from a seeded
+    generator, each on its own grid by the reference's grid rule (capped at
+    max_grid points per axis, a recorded choice: the rule gives 104^3-190^3 for
+    2-4 nm, the stated workload 64^3-160^3).  Returns [(material, diameter_nm,
+    Dot)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        mat = "CdSe" if i % 2 == 0 else "InP"
+        dia = float(rng.uniform(d_min_nm, d_max_nm))
+        cat, an, a_ang, pdir = MATERIALS[mat]
+        types, coords = zincblende_dot(5.0 * dia, a_ang, cat, an)
+        g = reference_grid(coords, d, ke_max)
+        if max(g.nx, g.ny, g.nz) > max_grid:
+            n_ = max_grid
+            g = Grid(n_, n_, n_, d, d, d, -n_ * d / 2, -n_ * d / 2, -n_ * d / 2, ke_max)
+        pot = local_pot(g, types, coords, pdir)
+        core = [k for k, t in enumerate(types) if not t.startswith("P")]
+        tab = so_radial(d, np.sqrt(r_nlcut2(d)))
+        proj = nlc_table(g, coords[core], np.full(len(core), 0.01), tab)
+        out.append((mat, dia, Dot(types, coords, g, pot, proj, 2, True, True, False)))
+    return out

@@ -121,7 +121,8 @@ typedef struct fbse_tuning {
                               x lines and y/z columns (no plane kernel).  Results differ in rounding only */
   int fft_plane_cluster;   /* 0: one CTA per 128 x 128 FP32 plane; 1: two-CTA clusters (same results) */
   long fft_chunk_blocks;   /* 3D blocks (state x spin) per FFT launch sequence; 0: autotuned */
-  int scatter_states;      /* states per projector-scatter thread, 1/2/4/8; 0: autotuned */
+  int scatter_states;      /* projector scatter: 1/2/4/8 states per thread (a thread per point), or
+                              18/20: a CTA per chunk of points with 2/4 states per group; 0: autotuned */
   int gather_points;       /* points per lane per projector-gather iteration, 1/2/4; 0: autotuned */
   int newton_ring;         /* Newton ring slots, 8..128 (the FP32 block sums depend on it); 0: 128 */
   int bse_simt;            /* 1: the mixed path's BSE contraction on the FP32 SIMT kernel instead of
@@ -130,6 +131,8 @@ typedef struct fbse_tuning {
   double ritz_cut;         /* overlap eigenvalues kept by fbse_ortho_diag_sigma, relative to the largest
                               (the role of SVDEPS, filter_mpi/fd.h); 0: 1e-12 (FP64), the mixed path's own
                               default otherwise */
+  int ritz_hpsi;           /* H psi of the mixed path's Rayleigh-Ritz step: 0 default (FP32), 1 FP32,
+                              2 FP64 (the FP64 operator's tables are held by every context) */
 } fbse_tuning;
 int fbse_get_tuning(fbse_ctx *ctx, fbse_tuning *t);
 int fbse_set_tuning(fbse_ctx *ctx, const fbse_tuning *t);
@@ -245,6 +248,37 @@ int fbse_rotate(fbse_ctx *ctx, const double *A, long na, const double *coef, lon
 int fbse_filter_job(fbse_ctx *ctx, const double *zn, const double *an, long ncheby, long m, double vmin, double de,
                     const double *psi0_host, long nstart, double sigma_cut, long *n_out, double *eval_host,
                     double *sigma_host, double *psi_host);
+
+/* ---- multi-dot filter in one CUDA graph (no counterpart in the reference) ----
+ * Independent dots of uneven size (each its own context: grid, potential,
+ * projector table) filtered by one graph launch instead of their kernels
+ * one by one.  fbse_batch_create validates every dot, uploads its Newton
+ * coefficients, runs each dot's filter once through fbse_newton_filter
+ * (buffers sized, launch shapes autotuned; filtered receives the result) and
+ * captures the filters of all dots into one graph, each dot an independent
+ * branch on its context's stream.  fbse_batch_run replays it (results
+ * bit-identical to the sequential path); fbse_batch_run_sequential runs
+ * fbse_newton_filter dot after dot, for comparison.  The dots' device
+ * buffers (psi0, filtered) must stay valid while the batch exists.  The
+ * reference's parallel dimension is the random starts of one dot, one MPI
+ * rank each (filter_mpi/filter.c:100-104, mod_filter.c:155-159). */
+typedef struct fbse_batch_dot {
+  fbse_ctx *ctx;          /* one context per dot */
+  const double *zn;       /* host [ncheby] */
+  const double *an;       /* host [m][ncheby] complex */
+  long ncheby, m;
+  double vmin, de;
+  const double *psi0;     /* device psitot [nstart] */
+  long nstart;
+  double *filtered;       /* device psitot [nstart * m] */
+} fbse_batch_dot;
+typedef struct fbse_batch fbse_batch;
+int fbse_batch_create(fbse_batch **out, const fbse_batch_dot *dots, int ndots);
+int fbse_batch_run(fbse_batch *b);
+int fbse_batch_run_sequential(fbse_batch *b);
+long fbse_batch_graph_nodes(const fbse_batch *b);
+const char *fbse_batch_last_error(const fbse_batch *b);
+void fbse_batch_destroy(fbse_batch *b);
 
 /* ---- learned residual preconditioner and refinement ------------------------
  * No counterpart in the reference: its only remedy for unconverged states is

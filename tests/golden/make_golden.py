@@ -22,6 +22,9 @@ Fixtures (all data outputs or inputs of the reference's own example runs):
                          OS.dat, OS0.dat, M0.dat, M.dat, rs0.dat, rs.dat and
                          the calcSpinAngStat files lsqr.dat, ls.dat,
                          spins.dat, orbital.dat, couple.dat, qp_spins.dat
+  inp/                   the In and P local-potential tables shipped with the
+                         In13P16 example (filter.zip, filter/In13_P16/potIn.par,
+                         potP.par), for the InP dots of the multi-dot workload
 """
 import os
 import shutil
@@ -69,6 +72,11 @@ def main():
     for fn in ("input.par", "conf.par", "potCs.par", "potI.par", "potPb.par", "SO_Cs.par", "SO_I.par", "SO_Pb.par"):
         shutil.copy(os.path.join(src, fn), d)
     shutil.copy(os.path.join(src, "reference_output", "eval.dat"), d)
+    di = os.path.join(OUT, "inp")
+    os.makedirs(di, exist_ok=True)
+    for a in ("In", "P"):
+        with open(os.path.join(di, f"pot{a}.par"), "wb") as f:
+            f.write(z.read(f"filter/In13_P16/pot{a}.par"))
     bse = os.path.join(REF, "bse_cplx", "EXAMPLES", "1x1x1_CsPbI3", "bse")
     shutil.copy(os.path.join(bse, "input.par"), os.path.join(d, "bse_input.par"))
     for fn in ("exciton.dat", "OS.dat", "OS0.dat", "M0.dat", "M.dat", "rs0.dat", "rs.dat", "lsqr.dat", "ls.dat",

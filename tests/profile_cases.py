@@ -1,0 +1,117 @@
+"""Small GPU programs whose kernels the per-kernel ncu summaries under
+profiles/ profile (pytest does not collect this file).  Each case builds its
+workload, runs it once to warm up (autotuner decisions, buffers) and then once
+more, so that a capture with `-s <launches of the warm-up>` sees the second
+run.  It needs a GPU and the built library.
+
+  python tests/profile_cases.py rr        Rayleigh-Ritz of 256 filtered spinor states
+                                          of the 3 nm CdSe dot (k_gram, k_jacobi_sweep,
+                                          k_rotate, k_quad_diag)
+  python tests/profile_cases.py filter    Newton filter, 16 spinor starts x 16 targets,
+                                          nCheby 256, 128^3 (k_newton_acc and H psi)
+  python tests/profile_cases.py bse       BSE kernel contraction, 40 holes x 40
+                                          electrons of spinor states on 128^3, mixed
+                                          path (k_pair_density, convolution FFTs,
+                                          k_tc_images, k_tc_gemm_nt)
+  python tests/profile_cases.py precond   learned preconditioner forward + backward on
+                                          8 spinor residuals of an 80^3 dot (k_conv,
+                                          k_conv_wgrad)
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+
+def _dot(radius=15.0):
+    from filterbse_gb300 import workload as W
+    return W.cdse_dot(radius, d=0.5, ke_max=10.0, spinor=True)
+
+
+def _ctx(F, dot, prec):
+    g = dot.grid
+    return F.Context(g, dot.pot, nspin=2, is_complex=True, so=True, nl=False, proj=dot.proj, precision=prec)
+
+
+def _filter_setup(F, dot, ctx, nc, nstart=16):
+    import torch
+    import bench as B
+    g = dot.grid
+    e0, e1, _ = ctx.energy_range(max_iter=400)
+    vmin, emax = e0 - 0.2 * abs(e0), e1 * 1.2
+    de = emax - vmin
+    zn, _ = F.samp_points(nc)
+    an = F.newton_coeff(zn, B.ene_targets(**B.TARGETS), vmin, de, (nc / (2.5 * de)) ** 2)
+    starts, _, _ = F.init_filter_states(nstart, g.ngrid, 2, True, g.dv, -(B.SEED))
+    return zn, an, vmin, de, torch.tensor(starts, device="cuda:0")
+
+
+def case_filter(F):
+    dot = _dot()
+    ctx = _ctx(F, dot, F.MIXED)
+    zn, an, vmin, de, d0 = _filter_setup(F, dot, ctx, 256)
+    for _ in range(2):
+        t = time.time()
+        ctx.newton_filter(zn, an, vmin, de, d0)
+        print(f"filter: {time.time() - t:.3f}s")
+
+
+def case_rr(F):
+    import torch
+    dot = _dot()
+    ctx = _ctx(F, dot, F.MIXED)
+    zn, an, vmin, de, d0 = _filter_setup(F, dot, ctx, 256)
+    filt = ctx.newton_filter(zn, an, vmin, de, d0).reshape(256, -1)
+    for _ in range(2):
+        t = torch.clone(filt)
+        t0 = time.time()
+        nk, ev, sg = ctx.ortho_diag_sigma(t)
+        print(f"rayleigh-ritz: {nk} pairs, {time.time() - t0:.3f}s")
+
+
+def case_bse(F):
+    import torch
+    dot = _dot()
+    ctx = _ctx(F, dot, F.MIXED)
+    g = dot.grid
+    nh = ne = 40
+    gen = torch.Generator(device="cuda:0").manual_seed(1)
+    pd = torch.randn((nh + ne, 2 * g.ngrid), dtype=torch.complex128, device="cuda:0", generator=gen)
+    pd /= torch.sqrt((pd.abs() ** 2).sum(dim=1, keepdim=True) * g.dv)
+    gx, gy, gz = g.axes()
+    bare, scr = ctx.bse_potentials(gx, gy, gz, g.xmin, g.ymin, g.zmin)
+    for _ in range(2):
+        t = time.time()
+        ctx.bse_kernel(pd, nh, ne, nh, bare, scr)
+        torch.cuda.synchronize()
+        print(f"bse kernel 40h x 40e: {time.time() - t:.3f}s")
+
+
+def case_precond(F):
+    import torch
+    dot = _dot(8.0)
+    ctx = _ctx(F, dot, F.MIXED)
+    rng = np.random.default_rng(2)
+    n = 8
+    r = torch.tensor(rng.normal(size=(n, ctx.stlen)), device="cuda:0")
+    c = torch.tensor(rng.normal(size=(n, ctx.stlen)) * 0.1, device="cuda:0")
+    e = rng.uniform(-0.3, -0.1, n)
+    pc = F.Precond(ctx, seed=3)
+    for _ in range(2):
+        t = time.time()
+        pc.apply(r, e)
+        pc.grad(r, c, e)
+        print(f"precond forward + gradient, {n} states: {time.time() - t:.3f}s")
+
+
+def main():
+    import filterbse_gb300 as F
+    F.load()
+    {"rr": case_rr, "filter": case_filter, "bse": case_bse, "precond": case_precond}[sys.argv[1]](F)
+
+
+if __name__ == "__main__":
+    main()

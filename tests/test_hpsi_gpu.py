@@ -141,14 +141,16 @@ def test_autotuner_choices_are_bit_identical(fbse, cuda, precision):
     ctx = _ctx(fbse, sysm, precision)
     auto = _run_hpsi(fbse, ctx, psis, cuda)
     rep = ctx.tuning_report()
-    kernels = {r["kernel"] for r in rep}
+    kernels = {r["kernel"].split(" (")[0] for r in rep}
     assert {"fft blocks per launch", "projector gather points per lane",
             "projector scatter states per thread"} <= kernels
     for r in rep:
         assert str(r["choice"]) in r["candidates"] and all(t > 0 for t in r["candidates"].values())
     for fixed in ({"fft_chunk_blocks": 2, "scatter_states": 1, "gather_points": 1},
                   {"fft_chunk_blocks": 18, "scatter_states": 8, "gather_points": 4},
-                  {"fft_chunk_blocks": 5, "scatter_states": 2, "gather_points": 2}):
+                  {"fft_chunk_blocks": 5, "scatter_states": 2, "gather_points": 2},
+                  {"fft_chunk_blocks": 3, "scatter_states": 18, "gather_points": 2},
+                  {"fft_chunk_blocks": 1, "scatter_states": 20, "gather_points": 1}):
         ctx.set_tuning(**fixed)
         assert np.array_equal(_run_hpsi(fbse, ctx, psis, cuda), auto), fixed
     with pytest.raises(fbse.FbseError):

@@ -153,12 +153,14 @@ def test_learned_refinement_gains_over_the_plain_filter(fbse, cuda):
         return c64, cmx, run
 
     # training pairs: short mixed filter vs the judge (FP64, 4x the terms)
-    c64, cmx, run = system(8.0, 1001)
+    c64, cmx, run = system(8.0, 1001, nstart=16, m=16)
     ps, n, ev, sg = run(cmx, 512)
     pj, nj, evj, sgj = run(c64, 2048)
     pairs = learn.training_pairs((cmx, ps, n, ev, sg), (c64, pj, nj, evj, sgj))
+    log(f"\n[learned] judge pairs with sigma <= {learn.SIGMA_CONVERGED}: {np.sum(sgj <= learn.SIGMA_CONVERGED)}, "
+        f"short-run pairs {n}")
     assert pairs is not None and pairs[0].shape[0] >= 16
-    log(f"\n[learned] {pairs[0].shape[0]} training pairs from the 1.6 nm dot")
+    log(f"[learned] {pairs[0].shape[0]} training pairs from the 1.6 nm dot")
     pc = fbse.Precond(cmx, seed=5)
     hist = learn.train(pc, pairs, steps=300, lr=2e-3, batch=8, log=log)
     assert np.mean(hist[-20:]) < 0.5 * np.mean(hist[:5])
