@@ -166,7 +166,7 @@ inline int launch_status(fbse_ctx *c)
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FBSE_OK : set_err(c, FBSE_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
 }
-enum CacheSlot { kSlotRing = 0, kSlotHpsi, kSlotRot, kSlotJobStarts, kSlotJobStates, kSlotJacobi };
+enum CacheSlot { kSlotRing = 0, kSlotHpsi, kSlotRot, kSlotJobStarts, kSlotJobStates, kSlotJacobi, kSlotTc };
 inline int cached(fbse_ctx *c, int slot, size_t need, void **out)
 {
   const int rc = ensure(c, &c->cache[slot], &c->cache_bytes[slot], need);

@@ -329,14 +329,13 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
   const long nsplit = sps * nchunk;
   const size_t img_a = (size_t)mp * nkb_c * kBK, img_b = (size_t)np * nkb_c * kBK;  // floats
   const size_t part_n = (size_t)nsplit * mp * np;
-  float *buf = nullptr;
-  int *status = nullptr;
-  const size_t need = (2 * img_a + 4 * img_b + 2 * part_n) * sizeof(float);
-  if (cudaMalloc(&buf, need) != cudaSuccess || cudaMalloc(&status, sizeof(int)) != cudaSuccess) {
-    cudaGetLastError();
-    if (buf) cudaFree(buf);
-    return set_err(c, FBSE_ERR_OOM, "tensor-core GEMM scratch");
-  }
+  // operand images, partial tiles and the wait status, kept in the context
+  // between calls (grown on demand, released by fbse_destroy)
+  const size_t need = (2 * img_a + 4 * img_b + 2 * part_n) * sizeof(float) + 256;
+  void *scratch = nullptr;
+  if (cached(c, kSlotTc, need, &scratch)) return set_err(c, FBSE_ERR_OOM, "tensor-core GEMM scratch");
+  float *buf = static_cast<float *>(scratch);
+  int *status = reinterpret_cast<int *>(static_cast<char *>(scratch) + need - 256);
   float *ah = buf, *al = ah + img_a;
   float *b0h = al + img_a, *b0l = b0h + img_b, *b1h = b0l + img_b, *b1l = b1h + img_b;
   float *p0 = b1l + img_b, *p1 = p0 + part_n;
@@ -396,8 +395,6 @@ int tc_complex_nt(fbse_ctx *c, const S *A, int ma, const S *B, int nb, long L, b
     }
   } while (0);
   cudaStreamSynchronize(c->stream);
-  cudaFree(buf);
-  cudaFree(status);
   return rc;
 }
 
