@@ -231,8 +231,8 @@ def run_gpu(args):
     d2h = int(k * stlen * 8 + 2 * k * 8)
 
     # ---- learned refinement, judged by the plain FP64 filter at 3x the terms
-    learned = learned_leg(args, F, W, dot, g, c64_grid=(g, dot), cmx=cmx, zn_an=(vmin, de), d_starts=d_starts,
-                          stlen=stlen, log=log) if args.learned and world == 1 else None
+    learned = learned_leg(args, F, W, dot, g, cmx=cmx, zn_an=(vmin, de), d_starts=d_starts, stlen=stlen,
+                          fp64=(ev64, sg64), log=log) if args.learned and world == 1 else None
 
     # ---- H psi roofline: one batched H psi of the 16 spinor starts (FP32)
     import torch as T
@@ -315,7 +315,7 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def learned_leg(args, F, W, dot, g, c64_grid, cmx, zn_an, d_starts, stlen, log):
+def learned_leg(args, F, W, dot, g, cmx, zn_an, d_starts, stlen, fp64, log):
     """The learned residual refinement on the headline workload.  Training
     pairs come from the filter on a 1.6 nm dot (mixed filter at nCheby/4
     against the plain FP64 filter at nCheby); the network trains on the GPU
@@ -367,7 +367,7 @@ def learned_leg(args, F, W, dot, g, c64_grid, cmx, zn_an, d_starts, stlen, log):
     _, nj, evj, sgj = run(c64, 3 * args.ncheby)
     ref = evj[sgj <= 1e-6]
     t_judge = time.time() - t1
-    _, n64, ev64, sg64 = run(c64, args.ncheby)
+    ev64, sg64 = fp64  # the plain FP64 pipeline of the main leg, same starts
     c64.close()
     torch.cuda.empty_cache()
     log(f"[learned] judge: {len(ref)} levels with sigma <= 1e-6 ({t_judge:.0f}s)")

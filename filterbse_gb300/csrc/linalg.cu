@@ -671,12 +671,14 @@ static int gram_t(fbse_ctx *c, const double *A, const double *B, int n, long L, 
   return FBSE_OK;
 }
 
-// default overlap cut of the mixed path, relative to the largest eigenvalue:
-// with the compensated Gram sums and the Rayleigh quotients from the FP64
-// small matrices, a lower cut keeps more of the filtered span; measured on
-// the 3 nm CdSe spinor dot (256 filtered states), 1e-10 keeps 250 pairs and
-// matches 148 to the FP64 pipeline's levels, against 228 and 142 at 1e-6
-constexpr double kMixedRitzCut = 1e-10;
+// default overlap cut of the mixed path, relative to the largest eigenvalue.
+// Measured on the 3 nm CdSe spinor dot (256 filtered states): a cut of 1e-10
+// keeps 250 pairs and matches 148 levels of the FP64 pipeline against 228 and
+// 142 at 1e-6, but the extra directions are noise of the FP32 recursion and
+// they leave the converged vectors less accurate (on the CsPbI3 cube the
+// smallest singular value of the mixed / FP64 cluster overlaps drops from
+// 1 - 4e-8 to 1 - 9e-6), so the default keeps 1e-6
+constexpr double kMixedRitzCut = 1e-6;
 
 template <typename T>
 static int ortho_diag_sigma_t(fbse_ctx *c, double *psitot, long n_, long *n_kept, double *eval, double *sigma)

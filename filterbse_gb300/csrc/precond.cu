@@ -642,7 +642,9 @@ int fbse_precond_create(fbse_ctx *c, fbse_precond **out, const float *weights, l
 void fbse_precond_destroy(fbse_precond *p)
 {
   if (!p) return;
-  if (p->c && p->c->stream) cudaStreamSynchronize(p->c->stream);
+  // waits for the whole device rather than the context's stream: the context
+  // may already be destroyed (destruction order is the caller's)
+  cudaDeviceSynchronize();
   cudaFree(p->w);
   if (p->buf) cudaFree(p->buf);
   delete p;

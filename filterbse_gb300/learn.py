@@ -83,6 +83,12 @@ def training_pairs(short, judge, tol_lo=1e-5, tol_hi=0.1, window=0.02, judge_sig
     psi = ps[keep].contiguous()
     corr = (tgt - psi).contiguous()
     res = residuals(jctx, psi, ev[keep])
+    # only the direction of a correction matters to the Rayleigh-Ritz step that
+    # uses it, and |c| / |r| spans orders of magnitude (about 1 / |E_k - E|):
+    # every target is scaled to its residual's norm, so the network learns
+    # directions and the loss weighs every pair alike
+    scale = (res.norm(dim=1) / corr.norm(dim=1).clamp_min(1e-300))[:, None]
+    corr = (corr * scale).contiguous()
     return res, corr, np.asarray(ev)[keep]
 
 

@@ -298,6 +298,8 @@ typedef struct fbse_precond fbse_precond;
 #define FBSE_PRECOND_NWEIGHTS 15120
 /* weights NULL: seeded random initialisation (scaled uniform) */
 int fbse_precond_create(fbse_ctx *ctx, fbse_precond **out, const float *weights_host, long seed);
+/* May come before or after fbse_destroy of its context (it touches only its
+ * own memory); every other fbse_precond_* call needs the context alive. */
 void fbse_precond_destroy(fbse_precond *p);
 int fbse_precond_get_weights(fbse_precond *p, float *weights_host);
 int fbse_precond_set_weights(fbse_precond *p, const float *weights_host);
