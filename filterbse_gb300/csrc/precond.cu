@@ -25,6 +25,7 @@
 #include <cmath>
 #include <vector>
 
+#include "fbse_async.cuh"
 #include "fbse_internal.cuh"
 
 namespace fbse {
@@ -32,6 +33,7 @@ namespace fbse {
 int pack_states(fbse_ctx *c, const double *src, void *dst, long nsrc);
 int unpack_states(fbse_ctx *c, const void *src, double *dst, long ndst);
 int ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, double *eval, double *sigma);
+int normalize_all(fbse_ctx *c, double *psitot, long n, double *norms);
 
 namespace pc {
 
@@ -54,14 +56,25 @@ struct Geo {
   int nx, ny, nz;
   long n;  // nx * ny * nz
   int tx, ty, tz;  // tiles per axis
+  int ntx, px;     // tensor-core path: 128-point x tiles, padded row length (see h8_index)
   __host__ __device__ long tiles() const { return (long)tx * ty * tz; }
 };
+
+// The inference path keeps the hidden activations channel-minor for the tensor
+// cores: [field][channel half][z][y][x + 1][8 channels] in BF16, each row
+// padded to ntx * 128 + 2 points with zeros at x = -1 and beyond nx, so that
+// the 130 points a 128-point output tile needs are one contiguous,
+// 16-byte-aligned run per channel half.
+__host__ __device__ __forceinline__ long h8_index(const Geo &g, long f, int c, int z, int y, int x)
+{
+  return ((((f * 2 + c / 8) * g.nz + z) * g.ny + y) * (long)g.px + (x + 1)) * 8 + c % 8;
+}
 
 __device__ __forceinline__ float ld_f(const float *p) { return *p; }
 __device__ __forceinline__ float ld_f(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
 
 // the halo of tile (tile) for channels [c0, c0 + cc) of field f into xs[cc][HALO]
-template <typename TI>
+template <typename TI, bool H8 = false>
 __device__ void load_halo(const TI *__restrict__ in, int cin, long f, int c0, int cc, const Geo &g, int bx, int by,
                           int bz, float *xs)
 {
@@ -72,14 +85,17 @@ __device__ void load_halo(const TI *__restrict__ in, int cin, long f, int c0, in
     const int x = x0 + hx, y = y0 + hy, z = z0 + hz;
     float v = 0.f;
     if (x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz)
-      v = ld_f(in + ((f * cin + c0 + ch) * g.n + ((long)z * g.ny + y) * g.nx + x));
+      v = H8 ? ld_f(in + h8_index(g, f, c0 + ch, z, y, x))
+             : ld_f(in + ((f * cin + c0 + ch) * g.n + ((long)z * g.ny + y) * g.nx + x));
     xs[i] = v;
   }
 }
 
 // out[f][co][p] = epi(sum_ci sum_k w[ci][k][co] in[f][ci][p + off_k])
-// MODE 0: BF16 tanh(acc); 1: FP32 acc; 2: FP32 acc * (1 - a^2), a = act[f][co][p]
-template <int CIN, int COUT, int MODE, typename TI>
+// MODE 0: BF16 tanh(acc); 1: FP32 acc; 2: FP32 acc * (1 - a^2), a = act[f][co][p];
+// 3: BF16 tanh(acc) in the channel-minor layout (h8_index).  H8: the input is
+// in the channel-minor layout.
+template <int CIN, int COUT, int MODE, typename TI, bool H8 = false>
 __global__ void __launch_bounds__(kThreads) k_conv(const TI *__restrict__ in, const float *__restrict__ w, void *out,
                                                    const __nv_bfloat16 *__restrict__ act, Geo g)
 {
@@ -99,7 +115,7 @@ __global__ void __launch_bounds__(kThreads) k_conv(const TI *__restrict__ in, co
     for (int o = 0; o < COUT; o++) acc[q][o] = 0.f;
   for (int c0 = 0; c0 < CIN; c0 += CC) {
     __syncthreads();
-    load_halo<TI>(in, CIN, f, c0, CC, g, bx, by, bz, xs);
+    load_halo<TI, H8>(in, CIN, f, c0, CC, g, bx, by, bz, xs);
     __syncthreads();
 #pragma unroll 1
     for (int cc = 0; cc < CC; cc++) {
@@ -136,6 +152,8 @@ __global__ void __launch_bounds__(kThreads) k_conv(const TI *__restrict__ in, co
       const long e = (f * COUT + o) * g.n + p;
       if (MODE == 0) {
         reinterpret_cast<__nv_bfloat16 *>(out)[e] = __float2bfloat16(tanhf(acc[q][o]));
+      } else if (MODE == 3) {
+        reinterpret_cast<__nv_bfloat16 *>(out)[h8_index(g, f, o, z, y, x)] = __float2bfloat16(tanhf(acc[q][o]));
       } else if (MODE == 1) {
         reinterpret_cast<float *>(out)[e] = acc[q][o];
       } else {
@@ -199,6 +217,229 @@ __global__ void __launch_bounds__(kThreads) k_conv_wgrad(const TI *__restrict__ 
     if (o < NO) part[(long)blockIdx.x * NO + o] = (double)acc[i];
   }
 }
+
+
+// ---------------------------------------------------------------------------
+// 16 -> 16 channel convolution on the tensor cores (tcgen05, kind::f16), the
+// two hidden layers of the inference path.  One CTA walks the rows y of one
+// (field, z, 128-point x tile).  An output row is a 128 x 16 tile
+//   D[x][c_out] = sum over the 27 offsets of  A_k[x][c_in] W_k[c_out][c_in],
+// A_k the input row (z + dz, y + dy) shifted by dx, read straight from a ring
+// of input rows in shared memory (no im2col): in the channel-minor layout
+// eight consecutive points of one channel half are one 128-byte core matrix,
+// so the shifted operand is the same descriptor with its start moved by 16
+// bytes per point.  The FP32 weights enter as two BF16 parts (hi + lo), 54
+// MMAs of M = 128, N = 16, K = 16 per row into 16 FP32 columns of tensor
+// memory; the four warps read the accumulator back (one lane per point),
+// apply tanh and store BF16.  Input rows arrive by bulk copies two rows ahead
+// of their first use; every wait is bounded, and on a timeout the kernel sets
+// the context's error flag, waits (bounded) for what it issued, frees its
+// tensor memory and returns.
+// ---------------------------------------------------------------------------
+namespace tcc {
+using namespace fbse::async;
+constexpr int kRowPts = 128 + 2;
+constexpr int kHalfBytes = kRowPts * 16;    // one channel half of an input row: 2080 B
+constexpr int kRowBytes = 2 * kHalfBytes;   // both halves
+constexpr int kSlots = 4;                   // ring of y rows
+constexpr int kSlotBytes = 3 * kRowBytes;   // rows z - 1, z, z + 1
+constexpr int kWTile = 512;                 // one weight tile: 16 x 16 BF16
+constexpr int kWBytes = 2 * 27 * kWTile;    // hi / lo tiles of one layer
+// slack after the ring: an operand's 16 core matrices span 15 x 128 + 2080 B
+// from its start, and they would span 15 x 2080 + 128 B with the two
+// descriptor strides exchanged; the slack keeps both inside this CTA's memory
+constexpr int kGuard = 15 * kHalfBytes + 256;
+constexpr size_t kSmem = kWBytes + kSlots * kSlotBytes + kGuard;
+
+// shared-memory matrix descriptor, K-major, no swizzle: core matrices of 8
+// rows x 16 bytes, lbo between core matrices along K, sbo along M (or N)
+__device__ __forceinline__ uint64_t desc_none(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+  uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // fixed 0b001; swizzle bits 61-63 stay 0
+  return d;
+}
+
+// instruction descriptor: D = F32, A = B = BF16, both K-major, N = 16, M = 128
+__host__ __device__ constexpr uint32_t idesc_bf16()
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t acc)
+{
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(idesc_bf16()), "r"(acc));
+}
+
+__device__ __forceinline__ void commit(uint64_t *bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__global__ void __launch_bounds__(128, 1) k_conv16_tc(const __nv_bfloat16 *__restrict__ in,
+                                                      const __nv_bfloat16 *__restrict__ wtc,
+                                                      __nv_bfloat16 *__restrict__ out, Geo g, int *status)
+{
+  extern __shared__ __align__(128) unsigned char sm_raw[];
+  unsigned char *wsm = sm_raw;            // [hi / lo][27][c_in half][c_out][8 c_in]
+  unsigned char *ring = sm_raw + kWBytes;  // [slot][dz][c half][130 points][8 channels]
+  __shared__ __align__(8) uint64_t full_bar[kSlots], done_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int fail;
+  const int warp = threadIdx.x >> 5;
+  const long blk = blockIdx.x;
+  const int xt = (int)(blk % g.ntx), z = (int)((blk / g.ntx) % g.nz);
+  const long f = blk / ((long)g.ntx * g.nz);
+  const int x0 = xt * 128;
+  for (int i = threadIdx.x; i < kWBytes / 16; i += blockDim.x)
+    reinterpret_cast<uint4 *>(wsm)[i] = reinterpret_cast<const uint4 *>(wtc)[i];
+  if (threadIdx.x == 0) {
+    for (int sl = 0; sl < kSlots; sl++) mbar_init(&full_bar[sl], 1);
+    mbar_init(&done_bar, 1);
+    fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_u32(&tmem_base)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base;
+  int nvalid = 0;
+  for (int dz = 0; dz < 3; dz++) nvalid += (z + dz - 1 >= 0 && z + dz - 1 < g.nz);
+  // producer: input row yy of the rows z - 1, z, z + 1 into slot yy % kSlots
+  auto load_row = [&](int yy) {
+    uint64_t *bar = &full_bar[yy % kSlots];
+    unsigned char *slot = ring + (yy % kSlots) * kSlotBytes;
+    mbar_expect_tx(bar, (uint32_t)(nvalid * kRowBytes));
+    for (int dz = 0; dz < 3; dz++) {
+      const int zz = z + dz - 1;
+      if (zz < 0 || zz >= g.nz) continue;
+      for (int h = 0; h < 2; h++)
+        bulk_copy(slot + dz * kRowBytes + h * kHalfBytes, in + h8_index(g, f, 8 * h, zz, yy, x0 - 1), kHalfBytes,
+                  bar);
+    }
+  };
+  int loaded = -1, waited = -1;  // rows issued by the producer / awaited by the MMA thread
+  if (threadIdx.x == 0) {
+    load_row(0);
+    loaded = 0;
+    if (g.ny > 1) {
+      load_row(1);
+      loaded = 1;
+    }
+  }
+  int committed = -1;
+  for (int y = 0; y < g.ny; y++) {
+    // the slot of row y + 2 held row y - 2, last read by row y - 1 (done)
+    if (threadIdx.x == 0 && y + 2 < g.ny) {
+      load_row(y + 2);
+      loaded = y + 2;
+    }
+    if (threadIdx.x == 32) {
+      bool ok = true;
+      for (int yy = waited + 1; yy <= y + 1 && yy < g.ny && ok; yy++) {
+        ok = mbar_wait(&full_bar[yy % kSlots], (uint32_t)((yy / kSlots) & 1));
+        if (ok) waited = yy;
+      }
+      if (!ok) {
+        atomicExch(&fail, 1);
+      } else {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        uint32_t acc = 0;
+        for (int dy = 0; dy < 3; dy++) {
+          const int yy = y + dy - 1;
+          if (yy < 0 || yy >= g.ny) continue;
+          for (int dz = 0; dz < 3; dz++) {
+            const int zz = z + dz - 1;
+            if (zz < 0 || zz >= g.nz) continue;
+            const uint32_t base = smem_u32(ring + (yy % kSlots) * kSlotBytes + dz * kRowBytes);
+            for (int dx = 0; dx < 3; dx++) {
+              const uint64_t a = desc_none(base + dx * 16, kHalfBytes, 128);
+              const int k = (dz * 3 + dy) * 3 + dx;
+              for (int hl = 0; hl < 2; hl++) {
+                mma_bf16(tmem, a, desc_none(smem_u32(wsm + (hl * 27 + k) * kWTile), 256, 128), acc);
+                acc = 1;
+              }
+            }
+          }
+        }
+        commit(&done_bar);
+        committed = y;
+      }
+    }
+    __syncthreads();
+    if (fail) break;
+    // epilogue: lane = point, 16 FP32 columns = output channels
+    bool ok = mbar_wait(&done_bar, (uint32_t)(y & 1));
+    ok = __all_sync(0xffffffffu, ok);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (ok) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      const int x = x0 + threadIdx.x;
+      if (x < g.nx) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+          for (int j = 0; j < 8; j++) v[j] = __float2bfloat16(tanhf(__uint_as_float(r[8 * h + j])));
+          *reinterpret_cast<uint4 *>(out + h8_index(g, f, 8 * h, z, y, x)) = *reinterpret_cast<uint4 *>(v);
+        }
+      }
+    } else {
+      atomicExch(&fail, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (fail) break;
+  }
+  if (fail) {
+    if (threadIdx.x == 0) {
+      atomicExch(status, 1);
+      // copies still in flight land before the CTA leaves (bounded)
+      for (int yy = (waited > loaded - 3 ? waited + 1 : loaded - 2); yy <= loaded; yy++)
+        if (yy >= 0) mbar_wait(&full_bar[yy % kSlots], (uint32_t)((yy / kSlots) & 1));
+    }
+    // MMAs still in flight finish before their tensor memory is released (bounded)
+    if (threadIdx.x == 32 && committed >= 0) mbar_wait(&done_bar, (uint32_t)(committed & 1));
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem));
+}
+
+// weight tiles of one 16 -> 16 layer: w[co][ci][27] FP32 -> hi and lo BF16
+// parts, tile (part, k) laid out [ci half][co][8 ci]
+__global__ void k_prep_wtc(const float *__restrict__ w, __nv_bfloat16 *__restrict__ out)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * 16 * 27; i += gridDim.x * blockDim.x) {
+    const int co = i / (16 * 27), ci = (i / 27) % 16, k = i % 27;
+    const float v = w[i];
+    const __nv_bfloat16 hi = __float2bfloat16(v);
+    const __nv_bfloat16 lo = __float2bfloat16(v - __bfloat162float(hi));
+    const int o = k * 256 + (ci / 8) * 128 + co * 8 + ci % 8;
+    out[o] = hi;
+    out[27 * 256 + o] = lo;
+  }
+}
+
+}  // namespace tcc
 
 // out[o] = sum_b part[b][o] in order b = 0, 1, ...
 __global__ void k_sum_parts(const double *__restrict__ part, int nb, int no, double *__restrict__ out)
@@ -331,6 +572,7 @@ struct fbse_precond {
   float *w = nullptr, *m = nullptr, *v = nullptr;  // weights and Adam moments (device)
   float *wf = nullptr, *wb = nullptr;              // per-layer forward / backward layouts (device)
   double *g = nullptr;                             // gradient (device, FP64 sums)
+  __nv_bfloat16 *wtc = nullptr;                    // tensor-core weight tiles of the two hidden layers
   long step = 0;
   // activations and scratch, grown on demand
   void *buf = nullptr;
@@ -342,16 +584,27 @@ namespace pc {
 
 static unsigned blocks_for(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 32)); }
 
-template <int CIN, int COUT, int MODE, typename TI>
+template <int CIN, int COUT, int MODE, typename TI, bool H8 = false>
 static int conv(fbse_precond *P, const TI *in, const float *w, void *out, const __nv_bfloat16 *act, const Geo &g,
                 long nf)
 {
   fbse_ctx *c = P->c;
   constexpr int CC = CIN < 4 ? CIN : 4;
   const size_t smem = (size_t)(CIN * 27 * COUT + CC * HALO) * sizeof(float);
-  FBSE_CUDA(c, cudaFuncSetAttribute(k_conv<CIN, COUT, MODE, TI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  FBSE_CUDA(c, cudaFuncSetAttribute(k_conv<CIN, COUT, MODE, TI, H8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
-  k_conv<CIN, COUT, MODE, TI><<<(unsigned)(nf * g.tiles()), kThreads, smem, c->stream>>>(in, w, out, act, g);
+  k_conv<CIN, COUT, MODE, TI, H8><<<(unsigned)(nf * g.tiles()), kThreads, smem, c->stream>>>(in, w, out, act, g);
+  FBSE_CHECK_LAUNCH(c);
+  return FBSE_OK;
+}
+
+// one hidden layer on the tensor cores (channel-minor input and output)
+static int conv_tc(fbse_precond *P, const __nv_bfloat16 *in, const __nv_bfloat16 *wtc, __nv_bfloat16 *out,
+                   const Geo &g, long nf)
+{
+  fbse_ctx *c = P->c;
+  FBSE_CUDA(c, cudaFuncSetAttribute(tcc::k_conv16_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcc::kSmem));
+  tcc::k_conv16_tc<<<(unsigned)(nf * g.nz * g.ntx), 128, tcc::kSmem, c->stream>>>(in, wtc, out, g, c->dstatus);
   FBSE_CHECK_LAUNCH(c);
   return FBSE_OK;
 }
@@ -370,11 +623,28 @@ static int wgrad(fbse_precond *P, const TI *x, const float *dy, const Geo &g, lo
   return FBSE_OK;
 }
 
+static Geo geo(fbse_ctx *c)
+{
+  Geo g;
+  g.nx = (int)c->nx;
+  g.ny = (int)c->ny;
+  g.nz = (int)c->nz;
+  g.n = c->ngrid;
+  g.tx = (g.nx + TX - 1) / TX;
+  g.ty = (g.ny + TY - 1) / TY;
+  g.tz = (g.nz + TZ - 1) / TZ;
+  g.ntx = (g.nx + 127) / 128;
+  g.px = g.ntx * 128 + 2;
+  return g;
+}
+
 // scratch layout for nf fields of the context's grid
 struct Bufs {
   double *rms, *ene, *lpart, *wpart;
   __nv_bfloat16 *x0, *a1, *a2, *a3;
   float *y, *t, *d4, *d3, *d2, *d1;
+  __nv_bfloat16 *h1, *h2, *h3;  // inference: channel-minor hidden activations
+  size_t h_bytes;
 };
 
 static int bufs(fbse_precond *P, long nf, long nstates, bool train, Bufs *b)
@@ -394,6 +664,13 @@ static int bufs(fbse_precond *P, long nf, long nstates, bool train, Bufs *b)
   add((size_t)nf * kC * N * 2);                    // a2
   add((size_t)nf * kC * N * 2);                    // a3
   add((size_t)nf * N * 4);                         // y
+  const Geo gg = geo(c);
+  const size_t hb = (size_t)nf * 2 * gg.nz * gg.ny * gg.px * 8 * 2;
+  if (!train) {
+    add(hb);                                       // h1
+    add(hb);                                       // h2
+    add(hb);                                       // h3
+  }
   if (train) {
     add((size_t)nf * N * 4);                       // t
     add((size_t)nf * N * 4);                       // d4
@@ -418,20 +695,11 @@ static int bufs(fbse_precond *P, long nf, long nstates, bool train, Bufs *b)
   b->d3 = train ? (float *)(B + off[11]) : nullptr;
   b->d2 = train ? (float *)(B + off[12]) : nullptr;
   b->d1 = train ? (float *)(B + off[13]) : nullptr;
+  b->h1 = train ? nullptr : (__nv_bfloat16 *)(B + off[9]);
+  b->h2 = train ? nullptr : (__nv_bfloat16 *)(B + off[10]);
+  b->h3 = train ? nullptr : (__nv_bfloat16 *)(B + off[11]);
+  b->h_bytes = train ? 0 : hb;
   return FBSE_OK;
-}
-
-static Geo geo(fbse_ctx *c)
-{
-  Geo g;
-  g.nx = (int)c->nx;
-  g.ny = (int)c->ny;
-  g.nz = (int)c->nz;
-  g.n = c->ngrid;
-  g.tx = (g.nx + TX - 1) / TX;
-  g.ty = (g.ny + TY - 1) / TY;
-  g.tz = (g.nz + TZ - 1) / TZ;
-  return g;
 }
 
 static int prep_weights(fbse_precond *P)
@@ -462,6 +730,19 @@ static int forward(fbse_precond *P, const double *resid, const double *corr, con
                                                         b->rms, b->x0, train ? b->t : nullptr);
   FBSE_CHECK_LAUNCH(c);
   const Geo g = geo(c);
+  if (!train) {
+    // inference: the hidden layers on the tensor cores in the channel-minor
+    // layout (zero padding columns: the kernels write interior points only)
+    FBSE_CUDA(c, cudaMemsetAsync(b->h1, 0, 3 * ((b->h_bytes + 255) / 256 * 256), c->stream));
+    for (int l = 1; l <= 2; l++) {
+      tcc::k_prep_wtc<<<27, 256, 0, c->stream>>>(P->w + kWOff[l], P->wtc + (l - 1) * (tcc::kWBytes / 2));
+      FBSE_CHECK_LAUNCH(c);
+    }
+    if ((rc = conv<2, kC, 3>(P, b->x0, P->wf + kWOff[0], b->h1, nullptr, g, nf))) return rc;
+    if ((rc = conv_tc(P, b->h1, P->wtc, b->h2, g, nf))) return rc;
+    if ((rc = conv_tc(P, b->h2, P->wtc + tcc::kWBytes / 2, b->h3, g, nf))) return rc;
+    return conv<kC, 1, 1, __nv_bfloat16, true>(P, b->h3, P->wf + kWOff[3], b->y, nullptr, g, nf);
+  }
   if ((rc = conv<2, kC, 0>(P, b->x0, P->wf + kWOff[0], b->a1, nullptr, g, nf))) return rc;
   if ((rc = conv<kC, kC, 0>(P, b->a1, P->wf + kWOff[1], b->a2, nullptr, g, nf))) return rc;
   if ((rc = conv<kC, kC, 0>(P, b->a2, P->wf + kWOff[2], b->a3, nullptr, g, nf))) return rc;
@@ -582,6 +863,10 @@ static int refine_round(fbse_ctx *c, fbse_precond *P, double *psitot, long n, lo
   } else {
     FBSE_CUDA(c, cudaMemcpyAsync(dst, res, nd * stlen * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   }
+  // unit norms: a residual's norm is sigma (1e-3 and below), so its overlap
+  // eigenvalue would fall under the Rayleigh-Ritz step's relative cut and the
+  // new direction would be dropped
+  if ((rc = normalize_all(c, dst, nd, nullptr))) return rc;
   // Rayleigh-Ritz on the n pairs and the nd new directions
   long nk = 0;
   if ((rc = ortho_diag_sigma(c, psitot, n + nd, &nk, eval, sigma))) return rc;
@@ -603,7 +888,7 @@ int fbse_precond_create(fbse_ctx *c, fbse_precond **out, const float *weights, l
   P->c = c;
   const size_t nw = FBSE_PRECOND_NWEIGHTS;
   void *m = nullptr;
-  if (cudaMalloc(&m, nw * sizeof(float) * 5 + nw * sizeof(double)) != cudaSuccess) {
+  if (cudaMalloc(&m, nw * sizeof(float) * 5 + nw * sizeof(double) + 2 * pc::tcc::kWBytes) != cudaSuccess) {
     cudaGetLastError();
     delete P;
     return set_err(c, FBSE_ERR_OOM, "fbse_precond_create");
@@ -614,6 +899,7 @@ int fbse_precond_create(fbse_ctx *c, fbse_precond **out, const float *weights, l
   P->wf = P->v + nw;
   P->wb = P->wf + nw;
   P->g = reinterpret_cast<double *>(P->wb + nw);
+  P->wtc = reinterpret_cast<__nv_bfloat16 *>(P->g + nw);
   std::vector<float> w(nw);
   if (weights) {
     std::copy(weights, weights + nw, w.begin());
@@ -688,7 +974,7 @@ int fbse_precond_apply(fbse_precond *p, const double *resid, const double *ene, 
     FBSE_CHECK_LAUNCH(c);
   }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return set_err(c, FBSE_ERR_CUDA, "fbse_precond_apply");
-  return FBSE_OK;
+  return check_dev_status(c);
 }
 
 int fbse_precond_grad(fbse_precond *p, const double *resid, const double *corr, const double *ene, long n,

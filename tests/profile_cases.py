@@ -2,20 +2,20 @@
 profiles/ profile (pytest does not collect this file).  Each case builds its
 workload, runs it once to warm up (autotuner decisions, buffers) and then once
 more, so that a capture with `-s <launches of the warm-up>` sees the second
-run.  It needs a GPU and the built library.
+run.  The cases are sized to hold a few GB on the device.  It needs a GPU and
+the built library.
 
-  python tests/profile_cases.py rr        Rayleigh-Ritz of 256 filtered spinor states
-                                          of the 3 nm CdSe dot (k_gram, k_jacobi_sweep,
+  python tests/profile_cases.py rr        Rayleigh-Ritz of 64 filtered spinor states of
+                                          a 2 nm CdSe dot, 96^3 (k_gram, k_jacobi_sweep,
                                           k_rotate, k_quad_diag)
-  python tests/profile_cases.py filter    Newton filter, 16 spinor starts x 16 targets,
-                                          nCheby 256, 128^3 (k_newton_acc and H psi)
-  python tests/profile_cases.py bse       BSE kernel contraction, 40 holes x 40
-                                          electrons of spinor states on 128^3, mixed
-                                          path (k_pair_density, convolution FFTs,
-                                          k_tc_images, k_tc_gemm_nt)
-  python tests/profile_cases.py precond   learned preconditioner forward + backward on
-                                          8 spinor residuals of an 80^3 dot (k_conv,
-                                          k_conv_wgrad)
+  python tests/profile_cases.py filter    Newton filter of 8 spinor starts x 16 targets,
+                                          nCheby 256, 2 nm dot, 32-slot ring (k_newton_acc)
+  python tests/profile_cases.py bse       BSE kernel of 16 hole x 16 electron spinor states
+                                          of the 2 nm dot, mixed path (k_pair_density,
+                                          convolution FFTs, k_tc_images, k_tc_gemm_nt)
+  python tests/profile_cases.py precond   learned preconditioner on 8 spinor residuals of a
+                                          1.6 nm dot, 80^3: inference (k_conv, k_conv16_tc)
+                                          and one gradient (k_conv, k_conv_wgrad)
 """
 import os
 import sys
@@ -26,17 +26,20 @@ import numpy as np
 sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 
-def _dot(radius=15.0):
+def _dot(radius):
     from filterbse_gb300 import workload as W
     return W.cdse_dot(radius, d=0.5, ke_max=10.0, spinor=True)
 
 
-def _ctx(F, dot, prec):
+def _ctx(F, dot, prec, ring=0):
     g = dot.grid
-    return F.Context(g, dot.pot, nspin=2, is_complex=True, so=True, nl=False, proj=dot.proj, precision=prec)
+    c = F.Context(g, dot.pot, nspin=2, is_complex=True, so=True, nl=False, proj=dot.proj, precision=prec)
+    if ring:
+        c.set_tuning(newton_ring=ring)
+    return c
 
 
-def _filter_setup(F, dot, ctx, nc, nstart=16):
+def _filter_setup(F, dot, ctx, nc, nstart):
     import torch
     import bench as B
     g = dot.grid
@@ -50,9 +53,9 @@ def _filter_setup(F, dot, ctx, nc, nstart=16):
 
 
 def case_filter(F):
-    dot = _dot()
-    ctx = _ctx(F, dot, F.MIXED)
-    zn, an, vmin, de, d0 = _filter_setup(F, dot, ctx, 256)
+    dot = _dot(10.0)
+    ctx = _ctx(F, dot, F.MIXED, ring=32)
+    zn, an, vmin, de, d0 = _filter_setup(F, dot, ctx, 256, 8)
     for _ in range(2):
         t = time.time()
         ctx.newton_filter(zn, an, vmin, de, d0)
@@ -61,10 +64,10 @@ def case_filter(F):
 
 def case_rr(F):
     import torch
-    dot = _dot()
-    ctx = _ctx(F, dot, F.MIXED)
-    zn, an, vmin, de, d0 = _filter_setup(F, dot, ctx, 256)
-    filt = ctx.newton_filter(zn, an, vmin, de, d0).reshape(256, -1)
+    dot = _dot(10.0)
+    ctx = _ctx(F, dot, F.MIXED, ring=32)
+    zn, an, vmin, de, d0 = _filter_setup(F, dot, ctx, 256, 4)
+    filt = ctx.newton_filter(zn, an, vmin, de, d0).reshape(64, -1)
     for _ in range(2):
         t = torch.clone(filt)
         t0 = time.time()
@@ -74,10 +77,10 @@ def case_rr(F):
 
 def case_bse(F):
     import torch
-    dot = _dot()
+    dot = _dot(10.0)
     ctx = _ctx(F, dot, F.MIXED)
     g = dot.grid
-    nh = ne = 40
+    nh = ne = 16
     gen = torch.Generator(device="cuda:0").manual_seed(1)
     pd = torch.randn((nh + ne, 2 * g.ngrid), dtype=torch.complex128, device="cuda:0", generator=gen)
     pd /= torch.sqrt((pd.abs() ** 2).sum(dim=1, keepdim=True) * g.dv)
@@ -87,7 +90,7 @@ def case_bse(F):
         t = time.time()
         ctx.bse_kernel(pd, nh, ne, nh, bare, scr)
         torch.cuda.synchronize()
-        print(f"bse kernel 40h x 40e: {time.time() - t:.3f}s")
+        print(f"bse kernel {nh}h x {ne}e: {time.time() - t:.3f}s")
 
 
 def case_precond(F):
@@ -101,10 +104,13 @@ def case_precond(F):
     e = rng.uniform(-0.3, -0.1, n)
     pc = F.Precond(ctx, seed=3)
     for _ in range(2):
+        torch.cuda.synchronize()
         t = time.time()
         pc.apply(r, e)
+        torch.cuda.synchronize()
+        t1 = time.time()
         pc.grad(r, c, e)
-        print(f"precond forward + gradient, {n} states: {time.time() - t:.3f}s")
+        print(f"precond inference {t1 - t:.3f}s, forward + gradient {time.time() - t1:.3f}s ({n} states)")
 
 
 def main():
