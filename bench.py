@@ -377,7 +377,7 @@ def learned_leg(args, F, W, dot, g, cmx, zn_an, d_starts, stlen, fp64, log):
     ext = torch.cuda.ExternalStream(cmx.stream_handle)
     net = F.Precond(cmx, weights=w)
     for name, p in (("refined", net), ("refined_plain", None)):
-        buf = torch.zeros((2 * n + n // 2, stlen), dtype=torch.float64, device=d_starts.device)
+        buf = torch.zeros((3 * n, stlen), dtype=torch.float64, device=d_starts.device)
         buf[:n] = ps[:n]
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()

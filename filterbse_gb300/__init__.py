@@ -77,7 +77,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("fft_kernels", ctypes.c_int), ("fft_plane_cluster", ctypes.c_int),
                 ("fft_chunk_blocks", ctypes.c_long), ("scatter_states", ctypes.c_int),
                 ("gather_points", ctypes.c_int), ("newton_ring", ctypes.c_int), ("bse_simt", ctypes.c_int),
-                ("tc_image_bytes", ctypes.c_double), ("ritz_cut", ctypes.c_double), ("ritz_hpsi", ctypes.c_int)]
+                ("tc_image_bytes", ctypes.c_double), ("ritz_cut", ctypes.c_double), ("ritz_hpsi", ctypes.c_int),
+                ("hpsi_fused", ctypes.c_int)]
 
 
 _lib = None

@@ -78,6 +78,119 @@ template <typename D, typename S> static int upload(fbse_ctx *c, D **dst, const 
   return FBSE_OK;
 }
 
+// plane-major projector table of the projector-fused plane passes (hpsi_fused.cuh),
+// built from the point-major table (covered points cj in increasing grid index,
+// entries cb[k] .. cb[k+1]-1 of point k in increasing atom order, per entry
+// its atom pa, Y_1m py[(m nent + e) 2 + re/im] and radial values ps / pn
+// [q nent + e]).  Per plane z: the atoms whose spheres meet it (slots), its
+// entries ordered by (layer = rank of the atom among the point's atoms, slot,
+// grid point), the layer offsets, and segments of at most kSegMax entries of
+// one (layer, slot) for the gather; per atom its segments in plane order.
+// Leaves fz_ok = 0 (the separate kernels then run) when the grid, the
+// precision or the table does not fit the kernel.
+static int build_plane_table(fbse_ctx *c, const std::vector<int> &cj, const std::vector<int> &cb,
+                             const std::vector<int> &pa, const std::vector<double> &py, const std::vector<double> &ps,
+                             const std::vector<double> &pn, size_t nent)
+{
+  ProjDev &p = c->proj;
+  p.fz_ok = 0;
+  const long NX = kPipeN;
+  if (c->precision != FBSE_MIXED || c->nx != NX || c->ny != NX || nent == 0)
+    return FBSE_OK;
+  for (size_t k = 0; k < nent; k++) {
+    const double y0 = py[2 * k], y1 = py[2 * k + 1];
+    if (py[(nent + k) * 2 + 1] != 0.0 || py[(2 * nent + k) * 2] != -y0 || py[(2 * nent + k) * 2 + 1] != y1)
+      return FBSE_OK;
+  }
+  const long nz = c->nz, nxy = NX * NX;
+  const int kPA = kPipePlaneAtoms, kML = kPipeMaxLayers, kSM = kPipeSegMax;
+  std::vector<unsigned> ent;
+  std::vector<float> fy[3], fso(nent * p.nproj), fnl(nent * p.nproj);
+  std::vector<int> lay(nz * (kML + 1), 0), atoms(nz * kPA, -1), natoms(nz, 0), seg_beg, plane_seg(nz + 1, 0), seg_atom;
+  ent.reserve(nent);
+  for (auto &v : fy) v.reserve(nent);
+  struct Item { int layer, slot, j, e; };
+  size_t k = 0;
+  for (long z = 0; z < nz; z++) {
+    size_t k1 = k;
+    while (k1 < cj.size() && cj[k1] / nxy == z) k1++;
+    std::vector<int> at;
+    for (int e = cb[k]; e < cb[k1]; e++) at.push_back(pa[e]);
+    std::sort(at.begin(), at.end());
+    at.erase(std::unique(at.begin(), at.end()), at.end());
+    if ((int)at.size() > kPA) return FBSE_OK;
+    natoms[z] = (int)at.size();
+    for (size_t s = 0; s < at.size(); s++) atoms[z * kPA + s] = at[s];
+    std::vector<Item> it;
+    for (size_t q = k; q < k1; q++)
+      for (int e = cb[q]; e < cb[q + 1]; e++) {
+        if (e - cb[q] >= kML) return FBSE_OK;
+        const int s = (int)(std::lower_bound(at.begin(), at.end(), pa[e]) - at.begin());
+        it.push_back({e - cb[q], s, cj[q], e});
+      }
+    std::sort(it.begin(), it.end(), [](const Item &x, const Item &y) {
+      return x.layer != y.layer ? x.layer < y.layer : x.slot != y.slot ? x.slot < y.slot : x.j < y.j;
+    });
+    plane_seg[z] = (int)seg_beg.size();
+    const int base = (int)ent.size();
+    for (int L = 0; L <= kML; L++) {
+      size_t i = 0;
+      while (i < it.size() && it[i].layer < L) i++;
+      lay[z * (kML + 1) + L] = base + (int)i;
+    }
+    for (size_t i = 0; i < it.size(); i++) {
+      const Item &x = it[i];
+      const bool start = i == 0 || x.layer != it[i - 1].layer || x.slot != it[i - 1].slot ||
+                         (int)ent.size() - seg_beg.back() >= kSM;
+      if (start) {
+        seg_beg.push_back((int)ent.size());
+        seg_atom.push_back(at[x.slot]);
+      }
+      const int xy = x.j % (int)nxy;
+      ent.push_back((unsigned)(xy % NX) | ((unsigned)(xy / NX) << 7) | ((unsigned)x.slot << 16));
+      fy[0].push_back((float)py[2 * x.e]);
+      fy[1].push_back((float)py[2 * x.e + 1]);
+      fy[2].push_back((float)py[(nent + x.e) * 2]);
+      const size_t o = ent.size() - 1;
+      for (int q = 0; q < p.nproj; q++) {
+        fso[q * nent + o] = (float)ps[q * nent + x.e];
+        fnl[q * nent + o] = (float)pn[q * nent + x.e];
+      }
+    }
+    k = k1;
+  }
+  plane_seg[nz] = (int)seg_beg.size();
+  const long nseg = (long)seg_beg.size();
+  seg_beg.push_back((int)ent.size());
+  // atom -> segments (stable counting sort keeps plane order)
+  std::vector<int> aseg_beg(p.nat + 1, 0), aseg(nseg ? nseg : 1, 0);
+  for (long s = 0; s < nseg; s++) aseg_beg[seg_atom[s] + 1]++;
+  for (long a = 0; a < p.nat; a++) aseg_beg[a + 1] += aseg_beg[a];
+  {
+    std::vector<int> fill(aseg_beg.begin(), aseg_beg.end() - 1);
+    for (long s = 0; s < nseg; s++) aseg[fill[seg_atom[s]]++] = (int)s;
+  }
+  std::vector<float> fyall;
+  fyall.reserve(3 * nent);
+  for (auto &v : fy) fyall.insert(fyall.end(), v.begin(), v.end());
+  int rc;
+  if ((rc = upload(c, &p.fz_ent, ent.data(), ent.size()))) return rc;
+  if ((rc = upload(c, &p.fz_y, fyall.data(), fyall.size()))) return rc;
+  if ((rc = upload(c, &p.fz_so, fso.data(), fso.size()))) return rc;
+  if ((rc = upload(c, &p.fz_nl, fnl.data(), fnl.size()))) return rc;
+  if ((rc = upload(c, &p.fz_lay, lay.data(), lay.size()))) return rc;
+  if ((rc = upload(c, &p.fz_atoms, atoms.data(), atoms.size()))) return rc;
+  if ((rc = upload(c, &p.fz_natoms, natoms.data(), natoms.size()))) return rc;
+  if ((rc = upload(c, &p.fz_seg_beg, seg_beg.data(), seg_beg.size()))) return rc;
+  if ((rc = upload(c, &p.fz_plane_seg, plane_seg.data(), plane_seg.size()))) return rc;
+  if ((rc = upload(c, &p.fz_aseg_beg, aseg_beg.data(), aseg_beg.size()))) return rc;
+  if ((rc = upload(c, &p.fz_aseg, aseg.data(), aseg.size()))) return rc;
+  p.fz_nent = (long)nent;
+  p.fz_nseg = nseg;
+  p.fz_ok = 1;
+  return FBSE_OK;
+}
+
 static void def_LS(double *ls)
 {  // def_LS (filter_mpi/hamiltonian.c:312-442): L.S in the flattened (s, m) basis
   const double h = std::sqrt(0.5);
@@ -270,6 +383,7 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
       if ((rc = upload(c, &p.pe_y1f, py.data(), py.size()))) return rc;
       if ((rc = upload(c, &p.pe_sopf, ps.data(), ps.size()))) return rc;
       if ((rc = upload(c, &p.pe_nlpf, pn.data(), pn.size()))) return rc;
+      if ((rc = build_plane_table(c, cj, cb, pa, py, ps, pn, nent))) return rc;
     }
     FBSE_CUDA(c, cudaMalloc(&p.LS, 36 * sizeof(double2)));
     FBSE_CUDA(c, cudaMemcpy(p.LS, ls, 36 * sizeof(double2), cudaMemcpyHostToDevice));
@@ -320,7 +434,9 @@ void fbse_destroy(fbse_ctx *c)
                   c->proj.nl_cnt, c->proj.jxyz, c->proj.y1, c->proj.sop, c->proj.nlp, c->proj.sgn, c->proj.LS,
                   c->proj.y1f, c->proj.sopf, c->proj.nlpf, c->proj.cov_j, c->proj.cov_beg, c->proj.pe_atom,
                   c->proj.pe_y1, c->proj.pe_sop, c->proj.pe_nlp, c->proj.pe_y1f, c->proj.pe_sopf, c->proj.pe_nlpf,
-                  c->proj.chunk_beg, c->proj.chunk_atoms, c->proj.pe_slot};
+                  c->proj.chunk_beg, c->proj.chunk_atoms, c->proj.pe_slot, c->proj.fz_ent, c->proj.fz_y,
+                  c->proj.fz_so, c->proj.fz_nl, c->proj.fz_lay, c->proj.fz_atoms, c->proj.fz_natoms,
+                  c->proj.fz_seg_beg, c->proj.fz_plane_seg, c->proj.fz_aseg_beg, c->proj.fz_aseg};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : c->cache)
@@ -388,7 +504,7 @@ int fbse_set_tuning(fbse_ctx *c, const fbse_tuning *t)
       !pow2_in(t->gather_points, 4) ||
       (t->newton_ring != 0 && (t->newton_ring < 8 || t->newton_ring > 128)) || t->bse_simt < 0 || t->bse_simt > 1 ||
       !(t->tc_image_bytes >= 0) || !(t->ritz_cut >= 0 && t->ritz_cut < 1) || t->ritz_hpsi < 0 ||
-      t->ritz_hpsi > 2)
+      t->ritz_hpsi > 2 || t->hpsi_fused < 0 || t->hpsi_fused > 1)
     return set_err(c, FBSE_ERR_ARG, "fbse_set_tuning: a field is out of range");
   c->tune = *t;
   c->tuned.clear();  // earlier decisions may rest on the old fixed choices
@@ -449,7 +565,8 @@ int fbse_newton_filter(fbse_ctx *c, const double *zn, const double *an, long nch
 int fbse_energy_range(fbse_ctx *c, long seed, long max_iter, double *emin, double *emax, long *iters)
 {
   if (!c || !emin || !emax || max_iter < 1) return c ? set_err(c, FBSE_ERR_ARG, "fbse_energy_range: bad arguments") : FBSE_ERR_ARG;
-  return energy_range(c, seed, max_iter, emin, emax, iters);
+  const int rc = energy_range(c, seed, max_iter, emin, emax, iters);
+  return rc ? rc : check_dev_status(c);
 }
 
 int fbse_normalize_all(fbse_ctx *c, double *psitot, long n, double *norms)
@@ -467,7 +584,8 @@ int fbse_energy_all(fbse_ctx *c, const double *psitot, long n, double *ene)
 int fbse_sigma_e(fbse_ctx *c, const double *psitot, long n, double *eval, double *sigma)
 {
   if (!c || !psitot || !eval || !sigma) return c ? set_err(c, FBSE_ERR_ARG, "fbse_sigma_e: null") : FBSE_ERR_ARG;
-  return energy_all(c, psitot, n, eval, sigma);
+  const int rc = energy_all(c, psitot, n, eval, sigma);
+  return rc ? rc : check_dev_status(c);
 }
 
 int fbse_gram(fbse_ctx *c, const double *A, long na, const double *B, long nb, long off, long len, double *out)
@@ -487,7 +605,8 @@ int fbse_ortho_diag_sigma(fbse_ctx *c, double *psitot, long n, long *n_kept, dou
 {
   if (!c || !psitot || !n_kept || !eval || !sigma || n < 1)
     return c ? set_err(c, FBSE_ERR_ARG, "fbse_ortho_diag_sigma: bad arguments") : FBSE_ERR_ARG;
-  return ortho_diag_sigma(c, psitot, n, n_kept, eval, sigma);
+  const int rc = ortho_diag_sigma(c, psitot, n, n_kept, eval, sigma);
+  return rc ? rc : check_dev_status(c);
 }
 
 }  // extern "C"

@@ -92,9 +92,22 @@ struct ProjDev {
   unsigned char *pe_slot = nullptr;
   double *pe_y1 = nullptr, *pe_sop = nullptr, *pe_nlp = nullptr;
   float *pe_y1f = nullptr, *pe_sopf = nullptr, *pe_nlpf = nullptr;
+  // plane-major copy for the projector-fused plane passes (hpsi_fused.cuh;
+  // FP32 contexts on 128 x 128 x nz grids whose Y_1m have the form (y0, y1),
+  // (y2, 0), (-y0, y1)): fz_ok when built
+  int fz_ok = 0;
+  long fz_nent = 0, fz_nseg = 0;
+  unsigned *fz_ent = nullptr;
+  float *fz_y = nullptr, *fz_so = nullptr, *fz_nl = nullptr;
+  int *fz_lay = nullptr, *fz_atoms = nullptr, *fz_natoms = nullptr, *fz_seg_beg = nullptr, *fz_plane_seg = nullptr;
+  int *fz_aseg_beg = nullptr, *fz_aseg = nullptr;
 };
 
 constexpr int kScatterChunkPoints = 128, kScatterChunkAtoms = 32;
+// projector-fused plane passes (hpsi_fused.cuh): plane edge, atoms whose
+// spheres meet one plane, entries of one grid point, table entries per gather
+// segment
+constexpr int kPipeN = 128, kPipePlaneAtoms = 192, kPipeMaxLayers = 8, kPipeSegMax = 128;
 
 // one decision of the autotuner: candidate values with their times (us)
 struct TuneRecord {
@@ -126,6 +139,7 @@ struct fbse_ctx {
   double *red = nullptr; size_t red_bytes = 0;   // reduction partials
   int *dstatus = nullptr;                        // device error flags of kernels with bounded waits
   int tc_poisoned = 0;  // a tensor-core wait timed out: MMAs may still be in flight, the path is refused
+  int nsm = 0;          // multiprocessors of the device (queried on first use)
   // large buffers kept between calls (grown on demand, freed by fbse_destroy):
   // the Newton ring, the Rayleigh-Ritz H psi and rotated states, the
   // filter job's device copies of the starts and filtered states
@@ -166,7 +180,7 @@ inline int launch_status(fbse_ctx *c)
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FBSE_OK : set_err(c, FBSE_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
 }
-enum CacheSlot { kSlotRing = 0, kSlotHpsi, kSlotRot, kSlotJobStarts, kSlotJobStates, kSlotJacobi, kSlotTc };
+enum CacheSlot { kSlotRing = 0, kSlotHpsi, kSlotRot, kSlotJobStarts, kSlotJobStates, kSlotJacobi, kSlotTc, kSlotProj };
 inline int cached(fbse_ctx *c, int slot, size_t need, void **out)
 {
   const int rc = ensure(c, &c->cache[slot], &c->cache_bytes[slot], need);
@@ -256,6 +270,13 @@ template <typename T>
 int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scale, C<T> *scratch = nullptr);
 template <typename T>
 int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, double b);
+// H psi with the projectors fused into the plane passes (hpsi_fused.cu):
+// whether it applies to this context, and out = a H in + b in
+bool hpsi_fused_ok(fbse_ctx *c);
+int hpsi_fused_apply(fbse_ctx *c, const float2 *in, float2 *out, long nstates, double a, double b);
+// the z pass of the kinetic operator (forward, min(k^2/2, KE_max)/N,
+// inverse) in place on nblk FP32 blocks (fft.cu)
+int zpass_kinetic(fbse_ctx *c, float2 *data, long nblk);
 
 // tensor-core complex products (tcgemm.cu):
 //   out[i][j] = scale * sum_r f(A[i][r]) B[j][r], f = conj when conj_a

@@ -528,6 +528,9 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
 template <typename T>
 int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, double b)
 {
+  if constexpr (sizeof(T) == 4) {
+    if (hpsi_fused_ok(c)) return hpsi_fused_apply(c, in, out, nstates, a, b);
+  }
   const size_t need = (size_t)nstates * c->nspin * c->ngrid * sizeof(C<T>);
   int rc = ensure(c, &c->wk, &c->wk_bytes, need);
   if (rc) return rc;

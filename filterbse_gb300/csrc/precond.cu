@@ -7,7 +7,7 @@
 //   x0 = [f / rms(f), f / rms(f) * (V - E) / 1 Ha]          2 channels, BF16
 //   a1 = tanh(W1 * x0), a2 = tanh(W2 * a1), a3 = tanh(W3 * a2)  16 channels, BF16
 //   y  = W4 * a3                                               1 channel, FP32
-//   correction = y * rms(f)
+//   correction = f + y * rms(f)       (residual connection: W4 = 0 gives f)
 // "*" is a 3x3x3 convolution over the grid with zero padding and no bias, so
 // the correction is an odd function of the residual.  Weights are FP32 in
 // the layout [c_out][c_in][27] per layer, k = (dz * 3 + dy) * 3 + dx.
@@ -489,7 +489,8 @@ __global__ void k_field_rms(const double *__restrict__ psi, long ngrid, int nspi
   if (threadIdx.x == 0) rms[f] = sqrt(red[0] / (double)ngrid);
 }
 
-// network input x0[f][2][p] (BF16) and, with corr, the target t[f][p] = corr / rms
+// network input x0[f][2][p] (BF16) and, with corr, the target of y,
+// t[f][p] = (corr - f) / rms (the output adds f back)
 __global__ void k_field_in(const double *__restrict__ psi, const double *__restrict__ corr, long nf, long ngrid,
                            int nspin, int cplx, const double *__restrict__ pot, const double *__restrict__ ene,
                            const double *__restrict__ rms, __nv_bfloat16 *__restrict__ x0, float *__restrict__ tgt)
@@ -505,13 +506,13 @@ __global__ void k_field_in(const double *__restrict__ psi, const double *__restr
     const double v = psi[e] * r;
     x0[(f * 2) * ngrid + p] = __float2bfloat16((float)v);
     x0[(f * 2 + 1) * ngrid + p] = __float2bfloat16((float)(v * (pot[p] - ene[st]) / kVScale));
-    if (tgt) tgt[i] = (float)(corr[e] * r);
+    if (tgt) tgt[i] = (float)((corr[e] - psi[e]) * r);
   }
 }
 
-// out (psitot layout) = y * rms
-__global__ void k_field_out(const float *__restrict__ y, long nf, long ngrid, int nspin, int cplx,
-                            const double *__restrict__ rms, double *__restrict__ out)
+// out (psitot layout) = resid + y * rms
+__global__ void k_field_out(const float *__restrict__ y, const double *__restrict__ resid, long nf, long ngrid,
+                            int nspin, int cplx, const double *__restrict__ rms, double *__restrict__ out)
 {
   const int fps = nspin * (cplx + 1);
   const long stlen = (long)(cplx + 1) * nspin * ngrid;
@@ -519,7 +520,8 @@ __global__ void k_field_out(const float *__restrict__ y, long nf, long ngrid, in
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     const long f = i / ngrid, p = i % ngrid, st = f / fps, comp = f % fps;
     const long spin = comp / (cplx + 1), part = comp % (cplx + 1);
-    out[st * stlen + (cplx ? (spin * ngrid + p) * 2 + part : spin * ngrid + p)] = (double)y[i] * rms[f];
+    const long e = st * stlen + (cplx ? (spin * ngrid + p) * 2 + part : spin * ngrid + p);
+    out[e] = resid[e] + (double)y[i] * rms[f];
   }
 }
 
@@ -904,11 +906,12 @@ int fbse_precond_create(fbse_ctx *c, fbse_precond **out, const float *weights, l
   if (weights) {
     std::copy(weights, weights + nw, w.begin());
   } else {
-    // uniform in +-sqrt(3 / fan_in) (unit variance through each layer), drawn
-    // with the reference's own generator (ran_nrc) from the seed
+    // uniform in +-sqrt(3 / fan_in) (unit variance through each layer), the
+    // last layer at a tenth of that so that P(r) = r + y rms starts near r;
+    // drawn with the reference's own generator (ran_nrc) from the seed
     long s = -std::labs(seed) - 1;
     for (int l = 0; l < pc::kLayers; l++) {
-      const double a = std::sqrt(3.0 / (pc::kCin[l] * 27.0));
+      const double a = std::sqrt(3.0 / (pc::kCin[l] * 27.0)) * (l == pc::kLayers - 1 ? 0.1 : 1.0);
       for (long i = pc::kWOff[l]; i < pc::kWOff[l + 1]; i++) w[i] = (float)(a * (2.0 * fbse_ran(&s) - 1.0));
     }
   }
@@ -969,8 +972,8 @@ int fbse_precond_apply(fbse_precond *p, const double *resid, const double *ene, 
     pc::Bufs b;
     long nf = 0;
     if ((rc = pc::forward(p, resid + s0 * stlen, nullptr, ene + s0, ns, false, &b, &nf))) return rc;
-    pc::k_field_out<<<pc::blocks_for(nf * c->ngrid), 256, 0, c->stream>>>(b.y, nf, c->ngrid, c->nspin,
-                                                                           c->is_complex, b.rms, out + s0 * stlen);
+    pc::k_field_out<<<pc::blocks_for(nf * c->ngrid), 256, 0, c->stream>>>(
+        b.y, resid + s0 * stlen, nf, c->ngrid, c->nspin, c->is_complex, b.rms, out + s0 * stlen);
     FBSE_CHECK_LAUNCH(c);
   }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return set_err(c, FBSE_ERR_CUDA, "fbse_precond_apply");
@@ -1016,7 +1019,8 @@ int fbse_residual(fbse_ctx *c, const double *psitot, long n, const double *ene, 
 {
   if (!c || !psitot || !ene || !out || n < 1 || out == psitot)
     return c ? set_err(c, FBSE_ERR_ARG, "fbse_residual: arguments") : FBSE_ERR_ARG;
-  return residual_host_e(c, psitot, n, ene, out);
+  const int rc = residual_host_e(c, psitot, n, ene, out);
+  return rc ? rc : check_dev_status(c);
 }
 
 int fbse_refine(fbse_ctx *c, fbse_precond *p, double *psitot, long n, long cap, int steps, double tol, long *n_out,
@@ -1034,7 +1038,7 @@ int fbse_refine(fbse_ctx *c, fbse_precond *p, double *psitot, long n, long cap, 
     cur = nk;
   }
   *n_out = cur;
-  return FBSE_OK;
+  return check_dev_status(c);
 }
 
 }  // extern "C"

@@ -133,6 +133,10 @@ typedef struct fbse_tuning {
                               default otherwise */
   int ritz_hpsi;           /* H psi of the mixed path's Rayleigh-Ritz step: 0 default (FP32), 1 FP32,
                               2 FP64 (the FP64 operator's tables are held by every context) */
+  int hpsi_fused;          /* 1: FP32 H psi on 128 x 128 x nz grids with the projector gather and scatter
+                              fused into the xy plane passes (slower than the separate projector
+                              kernels on the measured workloads); 0: separate projector kernels.
+                              Results differ in rounding only */
 } fbse_tuning;
 int fbse_get_tuning(fbse_ctx *ctx, fbse_tuning *t);
 int fbse_set_tuning(fbse_ctx *ctx, const fbse_tuning *t);
@@ -289,14 +293,17 @@ void fbse_batch_destroy(fbse_batch *b);
  * normalised by its RMS; the network sees it with the local potential as
  * [r^, r^ (V - E) / 1 Ha] (2 channels), runs four 3x3x3 convolutions with
  * 16 channels (tanh after the first three, no biases, so the correction is
- * odd in r) and returns one channel, scaled back by the RMS.  Weights are FP32
+ * odd in r) and returns one channel y, scaled back by the RMS and added to the
+ * input: P(r) = r + y rms (a residual connection, so a network whose last
+ * layer is zero is the plain residual refinement).  Weights are FP32
  * (FBSE_PRECOND_NWEIGHTS floats: layer l's [c_out][c_in][27] blocks in order),
  * activations BF16, arithmetic FP32.  Training (Adam, mean squared error
  * against target corrections) and inference run on the GPU in the library's
  * own forward and backward kernels. */
 typedef struct fbse_precond fbse_precond;
 #define FBSE_PRECOND_NWEIGHTS 15120
-/* weights NULL: seeded random initialisation (scaled uniform) */
+/* weights NULL: seeded random initialisation (scaled uniform; the last layer
+ * at a tenth of its scale, so P starts close to the identity) */
 int fbse_precond_create(fbse_ctx *ctx, fbse_precond **out, const float *weights_host, long seed);
 /* May come before or after fbse_destroy of its context (it touches only its
  * own memory); every other fbse_precond_* call needs the context alive. */
@@ -318,9 +325,10 @@ int fbse_precond_train_step(fbse_precond *p, const double *resid, const double *
 /* Residual refinement of n Ritz pairs (psitot rows 0..n-1 on the device,
  * normalised, with eval / sigma on the host as fbse_ortho_diag_sigma returns
  * them).  Each of `steps` rounds forms r = (H - E) psi for the pairs with
- * sigma > tol, appends P(r) (p NULL: r itself) as new rows and runs
- * fbse_ortho_diag_sigma on the enlarged set.  psitot must hold cap rows;
- * a round appends at most cap - n rows.  eval / sigma need cap doubles; *n_out
+ * sigma > tol, appends P(r) (p NULL: r itself) as new rows (each
+ * normalised) and runs fbse_ortho_diag_sigma on the enlarged set.  psitot
+ * must hold cap rows; a round appends at most cap - n rows (pairs in
+ * increasing row order while they fit).  eval / sigma need cap doubles; *n_out
  * receives the final number of Ritz pairs. */
 int fbse_refine(fbse_ctx *ctx, fbse_precond *p, double *psitot, long n, long cap, int steps, double tol,
                 long *n_out, double *eval, double *sigma);

@@ -9,10 +9,12 @@ backward kernels can be checked against it:
   per real field f of a residual (state-major, then spin block, then real /
   imaginary part), x0 = [f / rms(f), f / rms(f) * (V - E) / 1 Ha] rounded to
   BF16; a_l = BF16(tanh(W_l * a_{l-1})) for l = 1..3; y = W_4 * a_3 (FP32);
-  correction = y * rms(f).  "*" is a 3x3x3 convolution with zero padding and
-  no bias; W_l has the layout [c_out][c_in][27], k = (dz * 3 + dy) * 3 + dx.
+  correction = f + y * rms(f) (a residual connection).  "*" is a 3x3x3
+  convolution with zero padding and no bias; W_l has the layout
+  [c_out][c_in][27], k = (dz * 3 + dy) * 3 + dx.
 
-The loss is the mean over all fields and points of (y - corr / rms)^2.
+The loss is the mean over all fields and points of (correction - corr)^2 / rms^2,
+i.e. of (y - (corr - f) / rms)^2.
 Arithmetic here is FP64 with the BF16 rounding of the stored activations
 applied where the GPU stores them, so the two agree to FP32 summation-order
 differences except where an FP32 and an FP64 value round to neighbouring BF16
@@ -137,14 +139,15 @@ def forward(w, resid, ene, pot, nspin, cplx, shape, round_bf16=True):
 
 def apply(w, resid, ene, pot, nspin, cplx, shape):
     y, rms, _ = forward(w, resid, ene, pot, nspin, cplx, shape)
-    return unfields(y * rms[:, None, None, None], nspin, cplx)
+    return np.asarray(resid, np.float64) + unfields(y * rms[:, None, None, None], nspin, cplx)
 
 
 def loss_grad(w, resid, corr, ene, pot, nspin, cplx, shape, round_bf16=True):
-    """(loss, gradient [NWEIGHTS]) of mean (y - corr / rms)^2."""
+    """(loss, gradient [NWEIGHTS]) of mean (y - (corr - resid) / rms)^2."""
     W = layers(w)
     y, rms, acts = forward(w, resid, ene, pot, nspin, cplx, shape, round_bf16)
-    t = fields(corr, nspin, cplx, shape) / np.where(rms > 0, rms, np.inf)[:, None, None, None]
+    d = np.asarray(corr, np.float64) - np.asarray(resid, np.float64)
+    t = fields(d, nspin, cplx, shape) / np.where(rms > 0, rms, np.inf)[:, None, None, None]
     M = y.size
     loss = float(np.sum((y - t) ** 2) / M)
     g = [np.zeros_like(Wl) for Wl in W]

@@ -32,7 +32,7 @@ def _targets(vbmin, vbmax, cbmin, cbmax, nvb, ncb):
 
 
 def _run(fbse, cuda, grid, pot, targets, ncheby, nstart, nspin, cplx, so=False, nl=False, proj=None, seed=-31415,
-         precision=0, states=False, refine_steps=0):
+         precision=0, states=False):
     import torch
     ctx = fbse.Context(grid, pot, nspin=nspin, is_complex=cplx, so=so, nl=nl, proj=proj, precision=precision)
     e0, e1, it = ctx.energy_range()
@@ -46,14 +46,6 @@ def _run(fbse, cuda, grid, pot, targets, ncheby, nstart, nspin, cplx, so=False, 
     m = len(targets)
     psitot = filt.reshape(nstart * m, -1)
     nk, ev, sg = ctx.ortho_diag_sigma(psitot)
-    if refine_steps:
-        # residual refinement (plain residuals) of the pairs above 1e-4
-        buf = torch.zeros((3 * nk, ctx.stlen), dtype=torch.float64, device=cuda)
-        buf[:nk] = psitot[:nk]
-        n0 = np.sum(sg < 1e-4)
-        nk, ev, sg = ctx.refine(buf, nk, ev, sg, steps=refine_steps, tol=1e-4)
-        psitot = buf
-        print(f"\n[refine] sigma < 1e-4: {n0} -> {np.sum(sg < 1e-4)} of {nk} pairs")
     if states:
         return (emin, emax), ev, sg, psitot[:nk].cpu().numpy()
     return (emin, emax), ev, sg
@@ -68,8 +60,8 @@ def _match(ref, ev, sg, ref_sig, my_sig, tol):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_cdse22_real_matches_reference_eval(fbse, cuda, precision):
-    """2.2 nm CdSe, real, 57 x 52 x 45 at 0.8 bohr, 16 starts x 16 targets, nCheby 2048
-    (filter_mpi/EXAMPLES/2.2nm_CdSe/filter: input.par, eval.dat)."""
+    """2.2 nm CdSe, real, 57 x 52 x 45 at 0.8 bohr, 16 starts (FP64; 48 mixed) x 16 targets,
+    nCheby 2048 (filter_mpi/EXAMPLES/2.2nm_CdSe/filter: input.par, eval.dat)."""
     atyp, xyz = read_conf(os.path.join(GOLD, "cdse22", "conf.par"))
     types = sorted(set(atyp), key=atyp.index)
     # the grid of that run (localPot.cube header); its version used box = n d on odd axes
@@ -77,10 +69,14 @@ def test_cdse22_real_matches_reference_eval(fbse, cuda, precision):
     tabs = [read_pot(os.path.join(GOLD, "cdse22", f"pot{t}.par")) for t in types]
     pot = O.local_pot(g, xyz, np.array([types.index(a) for a in atyp]), tabs)
     targets = _targets(-0.31, -0.24, -0.15, -0.06, 10, 6)
-    # the mixed path: three rounds of residual refinement lift the pairs that
-    # the FP32 recursion's noise leaves above 1e-4 (fbse_refine)
-    (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, 16, 1, False, precision=precision,
-                                refine_steps=3 if precision else 0)
+    # the mixed path filters 48 starts: the FP32 recursion's noise (about 1e-4
+    # of each filtered state's norm) swamps the directions of the filtered
+    # subspace whose overlap eigenvalues lie below ~1e-6 of the largest, so a
+    # level that 16 starts carry only in such directions needs more starts
+    # (measured on this input: 16 starts match 64 of the 124 levels, 32 match
+    # 99, 48 match 107; the FP64 path matches 121 with 16)
+    nstart = 48 if precision else 16
+    (emin, emax), ev, sg = _run(fbse, cuda, g, pot, targets, 2048, nstart, 1, False, precision=precision)
     # run.dat:140 of the reference run: Emin = -1.13271, Emax = 12.3281.  Both
     # iterations stop at a relative change below 1e-6 per step (energy.c:239,
     # 282), not at the extremum, so the stopping values agree only to ~1e-3.
