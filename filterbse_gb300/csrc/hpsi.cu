@@ -301,18 +301,42 @@ __global__ void __launch_bounds__(256) k_proj_scatter(C<T> *__restrict__ out, co
 // scatter over chunks of covered points (ProjDev::chunk_beg ...): one CTA
 // per chunk (at most kScatterChunkPoints points, kScatterChunkAtoms atoms),
 // one thread per point, all states in groups of kG.  The coefficients of the
-// chunk's atoms for a group's states are staged in shared memory once and
-// shared by every point, and the table entries of the chunk stay in L1 across
-// the groups, so the table is read from L2 once per H psi.  The arithmetic of
-// each (state, point) is that of k_proj_scatter, in the same order.
-template <typename T, bool SO, bool NL, int kG>
+// chunk's atoms for a group's states are staged in shared memory once (16-byte
+// copies of the chunk's own atoms) and shared by every point; the table values
+// of a point's first entry stay in registers across the groups (NPJ: the
+// number of radial channels when it is 5, else 0 and read at run time).  The
+// arithmetic of each (state, point) is that of k_proj_scatter, in the same
+// order.
+template <typename T> struct Row6 {
+  static __device__ __forceinline__ void ld(const C<T> *d, C<T> r[6])
+  {
+#pragma unroll
+    for (int i = 0; i < 6; i++) r[i] = d[i];
+  }
+};
+template <> struct Row6<float> {
+  static __device__ __forceinline__ void ld(const float2 *d, float2 r[6])
+  {
+    const float4 *v = reinterpret_cast<const float4 *>(d);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float4 t = v[i];
+      r[2 * i] = make_float2(t.x, t.y);
+      r[2 * i + 1] = make_float2(t.z, t.w);
+    }
+  }
+};
+
+template <typename T, bool SO, bool NL, int kG, int NPJ>
 __global__ void __launch_bounds__(kScatterChunkPoints) k_proj_scatter_chunk(
     C<T> *__restrict__ out, const C<T> *__restrict__ coef, PtView<T> pv, const int *__restrict__ chunk_beg,
     const int *__restrict__ chunk_atoms, const unsigned char *__restrict__ slot, long nat, long nstates, long ngrid,
     int nspin, T scale)
 {
   constexpr int NCH = (SO ? 1 : 0) + (NL ? 1 : 0);
-  constexpr int ROW = NCH * kNC;  // coefficients per (state, atom)
+  constexpr int ROW = NCH * kNC;                          // coefficients per (state, atom)
+  constexpr int U16 = ROW * (int)sizeof(C<T>) / 16;       // 16-byte units per (state, atom)
+  constexpr int kCache = 1;                               // entries whose table values stay in registers
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C<T> *dsm = reinterpret_cast<C<T> *>(smem_raw);  // [kG][kScatterChunkAtoms][ROW]
   const int c = blockIdx.x;
@@ -322,17 +346,44 @@ __global__ void __launch_bounds__(kScatterChunkPoints) k_proj_scatter_chunk(
   const long k = p0 + (live ? t : 0);
   const long j = pv.cov_j[k];
   const int e0 = pv.cov_beg[k], e1 = live ? pv.cov_beg[k + 1] : e0;
-  const int npj = pv.nproj;
+  const int npj = NPJ ? NPJ : pv.nproj;
   const int ch0 = SO ? 0 : 1;
+  int na = 0;  // the chunk's atoms come first, unused slots are -1
+  while (na < kScatterChunkAtoms && chunk_atoms[c * kScatterChunkAtoms + na] >= 0) na++;
+  auto table = [&](int e, T yr[3], T yi[3], T bs[5], T bn[5]) {
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+      const C<T> y = pv.y1[m * pv.nent + e];
+      yr[m] = y.x;
+      yi[m] = y.y;
+    }
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+      bs[p] = (SO && p < npj) ? pv.sop[p * pv.nent + e] : T(0);
+      bn[p] = (NL && p < npj) ? pv.nlp[p * pv.nent + e] : T(0);
+    }
+  };
+  T cyr[kCache][3], cyi[kCache][3], cbs[kCache][5], cbn[kCache][5];
+  int csl[kCache];
+#pragma unroll
+  for (int q = 0; q < kCache; q++) {
+    if (e0 + q < e1) {
+      table(e0 + q, cyr[q], cyi[q], cbs[q], cbn[q]);
+      csl[q] = slot[e0 + q];
+    }
+  }
   for (long s0 = 0; s0 < nstates; s0 += kG) {
     const int ng = (int)(nstates - s0 < kG ? nstates - s0 : kG);
     __syncthreads();
-    for (int i = t; i < kG * kScatterChunkAtoms * ROW; i += blockDim.x) {
-      const int g = i / (kScatterChunkAtoms * ROW), sa = (i / ROW) % kScatterChunkAtoms, q = i % ROW;
-      const int a = chunk_atoms[c * kScatterChunkAtoms + sa];
-      C<T> v = mk<T>(T(0), T(0));
-      if (g < ng && a >= 0) v = coef[(((s0 + g) * nat + a) * 2 + ch0) * kNC + q];
-      dsm[i] = v;
+#pragma unroll
+    for (int g = 0; g < kG; g++) {
+      if (g >= ng) break;
+      for (int i = t; i < na * U16; i += blockDim.x) {
+        const int sa = i / U16, u = i - sa * U16;
+        const int a = chunk_atoms[c * kScatterChunkAtoms + sa];
+        reinterpret_cast<float4 *>(dsm + (g * kScatterChunkAtoms + sa) * ROW)[u] =
+            reinterpret_cast<const float4 *>(coef + (((s0 + g) * nat + a) * 2 + ch0) * kNC)[u];
+      }
     }
     __syncthreads();
     if (!live) continue;
@@ -349,19 +400,23 @@ __global__ void __launch_bounds__(kScatterChunkPoints) k_proj_scatter_chunk(
       ai[g][0] = ai[g][1] = T(0);
     }
     for (int e = e0; e < e1; e++) {
-      const int sl = slot[e];
-      T yr[3], yi[3];
+      int sl;
+      T yr[3], yi[3], bs[5], bn[5];
+      if (e == e0) {
 #pragma unroll
-      for (int m = 0; m < 3; m++) {
-        const C<T> y = pv.y1[m * pv.nent + e];
-        yr[m] = y.x;
-        yi[m] = y.y;
-      }
-      T bs[5], bn[5];
+        for (int m = 0; m < 3; m++) {
+          yr[m] = cyr[0][m];
+          yi[m] = cyi[0][m];
+        }
 #pragma unroll
-      for (int p = 0; p < 5; p++) {
-        bs[p] = (SO && p < npj) ? pv.sop[p * pv.nent + e] : T(0);
-        bn[p] = (NL && p < npj) ? pv.nlp[p * pv.nent + e] : T(0);
+        for (int p = 0; p < 5; p++) {
+          bs[p] = cbs[0][p];
+          bn[p] = cbn[0][p];
+        }
+        sl = csl[0];
+      } else {
+        table(e, yr, yi, bs, bn);
+        sl = slot[e];
       }
 #pragma unroll
       for (int g = 0; g < kG; g++) {
@@ -373,17 +428,18 @@ __global__ void __launch_bounds__(kScatterChunkPoints) k_proj_scatter_chunk(
 #pragma unroll
         for (int p = 0; p < 5; p++) {
           if (p >= npj) continue;
+          C<T> rs[6], rn[6];
+          if (SO) Row6<T>::ld(d + p * 6, rs);
+          if (NL) Row6<T>::ld(d + (SO ? kNC : 0) + p * 6, rn);
 #pragma unroll
           for (int q = 0; q < 6; q++) {
             if (SO) {
-              const C<T> r = d[p * 6 + q];
-              qr[q] += bs[p] * r.x;
-              qi[q] += bs[p] * r.y;
+              qr[q] += bs[p] * rs[q].x;
+              qi[q] += bs[p] * rs[q].y;
             }
             if (NL) {
-              const C<T> r = d[(SO ? kNC : 0) + p * 6 + q];
-              qr[q] += bn[p] * r.x;
-              qi[q] += bn[p] * r.y;
+              qr[q] += bn[p] * rn[q].x;
+              qi[q] += bn[p] * rn[q].y;
             }
           }
         }
@@ -424,17 +480,24 @@ static void launch_gather(fbse_ctx *c, dim3 g, const C<T> *in, C<T> *coef, const
                                                                       c->nspin, ch0, c->dv);
 }
 
-template <typename T, bool SO, bool NL, int kG>
-static int launch_scatter_chunk1(fbse_ctx *c, C<T> *out, const C<T> *coef, const PtView<T> &pt, long nstates, T sc)
+template <typename T, bool SO, bool NL, int kG, int NPJ>
+static int launch_scatter_chunk2(fbse_ctx *c, C<T> *out, const C<T> *coef, const PtView<T> &pt, long nstates, T sc)
 {
   const ProjDev &p = c->proj;
   constexpr int NCH = (SO ? 1 : 0) + (NL ? 1 : 0);
   const size_t smem = (size_t)kG * kScatterChunkAtoms * NCH * kNC * sizeof(C<T>);
-  FBSE_CUDA(c, cudaFuncSetAttribute(k_proj_scatter_chunk<T, SO, NL, kG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
-  k_proj_scatter_chunk<T, SO, NL, kG><<<(unsigned)p.nchunk, kScatterChunkPoints, smem, c->stream>>>(
+  FBSE_CUDA(c, cudaFuncSetAttribute(k_proj_scatter_chunk<T, SO, NL, kG, NPJ>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_proj_scatter_chunk<T, SO, NL, kG, NPJ><<<(unsigned)p.nchunk, kScatterChunkPoints, smem, c->stream>>>(
       out, coef, pt, p.chunk_beg, p.chunk_atoms, p.pe_slot, p.nat, nstates, c->ngrid, c->nspin, sc);
   return FBSE_OK;
+}
+
+template <typename T, bool SO, bool NL, int kG>
+static int launch_scatter_chunk1(fbse_ctx *c, C<T> *out, const C<T> *coef, const PtView<T> &pt, long nstates, T sc)
+{
+  if (pt.nproj == 5) return launch_scatter_chunk2<T, SO, NL, kG, 5>(c, out, coef, pt, nstates, sc);
+  return launch_scatter_chunk2<T, SO, NL, kG, 0>(c, out, coef, pt, nstates, sc);
 }
 
 template <typename T, int kG>
