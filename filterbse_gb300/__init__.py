@@ -26,7 +26,7 @@ EXPORTED = [
     "fbse_create", "fbse_destroy", "fbse_last_error", "fbse_version", "fbse_alloc", "fbse_free",
     "fbse_upload", "fbse_download", "fbse_sync", "fbse_stream", "fbse_hpsi", "fbse_hnorm",
     "fbse_newton_filter", "fbse_energy_range", "fbse_normalize_all", "fbse_energy_all", "fbse_sigma_e",
-    "fbse_ortho_diag_sigma", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
+    "fbse_ortho_diag_sigma", "fbse_angular_stats", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
     "fbse_init_filter_states", "fbse_launch_count", "fbse_filter_job", "fbse_build_local_pot",
     "fbse_bse_potentials", "fbse_bse_kernel", "fbse_bse_kernel_real", "fbse_bse_solve", "fbse_bse_dipoles", "fbse_bse_mag_dipoles",
     "fbse_bse_qp_ang_mom",
@@ -141,6 +141,7 @@ def load() -> ctypes.CDLL:
     L.fbse_bse_qp_ang_mom.argtypes = [_VP, _VP, _D, _D, _D, ctypes.c_long, ctypes.c_long, ctypes.c_long, _D, _D, _D,
                                       _D]
     L.fbse_bse_optical.argtypes = [_VP, _VP, _D, ctypes.c_long, ctypes.c_long, _D]
+    L.fbse_angular_stats.argtypes = [_VP, _VP, ctypes.c_long, _D, _D, _D, _D]
     L.fbse_get_tuning.argtypes = [_VP, ctypes.POINTER(Tuning)]
     L.fbse_set_tuning.argtypes = [_VP, ctypes.POINTER(Tuning)]
     L.fbse_tuning_report.argtypes = [_VP, ctypes.c_char_p, ctypes.c_long]
@@ -544,6 +545,17 @@ class Context:
                                               lumo_idx, _dp(s.view(np.float64)), _dp(l.view(np.float64)),
                                               _dp(l2.view(np.float64)), _dp(ls.view(np.float64))))
         return s.reshape(-1, 3), l.reshape(-1, 3), l2, ls
+
+    def angular_stats(self, states, gx, gy, gz):
+        """calc_angular_exp (filter_mpi/angular.c:4-165): per complex spinor
+        state (device, psitot layout), the angular.dat columns <Jx>, <Jx^2>,
+        <Jy>, <Jy^2>, <Jz>, <Jz^2>, <J^2>, norm as an [n, 8] array."""
+        gx, gy, gz = (np.ascontiguousarray(a, np.float64) for a in (gx, gy, gz))
+        n = int(states.shape[0])
+        out = np.empty((n, 8), np.float64)
+        self._torch_sync()
+        self._chk(self._L.fbse_angular_stats(self._h, self._ptr(states), n, _dp(gx), _dp(gy), _dp(gz), _dp(out)))
+        return out
 
     def bse_optical(self, coeff, mu_pairs, n_h, n_e):
         """calc_optical_exc (electric part): exciton dipoles [n_xton, 3] complex128

@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfbse_gpu.so")
-CU_SOURCES = ["hpsi_fused.cu", "fft.cu", "hpsi.cu", "filter.cu", "linalg.cu", "bse.cu", "tcgemm.cu", "setup.cu", "job.cu", "precond.cu", "batch.cu", "api.cu"]
+CU_SOURCES = ["hpsi_fused.cu", "fft.cu", "hpsi.cu", "filter.cu", "linalg.cu", "bse.cu", "angular.cu", "tcgemm.cu", "setup.cu", "job.cu", "precond.cu", "batch.cu", "api.cu"]
 C_SOURCES = ["host/fbse_host.c", "host/fbse_setup.c", "host/fbse_bse_stats.c"]
 EXECUTABLES = {"fbse_filter": "host/fbse_filter_main.c", "fbse_bse": "host/fbse_bse_main.c"}
 BIN = os.path.join(HERE, "bin")

@@ -248,6 +248,7 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
   for (int a = 0; a < 3; a++) {
     const double box = (ns[a] % 2 == 0) ? (double)ns[a] * ds[a] : (double)(ns[a] - 1) * ds[a];
     const double dk = dkin[a] > 0 ? dkin[a] : 6.28318530717958647692 / box;
+    c->dk[a] = dk;
     std::vector<double> k;
     axis_k2(ns[a], dk, ng_1, k);
     if ((rc = upload(c, dst[a], k.data(), k.size()))) return rc;

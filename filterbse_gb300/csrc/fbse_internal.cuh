@@ -124,6 +124,7 @@ struct fbse_ctx {
   int nspin = 1, is_complex = 0, so = 0, nl = 0;
   double dx = 0, dy = 0, dz = 0, dv = 0, ke_max = 0;
   double kemax_scaled = 0;                 // KE_max / N (init.c:338)
+  double dk[3] = {0, 0, 0};                // reciprocal spacings dkx, dky, dkz (init.c:65-80)
   fbse::AxisPlan ax[3];                    // x, y, z
   double *k2x = nullptr, *k2y = nullptr, *k2z = nullptr;  // per-axis 0.5 k^2 / N (device)
   float *k2xf = nullptr, *k2yf = nullptr, *k2zf = nullptr;  // the same rounded to FP32 (mixed path)

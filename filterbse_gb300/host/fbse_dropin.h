@@ -31,6 +31,7 @@ typedef struct {
   int read_coeffs; /* readCoeffs = 1: zn.dat and coeff-<t>.dat are read (mod_filter.c:116-126) */
   int input_psi_filt; /* inputPsiFilt = 1 <start> <end>: starts from psi-init.dat (init.c:1166-1203) */
   long init_psi_start, init_psi_end;
+  int calc_spin_ang_stat; /* calcSpinAngStat = 1: angular.dat (mod_optional_output.c:51-62) */
 } fbse_filter_params;
 
 /* the subset of bse_cplx/input.par (bse_cplx/read.c) */

@@ -15,7 +15,8 @@
  * The starts come from psi-init.dat with "inputPsiFilt = 1 <start> <end>".
  * Also written: conf.dat, seed-0.dat, zn.dat / coeff-<t>.dat (read back
  * instead of computed with readCoeffs = 1) and, with "printCubes = 1 <n>",
- * the homo-i / lumo+i cube files of mod_optional_output.
+ * the homo-i / lumo+i cube files of mod_optional_output; with
+ * "calcSpinAngStat = 1", angular.dat (calc_angular_exp).
  * Errors go to stderr and the process exits with EXIT_FAILURE, like the
  * reference.  One non-reference key: "mixedPrecision = 1" selects the FP32
  * recursion (default: the plain FP64 method). */
@@ -88,8 +89,20 @@ static void save_output(const char *path, const fbse_filter_params *p, long nato
   fclose(f);
 }
 
-/* print_eigstate_densities (mod_optional_output.c:74-240): homo is the last
- * converged state below fermiEnergy, lumo the next converged one; the cubes of
+/* homo_idx / lumo_idx of print_eigstate_densities (mod_optional_output.c:
+ * 103-147): homo is the last converged state below fermiEnergy, lumo the next
+ * converged one (0 when there is none), in eval.dat's order */
+static void homo_lumo(const fbse_filter_params *p, const double *eval, const double *sigma, long n, long *homo,
+                      long *lumo)
+{
+  *homo = *lumo = 0;
+  for (long i = 0; i < n; i++)
+    if (eval[i] < p->fermi_e && sigma[i] < p->sigma_e_cut) *homo = i;
+  for (long i = *homo + 1; i < n; i++)
+    if (sigma[i] < p->sigma_e_cut) { *lumo = i; break; }
+}
+
+/* print_eigstate_densities (mod_optional_output.c:74-240): the cubes of
  * homo-i and lumo+i (i < ncubes) hold |psi|^2 signed by the dominant component
  * (density_phase_sign, write.c:52-60), per spin block.  The states are the
  * ones written to psi.dat, in eval.dat's order. */
@@ -97,11 +110,8 @@ static void write_cubes(const fbse_filter_params *p, const double *psi, const do
                         long n, long nx, long ny, long nz, double xmin, double ymin, double zmin, int nspin, int cplx,
                         long natoms, const double *xyz, const int *atype, char names[][8])
 {
-  long homo = 0, lumo = 0;
-  for (long i = 0; i < n; i++)
-    if (eval[i] < p->fermi_e && sigma[i] < p->sigma_e_cut) homo = i;
-  for (long i = homo + 1; i < n; i++)
-    if (sigma[i] < p->sigma_e_cut) { lumo = i; break; }
+  long homo, lumo;
+  homo_lumo(p, eval, sigma, n, &homo, &lumo);
   printf("homo_idx = %ld; lumo_idx = %ld\n", homo, lumo);
   if (homo == 0 || lumo == 0) {
     printf("Did not converge enough electron or hole states to visualize cube files.\n");
@@ -131,6 +141,47 @@ static void write_cubes(const fbse_filter_params *p, const double *psi, const do
     }
   free(rho);
   free(sym8);
+}
+
+/* calcSpinAngStat (mod_optional_output.c:51-62 -> calc_angular_exp,
+ * angular.c:4-165): angular.dat with <Jx>, <Jx^2>, <Jy>, <Jy^2>, <Jz>, <Jz^2>,
+ * <J^2> and the norm of the states homo - 4 ... lumo + 11 of psi.dat.  The
+ * reference takes homo / lumo from print_eigstate_densities, which runs only
+ * with printCubes = 1 (otherwise the indices are never set), and reads outside
+ * psitot when homo < 4 or lumo + 12 exceeds the states; here the indices are
+ * found the same way in either case and the range is clipped to the states
+ * written. */
+static void write_angular(fbse_ctx *ctx, const fbse_filter_params *p, const double *psi, const double *eval,
+                          const double *sigma, long n, long stlen, const double *gx, const double *gy,
+                          const double *gz)
+{
+  long homo, lumo;
+  homo_lumo(p, eval, sigma, n, &homo, &lumo);
+  long start = homo - 4, stop = lumo + 12;
+  if (start < 0) start = 0;
+  if (stop > n) stop = n;
+  FILE *f = fopen("angular.dat", "w");
+  if (!f) die("cannot write", "angular.dat");
+  fprintf(f, "###    Jx        Jx^2       Jy        Jy^2      Jz       Jz^2       J^2      norm\n");
+  if (stop > start) {
+    const long cnt = stop - start;
+    const size_t bytes = (size_t)cnt * stlen * sizeof(double);
+    void *d = NULL;
+    double *st = malloc((size_t)cnt * 8 * sizeof(double));
+    if (!st) die("host allocation", NULL);
+    check(ctx, fbse_alloc(ctx, &d, bytes), "angular statistics buffer");
+    check(ctx, fbse_upload(ctx, d, psi + start * stlen, bytes), "upload");
+    check(ctx, fbse_angular_stats(ctx, d, cnt, gx, gy, gz, st), "spin / angular statistics");
+    check(ctx, fbse_free(ctx, d), "free");
+    for (long i = 0; i < cnt; i++) {
+      const double *r = st + 8 * i;
+      fprintf(f, "%i\t%f\t%f\t%f\t%f\t%f\t%f\t%f\t%f\n", (int)(start + i), r[0], r[1], r[2], r[3], r[4], r[5],
+              r[6], r[7]);
+    }
+    free(st);
+  }
+  fclose(f);
+  printf("angular.dat: states %ld to %ld\n", start, stop - 1);
 }
 
 /* zn.dat and coeff-<t>.dat as gen_newton_coeff writes them (coeff.c:66-108):
@@ -196,6 +247,8 @@ int main(void)
   char err[512];
   fbse_filter_params p;
   if (fbse_read_filter_params("input.par", &p, err, sizeof err)) die(err, NULL);
+  if (p.calc_spin_ang_stat == 1 && !p.use_spinors) /* read.c:82: statistics need spin-orbit (spinor) states */
+    die("calcSpinAngStat = 1 needs spinor states (useSpinors = 1)", NULL);
   long natoms;
   double *xyz;
   int *atype, ntypes;
@@ -540,6 +593,7 @@ int main(void)
   check(ctx, fbse_free(ctx, d_psi), "free");
   if (p.print_cubes == 1)
     write_cubes(&p, psi, eval, sigma, n_out, nx, ny, nz, xmin, ymin, zmin, nspin, cplx, natoms, xyz, atype, names);
+  if (p.calc_spin_ang_stat == 1) write_angular(ctx, &p, psi, eval, sigma, n_out, stlen, gx, gy, gz);
   fbse_destroy(ctx);
   return 0;
 }

@@ -47,7 +47,7 @@ static const char *k_ignored[] = {"nThreads", "hamThreads", "nestedOMP", "useFas
 /* keys whose non-zero value selects a path this library does not implement */
 static const char *k_unsupported[] = {"periodic", "useStrain", "longRange", "localStructureDependent",
                                       "useGaussianBasis", "readProj",
-                                      "restartFromCheckpoint", "interpolatePot", "calcSpinAngStat", NULL};
+                                      "restartFromCheckpoint", "interpolatePot", NULL};
 
 static int in_list(const char *k, const char **l)
 {
@@ -118,6 +118,7 @@ int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, 
         rc = -1;
     }
     else if (!strcmp(key, "printPsiDiag")) { rc = parse_long(val, &lv); p->print_psi_diag = (int)lv; }
+    else if (!strcmp(key, "calcSpinAngStat")) { rc = parse_long(val, &lv); p->calc_spin_ang_stat = (int)lv; }
     else if (!strcmp(key, "calcFilterOnly")) { rc = parse_long(val, &lv); p->calc_filter_only = (int)lv; }
     else if (!strcmp(key, "restartFromOrtho")) {
       /* "restartFromOrtho = 1 <states in psi-filt.dat>" (read.c:762-773) */

@@ -223,6 +223,24 @@ int fbse_normalize_all_noalloc(fbse_ctx *ctx, double *psitot, long n, double *no
  * sqrt|<H^2> - <H>^2| for normalised states. */
 int fbse_ortho_diag_sigma(fbse_ctx *ctx, double *psitot, long n, long *n_kept, double *eval, double *sigma);
 
+/* ---- spin and angular-momentum statistics of the filter's states ---------
+ * Replaces calc_angular_exp (filter_mpi/angular.c:4-165), the
+ * calcSpinAngStat output of mod_optional_output (mod_optional_output.c:51-62),
+ * for n complex spinor states (psitot layout, device, FP64; the context must
+ * have nspin = 2 and is_complex = 1, else FBSE_ERR_UNSUPPORTED).  Each state
+ * passes the reference's k-space low-pass (low_pass_filter, angular.c:403-455)
+ * and is normalised; J = L + S is applied with L = r x p, p = -i grad by FFT
+ * on the context's grid (apply_L_op, angular.c:218-400; coordinates gx, gy,
+ * gz on the host as grid->x / y / z, distribution centre at the origin as in
+ * the reference) and S = sigma / 2 (apply_J_op, angular.c:169-216).  stats
+ * (host, 8 n doubles) receives per state the columns of angular.dat:
+ * <Jx>, <Jx^2>, <Jy>, <Jy^2>, <Jz>, <Jz^2>, <J^2>, norm.  Every state is
+ * read from its own slot (angular.c:63 reads the spin-up imaginary part of
+ * state i > 0 from offset i * nspinngrid instead of 2 i * nspinngrid).
+ * Returns FBSE_ERR_NAN for a state whose low-passed norm is zero or NaN. */
+int fbse_angular_stats(fbse_ctx *ctx, const double *psitot, long n, const double *gx, const double *gy,
+                       const double *gz, double *stats);
+
 /* ---- slab products (FP64) ---------------------------------------------------
  * The two dense products of the Rayleigh-Ritz step restricted to a slab of
  * each state's values [off, off + len) (complex values for complex states, as

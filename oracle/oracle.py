@@ -801,6 +801,56 @@ def bse_qp_ang_mom(psi_qp, nh, ne, lumo, grid: Grid):
     return S, Lm, L2, LS
 
 
+def filter_angular_stats(psis, grid: Grid):
+    """calc_angular_exp (filter_mpi/angular.c:4-165) for complex spinor states
+    (rows of psitot, (re, im) interleaved, up block then down block): per
+    state low_pass_filter on each block (angular.c:403-455: FFTW round trip
+    with the mask kx^2 + ky^2 + kz^2 < (3 dkz)^2 on init_kvec's wave vectors,
+    which carry 1/N), normalize (norm.c:41-78), apply_J_op / apply_L_op
+    (angular.c:169-400: p_d = IFFT(k_d/N FFT), L = r x p with the centre at the
+    origin, plus sigma/2) and the eight sums times dv (angular.c:127-157).
+    Each state's own imaginary parts are read (angular.c:63 offsets the
+    spin-up imaginary part of state i > 0 by i * nspinngrid).  [n, 8]"""
+    N = grid.ngrid
+    shp = (grid.nz, grid.ny, grid.nx)
+    gx, gy, gz = grid.axes()
+    Z, Y, X = np.meshgrid(gz, gy, gx, indexing="ij")
+    dkx, dky, dkz = grid.dk()
+    kx, ky, kz = (init_kvec(n, dk) / N for n, dk in ((grid.nx, dkx), (grid.ny, dky), (grid.nz, dkz)))
+    KZ, KY, KX = np.meshgrid(kz, ky, kx, indexing="ij")
+    mask = (KX ** 2 + KY ** 2 + KZ ** 2) < (3.0 * dkz) ** 2
+    out = np.zeros((len(psis), 8))
+    for i, row in enumerate(psis):
+        z = np.asarray(row, np.float64).view(np.complex128)
+        blocks = []
+        for s in range(2):
+            f = np.fft.fftn(z[s * N:(s + 1) * N].reshape(shp))
+            blocks.append(np.fft.ifftn(np.where(mask, f, 0.0)) * N)  # FFTW's unnormalised backward
+        nrm = np.sqrt(sum(np.sum(np.abs(b) ** 2) for b in blocks) * grid.dv)
+        blocks = [b / nrm for b in blocks]
+        J = []
+        for b in blocks:
+            F = np.fft.fftn(b)
+            px, py, pz = (np.fft.ifftn(k * N * F) for k in (KX, KY, KZ))  # k carries 1/N; ifftn adds another
+            J.append([Y * pz - Z * py, Z * px - X * pz, X * py - Y * px])
+        u, d = blocks
+        J[0][0] = J[0][0] + 0.5 * d
+        J[1][0] = J[1][0] + 0.5 * u
+        J[0][1] = J[0][1] - 0.5j * d
+        J[1][1] = J[1][1] + 0.5j * u
+        J[0][2] = J[0][2] + 0.5 * u
+        J[1][2] = J[1][2] - 0.5 * d
+        r = np.zeros(8)
+        for s in range(2):
+            for a in range(3):
+                r[2 * a] += np.sum((np.conj(blocks[s]) * J[s][a]).real)
+                r[2 * a + 1] += np.sum(np.abs(J[s][a]) ** 2)
+            r[6] += sum(np.sum(np.abs(J[s][a]) ** 2) for a in range(3))
+            r[7] += np.sum(np.abs(blocks[s]) ** 2)
+        out[i] = r * grid.dv
+    return out
+
+
 def xton_ang_stats(C, S, Lm, L2, LS, nh, ne):
     """calc_xton_spin_mtrx and calc_xton_ang_mom_mtrx (bse_cplx/angular.c:692-1043):
     per exciton n: <S> (3), the spin sum of spins.dat, <L> (3), the orbital sum

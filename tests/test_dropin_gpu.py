@@ -54,7 +54,7 @@ def test_dropin_filter_mixed_matches_reference_eval(cuda, tmp_path):
 
 def test_dropin_filter_matches_reference_eval(cuda, tmp_path):
     text = open(os.path.join(GOLD, "cspbi3", "input.par")).read().replace("setSeed = 0", "setSeed = 1 31415")
-    _stage(tmp_path, text)
+    _stage(tmp_path, text + "calcSpinAngStat = 1\n")
     out = _run("fbse_filter", tmp_path)
     ev = np.loadtxt(tmp_path / "eval.dat")
     ref = np.loadtxt(os.path.join(GOLD, "cspbi3", "eval.dat"))
@@ -84,6 +84,32 @@ def test_dropin_filter_matches_reference_eval(cuda, tmp_path):
         dn = np.array(" ".join(open(tmp_path / f"{name}-Dn.cube").read().split("\n")[6 + 15:]).split(), float)
         assert up.size == dn.size == 44 ** 3
         assert abs((np.abs(up).sum() + np.abs(dn).sum()) * 0.125 - 1.0) < 1e-3
+    _check_angular_dat(tmp_path, ev, text)
+
+
+def _check_angular_dat(tmp, ev, text):
+    """angular.dat of calcSpinAngStat (filter_mpi/angular.c:4-165) against the
+    oracle's restatement on the same psi.dat states: the rows homo - 4 ...
+    lumo + 11 (mod_optional_output.c:61), columns printed with %f."""
+    from oracle import oracle as O
+    from tests.systems import read_conf
+    fermi = float(text.split("fermiEnergy =")[1].split()[0])
+    cut = float(text.split("sigmaECut =")[1].split()[0])
+    homo = max(i for i in range(len(ev)) if ev[i, 1] < fermi and ev[i, 2] < cut)
+    lumo = next(i for i in range(homo + 1, len(ev)) if ev[i, 2] < cut)
+    rows = np.loadtxt(tmp / "angular.dat", comments="#")
+    idx = np.arange(max(0, homo - 4), min(len(ev), lumo + 12))
+    assert rows.shape == (len(idx), 9) and np.array_equal(rows[:, 0], idx)
+    _, xyz = read_conf(os.path.join(GOLD, "cspbi3", "conf.par"))
+    g = O.reference_grid(np.ascontiguousarray(xyz), 0.5, (44,) * 3)
+    stlen = 2 * 2 * g.ngrid
+    psi = np.fromfile(tmp / "psi.dat", dtype=np.float64).reshape(len(ev), stlen)
+    want = O.filter_angular_stats(psi[idx], g)
+    dev = np.max(np.abs(rows[:, 1:] - want))
+    print(f"[fbse_filter cspbi3] angular.dat rows {idx[0]}..{idx[-1]}: <J^2> {rows[0, 7]:.4f} .. "
+          f"max dev from the oracle {dev:.1e}")
+    assert dev < 2e-6
+    assert np.allclose(rows[:, 8], 1.0) and np.all(rows[:, 7] > 0.7)  # normalised; <J^2> >= j(j+1) = 3/4
 
 
 def test_dropin_bse_matches_reference_exciton(cuda, tmp_path):
