@@ -27,7 +27,7 @@ EXPORTED = [
     "fbse_upload", "fbse_download", "fbse_sync", "fbse_stream", "fbse_hpsi", "fbse_hnorm",
     "fbse_newton_filter", "fbse_energy_range", "fbse_normalize_all", "fbse_energy_all", "fbse_sigma_e",
     "fbse_ortho_diag_sigma", "fbse_angular_stats", "fbse_samp_points", "fbse_newton_coeff", "fbse_ran",
-    "fbse_init_filter_states", "fbse_launch_count", "fbse_filter_job", "fbse_build_local_pot",
+    "fbse_init_filter_states", "fbse_launch_count", "fbse_filter_job", "fbse_build_local_pot", "fbse_build_nlc",
     "fbse_bse_potentials", "fbse_bse_kernel", "fbse_bse_kernel_real", "fbse_bse_solve", "fbse_bse_dipoles", "fbse_bse_mag_dipoles",
     "fbse_bse_qp_ang_mom",
     "fbse_bse_optical",
@@ -142,6 +142,11 @@ def load() -> ctypes.CDLL:
                                       _D]
     L.fbse_bse_optical.argtypes = [_VP, _VP, _D, ctypes.c_long, ctypes.c_long, _D]
     L.fbse_angular_stats.argtypes = [_VP, _VP, ctypes.c_long, _D, _D, _D, _D]
+    _Lp = ctypes.POINTER(ctypes.c_long)
+    L.fbse_build_nlc.argtypes = ([ctypes.c_long] * 3 + [_D] * 3 + [ctypes.c_long, _D, _D, _D, _D, ctypes.c_int,
+                                                                  ctypes.c_double, _Lp] +
+                                 [ctypes.POINTER(_Lp), ctypes.POINTER(ctypes.POINTER(ctypes.c_int))] +
+                                 [ctypes.POINTER(_D)] * 3)
     L.fbse_get_tuning.argtypes = [_VP, ctypes.POINTER(Tuning)]
     L.fbse_set_tuning.argtypes = [_VP, ctypes.POINTER(Tuning)]
     L.fbse_tuning_report.argtypes = [_VP, ctypes.c_char_p, ctypes.c_long]
@@ -209,6 +214,40 @@ def init_filter_states(n_filters, ngrid, nspin, is_complex, dv, seed):
     s = load().fbse_init_filter_states(_dp(out), n_filters, ngrid, nspin, int(is_complex), dv, seed,
                                        seeds.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
     return out.reshape(n_filters, stlen), seeds, s
+
+
+def build_nlc(axes, xyz, so_par, so_tab, nl_tab, nproj, rcut2):
+    """init_NL_projectors on the GPU (fbse_build_nlc): the projector table of
+    the atoms xyz [nat, 3] on the grid with coordinates axes = (gx, gy, gz).
+    so_tab [nproj, 1024] (scaled per atom by sqrt(so_par)) and nl_tab
+    [nat, nproj, 1024] may be None.  Returns (nl, npts, jxyz, y1, so_p, nl_p)
+    as numpy arrays (row stride npts)."""
+    L = load()
+    gx, gy, gz = (np.ascontiguousarray(a, np.float64) for a in axes)
+    xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+    nat = len(xyz)
+    sp = None if so_par is None else np.ascontiguousarray(so_par, np.float64)
+    st = None if so_tab is None else np.ascontiguousarray(so_tab, np.float64)
+    nt = None if nl_tab is None else np.ascontiguousarray(nl_tab, np.float64)
+    opt = lambda a: _dp(a) if a is not None else None
+    npts = ctypes.c_long()
+    p_nl = ctypes.POINTER(ctypes.c_long)()
+    p_jx = ctypes.POINTER(ctypes.c_int)()
+    p_y1, p_so, p_np = _D(), _D(), _D()
+    rc = L.fbse_build_nlc(len(gx), len(gy), len(gz), _dp(gx), _dp(gy), _dp(gz), nat, _dp(xyz), opt(sp), opt(st),
+                          opt(nt), int(nproj), float(rcut2), ctypes.byref(npts), ctypes.byref(p_nl),
+                          ctypes.byref(p_jx), ctypes.byref(p_y1), ctypes.byref(p_so), ctypes.byref(p_np))
+    if rc:
+        raise FbseError(rc, "fbse_build_nlc")
+    n = max(nat, 1) * npts.value
+    out = (np.ctypeslib.as_array(p_nl, (max(nat, 1),))[:nat].copy(), npts.value,
+           np.ctypeslib.as_array(p_jx, (n,)).copy(), np.ctypeslib.as_array(p_y1, (n * 6,)).copy(),
+           np.ctypeslib.as_array(p_so, (n * nproj,)).copy(), np.ctypeslib.as_array(p_np, (n * nproj,)).copy())
+    libc = ctypes.CDLL(None)
+    libc.free.argtypes = [ctypes.c_void_p]
+    for p in (p_nl, p_jx, p_y1, p_so, p_np):
+        libc.free(ctypes.cast(p, ctypes.c_void_p))
+    return out
 
 
 # ---------------------------------------------------------------------------

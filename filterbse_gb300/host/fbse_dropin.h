@@ -71,13 +71,8 @@ double fbse_r_nlcut2(double dx);
 int fbse_radial_projectors(double dx, double rcut, int kind, double lam1, double lam2, int nproj, double *out,
                            int *sgn);
 
-/* init_NL_projectors table (init.c:848-1135): projector atoms xyz[nat]; so
- * radial [nproj][N] scaled per atom by sqrt(so_par[a]); nl radial
- * [nat][nproj][N].  Allocates nl[nat], jxyz, y1, so_p, nl_p with row stride
- * *npts.  Returns 0 or -1. */
-int fbse_build_nlc(long nx, long ny, long nz, const double *gx, const double *gy, const double *gz, long nat,
-                   const double *xyz, const double *so_par, const double *so_tab, const double *nl_tab, int nproj,
-                   double rcut2, long *npts, long **nl, int **jxyz, double **y1, double **so_p, double **nl_p);
+/* the init_NL_projectors table: fbse_build_nlc (on the GPU, declared in
+ * include/fbse.h) */
 
 /* outputs (filter_mpi/write.c:263-299, save.c:446-503) */
 int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n);

@@ -528,92 +528,6 @@ int fbse_radial_projectors(double dx, double rcut, int kind, double lam1, double
   return 0;
 }
 
-/* linear interpolation of a radial table (the reference's interpolate) */
-static double interp(double r, double dr, const double *tab, long n)
-{
-  const long i = (long)(r / dr);
-  if (i > n - 2) return 0.0;
-  const double x0 = (double)i * dr, x1 = (double)(i + 1) * dr;
-  const double a = (tab[i + 1] - tab[i]) / (x1 - x0);
-  return a * r + (tab[i] - x0 * a);
-}
-
-int fbse_build_nlc(long nx, long ny, long nz, const double *gx, const double *gy, const double *gz, long nat,
-                   const double *xyz, const double *so_par, const double *so_tab, const double *nl_tab, int nproj,
-                   double rcut2, long *npts_out, long **nl_out, int **jxyz_out, double **y1_out, double **so_out,
-                   double **nl_p_out)
-{
-  const long N = FBSE_PROJ_LEN;
-  const double tmp1 = 0.5 * sqrt(3.0 / FBSE_PI), tmp2 = 0.5 * sqrt(3.0 / (2.0 * FBSE_PI));
-  const double drp = sqrt(rcut2) / (double)N;
-  long *nl = calloc(nat > 0 ? nat : 1, sizeof(long));
-  /* count the points of each sphere first (the row stride is the largest) */
-  long npts = 1;
-  for (long a = 0; a < nat; a++) {
-    long cnt = 0;
-    for (long jz = 0; jz < nz; jz++) {
-      const double dz = gz[jz] - xyz[3 * a + 2];
-      if (dz * dz >= rcut2) continue;
-      for (long jy = 0; jy < ny; jy++) {
-        const double dy = gy[jy] - xyz[3 * a + 1];
-        if (dy * dy + dz * dz >= rcut2) continue;
-        for (long jx = 0; jx < nx; jx++) {
-          const double ddx = gx[jx] - xyz[3 * a];
-          if (ddx * ddx + dy * dy + dz * dz < rcut2) cnt++;
-        }
-      }
-    }
-    nl[a] = cnt;
-    if (cnt > npts) npts = cnt;
-  }
-  const size_t ne = (size_t)(nat > 0 ? nat : 1) * npts;
-  int *jxyz = calloc(ne, sizeof(int));
-  double *y1 = calloc(ne * 6, sizeof(double));
-  double *sop = calloc(ne * nproj, sizeof(double));
-  double *nlp = calloc(ne * nproj, sizeof(double));
-  if (!nl || !jxyz || !y1 || !sop || !nlp) return -1;
-  for (long a = 0; a < nat; a++) {
-    long cnt = 0;
-    const double sq = so_par ? sqrt(so_par[a]) : 0.0;
-    for (long jz = 0; jz < nz; jz++) {
-      const double dz = gz[jz] - xyz[3 * a + 2], dzeps = dz + FBSE_EPSDX;
-      for (long jy = 0; jy < ny; jy++) {
-        const double dy = gy[jy] - xyz[3 * a + 1], dyeps = dy + FBSE_EPSDX;
-        for (long jx = 0; jx < nx; jx++) {
-          const double ddx = gx[jx] - xyz[3 * a], dxeps = ddx + FBSE_EPSDX;
-          const double d2 = ddx * ddx + dy * dy + dz * dz;
-          if (!(d2 < rcut2)) continue;
-          const size_t e = (size_t)a * npts + cnt;
-          jxyz[e] = (int)(nx * (ny * jz + jy) + jx);
-          /* Y_1m with the reference's EPSDX shifts (init.c:1002-1040) */
-          double r_1 = 1.0 / sqrt(ddx * ddx + dy * dy + dzeps * dzeps);
-          y1[e * 6 + 2] = tmp1 * dzeps * r_1;
-          y1[e * 6 + 3] = 0.0;
-          r_1 = 1.0 / sqrt(dxeps * dxeps + dy * dy + dz * dz);
-          y1[e * 6 + 4] = -tmp2 * dxeps * r_1;
-          y1[e * 6 + 0] = tmp2 * dxeps * r_1;
-          r_1 = 1.0 / sqrt(ddx * ddx + dyeps * dyeps + dz * dz);
-          y1[e * 6 + 5] = -tmp2 * dyeps * r_1;
-          y1[e * 6 + 1] = -tmp2 * dyeps * r_1;
-          const double r = sqrt(d2);
-          for (int p = 0; p < nproj; p++) {
-            sop[e * nproj + p] = so_tab ? interp(r, drp, so_tab + (long)p * N, N) * sq : 0.0;
-            nlp[e * nproj + p] = nl_tab ? interp(r, drp, nl_tab + ((long)a * nproj + p) * N, N) : 0.0;
-          }
-          cnt++;
-        }
-      }
-    }
-  }
-  *npts_out = npts;
-  *nl_out = nl;
-  *jxyz_out = jxyz;
-  *y1_out = y1;
-  *so_out = sop;
-  *nl_p_out = nlp;
-  return 0;
-}
-
 /* ---------------------------------------------------------------------------
  * outputs
  * ------------------------------------------------------------------------- */

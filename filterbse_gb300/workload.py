@@ -4,7 +4,7 @@ Builds what the reference reads from conf.par / pot*.par / SO_*.par and sets
 up in mod_init / mod_pseudopot: a passivated zincblende CdSe sphere, the
 grid of init_grid_params, the local potential of build_local_pot (on the GPU,
 fbse_build_local_pot), the spin-orbit radial projectors of gen_SO_projectors
-and the projector table of init_NL_projectors.  This is the input generator
+and the projector table of init_NL_projectors (on the GPU, fbse_build_nlc).  This is the input generator
 (the counterpart of the reference's example scripts), not part of the
 per-step hot path.
 
@@ -237,62 +237,13 @@ def so_radial(dx, rcut, nproj=NPROJ):
 
 
 def nlc_table(grid: Grid, coords, so_par, so_tab, nproj=NPROJ) -> ProjTable:
-    """init_NL_projectors (filter_mpi/init.c, body 508-589) vectorised per atom:
-    grid points with r^2 < R_NLcut2 in jz, jy, jx order, Y_1m with the
-    reference's EPSDX shifts, SO radial interpolated and scaled by sqrt(SO_par)."""
-    rc2 = r_nlcut2(grid.dx)
-    rc = np.sqrt(rc2)
-    gx, gy, gz = grid.axes()
-    N = PROJ_LEN
-    drp = rc / N
-    vr = np.arange(N) * drp
-    tmp1 = 0.5 * np.sqrt(3.0 / np.pi)
-    tmp2 = 0.5 * np.sqrt(3.0 / (2.0 * np.pi))
-    eps = 1e-20
-    rows = []
-    for a in range(len(coords)):
-        sx = np.nonzero(np.abs(gx - coords[a, 0]) < rc + grid.dx)[0]
-        sy = np.nonzero(np.abs(gy - coords[a, 1]) < rc + grid.dy)[0]
-        sz = np.nonzero(np.abs(gz - coords[a, 2]) < rc + grid.dz)[0]
-        JZ, JY, JX = np.meshgrid(sz, sy, sx, indexing="ij")
-        dx = gx[JX] - coords[a, 0]
-        dy = gy[JY] - coords[a, 1]
-        dz = gz[JZ] - coords[a, 2]
-        d2 = dx * dx + dy * dy + dz * dz
-        m = d2 < rc2
-        dx, dy, dz, d2 = dx[m], dy[m], dz[m], d2[m]
-        jxyz = (grid.nx * (grid.ny * JZ[m] + JY[m]) + JX[m]).astype(np.int32)
-        y = np.zeros((len(d2), 6))
-        r1 = 1.0 / np.sqrt(dx * dx + dy * dy + (dz + eps) ** 2)
-        y[:, 2] = tmp1 * (dz + eps) * r1
-        r1 = 1.0 / np.sqrt((dx + eps) ** 2 + dy * dy + dz * dz)
-        y[:, 4] = -tmp2 * (dx + eps) * r1
-        y[:, 0] = tmp2 * (dx + eps) * r1
-        r1 = 1.0 / np.sqrt(dx * dx + (dy + eps) ** 2 + dz * dz)
-        y[:, 5] = -tmp2 * (dy + eps) * r1
-        y[:, 1] = -tmp2 * (dy + eps) * r1
-        r = np.sqrt(d2)
-        i = (r / drp).astype(np.int64)
-        ok = i <= N - 2
-        ic = np.minimum(i, N - 2)
-        pr = np.empty((len(r), nproj))
-        for p in range(nproj):
-            t = so_tab[p]
-            sl = (t[ic + 1] - t[ic]) / (vr[ic + 1] - vr[ic])
-            pr[:, p] = np.where(ok, sl * r + (t[ic] - vr[ic] * sl), 0.0) * np.sqrt(so_par[a])
-        rows.append((jxyz, y, pr))
-    npts = max(1, max(len(r[0]) for r in rows))
-    nat = len(rows)
-    nl = np.array([len(r[0]) for r in rows], np.int64)
-    jx = np.zeros(nat * npts, np.int32)
-    y1 = np.zeros(nat * npts * 6)
-    pj = np.zeros(nat * npts * nproj)
-    for a, (j, y, p) in enumerate(rows):
-        c = len(j)
-        jx[a * npts:a * npts + c] = j
-        y1[a * npts * 6:(a * npts + c) * 6] = y.reshape(-1)
-        pj[a * npts * nproj:(a * npts + c) * nproj] = p.reshape(-1)
-    return ProjTable(nl, npts, jx, y1, pj, np.zeros_like(pj), np.zeros(nat * nproj, np.int32), nproj)
+    """init_NL_projectors (filter_mpi/init.c, body 508-589) on the GPU
+    (fbse_build_nlc): grid points with r^2 < R_NLcut2 in jz, jy, jx order,
+    Y_1m with the reference's EPSDX shifts, SO radial interpolated and scaled
+    by sqrt(SO_par); no NL channels."""
+    from . import build_nlc
+    nl, npts, jx, y1, pj, nlp = build_nlc(grid.axes(), coords, so_par, so_tab, None, nproj, r_nlcut2(grid.dx))
+    return ProjTable(nl.astype(np.int64), npts, jx, y1, pj, nlp, np.zeros(len(coords) * nproj, np.int32), nproj)
 
 
 def cdse_dot(radius_ang: float, d: float = 0.5, ke_max: float = 20.0, spinor: bool = True, so_par: float = 0.01,

@@ -441,6 +441,22 @@ int fbse_build_local_pot(long nx, long ny, long nz, const double *gx, const doub
                          long natoms, const double *coords, const int *atype, int ntypes, const double *tab_r,
                          const double *tab_v, const long *tab_off, const long *tab_len, double *pot);
 
+/* init_NL_projectors (filter_mpi/init.c:848-1135, body 508-589): for each of
+ * nat projector atoms (xyz [nat][3], host) the grid points with
+ * r^2 < rcut2 in jz, jy, jx order, with Y_1m under the reference's EPSDX
+ * shifts (init.c:1002-1040) and the radial projectors interpolated at r
+ * (interpolate(), linear): so_tab [nproj][1024] (PROJ_LEN) scaled per atom
+ * by sqrt(so_par[a]), nl_tab [nat][nproj][1024] (either may be NULL: zeros).
+ * Computed on the current CUDA device (one CTA per atom, no fused multiply-add,
+ * so the table is bit-identical to the plain IEEE evaluation); returns host
+ * arrays allocated with malloc (the caller frees them): nl[nat], and with
+ * row stride *npts (the largest count) jxyz[nat*npts], y1[nat*npts][6]
+ * (Y_1m, m = 0..2, re/im), so_p and nl_p [nat*npts][nproj] -- the arrays of
+ * fbse_proj_desc.  No context needed. */
+int fbse_build_nlc(long nx, long ny, long nz, const double *gx, const double *gy, const double *gz, long nat,
+                   const double *xyz, const double *so_par, const double *so_tab, const double *nl_tab, int nproj,
+                   double rcut2, long *npts, long **nl, int **jxyz, double **y1, double **so_p, double **nl_p);
+
 /* ---- host-side helpers (no device work) --------------------------------- */
 
 /* samp_points_ashkenazy on [-2, 2] (filter_mpi/coeff.c:227-293): writes

@@ -32,10 +32,13 @@ _I = ctypes.POINTER(ctypes.c_int)
 
 
 def build(force: bool = False) -> str:
-    """Compile the C restatement to oracle/liboracle.so (gcc, -O2, no -ffast-math)."""
+    """Compile the C restatement to oracle/liboracle.so (gcc, -O2, no -ffast-math,
+    no contraction into fused multiply-adds: plain IEEE arithmetic on every host)."""
     src = os.path.join(_HERE, "fbse_oracle.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
-        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu99", "-o", _LIB_PATH, src, "-lm"])
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(src),
+                                                                                     os.path.getmtime(__file__)):
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu99", "-ffp-contract=off", "-o", _LIB_PATH,
+                               src, "-lm"])
     return _LIB_PATH
 
 

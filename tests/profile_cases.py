@@ -16,6 +16,13 @@ the built library.
   python tests/profile_cases.py precond   learned preconditioner on 8 spinor residuals of a
                                           1.6 nm dot, 80^3: inference (k_conv, k_conv16_tc)
                                           and one gradient (k_conv, k_conv_wgrad)
+  python tests/profile_cases.py step      one mixed step of the benchmark workload (3 nm dot,
+                                          128^3, 16 starts x 16 targets, nCheby 2048: Newton
+                                          filter + Rayleigh-Ritz), the second one inside the
+                                          NVTX range "fbse_timed_steps" (a launch list selects
+                                          it with --nvtx --nvtx-include "fbse_timed_steps/")
+  python tests/profile_cases.py angular   spin / angular statistics of 8 random spinors of the
+                                          3 nm dot, 128^3 (k_ang_sums and the FP64 FFT passes)
 """
 import os
 import sys
@@ -113,10 +120,47 @@ def case_precond(F):
         print(f"precond inference {t1 - t:.3f}s, forward + gradient {time.time() - t1:.3f}s ({n} states)")
 
 
+def case_step(F):
+    import torch
+    dot = _dot(15.0)
+    ctx = _ctx(F, dot, F.MIXED)
+    zn, an, vmin, de, d0 = _filter_setup(F, dot, ctx, 2048, 16)
+    ext = torch.cuda.ExternalStream(ctx.stream_handle)
+    for it in range(2):
+        if it:
+            torch.cuda.nvtx.range_push("fbse_timed_steps")
+        l0 = F.launch_count()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(ext)
+        filt = ctx.newton_filter(zn, an, vmin, de, d0)
+        nk, ev, sg = ctx.ortho_diag_sigma(filt.reshape(256, -1))
+        b.record(ext)
+        b.synchronize()
+        if it:
+            torch.cuda.nvtx.range_pop()
+        print(f"step: {a.elapsed_time(b):.1f} ms, {F.launch_count() - l0} launches, {nk} Ritz pairs")
+
+
+def case_angular(F):
+    import torch
+    dot = _dot(15.0)
+    ctx = _ctx(F, dot, F.FP64)
+    g = dot.grid
+    gen = torch.Generator(device="cuda:0").manual_seed(4)
+    st = torch.randn((8, 4 * g.ngrid), dtype=torch.float64, device="cuda:0", generator=gen)
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t = time.time()
+        ctx.angular_stats(st, *g.axes())
+        print(f"angular statistics of 8 states: {time.time() - t:.3f}s")
+
+
 def main():
     import filterbse_gb300 as F
     F.load()
-    {"rr": case_rr, "filter": case_filter, "bse": case_bse, "precond": case_precond}[sys.argv[1]](F)
+    {"rr": case_rr, "filter": case_filter, "bse": case_bse, "precond": case_precond, "step": case_step,
+     "angular": case_angular}[sys.argv[1]](F)
 
 
 if __name__ == "__main__":

@@ -1,6 +1,7 @@
 """Host logic of the drop-in executables, on the CPU: input.par / conf.par
-parsing, the grid rule, the radial projectors and the projector table
-against the oracle, and the executables' refusal to run without a GPU."""
+parsing, the grid rule, the radial projectors against the oracle, and the
+executables' refusal to run without a GPU (the projector table is built on
+the GPU: tests/test_setup_gpu.py)."""
 import ctypes
 import os
 import shutil
@@ -34,7 +35,7 @@ class FilterParams(ctypes.Structure):
                 ("restart_from_sigma", ctypes.c_int), ("n_states_for_ortho", ctypes.c_long),
                 ("n_states_for_sigma", ctypes.c_long), ("print_cubes", ctypes.c_int), ("ncubes", ctypes.c_long),
                 ("read_coeffs", ctypes.c_int), ("input_psi_filt", ctypes.c_int), ("init_psi_start", ctypes.c_long),
-                ("init_psi_end", ctypes.c_long)]
+                ("init_psi_end", ctypes.c_long), ("calc_spin_ang_stat", ctypes.c_int)]
 
 
 @pytest.fixture(scope="module")
@@ -47,10 +48,6 @@ def lib():
     L.fbse_grid_rule.restype = None
     L.fbse_radial_projectors.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_int, D, I]
-    L.fbse_build_nlc.argtypes = ([ctypes.c_long] * 3 + [D] * 3 + [ctypes.c_long, D, D, D, D, ctypes.c_int,
-                                                                 ctypes.c_double, Lp] +
-                                 [ctypes.POINTER(Lp), ctypes.POINTER(I), ctypes.POINTER(D), ctypes.POINTER(D),
-                                  ctypes.POINTER(D)])
     return L
 
 
@@ -76,9 +73,9 @@ def test_read_filter_params_restarts(lib, tmp_path):
                                     "calcFilterOnly = 0\nsaveCheckpoints = 1\n")
     assert lib.fbse_read_filter_params(str(tmp_path / "a.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
     assert (p.restart_from_ortho, p.n_states_for_ortho, p.print_psi_filt, p.print_psi_diag) == (1, 8, 0, 1)
-    (tmp_path / "e.par").write_text(base + "readCoeffs = 1\nprintCubes = 1 2\n")
+    (tmp_path / "e.par").write_text(base + "readCoeffs = 1\nprintCubes = 1 2\ncalcSpinAngStat = 1\n")
     assert lib.fbse_read_filter_params(str(tmp_path / "e.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
-    assert (p.read_coeffs, p.print_cubes, p.ncubes) == (1, 1, 2)
+    assert (p.read_coeffs, p.print_cubes, p.ncubes, p.calc_spin_ang_stat) == (1, 1, 2, 1)
     (tmp_path / "f.par").write_text(base + "inputPsiFilt = 1 4 20\n")
     assert lib.fbse_read_filter_params(str(tmp_path / "f.par").encode(), ctypes.byref(p), err, 512) == 0, err.value
     assert (p.input_psi_filt, p.init_psi_start, p.init_psi_end) == (1, 4, 20)
@@ -148,32 +145,6 @@ def test_radial_projectors_match_oracle(lib, kind, lam):
         assert np.max(np.abs(s * o[p] - ref[p])) < 1e-10 * np.max(np.abs(ref[p]))
     if kind == 1:
         assert np.array_equal(sg, rs)
-
-
-def test_projector_table_matches_oracle(lib):
-    g = O.Grid(24, 22, 20, 0.5, 0.5, 0.5, -6.0, -5.5, -5.0)
-    rng = np.random.default_rng(4)
-    xyz = np.ascontiguousarray(rng.uniform(-3, 3, (3, 3)))
-    so_par = np.array([0.2, 0.5, 0.9])
-    rc2 = O.r_nlcut2(g.dx)
-    so_tab = np.ascontiguousarray(rng.normal(size=(5, 1024)))
-    nl_tab = np.ascontiguousarray(rng.normal(size=(3, 5, 1024)))
-    sgn = rng.choice([-1, 1], size=(3, 5)).astype(np.int32)
-    ref = O.nlc_table(g, xyz, so_par, so_tab, nl_tab, sgn)
-    gx, gy, gz = (np.ascontiguousarray(a) for a in g.axes())
-    npts = ctypes.c_long()
-    nl, jx, y1, sp, np_ = Lp(), I(), D(), D(), D()
-    assert lib.fbse_build_nlc(g.nx, g.ny, g.nz, gx.ctypes.data_as(D), gy.ctypes.data_as(D), gz.ctypes.data_as(D), 3,
-                              xyz.reshape(-1).ctypes.data_as(D), so_par.ctypes.data_as(D), so_tab.ctypes.data_as(D),
-                              nl_tab.ctypes.data_as(D), 5, rc2, ctypes.byref(npts), ctypes.byref(nl),
-                              ctypes.byref(jx), ctypes.byref(y1), ctypes.byref(sp), ctypes.byref(np_)) == 0
-    assert npts.value == ref.npts
-    n = 3 * ref.npts
-    assert np.array_equal(np.ctypeslib.as_array(nl, (3,)), ref.nl)
-    assert np.array_equal(np.ctypeslib.as_array(jx, (n,)), ref.jxyz)
-    assert np.array_equal(np.ctypeslib.as_array(y1, (n * 6,)), ref.y1)
-    assert np.allclose(np.ctypeslib.as_array(sp, (n * 5,)), ref.proj, rtol=1e-14, atol=1e-14)
-    assert np.allclose(np.ctypeslib.as_array(np_, (n * 5,)), ref.nlp, rtol=1e-14, atol=1e-14)
 
 
 def _cube_text(rho, n, d, lo, atoms):
