@@ -100,7 +100,7 @@ template <typename T, int N> struct PlaneCfg {
   static constexpr int P = Shape<N>::P, Q = Shape<N>::Q;
   static constexpr int PITCH = N + 8;
   static constexpr int THREADS = N * P;
-  static constexpr size_t smem() { return (size_t)(N + N * PITCH) * sizeof(C<T>); }
+  static constexpr size_t smem() { return (size_t)(N + N * PITCH + (N == 128 && sizeof(T) == 4 ? 128 : 0)) * sizeof(C<T>); }
 };
 
 template <typename T, int N>
@@ -136,6 +136,104 @@ __device__ __forceinline__ void row_texchange(C<T> *row, C<T> *v, int t)
   __syncwarp();
 }
 
+// ---------------------------------------------------------------------------
+// FP32 128-point rows as two 64-point transforms (even / odd split), so that
+// each of the 8 threads of a row moves adjacent complex pairs with 16-byte
+// accesses (x[2i], x[2i+1] with i = t + 8 m), half the global instructions
+// of the direct 128-point decomposition.  With w = e^{-2 pi i / 128}:
+//   forward: E, O = 64-point DFTs of x[2i], x[2i+1];
+//            X[k] = E[k] + w^k O[k], X[k + 64] = E[k] - w^k O[k]
+//   inverse: A[k] = X[k] + X[k + 64], B[k] = (X[k] - X[k + 64]) w^-k;
+//            x[2i] = A'[i], x[2i+1] = B'[i] (64-point inverse DFTs)
+// Tables in shared memory: tw64[k1 * 8 + t] = w^{2 t k1}, wk[k] = w^k (k < 64).
+// ---------------------------------------------------------------------------
+template <typename T, int N> struct SplitRows {
+  static constexpr bool on = (N == 128 && sizeof(T) == 4);
+  static constexpr int extra = on ? 128 : 0;  // complex table entries
+};
+
+__device__ __forceinline__ void load_split_tables(float2 *tw64, float2 *wk, const float2 *__restrict__ roots)
+{
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+    tw64[i] = roots[(2 * (i % 8) * (i / 8)) % 128];
+    wk[i] = roots[i];
+  }
+}
+
+// forward row: xin = the row in global memory, row = its shared slots; X in
+// natural order into row[0, 128)
+__device__ __forceinline__ void row128_fwd(const float2 *__restrict__ xin, float2 *row, int t, const float2 *tw64,
+                                          const float2 *wk)
+{
+  float2 e[8], o[8];
+  const float4 *src = reinterpret_cast<const float4 *>(xin);
+#pragma unroll
+  for (int m = 0; m < 8; m++) {
+    const float4 q = src[t + 8 * m];
+    e[m] = make_float2(q.x, q.y);
+    o[m] = make_float2(q.z, q.w);
+  }
+  inner_q<float, 64, false>(e, t, tw64);
+  inner_q<float, 64, false>(o, t, tw64);
+  row_exchange<float, 64>(row, e, t);
+  row_exchange<float, 64>(row + 64, o, t);
+  outer_p<float, 64, false>(e);
+  outer_p<float, 64, false>(o);
+#pragma unroll
+  for (int k2 = 0; k2 < 8; k2++) {
+    const int k = t + 8 * k2;
+    const float2 wo = cmul<float>(o[k2], wk[k]);
+    row[k] = cadd<float>(e[k2], wo);
+    row[k + 64] = csub<float>(e[k2], wo);
+  }
+}
+
+// inverse row from row[0, 128) (natural order): a[k2] = x[2 i], b[k2] =
+// x[2 i + 1] with i = t + 8 k2 (the row's shared slots are reused)
+__device__ __forceinline__ void row128_inv(float2 *row, int t, const float2 *tw64, const float2 *wk, float2 *a,
+                                          float2 *b)
+{
+#pragma unroll
+  for (int m = 0; m < 8; m++) {
+    const int k = t + 8 * m;
+    const float2 x0 = row[k], x1 = row[k + 64];
+    a[m] = cadd<float>(x0, x1);
+    b[m] = cmulc<float>(csub<float>(x0, x1), wk[k], true);
+  }
+  __syncwarp();
+  inner_q<float, 64, true>(a, t, tw64);
+  inner_q<float, 64, true>(b, t, tw64);
+  row_exchange<float, 64>(row, a, t);
+  row_exchange<float, 64>(row + 64, b, t);
+  outer_p<float, 64, true>(a);
+  outer_p<float, 64, true>(b);
+}
+
+// out[2i, 2i+1] = ca (x + V phi) + cb phi for the pairs of a row (16-byte
+// accesses; V as float2 pairs)
+__device__ __forceinline__ void row128_epilogue(const float2 *a, const float2 *b, int t,
+                                               const float2 *__restrict__ phi, const float *__restrict__ pot,
+                                               float2 *__restrict__ out, float ca, float cb)
+{
+  const float4 *ph4 = reinterpret_cast<const float4 *>(phi);
+  const float2 *v2 = reinterpret_cast<const float2 *>(pot);
+  float4 *o4 = reinterpret_cast<float4 *>(out);
+#pragma unroll
+  for (int k2 = 0; k2 < 8; k2++) {
+    const int i = t + 8 * k2;
+    const float4 ph = ph4[i];
+    float2 r0 = a[k2], r1 = b[k2];
+    if (pot) {
+      const float2 V = v2[i];
+      r0.x += V.x * ph.x;
+      r0.y += V.x * ph.y;
+      r1.x += V.y * ph.z;
+      r1.y += V.y * ph.w;
+    }
+    o4[i] = make_float4(ca * r0.x + cb * ph.x, ca * r0.y + cb * ph.y, ca * r1.x + cb * ph.z, ca * r1.y + cb * ph.w);
+  }
+}
+
 template <typename T, int N, int MODE>
 __global__ void __launch_bounds__(PlaneCfg<T, N>::THREADS, 1)
     k_plane_fast(const C<T> *__restrict__ in, C<T> *__restrict__ out, const C<T> *__restrict__ roots,
@@ -146,7 +244,10 @@ __global__ void __launch_bounds__(PlaneCfg<T, N>::THREADS, 1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C<T> *tw2 = reinterpret_cast<C<T> *>(smem_raw);
   C<T> *S = tw2 + N;
+  constexpr bool SPLIT = SplitRows<T, N>::on;
+  C<T> *tws = S + N * PITCH;  // SPLIT: tw64[64], wk[64]
   load_tw2<T, N>(tw2, roots);
+  if constexpr (SPLIT) load_split_tables(tws, tws + 64, roots);
   const long base = (long)blockIdx.x * N * N;
   const int rr = threadIdx.x / P, rt = threadIdx.x % P;  // row phase: row, thread in row
   const int cw = threadIdx.x >> 5;
@@ -155,16 +256,20 @@ __global__ void __launch_bounds__(PlaneCfg<T, N>::THREADS, 1)
   __syncthreads();
   if (MODE == 0) {
     // rows, forward
-#pragma unroll
-    for (int m = 0; m < Q; m++) v[m] = in[base + (long)rr * N + rt + P * m];
-    inner_q<T, N, false>(v, rt, tw2);
     C<T> *row = S + rr * PITCH;
-    row_exchange<T, N>(row, v, rt);
-    outer_p<T, N, false>(v);
+    if constexpr (SPLIT) {
+      row128_fwd(in + base + (long)rr * N, row, rt, tws, tws + 64);
+    } else {
 #pragma unroll
-    for (int j = 0; j < Q / P; j++)
+      for (int m = 0; m < Q; m++) v[m] = in[base + (long)rr * N + rt + P * m];
+      inner_q<T, N, false>(v, rt, tw2);
+      row_exchange<T, N>(row, v, rt);
+      outer_p<T, N, false>(v);
 #pragma unroll
-      for (int k2 = 0; k2 < P; k2++) row[rt + P * j + Q * k2] = v[j * P + k2];
+      for (int j = 0; j < Q / P; j++)
+#pragma unroll
+        for (int k2 = 0; k2 < P; k2++) row[rt + P * j + Q * k2] = v[j * P + k2];
+    }
     __syncthreads();
     // columns, forward
 #pragma unroll
@@ -206,27 +311,34 @@ __global__ void __launch_bounds__(PlaneCfg<T, N>::THREADS, 1)
     // modulo gives its offset in the potential)
     const long pbase = base % ngrid;
     C<T> *row = S + rr * PITCH;
+    if constexpr (SPLIT) {
+      C<T> a[8], b[8];
+      row128_inv(row, rt, tws, tws + 64, a, b);
+      const long o = (long)rr * N;
+      row128_epilogue(a, b, rt, phi + base + o, pot ? pot + pbase + o : nullptr, out + base + o, ca, cb);
+    } else {
 #pragma unroll
-    for (int m = 0; m < Q; m++) v[m] = row[rt + P * m];
-    __syncwarp();
-    inner_q<T, N, true>(v, rt, tw2);
-    row_exchange<T, N>(row, v, rt);
-    outer_p<T, N, true>(v);
+      for (int m = 0; m < Q; m++) v[m] = row[rt + P * m];
+      __syncwarp();
+      inner_q<T, N, true>(v, rt, tw2);
+      row_exchange<T, N>(row, v, rt);
+      outer_p<T, N, true>(v);
 #pragma unroll
-    for (int j = 0; j < Q / P; j++)
+      for (int j = 0; j < Q / P; j++)
 #pragma unroll
-      for (int k2 = 0; k2 < P; k2++) {
-        const long o = (long)rr * N + rt + P * j + Q * k2;
-        const long g = base + o;
-        C<T> r = v[j * P + k2];
-        const C<T> ph = phi[g];
-        if (pot) {
-          const T V = pot[pbase + o];
-          r.x += V * ph.x;
-          r.y += V * ph.y;
+        for (int k2 = 0; k2 < P; k2++) {
+          const long o = (long)rr * N + rt + P * j + Q * k2;
+          const long g = base + o;
+          C<T> r = v[j * P + k2];
+          const C<T> ph = phi[g];
+          if (pot) {
+            const T V = pot[pbase + o];
+            r.x += V * ph.x;
+            r.y += V * ph.y;
+          }
+          out[g] = mk<T>(ca * r.x + cb * ph.x, ca * r.y + cb * ph.y);
         }
-        out[g] = mk<T>(ca * r.x + cb * ph.x, ca * r.y + cb * ph.y);
-      }
+    }
   }
 }
 
@@ -399,7 +511,7 @@ template <typename T, int N> struct ClCfg {
   static constexpr int PITCH = N + 8;
   static constexpr int THREADS = HR * P;           // row phase: P threads per row
   static constexpr int CW = HR;                    // columns per CTA
-  static constexpr size_t smem() { return (size_t)(N + HR * PITCH) * sizeof(C<T>); }
+  static constexpr size_t smem() { return (size_t)(N + HR * PITCH + SplitRows<T, N>::extra) * sizeof(C<T>); }
 };
 
 template <typename T, int N, int MODE>
@@ -418,7 +530,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(ClCfg<T, N>::THREADS
   C<T> *const Hp = cluster.map_shared_rank(H, 1 - q);
   C<T> *const H0 = q == 0 ? H : Hp;  // rows [0, N/2)
   C<T> *const H1 = q == 0 ? Hp : H;  // rows [N/2, N)
+  constexpr bool SPLIT = SplitRows<T, N>::on;
+  C<T> *tws = H + HR * PITCH;  // SPLIT: tw64[64], wk[64]
   load_tw2<T, N>(tw2, roots);
+  if constexpr (SPLIT) load_split_tables(tws, tws + 64, roots);
   const long base = (long)(blockIdx.x / 2) * N * N;
   const int rr = threadIdx.x / P, rt = threadIdx.x % P;        // row phase: local row, thread in row
   const int cw = threadIdx.x >> 5;
@@ -429,16 +544,20 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(ClCfg<T, N>::THREADS
   if (MODE == 0) {
     // rows N/2 q + rr, forward
     const long rbase = base + (long)((int)q * HR + rr) * N;
-#pragma unroll
-    for (int m = 0; m < Q; m++) v[m] = in[rbase + rt + P * m];
-    inner_q<T, N, false>(v, rt, tw2);
     C<T> *row = H + rr * PITCH;
-    row_exchange<T, N>(row, v, rt);
-    outer_p<T, N, false>(v);
+    if constexpr (SPLIT) {
+      row128_fwd(in + rbase, row, rt, tws, tws + 64);
+    } else {
 #pragma unroll
-    for (int j = 0; j < Q / P; j++)
+      for (int m = 0; m < Q; m++) v[m] = in[rbase + rt + P * m];
+      inner_q<T, N, false>(v, rt, tw2);
+      row_exchange<T, N>(row, v, rt);
+      outer_p<T, N, false>(v);
 #pragma unroll
-      for (int k2 = 0; k2 < P; k2++) row[rt + P * j + Q * k2] = v[j * P + k2];
+      for (int j = 0; j < Q / P; j++)
+#pragma unroll
+        for (int k2 = 0; k2 < P; k2++) row[rt + P * j + Q * k2] = v[j * P + k2];
+    }
     cluster.sync();
     // columns, forward: rows R = ct + P m from the CTA that holds them
 #pragma unroll
@@ -486,27 +605,33 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(ClCfg<T, N>::THREADS
     const long o0 = (long)((int)q * HR + rr) * N;
     const long pbase = base % ngrid;
     C<T> *row = H + rr * PITCH;
+    if constexpr (SPLIT) {
+      C<T> a[8], b[8];
+      row128_inv(row, rt, tws, tws + 64, a, b);
+      row128_epilogue(a, b, rt, phi + base + o0, pot ? pot + pbase + o0 : nullptr, out + base + o0, ca, cb);
+    } else {
 #pragma unroll
-    for (int m = 0; m < Q; m++) v[m] = row[rt + P * m];
-    __syncwarp();
-    inner_q<T, N, true>(v, rt, tw2);
-    row_exchange<T, N>(row, v, rt);
-    outer_p<T, N, true>(v);
+      for (int m = 0; m < Q; m++) v[m] = row[rt + P * m];
+      __syncwarp();
+      inner_q<T, N, true>(v, rt, tw2);
+      row_exchange<T, N>(row, v, rt);
+      outer_p<T, N, true>(v);
 #pragma unroll
-    for (int j = 0; j < Q / P; j++)
+      for (int j = 0; j < Q / P; j++)
 #pragma unroll
-      for (int k2 = 0; k2 < P; k2++) {
-        const long o = o0 + rt + P * j + Q * k2;
-        const long g = base + o;
-        C<T> r = v[j * P + k2];
-        const C<T> ph = phi[g];
-        if (pot) {
-          const T V = pot[pbase + o];
-          r.x += V * ph.x;
-          r.y += V * ph.y;
+        for (int k2 = 0; k2 < P; k2++) {
+          const long o = o0 + rt + P * j + Q * k2;
+          const long g = base + o;
+          C<T> r = v[j * P + k2];
+          const C<T> ph = phi[g];
+          if (pot) {
+            const T V = pot[pbase + o];
+            r.x += V * ph.x;
+            r.y += V * ph.y;
+          }
+          out[g] = mk<T>(ca * r.x + cb * ph.x, ca * r.y + cb * ph.y);
         }
-        out[g] = mk<T>(ca * r.x + cb * ph.x, ca * r.y + cb * ph.y);
-      }
+    }
   }
 }
 

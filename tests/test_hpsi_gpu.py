@@ -155,3 +155,20 @@ def test_autotuner_choices_are_bit_identical(fbse, cuda, precision):
         assert np.array_equal(_run_hpsi(fbse, ctx, psis, cuda), auto), fixed
     with pytest.raises(fbse.FbseError):
         ctx.set_tuning(scatter_states=3)
+
+
+@pytest.mark.parametrize("shape,precision", [((128, 128, 64), 1), ((64, 64, 64), 0), ((64, 64, 256), 1)])
+def test_plane_variants_are_bit_identical(fbse, cuda, shape, precision):
+    """The one-CTA and the two-CTA-cluster plane kernels run the same
+    arithmetic (the FP32 128-point rows as two 64-point transforms in both):
+    H psi is bit-identical between them and matches the oracle."""
+    sysm = tiny_cluster(*shape, natoms=8, nspin=2, is_complex=True, so=True, nl=True)
+    psis = random_states(3, sysm, np.random.default_rng(8))
+    ctx = _ctx(fbse, sysm, precision)
+    outs = []
+    for var in (0, 1):
+        ctx.set_tuning(fft_plane_cluster=var)
+        outs.append(_run_hpsi(fbse, ctx, psis, cuda))
+    assert np.array_equal(outs[0], outs[1])
+    want = np.array([O.hamiltonian(p, sysm) for p in psis])
+    assert _relerr(outs[0], want) < TOL[precision]
