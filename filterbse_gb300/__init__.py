@@ -78,7 +78,7 @@ class Tuning(ctypes.Structure):
                 ("fft_chunk_blocks", ctypes.c_long), ("scatter_states", ctypes.c_int),
                 ("gather_points", ctypes.c_int), ("newton_ring", ctypes.c_int), ("bse_simt", ctypes.c_int),
                 ("tc_image_bytes", ctypes.c_double), ("ritz_cut", ctypes.c_double), ("ritz_hpsi", ctypes.c_int),
-                ("hpsi_fused", ctypes.c_int)]
+                ("hpsi_fused", ctypes.c_int), ("hpsi_streams", ctypes.c_int)]
 
 
 _lib = None

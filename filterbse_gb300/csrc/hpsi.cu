@@ -521,14 +521,12 @@ static void launch_scatter(fbse_ctx *c, C<T> *out, const C<T> *coef, const PtVie
     k_proj_scatter<T, false, true, kG><<<gs, 256, 0, c->stream>>>(out, coef, pt, p.nat, nstates, c->ngrid, c->nspin, sc);
 }
 
-// out += scale * (V_SO + V_NL) in for nstates states.  scratch (optional,
-// nstates states): where the autotuner may time scatter candidates; without
-// it the scatter runs its default shape until a call that has scratch.
+// the gather half of proj_apply: the projector coefficients of in into the
+// context's coefficient buffer, on the context's stream
 template <typename T>
-int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scale, C<T> *scratch)
+static int proj_gather(fbse_ctx *c, const C<T> *in, long nstates)
 {
   const ProjDev &p = c->proj;
-  if (!(c->so || c->nl) || p.nat == 0) return FBSE_OK;
   const size_t need = (size_t)nstates * p.nat * 2 * kNC * sizeof(C<T>);
   int rc = ensure(c, &c->coef, &c->coef_bytes, need);
   if (rc) return rc;
@@ -544,8 +542,8 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   const std::string prob = std::string(sizeof(T) == 4 ? "fp32" : "fp64") + " states=" + std::to_string(nstates) +
                            " atoms=" + std::to_string(p.nat) + " points=" + std::to_string(p.ncov) +
                            (c->so ? " SO" : "") + (c->nl ? " NL" : "");
-  // gather: points per lane per iteration (the same sums in the same order for
-  // every choice); the gather writes only coef, so candidates run in place
+  // points per lane per iteration (the same sums in the same order for every
+  // choice); the gather writes only coef, so candidates run in place
   long gu = c->tune.gather_points;
   auto gather = [&](long v) -> int {
     if (v == 1) launch_gather<T, 1>(c, gg, in, coef, pv, nstates, ch0);
@@ -556,11 +554,27 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   if (gu == 0 && (rc = autotune(c, "projector gather points per lane", prob, {1, 2, 4}, gather, &gu))) return rc;
   if ((rc = gather(gu))) return rc;
   FBSE_COUNT(1);
+  return FBSE_OK;
+}
+
+// the scatter half: out += scale * (projector terms of the gathered
+// coefficients).  scratch (optional, nstates states): where the autotuner may
+// time scatter candidates; without it the scatter runs its default shape
+// until a call that has scratch.
+template <typename T>
+static int proj_scatter(fbse_ctx *c, C<T> *out, long nstates, double scale, C<T> *scratch)
+{
+  const ProjDev &p = c->proj;
   if (p.ncov == 0) return FBSE_OK;
+  int rc;
+  const C<T> *coef = reinterpret_cast<const C<T> *>(c->coef);
+  const std::string prob = std::string(sizeof(T) == 4 ? "fp32" : "fp64") + " states=" + std::to_string(nstates) +
+                           " atoms=" + std::to_string(p.nat) + " points=" + std::to_string(p.ncov) +
+                           (c->so ? " SO" : "") + (c->nl ? " NL" : "");
   const PtView<T> pt = ptview<T>(c);
   const T sc = (T)scale;
-  // scatter: v = 1, 2, 4, 8: one thread per point and v states; v = 16 + g:
-  // one CTA per chunk of points, all states in groups of g with the chunk's
+  // v = 1, 2, 4, 8: one thread per point and v states; v = 16 + g: one CTA
+  // per chunk of points, all states in groups of g with the chunk's
   // coefficients in shared memory.  Each (state, point) is summed in the same
   // order for every choice; candidates are timed on the scratch states
   long kg = c->tune.scatter_states;
@@ -588,6 +602,17 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   return FBSE_OK;
 }
 
+static bool has_proj(fbse_ctx *c) { return (c->so || c->nl) && c->proj.nat > 0; }
+
+// out += scale * (V_SO + V_NL) in for nstates states
+template <typename T>
+int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scale, C<T> *scratch)
+{
+  if (!has_proj(c)) return FBSE_OK;
+  int rc = proj_gather<T>(c, in, nstates);
+  return rc ? rc : proj_scatter<T>(c, out, nstates, scale, scratch);
+}
+
 template <typename T>
 int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, double b)
 {
@@ -598,7 +623,30 @@ int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, d
   int rc = ensure(c, &c->wk, &c->wk_bytes, need);
   if (rc) return rc;
   C<T> *wk = reinterpret_cast<C<T> *>(c->wk);
-  if ((rc = kinetic_apply<T>(c, in, out, wk, nstates * c->nspin, a, b, 1))) return rc;
+  const long nblk = nstates * c->nspin;
+  // the gather reads only in and writes only the coefficients: with in and out
+  // apart it runs on the side stream while the FFT passes run on the main one
+  const char *i0 = reinterpret_cast<const char *>(in), *o0 = reinterpret_cast<const char *>(out);
+  const bool apart = i0 + need <= o0 || o0 + need <= i0;
+  if (has_proj(c) && apart && c->tune.hpsi_streams == 0 && c->side) {
+    // the coefficient buffer is sized here, on the main stream, so that the
+    // side stream never reallocates it under a scatter still in flight
+    if ((rc = ensure(c, &c->coef, &c->coef_bytes, (size_t)nstates * c->proj.nat * 2 * kNC * sizeof(C<T>))))
+      return rc;
+    FBSE_CUDA(c, cudaEventRecord(c->ev_fork, c->stream));
+    FBSE_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+    // (a first call's autotuner times the gather candidates on the side stream)
+    cudaStream_t main = c->stream;
+    c->stream = c->side;
+    rc = proj_gather<T>(c, in, nstates);
+    c->stream = main;
+    if (rc) return rc;
+    FBSE_CUDA(c, cudaEventRecord(c->ev_join, c->side));
+    if ((rc = kinetic_apply<T>(c, in, out, wk, nblk, a, b, 1))) return rc;
+    FBSE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    return proj_scatter<T>(c, out, nstates, a, wk);
+  }
+  if ((rc = kinetic_apply<T>(c, in, out, wk, nblk, a, b, 1))) return rc;
   // the FFT scratch is free again: the scatter's autotuner may time on it
   return proj_apply<T>(c, in, out, nstates, a, wk);
 }

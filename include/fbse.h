@@ -137,6 +137,9 @@ typedef struct fbse_tuning {
                               fused into the xy plane passes (slower than the separate projector
                               kernels on the measured workloads); 0: separate projector kernels.
                               Results differ in rounding only */
+  int hpsi_streams;        /* 0: the projector gather of H psi runs on a second stream of the context
+                              beside the FFT passes (when input and output do not overlap); 1: every
+                              kernel on the context's stream.  Same results */
 } fbse_tuning;
 int fbse_get_tuning(fbse_ctx *ctx, fbse_tuning *t);
 int fbse_set_tuning(fbse_ctx *ctx, const fbse_tuning *t);

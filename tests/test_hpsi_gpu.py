@@ -172,3 +172,18 @@ def test_plane_variants_are_bit_identical(fbse, cuda, shape, precision):
     assert np.array_equal(outs[0], outs[1])
     want = np.array([O.hamiltonian(p, sysm) for p in psis])
     assert _relerr(outs[0], want) < TOL[precision]
+
+
+@pytest.mark.parametrize("shape,precision", [((128, 128, 64), 1), ((20, 18, 21), 0)])
+def test_side_stream_gather_is_bit_identical(fbse, cuda, shape, precision):
+    """The projector gather on the context's second stream, beside the FFT
+    passes, gives the same bits as the one-stream order, call after call."""
+    sysm = tiny_cluster(*shape, natoms=10, nspin=2, is_complex=True, so=True, nl=True)
+    psis = random_states(4, sysm, np.random.default_rng(9))
+    ctx = _ctx(fbse, sysm, precision)
+    two = [_run_hpsi(fbse, ctx, psis, cuda) for _ in range(2)]
+    ctx.set_tuning(hpsi_streams=1)
+    one = _run_hpsi(fbse, ctx, psis, cuda)
+    assert np.array_equal(two[0], one) and np.array_equal(two[1], one)
+    want = np.array([O.hamiltonian(p, sysm) for p in psis])
+    assert _relerr(one, want) < TOL[precision]
