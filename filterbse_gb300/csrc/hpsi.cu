@@ -524,13 +524,14 @@ static void launch_scatter(fbse_ctx *c, C<T> *out, const C<T> *coef, const PtVie
 // the gather half of proj_apply: the projector coefficients of in into the
 // context's coefficient buffer, on the context's stream
 template <typename T>
-static int proj_gather(fbse_ctx *c, const C<T> *in, long nstates)
+static int proj_gather(fbse_ctx *c, const C<T> *in, long nstates, long st0 = 0)
 {
+  // st0: the states' offset in the coefficient buffer (sized for st0 + nstates)
   const ProjDev &p = c->proj;
-  const size_t need = (size_t)nstates * p.nat * 2 * kNC * sizeof(C<T>);
+  const size_t need = (size_t)(st0 + nstates) * p.nat * 2 * kNC * sizeof(C<T>);
   int rc = ensure(c, &c->coef, &c->coef_bytes, need);
   if (rc) return rc;
-  C<T> *coef = reinterpret_cast<C<T> *>(c->coef);
+  C<T> *coef = reinterpret_cast<C<T> *>(c->coef) + st0 * p.nat * 2 * kNC;
   const long spc = kSW / c->nspin;
   const long ggroups = (nstates + spc - 1) / spc;
   if (ggroups > 65535 || p.nat > 2147483647L || nstates > 65535)
@@ -562,12 +563,12 @@ static int proj_gather(fbse_ctx *c, const C<T> *in, long nstates)
 // time scatter candidates; without it the scatter runs its default shape
 // until a call that has scratch.
 template <typename T>
-static int proj_scatter(fbse_ctx *c, C<T> *out, long nstates, double scale, C<T> *scratch)
+static int proj_scatter(fbse_ctx *c, C<T> *out, long nstates, double scale, C<T> *scratch, long st0 = 0)
 {
   const ProjDev &p = c->proj;
   if (p.ncov == 0) return FBSE_OK;
   int rc;
-  const C<T> *coef = reinterpret_cast<const C<T> *>(c->coef);
+  const C<T> *coef = reinterpret_cast<const C<T> *>(c->coef) + st0 * p.nat * 2 * kNC;
   const std::string prob = std::string(sizeof(T) == 4 ? "fp32" : "fp64") + " states=" + std::to_string(nstates) +
                            " atoms=" + std::to_string(p.nat) + " points=" + std::to_string(p.ncov) +
                            (c->so ? " SO" : "") + (c->nl ? " NL" : "");
@@ -613,6 +614,17 @@ int proj_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double scal
   return rc ? rc : proj_scatter<T>(c, out, nstates, scale, scratch);
 }
 
+// one part of a split H psi: gather, FFT passes, scatter of nstates states
+// whose coefficients sit at state offset st0, on the context's current stream
+template <typename T>
+static int hpsi_part(fbse_ctx *c, const C<T> *in, C<T> *out, C<T> *wk, long nstates, double a, double b, long st0)
+{
+  int rc = proj_gather<T>(c, in, nstates, st0);
+  if (!rc) rc = kinetic_apply<T>(c, in, out, wk, nstates * c->nspin, a, b, 1);
+  // the FFT scratch is free again: the scatter's autotuner may time on it
+  return rc ? rc : proj_scatter<T>(c, out, nstates, a, wk, st0);
+}
+
 template <typename T>
 int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, double b)
 {
@@ -624,30 +636,33 @@ int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, d
   if (rc) return rc;
   C<T> *wk = reinterpret_cast<C<T> *>(c->wk);
   const long nblk = nstates * c->nspin;
-  // the gather reads only in and writes only the coefficients: with in and out
-  // apart it runs on the side stream while the FFT passes run on the main one
+  // with the projectors on and input and output apart, the batch runs as two
+  // halves on the context's two streams, each gather -> FFT passes ->
+  // scatter, so that one half's projector kernels (latency bound) overlap the
+  // other half's FFT passes (bandwidth bound); every state sees the same
+  // kernels either way
   const char *i0 = reinterpret_cast<const char *>(in), *o0 = reinterpret_cast<const char *>(out);
   const bool apart = i0 + need <= o0 || o0 + need <= i0;
-  if (has_proj(c) && apart && c->tune.hpsi_streams == 0 && c->side) {
-    // the coefficient buffer is sized here, on the main stream, so that the
-    // side stream never reallocates it under a scatter still in flight
+  if (has_proj(c) && apart && nstates >= 2 && c->tune.hpsi_streams == 0 && c->side) {
+    // buffers sized on the main stream: neither half reallocates under the other
     if ((rc = ensure(c, &c->coef, &c->coef_bytes, (size_t)nstates * c->proj.nat * 2 * kNC * sizeof(C<T>))))
       return rc;
+    const long h = nstates / 2;
+    const long off = h * c->nspin * c->ngrid;
     FBSE_CUDA(c, cudaEventRecord(c->ev_fork, c->stream));
     FBSE_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-    // (a first call's autotuner times the gather candidates on the side stream)
+    // (a first call's autotuners time their candidates on the stream of the part they serve)
     cudaStream_t main = c->stream;
     c->stream = c->side;
-    rc = proj_gather<T>(c, in, nstates);
+    rc = hpsi_part<T>(c, in + off, out + off, wk + off, nstates - h, a, b, h);
     c->stream = main;
     if (rc) return rc;
     FBSE_CUDA(c, cudaEventRecord(c->ev_join, c->side));
-    if ((rc = kinetic_apply<T>(c, in, out, wk, nblk, a, b, 1))) return rc;
+    if ((rc = hpsi_part<T>(c, in, out, wk, h, a, b, 0))) return rc;
     FBSE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
-    return proj_scatter<T>(c, out, nstates, a, wk);
+    return FBSE_OK;
   }
   if ((rc = kinetic_apply<T>(c, in, out, wk, nblk, a, b, 1))) return rc;
-  // the FFT scratch is free again: the scatter's autotuner may time on it
   return proj_apply<T>(c, in, out, nstates, a, wk);
 }
 

@@ -137,9 +137,10 @@ typedef struct fbse_tuning {
                               fused into the xy plane passes (slower than the separate projector
                               kernels on the measured workloads); 0: separate projector kernels.
                               Results differ in rounding only */
-  int hpsi_streams;        /* 0: the projector gather of H psi runs on a second stream of the context
-                              beside the FFT passes (when input and output do not overlap); 1: every
-                              kernel on the context's stream.  Same results */
+  int hpsi_streams;        /* 0: an H psi batch of two or more states with projectors runs as two halves
+                              on the context's two streams (when input and output do not overlap), so
+                              that one half's projector kernels overlap the other's FFT passes; 1: the
+                              whole batch on the context's stream.  Same results */
 } fbse_tuning;
 int fbse_get_tuning(fbse_ctx *ctx, fbse_tuning *t);
 int fbse_set_tuning(fbse_ctx *ctx, const fbse_tuning *t);

@@ -175,11 +175,11 @@ def test_plane_variants_are_bit_identical(fbse, cuda, shape, precision):
 
 
 @pytest.mark.parametrize("shape,precision", [((128, 128, 64), 1), ((20, 18, 21), 0)])
-def test_side_stream_gather_is_bit_identical(fbse, cuda, shape, precision):
-    """The projector gather on the context's second stream, beside the FFT
-    passes, gives the same bits as the one-stream order, call after call."""
+def test_two_stream_halves_are_bit_identical(fbse, cuda, shape, precision):
+    """H psi as two halves of the batch on the context's two streams gives
+    the same bits as the whole batch on one stream, call after call."""
     sysm = tiny_cluster(*shape, natoms=10, nspin=2, is_complex=True, so=True, nl=True)
-    psis = random_states(4, sysm, np.random.default_rng(9))
+    psis = random_states(5, sysm, np.random.default_rng(9))
     ctx = _ctx(fbse, sysm, precision)
     two = [_run_hpsi(fbse, ctx, psis, cuda) for _ in range(2)]
     ctx.set_tuning(hpsi_streams=1)
