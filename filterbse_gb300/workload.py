@@ -260,14 +260,31 @@ def cdse_dot(radius_ang: float, d: float = 0.5, ke_max: float = 20.0, spinor: bo
     return Dot(types, coords, grid, pot, proj, 2 if spinor else 1, spinor, spinor, False)
 
 
+def smooth_size(n: int) -> int:
+    """The smallest m >= n whose prime factors are all at most 7 (the radices
+    the FFT kernels keep in registers)."""
+    m = n
+    while True:
+        r = m
+        for p in (2, 3, 5, 7):
+            while r % p == 0:
+                r //= p
+        if r == 1:
+            return m
+        m += 1
+
+
 def uneven_dots(n: int = 24, seed: int = 20261206, d_min_nm: float = 2.0, d_max_nm: float = 4.0, d: float = 0.5,
-                ke_max: float = 10.0, max_grid: int = 160):
+                ke_max: float = 10.0, max_grid: int = 160, smooth: bool = True):
     """The multi-dot workload: n passivated zincblende dots, CdSe and InP
     alternating, diameters uniform in [d_min_nm, d_max_nm] from a seeded
     generator, each on its own grid by the reference's grid rule (capped at
     max_grid points per axis, a recorded choice: the rule gives 104^3-190^3 for
-    2-4 nm, the stated workload 64^3-160^3).  Returns [(material, diameter_nm,
-    Dot)]."""
+    2-4 nm, the stated workload 64^3-160^3).  smooth: each axis grows to the
+    next size with prime factors <= 7 (the rule's size is a minimum; the rule
+    gives sizes such as 116 = 4 x 29 and 148 = 4 x 37, whose large prime radix
+    takes the slow direct-DFT pass; the extra points are vacuum), a recorded
+    choice.  Returns [(material, diameter_nm, Dot)]."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
@@ -279,6 +296,10 @@ def uneven_dots(n: int = 24, seed: int = 20261206, d_min_nm: float = 2.0, d_max_
         if max(g.nx, g.ny, g.nz) > max_grid:
             n_ = max_grid
             g = Grid(n_, n_, n_, d, d, d, -n_ * d / 2, -n_ * d / 2, -n_ * d / 2, ke_max)
+        elif smooth:
+            ns_ = [smooth_size(v) for v in (g.nx, g.ny, g.nz)]
+            if ns_ != [g.nx, g.ny, g.nz]:
+                g = reference_grid(coords, d, ke_max, n_in=tuple(ns_))
         pot = local_pot(g, types, coords, pdir)
         core = [k for k, t in enumerate(types) if not t.startswith("P")]
         tab = so_radial(d, np.sqrt(r_nlcut2(d)))
