@@ -233,9 +233,11 @@ static int create(fbse_ctx *c, const fbse_grid_desc *g, const double *pot, const
   const double ng_1 = nx_1 * ny_1 * nz_1;
   c->kemax_scaled = g->ke_max * (ny_1 * nx_1 * nz_1);
   FBSE_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  FBSE_CUDA(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
   FBSE_CUDA(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
-  FBSE_CUDA(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+  for (int k = 0; k < fbse_ctx::kSide; k++) {
+    FBSE_CUDA(c, cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking));
+    FBSE_CUDA(c, cudaEventCreateWithFlags(&c->ev_join[k], cudaEventDisableTiming));
+  }
   FBSE_CUDA(c, cudaMalloc(&c->dstatus, 4 * sizeof(int)));
   FBSE_CUDA(c, cudaMemset(c->dstatus, 0, 4 * sizeof(int)));
   int rc;
@@ -445,10 +447,12 @@ void fbse_destroy(fbse_ctx *c)
     if (b) cudaFree(b);
   for (void *b : c->cache)
     if (b) cudaFree(b);
-  if (c->side) cudaStreamSynchronize(c->side);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-  if (c->ev_join) cudaEventDestroy(c->ev_join);
-  if (c->side) cudaStreamDestroy(c->side);
+  for (int k = 0; k < fbse_ctx::kSide; k++) {
+    if (c->side[k]) cudaStreamSynchronize(c->side[k]);
+    if (c->ev_join[k]) cudaEventDestroy(c->ev_join[k]);
+    if (c->side[k]) cudaStreamDestroy(c->side[k]);
+  }
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -512,7 +516,7 @@ int fbse_set_tuning(fbse_ctx *c, const fbse_tuning *t)
       !pow2_in(t->gather_points, 4) ||
       (t->newton_ring != 0 && (t->newton_ring < 8 || t->newton_ring > 128)) || t->bse_simt < 0 || t->bse_simt > 1 ||
       !(t->tc_image_bytes >= 0) || !(t->ritz_cut >= 0 && t->ritz_cut < 1) || t->ritz_hpsi < 0 ||
-      t->ritz_hpsi > 2 || t->hpsi_fused < 0 || t->hpsi_fused > 1 || t->hpsi_streams < 0 || t->hpsi_streams > 1)
+      t->ritz_hpsi > 2 || t->hpsi_fused < 0 || t->hpsi_fused > 1 || t->hpsi_streams < 0 || t->hpsi_streams > 4)
     return set_err(c, FBSE_ERR_ARG, "fbse_set_tuning: a field is out of range");
   c->tune = *t;
   c->tuned.clear();  // earlier decisions may rest on the old fixed choices

@@ -133,8 +133,9 @@ struct fbse_ctx {
   double vpot_min = 0, vpot_max = 0;
   fbse::ProjDev proj;
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;             // second stream: the projector gather beside the FFT passes
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  static constexpr int kSide = 3;
+  cudaStream_t side[kSide] = {};           // further streams: parts of an H psi batch beside the first
+  cudaEvent_t ev_fork = nullptr, ev_join[kSide] = {};
   // scratch (grown on demand)
   void *wk = nullptr; size_t wk_bytes = 0;       // FFT work states
   void *coef = nullptr; size_t coef_bytes = 0;   // projector coefficients

@@ -636,30 +636,35 @@ int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, d
   if (rc) return rc;
   C<T> *wk = reinterpret_cast<C<T> *>(c->wk);
   const long nblk = nstates * c->nspin;
-  // with the projectors on and input and output apart, the batch runs as two
-  // halves on the context's two streams, each gather -> FFT passes ->
-  // scatter, so that one half's projector kernels (latency bound) overlap the
-  // other half's FFT passes (bandwidth bound); every state sees the same
-  // kernels either way
+  // with the projectors on and input and output apart, the batch runs as
+  // parts (two by default) on the context's streams, each gather -> FFT
+  // passes -> scatter, so that one part's projector kernels (latency bound)
+  // and tail waves overlap the other parts' kernels; every state sees the
+  // same kernels either way
   const char *i0 = reinterpret_cast<const char *>(in), *o0 = reinterpret_cast<const char *>(out);
   const bool apart = i0 + need <= o0 || o0 + need <= i0;
-  if (has_proj(c) && apart && nstates >= 2 && c->tune.hpsi_streams == 0 && c->side) {
-    // buffers sized on the main stream: neither half reallocates under the other
+  const long parts = std::min<long>(nstates, c->tune.hpsi_streams == 0 ? 2 : c->tune.hpsi_streams);
+  if (has_proj(c) && apart && parts >= 2 && c->side[0]) {
+    // buffers sized on the main stream: no part reallocates under another
     if ((rc = ensure(c, &c->coef, &c->coef_bytes, (size_t)nstates * c->proj.nat * 2 * kNC * sizeof(C<T>))))
       return rc;
-    const long h = nstates / 2;
-    const long off = h * c->nspin * c->ngrid;
     FBSE_CUDA(c, cudaEventRecord(c->ev_fork, c->stream));
-    FBSE_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-    // (a first call's autotuners time their candidates on the stream of the part they serve)
     cudaStream_t main = c->stream;
-    c->stream = c->side;
-    rc = hpsi_part<T>(c, in + off, out + off, wk + off, nstates - h, a, b, h);
-    c->stream = main;
-    if (rc) return rc;
-    FBSE_CUDA(c, cudaEventRecord(c->ev_join, c->side));
-    if ((rc = hpsi_part<T>(c, in, out, wk, h, a, b, 0))) return rc;
-    FBSE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    // parts 1.. on the side streams, part 0 on the context's stream
+    // (a first call's autotuners time their candidates on the stream of the part they serve)
+    for (long k = parts - 1; k >= 0; k--) {
+      const long s0 = nstates * k / parts, s1 = nstates * (k + 1) / parts;
+      const long off = s0 * c->nspin * c->ngrid;
+      if (k > 0) {
+        FBSE_CUDA(c, cudaStreamWaitEvent(c->side[k - 1], c->ev_fork, 0));
+        c->stream = c->side[k - 1];
+      }
+      rc = hpsi_part<T>(c, in + off, out + off, wk + off, s1 - s0, a, b, s0);
+      c->stream = main;
+      if (rc) return rc;
+      if (k > 0) FBSE_CUDA(c, cudaEventRecord(c->ev_join[k - 1], c->side[k - 1]));
+    }
+    for (long k = 1; k < parts; k++) FBSE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_join[k - 1], 0));
     return FBSE_OK;
   }
   if ((rc = kinetic_apply<T>(c, in, out, wk, nblk, a, b, 1))) return rc;

@@ -137,10 +137,10 @@ typedef struct fbse_tuning {
                               fused into the xy plane passes (slower than the separate projector
                               kernels on the measured workloads); 0: separate projector kernels.
                               Results differ in rounding only */
-  int hpsi_streams;        /* 0: an H psi batch of two or more states with projectors runs as two halves
-                              on the context's two streams (when input and output do not overlap), so
-                              that one half's projector kernels overlap the other's FFT passes; 1: the
-                              whole batch on the context's stream.  Same results */
+  int hpsi_streams;        /* parts of an H psi batch with projectors, each on its own stream of the
+                              context (when input and output do not overlap), so that one part's
+                              projector kernels and tail waves overlap the others' kernels: 0 = 2,
+                              1 = the whole batch on the context's stream, 2..4.  Same results */
 } fbse_tuning;
 int fbse_get_tuning(fbse_ctx *ctx, fbse_tuning *t);
 int fbse_set_tuning(fbse_ctx *ctx, const fbse_tuning *t);

@@ -175,9 +175,9 @@ def test_plane_variants_are_bit_identical(fbse, cuda, shape, precision):
 
 
 @pytest.mark.parametrize("shape,precision", [((128, 128, 64), 1), ((20, 18, 21), 0)])
-def test_two_stream_halves_are_bit_identical(fbse, cuda, shape, precision):
-    """H psi as two halves of the batch on the context's two streams gives
-    the same bits as the whole batch on one stream, call after call."""
+def test_stream_parts_are_bit_identical(fbse, cuda, shape, precision):
+    """H psi as 2, 3 or 4 parts of the batch on the context's streams gives the
+    same bits as the whole batch on one stream, call after call."""
     sysm = tiny_cluster(*shape, natoms=10, nspin=2, is_complex=True, so=True, nl=True)
     psis = random_states(5, sysm, np.random.default_rng(9))
     ctx = _ctx(fbse, sysm, precision)
@@ -185,5 +185,8 @@ def test_two_stream_halves_are_bit_identical(fbse, cuda, shape, precision):
     ctx.set_tuning(hpsi_streams=1)
     one = _run_hpsi(fbse, ctx, psis, cuda)
     assert np.array_equal(two[0], one) and np.array_equal(two[1], one)
+    for parts in (3, 4):
+        ctx.set_tuning(hpsi_streams=parts)
+        assert np.array_equal(_run_hpsi(fbse, ctx, psis, cuda), one), parts
     want = np.array([O.hamiltonian(p, sysm) for p in psis])
     assert _relerr(one, want) < TOL[precision]
