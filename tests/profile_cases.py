@@ -23,6 +23,8 @@ the built library.
                                           it with --nvtx --nvtx-include "fbse_timed_steps/")
   python tests/profile_cases.py angular   spin / angular statistics of 8 random spinors of the
                                           3 nm dot, 128^3 (k_ang_sums and the FP64 FFT passes)
+  python tests/profile_cases.py setup     local potential and projector table of the 3 nm dot,
+                                          128^3 (k_local_pot, k_nlc_count, k_nlc_fill)
 """
 import os
 import sys
@@ -156,11 +158,18 @@ def case_angular(F):
         print(f"angular statistics of 8 states: {time.time() - t:.3f}s")
 
 
+def case_setup(F):
+    for _ in range(2):
+        t = time.time()
+        dot = _dot(15.0)  # builds the local potential and the projector table on the GPU
+        print(f"setup of the 3 nm dot: {time.time() - t:.3f}s, {int(np.sum(dot.proj.nl))} table entries")
+
+
 def main():
     import filterbse_gb300 as F
     F.load()
     {"rr": case_rr, "filter": case_filter, "bse": case_bse, "precond": case_precond, "step": case_step,
-     "angular": case_angular}[sys.argv[1]](F)
+     "angular": case_angular, "setup": case_setup}[sys.argv[1]](F)
 
 
 if __name__ == "__main__":
