@@ -661,7 +661,11 @@ int hpsi_apply(fbse_ctx *c, const C<T> *in, C<T> *out, long nstates, double a, d
       }
       rc = hpsi_part<T>(c, in + off, out + off, wk + off, s1 - s0, a, b, s0);
       c->stream = main;
-      if (rc) return rc;
+      if (rc) {
+        // parts already enqueued finish before the caller may free or reuse buffers
+        for (int q = 0; q < fbse_ctx::kSide; q++) cudaStreamSynchronize(c->side[q]);
+        return rc;
+      }
       if (k > 0) FBSE_CUDA(c, cudaEventRecord(c->ev_join[k - 1], c->side[k - 1]));
     }
     for (long k = 1; k < parts; k++) FBSE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_join[k - 1], 0));
