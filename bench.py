@@ -395,6 +395,16 @@ def learned_leg(args, F, W, dot, g, cmx, zn_an, d_starts, stlen, fp64, log):
     return out
 
 
+def _oracle_table(W, O, og, core_coords):
+    """The projector table of the CPU legs, built by the oracle on the host
+    (the same table as the library's GPU builder): spin-orbit channels of the
+    workload (SO_par 0.01, no NL)."""
+    n = len(core_coords)
+    tab = W.so_radial(0.5, np.sqrt(W.r_nlcut2(0.5)))
+    return O.nlc_table(og, np.ascontiguousarray(core_coords), np.full(n, 0.01), tab, np.zeros((n, 5, 1024)),
+                       np.zeros((n, 5), np.int32))
+
+
 def _cpu_sample(radius, ncheby, nstart, sample_terms, seed):
     """Times the oracle on one spinor start: one H psi and the m axpys of one
     Newton term (filter.c:318-359) at the full grid."""
@@ -407,9 +417,7 @@ def _cpu_sample(radius, ncheby, nstart, sample_terms, seed):
     # the per-term cost does not depend on the potential's values
     pot = np.random.default_rng(seed).uniform(-1.5, 0.3, og.ngrid)
     t_pot = 0.0
-    tab = W.so_radial(0.5, np.sqrt(W.r_nlcut2(0.5)))
-    pt = W.nlc_table(g, coords[core], np.full(len(core), 0.01), tab)
-    proj = O.Projectors(pt.nl, pt.npts, pt.jxyz, pt.y1, pt.proj, pt.nlp, pt.sgn)
+    proj = _oracle_table(W, O, og, coords[core])
     sysm = O.System(og, pot, nspin=2, is_complex=True, so=True, nlflag=False, proj=proj)
     rng = np.random.default_rng(seed)
     psi = rng.uniform(-1, 1, 2 * og.ngrid) + 1j * rng.uniform(-1, 1, 2 * og.ngrid)
@@ -445,9 +453,7 @@ def _worker(q, radius, ncheby, nstart, seed, nrep):
     core = [i for i, t in enumerate(types) if not t.startswith("P")]
     og = O.Grid(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, g.xmin, g.ymin, g.zmin, KE_MAX)
     pot = np.random.default_rng(seed).uniform(-1.5, 0.3, og.ngrid)
-    tab = W.so_radial(0.5, np.sqrt(W.r_nlcut2(0.5)))
-    pt = W.nlc_table(g, coords[core], np.full(len(core), 0.01), tab)
-    proj = O.Projectors(pt.nl, pt.npts, pt.jxyz, pt.y1, pt.proj, pt.nlp, pt.sgn)
+    proj = _oracle_table(W, O, og, coords[core])
     sysm = O.System(og, pot, nspin=2, is_complex=True, so=True, nlflag=False, proj=proj)
     rng = np.random.default_rng(seed)
     psi = rng.uniform(-1, 1, 2 * og.ngrid) + 1j * rng.uniform(-1, 1, 2 * og.ngrid)
