@@ -3,10 +3,125 @@
  * reference tree with the FFTW subset of fftw_shim.c, so the tests can pin
  * the oracle's kinetic term and angular statistics against the reference's
  * own code. */
+#include <stdlib.h>
 #include <string.h>
 
 #include "fd.h"
 #include "angular.h"
+#include "hamiltonian.h"
+
+void filter_cycle(double *psi_rank, long jns, zomplex *psi, zomplex *phi, double *pot_local, zomplex *LS, nlc_st *nlc,
+                  long *nl, double *ksqr, zomplex *an, double *zn, double *ene_targets, grid_st *grid, index_st *ist,
+                  par_st *par, flag_st *flag, parallel_st *parallel, fftw_plan_loc planfw, fftw_plan_loc planbw,
+                  fftw_complex *fftwpsi);
+
+/* the job description and projector table of one H psi, in the reference's
+ * structs (nlc_st array of structures from the oracle's SoA table) */
+struct job {
+  index_st ist;
+  par_st par;
+  flag_st flag;
+  parallel_st pl;
+  nlc_st *nlc;
+  fftw_complex *buf;
+  fftw_plan fw, bw;
+};
+
+static void job_init(struct job *j, long nx, long ny, long nz, int nspin, int is_complex, int so, int nl, long nat,
+                     long npts, long nproj, const int *jxyz, const double *y1, const double *proj, const double *nlp,
+                     const int *sgn, double dv)
+{
+  memset(j, 0, sizeof *j);
+  j->ist.nx = nx;
+  j->ist.ny = ny;
+  j->ist.nz = nz;
+  j->ist.ngrid = nx * ny * nz;
+  j->ist.nspin = nspin;
+  j->ist.nspinngrid = nspin * j->ist.ngrid;
+  j->ist.complex_idx = is_complex ? 2 : 1;
+  j->ist.n_NL_atoms = nat;
+  j->ist.n_NL_gridpts = npts;
+  j->ist.nproj = nproj;
+  j->ist.n_s_ang_mom = 2;
+  j->ist.n_l_ang_mom = 3;
+  j->ist.n_j_ang_mom = 6;
+  j->par.dv = dv;
+  j->par.ham_threads = 1;
+  j->flag.SO = so;
+  j->flag.NL = nl;
+  j->flag.isComplex = is_complex;
+  j->flag.useSpinors = nspin == 2;
+  j->pl.nthreads = 1;
+  j->pl.mpi_rank = 1; /* no progress bar */
+  j->nlc = calloc(nat * npts > 0 ? nat * npts : 1, sizeof(nlc_st));
+  for (long a = 0; a < nat; a++)
+    for (long g = 0; g < npts; g++) {
+      const long e = a * npts + g;
+      j->nlc[e].jxyz = jxyz[e];
+      for (int m = 0; m < 3; m++) {
+        j->nlc[e].y1[m].re = y1[e * 6 + 2 * m];
+        j->nlc[e].y1[m].im = y1[e * 6 + 2 * m + 1];
+      }
+      for (long p = 0; p < nproj; p++) {
+        j->nlc[e].proj[p] = proj[e * nproj + p];
+        j->nlc[e].NL_proj[p] = nlp[e * nproj + p];
+        j->nlc[e].NL_proj_sign[p] = sgn[a * nproj + p];
+      }
+    }
+  j->buf = fftw_malloc(j->ist.ngrid * sizeof(fftw_complex));
+  j->fw = fftw_plan_dft_3d((int)nz, (int)ny, (int)nx, j->buf, j->buf, FFTW_FORWARD, FFTW_MEASURE);
+  j->bw = fftw_plan_dft_3d((int)nz, (int)ny, (int)nx, j->buf, j->buf, FFTW_BACKWARD, FFTW_MEASURE);
+}
+
+static void job_free(struct job *j)
+{
+  fftw_destroy_plan(j->fw);
+  fftw_destroy_plan(j->bw);
+  fftw_free(j->buf);
+  free(j->nlc);
+}
+
+/* p_hamiltonian (phamiltonian.c:10-60) on one state: out = H psi (zomplex,
+ * nspin * ngrid); pot2 holds the local potential twice as init.c:666 leaves it */
+void ref_hamiltonian(double *out, const double *psi, long nx, long ny, long nz, int nspin, int is_complex, int so,
+                     int nl, double *pot2, double *ls, double *ksqr, long nat, long npts, long nproj, long *nlcnt,
+                     const int *jxyz, const double *y1, const double *proj, const double *nlp, const int *sgn,
+                     double dv)
+{
+  struct job j;
+  job_init(&j, nx, ny, nz, nspin, is_complex, so, nl, nat, npts, nproj, jxyz, y1, proj, nlp, sgn, dv);
+  zomplex *tmp = calloc(j.ist.nspinngrid, sizeof(zomplex));
+  memcpy(out, psi, j.ist.nspinngrid * sizeof(zomplex));
+  p_hamiltonian((zomplex *)out, tmp, pot2, (zomplex *)ls, j.nlc, nlcnt, ksqr, &j.ist, &j.par, &j.flag, j.fw, j.bw,
+                j.buf, 1);
+  free(tmp);
+  job_free(&j);
+}
+
+/* filter_cycle (filter.c:187-371) of one start: psi_rank holds the start in
+ * its first stlen doubles on entry and the m filtered states on return;
+ * an [m][ncheby] zomplex, zn [ncheby] */
+void ref_filter_cycle(double *psi_rank, long nx, long ny, long nz, int nspin, int is_complex, int so, int nl,
+                      double *pot2, double *ls, double *ksqr, long nat, long npts, long nproj, long *nlcnt,
+                      const int *jxyz, const double *y1, const double *proj, const double *nlp, const int *sgn,
+                      double dv, double *an, double *zn, long ncheby, long m, double vmin, double de)
+{
+  struct job j;
+  job_init(&j, nx, ny, nz, nspin, is_complex, so, nl, nat, npts, nproj, jxyz, y1, proj, nlp, sgn, dv);
+  j.ist.ncheby = ncheby;
+  j.ist.m_states_per_filter = m;
+  j.par.Vmin = vmin;
+  j.par.dE = de;
+  j.par.dE_1 = 4.0 / de;
+  zomplex *psi = calloc(j.ist.nspinngrid, sizeof(zomplex)), *phi = calloc(j.ist.nspinngrid, sizeof(zomplex));
+  grid_st grid;
+  memset(&grid, 0, sizeof grid);
+  filter_cycle(psi_rank, 0, psi, phi, pot2, (zomplex *)ls, j.nlc, nlcnt, ksqr, (zomplex *)an, zn, NULL, &grid, &j.ist,
+               &j.par, &j.flag, &j.pl, j.fw, j.bw, j.buf);
+  free(psi);
+  free(phi);
+  job_free(&j);
+}
 
 /* kinetic() (hamiltonian.c:62-99) on one block of ngrid complex values:
  * out = FFTW_BACKWARD(ksqr * FFTW_FORWARD(psi)), ksqr as build_grid_ksqr

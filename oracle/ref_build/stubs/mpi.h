@@ -3,5 +3,16 @@
  * compiled functions communicates. */
 #pragma once
 typedef int MPI_Comm;
+typedef int MPI_Datatype;
+typedef struct { int source, tag, error; } MPI_Status;
 #define MPI_COMM_WORLD 0
 #define MPI_COMM_NULL (-1)
+#define MPI_DOUBLE 1
+/* declared so that filter.c compiles; the test-only library defines them as
+ * aborting stubs (ref_fft_stubs.c): the pinned single-rank paths never call them */
+int MPI_Comm_rank(MPI_Comm comm, int *rank);
+int MPI_Comm_size(MPI_Comm comm, int *size);
+int MPI_Gather(const void *s, int sc, MPI_Datatype st, void *r, int rc, MPI_Datatype rt, int root, MPI_Comm comm);
+int MPI_Send(const void *b, int c, MPI_Datatype t, int dest, int tag, MPI_Comm comm);
+int MPI_Recv(void *b, int c, MPI_Datatype t, int src, int tag, MPI_Comm comm, MPI_Status *st);
+int MPI_Abort(MPI_Comm comm, int code);

@@ -51,7 +51,23 @@ def ref_fft():
     L.ref_kinetic.argtypes = [D, D, ctypes.c_long, ctypes.c_long, ctypes.c_long, D]
     L.ref_angular.argtypes = ([D] + [ctypes.c_long] * 4 + [ctypes.c_double] * 3 + [D] * 3 + [ctypes.c_double] * 3 +
                               [ctypes.c_int] * 2)
+    LP, IP = ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_int)
+    table = [ctypes.c_long] * 3 + [LP, IP, D, D, D, IP, ctypes.c_double]
+    L.ref_hamiltonian.argtypes = [D, D] + [ctypes.c_long] * 3 + [ctypes.c_int] * 4 + [D] * 3 + table
+    L.ref_filter_cycle.argtypes = ([D] + [ctypes.c_long] * 3 + [ctypes.c_int] * 4 + [D] * 3 + table +
+                                   [D, D, ctypes.c_long, ctypes.c_long, ctypes.c_double, ctypes.c_double])
     return L
+
+
+def _table_args(sysm, so, nl):
+    """the projector-table arguments of the reference harness for sysm"""
+    pr = sysm.proj
+    if pr is None:
+        pr = O.Projectors(np.zeros(1, np.int64), 1, np.zeros(1, np.int32), np.zeros(6), np.zeros(5), np.zeros(5),
+                          np.zeros(5, np.int32))
+    return [pr.nat if (so or nl) else 0, pr.npts, pr.nproj, pr.nl.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+            pr.jxyz.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _p(pr.y1), _p(pr.proj), _p(pr.nlp),
+            pr.sgn.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), sysm.grid.dv]
 
 
 # ---------------------------------------------------------------- golden vectors
@@ -252,3 +268,57 @@ def test_angular_stats_match_reference(ref_fft, tmp_path, monkeypatch):
     mine1 = O.filter_angular_stats([quirk.view(np.float64)], g)[0]
     assert np.max(np.abs(rows[1, 1:] - mine1)) < 6e-7
     assert np.max(np.abs(rows[1, 1:] - O.filter_angular_stats(states[1:], g)[0])) > 1e-3
+
+
+@pytest.mark.parametrize("so,nl,cplx", [(1, 1, 1), (0, 1, 0), (0, 0, 1)])
+def test_hamiltonian_matches_reference(ref_fft, so, nl, cplx):
+    """p_hamiltonian (filter_mpi/phamiltonian.c:10-60: kinetic FFT term, local
+    potential, spin-orbit and nonlocal projectors) run from the reference's
+    own source against the oracle's H psi."""
+    from tests.systems import tiny_cluster
+    nspin = 2 if so else 1
+    sysm = tiny_cluster(12, 11, 13, natoms=6, nspin=nspin, is_complex=bool(cplx), so=bool(so), nl=bool(nl))
+    rng = np.random.default_rng(17)
+    L = nspin * sysm.ngrid
+    psi = rng.uniform(-1, 1, L) + 1j * (rng.uniform(-1, 1, L) if cplx else 0)
+    pot2 = np.concatenate([sysm.pot, sysm.pot])
+    ls = np.ascontiguousarray(sysm.LS).view(np.float64)
+    ksqr = np.ascontiguousarray(sysm.grid.ksqr())
+    theirs = np.empty(L, np.complex128)
+    g = sysm.grid
+    ref_fft.ref_hamiltonian(_p(theirs.view(np.float64)), _p(psi.view(np.float64)), g.nx, g.ny, g.nz, nspin, cplx, so,
+                            nl, _p(pot2), _p(ls), _p(ksqr), *_table_args(sysm, so, nl))
+    mine = O.hamiltonian(psi, sysm)
+    assert np.max(np.abs(mine - theirs)) < 1e-12 * np.max(np.abs(theirs))
+
+
+def test_filter_cycle_matches_reference(ref_fft):
+    """filter_cycle (filter_mpi/filter.c:187-371, with p_hnorm :375-410) of one
+    spinor start with spin-orbit and nonlocal projectors, 24 Newton terms and
+    3 energy targets, run from the reference's own source against the
+    oracle's Newton recursion."""
+    from tests.systems import tiny_cluster
+    sysm = tiny_cluster(10, 11, 9, natoms=5, nspin=2, is_complex=True, so=True, nl=True)
+    g = sysm.grid
+    rng = np.random.default_rng(23)
+    L = 2 * g.ngrid
+    psi0 = rng.uniform(-1, 1, L) + 1j * rng.uniform(-1, 1, L)
+    psi0 /= np.sqrt(np.sum(np.abs(psi0) ** 2) * g.dv)
+    nc, m = 24, 3
+    zn, _, _ = O.samp_points(nc)
+    emin, emax = float(sysm.pot.min()) - 1.0, float(sysm.pot.max()) + g.ke_max + 2.0
+    de = emax - emin
+    an = O.newton_coeff(zn, np.array([emin + 0.2 * de, emin + 0.3 * de, emin + 0.4 * de]), emin, de,
+                        O.filter_dt(nc, de))
+    mine = O.filter_cycle(psi0, sysm, an, zn, emin, de)
+    psi_rank = np.zeros(m * L, np.complex128)
+    psi_rank[:L] = psi0
+    pot2 = np.concatenate([sysm.pot, sysm.pot])
+    ls = np.ascontiguousarray(sysm.LS).view(np.float64)
+    ksqr = np.ascontiguousarray(g.ksqr())
+    anc = np.ascontiguousarray(an, np.complex128)
+    znc = np.ascontiguousarray(zn, np.float64)
+    ref_fft.ref_filter_cycle(_p(psi_rank.view(np.float64)), g.nx, g.ny, g.nz, 2, 1, 1, 1, _p(pot2), _p(ls),
+                             _p(ksqr), *_table_args(sysm, 1, 1), _p(anc.view(np.float64)), _p(znc), nc, m, emin, de)
+    theirs = psi_rank.reshape(m, L)
+    assert np.max(np.abs(mine - theirs)) < 1e-10 * np.max(np.abs(theirs))
