@@ -193,3 +193,38 @@ void ref_angular(double *psitot, long n_states, long nx, long ny, long nz, doubl
   pl.nthreads = 1;
   calc_angular_exp(psitot, &grid, start, stop, &ist, &par, &flag, &pl);
 }
+
+long ortho_cplx(MKL_Complex16 *psitot, double dv, long n_cols, index_st *ist, par_st *par, flag_st *flag,
+                parallel_st *parallel);
+void normalize_all(double *psitot, long n_states, index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+void diag_H(double *psitot, double *pot_local, vector *G_vecs, vector *k_vecs, zomplex *LS, nlc_st *nlc, long *nl,
+            double *ksqr, double *eval, long n_states, int k_idx, index_st *ist, par_st *par, flag_st *flag,
+            parallel_st *parallel);
+void calc_sigma_E(double *psitot, double *pot_local, zomplex *LS, nlc_st *nlc, long *nl, double *ksqr,
+                  double *sigma_E, index_st *ist, par_st *par, flag_st *flag);
+int ref_set_lapack(const char *path);
+
+/* mod_ortho's orthogonalisation of n complex states (ortho_cplx,
+ * ortho.c:93-185, then normalize_all as mod_ortho.c:84 does) followed by
+ * mod_diag's diag_H (Hmat.c:5-297) and normalize_all (mod_diag.c:424-433) and
+ * mod_sigma's calc_sigma_E (energy.c:383-539):
+ * psitot holds the n states on entry and the kept eigenvectors on return;
+ * eval and sigma receive n_kept values; returns n_kept.  Writes hmat-0.dat
+ * and eval_aux.dat into the working directory as the reference does. */
+long ref_ritz(double *psitot, long n, long nx, long ny, long nz, int nspin, int so, int nl, double *pot2, double *ls,
+              double *ksqr, long nat, long npts, long nproj, long *nlcnt, const int *jxyz, const double *y1,
+              const double *proj, const double *nlp, const int *sgn, double dv, double *eval, double *sigma)
+{
+  struct job j;
+  job_init(&j, nx, ny, nz, nspin, 1, so, nl, nat, npts, nproj, jxyz, y1, proj, nlp, sgn, dv);
+  j.pl.k_rank = 1; /* quiet */
+  j.ist.nthreads = 1;
+  const long kept = ortho_cplx((MKL_Complex16 *)psitot, dv, n, &j.ist, &j.par, &j.flag, &j.pl);
+  normalize_all(psitot, kept, &j.ist, &j.par, &j.flag, &j.pl);
+  j.ist.mn_states_tot = kept;
+  diag_H(psitot, pot2, NULL, NULL, (zomplex *)ls, j.nlc, nlcnt, ksqr, eval, kept, 0, &j.ist, &j.par, &j.flag, &j.pl);
+  normalize_all(psitot, kept, &j.ist, &j.par, &j.flag, &j.pl); /* mod_diag.c:110 */
+  calc_sigma_E(psitot, pot2, (zomplex *)ls, j.nlc, nlcnt, ksqr, sigma, &j.ist, &j.par, &j.flag);
+  job_free(&j);
+  return kept;
+}

@@ -56,7 +56,19 @@ def ref_fft():
     L.ref_hamiltonian.argtypes = [D, D] + [ctypes.c_long] * 3 + [ctypes.c_int] * 4 + [D] * 3 + table
     L.ref_filter_cycle.argtypes = ([D] + [ctypes.c_long] * 3 + [ctypes.c_int] * 4 + [D] * 3 + table +
                                    [D, D, ctypes.c_long, ctypes.c_long, ctypes.c_double, ctypes.c_double])
+    L.ref_ritz.argtypes = [D] + [ctypes.c_long] * 4 + [ctypes.c_int] * 3 + [D] * 3 + table + [D, D]
+    L.ref_ritz.restype = ctypes.c_long
+    L.ref_set_lapack.argtypes = [ctypes.c_char_p]
     return L
+
+
+def _numpy_lapack():
+    """numpy's bundled ILP64 LAPACK (OpenBLAS), which the reference's LAPACK
+    calls are forwarded to in the pin library"""
+    import glob
+    here = os.path.dirname(os.path.dirname(np.__file__))
+    found = glob.glob(os.path.join(here, "numpy.libs", "libscipy_openblas64_*.so"))
+    return found[0] if found else None
 
 
 def _table_args(sysm, so, nl):
@@ -322,3 +334,44 @@ def test_filter_cycle_matches_reference(ref_fft):
                              _p(ksqr), *_table_args(sysm, 1, 1), _p(anc.view(np.float64)), _p(znc), nc, m, emin, de)
     theirs = psi_rank.reshape(m, L)
     assert np.max(np.abs(mine - theirs)) < 1e-10 * np.max(np.abs(theirs))
+
+
+def test_rayleigh_ritz_matches_reference(ref_fft, tmp_path, monkeypatch):
+    """The reference's own mod_ortho + mod_diag + mod_sigma sequence
+    (ortho_cplx with LAPACK's zgesvd, normalize_all, diag_H with zheev,
+    normalize_all, calc_sigma_E; filter_mpi/ortho.c:93-185, Hmat.c:5-297,
+    energy.c:383-539) against the oracle's ortho / diag / sigma_e on the same
+    spinor states: the kept count, the Ritz values, sigma_E and every Ritz
+    vector (up to its phase)."""
+    from tests.systems import tiny_cluster
+    lap = _numpy_lapack()
+    if lap is None or not ref_fft.ref_set_lapack(lap.encode()):
+        pytest.skip("numpy's ILP64 LAPACK is not available")
+    monkeypatch.chdir(tmp_path)  # diag_H and calc_sigma_E write hmat-0.dat / eval_aux.dat
+    sysm = tiny_cluster(10, 9, 11, natoms=5, nspin=2, is_complex=True, so=True, nl=True)
+    g = sysm.grid
+    L = 2 * g.ngrid
+    rng = np.random.default_rng(31)
+    n = 6
+    base = rng.normal(size=(4, L)) + 1j * rng.normal(size=(4, L))
+    # two of the six states lie in the span of the others: the rank cut keeps four
+    psis = np.concatenate([base, (base[:2].T @ rng.normal(size=(2, 2))).T])
+    assert psis.shape == (n, L)
+    ov, s = O.ortho(psis, True, 1e-10, g.dv)
+    e_mine, v_mine = O.diag(ov, sysm)
+    _, sg_mine = O.sigma_e(v_mine, sysm)
+    buf = np.ascontiguousarray(psis)
+    ev, sg = np.zeros(n), np.zeros(n)
+    pot2 = np.concatenate([sysm.pot, sysm.pot])
+    ls = np.ascontiguousarray(sysm.LS).view(np.float64)
+    ksqr = np.ascontiguousarray(g.ksqr())
+    kept = ref_fft.ref_ritz(_p(buf.view(np.float64)), n, g.nx, g.ny, g.nz, 2, 1, 1, _p(pot2), _p(ls), _p(ksqr),
+                            *_table_args(sysm, 1, 1), _p(ev), _p(sg))
+    assert kept == len(e_mine) == 4
+    print(f"\n[reference Rayleigh-Ritz] Ritz values {ev[:kept]}, max |dE| {np.max(np.abs(ev[:kept] - e_mine)):.1e}, "
+          f"sigma {sg[:kept]}")
+    assert np.allclose(ev[:kept], e_mine, rtol=0, atol=1e-11 * np.max(np.abs(e_mine)))
+    assert np.allclose(sg[:kept], sg_mine, rtol=1e-7, atol=1e-9)
+    theirs = buf[:kept]
+    for a, b in zip(theirs, v_mine):
+        assert abs(abs(np.vdot(a, b)) * g.dv - 1.0) < 1e-10
