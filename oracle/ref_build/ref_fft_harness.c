@@ -228,3 +228,31 @@ long ref_ritz(double *psitot, long n, long nx, long ny, long nz, int nspin, int 
   job_free(&j);
   return kept;
 }
+
+void get_energy_range(zomplex *psi, zomplex *phi, double *pot_local, grid_st *grid, zomplex *LS, nlc_st *nlc,
+                      long *nl, double *ksqr, index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+
+/* get_energy_range (energy.c:169-379, iterative branch) of a complex job:
+ * vmin and de as it leaves them in par (Vmin, dE).  Writes Emin-init.dat and
+ * Emax-init.dat into the working directory as the reference does. */
+void ref_energy_range(long nx, long ny, long nz, int nspin, int so, int nl, double *pot2, double *ls, double *ksqr,
+                      long nat, long npts, long nproj, long *nlcnt, const int *jxyz, const double *y1,
+                      const double *proj, const double *nlp, const int *sgn, double dv, double *vmin, double *de)
+{
+  struct job j;
+  job_init(&j, nx, ny, nz, nspin, 1, so, nl, nat, npts, nproj, jxyz, y1, proj, nlp, sgn, dv);
+  grid_st grid;
+  memset(&grid, 0, sizeof grid);
+  grid.nx = nx;
+  grid.ny = ny;
+  grid.nz = nz;
+  grid.ngrid = nx * ny * nz;
+  grid.dv = dv;
+  zomplex *psi = calloc(j.ist.nspinngrid, sizeof(zomplex)), *phi = calloc(j.ist.nspinngrid, sizeof(zomplex));
+  get_energy_range(psi, phi, pot2, &grid, (zomplex *)ls, j.nlc, nlcnt, ksqr, &j.ist, &j.par, &j.flag, &j.pl);
+  *vmin = j.par.Vmin;
+  *de = j.par.dE;
+  free(psi);
+  free(phi);
+  job_free(&j);
+}

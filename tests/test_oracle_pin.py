@@ -59,6 +59,7 @@ def ref_fft():
     L.ref_ritz.argtypes = [D] + [ctypes.c_long] * 4 + [ctypes.c_int] * 3 + [D] * 3 + table + [D, D]
     L.ref_ritz.restype = ctypes.c_long
     L.ref_set_lapack.argtypes = [ctypes.c_char_p]
+    L.ref_energy_range.argtypes = [ctypes.c_long] * 3 + [ctypes.c_int] * 3 + [D] * 3 + table + [D, D]
     return L
 
 
@@ -375,3 +376,24 @@ def test_rayleigh_ritz_matches_reference(ref_fft, tmp_path, monkeypatch):
     theirs = buf[:kept]
     for a, b in zip(theirs, v_mine):
         assert abs(abs(np.vdot(a, b)) * g.dv - 1.0) < 1e-10
+
+
+def test_energy_range_matches_reference(ref_fft, tmp_path, monkeypatch):
+    """get_energy_range (filter_mpi/energy.c:169-379: imaginary-time descent to
+    E_min, power iteration to E_max from init_psi's random states, then the
+    inflation) run from the reference's own source against the oracle, spinor
+    job with spin-orbit and nonlocal projectors."""
+    from tests.systems import tiny_cluster
+    monkeypatch.chdir(tmp_path)  # Emin-init.dat / Emax-init.dat
+    sysm = tiny_cluster(9, 10, 8, natoms=4, nspin=2, is_complex=True, so=True, nl=True)
+    g = sysm.grid
+    pot2 = np.concatenate([sysm.pot, sysm.pot])
+    ls = np.ascontiguousarray(sysm.LS).view(np.float64)
+    ksqr = np.ascontiguousarray(g.ksqr())
+    vmin, de = ctypes.c_double(), ctypes.c_double()
+    ref_fft.ref_energy_range(g.nx, g.ny, g.nz, 2, 1, 1, _p(pot2), _p(ls), _p(ksqr), *_table_args(sysm, 1, 1),
+                             ctypes.byref(vmin), ctypes.byref(de))
+    mine_vmin, mine_de, _, _ = O.energy_range(sysm)
+    print(f"\n[reference energy range] Vmin {vmin.value:.10f} dE {de.value:.10f}; oracle {mine_vmin:.10f} {mine_de:.10f}")
+    assert abs(vmin.value - mine_vmin) < 1e-9 * abs(mine_vmin)
+    assert abs(de.value - mine_de) < 1e-9 * mine_de
