@@ -60,3 +60,34 @@ void dsyev_(const char *jobz, const char *uplo, const ll *n, double *a, const ll
 {
   ((syev_d)sym("scipy_dsyev_64_"))(jobz, uplo, n, a, lda, w, work, lwork, info, 1, 1);
 }
+
+/* LAPACKE_zheev (row-major, bse_cplx/diag.c:38): the row-major matrix is
+ * copied to column-major storage of the same logical matrix, zheev_ runs on
+ * it, and the eigenvectors (columns) are copied back, as LAPACKE does */
+typedef struct { double re, im; } zc;
+ll LAPACKE_zheev(int layout, char jobz, char uplo, ll n, void *a, ll lda, double *w)
+{
+  zc *m = (zc *)a;
+  zc *t = malloc((size_t)(n > 0 ? n * n : 1) * sizeof(zc));
+  double *rwork = malloc((size_t)(3 * n > 1 ? 3 * n : 1) * sizeof(double));
+  ll info = 0, lwork = -1;
+  zc q;
+  if (!t || !rwork) abort();
+  for (ll i = 0; i < n; i++)
+    for (ll j = 0; j < n; j++) t[i + j * n] = layout == 101 ? m[i * lda + j] : m[i + j * lda];
+  const ll ldt = n > 0 ? n : 1;
+  zheev_(&jobz, &uplo, &n, t, &ldt, w, &q, &lwork, rwork, &info);  /* workspace query */
+  lwork = (ll)q.re;
+  zc *work = malloc((size_t)(lwork > 0 ? lwork : 1) * sizeof(zc));
+  if (!work) abort();
+  zheev_(&jobz, &uplo, &n, t, &ldt, w, work, &lwork, rwork, &info);
+  for (ll i = 0; i < n; i++)
+    for (ll j = 0; j < n; j++) {
+      if (layout == 101) m[i * lda + j] = t[i + j * n];
+      else m[i + j * lda] = t[i + j * n];
+    }
+  free(work);
+  free(rwork);
+  free(t);
+  return info;
+}

@@ -1,0 +1,134 @@
+/* Test-only harness of oracle/_ref/libfbse_ref_bse.so: the reference's BSE
+ * stage (bse_cplx/) compiled from where it lies with the FFTW subset
+ * (fftw_shim.c), the LAPACKE / LAPACK forwarders (lapack_shim.c) and one-rank
+ * MPI (mpi_single.c), behind plain-argument wrappers for the pin tests. */
+#include <string.h>
+
+#include "fd.h"
+
+void init_elec_hole_kernel(double complex *pot_bare, double complex *pot_screened, grid_st *grid, index_st *ist,
+                           par_st *par, flag_st *flag, parallel_st *parallel);
+void calc_eh_kernel_cplx(double complex *psi_qp, double complex *pot_bare, double complex *pot_screened,
+                         double complex *direct, double complex *exchange, index_st *ist, par_st *par, flag_st *flag,
+                         parallel_st *parallel);
+void build_h0_mat(double *h0mat, double *eval, index_st *ist);
+void build_BSE_mat(double complex *bsmat, double complex *direct, double complex *exchange, index_st *ist);
+void bethe_salpeter(double complex *direct, double complex *exchange, double complex *bsmat, double complex *bs_coeff,
+                    double *h0mat, double *xton_ene, grid_st *grid, index_st *ist, par_st *par, flag_st *flag,
+                    parallel_st *parallel);
+void calc_elec_dipole(xyz_st *elec_dip, double complex *psi_qp, double *eig_vals, grid_st *grid, index_st *ist,
+                      par_st *par, flag_st *flag);
+
+struct bjob {
+  grid_st grid;
+  index_st ist;
+  par_st par;
+  flag_st flag;
+  parallel_st pl;
+};
+
+/* the grid of the BSE stage (x_j = xmin + j dx as bse_cplx/read.c:398-409
+ * builds it, coordinates passed in) and the spinor job of n_h holes and
+ * n_e electrons at lumo_idx */
+static void bjob_init(struct bjob *j, long nx, long ny, long nz, double dx, double dy, double dz, double xmin,
+                      double ymin, double zmin, double *gx, double *gy, double *gz, long nh, long ne, long lumo)
+{
+  memset(j, 0, sizeof *j);
+  j->grid.nx = nx;
+  j->grid.ny = ny;
+  j->grid.nz = nz;
+  j->grid.ngrid = nx * ny * nz;
+  j->grid.dx = dx;
+  j->grid.dy = dy;
+  j->grid.dz = dz;
+  j->grid.dv = dx * dy * dz;
+  j->grid.xmin = xmin;
+  j->grid.ymin = ymin;
+  j->grid.zmin = zmin;
+  j->grid.x = gx;
+  j->grid.y = gy;
+  j->grid.z = gz;
+  j->ist.nx = nx;
+  j->ist.ny = ny;
+  j->ist.nz = nz;
+  j->ist.ngrid = nx * ny * nz;
+  j->ist.ngrid_1 = 1.0 / (double)j->ist.ngrid;
+  j->ist.nspin = 2;
+  j->ist.nspinngrid = 2 * j->ist.ngrid;
+  j->ist.complex_idx = 2;
+  j->ist.nthreads = 1;
+  j->ist.n_holes = nh;
+  j->ist.n_elecs = ne;
+  j->ist.lumo_idx = lumo;
+  j->ist.n_xton = nh * ne;
+  j->par.dv = j->grid.dv;
+  j->par.dx = dx;
+  j->par.dy = dy;
+  j->par.dz = dz;
+  j->flag.SO = 1;
+  j->flag.useSpinors = 1;
+  j->flag.isComplex = 1;
+  j->pl.nthreads = 1;
+  j->pl.mpi_rank = 0;
+  j->pl.mpi_size = 1;
+}
+
+/* init_elec_hole_kernel (bse_cplx/init.c:8-268): bare and screened
+ * interactions in k space (ngrid complex each) */
+void ref_bse_potentials(long nx, long ny, long nz, double dx, double dy, double dz, double xmin, double ymin,
+                        double zmin, double *gx, double *gy, double *gz, double epsx, double epsy, double epsz,
+                        double *bare, double *scr)
+{
+  struct bjob j;
+  bjob_init(&j, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, gx, gy, gz, 1, 1, 1);
+  j.par.epsX = epsx;
+  j.par.epsY = epsy;
+  j.par.epsZ = epsz;
+  j.pl.mpi_rank = 1; /* quiet */
+  init_elec_hole_kernel((double complex *)bare, (double complex *)scr, &j.grid, &j.ist, &j.par, &j.flag, &j.pl);
+}
+
+/* calc_eh_kernel_cplx (bse_cplx/coulomb.c:20-738) at one rank: direct and
+ * exchange [n_xton][n_xton] complex (the triangles the reference fills);
+ * writes its kernel files into the working directory */
+void ref_bse_kernel(double *psi_qp, long nh, long ne, long lumo, long nx, long ny, long nz, double dx, double dy,
+                    double dz, double xmin, double ymin, double zmin, double *gx, double *gy, double *gz,
+                    double *bare, double *scr, double *direct, double *exchange)
+{
+  struct bjob j;
+  bjob_init(&j, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, gx, gy, gz, nh, ne, lumo);
+  calc_eh_kernel_cplx((double complex *)psi_qp, (double complex *)bare, (double complex *)scr,
+                      (double complex *)direct, (double complex *)exchange, &j.ist, &j.par, &j.flag, &j.pl);
+}
+
+/* build_h0_mat + build_BSE_mat + bethe_salpeter (bse_cplx/mod_bse.c:54-148,
+ * bethe-salpeter.c:7-350): exciton energies and coefficients (column j of the
+ * row-major [n_xton][n_xton] matrix); writes h0.dat, bs*.dat, HBSmat*.dat,
+ * BSEcoeff*.dat and exciton.dat into the working directory */
+void ref_bse_solve(double *direct, double *exchange, double *eval_qp, long nh, long ne, long lumo, double *xton_ene,
+                   double *coeff)
+{
+  struct bjob j;
+  double gx = 0, gy = 0, gz = 0;
+  bjob_init(&j, 1, 1, 1, 1, 1, 1, 0, 0, 0, &gx, &gy, &gz, nh, ne, lumo);
+  const long n = nh * ne;
+  double *h0 = calloc(n * n, sizeof(double));
+  double complex *bs = calloc(n * n, sizeof(double complex));
+  build_h0_mat(h0, eval_qp, &j.ist);
+  build_BSE_mat(bs, (double complex *)direct, (double complex *)exchange, &j.ist);
+  bethe_salpeter((double complex *)direct, (double complex *)exchange, bs, (double complex *)coeff, h0, xton_ene,
+                 &j.grid, &j.ist, &j.par, &j.flag, &j.pl);
+  free(h0);
+  free(bs);
+}
+
+/* calc_elec_dipole (bse_cplx/dipole.c:7-158): mu [n_h * n_e][3] complex;
+ * writes OS0.dat into the working directory */
+void ref_bse_dipoles(double *psi_qp, double *eval_qp, long nh, long ne, long lumo, long nx, long ny, long nz,
+                     double dx, double dy, double dz, double xmin, double ymin, double zmin, double *gx, double *gy,
+                     double *gz, double *mu)
+{
+  struct bjob j;
+  bjob_init(&j, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, gx, gy, gz, nh, ne, lumo);
+  calc_elec_dipole((xyz_st *)mu, (double complex *)psi_qp, eval_qp, &j.grid, &j.ist, &j.par, &j.flag);
+}

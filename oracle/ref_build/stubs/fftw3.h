@@ -1,9 +1,15 @@
-/* Type-only stand-in for <fftw3.h>, used only to compile the reference's
- * pure-C hot-path files into the test-only oracle/_ref library.  The
- * reference's FFT calls (fftw_execute etc.) are declared here but resolved
- * by aborting stubs in ref_harness.c: no transform is ever run through them. */
+/* Stand-in for <fftw3.h>, used only to compile the reference's hot-path C
+ * files into the test-only oracle/_ref libraries.  In libfbse_ref.so the
+ * transform resolves to an aborting stub (ref_harness.c); in
+ * libfbse_ref_fft.so / libfbse_ref_bse.so to the project-written FFTW subset
+ * (fftw_shim.c). */
 #pragma once
+/* as FFTW's own header: a C99 complex type when <complex.h> came first */
+#if defined(_Complex_I) && defined(complex) && defined(I)
+typedef double _Complex fftw_complex;
+#else
 typedef double fftw_complex[2];
+#endif
 typedef struct fbse_ref_fftw_plan_s *fftw_plan;
 #define FFTW_FORWARD (-1)
 #define FFTW_BACKWARD (+1)

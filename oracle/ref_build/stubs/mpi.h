@@ -8,8 +8,18 @@ typedef struct { int source, tag, error; } MPI_Status;
 #define MPI_COMM_WORLD 0
 #define MPI_COMM_NULL (-1)
 #define MPI_DOUBLE 1
-/* declared so that filter.c compiles; the test-only library defines them as
- * aborting stubs (ref_fft_stubs.c): the pinned single-rank paths never call them */
+typedef int MPI_Op;
+#define MPI_SUM 1
+#define MPI_IN_PLACE ((void *)1)
+#define MPI_STATUS_IGNORE ((MPI_Status *)0)
+/* declared so that filter.c and the BSE files compile; libfbse_ref_fft.so
+ * defines them as aborting stubs (ref_fft_stubs.c: the pinned filter paths
+ * never communicate), libfbse_ref_bse.so with one-rank semantics
+ * (mpi_single.c: the reference's BSE kernel calls its collectives at one rank too) */
+int MPI_Barrier(MPI_Comm comm);
+int MPI_Comm_split(MPI_Comm comm, int color, int key, MPI_Comm *newcomm);
+int MPI_Comm_free(MPI_Comm *comm);
+int MPI_Reduce(const void *s, void *r, int count, MPI_Datatype t, MPI_Op op, int root, MPI_Comm comm);
 int MPI_Comm_rank(MPI_Comm comm, int *rank);
 int MPI_Comm_size(MPI_Comm comm, int *size);
 int MPI_Gather(const void *s, int sc, MPI_Datatype st, void *r, int rc, MPI_Datatype rt, int root, MPI_Comm comm);

@@ -1,0 +1,129 @@
+"""Pins the oracle's Bethe-Salpeter stage against the reference's own BSE code
+(bse_cplx/ compiled from where it lies into oracle/_ref/libfbse_ref_bse.so with
+the project-written FFTW subset, LAPACKE forwarder and one-rank MPI; CPU):
+the bare and screened interactions, the direct and exchange kernels, the BSE
+solve with its exciton expectation values, and the electric transition
+dipoles, on smooth seeded spinor states."""
+import ctypes
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.test_bse_gpu import qp_states
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_BSE_SO = os.path.join(ROOT, "oracle", "_ref", "libfbse_ref_bse.so")
+D = ctypes.POINTER(ctypes.c_double)
+GRID = O.Grid(14, 13, 12, 0.8, 0.8, 0.8, -5.6, -5.2, -4.8)
+
+
+def _p(a):
+    return np.ascontiguousarray(a).ctypes.data_as(D)
+
+
+@pytest.fixture(scope="module")
+def rb():
+    if not os.path.exists(REF_BSE_SO):
+        pytest.skip("oracle/_ref not built (the reference tree is not mounted here)")
+    L = ctypes.CDLL(REF_BSE_SO)
+    gargs = [ctypes.c_long] * 3 + [ctypes.c_double] * 6 + [D] * 3
+    L.ref_bse_potentials.argtypes = gargs + [ctypes.c_double] * 3 + [D, D]
+    L.ref_bse_kernel.argtypes = [D] + [ctypes.c_long] * 3 + gargs + [D] * 4
+    L.ref_bse_solve.argtypes = [D, D, D] + [ctypes.c_long] * 3 + [D, D]
+    L.ref_bse_dipoles.argtypes = [D, D] + [ctypes.c_long] * 3 + gargs + [D]
+    L.ref_set_lapack.argtypes = [ctypes.c_char_p]
+    here = os.path.dirname(os.path.dirname(np.__file__))
+    lap = glob.glob(os.path.join(here, "numpy.libs", "libscipy_openblas64_*.so"))
+    if not lap or not L.ref_set_lapack(lap[0].encode()):
+        pytest.skip("numpy's ILP64 LAPACK is not available")
+    return L
+
+
+def _grid_args(g):
+    axes = [np.ascontiguousarray(a) for a in O.bse_axes(g)]
+    return axes, [g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, g.xmin, g.ymin, g.zmin] + [_p(a) for a in axes]
+
+
+@pytest.mark.parametrize("g", [GRID, O.Grid(12, 10, 13, 0.8, 0.8, 0.8, -4.8, -4.0, -5.2)])
+def test_bse_potentials_match_reference(rb, g):
+    """init_elec_hole_kernel (bse_cplx/init.c:8-268)"""
+    keep, ga = _grid_args(g)
+    eps = (6.1, 5.3, 7.2)
+    bare = np.empty(g.ngrid, np.complex128)
+    scr = np.empty(g.ngrid, np.complex128)
+    rb.ref_bse_potentials(*ga, *eps, _p(bare.view(np.float64)), _p(scr.view(np.float64)))
+    mb, ms = O.bse_potentials(g, eps)
+    assert np.max(np.abs(mb - bare)) < 1e-12 * np.max(np.abs(bare))
+    assert np.max(np.abs(ms - scr)) < 1e-12 * np.max(np.abs(scr))
+
+
+def _kernels(rb, g, psi, nh, ne, lumo, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)  # the kernel files
+    keep, ga = _grid_args(g)
+    bare, scr = O.bse_potentials(g, (6.0, 6.0, 6.0))
+    n = nh * ne
+    dr = np.zeros((n, n), np.complex128)
+    xr = np.zeros((n, n), np.complex128)
+    rb.ref_bse_kernel(_p(psi.view(np.float64)), nh, ne, lumo, *ga, _p(bare.view(np.float64)),
+                      _p(scr.view(np.float64)), _p(dr.view(np.float64)), _p(xr.view(np.float64)))
+    return bare, scr, dr, xr
+
+
+def test_bse_kernels_match_reference(rb, tmp_path, monkeypatch):
+    """calc_eh_kernel_cplx (bse_cplx/coulomb.c:20-738) at one rank: the lower
+    triangles (ibs >= jbs) of the screened direct and bare exchange kernels"""
+    nh, ne, lumo = 3, 2, 4
+    psi = np.ascontiguousarray(qp_states(GRID, lumo + ne, 41))
+    bare, scr, dr, xr = _kernels(rb, GRID, psi, nh, ne, lumo, tmp_path, monkeypatch)
+    dm, xm = O.bse_kernels(psi, nh, ne, lumo, bare, scr, GRID)
+    low = np.tril(np.ones((nh * ne, nh * ne), bool))
+    scale = max(np.max(np.abs(dm)), np.max(np.abs(xm)))
+    print(f"\n[reference BSE kernels] max |K^d| {np.max(np.abs(dm)):.3e}, max |K^x| {np.max(np.abs(xm)):.3e}, "
+          f"max dev {max(np.max(np.abs(dm - dr)[low]), np.max(np.abs(xm - xr)[low])):.1e}")
+    assert np.max(np.abs(dm - dr)[low]) < 1e-12 * scale
+    assert np.max(np.abs(xm - xr)[low]) < 1e-12 * scale
+
+
+def test_bse_solve_matches_reference(rb, tmp_path, monkeypatch):
+    """build_h0_mat, build_BSE_mat, bethe_salpeter (bse_cplx/mod_bse.c:54-148,
+    bethe-salpeter.c:7-350): exciton energies, coefficients (up to phase,
+    non-degenerate excitons) and the expectation values of exciton.dat"""
+    nh, ne, lumo = 3, 2, 4
+    psi = np.ascontiguousarray(qp_states(GRID, lumo + ne, 43))
+    _, _, dr, xr = _kernels(rb, GRID, psi, nh, ne, lumo, tmp_path, monkeypatch)
+    rng = np.random.default_rng(5)
+    ev = np.sort(np.concatenate([rng.uniform(-0.30, -0.20, lumo), rng.uniform(-0.05, 0.05, ne)]))
+    n = nh * ne
+    xe = np.zeros(n)
+    cf = np.zeros((n, n), np.complex128)
+    # the reference's solve works in its kernel arrays: hand it copies
+    rb.ref_bse_solve(_p(dr.copy().view(np.float64)), _p(xr.copy().view(np.float64)), _p(ev), nh, ne, lumo, _p(xe),
+                     _p(cf.view(np.float64)))
+    e, C, eh, ed, ex, e0 = O.bse_solve(ev, nh, ne, lumo, dr, xr)
+    assert np.max(np.abs(xe - e)) < 1e-13
+    gaps = np.diff(e)
+    for j in range(n):
+        if (j == 0 or gaps[j - 1] > 1e-8) and (j == n - 1 or gaps[j] > 1e-8):
+            assert abs(abs(np.vdot(cf[:, j], C[:, j])) - 1.0) < 1e-10
+    rows = np.loadtxt(tmp_path / "exciton.dat")
+    assert rows.shape == (n, 7)
+    # E_n, <H>, <H_dir>, <H_exc>, <H_0> ("% .12f", bethe-salpeter.c:337-346)
+    for col, want in ((1, e), (2, eh), (3, ed), (4, ex), (5, e0)):
+        assert np.allclose(rows[:, col], want, atol=1e-11), col
+
+
+def test_bse_dipoles_match_reference(rb, tmp_path, monkeypatch):
+    """calc_elec_dipole (bse_cplx/dipole.c:7-158): <i| r |a> for every hole /
+    electron pair"""
+    monkeypatch.chdir(tmp_path)
+    nh, ne, lumo = 3, 2, 4
+    psi = np.ascontiguousarray(qp_states(GRID, lumo + ne, 47))
+    ev = np.linspace(-0.3, 0.0, lumo + ne)
+    keep, ga = _grid_args(GRID)
+    mu = np.zeros((nh * ne, 3), np.complex128)
+    rb.ref_bse_dipoles(_p(psi.view(np.float64)), _p(ev), nh, ne, lumo, *ga, _p(mu.view(np.float64)))
+    mine = O.bse_dipoles(psi, nh, ne, lumo, GRID)
+    assert np.max(np.abs(mine - mu)) < 1e-12 * np.max(np.abs(mine))
