@@ -42,6 +42,13 @@ static void bjob_init(struct bjob *j, long nx, long ny, long nz, double dx, doub
   j->grid.dy = dy;
   j->grid.dz = dz;
   j->grid.dv = dx * dy * dz;
+  /* set by read_input (read.c:353) and init_elec_hole_kernel (init.c:132) */
+  j->grid.nx_1 = 1.0 / (double)nx;
+  j->grid.ny_1 = 1.0 / (double)ny;
+  j->grid.nz_1 = 1.0 / (double)nz;
+  j->grid.dkx = 2.0 * 3.14159265358979323846 / ((double)nx * dx);
+  j->grid.dky = 2.0 * 3.14159265358979323846 / ((double)ny * dy);
+  j->grid.dkz = 2.0 * 3.14159265358979323846 / ((double)nz * dz);
   j->grid.xmin = xmin;
   j->grid.ymin = ymin;
   j->grid.zmin = zmin;
@@ -131,4 +138,31 @@ void ref_bse_dipoles(double *psi_qp, double *eval_qp, long nh, long ne, long lum
   struct bjob j;
   bjob_init(&j, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, gx, gy, gz, nh, ne, lumo);
   calc_elec_dipole((xyz_st *)mu, (double complex *)psi_qp, eval_qp, &j.grid, &j.ist, &j.par, &j.flag);
+}
+
+void calc_mag_dipole(xyz_st *mag_dip, double complex *psi_qp, double *eig_vals, grid_st *grid, index_st *ist,
+                     par_st *par, flag_st *flag);
+void calc_optical_exc(double complex *bs_coeff, double *xton_ene, double *eig_vals, xyz_st *mu, xyz_st *m,
+                      index_st *ist, par_st *par);
+
+/* calc_mag_dipole (bse_cplx/dipole.c:160-331): m [n_h * n_e][3] complex;
+ * writes M0.dat into the working directory */
+void ref_bse_mag_dipoles(double *psi_qp, double *eval_qp, long nh, long ne, long lumo, long nx, long ny, long nz,
+                         double dx, double dy, double dz, double xmin, double ymin, double zmin, double *gx,
+                         double *gy, double *gz, double *m)
+{
+  struct bjob j;
+  bjob_init(&j, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, gx, gy, gz, nh, ne, lumo);
+  calc_mag_dipole((xyz_st *)m, (double complex *)psi_qp, eval_qp, &j.grid, &j.ist, &j.par, &j.flag);
+}
+
+/* calc_optical_exc (bse_cplx/optical.c:6-99): writes OS.dat, M.dat, rs.dat
+ * and bs-coeff-<j>.dat into the working directory */
+void ref_bse_optical(double *coeff, double *xton_ene, double *eval_qp, double *mu, double *m, long nh, long ne,
+                     long lumo)
+{
+  struct bjob j;
+  double g0 = 0;
+  bjob_init(&j, 1, 1, 1, 1, 1, 1, 0, 0, 0, &g0, &g0, &g0, nh, ne, lumo);
+  calc_optical_exc((double complex *)coeff, xton_ene, eval_qp, (xyz_st *)mu, (xyz_st *)m, &j.ist, &j.par);
 }

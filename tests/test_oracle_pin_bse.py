@@ -2,8 +2,9 @@
 (bse_cplx/ compiled from where it lies into oracle/_ref/libfbse_ref_bse.so with
 the project-written FFTW subset, LAPACKE forwarder and one-rank MPI; CPU):
 the bare and screened interactions, the direct and exchange kernels, the BSE
-solve with its exciton expectation values, and the electric transition
-dipoles, on smooth seeded spinor states."""
+solve with its exciton expectation values, the electric and magnetic
+transition dipoles and the optical outputs (OS.dat, M.dat), on smooth seeded
+spinor states."""
 import ctypes
 import glob
 import os
@@ -34,6 +35,8 @@ def rb():
     L.ref_bse_kernel.argtypes = [D] + [ctypes.c_long] * 3 + gargs + [D] * 4
     L.ref_bse_solve.argtypes = [D, D, D] + [ctypes.c_long] * 3 + [D, D]
     L.ref_bse_dipoles.argtypes = [D, D] + [ctypes.c_long] * 3 + gargs + [D]
+    L.ref_bse_mag_dipoles.argtypes = [D, D] + [ctypes.c_long] * 3 + gargs + [D]
+    L.ref_bse_optical.argtypes = [D] * 5 + [ctypes.c_long] * 3
     L.ref_set_lapack.argtypes = [ctypes.c_char_p]
     here = os.path.dirname(os.path.dirname(np.__file__))
     lap = glob.glob(os.path.join(here, "numpy.libs", "libscipy_openblas64_*.so"))
@@ -127,3 +130,36 @@ def test_bse_dipoles_match_reference(rb, tmp_path, monkeypatch):
     rb.ref_bse_dipoles(_p(psi.view(np.float64)), _p(ev), nh, ne, lumo, *ga, _p(mu.view(np.float64)))
     mine = O.bse_dipoles(psi, nh, ne, lumo, GRID)
     assert np.max(np.abs(mine - mu)) < 1e-12 * np.max(np.abs(mine))
+
+
+def test_bse_mag_dipoles_and_optical_match_reference(rb, tmp_path, monkeypatch):
+    """calc_mag_dipole (bse_cplx/dipole.c:160-331) against the oracle, and
+    calc_optical_exc (optical.c:6-99) on the reference's own exciton
+    coefficients: OS.dat's |mu|, E and (2/3) E |mu|^2 and M.dat's |m| from the
+    oracle's exciton dipoles"""
+    monkeypatch.chdir(tmp_path)
+    nh, ne, lumo = 3, 2, 4
+    psi = np.ascontiguousarray(qp_states(GRID, lumo + ne, 53))
+    ev = np.linspace(-0.3, 0.0, lumo + ne)
+    keep, ga = _grid_args(GRID)
+    m = np.zeros((nh * ne, 3), np.complex128)
+    rb.ref_bse_mag_dipoles(_p(psi.view(np.float64)), _p(ev), nh, ne, lumo, *ga, _p(m.view(np.float64)))
+    mine_m = O.bse_mag_dipoles(psi, nh, ne, lumo, GRID)
+    assert np.max(np.abs(mine_m - m)) < 1e-12 * np.max(np.abs(mine_m))
+    mu = O.bse_dipoles(psi, nh, ne, lumo, GRID)
+    _, _, dr, xr = _kernels(rb, GRID, psi, nh, ne, lumo, tmp_path, monkeypatch)
+    e, C, *_ = O.bse_solve(ev, nh, ne, lumo, dr, xr)
+    n = nh * ne
+    rb.ref_bse_optical(_p(np.ascontiguousarray(C).view(np.float64)), _p(e), _p(ev),
+                       _p(np.ascontiguousarray(mu).view(np.float64)), _p(np.ascontiguousarray(m).view(np.float64)),
+                       nh, ne, lumo)
+    os_rows = np.loadtxt(tmp_path / "OS.dat")
+    m_rows = np.loadtxt(tmp_path / "M.dat")
+    mx = O.bse_optical(C, mu, nh, ne)
+    mm = O.bse_optical(C, m, nh, ne)
+    osc = np.sum(np.abs(mx) ** 2, axis=1)
+    assert os_rows.shape[0] == m_rows.shape[0] == n
+    assert np.allclose(os_rows[:, 1], np.sqrt(osc), atol=2e-8)
+    assert np.allclose(os_rows[:, 2], e, atol=2e-8)
+    assert np.allclose(os_rows[:, 3], 2.0 / 3.0 * e * osc, atol=2e-8)
+    assert np.allclose(m_rows[:, 1], np.sqrt(np.sum(np.abs(mm) ** 2, axis=1)), atol=2e-8)
