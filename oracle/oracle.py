@@ -804,6 +804,30 @@ def bse_qp_ang_mom(psi_qp, nh, ne, lumo, grid: Grid):
     return S, Lm, L2, LS
 
 
+def bse_electron_ls_as_written(psi_qp, nh, ne, lumo, grid: Grid):
+    """The electron block of ldots as calc_qp_ang_mom_mtrx computes it
+    (bse_cplx/angular.c:582-604): its L.S loop sets jsg = ngrid once and never
+    advances it, so every term that should read the spin-down point jg reads
+    the first spin-down point.  Upper triangle with the diagonal from the loop,
+    strict lower triangle by conjugation (angular.c:614-631).  [ne^2] complex, row a, column b.
+    Only for pinning the reference; bse_qp_ang_mom holds the L.S sums."""
+    N, dv = grid.ngrid, grid.dv
+    out = np.zeros(ne * ne, np.complex128)
+    for a in range(ne):
+        pa = psi_qp[lumo + a]
+        Lx, Ly, Lz = (np.concatenate([u, d]) for u, d in zip(_l_prime(pa[:N], grid), _l_prime(pa[N:], grid)))
+        for b in range(a, ne):
+            pb = psi_qp[lumo + b]
+            up, d0 = pb[:N], pb[N]
+            c = np.conj
+            ls = (c(d0) * np.sum(Lx[:N]) + np.sum(c(up)) * Lx[N] + 1j * c(d0) * np.sum(Ly[:N])
+                  - 1j * np.sum(c(up)) * Ly[N] + np.sum(c(up) * Lz[:N]) - N * c(d0) * Lz[N])
+            out[a * ne + b] = 0.5 * ls * dv
+            if b > a:
+                out[b * ne + a] = np.conj(out[a * ne + b])
+    return out
+
+
 def filter_angular_stats(psis, grid: Grid):
     """calc_angular_exp (filter_mpi/angular.c:4-165) for complex spinor states
     (rows of psitot, (re, im) interleaved, up block then down block): per

@@ -166,3 +166,39 @@ void ref_bse_optical(double *coeff, double *xton_ene, double *eval_qp, double *m
   bjob_init(&j, 1, 1, 1, 1, 1, 1, 0, 0, 0, &g0, &g0, &g0, nh, ne, lumo);
   calc_optical_exc((double complex *)coeff, xton_ene, eval_qp, (xyz_st *)mu, (xyz_st *)m, &j.ist, &j.par);
 }
+
+void calc_qp_spin_mtrx(double complex *psi_qp, xyz_st *s_mom, grid_st *grid, index_st *ist, par_st *par);
+void calc_qp_ang_mom_mtrx(double complex *psi_qp, xyz_st *l_mom, double complex *l2_mom, double complex *ldots,
+                          grid_st *grid, index_st *ist, par_st *par);
+void calc_xton_spin_mtrx(double complex *bs_coeff, xyz_st *s_mom, index_st *ist, par_st *par, flag_st *flag,
+                         parallel_st *parallel);
+void calc_xton_ang_mom_mtrx(double complex *bs_coeff, xyz_st *s_mom, xyz_st *l_mom, double complex *l2_mom,
+                            double complex *ldots, index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+
+/* calc_qp_spin_mtrx + calc_qp_ang_mom_mtrx (bse_cplx/angular.c:7-690): the
+ * hole-hole then electron-electron blocks, s and l [nh^2 + ne^2][3] complex,
+ * l2 and ls [nh^2 + ne^2] complex; writes sx/sy/sz, lx/ly/lz, lsqr and ls
+ * .dat files into the working directory */
+void ref_bse_qp_ang_mom(double *psi_qp, long nh, long ne, long lumo, long nx, long ny, long nz, double dx, double dy,
+                        double dz, double xmin, double ymin, double zmin, double *gx, double *gy, double *gz,
+                        double *s, double *l, double *l2, double *ls)
+{
+  struct bjob j;
+  bjob_init(&j, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, gx, gy, gz, nh, ne, lumo);
+  calc_qp_spin_mtrx((double complex *)psi_qp, (xyz_st *)s, &j.grid, &j.ist, &j.par);
+  calc_qp_ang_mom_mtrx((double complex *)psi_qp, (xyz_st *)l, (double complex *)l2, (double complex *)ls, &j.grid,
+                       &j.ist, &j.par);
+}
+
+/* calc_xton_spin_mtrx + calc_xton_ang_mom_mtrx (bse_cplx/angular.c:692-1043)
+ * on exciton coefficients [n_xton][n_xton] (column n = exciton n); writes
+ * spins.dat, orbital.dat and couple.dat into the working directory */
+void ref_bse_xton_ang(double *coeff, double *s, double *l, double *l2, double *ls, long nh, long ne, long lumo)
+{
+  struct bjob j;
+  double g0 = 0;
+  bjob_init(&j, 1, 1, 1, 1, 1, 1, 0, 0, 0, &g0, &g0, &g0, nh, ne, lumo);
+  calc_xton_spin_mtrx((double complex *)coeff, (xyz_st *)s, &j.ist, &j.par, &j.flag, &j.pl);
+  calc_xton_ang_mom_mtrx((double complex *)coeff, (xyz_st *)s, (xyz_st *)l, (double complex *)l2,
+                         (double complex *)ls, &j.ist, &j.par, &j.flag, &j.pl);
+}

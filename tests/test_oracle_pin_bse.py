@@ -37,6 +37,8 @@ def rb():
     L.ref_bse_dipoles.argtypes = [D, D] + [ctypes.c_long] * 3 + gargs + [D]
     L.ref_bse_mag_dipoles.argtypes = [D, D] + [ctypes.c_long] * 3 + gargs + [D]
     L.ref_bse_optical.argtypes = [D] * 5 + [ctypes.c_long] * 3
+    L.ref_bse_qp_ang_mom.argtypes = [D] + [ctypes.c_long] * 3 + gargs + [D] * 4
+    L.ref_bse_xton_ang.argtypes = [D] * 5 + [ctypes.c_long] * 3
     L.ref_set_lapack.argtypes = [ctypes.c_char_p]
     here = os.path.dirname(os.path.dirname(np.__file__))
     lap = glob.glob(os.path.join(here, "numpy.libs", "libscipy_openblas64_*.so"))
@@ -163,3 +165,54 @@ def test_bse_mag_dipoles_and_optical_match_reference(rb, tmp_path, monkeypatch):
     assert np.allclose(os_rows[:, 2], e, atol=2e-8)
     assert np.allclose(os_rows[:, 3], 2.0 / 3.0 * e * osc, atol=2e-8)
     assert np.allclose(m_rows[:, 1], np.sqrt(np.sum(np.abs(mm) ** 2, axis=1)), atol=2e-8)
+
+
+def test_bse_spin_and_angular_matrices_match_reference(rb, tmp_path, monkeypatch):
+    """calc_qp_spin_mtrx and calc_qp_ang_mom_mtrx (bse_cplx/angular.c:7-690)
+    against the oracle's quasiparticle s, l, l^2 and l.s matrices; then
+    calc_xton_spin_mtrx and calc_xton_ang_mom_mtrx (angular.c:692-1043) on the
+    reference's matrices and the oracle's exciton coefficients: spins.dat,
+    orbital.dat and couple.dat against the oracle's exciton sums to their
+    printed digits.  The electron block of <L.S> is the reference's loop as
+    written (its spin-down index stays at the first point), which the oracle
+    restates separately; the library computes the L.S sums for both blocks."""
+    monkeypatch.chdir(tmp_path)
+    nh, ne, lumo = 3, 2, 4
+    psi = np.ascontiguousarray(qp_states(GRID, lumo + ne, 67))
+    keep, ga = _grid_args(GRID)
+    nq = nh * nh + ne * ne
+    s = np.zeros((nq, 3), np.complex128)
+    l = np.zeros((nq, 3), np.complex128)
+    l2 = np.zeros(nq, np.complex128)
+    ls = np.zeros(nq, np.complex128)
+    rb.ref_bse_qp_ang_mom(_p(psi.view(np.float64)), nh, ne, lumo, *ga, *[_p(a.view(np.float64)) for a in (s, l, l2, ls)])
+    S, Lm, L2, LS = O.bse_qp_ang_mom(psi, nh, ne, lumo, GRID)
+    hh = nh * nh
+    for mine, ref in ((S, s), (Lm, l), (L2, l2), (LS[:hh], ls[:hh])):
+        assert np.max(np.abs(mine - ref)) < 1e-12 * max(1.0, np.max(np.abs(ref)))
+    # the electron L.S loop (angular.c:582-604) never advances its spin-down
+    # index: the reference's numbers are that loop as written, not the L.S sums
+    quirk = O.bse_electron_ls_as_written(psi, nh, ne, lumo, GRID)
+    assert np.max(np.abs(quirk - ls[hh:])) < 1e-12 * max(1.0, np.max(np.abs(quirk)))
+    assert np.max(np.abs(LS[hh:] - ls[hh:])) > 1e-3
+    ev = np.linspace(-0.3, 0.0, lumo + ne)
+    _, _, dr, xr = _kernels(rb, GRID, psi, nh, ne, lumo, tmp_path, monkeypatch)
+    e, C, *_ = O.bse_solve(ev, nh, ne, lumo, dr, xr)
+    C = np.ascontiguousarray(C)
+    rb.ref_bse_xton_ang(_p(C.view(np.float64)), *[_p(a.view(np.float64)) for a in (s, l, l2, ls)], nh, ne, lumo)
+    # both sides on the reference's own matrices (its electron L.S included)
+    spin, stot, orb, otot, lstot = O.xton_ang_stats(C, s, l, l2, ls, nh, ne)
+    n = nh * ne
+    def rows(name):  # "(imaginary part)" columns read as plain numbers
+        return np.array([[float(t) for t in line.replace("(", " ").replace(")", " ").split()]
+                         for line in open(tmp_path / name)])
+
+    sp, ob, cp = rows("spins.dat"), rows("orbital.dat"), rows("couple.dat")
+    assert sp.shape == (n, 9) and ob.shape == (n, 6) and cp.shape == (n, 3)
+    # spins.dat: %.5g of Re/Im <S_d>, then 1.5 + 2 Re(sum), (2 Im(sum))
+    want = np.column_stack([spin.real[:, 0], spin.imag[:, 0], spin.real[:, 1], spin.imag[:, 1],
+                            spin.real[:, 2], spin.imag[:, 2], 1.5 + 2 * stot.real, 2 * stot.imag])
+    assert np.allclose(sp[:, 1:], want, rtol=1e-4, atol=1e-9)
+    # orbital.dat and couple.dat: %.5f
+    assert np.allclose(ob[:, 1:], np.column_stack([orb.real, otot.real, otot.imag]), atol=6e-6)
+    assert np.allclose(cp[:, 1:], np.column_stack([lstot.real, lstot.imag]), atol=6e-6)
