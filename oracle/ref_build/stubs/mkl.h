@@ -4,6 +4,7 @@
 #include <stdlib.h>
 typedef struct { double real; double imag; } MKL_Complex16;
 static inline void mkl_set_num_threads(int n) { (void)n; }
+static inline void mkl_set_dynamic(int n) { (void)n; }
 /* the LAPACKE row-major interface the BSE solve uses (bse_cplx/diag.c:38),
  * ILP64 as the reference builds it; defined in lapack_shim.c */
 typedef long long lapack_int;
