@@ -74,6 +74,17 @@ int fbse_radial_projectors(double dx, double rcut, int kind, double lam1, double
 /* the init_NL_projectors table: fbse_build_nlc (on the GPU, declared in
  * include/fbse.h) */
 
+/* NL spectral bounds of the table (init.c:1095-1130) */
+void fbse_nl_bounds(long nat, long npts, int nproj, const long *nl, const double *y1, const double *nlp,
+                    const int *sgn, double dv, double *lam_min, double *lam_max);
+
+/* spectrum range rule of get_energy_range (energy.c:302-369): approx = 1
+ * builds [Emin, Emax] from Vmax_local, KE_max and the projector pads; both
+ * then get the inflation.  emin / emax in (approx = 0: the iterated
+ * extremes) and out. */
+void fbse_energy_range_rule(int approx, int so, int nl, double vmin_loc, double vmax_loc, double ke_max,
+                            double lam_min, double lam_max, double *emin, double *emax);
+
 /* outputs (filter_mpi/write.c:263-299, save.c:446-503) */
 int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n);
 int fbse_write_psi(const char *path, const double *psi, long n_doubles);

@@ -311,7 +311,7 @@ int main(void)
   memset(&pd, 0, sizeof pd);
   long *nl = NULL;
   int *jx = NULL, *sgn = NULL;
-  double *y1 = NULL, *sop = NULL, *nlp = NULL, nl_lam_min = 0.0;
+  double *y1 = NULL, *sop = NULL, *nlp = NULL, nl_lam_min = 0.0, nl_lam_max = 0.0;
   if (p.so || p.nl) {
     const int np = FBSE_NPROJ;
     const long N = FBSE_PROJ_LEN;
@@ -362,26 +362,8 @@ int main(void)
                        &npts, &nl, &jx, &y1, &sop, &nlp))
       die("projector table", NULL);
     printf("projectors: %ld atoms, %ld grid points per sphere\n", nat, npts);
-    if (p.nl) {
-      /* NL spectral bounds (filter_mpi/init.c:1095-1130) for the range rule */
-      const double dv = p.dx * p.dy * p.dz;
-      double lmin = 0.0;
-      for (long a = 0; a < nat; a++)
-        for (int q = 0; q < np; q++) {
-          double gm[3] = {0, 0, 0};
-          for (long g = 0; g < nl[a]; g++) {
-            const long e = a * npts + g;
-            const double b2 = nlp[e * np + q] * nlp[e * np + q];
-            for (int m = 0; m < 3; m++) gm[m] += b2 * (y1[e * 6 + 2 * m] * y1[e * 6 + 2 * m] +
-                                                       y1[e * 6 + 2 * m + 1] * y1[e * 6 + 2 * m + 1]);
-          }
-          for (int m = 0; m < 3; m++) {
-            const double l = (double)sgn[a * np + q] * dv * gm[m];
-            if (l < lmin) lmin = l;
-          }
-        }
-      nl_lam_min = lmin;
-    }
+    if (p.nl) /* NL spectral bounds (filter_mpi/init.c:1095-1130) for the range rule */
+      fbse_nl_bounds(nat, npts, np, nl, y1, nlp, sgn, p.dx * p.dy * p.dz, &nl_lam_min, &nl_lam_max);
     pd.n_atoms = nat;
     pd.npts = npts;
     pd.nproj = np;
@@ -436,26 +418,15 @@ int main(void)
     host_psi = NULL;
   } else {
     /* energy range (get_energy_range, filter_mpi/energy.c:169-379) */
-    double emin, emax;
-    if (p.approx_energy_range) {
-      emin = -0.8; /* energy.c:307-308 */
-      emax = vmax_loc + p.ke_max;
-      if (p.so) emax += 3.5;
-      if (p.nl && nl_lam_min < 0.0) emin += 1.15 * nl_lam_min;
-    } else {
+    double emin = 0.0, emax = 0.0;
+    if (!p.approx_energy_range) {
       long iters = 0;
       check(ctx, fbse_energy_range(ctx, -874917403, 1500, &emin, &emax, &iters), "energy range");
       printf("energy range: Emin %g, Emax %g (%ld iterations)\n", emin, emax, iters);
     }
-    if (p.nl && !p.so && nl_lam_min < 0.0) { /* energy.c:350-362 */
-      emax *= 1.05;
-      emin -= 0.1 * fabs(emin);
-      const double weyl = 1.05 * (vmin_loc + nl_lam_min);
-      if (emin > weyl) emin = weyl;
-    } else {
-      emax *= 1.2;
-      emin -= 0.2 * fabs(emin);
-    }
+    /* the approximate range with its projector pads, then the inflation (energy.c:302-369) */
+    fbse_energy_range_rule(p.approx_energy_range, p.so, p.nl, vmin_loc, vmax_loc, p.ke_max, nl_lam_min, nl_lam_max,
+                           &emin, &emax);
     const double de = emax - emin;
     printf("Emin = %g, Emax = %g, dE = %g\n", emin, emax, de);
 

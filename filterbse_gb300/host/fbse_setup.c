@@ -315,6 +315,66 @@ void fbse_grid_axis(long n, double lo, double d, double *out)
 
 double fbse_r_nlcut2(double dx) { return 1.5 + 6.0 * log(10.0) + 3.0 * dx; }
 
+/* The extreme single-channel eigenvalues of the NL (KB) operator: each
+ * (atom, projector, m) channel sgn dv |b Y_1m><b Y_1m| has eigenvalue
+ * sgn dv sum_points b^2 |Y_1m|^2; lam_min / lam_max are the most negative /
+ * most positive of them, 0 when none is (init.c:1095-1130). */
+void fbse_nl_bounds(long nat, long npts, int nproj, const long *nl, const double *y1, const double *nlp,
+                    const int *sgn, double dv, double *lam_min, double *lam_max)
+{
+  double lo = 0.0, hi = 0.0;
+  for (long a = 0; a < nat; a++)
+    for (int q = 0; q < nproj; q++) {
+      double gm[3] = {0.0, 0.0, 0.0};
+      for (long g = 0; g < nl[a]; g++) {
+        const long e = a * npts + g;
+        const double b2 = nlp[e * nproj + q] * nlp[e * nproj + q];
+        for (int m = 0; m < 3; m++)
+          gm[m] += b2 * (y1[e * 6 + 2 * m] * y1[e * 6 + 2 * m] + y1[e * 6 + 2 * m + 1] * y1[e * 6 + 2 * m + 1]);
+      }
+      for (int m = 0; m < 3; m++) {
+        const double l = (double)sgn[a * nproj + q] * dv * gm[m];
+        if (l < lo) lo = l;
+        if (l > hi) hi = l;
+      }
+    }
+  *lam_min = lo;
+  *lam_max = hi;
+}
+
+/* The spectrum range rule of get_energy_range (energy.c:302-369).  approx = 1:
+ * [-0.8, Vmax + KE_max], + 3.5 on Emax with spin-orbit, and with NL projectors
+ * 1.15 lam_max onto Emax and 1.15 lam_min onto Emin (each only with its sign).
+ * approx = 0: emin / emax come in as the iterated extremes.  Then the
+ * inflation: NL without SO and lam_min < 0: Emax x 1.05, Emin - 0.1 |Emin|,
+ * clamped to 1.05 (Vmin_local + lam_min); otherwise Emax x 1.2,
+ * Emin - 0.2 |Emin|. */
+void fbse_energy_range_rule(int approx, int so, int nl, double vmin_loc, double vmax_loc, double ke_max,
+                            double lam_min, double lam_max, double *emin, double *emax)
+{
+  double lo = *emin, hi = *emax;
+  if (approx) {
+    lo = -0.8;
+    hi = vmax_loc + ke_max;
+    if (so) hi += 3.5;
+    if (nl) {
+      if (lam_max > 0.0) hi += 1.15 * lam_max;
+      if (lam_min < 0.0) lo += 1.15 * lam_min;
+    }
+  }
+  if (nl && !so && lam_min < 0.0) {
+    hi *= 1.05;
+    lo -= 0.1 * fabs(lo);
+    const double weyl = 1.05 * (vmin_loc + lam_min);
+    if (lo > weyl) lo = weyl;
+  } else {
+    hi *= 1.2;
+    lo -= 0.2 * fabs(lo);
+  }
+  *emin = lo;
+  *emax = hi;
+}
+
 /* ---------------------------------------------------------------------------
  * radial projectors (filter_mpi/projectors.c:12-228).  The reference forms
  * the PROJ_LEN x PROJ_LEN matrix

@@ -334,8 +334,10 @@ def r_nlcut2(dx: float) -> float:
 
 
 def nlc_table(grid: Grid, coords, so_par, so_tab, nl_tabs, nl_sgn, nproj=NPROJ) -> Projectors:
-    """init_NL_projectors (filter_mpi/init.c:848-1135 region, body 508-589) over the
-    projector atoms (coords rows), using the reference's EPSDX-shifted Y_1m."""
+    """init_NL_projectors (filter_mpi/init.c:848-1060) over the projector atoms
+    (coords rows), using the reference's EPSDX-shifted Y_1m; the points per
+    atom are bounded by the largest sphere count (build_grid_ksqr,
+    init.c:353-393)."""
     rc2 = r_nlcut2(grid.dx)
     gx, gy, gz = grid.axes()
     nat = len(coords)
@@ -480,6 +482,35 @@ def energy_range(sysm: System, max_iter: int = 1500, seed: int = -874917403):
         emax = energy(psi, sysm)
         i += 1
     return inflate_range(sysm, emin, emax)
+
+
+def nl_bounds(proj: "Projectors", dv: float):
+    """The NL spectral-bound estimate of init_NL_projectors
+    (filter_mpi/init.c:1095-1130): per (atom, projector, m) channel
+    lam = sgn dv sum_points NL_proj^2 |Y_1m|^2; (min(0, lam...), max(0, lam...))."""
+    lo = hi = 0.0
+    for a in range(len(proj.nl)):
+        sl = slice(a * proj.npts, a * proj.npts + int(proj.nl[a]))
+        b2 = proj.nlp.reshape(-1, proj.nproj)[sl] ** 2
+        y = proj.y1.reshape(-1, 3, 2)[sl]
+        y2 = y[..., 0] ** 2 + y[..., 1] ** 2
+        for q in range(proj.nproj):
+            for m in range(3):
+                lam = float(proj.sgn[a * proj.nproj + q]) * dv * float(np.sum(b2[:, q] * y2[:, m]))
+                lo, hi = min(lo, lam), max(hi, lam)
+    return lo, hi
+
+
+def approx_energy_range(vmax_loc: float, ke_max: float, so: bool, nl: bool, lam_min: float, lam_max: float):
+    """The approxEnergyRange branch of get_energy_range (filter_mpi/energy.c:302-335):
+    [-0.8, Vmax + KE_max], + 3.5 on Emax with SO, the NL pads 1.15 lam."""
+    emin, emax = -0.8, vmax_loc + ke_max
+    if so:
+        emax += 3.5
+    if nl:
+        emax += 1.15 * lam_max if lam_max > 0.0 else 0.0
+        emin += 1.15 * lam_min if lam_min < 0.0 else 0.0
+    return emin, emax
 
 
 def inflate_range(sysm: System, emin: float, emax: float, nl_lambda_min: float = 0.0):

@@ -256,3 +256,119 @@ void ref_energy_range(long nx, long ny, long nz, int nspin, int so, int nl, doub
   free(phi);
   job_free(&j);
 }
+
+void gen_SO_projectors(double dx, double rcut, long nproj, double *projectors, double *vr);
+void init_NL_projectors(nlc_st *nlc, long *nl, double *SO_projectors, grid_st *grid, xyz_st *R, atom_info *atom,
+                        index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+
+/* gen_SO_projectors (projectors.c:12-84) on init_NL_projectors' radial grid
+ * r_j = j sqrt(rc2) / PROJ_LEN: so_tab [nproj][PROJ_LEN]; writes its
+ * projector files into the working directory */
+void ref_so_projectors(double dx, double rc2, long nproj, double *so_tab)
+{
+  double *vr = malloc(PROJ_LEN * sizeof(double));
+  const double dr = sqrt(rc2) / (double)PROJ_LEN;
+  for (long j = 0; j < PROJ_LEN; j++) vr[j] = (double)j * dr;
+  gen_SO_projectors(dx, sqrt(rc2), nproj, so_tab, vr);
+  free(vr);
+}
+
+/* init_NL_projectors (init.c:848-1135) with the NL radial projectors made on
+ * the fly by gen_nlc_projectors (projectors.c:87-228; NL_par per atom) and the
+ * given SO radial projectors, non-periodic, at one rank.  Outputs the table
+ * in the library's layout (nl[nat]; per entry e = atom * npts + point: jxyz,
+ * y1 as (re, im) x 3, proj and NL_proj x nproj; sgn [nat][nproj]) and
+ * lam = {NL_lambda_min, NL_lambda_max}.  Writes list_NL_grid.dat and the
+ * projector files into the working directory. */
+void ref_nl_projectors(long nx, long ny, long nz, double dx, double dy, double dz, double *gx, double *gy, double *gz,
+                       long nat, const double *xyz, const double *so_par, const double *nl_par, double *so_tab,
+                       double rc2, long nproj, long npts, long *nl, int *jxyz, double *y1, double *proj, double *nlp,
+                       int *sgn, double *lam)
+{
+  grid_st grid;
+  index_st ist;
+  par_st par;
+  flag_st flag;
+  parallel_st pl;
+  memset(&grid, 0, sizeof grid);
+  memset(&ist, 0, sizeof ist);
+  memset(&par, 0, sizeof par);
+  memset(&flag, 0, sizeof flag);
+  memset(&pl, 0, sizeof pl);
+  grid.nx = nx;
+  grid.ny = ny;
+  grid.nz = nz;
+  grid.ngrid = nx * ny * nz;
+  grid.dx = dx;
+  grid.dy = dy;
+  grid.dz = dz;
+  grid.dv = dx * dy * dz;
+  grid.x = gx;
+  grid.y = gy;
+  grid.z = gz;
+  ist.n_NL_atoms = nat;
+  ist.n_NL_gridpts = npts;
+  ist.nproj = nproj;
+  ist.n_l_ang_mom = 3;
+  par.R_NLcut2 = rc2;
+  pl.nthreads = 1;
+  pl.mpi_rank = 1; /* quiet */
+  xyz_st *R = calloc(nat, sizeof(xyz_st));
+  atom_info *atom = calloc(nat, sizeof(atom_info));
+  for (long a = 0; a < nat; a++) {
+    R[a].x = xyz[3 * a];
+    R[a].y = xyz[3 * a + 1];
+    R[a].z = xyz[3 * a + 2];
+    atom[a].Zval = 1;
+    atom[a].SO_par = so_par[a];
+    atom[a].NL_par[0] = nl_par[2 * a];
+    atom[a].NL_par[1] = nl_par[2 * a + 1];
+  }
+  nlc_st *nlc = calloc(nat * npts, sizeof(nlc_st));
+  init_NL_projectors(nlc, nl, so_tab, &grid, R, atom, &ist, &par, &flag, &pl);
+  for (long a = 0; a < nat; a++) {
+    for (long p = 0; p < nproj; p++) sgn[a * nproj + p] = nlc[a * npts].NL_proj_sign[p];
+    for (long g = 0; g < nl[a]; g++) {
+      const long e = a * npts + g;
+      jxyz[e] = (int)nlc[e].jxyz;
+      for (int m = 0; m < 3; m++) {
+        y1[e * 6 + 2 * m] = nlc[e].y1[m].re;
+        y1[e * 6 + 2 * m + 1] = nlc[e].y1[m].im;
+      }
+      for (long p = 0; p < nproj; p++) {
+        proj[e * nproj + p] = nlc[e].proj[p];
+        nlp[e * nproj + p] = nlc[e].NL_proj[p];
+      }
+    }
+  }
+  lam[0] = par.NL_lambda_min;
+  lam[1] = par.NL_lambda_max;
+  free(nlc);
+  free(atom);
+  free(R);
+}
+
+/* get_energy_range's approxEnergyRange branch and range inflation
+ * (energy.c:302-369): the local potential's Vmin / Vmax, KE_max and the NL
+ * bounds in, Vmin (= Emin) and dE out */
+void ref_energy_range_approx(int so, int nl, double vmin_loc, double vmax_loc, double ke_max, double lam_min,
+                             double lam_max, double *emin, double *de)
+{
+  struct job j;
+  job_init(&j, 1, 1, 1, 1, 1, so, nl, 0, 0, 0, NULL, NULL, NULL, NULL, NULL, 1.0);
+  j.flag.approxEnergyRange = 1;
+  j.par.Vmin = vmin_loc;
+  j.par.Vmax = vmax_loc;
+  j.par.KE_max = ke_max;
+  j.par.NL_lambda_min = lam_min;
+  j.par.NL_lambda_max = lam_max;
+  grid_st grid;
+  memset(&grid, 0, sizeof grid);
+  grid.nx = grid.ny = grid.nz = 1;
+  grid.ngrid = 1;
+  grid.dv = 1.0;
+  get_energy_range(NULL, NULL, NULL, &grid, NULL, j.nlc, NULL, NULL, &j.ist, &j.par, &j.flag, &j.pl);
+  *emin = j.par.Vmin;
+  *de = j.par.dE;
+  job_free(&j);
+}

@@ -1,9 +1,9 @@
 /* Test-only: the functions that the reference files compiled into
  * oracle/_ref/libfbse_ref_fft.so call in files that are not compiled (file
- * readers, strain, LAPACK-based projector generation, MPI, the periodic
- * k-point path).  The pinned single-rank, non-periodic paths (kinetic,
- * p_hamiltonian, filter_cycle, ortho_cplx, diag_H, calc_sigma_E,
- * calc_angular_exp) never reach them; these definitions only satisfy the
+ * readers, strain, MPI, the periodic k-point path).  The pinned single-rank,
+ * non-periodic paths (kinetic, p_hamiltonian, filter_cycle, ortho_cplx,
+ * diag_H, calc_sigma_E, calc_angular_exp, get_energy_range,
+ * init_NL_projectors) never reach them; these definitions only satisfy the
  * linker and stop the process loudly if one is ever called. */
 #include <stdio.h>
 #include <stdlib.h>
@@ -23,8 +23,6 @@ void MPI_Send(void) { unreachable("MPI_Send"); }
 void assign_atom_number(void) { unreachable("assign_atom_number"); }
 void calc_strain_scale(void) { unreachable("calc_strain_scale"); }
 void e_ikr(void) { unreachable("e_ikr"); }
-void gen_SO_projectors(void) { unreachable("gen_SO_projectors"); }
-void gen_nlc_projectors(void) { unreachable("gen_nlc_projectors"); }
 void hamiltonian_k(void) { unreachable("hamiltonian_k"); }
 void kinetic_k(void) { unreachable("kinetic_k"); }
 void p_hamiltonian_k(void) { unreachable("p_hamiltonian_k"); }

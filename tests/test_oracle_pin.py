@@ -397,3 +397,105 @@ def test_energy_range_matches_reference(ref_fft, tmp_path, monkeypatch):
     print(f"\n[reference energy range] Vmin {vmin.value:.10f} dE {de.value:.10f}; oracle {mine_vmin:.10f} {mine_de:.10f}")
     assert abs(vmin.value - mine_vmin) < 1e-9 * abs(mine_vmin)
     assert abs(de.value - mine_de) < 1e-9 * mine_de
+
+
+def _align(mine, ref):
+    """mine with each row's sign chosen to match ref (eigenvector phase)"""
+    s = np.sign(np.sum(mine * ref, axis=-1, keepdims=True))
+    s[s == 0] = 1.0
+    return mine * s
+
+
+def test_projector_table_and_nl_bounds_match_reference(ref_fft, tmp_path, monkeypatch):
+    """gen_SO_projectors (projectors.c:12-84) against the oracle's radial SO
+    projectors (up to sign); then init_NL_projectors (init.c:848-1135) with the
+    NL radial projectors made on the fly by gen_nlc_projectors
+    (projectors.c:87-228; one atom with NL_par 0): point counts, grid indices,
+    Y_1m, SO projectors, NL projectors (up to sign per atom and projector),
+    signs, and the NL spectral bounds (init.c:1095-1130) against the oracle's
+    table and bounds and the library's host fbse_nl_bounds"""
+    import filterbse_gb300 as F
+    lap = _numpy_lapack()
+    if lap is None or not ref_fft.ref_set_lapack(lap.encode()):
+        pytest.skip("numpy's ILP64 LAPACK is not available")
+    monkeypatch.chdir(tmp_path)  # the reference's projector files
+    LP, IP = ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_int)
+    ref_fft.ref_so_projectors.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_long, D]
+    ref_fft.ref_nl_projectors.argtypes = ([ctypes.c_long] * 3 + [ctypes.c_double] * 3 + [D] * 3 + [ctypes.c_long] +
+                                          [D] * 4 + [ctypes.c_double, ctypes.c_long, ctypes.c_long, LP, IP, D, D, D,
+                                                     IP, D])
+    g = O.Grid(18, 17, 16, 0.8, 0.8, 0.8, -6.8, -6.4, -6.0)
+    rc2 = O.r_nlcut2(g.dx)
+    so_ref = np.zeros((O.NPROJ, O.PROJ_LEN))
+    ref_fft.ref_so_projectors(g.dx, rc2, O.NPROJ, _p(so_ref))
+    so_me = O.so_radial(g.dx, np.sqrt(rc2))
+    assert np.max(np.abs(_align(so_me, so_ref) - so_ref)) < 1e-9 * np.max(np.abs(so_ref))
+
+    coords = np.array([[0.3, -0.2, 0.1], [-2.1, 1.7, 0.4], [2.4, 0.9, -1.8]])
+    so_par = np.array([0.4, 0.0, 1.3])
+    nl_par = np.array([[-0.35, 0.6], [0.0, 0.0], [0.5, -0.2]])
+    tabs, sgns = zip(*(O.nl_radial(g.dx, np.sqrt(rc2), *p) for p in nl_par))
+    me = O.nlc_table(g, coords, so_par, so_ref, np.array(tabs), np.concatenate(sgns))
+    nat, npts, np_ = len(coords), me.npts, O.NPROJ
+    nl = np.zeros(nat, np.int64)
+    jx = np.zeros(nat * npts, np.int32)
+    y1 = np.zeros(nat * npts * 6)
+    pr = np.zeros(nat * npts * np_)
+    nlp = np.zeros(nat * npts * np_)
+    sgn = np.zeros(nat * np_, np.int32)
+    lam = np.zeros(2)
+    axes = [np.ascontiguousarray(a) for a in g.axes()]
+    ref_fft.ref_nl_projectors(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, *[_p(a) for a in axes], nat,
+                              _p(np.ascontiguousarray(coords)), _p(so_par), _p(np.ascontiguousarray(nl_par)),
+                              _p(so_ref), rc2, np_, npts, _p(nl, LP), _p(jx, IP), _p(y1), _p(pr), _p(nlp),
+                              _p(sgn, IP), _p(lam))
+    assert np.array_equal(nl, me.nl) and nl.max() == npts
+    assert np.array_equal(sgn, me.sgn)
+    assert list(sgn[np_:2 * np_]) == [0] * np_  # NL_par 0: zero projectors, sign 0 (projectors.c:113-125)
+    for a in range(nat):
+        sl = slice(a * npts, a * npts + int(nl[a]))
+        assert np.array_equal(jx[sl], me.jxyz[sl])
+        assert np.max(np.abs(y1.reshape(-1, 6)[sl] - me.y1.reshape(-1, 6)[sl])) < 1e-15
+        assert np.max(np.abs(pr.reshape(-1, np_)[sl] - me.proj.reshape(-1, np_)[sl])) < 1e-13
+        r, m = nlp.reshape(-1, np_)[sl].T, me.nlp.reshape(-1, np_)[sl].T
+        assert np.max(np.abs(_align(m, r) - r)) <= 1e-9 * max(1.0, np.max(np.abs(r)))
+    lo, hi = O.nl_bounds(me, g.dv)
+    assert lam[0] < 0.0 < lam[1]
+    assert abs(lo - lam[0]) < 1e-9 * abs(lam[0]) and abs(hi - lam[1]) < 1e-9 * abs(lam[1])
+    L = F.load()
+    L.fbse_nl_bounds.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_int, LP, D, D, IP, ctypes.c_double, D, D]
+    L.fbse_nl_bounds.restype = None
+    hlo, hhi = ctypes.c_double(), ctypes.c_double()
+    L.fbse_nl_bounds(nat, npts, np_, _p(nl, LP), _p(y1), _p(nlp), _p(sgn, IP), g.dv, ctypes.byref(hlo),
+                     ctypes.byref(hhi))
+    assert abs(hlo.value - lam[0]) <= 1e-14 * abs(lam[0]) and abs(hhi.value - lam[1]) <= 1e-14 * abs(lam[1])
+
+
+@pytest.mark.parametrize("so,nl,lmin,lmax", [(0, 1, -0.7, 0.9), (1, 1, -0.7, 0.9), (0, 1, 0.0, 0.4),
+                                             (0, 1, -0.3, 0.0), (1, 0, 0.0, 0.0), (0, 0, 0.0, 0.0)])
+def test_approx_energy_range_matches_reference(ref_fft, so, nl, lmin, lmax):
+    """get_energy_range's approxEnergyRange branch with the projector pads and
+    the range inflation (energy.c:302-369) against the library's host
+    fbse_energy_range_rule and the oracle; the rule's iterated branch (approx
+    = 0) against the oracle's inflate_range"""
+    import types
+    import filterbse_gb300 as F
+    ref_fft.ref_energy_range_approx.argtypes = [ctypes.c_int] * 2 + [ctypes.c_double] * 5 + [D, D]
+    vmin, vmax, ke = -1.3, 0.9, 7.5
+    e, de = ctypes.c_double(), ctypes.c_double()
+    ref_fft.ref_energy_range_approx(so, nl, vmin, vmax, ke, lmin, lmax, ctypes.byref(e), ctypes.byref(de))
+    L = F.load()
+    L.fbse_energy_range_rule.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 5 + [D, D]
+    L.fbse_energy_range_rule.restype = None
+    lo, hi = ctypes.c_double(), ctypes.c_double()
+    L.fbse_energy_range_rule(1, so, nl, vmin, vmax, ke, lmin, lmax, ctypes.byref(lo), ctypes.byref(hi))
+    assert lo.value == e.value and abs((hi.value - lo.value) - de.value) <= 1e-15 * de.value
+    sysm = types.SimpleNamespace(nlflag=bool(nl), so=bool(so), pot=np.array([vmin, vmax]))
+    oe, oE = O.approx_energy_range(vmax, ke, bool(so), bool(nl), lmin, lmax)
+    emin_i, de_i, _, _ = O.inflate_range(sysm, oe, oE, lmin)
+    assert emin_i == e.value and abs(de_i - de.value) <= 1e-15 * de.value
+    # the iterated branch: the extremes come in, only the inflation applies
+    lo.value, hi.value = -0.91, 4.37
+    L.fbse_energy_range_rule(0, so, nl, vmin, vmax, ke, lmin, lmax, ctypes.byref(lo), ctypes.byref(hi))
+    emin_i, de_i, _, _ = O.inflate_range(sysm, -0.91, 4.37, lmin)
+    assert lo.value == emin_i and abs((hi.value - lo.value) - de_i) <= 1e-15 * de_i
