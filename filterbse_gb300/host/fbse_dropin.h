@@ -53,6 +53,13 @@ int fbse_read_bse_params(const char *path, fbse_bse_params *p, char *err, size_t
 int fbse_read_conf(const char *path, long *natoms, double **xyz, int **types, char names[][8], int *ntypes,
                    char *err, size_t errlen);
 
+/* 1 for the ligand labels (P1-P4, PC5, PC6, PR1-3, PA1-3, C1-3), which carry
+ * no SO / NL projectors */
+int fbse_is_ligand(const char *atyp);
+
+/* SO_<atyp>.par from the working directory: SO_par and NL_par[2]; 0 or -1 */
+int fbse_read_so_params(const char *atyp, double *so_par, double *nl_par, char *err, size_t errlen);
+
 /* two-column table (r, V): returns the number of rows (or -1) */
 long fbse_read_table(const char *path, double **r, double **v);
 

@@ -44,15 +44,6 @@ static void check(fbse_ctx *c, int rc, const char *what)
   }
 }
 
-static int is_ligand(const char *t)
-{ /* is_ligand, filter_mpi/read.c:2425-2447 */
-  static const char *lig[] = {"P1", "P2", "P3", "P4", "PC5", "PC6", "PR1", "PR2", "PR3",
-                              "PA1", "PA2", "PA3", "C1", "C2", "C3", NULL};
-  for (int i = 0; lig[i]; i++)
-    if (!strcmp(t, lig[i])) return 1;
-  return 0;
-}
-
 static void save_output(const char *path, const fbse_filter_params *p, long natoms, const double *xyz,
                         int ntypes, long nx, long ny, long nz, double dx, double dy, double dz, const double *gx,
                         const double *gy, const double *gz, double xmin, double ymin, double zmin, int nspin,
@@ -319,19 +310,12 @@ int main(void)
     double so_par[FBSE_MAX_TYPES], lam[FBSE_MAX_TYPES][2];
     for (int t = 0; t < ntypes; t++) {
       so_par[t] = lam[t][0] = lam[t][1] = 0.0;
-      if (is_ligand(names[t])) continue;
-      char path[64];
-      snprintf(path, sizeof path, "SO_%s.par", names[t]);
-      FILE *f = fopen(path, "r");
-      if (!f) die("No SO(+NL) pot found in", path);
-      if (fscanf(f, "%lg %*g", &so_par[t]) != 1 || fscanf(f, "%lg %*g", &lam[t][0]) != 1 ||
-          fscanf(f, "%lg %*g", &lam[t][1]) != 1)
-        die("cannot read", path);
-      fclose(f);
+      if (fbse_is_ligand(names[t])) continue;
+      if (fbse_read_so_params(names[t], &so_par[t], lam[t], err, sizeof err)) die(err, NULL);
     }
     long nat = 0;
     for (long a = 0; a < natoms; a++)
-      if (!is_ligand(names[atype[a]])) nat++;
+      if (!fbse_is_ligand(names[atype[a]])) nat++;
     double *pxyz = malloc(3 * (nat ? nat : 1) * sizeof(double)), *psp = malloc((nat ? nat : 1) * sizeof(double));
     double *so_tab = calloc(np * N, sizeof(double));
     double *nl_tab = calloc((size_t)(nat ? nat : 1) * np * N, sizeof(double));
@@ -341,14 +325,14 @@ int main(void)
     if (p.so && fbse_radial_projectors(p.dx, rc, 0, 0.0, 0.0, np, so_tab, NULL)) die("SO projectors", NULL);
     if (p.nl)
       for (int t = 0; t < ntypes; t++)
-        if (!is_ligand(names[t]) &&
+        if (!fbse_is_ligand(names[t]) &&
             fbse_radial_projectors(p.dx, rc, 1, lam[t][0], lam[t][1], np, type_nl + (long)t * np * N,
                                    type_sg + t * np))
           die("NL projectors", names[t]);
     long k = 0;
     for (long a = 0; a < natoms; a++) {
       const int t = atype[a];
-      if (is_ligand(names[t])) continue;
+      if (fbse_is_ligand(names[t])) continue;
       memcpy(pxyz + 3 * k, xyz + 3 * a, 3 * sizeof(double));
       psp[k] = so_par[t];
       if (p.nl) {

@@ -257,6 +257,29 @@ int fbse_read_conf(const char *path, long *natoms, double **xyz, int **types, ch
   return 0;
 }
 
+int fbse_is_ligand(const char *t)
+{ /* the ligand labels of read_pot's SO loop (filter_mpi/read.c:1739-1746) */
+  static const char *lig[] = {"P1", "P2", "P3", "P4", "PC5", "PC6", "PR1", "PR2", "PR3",
+                              "PA1", "PA2", "PA3", "C1", "C2", "C3", NULL};
+  for (int i = 0; lig[i]; i++)
+    if (!strcmp(t, lig[i])) return 1;
+  return 0;
+}
+
+int fbse_read_so_params(const char *atyp, double *so_par, double *nl_par, char *err, size_t errlen)
+{ /* SO_<Atm>.par (filter_mpi/read.c:1732-1782): SO_par, NL_par[0], NL_par[1],
+   * the first value of each of the first three lines */
+  char path[64];
+  snprintf(path, sizeof path, "SO_%s.par", atyp);
+  FILE *f = fopen(path, "r");
+  if (!f) { seterr(err, errlen, "No SO(+NL) pot found in", path); return -1; }
+  const int ok = fscanf(f, "%lg %*g", so_par) == 1 && fscanf(f, "%lg %*g", &nl_par[0]) == 1 &&
+                 fscanf(f, "%lg %*g", &nl_par[1]) == 1;
+  fclose(f);
+  if (!ok) { seterr(err, errlen, "cannot read", path); return -1; }
+  return 0;
+}
+
 long fbse_read_table(const char *path, double **r, double **v)
 {
   FILE *f = fopen(path, "r");

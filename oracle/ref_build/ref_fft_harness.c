@@ -372,3 +372,120 @@ void ref_energy_range_approx(int so, int nl, double vmin_loc, double vmax_loc, d
   *de = j.par.dE;
   job_free(&j);
 }
+
+void read_conf(xyz_st *R, atom_info *atom, index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+void init_grid_params(grid_st *grid, xyz_st *R, index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+void build_grid_ksqr(double *ksqr, xyz_st *R, grid_st *grid, index_st *ist, par_st *par, flag_st *flag,
+                     parallel_st *parallel);
+void build_local_pot(double *pot_local, pot_st *pot, xyz_st *R, atom_info *atom, grid_st *grid, index_st *ist,
+                     par_st *par, flag_st *flag, parallel_st *parallel);
+
+/* The setup chain of mod_init + mod_pseudopot (mod_init.c, mod_pseudopot.c)
+ * at one rank, non-periodic, without strain, LSD or interpolated potentials:
+ * read_conf (read.c:998-1172, conf.par in the working directory, centred at
+ * the centre of mass), init_grid_params (init.c:5-256) from the input.par
+ * grid (n_in, dgrid), build_grid_ksqr (init.c:259-398) and build_local_pot
+ * (init.c:481-703, pot<Atm>.par in the working directory).  Outputs into
+ * caller buffers: natoms, zval / type index / coordinates per atom (up to
+ * cap_atoms), SO_par, NL_par[0], NL_par[1] per atom (sonl, read from
+ * SO_<Atm>.par by read_pot when SO or NL is on), the grid counts n[3] and
+ * origins lo[3], the axes (up to cap_axis
+ * each), ksqr and the local potential (up to cap_grid), Vmin / Vmax,
+ * n_NL_atoms and n_NL_gridpts (nlinfo).  Returns 0, or -1 if a capacity is
+ * short or conf.par cannot be read. */
+int ref_setup(double dgrid, const long *n_in, double ke_max, int so, int nl, long cap_atoms, long cap_axis,
+              long cap_grid, long *natoms, long *zval, long *tidx, double *xyz, double *sonl, long *n, double *lo,
+              double *gx, double *gy, double *gz, double *ksqr, double *pot, double *vrange, long *nlinfo)
+{
+  FILE *pf = fopen("conf.par", "r");
+  long nat = 0;
+  if (!pf || fscanf(pf, "%ld", &nat) != 1) {
+    if (pf) fclose(pf);
+    return -1;
+  }
+  fclose(pf);
+  if (nat > cap_atoms) return -1;
+  grid_st grid;
+  index_st ist;
+  par_st par;
+  flag_st flag;
+  parallel_st pl;
+  memset(&grid, 0, sizeof grid);
+  memset(&ist, 0, sizeof ist);
+  memset(&par, 0, sizeof par);
+  memset(&flag, 0, sizeof flag);
+  memset(&pl, 0, sizeof pl);
+  /* the read_input defaults this chain reads (read.c:9-61) */
+  ist.n_max_atom_types = N_MAX_ATOM_TYPES;
+  ist.atom_types = calloc(N_MAX_ATOM_TYPES, sizeof(long));
+  ist.max_pot_file_len = 8192;
+  ist.ngeoms = 1;
+  ist.natoms = nat;
+  ist.nspin = so ? 2 : 1;
+  ist.complex_idx = so ? 2 : 1;
+  par.scale_surface_Cs = 1.0;
+  par.pot_cut_rad2 = 225.0;
+  par.KE_max = ke_max;
+  flag.centerConf = 1;
+  flag.SO = so;
+  flag.NL = nl;
+  pl.nthreads = 1;
+  pl.mpi_rank = 1; /* quiet */
+  grid.nx = n_in[0];
+  grid.ny = n_in[1];
+  grid.nz = n_in[2];
+  grid.dx = grid.dy = grid.dz = dgrid;
+  par.R_NLcut2 = 1.5 + 6.0 * log(10.0) + 3.0 * dgrid; /* read.c:908 */
+  xyz_st *R = calloc(nat, sizeof(xyz_st));
+  atom_info *atom = calloc(nat, sizeof(atom_info));
+  int rc = -1;
+  read_conf(R, atom, &ist, &par, &flag, &pl);
+  init_grid_params(&grid, R, &ist, &par, &flag, &pl);
+  if (grid.nx > cap_axis || grid.ny > cap_axis || grid.nz > cap_axis || grid.ngrid > cap_grid) goto out;
+  grid.x = gx;
+  grid.y = gy;
+  grid.z = gz;
+  build_grid_ksqr(ksqr, R, &grid, &ist, &par, &flag, &pl);
+  pot_st pt;
+  memset(&pt, 0, sizeof pt);
+  const long atyp_tot = ist.ngeoms * ist.n_atom_types, potfl = atyp_tot * ist.max_pot_file_len;
+  pt.file_lens = calloc(atyp_tot, sizeof(long));
+  pt.dr = calloc(atyp_tot, sizeof(double));
+  pt.r = calloc(potfl, sizeof(double));
+  pt.pseudo = calloc(potfl, sizeof(double));
+  double *pl2 = calloc(2 * grid.ngrid, sizeof(double));
+  build_local_pot(pl2, &pt, R, atom, &grid, &ist, &par, &flag, &pl);
+  memcpy(pot, pl2, grid.ngrid * sizeof(double));
+  free(pl2);
+  free(pt.file_lens);
+  free(pt.dr);
+  free(pt.r);
+  free(pt.pseudo);
+  *natoms = nat;
+  for (long a = 0; a < nat; a++) {
+    zval[a] = atom[a].Zval;
+    tidx[a] = atom[a].idx;
+    xyz[3 * a] = R[a].x;
+    xyz[3 * a + 1] = R[a].y;
+    xyz[3 * a + 2] = R[a].z;
+    sonl[3 * a] = atom[a].SO_par;
+    sonl[3 * a + 1] = atom[a].NL_par[0];
+    sonl[3 * a + 2] = atom[a].NL_par[1];
+  }
+  n[0] = grid.nx;
+  n[1] = grid.ny;
+  n[2] = grid.nz;
+  lo[0] = grid.xmin;
+  lo[1] = grid.ymin;
+  lo[2] = grid.zmin;
+  vrange[0] = par.Vmin;
+  vrange[1] = par.Vmax;
+  nlinfo[0] = ist.n_NL_atoms;
+  nlinfo[1] = ist.n_NL_gridpts;
+  rc = 0;
+out:
+  free(R);
+  free(atom);
+  free(ist.atom_types);
+  return rc;
+}

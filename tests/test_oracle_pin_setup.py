@@ -1,0 +1,158 @@
+"""Pins the setup chain that the drop-in filter runs before the hot path
+against the reference's own code (oracle/_ref/libfbse_ref_fft.so, CPU):
+read_conf, init_grid_params, build_grid_ksqr and build_local_pot (with its
+read_pot), on the example configurations and pseudopotential files, against
+the library's host conf.par reader, grid rule and table reader and the
+oracle's k^2 grid and local potential, at full precision."""
+import ctypes
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.systems import GOLD
+from tests.test_dropin import FilterParams
+from tests.test_oracle_pin import REF_FFT_SO
+
+D = ctypes.POINTER(ctypes.c_double)
+LP = ctypes.POINTER(ctypes.c_long)
+IP = ctypes.POINTER(ctypes.c_int)
+
+
+def _p(a, t=D):
+    return a.ctypes.data_as(t)
+
+
+@pytest.fixture(scope="module")
+def rs():
+    if not os.path.exists(REF_FFT_SO):
+        pytest.skip("oracle/_ref not built (the reference tree is not mounted here)")
+    L = ctypes.CDLL(REF_FFT_SO)
+    L.ref_setup.argtypes = ([ctypes.c_double, LP, ctypes.c_double, ctypes.c_int, ctypes.c_int] + [ctypes.c_long] * 3 +
+                            [LP, LP, LP, D, D, LP, D, D, D, D, D, D, D, LP])
+    L.ref_setup.restype = ctypes.c_int
+    return L
+
+
+@pytest.fixture(scope="module")
+def host():
+    import filterbse_gb300 as F
+    L = F.load()
+    L.fbse_read_filter_params.argtypes = [ctypes.c_char_p, ctypes.POINTER(FilterParams), ctypes.c_char_p,
+                                          ctypes.c_size_t]
+    L.fbse_read_conf.argtypes = [ctypes.c_char_p, LP, ctypes.POINTER(D), ctypes.POINTER(IP),
+                                 ctypes.POINTER(ctypes.c_char * 8), IP, ctypes.c_char_p, ctypes.c_size_t]
+    L.fbse_grid_rule.argtypes = [D, ctypes.c_long, ctypes.c_double, ctypes.c_long, ctypes.c_int, LP, D]
+    L.fbse_grid_rule.restype = None
+    L.fbse_grid_axis.argtypes = [ctypes.c_long, ctypes.c_double, ctypes.c_double, D]
+    L.fbse_grid_axis.restype = None
+    L.fbse_read_table.argtypes = [ctypes.c_char_p, ctypes.POINTER(D), ctypes.POINTER(D)]
+    L.fbse_read_table.restype = ctypes.c_long
+    L.fbse_is_ligand.argtypes = [ctypes.c_char_p]
+    L.fbse_read_so_params.argtypes = [ctypes.c_char_p, D, D, ctypes.c_char_p, ctypes.c_size_t]
+    return L
+
+
+@pytest.mark.parametrize("name", ["cdse22", "cspbi3"])
+def test_setup_chain_matches_reference(rs, host, tmp_path, monkeypatch, name):
+    """read_conf (read.c:998-1172) with centerConf, init_grid_params
+    (init.c:5-256), build_grid_ksqr (init.c:259-398) and build_local_pot
+    (init.c:481-703) with read_pot (read.c:1175-1800) on an example's
+    conf.par and pot<Atm>.par: atoms, type indices and centred coordinates,
+    grid counts and origins, the axes, the SO / NL parameters of SO_<Atm>.par
+    and the NL sphere size exactly; ksqr and the local potential to 1e-14 of
+    their largest magnitude"""
+    src = os.path.join(GOLD, name)
+    for f in os.listdir(src):
+        if f == "conf.par" or (f.startswith(("pot", "SO_")) and f.endswith(".par")):
+            shutil.copy(os.path.join(src, f), tmp_path / f)
+    monkeypatch.chdir(tmp_path)
+    prm = FilterParams()
+    err = ctypes.create_string_buffer(512)
+    assert host.fbse_read_filter_params(os.path.join(src, "input.par").encode(), ctypes.byref(prm), err, 512) == 0
+    so, nl = int(prm.so), int(prm.nl)
+
+    cap_atoms, cap_axis, cap_grid = 4096, 512, 8_000_000
+    natoms = ctypes.c_long()
+    zval = np.zeros(cap_atoms, np.int64)
+    tidx = np.zeros(cap_atoms, np.int64)
+    xyz = np.zeros(3 * cap_atoms)
+    sonl = np.zeros(3 * cap_atoms)
+    n = np.zeros(3, np.int64)
+    lo = np.zeros(3)
+    axes = [np.zeros(cap_axis) for _ in range(3)]
+    ksqr = np.zeros(cap_grid)
+    pot = np.zeros(cap_grid)
+    vr = np.zeros(2)
+    nlinfo = np.zeros(2, np.int64)
+    n_in = np.array([prm.nx, prm.ny, prm.nz], np.int64)
+    rc = rs.ref_setup(prm.dx, _p(n_in, LP), prm.ke_max, so, nl, cap_atoms, cap_axis, cap_grid, ctypes.byref(natoms),
+                      _p(zval, LP), _p(tidx, LP), _p(xyz), _p(sonl), _p(n, LP), _p(lo), *[_p(a) for a in axes], _p(ksqr),
+                      _p(pot), _p(vr), _p(nlinfo, LP))
+    assert rc == 0
+    na = natoms.value
+
+    # the library's host reader: same atoms, first-appearance type order, centred coordinates
+    hn = ctypes.c_long()
+    hx, ht = D(), IP()
+    names = (ctypes.c_char * 8 * 32)()
+    nt = ctypes.c_int()
+    assert host.fbse_read_conf(b"conf.par", ctypes.byref(hn), ctypes.byref(hx), ctypes.byref(ht), names,
+                               ctypes.byref(nt), err, 512) == 0, err.value
+    assert hn.value == na
+    hxyz = np.ctypeslib.as_array(hx, (3 * na,)).copy()
+    htyp = np.ctypeslib.as_array(ht, (na,)).copy()
+    assert np.array_equal(hxyz, xyz[:3 * na])
+    assert np.array_equal(htyp, tidx[:na])
+
+    # grid rule and axes
+    g_n, g_lo = [], []
+    for ax in range(3):
+        nn, x0 = ctypes.c_long(), ctypes.c_double()
+        host.fbse_grid_rule(_p(hxyz), na, prm.dx, int(n_in[ax]), ax, ctypes.byref(nn), ctypes.byref(x0))
+        g_n.append(nn.value)
+        g_lo.append(x0.value)
+        hax = np.zeros(nn.value)
+        host.fbse_grid_axis(nn.value, x0.value, prm.dx, _p(hax))
+        assert np.array_equal(hax, axes[ax][:nn.value])
+    assert g_n == list(n) and g_lo == list(lo)
+    g = O.Grid(int(n[0]), int(n[1]), int(n[2]), prm.dx, prm.dx, prm.dx, lo[0], lo[1], lo[2], prm.ke_max)
+    N = g.ngrid
+    assert np.max(np.abs(g.ksqr() - ksqr[:N])) <= 1e-14 * np.max(ksqr[:N])
+
+    # local potential from the host-read tables, per type in first-appearance order
+    tables = []
+    for k in range(nt.value):
+        r, v = D(), D()
+        m = host.fbse_read_table(f"pot{names[k].value.decode()}.par".encode(), ctypes.byref(r), ctypes.byref(v))
+        assert m > 1
+        tables.append((np.ctypeslib.as_array(r, (m,)).copy(), np.ctypeslib.as_array(v, (m,)).copy()))
+    mine = O.local_pot(g, hxyz.reshape(-1, 3), htyp, tables)
+    ref = pot[:N]
+    print(f"\n[{name}] grid {tuple(n)}, {na} atoms, V in [{vr[0]:.6f}, {vr[1]:.6f}], "
+          f"max |dV| {np.max(np.abs(mine - ref)):.2e}")
+    assert np.max(np.abs(mine - ref)) <= 1e-14 * np.max(np.abs(ref))
+    assert (vr[0], vr[1]) == (ref.min(), ref.max())
+
+    # SO_par / NL_par per atom: the host reader per type, zero on ligands
+    if so or nl:
+        for a in range(na):
+            t = names[htyp[a]].value
+            if host.fbse_is_ligand(t):
+                assert not np.any(sonl[3 * a:3 * a + 3])
+                continue
+            sp, lam = ctypes.c_double(), np.zeros(2)
+            assert host.fbse_read_so_params(t, ctypes.byref(sp), _p(lam), err, 512) == 0, err.value
+            assert (sp.value, lam[0], lam[1]) == tuple(sonl[3 * a:3 * a + 3])
+
+    # the NL sphere size (build_grid_ksqr counts the points within R_NLcut of
+    # the first n_NL_atoms atoms): the oracle table's row stride
+    if so or nl:
+        assert nlinfo[0] == na  # no ligands in this configuration
+        rc2 = O.r_nlcut2(prm.dx)
+        gx, gy, gz = g.axes()
+        cnt = max(int(np.count_nonzero((gx[None, None, :] - c[0]) ** 2 + (gy[None, :, None] - c[1]) ** 2 +
+                                       (gz[:, None, None] - c[2]) ** 2 < rc2)) for c in hxyz.reshape(-1, 3))
+        assert nlinfo[1] == cnt
