@@ -489,3 +489,31 @@ out:
   free(ist.atom_types);
   return rc;
 }
+
+void init_filter_states(double *psi_rank, zomplex *psi, grid_st *grid, long *rand_seed, index_st *ist, par_st *par,
+                        flag_st *flag, parallel_st *parallel);
+
+/* init_filter_states (init.c:1138-1255) with init_psi (init.c:1256-1306) at
+ * one rank: n_filters random starts, start j at state j * m of psi_rank
+ * (m * n_filters states of nspin * ngrid * complex_idx doubles); returns the
+ * advanced seed and writes seed-1.dat into the working directory */
+long ref_init_filter_states(double *psi_rank, long nx, long ny, long nz, int nspin, int is_complex, double dv,
+                            long n_filters, long m, long seed)
+{
+  struct job j;
+  job_init(&j, nx, ny, nz, nspin, is_complex, 0, 0, 0, 0, 0, NULL, NULL, NULL, NULL, NULL, dv);
+  j.ist.n_filters_per_rank = n_filters;
+  j.ist.m_states_per_filter = m;
+  grid_st grid;
+  memset(&grid, 0, sizeof grid);
+  grid.nx = nx;
+  grid.ny = ny;
+  grid.nz = nz;
+  grid.ngrid = nx * ny * nz;
+  grid.dv = dv;
+  zomplex *psi = calloc(j.ist.nspinngrid, sizeof(zomplex));
+  init_filter_states(psi_rank, psi, &grid, &seed, &j.ist, &j.par, &j.flag, &j.pl);
+  free(psi);
+  job_free(&j);
+  return seed;
+}

@@ -499,3 +499,27 @@ def test_approx_energy_range_matches_reference(ref_fft, so, nl, lmin, lmax):
     L.fbse_energy_range_rule(0, so, nl, vmin, vmax, ke, lmin, lmax, ctypes.byref(lo), ctypes.byref(hi))
     emin_i, de_i, _, _ = O.inflate_range(sysm, -0.91, 4.37, lmin)
     assert lo.value == emin_i and abs((hi.value - lo.value) - de_i) <= 1e-15 * de_i
+
+
+@pytest.mark.parametrize("nspin,cplx", [(1, False), (1, True), (2, True)])
+def test_init_filter_states_match_reference(ref_fft, tmp_path, monkeypatch, nspin, cplx):
+    """init_filter_states + init_psi (init.c:1138-1306) at one rank: every
+    start bit for bit against the oracle (start j at state j * m of the
+    reference's psi_rank), the seeds of seed-<rank>.dat and the advanced seed"""
+    monkeypatch.chdir(tmp_path)
+    ref_fft.ref_init_filter_states.argtypes = [D] + [ctypes.c_long] * 3 + [ctypes.c_int] * 2 + [ctypes.c_double] + \
+        [ctypes.c_long] * 3
+    ref_fft.ref_init_filter_states.restype = ctypes.c_long
+    nx, ny, nz, dv = 9, 8, 7, 0.512
+    n_filters, m = 3, 4
+    stlen = (2 if cplx else 1) * nspin * nx * ny * nz
+    rk = np.zeros(n_filters * m * stlen)
+    end = ref_fft.ref_init_filter_states(_p(rk), nx, ny, nz, nspin, int(cplx), dv, n_filters, m, -4242)
+    want, seeds, w_end = O.init_filter_states(-4242, n_filters, nx * ny * nz, nspin, cplx, dv)
+    got = rk.reshape(n_filters, m, stlen)[:, 0, :]
+    w = np.ascontiguousarray(want).view(np.float64) if cplx else np.ascontiguousarray(want.real)
+    assert np.array_equal(got, w.reshape(n_filters, stlen))
+    assert end == w_end
+    rows = np.loadtxt(tmp_path / "seed-1.dat", skiprows=1, dtype=np.int64)
+    assert np.array_equal(rows[:, 0], np.arange(n_filters * nspin))
+    assert np.array_equal(rows[:, 1], np.asarray(seeds, np.int64).reshape(-1))
