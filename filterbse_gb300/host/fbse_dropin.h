@@ -53,6 +53,10 @@ int fbse_read_bse_params(const char *path, fbse_bse_params *p, char *err, size_t
 int fbse_read_conf(const char *path, long *natoms, double **xyz, int **types, char names[][8], int *ntypes,
                    char *err, size_t errlen);
 
+/* energy targets of one filter (set_ene_targets, init.c:401-478): n_vb in
+ * the valence window, m - n_vb in the conduction window; targets [m] */
+void fbse_ene_targets(long m, long n_vb, double vbmin, double vbmax, double cbmin, double cbmax, double *targets);
+
 /* 1 for the ligand labels (P1-P4, PC5, PC6, PR1-3, PA1-3, C1-3), which carry
  * no SO / NL projectors */
 int fbse_is_ligand(const char *atyp);

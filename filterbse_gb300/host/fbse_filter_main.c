@@ -417,10 +417,7 @@ int main(void)
     /* targets (set_ene_targets, init.c:401-478) and Newton coefficients */
     const long m = p.m_states_per_filter, nc = p.ncheby, ns = p.n_filter_cycles;
     double *targets = malloc(m * sizeof(double));
-    double del = (p.vbmax - p.vbmin) / (double)p.n_targets_vb;
-    for (long j = 0; j < p.n_targets_vb; j++) targets[p.n_targets_vb - j - 1] = p.vbmax - (double)j * del;
-    del = (p.cbmax - p.cbmin) / (double)p.n_targets_cb;
-    for (long j = p.n_targets_vb; j < m; j++) targets[j] = p.cbmin + (double)(j - p.n_targets_vb) * del;
+    fbse_ene_targets(m, p.n_targets_vb, p.vbmin, p.vbmax, p.cbmin, p.cbmax, targets);
     double *zn = malloc(nc * sizeof(double)), *an = malloc(2 * m * nc * sizeof(double));
     if (p.read_coeffs == 1) {
       read_coeff_files(zn, an, nc, m);

@@ -257,6 +257,16 @@ int fbse_read_conf(const char *path, long *natoms, double **xyz, int **types, ch
   return 0;
 }
 
+void fbse_ene_targets(long m, long n_vb, double vbmin, double vbmax, double cbmin, double cbmax, double *targets)
+{ /* set_ene_targets (filter_mpi/init.c:438-455): n_vb targets spaced down from
+   * VBmax (VBmax included), the other m - n_vb spaced up from CBmin */
+  const long n_cb = m - n_vb;
+  double del = (vbmax - vbmin) / (double)n_vb;
+  for (long j = 0; j < n_vb; j++) targets[n_vb - j - 1] = vbmax - (double)j * del;
+  del = (cbmax - cbmin) / (double)n_cb;
+  for (long j = n_vb; j < m; j++) targets[j] = cbmin + (double)(j - n_vb) * del;
+}
+
 int fbse_is_ligand(const char *t)
 { /* the ligand labels of read_pot's SO loop (filter_mpi/read.c:1739-1746) */
   static const char *lig[] = {"P1", "P2", "P3", "P4", "PC5", "PC6", "PR1", "PR2", "PR3",

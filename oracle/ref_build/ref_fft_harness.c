@@ -517,3 +517,30 @@ long ref_init_filter_states(double *psi_rank, long nx, long ny, long nz, int nsp
   job_free(&j);
   return seed;
 }
+
+void set_ene_targets(double *ene_targets, index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+
+/* set_ene_targets (init.c:401-478) with setTargets = 1 (n_vb valence and
+ * m - n_vb conduction targets); writes ene_targets.dat into the working
+ * directory */
+void ref_ene_targets(long m, long n_vb, double vbmin, double vbmax, double cbmin, double cbmax, double *targets)
+{
+  index_st ist;
+  par_st par;
+  flag_st flag;
+  parallel_st pl;
+  memset(&ist, 0, sizeof ist);
+  memset(&par, 0, sizeof par);
+  memset(&flag, 0, sizeof flag);
+  memset(&pl, 0, sizeof pl);
+  ist.m_states_per_filter = m;
+  par.n_targets_VB = n_vb;
+  par.n_targets_CB = m - n_vb;
+  par.VBmin = vbmin;
+  par.VBmax = vbmax;
+  par.CBmin = cbmin;
+  par.CBmax = cbmax;
+  flag.setTargets = 1;
+  pl.mpi_rank = 1; /* quiet */
+  set_ene_targets(targets, &ist, &par, &flag, &pl);
+}

@@ -523,3 +523,21 @@ def test_init_filter_states_match_reference(ref_fft, tmp_path, monkeypatch, nspi
     rows = np.loadtxt(tmp_path / "seed-1.dat", skiprows=1, dtype=np.int64)
     assert np.array_equal(rows[:, 0], np.arange(n_filters * nspin))
     assert np.array_equal(rows[:, 1], np.asarray(seeds, np.int64).reshape(-1))
+
+
+@pytest.mark.parametrize("m,n_vb,win", [(16, 10, (-0.31, -0.24, -0.15, -0.06)), (16, 8, (-0.50, -0.20, -0.167, -0.10)),
+                                        (5, 1, (-0.4, -0.3, -0.1, 0.2)), (7, 6, (-1.0, -0.5, 0.0, 0.5))])
+def test_ene_targets_match_reference(ref_fft, tmp_path, monkeypatch, m, n_vb, win):
+    """set_ene_targets (init.c:401-478) with setTargets = 1 against the
+    library's host fbse_ene_targets, bit for bit"""
+    import filterbse_gb300 as F
+    monkeypatch.chdir(tmp_path)
+    ref_fft.ref_ene_targets.argtypes = [ctypes.c_long] * 2 + [ctypes.c_double] * 4 + [D]
+    L = F.load()
+    L.fbse_ene_targets.argtypes = [ctypes.c_long] * 2 + [ctypes.c_double] * 4 + [D]
+    L.fbse_ene_targets.restype = None
+    ref, mine = np.zeros(m), np.zeros(m)
+    ref_fft.ref_ene_targets(m, n_vb, *win, _p(ref))
+    L.fbse_ene_targets(m, n_vb, *win, _p(mine))
+    assert np.array_equal(ref, mine)
+    assert ref[n_vb - 1] == win[1] and ref[n_vb] == win[2]
