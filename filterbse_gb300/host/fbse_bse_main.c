@@ -318,23 +318,12 @@ int main(void)
     die("output.dat holds neither complex spinors (bse_cplx) nor real one-component states (bse_real)", NULL);
 
   /* get_qp_basis_indices (bse_cplx/basis.c:7-254) */
-  long *hole = malloc(o.mn * sizeof(long)), *elec = malloc(o.mn * sizeof(long)), nh = 0, ne = 0;
-  for (long i = 0; i < o.mn; i++) {
-    if (o.sigma[i] < p.sigma_e_cut && o.eval[i] < p.fermi_e) hole[nh++] = i;
-    if (o.sigma[i] < p.sigma_e_cut && o.eval[i] > p.fermi_e) elec[ne++] = i;
-  }
+  long *sel = malloc((o.mn ? o.mn : 1) * sizeof(long)), nh = 0, ne = 0;
+  fbse_qp_basis(o.eval, o.sigma, o.mn, p.sigma_e_cut, p.fermi_e, p.max_hole_states, p.max_elec_states, sel, &nh,
+                &ne);
   if (nh < 1 || ne < 1) die("no converged hole or electron states below/above fermiEnergy", NULL);
-  long h0 = 0;
-  if (p.max_hole_states != -1 && nh > p.max_hole_states) {
-    h0 = nh - p.max_hole_states; /* keep the holes closest to the gap */
-    nh = p.max_hole_states;
-  }
-  if (p.max_elec_states != -1 && ne > p.max_elec_states) ne = p.max_elec_states;
   const long nqp = nh + ne, lumo = nh, nx = nh * ne;
   double *eqp = malloc(nqp * sizeof(double));
-  long *sel = malloc(nqp * sizeof(long));
-  for (long i = 0; i < nh; i++) sel[i] = hole[h0 + i];
-  for (long i = 0; i < ne; i++) sel[nh + i] = elec[i];
   FILE *fe = fopen("BSEeval.par", "w");
   for (long i = 0; i < nqp; i++) {
     eqp[i] = o.eval[sel[i]];

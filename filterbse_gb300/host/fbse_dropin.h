@@ -57,6 +57,12 @@ int fbse_read_conf(const char *path, long *natoms, double **xyz, int **types, ch
  * the valence window, m - n_vb in the conduction window; targets [m] */
 void fbse_ene_targets(long m, long n_vb, double vbmin, double vbmax, double cbmin, double cbmax, double *targets);
 
+/* quasiparticle basis of the BSE stage (get_qp_basis_indices,
+ * bse_cplx/basis.c:7-254): sel [n] receives the eval.dat indices of the kept
+ * holes then electrons; returns their number */
+long fbse_qp_basis(const double *eval, const double *sigma, long n, double sigma_cut, double fermi_e,
+                   long max_holes, long max_elecs, long *sel, long *n_holes, long *n_elecs);
+
 /* 1 for the ligand labels (P1-P4, PC5, PC6, PR1-3, PA1-3, C1-3), which carry
  * no SO / NL projectors */
 int fbse_is_ligand(const char *atyp);

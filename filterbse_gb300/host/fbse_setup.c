@@ -267,6 +267,33 @@ void fbse_ene_targets(long m, long n_vb, double vbmin, double vbmax, double cbmi
   for (long j = n_vb; j < m; j++) targets[j] = cbmin + (double)(j - n_vb) * del;
 }
 
+long fbse_qp_basis(const double *eval, const double *sigma, long n, double sigma_cut, double fermi_e,
+                   long max_holes, long max_elecs, long *sel, long *n_holes, long *n_elecs)
+{ /* get_qp_basis_indices (bse_cplx/basis.c:7-254): the converged states
+   * (sigma < cut) below and above the Fermi energy, in eval.dat order; with a
+   * maximum, the holes nearest the gap and the first electrons */
+  long nh = 0, ne = 0;
+  for (long i = 0; i < n; i++)
+    if (sigma[i] < sigma_cut && eval[i] < fermi_e) nh++;
+  long h = 0, e = 0;
+  const long h0 = (max_holes != -1 && nh > max_holes) ? nh - max_holes : 0;
+  const long nh_keep = nh - h0;
+  for (long i = 0; i < n; i++) {
+    if (sigma[i] < sigma_cut && eval[i] < fermi_e) {
+      if (h >= h0) sel[h - h0] = i;
+      h++;
+    }
+    if (sigma[i] < sigma_cut && eval[i] > fermi_e) {
+      if (max_elecs == -1 || e < max_elecs) sel[nh_keep + e] = i;
+      e++;
+    }
+  }
+  ne = (max_elecs != -1 && e > max_elecs) ? max_elecs : e;
+  *n_holes = nh_keep;
+  *n_elecs = ne;
+  return nh_keep + ne;
+}
+
 int fbse_is_ligand(const char *t)
 { /* the ligand labels of read_pot's SO loop (filter_mpi/read.c:1739-1746) */
   static const char *lig[] = {"P1", "P2", "P3", "P4", "PC5", "PC6", "PR1", "PR2", "PR3",

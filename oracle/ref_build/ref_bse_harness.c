@@ -142,3 +142,34 @@ void ref_bse_xton_ang(double *coeff, double *s, double *l, double *l2, double *l
   calc_xton_ang_mom_mtrx((double complex *)coeff, (xyz_st *)s, (xyz_st *)l, (double complex *)l2,
                          (double complex *)ls, &j.ist, &j.par, &j.flag, &j.pl);
 }
+
+void get_qp_basis_indices(double *eig_vals, double *sigma_E, long **eval_hole_idxs, long **eval_elec_idxs,
+                          index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+
+/* get_qp_basis_indices (bse_cplx/basis.c:7-254) at rank 0 over n eval.dat
+ * entries (eval and sigma are reordered in place, as the reference does):
+ * the eval.dat indices of the kept holes then electrons into sel, the counts
+ * and homo / lumo positions into info[4]; writes BSEeval.par into the working
+ * directory */
+void ref_bse_qp_basis(double *eval, double *sigma, long n, double sigma_cut, double fermi_e, long max_holes,
+                      long max_elecs, long *sel, long *info)
+{
+  struct bjob j;
+  double g0 = 0;
+  bjob_init(&j, 1, 1, 1, 1, 1, 1, 0, 0, 0, &g0, &g0, &g0, 0, 0, 0);
+  j.ist.mn_states_tot = n;
+  j.ist.max_hole_states = max_holes;
+  j.ist.max_elec_states = max_elecs;
+  j.par.sigma_E_cut = sigma_cut;
+  j.par.fermi_E = fermi_e;
+  long *hole = NULL, *elec = NULL;
+  get_qp_basis_indices(eval, sigma, &hole, &elec, &j.ist, &j.par, &j.flag, &j.pl);
+  for (long i = 0; i < j.ist.n_holes; i++) sel[i] = hole[i];
+  for (long i = 0; i < j.ist.n_elecs; i++) sel[j.ist.n_holes + i] = elec[i];
+  info[0] = j.ist.n_holes;
+  info[1] = j.ist.n_elecs;
+  info[2] = j.ist.homo_idx;
+  info[3] = j.ist.lumo_idx;
+  free(hole);
+  free(elec);
+}

@@ -216,3 +216,49 @@ def test_bse_spin_and_angular_matrices_match_reference(rb, tmp_path, monkeypatch
     # orbital.dat and couple.dat: %.5f
     assert np.allclose(ob[:, 1:], np.column_stack([orb.real, otot.real, otot.imag]), atol=6e-6)
     assert np.allclose(cp[:, 1:], np.column_stack([lstot.real, lstot.imag]), atol=6e-6)
+
+
+@pytest.mark.parametrize("name,cut,fermi,mh,me", [("cspbi3", 1e-4, -0.19, 10, 10), ("cspbi3", 1e-4, -0.19, -1, -1),
+                                                  ("cspbi3", 1e-4, -0.19, 3, -1), ("cdse22", 1e-3, -0.18, 4, 3),
+                                                  ("cdse22", 1e-3, -0.18, -1, 2), ("cdse22", 5e-4, -0.18, 100, 100)])
+def test_qp_basis_matches_reference(rb, tmp_path, monkeypatch, name, cut, fermi, mh, me):
+    """get_qp_basis_indices (bse_cplx/basis.c:7-254) on the examples' eval.dat
+    against the library's host fbse_qp_basis: the kept holes (nearest the gap)
+    and electrons, their eval.dat indices and counts, and the energies the
+    reference carries for them"""
+    import filterbse_gb300 as F
+    monkeypatch.chdir(tmp_path)
+    rb.ref_bse_qp_basis.argtypes = [D, D, ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_long,
+                                    ctypes.c_long, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
+    ev = np.loadtxt(os.path.join(ROOT, "tests", "golden", name, "eval.dat"))
+    n = len(ev)
+    e, s = np.ascontiguousarray(ev[:, 1]), np.ascontiguousarray(ev[:, 2])
+    sel = np.zeros(n, np.int64)
+    info = np.zeros(4, np.int64)
+    er, sr = e.copy(), s.copy()  # the reference reorders them in place
+    rb.ref_bse_qp_basis(_p(er), _p(sr), n, cut, fermi, mh, me, sel.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                        info.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+    nh, ne = int(info[0]), int(info[1])
+    assert nh >= 1 and ne >= 1 and info[3] == info[2] + 1 == nh
+    L = F.load()
+    Lp = ctypes.POINTER(ctypes.c_long)
+    L.fbse_qp_basis.argtypes = [D, D, ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_long, ctypes.c_long,
+                                Lp, Lp, Lp]
+    L.fbse_qp_basis.restype = ctypes.c_long
+    mine = np.zeros(n, np.int64)
+    hn, hne = ctypes.c_long(), ctypes.c_long()
+    nq = L.fbse_qp_basis(_p(e), _p(s), n, cut, fermi, mh, me, mine.ctypes.data_as(Lp), ctypes.byref(hn),
+                         ctypes.byref(hne))
+    assert (hn.value, hne.value, nq) == (nh, ne, nh + ne)
+    assert np.array_equal(mine[:nq], sel[:nq])
+    assert np.array_equal(er[:nh], e[mine[:nh]])
+    conv = np.flatnonzero(s < cut)
+    if me == -1 and mh != -1 and int(np.sum(e[conv] < fermi)) > mh:
+        # holes cut to maxHoleStates with maxElecStates = -1: the reference
+        # skips its electron reordering (basis.c:176-198), so the energies it
+        # keeps for the electrons are the converged list's entries after the
+        # kept holes -- dropped holes -- not the electrons'
+        compact = e[conv]
+        assert np.array_equal(er[nh:nq], compact[nh:nq]) and not np.array_equal(er[nh:nq], e[mine[nh:nq]])
+    else:
+        assert np.array_equal(er[nh:nq], e[mine[nh:nq]])
