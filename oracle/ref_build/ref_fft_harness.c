@@ -544,3 +544,33 @@ void ref_ene_targets(long m, long n_vb, double vbmin, double vbmax, double cbmin
   pl.mpi_rank = 1; /* quiet */
   set_ene_targets(targets, &ist, &par, &flag, &pl);
 }
+
+void write_cube_file(double *rho, grid_st *grid, char *fileName);
+void write_eval_dat(double *eig_vals, double *sigma_E, long n_elems, char *fileName);
+void write_psi_dat(double *psitot, long n_elems, char *fileName);
+
+/* write_cube_file (write.c:65-139; atoms from conf.dat in the working
+ * directory), write_eval_dat (write.c:263-282) and write_psi_dat
+ * (write.c:285-296) into the working directory.  write_psi_dat leaves its
+ * stream open, so the data reaches the file at process exit; fflush(NULL)
+ * stands in for that exit here. */
+void ref_write_outputs(const double *rho, long nx, long ny, long nz, double dx, double dy, double dz, double xmin,
+                       double ymin, double zmin, const double *eval, const double *sigma, long n, const double *psi,
+                       long n_doubles)
+{
+  grid_st grid;
+  memset(&grid, 0, sizeof grid);
+  grid.nx = nx;
+  grid.ny = ny;
+  grid.nz = nz;
+  grid.dx = dx;
+  grid.dy = dy;
+  grid.dz = dz;
+  grid.xmin = xmin;
+  grid.ymin = ymin;
+  grid.zmin = zmin;
+  write_cube_file((double *)rho, &grid, "ref.cube");
+  write_eval_dat((double *)eval, (double *)sigma, n, "ref_eval.dat");
+  write_psi_dat((double *)psi, n_doubles, "ref_psi.dat");
+  fflush(NULL);
+}

@@ -156,3 +156,53 @@ def test_setup_chain_matches_reference(rs, host, tmp_path, monkeypatch, name):
         cnt = max(int(np.count_nonzero((gx[None, None, :] - c[0]) ** 2 + (gy[None, :, None] - c[1]) ** 2 +
                                        (gz[:, None, None] - c[2]) ** 2 < rc2)) for c in hxyz.reshape(-1, 3))
         assert nlinfo[1] == cnt
+
+
+@pytest.mark.parametrize("name", ["cdse22", "cspbi3"])
+def test_output_writers_match_reference(rs, host, tmp_path, monkeypatch, name):
+    """write_cube_file, write_eval_dat and write_psi_dat (write.c:65-296)
+    against the library's host fbse_write_cube / fbse_write_eval /
+    fbse_write_psi, byte for byte: the cube of an example's atoms (read back
+    from the conf.dat that read_conf writes) on its grid, an eval.dat and a
+    psi.dat"""
+    src = os.path.join(GOLD, name)
+    shutil.copy(os.path.join(src, "conf.par"), tmp_path / "conf.par")
+    monkeypatch.chdir(tmp_path)
+    err = ctypes.create_string_buffer(512)
+    hn = ctypes.c_long()
+    hx, ht = D(), IP()
+    names = (ctypes.c_char * 8 * 32)()
+    nt = ctypes.c_int()
+    assert host.fbse_read_conf(b"conf.par", ctypes.byref(hn), ctypes.byref(hx), ctypes.byref(ht), names,
+                               ctypes.byref(nt), err, 512) == 0
+    na = hn.value
+    xyz = np.ctypeslib.as_array(hx, (3 * na,)).copy()
+    typ = np.ctypeslib.as_array(ht, (na,)).copy()
+    # conf.dat as read_conf writes it (read.c:1150-1156), which write_cube_file reads
+    with open("conf.dat", "w") as f:
+        f.write(f"{na}\n")
+        for a in range(na):
+            f.write("%3s % .16g % .16g % .16g\n" % (names[typ[a]].value.decode(), *xyz[3 * a:3 * a + 3]))
+    rng = np.random.default_rng(3)
+    nx, ny, nz, d = 13, 11, 9, 0.7
+    lo = (-4.55, -3.85, -3.15)
+    rho = np.ascontiguousarray(rng.standard_normal(nx * ny * nz) * np.logspace(-9, 2, nx * ny * nz))
+    ev = np.ascontiguousarray(np.sort(rng.uniform(-0.5, 0.1, 40)))
+    sg = np.ascontiguousarray(10.0 ** rng.uniform(-9, -2, 40))
+    psi = np.ascontiguousarray(rng.standard_normal(3 * 2 * 2 * nx * ny * nz))
+    rs.ref_write_outputs.argtypes = [D] + [ctypes.c_long] * 3 + [ctypes.c_double] * 6 + [D, D, ctypes.c_long, D,
+                                                                                          ctypes.c_long]
+    rs.ref_write_outputs(_p(rho), nx, ny, nz, d, d, d, *lo, _p(ev), _p(sg), len(ev), _p(psi), psi.size)
+    sym8 = np.zeros((na, 8), np.uint8)
+    for a in range(na):
+        b = names[typ[a]].value
+        sym8[a, :len(b)] = np.frombuffer(b, np.uint8)
+    host.fbse_write_cube.argtypes = [ctypes.c_char_p, D] + [ctypes.c_long] * 3 + [ctypes.c_double] * 6 + \
+        [ctypes.c_long, ctypes.c_char_p, D]
+    host.fbse_write_eval.argtypes = [ctypes.c_char_p, D, D, ctypes.c_long]
+    host.fbse_write_psi.argtypes = [ctypes.c_char_p, D, ctypes.c_long]
+    assert host.fbse_write_cube(b"mine.cube", _p(rho), nx, ny, nz, d, d, d, *lo, na, sym8.tobytes(), _p(xyz)) == 0
+    assert host.fbse_write_eval(b"mine_eval.dat", _p(ev), _p(sg), len(ev)) == 0
+    assert host.fbse_write_psi(b"mine_psi.dat", _p(psi), psi.size) == 0
+    for mine, ref in (("mine.cube", "ref.cube"), ("mine_eval.dat", "ref_eval.dat"), ("mine_psi.dat", "ref_psi.dat")):
+        assert open(mine, "rb").read() == open(ref, "rb").read(), mine
