@@ -574,3 +574,43 @@ void ref_write_outputs(const double *rho, long nx, long ny, long nz, double dx, 
   write_psi_dat((double *)psi, n_doubles, "ref_psi.dat");
   fflush(NULL);
 }
+
+void read_input(flag_st *flag, grid_st *grid, index_st *ist, par_st *par, parallel_st *parallel);
+
+/* read_input (read.c:5-995) at a non-zero rank of one (so that it prints no
+ * job state) on input.par and conf.par in the working directory.  d[10]: dx,
+ * dy, dz, VBmin, VBmax, CBmin, CBmax, KE_max, fermi_E, sigma_E_cut.  l[31]:
+ * nx, ny, nz, m_states_per_filter, n_filter_cycles, ncheby, setTargets,
+ * n_targets_VB, n_targets_CB, setSeed, rand_seed, useSpinors, SO, NL,
+ * getAllStates, approxEnergyRange, printPsiFilt, printPsiDiag,
+ * calcFilterOnly, restartFromOrtho, restartFromSigma, n_states_for_ortho,
+ * n_states_for_sigma, printCubes, ncubes, readCoeffs, inputPsiFilt,
+ * init_psi_start, init_psi_end, calcSpinAngStat, isComplex. */
+void ref_read_input(double *d, long *l)
+{
+  grid_st grid;
+  index_st ist;
+  par_st par;
+  flag_st flag;
+  parallel_st pl;
+  memset(&grid, 0, sizeof grid);
+  memset(&ist, 0, sizeof ist);
+  memset(&par, 0, sizeof par);
+  memset(&flag, 0, sizeof flag);
+  memset(&pl, 0, sizeof pl);
+  pl.mpi_rank = 1;
+  pl.mpi_size = 1;
+  pl.nthreads = 1;
+  read_input(&flag, &grid, &ist, &par, &pl);
+  const double dv[10] = {grid.dx, grid.dy, grid.dz, par.VBmin, par.VBmax, par.CBmin, par.CBmax, par.KE_max,
+                         par.fermi_E, par.sigma_E_cut};
+  const long lv[31] = {grid.nx, grid.ny, grid.nz, ist.m_states_per_filter, ist.n_filter_cycles, ist.ncheby,
+                       flag.setTargets, par.n_targets_VB, par.n_targets_CB, flag.setSeed, par.rand_seed,
+                       flag.useSpinors, flag.SO, flag.NL, flag.getAllStates, flag.approxEnergyRange,
+                       flag.printPsiFilt, flag.printPsiDiag, flag.calcFilterOnly, flag.restartFromOrtho,
+                       flag.restartFromSigma, ist.n_states_for_ortho, ist.n_states_for_sigma, flag.printCubes,
+                       ist.ncubes, flag.readCoeffs, flag.inputPsiFilt, ist.init_psi_start, ist.init_psi_end,
+                       flag.calcSpinAngStat, flag.isComplex};
+  memcpy(d, dv, sizeof dv);
+  memcpy(l, lv, sizeof lv);
+}

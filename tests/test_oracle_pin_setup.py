@@ -206,3 +206,74 @@ def test_output_writers_match_reference(rs, host, tmp_path, monkeypatch, name):
     assert host.fbse_write_psi(b"mine_psi.dat", _p(psi), psi.size) == 0
     for mine, ref in (("mine.cube", "ref.cube"), ("mine_eval.dat", "ref_eval.dat"), ("mine_psi.dat", "ref_psi.dat")):
         assert open(mine, "rb").read() == open(ref, "rb").read(), mine
+
+
+_SYNTH = """nx = 48
+ny = 44
+nz = 40
+dx = 0.7
+dy = 0.75
+dz = 0.8
+mStatesPerFilter = 12
+nFilterCycles = 3
+nCheby = 512
+VBmin = -0.42
+VBmax = -0.21
+CBmin = -0.16
+CBmax = -0.02
+KEmax = 12.5
+fermiEnergy = -0.185
+sigmaECut = 0.0005
+setTargets = 1 7 5
+setSeed = 1 -12345
+spinOrbit = 1
+NonLocal = 1
+getAllStates = 1
+approxEnergyRange = 1
+printPsiFilt = 0
+printPsiDiag = 1
+calcFilterOnly = 0
+restartFromOrtho = 1 36
+printCubes = 1 6
+readCoeffs = 1
+inputPsiFilt = 1 4 40
+calcSpinAngStat = 1
+"""
+
+
+@pytest.mark.parametrize("name", ["cdse22", "cspbi3", "synthetic"])
+def test_input_parser_matches_reference(rs, host, tmp_path, monkeypatch, name):
+    """read_input (read.c:5-995) against the library's host
+    fbse_read_filter_params on the examples' input.par and on one that sets
+    every key the drop-in reads, multi-value keys included: grid, windows,
+    targets, seed, projector switches (spinors and complex storage follow
+    spinOrbit), output and restart switches with their counts"""
+    if name == "synthetic":
+        (tmp_path / "input.par").write_text(_SYNTH)
+        shutil.copy(os.path.join(GOLD, "cspbi3", "conf.par"), tmp_path / "conf.par")
+    else:
+        for f in ("input.par", "conf.par"):
+            shutil.copy(os.path.join(GOLD, name, f), tmp_path / f)
+    monkeypatch.chdir(tmp_path)
+    rs.ref_read_input.argtypes = [D, LP]
+    d = np.zeros(10)
+    lv = np.zeros(31, np.int64)
+    rs.ref_read_input(_p(d), _p(lv, LP))
+    p = FilterParams()
+    err = ctypes.create_string_buffer(512)
+    assert host.fbse_read_filter_params(b"input.par", ctypes.byref(p), err, 512) == 0, err.value
+    mine_d = [p.dx, p.dy, p.dz, p.vbmin, p.vbmax, p.cbmin, p.cbmax, p.ke_max, p.fermi_e, p.sigma_e_cut]
+    assert mine_d == list(d)
+    keys = ["nx", "ny", "nz", "m_states_per_filter", "n_filter_cycles", "ncheby", "set_targets", "n_targets_vb",
+            "n_targets_cb", "set_seed", "seed", "use_spinors", "so", "nl", "get_all_states", "approx_energy_range",
+            "print_psi_filt", "print_psi_diag", "calc_filter_only", "restart_from_ortho", "restart_from_sigma",
+            "n_states_for_ortho", "n_states_for_sigma", "print_cubes", "ncubes", "read_coeffs", "input_psi_filt",
+            "init_psi_start", "init_psi_end", "calc_spin_ang_stat"]
+    ref = dict(zip(keys + ["is_complex"], (int(v) for v in lv)))
+    if not ref["set_targets"]:
+        # read_input leaves the counts unset; the host holds set_ene_targets' half / half split
+        for k in ("n_targets_vb", "n_targets_cb"):
+            ref.pop(k)
+    mine = {k: int(getattr(p, k)) for k in keys if k in ref}
+    assert mine == {k: v for k, v in ref.items() if k != "is_complex"}
+    assert ref["is_complex"] == ref["use_spinors"]  # complex storage follows the spinors (read.c:916-920)
