@@ -171,11 +171,15 @@ int fbse_read_filter_params(const char *path, fbse_filter_params *p, char *err, 
 int fbse_read_bse_params(const char *path, fbse_bse_params *p, char *err, size_t errlen)
 {
   memset(p, 0, sizeof(*p));
+  /* the defaults of bse_cplx/read.c:38-63; the dielectric constants have
+   * none there (zero, which leaves the screened interaction unusable), so
+   * they default to vacuum here */
   p->max_hole_states = -1;
   p->max_elec_states = -1;
-  p->sigma_e_cut = 0.01;
+  p->sigma_e_cut = 0.0001;
   p->eps_x = p->eps_y = p->eps_z = 1.0;
   p->fermi_e = -0.18;
+  p->calc_spin_ang_stat = 1;
   FILE *f = fopen(path, "r");
   if (!f) { seterr(err, errlen, "cannot open", path); return -1; }
   char key[1000], val[1000];

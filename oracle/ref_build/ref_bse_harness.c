@@ -173,3 +173,26 @@ void ref_bse_qp_basis(double *eval, double *sigma, long n, double sigma_cut, dou
   free(hole);
   free(elec);
 }
+
+void read_input(flag_st *flag, grid_st *grid, index_st *ist, par_st *par, parallel_st *parallel);
+
+/* read_input of the BSE stage (bse_cplx/read.c:7-220) at a non-zero rank on
+ * input.par in the working directory.  d[8]: sigma_E_cut, epsX, epsY, epsZ,
+ * fermi_E, delta_E_hole, delta_E_elec, KE_max.  l[9]: max_hole_states,
+ * max_elec_states, coulombDone, restartCoulomb, calcCoulombOnly,
+ * calcSpinAngStat, SO, NL, useSpinors. */
+void ref_bse_read_input(double *d, long *l)
+{
+  struct bjob j;
+  double g0 = 0;
+  bjob_init(&j, 1, 1, 1, 1, 1, 1, 0, 0, 0, &g0, &g0, &g0, 0, 0, 0);
+  memset(&j.flag, 0, sizeof j.flag);
+  j.pl.mpi_rank = 1;
+  read_input(&j.flag, &j.grid, &j.ist, &j.par, &j.pl);
+  const double dv[8] = {j.par.sigma_E_cut, j.par.epsX, j.par.epsY, j.par.epsZ,
+                        j.par.fermi_E, j.par.delta_E_hole, j.par.delta_E_elec, j.par.KE_max};
+  const long lv[9] = {j.ist.max_hole_states, j.ist.max_elec_states, j.flag.coulombDone, j.flag.restartCoulomb,
+                      j.flag.calcCoulombOnly, j.flag.calcSpinAngStat, j.flag.SO, j.flag.NL, j.flag.useSpinors};
+  memcpy(d, dv, sizeof dv);
+  memcpy(l, lv, sizeof lv);
+}

@@ -262,3 +262,41 @@ def test_qp_basis_matches_reference(rb, tmp_path, monkeypatch, name, cut, fermi,
         assert np.array_equal(er[nh:nq], compact[nh:nq]) and not np.array_equal(er[nh:nq], e[mine[nh:nq]])
     else:
         assert np.array_equal(er[nh:nq], e[mine[nh:nq]])
+
+
+class BseParams(ctypes.Structure):
+    _fields_ = [("max_hole_states", ctypes.c_long), ("max_elec_states", ctypes.c_long),
+                ("sigma_e_cut", ctypes.c_double), ("eps_x", ctypes.c_double), ("eps_y", ctypes.c_double),
+                ("eps_z", ctypes.c_double), ("fermi_e", ctypes.c_double), ("delta_e_hole", ctypes.c_double),
+                ("delta_e_elec", ctypes.c_double), ("precision", ctypes.c_int), ("coulomb_done", ctypes.c_int),
+                ("restart_coulomb", ctypes.c_int), ("calc_coulomb_only", ctypes.c_int),
+                ("calc_spin_ang_stat", ctypes.c_int)]
+
+
+@pytest.mark.parametrize("text", [
+    "epsX = 5.0\nepsY = 5.0\nepsZ = 5.0\n",
+    "maxHoleStates = 10\nmaxElecStates = 10\nsigmaECut = 0.0001\nepsX = 6.1\nepsY = 6.1\nepsZ = 6.1\n"
+    "nThreads = 1\nspinOrbit = 1\nNonLocal = 1\ncalcDarkStates = 0\ncalcSpinAngStat = 0\n",
+    "maxHoleStates = 4\nmaxElecStates = 3\nsigmaECut = 0.01\nepsX = 5.0\nepsY = 5.5\nepsZ = 6.0\n"
+    "fermiEnergy = -0.2\ndeltaEhole = 0.1\ndeltaEelec = 0.05\ncoulombDone = 1\nrestartCoulomb = 0\n"
+    "calcCoulombOnly = 1\n"])
+def test_bse_input_parser_matches_reference(rb, tmp_path, monkeypatch, text):
+    """read_input of the BSE stage (bse_cplx/read.c:7-220) against the
+    library's host fbse_read_bse_params: basis limits, cut, dielectric
+    constants, Fermi energy, energy spans, kernel-file switches and
+    calcSpinAngStat, defaults included"""
+    import filterbse_gb300 as F
+    (tmp_path / "input.par").write_text(text)
+    monkeypatch.chdir(tmp_path)
+    rb.ref_bse_read_input.argtypes = [D, ctypes.POINTER(ctypes.c_long)]
+    d = np.zeros(8)
+    lv = np.zeros(9, np.int64)
+    rb.ref_bse_read_input(_p(d), lv.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+    L = F.load()
+    L.fbse_read_bse_params.argtypes = [ctypes.c_char_p, ctypes.POINTER(BseParams), ctypes.c_char_p, ctypes.c_size_t]
+    p = BseParams()
+    err = ctypes.create_string_buffer(512)
+    assert L.fbse_read_bse_params(b"input.par", ctypes.byref(p), err, 512) == 0, err.value
+    assert [p.sigma_e_cut, p.eps_x, p.eps_y, p.eps_z, p.fermi_e, p.delta_e_hole, p.delta_e_elec] == list(d[:7])
+    assert [p.max_hole_states, p.max_elec_states, p.coulomb_done, p.restart_coulomb, p.calc_coulomb_only,
+            p.calc_spin_ang_stat] == [int(v) for v in lv[:6]]
