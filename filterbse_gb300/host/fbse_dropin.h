@@ -106,6 +106,19 @@ void fbse_energy_range_rule(int approx, int so, int nl, double vmin_loc, double 
 int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n);
 int fbse_write_psi(const char *path, const double *psi, long n_doubles);
 
+/* the atom id of a conf.par label (assign_atom_number, read.c:2452-2545) */
+long fbse_atom_number(const char *label);
+
+/* output.dat (save_output, save.c:446-503): tag on the first line, the
+ * types' ids from their labels (labels8: ntypes x 8 chars), the grid
+ * metadata as init_grid_params leaves it, then axes, eval, sigma and the
+ * states.  Returns 0 or -1. */
+int fbse_write_output(const char *path, long tag, long natoms, const double *xyz, int ntypes, const char *labels8,
+                      long nx, long ny, long nz, double dx, double dy, double dz, const double *gx, const double *gy,
+                      const double *gz, double xmin, double ymin, double zmin, double ke_max, double fermi_e, int so,
+                      int nl, int use_spinors, int nspin, int cplx, long n, const double *eval, const double *sigma,
+                      const double *psi);
+
 /* calc_xton_spin_mtrx + calc_xton_ang_mom_mtrx (bse_cplx/angular.c:692-1043):
  * per exciton n (complex, interleaved) <S> spin[n][3], the two-body spin sum
  * spintot[n] (spins.dat prints 1.5 + 2 Re), <L> orbit[n][3], the <L^2> sum

@@ -44,42 +44,6 @@ static void check(fbse_ctx *c, int rc, const char *what)
   }
 }
 
-static void save_output(const char *path, const fbse_filter_params *p, long natoms, const double *xyz,
-                        int ntypes, long nx, long ny, long nz, double dx, double dy, double dz, const double *gx,
-                        const double *gy, const double *gz, double xmin, double ymin, double zmin, int nspin,
-                        int cplx, long n, const double *eval, const double *sigma, const double *psi)
-{ /* save_output (filter_mpi/save.c:446-503) */
-  FILE *f = fopen(path, "wb");
-  if (!f) die("cannot write", path);
-  const long ngrid = nx * ny * nz;
-  const double dkx = 2.0 * M_PI / ((nx % 2 == 0) ? nx * dx : (nx - 1) * dx);
-  const double dky = 2.0 * M_PI / ((ny % 2 == 0) ? ny * dy : (ny - 1) * dy);
-  const double dkz = 2.0 * M_PI / ((nz % 2 == 0) ? nz * dz : (nz - 1) * dz);
-  fprintf(f, "%ld\n", (long)random());
-  fprintf(f, "%ld %ld\n", ngrid, nspin * ngrid);
-  fprintf(f, "%ld\n", n);
-  fprintf(f, "%ld %d\n", natoms, ntypes);
-  for (int j = 0; j < ntypes; j++) fprintf(f, "%d ", j);
-  fprintf(f, "%d\n", nspin);
-  fprintf(f, "%d\n", cplx + 1);
-  fprintf(f, "%g %g\n", p->ke_max, p->fermi_e);
-  fprintf(f, "%d %d %d %d %d\n", p->so, p->nl, 0, p->use_spinors, cplx);
-  for (long j = 0; j < natoms; j++) fprintf(f, "%g %g %g\n", xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2]);
-  fprintf(f, "%g %g %g %g %g %g %g %g\n", dx, dy, dz, sqrt(dx * dx + dy * dy + dz * dz), dx * dy * dz, dkx, dky, dkz);
-  fprintf(f, "%g %g %g %g %g %g\n", xmin, -xmin, ymin, -ymin, zmin, -zmin);
-  fprintf(f, "%ld %ld %ld\n", nx, ny, nz);
-  fprintf(f, "%g %g %g\n", 1.0 / nx, 1.0 / ny, 1.0 / nz);
-  fprintf(f, "%ld", ngrid);
-  fwrite(gx, sizeof(double), nx, f);
-  fwrite(gy, sizeof(double), ny, f);
-  fwrite(gz, sizeof(double), nz, f);
-  fwrite(eval, sizeof(double), n, f);
-  fwrite(sigma, sizeof(double), n, f);
-  fwrite(psi, sizeof(double), (size_t)(cplx + 1) * nspin * ngrid * n, f);
-  fprintf(f, "\n\nEOF\n");
-  fclose(f);
-}
-
 /* homo_idx / lumo_idx of print_eigstate_densities (mod_optional_output.c:
  * 103-147): homo is the last converged state below fermiEnergy, lumo the next
  * converged one (0 when there is none), in eval.dat's order */
@@ -540,8 +504,11 @@ int main(void)
   printf("%ld eigenstates written\n", n_out);
   if (fbse_write_eval("eval.dat", eval, sigma, n_out)) die("cannot write", "eval.dat");
   if (fbse_write_psi("psi.dat", psi, n_out * stlen)) die("cannot write", "psi.dat");
-  save_output("output.dat", &p, natoms, xyz, ntypes, nx, ny, nz, p.dx, p.dy, p.dz, gx, gy, gz, xmin, ymin, zmin,
-              nspin, cplx, n_out, eval, sigma, psi);
+  /* save_output (filter_mpi/save.c:446-503); its first line is a random tag */
+  if (fbse_write_output("output.dat", (long)random(), natoms, xyz, ntypes, (const char *)names, nx, ny, nz, p.dx, p.dy,
+                        p.dz, gx, gy, gz, xmin, ymin, zmin, p.ke_max, p.fermi_e, p.so, p.nl, p.use_spinors, nspin,
+                        cplx, n_out, eval, sigma, psi))
+    die("cannot write", "output.dat");
   check(ctx, fbse_free(ctx, d_psi), "free");
   if (p.print_cubes == 1)
     write_cubes(&p, psi, eval, sigma, n_out, nx, ny, nz, xmin, ymin, zmin, nspin, cplx, natoms, xyz, atype, names);

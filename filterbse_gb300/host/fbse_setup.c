@@ -711,6 +711,66 @@ int fbse_write_cube(const char *path, const double *rho, long nx, long ny, long 
   return 0;
 }
 
+long fbse_atom_number(const char *label)
+{ /* the atom ids of read_conf (assign_atom_number, filter_mpi/read.c:2452-2545):
+   * elements by atomic number, the ligand and pseudo-atom labels by their own
+   * small ids, 0 for a label outside the list */
+  static const struct { const char *sym; long id; } tab[] = {
+      {"H", 1},    {"P1", 2},   {"P2", 3},   {"P3", 4},   {"PC5", 5},  {"C", 6},    {"PC6", 7},  {"PR1", 8},
+      {"PR2", 9},  {"PR3", 10}, {"PA1", 11}, {"PA2", 12}, {"PA3", 13}, {"Si", 14},  {"P", 15},   {"S", 16},
+      {"Cl", 17},  {"C1", 18},  {"C2", 19},  {"C3", 20},  {"Zn", 30},  {"Ga", 31},  {"As", 33},  {"Se", 34},
+      {"Br", 35},  {"Cd", 48},  {"In", 49},  {"Te", 52},  {"I", 53},   {"Cs", 55},  {"Pb", 82},  {"Br0", 100},
+      {"Br1", 101}, {"I0", 102}, {"I1", 103}, {NULL, 0}};
+  for (int i = 0; tab[i].sym; i++)
+    if (!strcmp(label, tab[i].sym)) return tab[i].id;
+  return 0;
+}
+
+int fbse_write_output(const char *path, long tag, long natoms, const double *xyz, int ntypes, const char *labels8,
+                      long nx, long ny, long nz, double dx, double dy, double dz, const double *gx, const double *gy,
+                      const double *gz, double xmin, double ymin, double zmin, double ke_max, double fermi_e, int so,
+                      int nl, int use_spinors, int nspin, int cplx, long n, const double *eval, const double *sigma,
+                      const double *psi)
+{ /* save_output (filter_mpi/save.c:446-503) with the grid as init_grid_params
+   * leaves it (init.c:5-256): box n d (even n) or (n - 1) d (odd n), max
+   * (n - 1) d / 2, dk = 2 pi / box */
+  FILE *f = fopen(path, "wb");
+  if (!f) return -1;
+  const long ngrid = nx * ny * nz;
+  const long n3[3] = {nx, ny, nz};
+  const double d3[3] = {dx, dy, dz};
+  double dk[3], mx[3];
+  for (int a = 0; a < 3; a++) {
+    const double box = (n3[a] % 2 == 0) ? (double)n3[a] * d3[a] : (double)(n3[a] - 1) * d3[a];
+    dk[a] = 6.283185307179586476925 / box;
+    mx[a] = ((double)(n3[a] - 1) * d3[a]) / 2.0;
+  }
+  fprintf(f, "%ld\n", tag);
+  fprintf(f, "%ld %ld\n", ngrid, nspin * ngrid);
+  fprintf(f, "%ld\n", n);
+  fprintf(f, "%ld %d\n", natoms, ntypes);
+  for (int j = 0; j < ntypes; j++) fprintf(f, "%ld ", fbse_atom_number(labels8 + 8 * j));
+  fprintf(f, "%d\n", nspin);
+  fprintf(f, "%d\n", cplx + 1);
+  fprintf(f, "%g %g\n", ke_max, fermi_e);
+  fprintf(f, "%d %d %d %d %d\n", so, nl, 0, use_spinors, cplx);
+  for (long j = 0; j < natoms; j++) fprintf(f, "%g %g %g\n", xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2]);
+  fprintf(f, "%g %g %g %g %g %g %g %g\n", dx, dy, dz, sqrt(dx * dx + dy * dy + dz * dz), dx * dy * dz, dk[0], dk[1],
+          dk[2]);
+  fprintf(f, "%g %g %g %g %g %g\n", xmin, mx[0], ymin, mx[1], zmin, mx[2]);
+  fprintf(f, "%ld %ld %ld\n", nx, ny, nz);
+  fprintf(f, "%g %g %g\n", 1.0 / (double)nx, 1.0 / (double)ny, 1.0 / (double)nz);
+  fprintf(f, "%ld", ngrid);
+  fwrite(gx, sizeof(double), nx, f);
+  fwrite(gy, sizeof(double), ny, f);
+  fwrite(gz, sizeof(double), nz, f);
+  fwrite(eval, sizeof(double), n, f);
+  fwrite(sigma, sizeof(double), n, f);
+  fwrite(psi, sizeof(double), (size_t)(cplx + 1) * nspin * ngrid * n, f);
+  fprintf(f, "\n\nEOF\n");
+  return fclose(f) ? -1 : 0;
+}
+
 int fbse_write_psi(const char *path, const double *psi, long n_doubles)
 {
   FILE *f = fopen(path, "wb");

@@ -614,3 +614,69 @@ void ref_read_input(double *d, long *l)
   memcpy(d, dv, sizeof dv);
   memcpy(l, lv, sizeof lv);
 }
+
+void save_output(char *file_name, double *psitot, double *eig_vals, double *sigma_E, xyz_st *R, grid_st *grid,
+                 index_st *ist, par_st *par, flag_st *flag, parallel_st *parallel);
+
+/* save_output (save.c:446-503) into ref_output.dat after read_conf,
+ * init_grid_params and the axes of build_grid_ksqr (init.c:259-290) on
+ * conf.par in the working directory, for n states of psitot with their
+ * eigenvalues and variances.  Returns 0 or -1. */
+int ref_save_output(double dgrid, const long *n_in, double ke_max, double fermi_e, int so, int nl, long n,
+                    double *eval, double *sigma, double *psitot)
+{
+  FILE *pf = fopen("conf.par", "r");
+  long nat = 0;
+  if (!pf || fscanf(pf, "%ld", &nat) != 1) {
+    if (pf) fclose(pf);
+    return -1;
+  }
+  fclose(pf);
+  grid_st grid;
+  index_st ist;
+  par_st par;
+  flag_st flag;
+  parallel_st pl;
+  memset(&grid, 0, sizeof grid);
+  memset(&ist, 0, sizeof ist);
+  memset(&par, 0, sizeof par);
+  memset(&flag, 0, sizeof flag);
+  memset(&pl, 0, sizeof pl);
+  ist.n_max_atom_types = N_MAX_ATOM_TYPES;
+  ist.atom_types = calloc(N_MAX_ATOM_TYPES, sizeof(long));
+  ist.natoms = nat;
+  flag.centerConf = 1;
+  flag.SO = so;
+  flag.NL = nl;
+  flag.useSpinors = so;
+  flag.isComplex = so;
+  ist.nspin = so ? 2 : 1;
+  ist.complex_idx = so ? 2 : 1;
+  ist.mn_states_tot = n;
+  par.KE_max = ke_max;
+  par.fermi_E = fermi_e;
+  pl.nthreads = 1;
+  pl.mpi_rank = 1;
+  grid.nx = n_in[0];
+  grid.ny = n_in[1];
+  grid.nz = n_in[2];
+  grid.dx = grid.dy = grid.dz = dgrid;
+  xyz_st *R = calloc(nat, sizeof(xyz_st));
+  atom_info *atom = calloc(nat, sizeof(atom_info));
+  read_conf(R, atom, &ist, &par, &flag, &pl);
+  init_grid_params(&grid, R, &ist, &par, &flag, &pl);
+  grid.x = calloc(grid.nx, sizeof(double));
+  grid.y = calloc(grid.ny, sizeof(double));
+  grid.z = calloc(grid.nz, sizeof(double));
+  double *ksqr = calloc(grid.ngrid, sizeof(double));
+  build_grid_ksqr(ksqr, R, &grid, &ist, &par, &flag, &pl);
+  save_output("ref_output.dat", psitot, eval, sigma, R, &grid, &ist, &par, &flag, &pl);
+  free(ksqr);
+  free(grid.x);
+  free(grid.y);
+  free(grid.z);
+  free(R);
+  free(atom);
+  free(ist.atom_types);
+  return 0;
+}

@@ -27,5 +27,4 @@ void hamiltonian_k(void) { unreachable("hamiltonian_k"); }
 void kinetic_k(void) { unreachable("kinetic_k"); }
 void p_hamiltonian_k(void) { unreachable("p_hamiltonian_k"); }
 void read_nearest_neighbors(void) { unreachable("read_nearest_neighbors"); }
-void print_input_state(void) { unreachable("print_input_state"); }
 void retScaledVector(void) { unreachable("retScaledVector"); }

@@ -277,3 +277,58 @@ def test_input_parser_matches_reference(rs, host, tmp_path, monkeypatch, name):
     mine = {k: int(getattr(p, k)) for k in keys if k in ref}
     assert mine == {k: v for k, v in ref.items() if k != "is_complex"}
     assert ref["is_complex"] == ref["use_spinors"]  # complex storage follows the spinors (read.c:916-920)
+
+
+@pytest.mark.parametrize("name", ["cdse22", "cspbi3"])
+def test_output_dat_matches_reference(rs, host, tmp_path, monkeypatch, name):
+    """save_output (save.c:446-503) after read_conf / init_grid_params /
+    build_grid_ksqr against the library's host fbse_write_output on the same
+    job: every byte after the random tag of the first line (sizes, the types'
+    atom ids, switches, centred atoms, the grid metadata, axes, eigenvalues,
+    variances and states)"""
+    src = os.path.join(GOLD, name)
+    shutil.copy(os.path.join(src, "conf.par"), tmp_path / "conf.par")
+    monkeypatch.chdir(tmp_path)
+    prm = FilterParams()
+    err = ctypes.create_string_buffer(512)
+    assert host.fbse_read_filter_params(os.path.join(src, "input.par").encode(), ctypes.byref(prm), err, 512) == 0
+    so, nl = int(prm.so), int(prm.nl)
+    nspin, cplx = (2, 1) if so else (1, 0)
+    hn = ctypes.c_long()
+    hx, ht = D(), IP()
+    names = (ctypes.c_char * 8 * 32)()
+    nt = ctypes.c_int()
+    assert host.fbse_read_conf(b"conf.par", ctypes.byref(hn), ctypes.byref(hx), ctypes.byref(ht), names,
+                               ctypes.byref(nt), err, 512) == 0
+    na = hn.value
+    xyz = np.ctypeslib.as_array(hx, (3 * na,)).copy()
+    n3, lo, axes = [], [], []
+    for ax, nin in enumerate((prm.nx, prm.ny, prm.nz)):
+        nn, x0 = ctypes.c_long(), ctypes.c_double()
+        host.fbse_grid_rule(_p(xyz), na, prm.dx, nin, ax, ctypes.byref(nn), ctypes.byref(x0))
+        a = np.zeros(nn.value)
+        host.fbse_grid_axis(nn.value, x0.value, prm.dx, _p(a))
+        n3.append(nn.value)
+        lo.append(x0.value)
+        axes.append(a)
+    ngrid = n3[0] * n3[1] * n3[2]
+    rng = np.random.default_rng(11)
+    n = 3
+    ev = np.ascontiguousarray(np.sort(rng.uniform(-0.4, 0.0, n)))
+    sg = np.ascontiguousarray(10.0 ** rng.uniform(-8, -3, n))
+    psi = np.ascontiguousarray(rng.standard_normal(n * (cplx + 1) * nspin * ngrid))
+    rs.ref_save_output.argtypes = [ctypes.c_double, LP, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_long, D, D, D]
+    n_in = np.array([prm.nx, prm.ny, prm.nz], np.int64)
+    assert rs.ref_save_output(prm.dx, _p(n_in, LP), prm.ke_max, prm.fermi_e, so, nl, n, _p(ev.copy()), _p(sg.copy()),
+                              _p(psi)) == 0
+    host.fbse_write_output.argtypes = ([ctypes.c_char_p, ctypes.c_long, ctypes.c_long, D, ctypes.c_int,
+                                        ctypes.c_char_p] + [ctypes.c_long] * 3 + [ctypes.c_double] * 3 + [D] * 3 +
+                                       [ctypes.c_double] * 5 + [ctypes.c_int] * 5 + [ctypes.c_long, D, D, D])
+    labels = b"".join(names[k].value.ljust(8, b"\0") for k in range(nt.value))
+    assert host.fbse_write_output(b"mine_output.dat", 0, na, _p(xyz), nt.value, labels, *n3, prm.dx, prm.dx, prm.dx,
+                                  *[_p(a) for a in axes], *lo, prm.ke_max, prm.fermi_e, so, nl, so, nspin, cplx, n,
+                                  _p(ev), _p(sg), _p(psi)) == 0
+    ref = open("ref_output.dat", "rb").read()
+    mine = open("mine_output.dat", "rb").read()
+    assert mine.split(b"\n", 1)[1] == ref.split(b"\n", 1)[1]
