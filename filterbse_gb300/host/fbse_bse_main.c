@@ -153,24 +153,6 @@ static void write_matrices(fbse_ctx *ctx, void *d_dir, void *d_exc, void *d_coef
   free(cm);
 }
 
-/* qp_spin_frac (bse_cplx/spin.c:3-60): the norm of each spin block of every
- * quasiparticle spinor, qp_spins.dat */
-static void write_qp_spins(const double *psi, const double *eqp, long nqp, long ngrid, double dv)
-{
-  FILE *f = fopen("qp_spins.dat", "w");
-  if (!f) die("cannot write", "qp_spins.dat");
-  for (long i = 0; i < nqp; i++) {
-    fprintf(f, "\nStats on state%lu: (E=%lg)\n", (unsigned long)i, eqp[i]);
-    for (int s = 0; s < 2; s++) {
-      const double *q = psi + (i * 2 + s) * 2 * ngrid;
-      double pct = 0.0;
-      for (long g = 0; g < ngrid; g++) pct += q[2 * g] * q[2 * g] + q[2 * g + 1] * q[2 * g + 1];
-      fprintf(f, " Spin %d fraction: %f\n", s, pct * dv);
-    }
-  }
-  fclose(f);
-}
-
 /* calcSpinAngStat (bse_cplx/main.c:160-195): the quasiparticle spin and
  * angular-momentum matrices (sx/sy/sz.dat, lx/ly/lz/lsqr/ls.dat,
  * angular.c:116-129, 200-211, 436-460, 562-586) and the exciton statistics
@@ -503,7 +485,8 @@ int main(void)
               (2.0 / 3.0) * ene[j] * os, m[0], m[1], m[2], m[3], m[4], m[5]);
   }
   fclose(po);
-  if (!real) write_qp_spins(psi_host, eqp, nqp, o.ngrid, o.dx * o.dy * o.dz);
+  if (!real && fbse_write_qp_spins("qp_spins.dat", psi_host, eqp, nqp, o.ngrid, o.dx * o.dy * o.dz))
+    die("cannot write", "qp_spins.dat");
   /* M.dat, rs.dat and bs-coeff-<j>.dat for j < 10 (optical.c:29-95) */
   FILE *pm = fopen("M.dat", "w"), *prs = fopen("rs.dat", "w");
   if (!pm || !prs) die("cannot write", "M.dat / rs.dat");

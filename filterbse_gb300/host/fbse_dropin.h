@@ -106,6 +106,10 @@ void fbse_energy_range_rule(int approx, int so, int nl, double vmin_loc, double 
 int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n);
 int fbse_write_psi(const char *path, const double *psi, long n_doubles);
 
+/* qp_spins.dat (qp_spin_frac, bse_cplx/spin.c:3-60): per spinor of psi
+ * (nqp complex spinors of 2 ngrid points) its two spin-block norms; 0 or -1 */
+int fbse_write_qp_spins(const char *path, const double *psi, const double *eqp, long nqp, long ngrid, double dv);
+
 /* the atom id of a conf.par label (assign_atom_number, read.c:2452-2545) */
 long fbse_atom_number(const char *label);
 

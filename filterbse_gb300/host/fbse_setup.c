@@ -711,6 +711,23 @@ int fbse_write_cube(const char *path, const double *rho, long nx, long ny, long 
   return 0;
 }
 
+int fbse_write_qp_spins(const char *path, const double *psi, const double *eqp, long nqp, long ngrid, double dv)
+{ /* qp_spin_frac (bse_cplx/spin.c:3-60): the norm of each spin block of every
+   * quasiparticle spinor (complex, interleaved, up block then down block) */
+  FILE *f = fopen(path, "w");
+  if (!f) return -1;
+  for (long i = 0; i < nqp; i++) {
+    fprintf(f, "\nStats on state%lu: (E=%lg)\n", (unsigned long)i, eqp[i]);
+    for (int s = 0; s < 2; s++) {
+      const double *q = psi + (i * 2 + s) * 2 * ngrid;
+      double pct = 0.0;
+      for (long g = 0; g < ngrid; g++) pct += q[2 * g] * q[2 * g] + q[2 * g + 1] * q[2 * g + 1];
+      fprintf(f, " Spin %d fraction: %f\n", s, pct * dv);
+    }
+  }
+  return fclose(f) ? -1 : 0;
+}
+
 long fbse_atom_number(const char *label)
 { /* the atom ids of read_conf (assign_atom_number, filter_mpi/read.c:2452-2545):
    * elements by atomic number, the ligand and pseudo-atom labels by their own

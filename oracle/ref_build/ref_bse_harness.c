@@ -196,3 +196,18 @@ void ref_bse_read_input(double *d, long *l)
   memcpy(d, dv, sizeof dv);
   memcpy(l, lv, sizeof lv);
 }
+
+void qp_spin_frac(double complex *psi_qp, double *eig_vals, grid_st *grid, index_st *ist, par_st *par,
+                  flag_st *flag, parallel_st *parallel);
+
+/* qp_spin_frac (bse_cplx/spin.c:3-60): qp_spins.dat for n_qp complex spinors
+ * of ngrid points per spin block, into the working directory */
+void ref_bse_qp_spins(double *psi_qp, double *eval, long n_qp, long nx, long ny, long nz, double dv)
+{
+  struct bjob j;
+  double g0 = 0;
+  bjob_init(&j, nx, ny, nz, 1, 1, dv, 0, 0, 0, &g0, &g0, &g0, 0, 0, 0);
+  j.ist.n_qp = n_qp;
+  j.par.dv = dv;
+  qp_spin_frac((double complex *)psi_qp, eval, &j.grid, &j.ist, &j.par, &j.flag, &j.pl);
+}

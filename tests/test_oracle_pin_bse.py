@@ -300,3 +300,18 @@ def test_bse_input_parser_matches_reference(rb, tmp_path, monkeypatch, text):
     assert [p.sigma_e_cut, p.eps_x, p.eps_y, p.eps_z, p.fermi_e, p.delta_e_hole, p.delta_e_elec] == list(d[:7])
     assert [p.max_hole_states, p.max_elec_states, p.coulomb_done, p.restart_coulomb, p.calc_coulomb_only,
             p.calc_spin_ang_stat] == [int(v) for v in lv[:6]]
+
+
+def test_qp_spins_dat_matches_reference(rb, tmp_path, monkeypatch):
+    """qp_spin_frac (bse_cplx/spin.c:3-60) against the library's host
+    fbse_write_qp_spins: qp_spins.dat byte for byte"""
+    import filterbse_gb300 as F
+    monkeypatch.chdir(tmp_path)
+    rb.ref_bse_qp_spins.argtypes = [D, D] + [ctypes.c_long] * 4 + [ctypes.c_double]
+    psi = np.ascontiguousarray(qp_states(GRID, 7, 79))
+    ev = np.ascontiguousarray(np.linspace(-0.31, -0.02, 7))
+    rb.ref_bse_qp_spins(_p(psi.view(np.float64)), _p(ev), 7, GRID.nx, GRID.ny, GRID.nz, GRID.dv)
+    L = F.load()
+    L.fbse_write_qp_spins.argtypes = [ctypes.c_char_p, D, D, ctypes.c_long, ctypes.c_long, ctypes.c_double]
+    assert L.fbse_write_qp_spins(b"mine_qp_spins.dat", _p(psi.view(np.float64)), _p(ev), 7, GRID.ngrid, GRID.dv) == 0
+    assert open("mine_qp_spins.dat", "rb").read() == open("qp_spins.dat", "rb").read()
