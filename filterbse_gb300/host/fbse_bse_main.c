@@ -222,43 +222,6 @@ static double im_dot_conj(const double *mu, const double *m)
   return r;
 }
 
-/* direct-<rank>.dat / exchange-<rank>.dat (bse_cplx/coulomb.c:289-371,
- * 534-602; one rank): "a b i j ibs jbs re im" per element.  direct: every
- * (a, b, i, j) in a, b, i, j order, zero above the diagonal (coulomb.c:360-371);
- * exchange: (a, i, b, j) order, lower triangle only (coulomb.c:586-600). */
-static void kline(FILE *f, long a, long b, long i, long j, long ibs, long jbs, const double *v, int real)
-{
-  if (real) /* bse_real/coulomb.c:352, 583: one value */
-    fprintf(f, "%03ld %03ld %03ld %03ld %ld %ld %.12f\n", a, b, i, j, ibs, jbs, v[0]);
-  else
-    fprintf(f, "%03ld %03ld %03ld %03ld %ld %ld %.12f %.12f\n", a, b, i, j, ibs, jbs, v[0], v[1]);
-}
-
-static void write_kernel_files(const double *dir, const double *exc, long nh, long ne, long lumo, int real)
-{
-  const long nx = nh * ne;
-  FILE *f = fopen("direct-0.dat", "w");
-  if (!f) die("cannot write", "direct-0.dat");
-  for (long a = lumo; a < lumo + ne; a++)
-    for (long b = lumo; b < lumo + ne; b++)
-      for (long i = 0; i < nh; i++)
-        for (long j = 0; j < nh; j++) {
-          const long ibs = (a - lumo) * nh + i, jbs = (b - lumo) * nh + j;
-          kline(f, a, b, i, j, ibs, jbs, dir + 2 * (ibs * nx + jbs), real);
-        }
-  fclose(f);
-  f = fopen("exchange-0.dat", "w");
-  if (!f) die("cannot write", "exchange-0.dat");
-  for (long a = lumo; a < lumo + ne; a++)
-    for (long i = 0; i < nh; i++)
-      for (long b = lumo; b < lumo + ne; b++)
-        for (long j = 0; j < nh; j++) {
-          const long ibs = (a - lumo) * nh + i, jbs = (b - lumo) * nh + j;
-          if (ibs < jbs) continue;
-          kline(f, a, b, i, j, ibs, jbs, exc + 2 * (ibs * nx + jbs), real);
-        }
-  fclose(f);
-}
 
 /* load_coulomb_mat (bse_cplx/coulomb.c:742-817): fills mat[ibs][jbs] from the
  * lines of path; the file is complete when the largest a, b reach the last
@@ -395,14 +358,14 @@ int main(void)
       fbse_free(ctx, d_xr);
       check(ctx, fbse_upload(ctx, d_dir, hd, mbytes), "upload");
       check(ctx, fbse_upload(ctx, d_exc, hx, mbytes), "upload");
-      write_kernel_files(hd, hx, nh, ne, lumo, 1);
+      if (fbse_write_kernel_files(hd, hx, nh, ne, lumo, 1)) die("cannot write", "direct-0.dat / exchange-0.dat");
     } else {
       /* restartCoulomb = 1 continues an interrupted CPU run in the reference;
        * here the whole kernel is recomputed, which gives the same matrices */
       check(ctx, fbse_bse_kernel(ctx, d_psi, nh, ne, lumo, d_bare, d_scr, d_dir, d_exc), "BSE kernels");
       check(ctx, fbse_download(ctx, hd, d_dir, mbytes), "download");
       check(ctx, fbse_download(ctx, hx, d_exc, mbytes), "download");
-      write_kernel_files(hd, hx, nh, ne, lumo, 0);
+      if (fbse_write_kernel_files(hd, hx, nh, ne, lumo, 0)) die("cannot write", "direct-0.dat / exchange-0.dat");
     }
     free(hd);
     free(hx);

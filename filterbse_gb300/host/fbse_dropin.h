@@ -106,6 +106,11 @@ void fbse_energy_range_rule(int approx, int so, int nl, double vmin_loc, double 
 int fbse_write_eval(const char *path, const double *eval, const double *sigma, long n);
 int fbse_write_psi(const char *path, const double *psi, long n_doubles);
 
+/* direct-0.dat / exchange-0.dat in the working directory (bse_cplx/coulomb.c:
+ * 289-371, 534-602; bse_real/coulomb.c:352, 583): dir / exc [n_xton][n_xton]
+ * as (re, im) pairs; 0 or -1 */
+int fbse_write_kernel_files(const double *dir, const double *exc, long nh, long ne, long lumo, int real);
+
 /* qp_spins.dat (qp_spin_frac, bse_cplx/spin.c:3-60): per spinor of psi
  * (nqp complex spinors of 2 ngrid points) its two spin-block norms; 0 or -1 */
 int fbse_write_qp_spins(const char *path, const double *psi, const double *eqp, long nqp, long ngrid, double dv);

@@ -711,6 +711,46 @@ int fbse_write_cube(const char *path, const double *rho, long nx, long ny, long 
   return 0;
 }
 
+/* direct-<rank>.dat / exchange-<rank>.dat (bse_cplx/coulomb.c:289-371,
+ * 534-602; one rank): "a b i j ibs jbs re im" per element.  direct: every
+ * (a, b, i, j) in a, b, i, j order, zero above the diagonal (coulomb.c:360-371);
+ * exchange: (a, i, b, j) order, lower triangle only (coulomb.c:586-600).
+ * dir / exc: [n_xton][n_xton] as (re, im) pairs; real = 1 prints the real
+ * parts alone, as bse_real does. */
+static void kernel_line(FILE *f, long a, long b, long i, long j, long ibs, long jbs, const double *v, int real)
+{
+  if (real) /* bse_real/coulomb.c:352, 583: one value */
+    fprintf(f, "%03ld %03ld %03ld %03ld %ld %ld %.12f\n", a, b, i, j, ibs, jbs, v[0]);
+  else
+    fprintf(f, "%03ld %03ld %03ld %03ld %ld %ld %.12f %.12f\n", a, b, i, j, ibs, jbs, v[0], v[1]);
+}
+
+int fbse_write_kernel_files(const double *dir, const double *exc, long nh, long ne, long lumo, int real)
+{
+  const long nx = nh * ne;
+  FILE *f = fopen("direct-0.dat", "w");
+  if (!f) return -1;
+  for (long a = lumo; a < lumo + ne; a++)
+    for (long b = lumo; b < lumo + ne; b++)
+      for (long i = 0; i < nh; i++)
+        for (long j = 0; j < nh; j++) {
+          const long ibs = (a - lumo) * nh + i, jbs = (b - lumo) * nh + j;
+          kernel_line(f, a, b, i, j, ibs, jbs, dir + 2 * (ibs * nx + jbs), real);
+        }
+  fclose(f);
+  f = fopen("exchange-0.dat", "w");
+  if (!f) return -1;
+  for (long a = lumo; a < lumo + ne; a++)
+    for (long i = 0; i < nh; i++)
+      for (long b = lumo; b < lumo + ne; b++)
+        for (long j = 0; j < nh; j++) {
+          const long ibs = (a - lumo) * nh + i, jbs = (b - lumo) * nh + j;
+          if (ibs < jbs) continue;
+          kernel_line(f, a, b, i, j, ibs, jbs, exc + 2 * (ibs * nx + jbs), real);
+        }
+  return fclose(f) ? -1 : 0;
+}
+
 int fbse_write_qp_spins(const char *path, const double *psi, const double *eqp, long nqp, long ngrid, double dv)
 { /* qp_spin_frac (bse_cplx/spin.c:3-60): the norm of each spin block of every
    * quasiparticle spinor (complex, interleaved, up block then down block) */

@@ -315,3 +315,21 @@ def test_qp_spins_dat_matches_reference(rb, tmp_path, monkeypatch):
     L.fbse_write_qp_spins.argtypes = [ctypes.c_char_p, D, D, ctypes.c_long, ctypes.c_long, ctypes.c_double]
     assert L.fbse_write_qp_spins(b"mine_qp_spins.dat", _p(psi.view(np.float64)), _p(ev), 7, GRID.ngrid, GRID.dv) == 0
     assert open("mine_qp_spins.dat", "rb").read() == open("qp_spins.dat", "rb").read()
+
+
+def test_kernel_files_match_reference(rb, tmp_path, monkeypatch):
+    """direct-0.dat / exchange-0.dat as calc_eh_kernel_cplx writes them
+    (bse_cplx/coulomb.c:289-371, 534-602) against the library's host
+    fbse_write_kernel_files on the reference's own kernels, byte for byte"""
+    import filterbse_gb300 as F
+    nh, ne, lumo = 3, 2, 4
+    psi = np.ascontiguousarray(qp_states(GRID, lumo + ne, 83))
+    _, _, dr, xr = _kernels(rb, GRID, psi, nh, ne, lumo, tmp_path, monkeypatch)
+    mine = tmp_path / "mine"
+    mine.mkdir()
+    monkeypatch.chdir(mine)
+    L = F.load()
+    L.fbse_write_kernel_files.argtypes = [D, D] + [ctypes.c_long] * 3 + [ctypes.c_int]
+    assert L.fbse_write_kernel_files(_p(dr.view(np.float64)), _p(xr.view(np.float64)), nh, ne, lumo, 0) == 0
+    for name in ("direct-0.dat", "exchange-0.dat"):
+        assert (mine / name).read_bytes() == (tmp_path / name).read_bytes(), name

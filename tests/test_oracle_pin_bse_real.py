@@ -147,3 +147,23 @@ def test_bse_real_dipoles_and_optical_match_reference(rr, tmp_path, monkeypatch)
     assert np.allclose(os_rows[:, 3], 2.0 / 3.0 * xe * osc, atol=2e-8)
     assert np.allclose(os_rows[:, 4:7], mx.real, atol=2e-12)
     assert np.allclose(m_rows[:, 1], np.sqrt(np.sum(np.abs(mm) ** 2, axis=1)), atol=2e-8)
+
+
+def test_bse_real_kernel_files_match_reference(rr, tmp_path, monkeypatch):
+    """direct-0.dat / exchange-0.dat of the real stage (bse_real/coulomb.c:352,
+    583: one value per element) against the library's host
+    fbse_write_kernel_files (real = 1) on the reference's own kernels"""
+    import filterbse_gb300 as F
+    monkeypatch.chdir(tmp_path)
+    nh, ne, lumo = 3, 2, 4
+    psi = real_states(GRID, lumo + ne, 89)
+    _, _, dr, xr = _kernels(rr, psi, nh, ne, lumo)
+    mine = tmp_path / "mine"
+    mine.mkdir()
+    monkeypatch.chdir(mine)
+    L = F.load()
+    L.fbse_write_kernel_files.argtypes = [D, D] + [ctypes.c_long] * 3 + [ctypes.c_int]
+    pairs = [np.ascontiguousarray(np.stack([m, np.zeros_like(m)], axis=-1)) for m in (dr, xr)]
+    assert L.fbse_write_kernel_files(_p(pairs[0]), _p(pairs[1]), nh, ne, lumo, 1) == 0
+    for name in ("direct-0.dat", "exchange-0.dat"):
+        assert (mine / name).read_bytes() == (tmp_path / name).read_bytes(), name
