@@ -97,23 +97,9 @@ static void read_output(const char *path, output_dat *o)
 }
 
 /* one part (0: re, 1: im) of an n x n complex row-major matrix as text rows */
-static void write_part(const char *path, const double *m, long n, int part, const char *fmt, int prec)
-{
-  FILE *f = fopen(path, "w");
-  if (!f) die("cannot write", path);
-  for (long i = 0; i < n; i++, fputc('\n', f))
-    for (long j = 0; j < n; j++) fprintf(f, fmt, prec, m[2 * (i * n + j) + part]);
-  fclose(f);
-}
-
-/* the matrix files of build_h0_mat, build_BSE_mat and bethe_salpeter:
- * h0.dat (mod_bse.c:73-84, "%.6g "), bsRE/bsIM.dat = K^d + K^x
- * (mod_bse.c:126-144), HBSmatRE/IM.dat = h0 - K (bethe-salpeter.c:71-95) and
- * BSEcoeffRE/IM.dat, column j = exciton j (bethe-salpeter.c:115-133), all with
- * PR_LEN = 6 significant digits (bse_cplx/fd.h:131) */
 static void write_matrices(fbse_ctx *ctx, void *d_dir, void *d_exc, void *d_coef, const double *eqp, long nh,
                            long ne, long lumo, int real)
-{
+{ /* the matrix files of the solve, from the device kernels and coefficients */
   const long n = nh * ne;
   const size_t bytes = (size_t)n * n * 2 * sizeof(double);
   double *dm = malloc(bytes), *xm = malloc(bytes), *cm = malloc(bytes);
@@ -121,33 +107,7 @@ static void write_matrices(fbse_ctx *ctx, void *d_dir, void *d_exc, void *d_coef
   check(ctx, fbse_download(ctx, dm, d_dir, bytes), "download");
   check(ctx, fbse_download(ctx, xm, d_exc, bytes), "download");
   check(ctx, fbse_download(ctx, cm, d_coef, bytes), "download");
-  FILE *f = fopen("h0.dat", "w");
-  if (!f) die("cannot write", "h0.dat");
-  for (long i = 0; i < n; i++, fputc('\n', f))
-    for (long j = 0; j < n; j++) fprintf(f, "%.6g ", i == j ? eqp[lumo + i / nh] - eqp[i % nh] : 0.0);
-  fclose(f);
-  for (size_t k = 0; k < (size_t)n * n * 2; k++) dm[k] += xm[k]; /* K = K^d + K^x */
-  if (real) {
-    /* bse_real: bs.dat, HBSmat.dat, BSEcoeff.dat with row j = exciton j
-     * (bse_real/mod_bse.c:124-131, bethe-salpeter.c:78-114) */
-    write_part("bs.dat", dm, n, 0, "%.*g ", 6);
-  } else {
-    write_part("bsRE.dat", dm, n, 0, "%.*g ", 6);
-    write_part("bsIM.dat", dm, n, 1, "%.*g ", 6);
-  }
-  for (size_t k = 0; k < (size_t)n * n * 2; k++) dm[k] = -dm[k];
-  for (long i = 0; i < n; i++) dm[2 * (i * n + i)] += eqp[lumo + i / nh] - eqp[i % nh];
-  if (real) {
-    write_part("HBSmat.dat", dm, n, 0, "%.*g \t", 6);
-    for (long i = 0; i < n; i++) /* transpose */
-      for (long j = 0; j < n; j++) xm[2 * (i * n + j)] = cm[2 * (j * n + i)];
-    write_part("BSEcoeff.dat", xm, n, 0, "%.*g\t", 6);
-  } else {
-    write_part("HBSmatRE.dat", dm, n, 0, "%.*g \t", 6);
-    write_part("HBSmatIM.dat", dm, n, 1, "%.*g \t", 6);
-    write_part("BSEcoeffRE.dat", cm, n, 0, "%.*g\t", 6);
-    write_part("BSEcoeffIM.dat", cm, n, 1, "%.*g\t", 6);
-  }
+  if (fbse_write_bse_matrices(dm, xm, cm, eqp, nh, ne, lumo, real)) die("cannot write", "the BSE matrix files");
   free(dm);
   free(xm);
   free(cm);

@@ -111,6 +111,12 @@ int fbse_write_psi(const char *path, const double *psi, long n_doubles);
  * as (re, im) pairs; 0 or -1 */
 int fbse_write_kernel_files(const double *dir, const double *exc, long nh, long ne, long lumo, int real);
 
+/* h0.dat, bs*.dat, HBSmat*.dat, BSEcoeff*.dat of the solve (bse_cplx/mod_bse.c,
+ * bethe-salpeter.c; bse_real's single-part files when real = 1) from the full
+ * kernels and the eigenvectors ([n_xton][n_xton] (re, im) pairs); 0 or -1 */
+int fbse_write_bse_matrices(const double *dir, const double *exc, const double *coef, const double *eqp, long nh,
+                            long ne, long lumo, int real);
+
 /* qp_spins.dat (qp_spin_frac, bse_cplx/spin.c:3-60): per spinor of psi
  * (nqp complex spinors of 2 ngrid points) its two spin-block norms; 0 or -1 */
 int fbse_write_qp_spins(const char *path, const double *psi, const double *eqp, long nqp, long ngrid, double dv);

@@ -751,6 +751,72 @@ int fbse_write_kernel_files(const double *dir, const double *exc, long nh, long 
   return fclose(f) ? -1 : 0;
 }
 
+static int write_part(const char *path, const double *m, long n, int part, const char *fmt, int prec)
+{
+  FILE *f = fopen(path, "w");
+  if (!f) return -1;
+  for (long i = 0; i < n; i++, fputc('\n', f))
+    for (long j = 0; j < n; j++) fprintf(f, fmt, prec, m[2 * (i * n + j) + part]);
+  return fclose(f) ? -1 : 0;
+}
+
+/* the matrix files of build_h0_mat, build_BSE_mat and bethe_salpeter:
+ * h0.dat (mod_bse.c:73-84, "%.6g "), bsRE/bsIM.dat = K^d + K^x
+ * (mod_bse.c:126-144), HBSmatRE/IM.dat = h0 - K (bethe-salpeter.c:71-95) and
+ * BSEcoeffRE/IM.dat, column j = exciton j (bethe-salpeter.c:115-133), all with
+ * PR_LEN = 6 significant digits (bse_cplx/fd.h:131).  dir / exc: the full
+ * kernels, coef the eigenvectors, each [n_xton][n_xton] as (re, im) pairs;
+ * the files go to the working directory. */
+int fbse_write_bse_matrices(const double *dir, const double *exc, const double *coef, const double *eqp, long nh,
+                            long ne, long lumo, int real)
+{
+  const long n = nh * ne;
+  const size_t bytes = (size_t)n * n * 2 * sizeof(double);
+  double *dm = malloc(bytes), *xm = malloc(bytes);
+  const double *cm = coef;
+  int rc = 0;
+  if (!dm || !xm) { free(dm); free(xm); return -1; }
+  memcpy(dm, dir, bytes);
+  memcpy(xm, exc, bytes);
+  FILE *f = fopen("h0.dat", "w");
+  if (!f) { free(dm); free(xm); return -1; }
+  for (long i = 0; i < n; i++, fputc('\n', f))
+    for (long j = 0; j < n; j++) fprintf(f, "%.6g ", i == j ? eqp[lumo + i / nh] - eqp[i % nh] : 0.0);
+  fclose(f);
+  for (size_t k = 0; k < (size_t)n * n * 2; k++) dm[k] += xm[k]; /* K = K^d + K^x */
+  for (long i = 0; i < n; i++) dm[2 * (i * n + i) + 1] = 0.0;   /* Hermitian diagonal (mod_bse.c:117-121) */
+  if (real) {
+    /* bse_real: bs.dat, HBSmat.dat, BSEcoeff.dat with row j = exciton j
+     * (bse_real/mod_bse.c:124-131, bethe-salpeter.c:78-114) */
+    rc |= write_part("bs.dat", dm, n, 0, "%.*g ", 6);
+  } else {
+    rc |= write_part("bsRE.dat", dm, n, 0, "%.*g ", 6);
+    rc |= write_part("bsIM.dat", dm, n, 1, "%.*g ", 6);
+  }
+  /* H = h0 - K with a real h0, as C evaluates real - complex
+   * (bethe-salpeter.c:71-74): real part h0 - Re K, imaginary part -Im K */
+  for (long i = 0; i < n; i++)
+    for (long j = 0; j < n; j++) {
+      const double h0 = i == j ? eqp[lumo + i / nh] - eqp[i % nh] : 0.0;
+      dm[2 * (i * n + j)] = h0 - dm[2 * (i * n + j)];
+      dm[2 * (i * n + j) + 1] = -dm[2 * (i * n + j) + 1];
+    }
+  if (real) {
+    rc |= write_part("HBSmat.dat", dm, n, 0, "%.*g \t", 6);
+    for (long i = 0; i < n; i++) /* transpose */
+      for (long j = 0; j < n; j++) xm[2 * (i * n + j)] = cm[2 * (j * n + i)];
+    rc |= write_part("BSEcoeff.dat", xm, n, 0, "%.*g\t", 6);
+  } else {
+    rc |= write_part("HBSmatRE.dat", dm, n, 0, "%.*g \t", 6);
+    rc |= write_part("HBSmatIM.dat", dm, n, 1, "%.*g \t", 6);
+    rc |= write_part("BSEcoeffRE.dat", cm, n, 0, "%.*g\t", 6);
+    rc |= write_part("BSEcoeffIM.dat", cm, n, 1, "%.*g\t", 6);
+  }
+  free(dm);
+  free(xm);
+  return rc ? -1 : 0;
+}
+
 int fbse_write_qp_spins(const char *path, const double *psi, const double *eqp, long nqp, long ngrid, double dv)
 { /* qp_spin_frac (bse_cplx/spin.c:3-60): the norm of each spin block of every
    * quasiparticle spinor (complex, interleaved, up block then down block) */

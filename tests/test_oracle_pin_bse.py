@@ -333,3 +333,32 @@ def test_kernel_files_match_reference(rb, tmp_path, monkeypatch):
     assert L.fbse_write_kernel_files(_p(dr.view(np.float64)), _p(xr.view(np.float64)), nh, ne, lumo, 0) == 0
     for name in ("direct-0.dat", "exchange-0.dat"):
         assert (mine / name).read_bytes() == (tmp_path / name).read_bytes(), name
+
+
+def test_bse_matrix_files_match_reference(rb, tmp_path, monkeypatch):
+    """h0.dat, bsRE/IM.dat, HBSmatRE/IM.dat and BSEcoeffRE/IM.dat as
+    build_h0_mat / build_BSE_mat / bethe_salpeter write them
+    (bse_cplx/mod_bse.c:54-148, bethe-salpeter.c:7-133) against the library's
+    host fbse_write_bse_matrices on the same kernels (full Hermitian) and the
+    reference's own eigenvectors, byte for byte"""
+    import filterbse_gb300 as F
+    nh, ne, lumo = 3, 2, 4
+    psi = np.ascontiguousarray(qp_states(GRID, lumo + ne, 97))
+    _, _, dr, xr = _kernels(rb, GRID, psi, nh, ne, lumo, tmp_path, monkeypatch)
+    ev = np.ascontiguousarray(np.linspace(-0.3, 0.02, lumo + ne))
+    n = nh * ne
+    xe = np.zeros(n)
+    cf = np.zeros((n, n), np.complex128)
+    rb.ref_bse_solve(_p(dr.copy().view(np.float64)), _p(xr.copy().view(np.float64)), _p(ev), nh, ne, lumo, _p(xe),
+                     _p(cf.view(np.float64)))
+    full = [np.ascontiguousarray(np.tril(m) + np.conj(np.tril(m, -1)).T) for m in (dr, xr)]
+    mine = tmp_path / "mine"
+    mine.mkdir()
+    monkeypatch.chdir(mine)
+    L = F.load()
+    L.fbse_write_bse_matrices.argtypes = [D, D, D, D] + [ctypes.c_long] * 3 + [ctypes.c_int]
+    assert L.fbse_write_bse_matrices(_p(full[0].view(np.float64)), _p(full[1].view(np.float64)),
+                                     _p(cf.view(np.float64)), _p(ev), nh, ne, lumo, 0) == 0
+    for name in ("h0.dat", "bsRE.dat", "bsIM.dat", "HBSmatRE.dat", "HBSmatIM.dat", "BSEcoeffRE.dat",
+                 "BSEcoeffIM.dat"):
+        assert (mine / name).read_bytes() == (tmp_path / name).read_bytes(), name

@@ -167,3 +167,30 @@ def test_bse_real_kernel_files_match_reference(rr, tmp_path, monkeypatch):
     assert L.fbse_write_kernel_files(_p(pairs[0]), _p(pairs[1]), nh, ne, lumo, 1) == 0
     for name in ("direct-0.dat", "exchange-0.dat"):
         assert (mine / name).read_bytes() == (tmp_path / name).read_bytes(), name
+
+
+def test_bse_real_matrix_files_match_reference(rr, tmp_path, monkeypatch):
+    """h0.dat, bs.dat, HBSmat.dat and BSEcoeff.dat of the real stage
+    (bse_real/mod_bse.c:59-130, bethe-salpeter.c:70-114; BSEcoeff row n =
+    exciton n) against the library's host fbse_write_bse_matrices (real = 1)
+    on the same kernels and the reference's own eigenvectors, byte for byte"""
+    import filterbse_gb300 as F
+    monkeypatch.chdir(tmp_path)
+    nh, ne, lumo = 3, 2, 4
+    psi = real_states(GRID, lumo + ne, 101)
+    _, _, dr, xr = _kernels(rr, psi, nh, ne, lumo)
+    ev = np.ascontiguousarray(np.linspace(-0.3, 0.02, lumo + ne))
+    n = nh * ne
+    xe = np.zeros(n)
+    cf = np.zeros((n, n))
+    rr.ref_bser_solve(_p(dr.copy()), _p(xr.copy()), _p(ev), nh, ne, lumo, _p(xe), _p(cf))
+    full = [np.tril(m) + np.tril(m, -1).T for m in (dr, xr)]
+    pairs = [np.ascontiguousarray(np.stack([m, np.zeros_like(m)], axis=-1)) for m in full + [cf.T]]
+    mine = tmp_path / "mine"
+    mine.mkdir()
+    monkeypatch.chdir(mine)
+    L = F.load()
+    L.fbse_write_bse_matrices.argtypes = [D, D, D, D] + [ctypes.c_long] * 3 + [ctypes.c_int]
+    assert L.fbse_write_bse_matrices(_p(pairs[0]), _p(pairs[1]), _p(pairs[2]), _p(ev), nh, ne, lumo, 1) == 0
+    for name in ("h0.dat", "bs.dat", "HBSmat.dat", "BSEcoeff.dat"):
+        assert (mine / name).read_bytes() == (tmp_path / name).read_bytes(), name
